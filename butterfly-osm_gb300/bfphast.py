@@ -1,0 +1,271 @@
+"""Python host binding of the C ABI in include/bf_phast.h (ctypes).
+
+This mirrors the reference engine's call surface for tests and benchmarks:
+
+  Graph(csr)                 BatchedPhastEngine::new      route/src/matrix/batched_phast.rs:89
+  Graph.query_batch(src, T)  query_batch / query_batch_bounded  batched_phast.rs:131, :271
+  Graph.phast_query(o)       PhastEngine::query           route/src/range/phast.rs:155
+  Graph.matrix(src, tgt, T)  compute_matrix_flat          batched_phast.rs:667
+
+The native library is mandatory: importing this module raises if
+lib/libbf_phast.so is missing. There is no CPU fallback.
+"""
+import ctypes
+import pathlib
+
+import numpy as np
+
+_HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = _HERE / "lib" / "libbf_phast.so"
+INF = 0xFFFFFFFF
+
+BF_OK, BF_ERR_INVALID, BF_ERR_OOM, BF_ERR_DEVICE, BF_ERR_TIMEOUT, BF_ERR_CANCELLED, BF_ERR_BUSY, \
+    BF_ERR_UNSUPPORTED = range(8)
+ENGINE_AUTO, ENGINE_PLAIN, ENGINE_BATCHED = 0, 1, 2
+REQ_MATRIX, REQ_ISOCHRONE = 1, 2
+
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+class CchCsr(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("up_offsets", _u64p), ("up_targets", _u32p), ("up_weights", _u32p),
+                ("down_offsets", _u64p), ("down_targets", _u32p), ("down_weights", _u32p)]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("engine", ctypes.c_uint32),
+                ("k_lanes", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+                ("hbm_budget_bytes", ctypes.c_uint64), ("subtree_nodes", ctypes.c_uint32),
+                ("reserved2", ctypes.c_uint32)]
+
+
+class GraphInfo(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_uint32), ("n_levels", ctypes.c_uint32),
+                ("n_up", ctypes.c_uint64), ("n_down", ctypes.c_uint64),
+                ("max_depth", ctypes.c_uint32), ("n_top_nodes", ctypes.c_uint32),
+                ("n_subtrees", ctypes.c_uint32), ("k_lanes", ctypes.c_uint32),
+                ("device_bytes", ctypes.c_uint64)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("n_sources", ctypes.c_uint64), ("n_targets", ctypes.c_uint64),
+                ("n_batches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
+                ("upward_ms", ctypes.c_double), ("downward_ms", ctypes.c_double),
+                ("extract_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Seed(ctypes.Structure):
+    _fields_ = [("rank", ctypes.c_uint32), ("cost", ctypes.c_uint32)]
+
+
+class ServerCfg(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
+                ("max_queue", ctypes.c_uint32), ("timeout_ms", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("threshold", ctypes.c_uint32),
+                ("sources", _u32p), ("n_sources", ctypes.c_uint64),
+                ("targets", _u32p), ("n_targets", ctypes.c_uint64),
+                ("out", ctypes.c_void_p), ("user_tag", ctypes.c_uint64)]
+
+
+class Completion(ctypes.Structure):
+    _fields_ = [("user_tag", ctypes.c_uint64), ("ticket", ctypes.c_uint64),
+                ("status", ctypes.c_int32), ("reserved", ctypes.c_uint32),
+                ("submit_s", ctypes.c_double), ("admit_s", ctypes.c_double),
+                ("done_s", ctypes.c_double)]
+
+
+# Every symbol include/bf_phast.h declares, with its ctypes signature.
+_SIGNATURES = {
+    "bf_graph_create": (ctypes.c_int, [ctypes.POINTER(CchCsr), ctypes.POINTER(Config),
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    "bf_graph_destroy": (None, [ctypes.c_void_p]),
+    "bf_graph_info_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(GraphInfo)]),
+    "bf_graph_set_engine": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
+    "bf_query_batch": (ctypes.c_int, [ctypes.c_void_p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
+                                      _u32p]),
+    "bf_phast_query": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _u32p]),
+    "bf_matrix": (ctypes.c_int, [ctypes.c_void_p, _u32p, ctypes.c_uint64, _u32p, ctypes.c_uint64,
+                                 ctypes.c_uint32, _u32p, ctypes.POINTER(Stats)]),
+    "bf_matrix_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                        ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "bf_matrix_seeded": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Seed), _u64p,
+                                        ctypes.c_uint64, ctypes.POINTER(Seed), _u64p,
+                                        ctypes.c_uint64, ctypes.c_uint32, _u32p,
+                                        ctypes.POINTER(Stats)]),
+    "bf_phast_bounded_seeded": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Seed),
+                                               ctypes.c_uint32, ctypes.c_uint32, _u32p, _u32p,
+                                               ctypes.c_uint64, _u64p]),
+    "bf_isochrone_bitsets": (ctypes.c_int, [ctypes.c_void_p, _u32p, _u32p, ctypes.c_uint64,
+                                            _u64p, _u64p, ctypes.POINTER(Stats)]),
+    "bf_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerCfg),
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "bf_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Request), _u64p]),
+    "bf_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Completion),
+                                      ctypes.c_uint32, ctypes.c_uint32, _u32p]),
+    "bf_server_cancel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "bf_server_destroy": (None, [ctypes.c_void_p]),
+    "bf_last_error": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the native library (raises OSError if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not pathlib.Path(path).exists():
+            raise OSError("native engine %s is missing: run __graft_entry__.build()" % path)
+        lib = ctypes.CDLL(str(path))
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+class BfError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("bf status %d: %s" % (status, msg))
+        self.status = status
+
+
+def _check(rc):
+    if rc != BF_OK:
+        raise BfError(rc, load().bf_last_error().decode(errors="replace"))
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def _ptr(a, t=_u32p):
+    return a.ctypes.data_as(t)
+
+
+class Graph:
+    """A CCH resident on the GPU (owns a bf_graph handle)."""
+
+    def __init__(self, n_nodes, up_off, up_tgt, up_w, down_off, down_tgt, down_w, device=0,
+                 engine=ENGINE_AUTO, k_lanes=0, subtree_nodes=0, hbm_budget=0):
+        lib = load()
+        self._keep = [np.ascontiguousarray(up_off, dtype=np.uint64), _u32(up_tgt), _u32(up_w),
+                      np.ascontiguousarray(down_off, dtype=np.uint64), _u32(down_tgt),
+                      _u32(down_w)]
+        uo, ut, uw, do, dt, dw = self._keep
+        csr = CchCsr(n_nodes, 0, _ptr(uo, _u64p), _ptr(ut), _ptr(uw), _ptr(do, _u64p), _ptr(dt),
+                     _ptr(dw))
+        cfg = Config(device, engine, k_lanes, 0, hbm_budget, subtree_nodes, 0)
+        h = ctypes.c_void_p()
+        _check(lib.bf_graph_create(ctypes.byref(csr), ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._keep = None  # the library copied what it needs
+        self.n = n_nodes
+
+    @classmethod
+    def from_cch(cls, cch, **kw):
+        return cls(cch["n"], cch["up_off"], cch["up_tgt"], cch["up_w"], cch["down_off"],
+                   cch["down_tgt"], cch["down_w"], **kw)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bf_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self):
+        i = GraphInfo()
+        _check(load().bf_graph_info_get(self._h, ctypes.byref(i)))
+        return {f: getattr(i, f) for f, _ in i._fields_}
+
+    def set_engine(self, engine, k_lanes=0):
+        _check(load().bf_graph_set_engine(self._h, engine, k_lanes))
+
+    def query_batch(self, sources, threshold=INF):
+        s = _u32(sources)
+        out = np.empty((len(s), self.n), dtype=np.uint32)
+        _check(load().bf_query_batch(self._h, _ptr(s), len(s), threshold, _ptr(out)))
+        return out
+
+    def phast_query(self, origin):
+        out = np.empty(self.n, dtype=np.uint32)
+        _check(load().bf_phast_query(self._h, int(origin), _ptr(out)))
+        return out
+
+    def matrix(self, sources, targets, threshold=INF, out=None, stats=False):
+        s, t = _u32(sources), _u32(targets)
+        if out is None:
+            out = np.empty((len(s), len(t)), dtype=np.uint32)
+        st = Stats()
+        _check(load().bf_matrix(self._h, _ptr(s), len(s), _ptr(t), len(t), threshold, _ptr(out),
+                                ctypes.byref(st)))
+        return (out, st.as_dict()) if stats else out
+
+    def matrix_device(self, d_src, S, d_tgt, T, d_out, threshold=INF, stream=None):
+        """Device-pointer variant: d_* are integer device addresses."""
+        st = Stats()
+        _check(load().bf_matrix_device(self._h, ctypes.c_void_p(d_src), S, ctypes.c_void_p(d_tgt),
+                                       T, threshold, ctypes.c_void_p(d_out),
+                                       ctypes.c_void_p(stream or 0), ctypes.byref(st)))
+        return st.as_dict()
+
+    def matrix_seeded(self, src_seeds, tgt_seeds, threshold=INF):
+        """src_seeds / tgt_seeds: lists of lists of (rank, cost)."""
+        def pack(sets):
+            off = np.zeros(len(sets) + 1, dtype=np.uint64)
+            flat = []
+            for i, ss in enumerate(sets):
+                flat.extend(ss)
+                off[i + 1] = len(flat)
+            arr = (Seed * max(1, len(flat)))(*[Seed(int(r), int(c)) for r, c in flat])
+            return arr, off
+        sa, so = pack(src_seeds)
+        ta, to = pack(tgt_seeds)
+        out = np.empty((len(src_seeds), len(tgt_seeds)), dtype=np.uint32)
+        st = Stats()
+        _check(load().bf_matrix_seeded(self._h, sa, _ptr(so, _u64p), len(src_seeds), ta,
+                                       _ptr(to, _u64p), len(tgt_seeds), threshold, _ptr(out),
+                                       ctypes.byref(st)))
+        return out
+
+    def phast_bounded_seeded(self, seeds, threshold):
+        arr = (Seed * max(1, len(seeds)))(*[Seed(int(r), int(c)) for r, c in seeds])
+        cap = self.n
+        rk = np.empty(cap, dtype=np.uint32)
+        ds = np.empty(cap, dtype=np.uint32)
+        cnt = ctypes.c_uint64()
+        _check(load().bf_phast_bounded_seeded(self._h, arr, len(seeds), threshold, _ptr(rk),
+                                              _ptr(ds), cap, ctypes.byref(cnt)))
+        c = cnt.value
+        return rk[:c].copy(), ds[:c].copy()
+
+    def isochrone_bitsets(self, origins, thresholds, stats=False):
+        o, t = _u32(origins), _u32(thresholds)
+        words = (self.n + 63) // 64
+        bits = np.empty((len(o), words), dtype=np.uint64)
+        counts = np.empty(len(o), dtype=np.uint64)
+        st = Stats()
+        _check(load().bf_isochrone_bitsets(self._h, _ptr(o), _ptr(t), len(o), _ptr(bits, _u64p),
+                                           _ptr(counts, _u64p), ctypes.byref(st)))
+        return (bits, counts, st.as_dict()) if stats else (bits, counts)

@@ -1,0 +1,334 @@
+// api.cu — extern "C" entry points of bf_phast.h.
+//
+// Every entry point validates its arguments on the host, takes the graph's
+// mutex (a graph is shared by host threads the way the reference shares its
+// &self engines across rayon workers, batched_phast.rs:45), runs on the
+// graph's stream (or the caller's), checks the device error word and returns
+// a status; nothing aborts.
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <new>
+
+#include "engine.cuh"
+
+namespace bf {
+
+static thread_local std::string t_err;
+
+void set_error(const std::string& msg) { t_err = msg; }
+
+bf_status cuda_status(cudaError_t e, const char* what) {
+  cudaGetLastError();
+  t_err = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return BF_ERR_OOM;
+  return BF_ERR_DEVICE;
+}
+
+namespace {
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  bf_status alloc(size_t bytes) {
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 4)) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      set_error("cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+      return BF_ERR_OOM;
+    }
+    return BF_OK;
+  }
+  template <class T>
+  T* as() {
+    return (T*)p;
+  }
+};
+
+bf_status check_ids(const uint32_t* ids, uint64_t m, uint32_t n, const char* what) {
+  for (uint64_t i = 0; i < m; ++i)
+    if (ids[i] >= n) {
+      set_error(std::string(what) + "[" + std::to_string(i) + "] = " + std::to_string(ids[i]) +
+                " is not a node of the graph (n_nodes = " + std::to_string(n) + ")");
+      return BF_ERR_INVALID;
+    }
+  return BF_OK;
+}
+
+// Run the selected engine on device buffers.
+bf_status run_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
+                     uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
+                     bf_stats* stats) {
+  bf_status s;
+  if (g->engine == BF_ENGINE_PLAIN || !g->bt.ready) {
+    DevBuf tpos;
+    if ((s = tpos.alloc(T * 4))) return s;
+    if ((s = to_positions(g, d_tgt, T, tpos.as<uint32_t>(), st))) return s;
+    if ((s = plain_matrix(g, d_src, S, tpos.as<uint32_t>(), T, threshold, d_out, st, stats)))
+      return s;
+    if (stats) stats->kernel_launches += 1;
+  } else {
+    if ((s = batched_matrix(g, d_src, S, d_tgt, T, threshold, d_out, st, stats))) return s;
+  }
+  return check_device_error(g, st);
+}
+
+}  // namespace
+}  // namespace bf
+
+using namespace bf;
+
+struct bf_graph {
+  Graph g;
+};
+
+extern "C" {
+
+bf_status bf_graph_create(const bf_cch_csr* csr, const bf_config* cfg, bf_graph** out) {
+  if (out) *out = nullptr;
+  if (!csr || !out || !csr->up_offsets || !csr->down_offsets || csr->n_nodes == 0) {
+    set_error("bf_graph_create: null argument or empty graph");
+    return BF_ERR_INVALID;
+  }
+  if ((csr->up_offsets[csr->n_nodes] && (!csr->up_targets || !csr->up_weights)) ||
+      (csr->down_offsets[csr->n_nodes] && (!csr->down_targets || !csr->down_weights))) {
+    set_error("bf_graph_create: edge arrays missing");
+    return BF_ERR_INVALID;
+  }
+  bf_config c{};
+  if (cfg) c = *cfg;
+  if (c.engine > BF_ENGINE_BATCHED || (c.k_lanes && c.k_lanes != 16 && c.k_lanes != 32 &&
+                                       c.k_lanes != 64 && c.k_lanes != 128)) {
+    set_error("bf_graph_create: invalid engine or k_lanes");
+    return BF_ERR_INVALID;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device");
+    return BF_ERR_DEVICE;
+  }
+  if (c.device < 0 || c.device >= ndev) {
+    set_error("bf_graph_create: device ordinal out of range");
+    return BF_ERR_INVALID;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, c.device) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaGetDeviceProperties failed");
+    return BF_ERR_DEVICE;
+  }
+  if (prop.major != 10 || prop.minor != 3) {
+    set_error(std::string("this library is built for sm_103 (GB300); device is ") + prop.name);
+    return BF_ERR_DEVICE;
+  }
+  bf_graph* h = new (std::nothrow) bf_graph();
+  if (!h) {
+    set_error("out of host memory");
+    return BF_ERR_OOM;
+  }
+  Graph* g = &h->g;
+  g->device = c.device;
+  g->engine = c.engine == BF_ENGINE_AUTO ? BF_ENGINE_BATCHED : c.engine;
+  g->k_lanes = c.k_lanes;
+  if (cudaSetDevice(c.device) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    set_error("cudaSetDevice failed");
+    return BF_ERR_DEVICE;
+  }
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  g->hbm_budget = c.hbm_budget_bytes ? c.hbm_budget_bytes : (uint64_t)(fr * 0.85);
+  bf_status s;
+  try {
+    s = build_graph(csr, &c, g);
+    if (s == BF_OK) s = batched_prepare(g, c.subtree_nodes);
+  } catch (const std::bad_alloc&) {
+    set_error("out of host memory");
+    s = BF_ERR_OOM;
+  }
+  if (s != BF_OK) {
+    free_graph(g);
+    delete h;
+    return s;
+  }
+  *out = h;
+  return BF_OK;
+}
+
+void bf_graph_destroy(bf_graph* h) {
+  if (!h) return;
+  free_graph(&h->g);
+  delete h;
+}
+
+bf_status bf_graph_info_get(const bf_graph* h, bf_graph_info* o) {
+  if (!h || !o) {
+    set_error("bf_graph_info_get: null argument");
+    return BF_ERR_INVALID;
+  }
+  const Graph& g = h->g;
+  std::memset(o, 0, sizeof(*o));
+  o->n_nodes = g.n;
+  o->n_levels = g.n_levels;
+  o->n_up = g.n_up;
+  o->n_down = g.n_down;
+  o->max_depth = g.max_depth;
+  o->n_top_nodes = g.bt.n_top;
+  o->n_subtrees = g.bt.n_sub;
+  o->k_lanes = g.k_lanes;
+  o->device_bytes = g.device_bytes;
+  return BF_OK;
+}
+
+bf_status bf_graph_set_engine(bf_graph* h, uint32_t engine, uint32_t k_lanes) {
+  if (!h || engine > BF_ENGINE_BATCHED ||
+      (k_lanes && k_lanes != 16 && k_lanes != 32 && k_lanes != 64 && k_lanes != 128)) {
+    set_error("bf_graph_set_engine: invalid argument");
+    return BF_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(h->g.mu);
+  h->g.engine = engine == BF_ENGINE_AUTO ? BF_ENGINE_BATCHED : engine;
+  if (k_lanes) h->g.k_lanes = k_lanes;
+  return BF_OK;
+}
+
+bf_status bf_matrix_device(bf_graph* h, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
+                           uint64_t T, uint32_t threshold, uint32_t* d_out, void* stream,
+                           bf_stats* st) {
+  if (!h || (S && !d_src) || (T && !d_tgt) || (S && T && !d_out)) {
+    set_error("bf_matrix_device: null argument");
+    return BF_ERR_INVALID;
+  }
+  double t0 = now_s();
+  Graph* g = &h->g;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+  if (st) std::memset(st, 0, sizeof(*st));
+  bf_status rc = BF_OK;
+  if (S && T) rc = run_matrix(g, d_src, S, d_tgt, T, threshold, d_out, s, st);
+  if (rc == BF_OK && cudaStreamSynchronize(s) != cudaSuccess)
+    rc = cuda_status(cudaGetLastError(), "cudaStreamSynchronize");
+  if (st) {
+    st->n_sources = S;
+    st->n_targets = T;
+    st->total_ms = (now_s() - t0) * 1e3;
+  }
+  return rc;
+}
+
+bf_status bf_matrix(bf_graph* h, const uint32_t* src, uint64_t S, const uint32_t* tgt, uint64_t T,
+                    uint32_t threshold, uint32_t* out, bf_stats* st) {
+  if (!h || (S && !src) || (T && !tgt) || (S && T && !out)) {
+    set_error("bf_matrix: null argument");
+    return BF_ERR_INVALID;
+  }
+  double t0 = now_s();
+  Graph* g = &h->g;
+  bf_status rc;
+  if ((rc = check_ids(src, S, g->n, "sources"))) return rc;
+  if ((rc = check_ids(tgt, T, g->n, "targets"))) return rc;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (!S || !T) return BF_OK;
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t s = g->stream;
+  DevBuf ds, dt, dout;
+  if ((rc = ds.alloc(S * 4)) || (rc = dt.alloc(T * 4)) || (rc = dout.alloc(S * T * 4))) return rc;
+  BF_CUDA(cudaMemcpyAsync(ds.p, src, S * 4, cudaMemcpyHostToDevice, s));
+  BF_CUDA(cudaMemcpyAsync(dt.p, tgt, T * 4, cudaMemcpyHostToDevice, s));
+  if ((rc = run_matrix(g, ds.as<uint32_t>(), S, dt.as<uint32_t>(), T, threshold,
+                       dout.as<uint32_t>(), s, st)))
+    return rc;
+  BF_CUDA(cudaMemcpyAsync(out, dout.p, S * T * 4, cudaMemcpyDeviceToHost, s));
+  BF_CUDA(cudaStreamSynchronize(s));
+  if (st) {
+    st->n_sources = S;
+    st->n_targets = T;
+    st->h2d_bytes = (S + T) * 4;
+    st->d2h_bytes = S * T * 4;
+    st->total_ms = (now_s() - t0) * 1e3;
+  }
+  return BF_OK;
+}
+
+bf_status bf_query_batch(bf_graph* h, const uint32_t* src, uint32_t k, uint32_t threshold,
+                         uint32_t* dist_out) {
+  if (!h || (k && (!src || !dist_out)) || k > 128) {
+    set_error("bf_query_batch: null argument or k > 128");
+    return BF_ERR_INVALID;
+  }
+  Graph* g = &h->g;
+  bf_status rc;
+  if ((rc = check_ids(src, k, g->n, "sources"))) return rc;
+  if (!k) return BF_OK;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t s = g->stream;
+  DevBuf ds, dout;
+  if ((rc = ds.alloc(k * 4)) || (rc = dout.alloc((size_t)k * g->n * 4))) return rc;
+  BF_CUDA(cudaMemcpyAsync(ds.p, src, k * 4, cudaMemcpyHostToDevice, s));
+  // every rank is a target: positions are the rank -> position table itself
+  if ((rc = plain_matrix(g, ds.as<uint32_t>(), k, g->d_pos_of, g->n, threshold,
+                         dout.as<uint32_t>(), s, nullptr)))
+    return rc;
+  if ((rc = check_device_error(g, s))) return rc;
+  BF_CUDA(cudaMemcpyAsync(dist_out, dout.p, (size_t)k * g->n * 4, cudaMemcpyDeviceToHost, s));
+  BF_CUDA(cudaStreamSynchronize(s));
+  return BF_OK;
+}
+
+bf_status bf_phast_query(bf_graph* h, uint32_t origin, uint32_t* dist_out) {
+  return bf_query_batch(h, &origin, 1, BF_INF, dist_out);
+}
+
+bf_status bf_matrix_seeded(bf_graph*, const bf_seed*, const uint64_t*, uint64_t, const bf_seed*,
+                           const uint64_t*, uint64_t, uint32_t, uint32_t*, bf_stats*) {
+  set_error("bf_matrix_seeded: not implemented yet");
+  return BF_ERR_UNSUPPORTED;
+}
+
+bf_status bf_phast_bounded_seeded(bf_graph*, const bf_seed*, uint32_t, uint32_t, uint32_t*,
+                                  uint32_t*, uint64_t, uint64_t*) {
+  set_error("bf_phast_bounded_seeded: not implemented yet");
+  return BF_ERR_UNSUPPORTED;
+}
+
+bf_status bf_isochrone_bitsets(bf_graph*, const uint32_t*, const uint32_t*, uint64_t, uint64_t*,
+                               uint64_t*, bf_stats*) {
+  set_error("bf_isochrone_bitsets: not implemented yet");
+  return BF_ERR_UNSUPPORTED;
+}
+
+bf_status bf_server_create(bf_graph*, const bf_server_cfg*, bf_server** out) {
+  if (out) *out = nullptr;
+  set_error("bf_server_create: not implemented yet");
+  return BF_ERR_UNSUPPORTED;
+}
+bf_status bf_server_submit(bf_server*, const bf_request*, uint64_t*) {
+  set_error("bf_server_submit: not implemented yet");
+  return BF_ERR_UNSUPPORTED;
+}
+bf_status bf_server_poll(bf_server*, bf_completion*, uint32_t, uint32_t, uint32_t* n_out) {
+  if (n_out) *n_out = 0;
+  set_error("bf_server_poll: not implemented yet");
+  return BF_ERR_UNSUPPORTED;
+}
+bf_status bf_server_cancel(bf_server*, uint64_t) {
+  set_error("bf_server_cancel: not implemented yet");
+  return BF_ERR_UNSUPPORTED;
+}
+void bf_server_destroy(bf_server*) {}
+
+const char* bf_last_error(void) { return t_err.c_str(); }
+
+}  // extern "C"

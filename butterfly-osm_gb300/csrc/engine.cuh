@@ -1,0 +1,141 @@
+// engine.cuh — internal declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/bf_phast.h"
+
+namespace bf {
+
+constexpr uint32_t INF = 0xFFFFFFFFu;
+constexpr uint32_t NONE = 0xFFFFFFFFu;
+
+// Device error codes written into the per-graph error word by kernels that
+// detect an inconsistency; the host turns them into BF_ERR_DEVICE.
+enum : uint32_t {
+  DEVERR_PATH = 1u,       // ancestor path inconsistent with the depth table
+  DEVERR_EDGE = 2u,       // upward edge leaves the ancestor path
+  DEVERR_TIMEOUT = 4u,    // a bounded spin-wait ran out
+  DEVERR_SMEM = 8u        // a subtree does not fit its shared-memory tile
+};
+
+__host__ __device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) {
+  uint32_t s = a + b;
+  return (s < a) ? INF : s;  // wraps only on overflow; INF + x also saturates
+}
+
+// Lanes per batch of the plain engine (one warp lane per source).
+constexpr uint32_t PLAIN_K = 32;
+// Ancestor-path entries a warp keeps in shared memory during the upward pass.
+constexpr uint32_t UPWARD_SMEM_PATH = 2048;
+constexpr uint32_t UPWARD_WARPS = 4;
+
+// Shared-memory subtree task of the batched engine.
+struct SubtreeMeta {
+  uint32_t node0;      // first subtree position (positions are contiguous)
+  uint32_t n_nodes;    // nodes in the subtree
+  uint32_t lvl0;       // first entry in the subtree-level table
+  uint32_t n_lvls;     // local levels
+  uint64_t edge0;      // first edge record
+  uint64_t n_edges;    // edge records (internal + boundary)
+};
+
+struct Graph {
+  int device = 0;
+  uint32_t n = 0;
+  uint64_t n_up = 0, n_down = 0;
+  uint32_t n_levels = 0, max_depth = 0;
+  uint32_t engine = BF_ENGINE_BATCHED;
+  uint32_t k_lanes = 0;
+  uint64_t device_bytes = 0;
+  uint64_t hbm_budget = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8] = {};
+  std::mutex mu;
+
+  // host tables
+  std::vector<uint32_t> pos_of;     // rank -> slab position (plain engine)
+  std::vector<uint32_t> lvl_start;  // level -> first position, n_levels + 1
+
+  // device: elimination tree / upward
+  uint32_t* d_parent = nullptr;   // [n] etree parent rank (NONE at roots)
+  uint32_t* d_run_end = nullptr;  // [n] last rank of the consecutive-parent run from r
+  uint32_t* d_depth = nullptr;    // [n] etree depth
+  uint64_t* d_up_off = nullptr;   // [n+1] finite UP edges by source rank
+  uint2* d_up_rec = nullptr;      // {depth(src) - depth(dst), w}
+  uint32_t* d_pos_of = nullptr;   // [n] rank -> plain slab position
+  uint32_t* d_rank_at = nullptr;  // [n] plain slab position -> rank
+  // device: level-ordered pull CSR (plain engine)
+  uint64_t* d_in_off = nullptr;   // [n+1] by slab position
+  uint2* d_in_rec = nullptr;      // {source slab position, w}
+  // device: plain engine work buffers
+  uint32_t* d_dist = nullptr;     // [n][32]
+  uint32_t* d_seed = nullptr;     // [n][32], all INF between calls
+  uint32_t* d_flag = nullptr;     // [ceil(n/32)] seeded-row bits, all 0 between calls
+  uint32_t* d_err = nullptr;      // device error word
+  uint32_t* d_gpath = nullptr;    // global fallback for deep ancestor paths
+  uint32_t gpath_stride = 0;      // entries per warp in d_gpath (2 * (max_depth + 1))
+
+  // ---- batched engine (shared-memory subtrees) ----
+  struct Batched {
+    bool ready = false;
+    uint32_t S_max = 0;             // max subtree nodes
+    uint32_t n_top = 0;             // nodes above the subtrees
+    uint32_t n_sub = 0;             // subtrees
+    std::vector<uint32_t> tchunk;   // top schedule: chunk start (top positions), n_chunks + 1
+    std::vector<uint64_t> tchunk_e; // top schedule: chunk edge start, n_chunks + 1
+    std::vector<uint8_t> tchunk_sync; // 1 = a CTA barrier precedes this chunk
+    uint32_t* d_tchunk = nullptr;
+    uint64_t* d_tchunk_e = nullptr;
+    uint8_t* d_tchunk_sync = nullptr;
+    uint32_t n_tchunks = 0;
+    uint4* d_top_rec = nullptr;     // top-tree edges {src top pos, w, dst slot, 0}
+    uint32_t* d_top_of = nullptr;   // [n] rank -> top position or NONE
+    uint32_t* d_sub_of = nullptr;   // [n] rank -> subtree id or NONE
+    uint32_t* d_loc_of = nullptr;   // [n] rank -> position inside its subtree
+    uint32_t* d_top_rank = nullptr; // [n_top] top position -> rank
+    SubtreeMeta* d_sub = nullptr;   // [n_sub]
+    uint32_t* d_slvl = nullptr;     // subtree level table: local level start (local index)
+    uint4* d_sub_rec = nullptr;     // subtree edges {src, w, dst local, is_boundary}
+    uint32_t* d_sub_rank = nullptr; // [n] subtree-ordered rank list (node0 + local)
+    std::vector<SubtreeMeta> sub;
+    uint64_t n_top_edges = 0, n_sub_edges = 0;
+  } bt;
+};
+
+// graph.cu
+bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g);
+void free_graph(Graph* g);
+
+// engine_plain.cu
+bf_status plain_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tpos,
+                       uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
+                       bf_stats* stats);
+bf_status plain_dist(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,
+                     uint32_t* d_out_rank_major, cudaStream_t st);
+bf_status to_positions(Graph* g, const uint32_t* d_rank, uint64_t n, uint32_t* d_pos,
+                       cudaStream_t st);
+bf_status check_device_error(Graph* g, cudaStream_t st);
+
+// engine_batched.cu
+bf_status batched_prepare(Graph* g, uint32_t S_max);
+bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
+                         uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
+                         bf_stats* stats);
+
+// api.cu
+void set_error(const std::string& msg);
+bf_status cuda_status(cudaError_t e, const char* what);
+
+}  // namespace bf
+
+#define BF_CUDA(call)                                                    \
+  do {                                                                   \
+    cudaError_t _e = (call);                                             \
+    if (_e != cudaSuccess) return ::bf::cuda_status(_e, #call);          \
+  } while (0)

@@ -1,0 +1,308 @@
+// engine_plain.cu — the plain GPU sweep: one K = 32 batch at a time.
+//
+//   1. k_upward: one warp per source walks the source's elimination-tree
+//      ancestor path in increasing rank order and relaxes UP edges into a
+//      path-indexed distance array (replaces the per-lane BinaryHeap Dijkstra
+//      of batched_phast.rs:156-189; ranks are a topological order of the UP
+//      DAG, so a node's distance is final once every lower path node has
+//      pushed). Settled (node, dist) pairs land in a seed slab.
+//   2. k_sweep_level: one launch per level of the pull DAG; a warp per node,
+//      lane = source. dist[v][lane] = min(seed, min over DOWN in-edges
+//      (u -> v, w) of dist[u][lane] + w) — the pull form of the rank-
+//      descending push scan of batched_phast.rs:205-250.
+//   3. k_extract: gathers the target rows and writes the S x T row-major
+//      matrix through a shared-memory transpose (batched_phast.rs:693-701).
+
+#include <algorithm>
+
+#include "engine.cuh"
+
+namespace bf {
+
+namespace {
+
+// Ancestor path of `s` written into pn[0 .. D): runs of consecutive ranks are
+// emitted by the whole warp at once. Returns D (or 0 on inconsistency).
+__device__ uint32_t walk_path(uint32_t s, uint32_t D, const uint32_t* __restrict__ parent,
+                              const uint32_t* __restrict__ run_end, uint32_t* pn, uint32_t lane) {
+  uint32_t i = 0, x = s;
+  while (x != NONE) {
+    uint32_t e = run_end[x];
+    uint32_t len = e - x + 1;
+    if (i + len > D) return 0;
+    for (uint32_t l = lane; l < len; l += 32) pn[i + l] = x + l;
+    i += len;
+    x = parent[e];
+  }
+  return i == D ? D : 0;
+}
+
+template <bool GLOBAL_PATH>
+__device__ __forceinline__ uint32_t pd_load(const uint32_t* p) {
+  if (GLOBAL_PATH) return __ldcg(p);
+  return *(const volatile uint32_t*)p;
+}
+
+}  // namespace
+
+// Upward pass for one batch. Warp w handles source src[w] (w < k) and writes
+// its settled pairs into seed[pos * K + lane_base + w] (+ the seeded bit).
+template <bool GLOBAL_PATH>
+__global__ void __launch_bounds__(UPWARD_WARPS * 32)
+    k_upward(const uint32_t* __restrict__ src, uint32_t k, uint32_t threshold,
+             const uint32_t* __restrict__ parent, const uint32_t* __restrict__ run_end,
+             const uint32_t* __restrict__ depth, const uint64_t* __restrict__ up_off,
+             const uint2* __restrict__ up_rec, const uint32_t* __restrict__ pos_of, uint32_t n,
+             uint32_t* __restrict__ seed, uint32_t seed_stride, uint32_t* __restrict__ flag,
+             uint32_t* __restrict__ gpath, uint32_t gpath_stride, uint32_t* __restrict__ err) {
+  extern __shared__ uint32_t smem[];
+  const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t w = blockIdx.x * UPWARD_WARPS + wib;
+  if (w >= k) return;
+  const uint32_t s = src[w];
+  if (s >= n) {
+    if (lane == 0) atomicOr(err, DEVERR_PATH);
+    return;
+  }
+  const uint32_t D = depth[s] + 1;
+  uint32_t *pd, *pn;
+  if (GLOBAL_PATH) {
+    pd = gpath + (size_t)w * gpath_stride;
+    pn = pd + gpath_stride / 2;
+  } else {
+    pd = smem + wib * 2 * UPWARD_SMEM_PATH;
+    pn = pd + UPWARD_SMEM_PATH;
+  }
+  if (walk_path(s, D, parent, run_end, pn, lane) != D) {
+    if (lane == 0) atomicOr(err, DEVERR_PATH);
+    return;
+  }
+  for (uint32_t l = lane; l < D; l += 32) pd[l] = (l == 0) ? 0u : INF;
+  if (GLOBAL_PATH) __threadfence_block();
+  __syncwarp();
+  for (uint32_t i = 0; i < D; ++i) {
+    uint32_t d = pd_load<GLOBAL_PATH>(&pd[i]);
+    if (d == INF || d > threshold) continue;
+    uint32_t x = GLOBAL_PATH ? __ldcg(&pn[i]) : pn[i];
+    uint64_t e1 = up_off[x + 1];
+    for (uint64_t e = up_off[x] + lane; e < e1; e += 32) {
+      uint2 r = up_rec[e];
+      uint32_t j = i + r.x;
+      if (j >= D) {
+        atomicOr(err, DEVERR_EDGE);
+        continue;
+      }
+      atomicMin(&pd[j], sat_add(d, r.y));
+    }
+    __syncwarp();
+  }
+  if (GLOBAL_PATH) __threadfence_block();
+  __syncwarp();
+  for (uint32_t l = lane; l < D; l += 32) {
+    uint32_t d = pd_load<GLOBAL_PATH>(&pd[l]);
+    if (d == INF || d > threshold) continue;
+    uint32_t x = GLOBAL_PATH ? __ldcg(&pn[l]) : pn[l];
+    uint32_t p = pos_of[x];
+    seed[(size_t)p * seed_stride + w] = d;
+    atomicOr(&flag[p >> 5], 1u << (p & 31));
+  }
+}
+
+// One level of the pull sweep: positions [p0, p1), a warp per node.
+__global__ void __launch_bounds__(256)
+    k_sweep_level(uint32_t p0, uint32_t p1, const uint64_t* __restrict__ in_off,
+                  const uint2* __restrict__ in_rec, uint32_t* __restrict__ dist,
+                  uint32_t* __restrict__ seed, uint32_t* __restrict__ flag, uint32_t threshold) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t p = p0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (p >= p1) return;
+  uint32_t best = INF;
+  const uint32_t bit = 1u << (p & 31);
+  if (flag[p >> 5] & bit) {
+    best = seed[(size_t)p * PLAIN_K + lane];
+    seed[(size_t)p * PLAIN_K + lane] = INF;
+    __syncwarp();
+    if (lane == 0) atomicAnd(&flag[p >> 5], ~bit);
+  }
+  uint64_t e = in_off[p];
+  const uint64_t e1 = in_off[p + 1];
+  for (; e + 4 <= e1; e += 4) {
+    uint2 r0 = in_rec[e], r1 = in_rec[e + 1], r2 = in_rec[e + 2], r3 = in_rec[e + 3];
+    uint32_t a0 = dist[(size_t)r0.x * PLAIN_K + lane];
+    uint32_t a1 = dist[(size_t)r1.x * PLAIN_K + lane];
+    uint32_t a2 = dist[(size_t)r2.x * PLAIN_K + lane];
+    uint32_t a3 = dist[(size_t)r3.x * PLAIN_K + lane];
+    best = min(best, min(min(sat_add(a0, r0.y), sat_add(a1, r1.y)),
+                         min(sat_add(a2, r2.y), sat_add(a3, r3.y))));
+  }
+  for (; e < e1; ++e) {
+    uint2 r = in_rec[e];
+    best = min(best, sat_add(dist[(size_t)r.x * PLAIN_K + lane], r.y));
+  }
+  if (best > threshold) best = INF;
+  dist[(size_t)p * PLAIN_K + lane] = best;
+}
+
+// out[(row0 + l) * T + t] = slab[tpos[t]][l] for l < k; tiles of 32 targets.
+__global__ void __launch_bounds__(256)
+    k_extract(const uint32_t* __restrict__ slab, uint32_t slab_stride,
+              const uint32_t* __restrict__ tpos, uint64_t T, uint32_t k,
+              uint32_t* __restrict__ out) {
+  __shared__ uint32_t tile[32][33];
+  const uint64_t t0 = (uint64_t)blockIdx.x * 32;
+  for (uint32_t r = threadIdx.y; r < 32; r += 8) {
+    uint64_t t = t0 + r;
+    tile[r][threadIdx.x] = (t < T) ? slab[(size_t)tpos[t] * slab_stride + threadIdx.x] : INF;
+  }
+  __syncthreads();
+  for (uint32_t l = threadIdx.y; l < k; l += 8) {
+    uint64_t t = t0 + threadIdx.x;
+    if (t < T) out[(uint64_t)l * T + t] = tile[threadIdx.x][l];
+  }
+}
+
+__global__ void k_to_positions(const uint32_t* __restrict__ ranks, uint64_t m,
+                               const uint32_t* __restrict__ pos_of, uint32_t n,
+                               uint32_t* __restrict__ pos, uint32_t* __restrict__ err) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  uint32_t r = ranks[i];
+  if (r >= n) {
+    atomicOr(err, DEVERR_PATH);
+    pos[i] = 0;
+  } else {
+    pos[i] = pos_of[r];
+  }
+}
+
+bf_status to_positions(Graph* g, const uint32_t* d_rank, uint64_t m, uint32_t* d_pos,
+                       cudaStream_t st) {
+  if (!m) return BF_OK;
+  k_to_positions<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(d_rank, m, g->d_pos_of, g->n, d_pos,
+                                                              g->d_err);
+  BF_CUDA(cudaGetLastError());
+  return BF_OK;
+}
+
+bf_status check_device_error(Graph* g, cudaStream_t st) {
+  uint32_t h = 0;
+  BF_CUDA(cudaMemcpyAsync(&h, g->d_err, 4, cudaMemcpyDeviceToHost, st));
+  BF_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    BF_CUDA(cudaMemsetAsync(g->d_err, 0, 4, st));
+    BF_CUDA(cudaStreamSynchronize(st));
+    set_error("device reported error bits 0x" + std::to_string(h) +
+              " (invalid node id or CCH inconsistent with its elimination tree)");
+    return BF_ERR_INVALID;
+  }
+  return BF_OK;
+}
+
+static bf_status plain_buffers(Graph* g) {
+  if (g->d_dist) return BF_OK;
+  const size_t slab = (size_t)g->n * PLAIN_K * sizeof(uint32_t);
+  if (cudaMalloc(&g->d_dist, slab) != cudaSuccess || cudaMalloc(&g->d_seed, slab) != cudaSuccess ||
+      cudaMalloc(&g->d_flag, ((g->n + 31) / 32) * 4) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cannot allocate the plain engine's distance slabs");
+    return BF_ERR_OOM;
+  }
+  g->device_bytes += 2 * slab + ((g->n + 31) / 32) * 4;
+  BF_CUDA(cudaMemset(g->d_seed, 0xFF, slab));
+  BF_CUDA(cudaMemset(g->d_flag, 0, ((g->n + 31) / 32) * 4));
+  if (g->max_depth + 1 > UPWARD_SMEM_PATH) {
+    g->gpath_stride = 2 * (g->max_depth + 1);
+    size_t bytes = (size_t)PLAIN_K * g->gpath_stride * 4;
+    if (cudaMalloc(&g->d_gpath, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cannot allocate the ancestor-path scratch");
+      return BF_ERR_OOM;
+    }
+    g->device_bytes += bytes;
+  }
+  static bool attr_set = false;
+  if (!attr_set) {
+    BF_CUDA(cudaFuncSetAttribute(k_upward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 UPWARD_WARPS * 2 * UPWARD_SMEM_PATH * 4));
+    attr_set = true;
+  }
+  return BF_OK;
+}
+
+// Launch one upward pass for k <= 32 sources writing into the plain slabs.
+static bf_status plain_upward(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,
+                              cudaStream_t st) {
+  const unsigned blocks = (k + UPWARD_WARPS - 1) / UPWARD_WARPS;
+  if (g->d_gpath) {
+    k_upward<true><<<blocks, UPWARD_WARPS * 32, 0, st>>>(
+        d_src, k, threshold, g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec,
+        g->d_pos_of, g->n, g->d_seed, PLAIN_K, g->d_flag, g->d_gpath, g->gpath_stride, g->d_err);
+  } else {
+    k_upward<false><<<blocks, UPWARD_WARPS * 32, UPWARD_WARPS * 2 * UPWARD_SMEM_PATH * 4, st>>>(
+        d_src, k, threshold, g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec,
+        g->d_pos_of, g->n, g->d_seed, PLAIN_K, g->d_flag, nullptr, 0, g->d_err);
+  }
+  BF_CUDA(cudaGetLastError());
+  return BF_OK;
+}
+
+static bf_status plain_sweep(Graph* g, uint32_t threshold, cudaStream_t st, uint64_t* launches) {
+  for (uint32_t l = 0; l < g->n_levels; ++l) {
+    uint32_t p0 = g->lvl_start[l], p1 = g->lvl_start[l + 1];
+    if (p1 == p0) continue;
+    unsigned blocks = (unsigned)(((uint64_t)(p1 - p0) * 32 + 255) / 256);
+    k_sweep_level<<<blocks, 256, 0, st>>>(p0, p1, g->d_in_off, g->d_in_rec, g->d_dist, g->d_seed,
+                                          g->d_flag, threshold);
+    ++*launches;
+  }
+  BF_CUDA(cudaGetLastError());
+  return BF_OK;
+}
+
+bf_status plain_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tpos,
+                       uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
+                       bf_stats* stats) {
+  bf_status s;
+  if ((s = plain_buffers(g))) return s;
+  const uint64_t nb = (S + PLAIN_K - 1) / PLAIN_K;
+  uint64_t launches = 0;
+  float t_up = 0, t_dn = 0, t_ex = 0;
+  for (uint64_t b = 0; b < nb; ++b) {
+    const uint64_t s0 = b * PLAIN_K;
+    const uint32_t k = (uint32_t)std::min<uint64_t>(PLAIN_K, S - s0);
+    if (stats) BF_CUDA(cudaEventRecord(g->ev[0], st));
+    if ((s = plain_upward(g, d_src + s0, k, threshold, st))) return s;
+    ++launches;
+    if (stats) BF_CUDA(cudaEventRecord(g->ev[1], st));
+    if ((s = plain_sweep(g, threshold, st, &launches))) return s;
+    if (stats) BF_CUDA(cudaEventRecord(g->ev[2], st));
+    if (T) {
+      dim3 blk(32, 8);
+      k_extract<<<(unsigned)((T + 31) / 32), blk, 0, st>>>(g->d_dist, PLAIN_K, d_tpos, T, k,
+                                                          d_out + s0 * T);
+      BF_CUDA(cudaGetLastError());
+      ++launches;
+    }
+    if (stats) {
+      BF_CUDA(cudaEventRecord(g->ev[3], st));
+      BF_CUDA(cudaEventSynchronize(g->ev[3]));
+      float a, c, d;
+      BF_CUDA(cudaEventElapsedTime(&a, g->ev[0], g->ev[1]));
+      BF_CUDA(cudaEventElapsedTime(&c, g->ev[1], g->ev[2]));
+      BF_CUDA(cudaEventElapsedTime(&d, g->ev[2], g->ev[3]));
+      t_up += a;
+      t_dn += c;
+      t_ex += d;
+    }
+  }
+  if (stats) {
+    stats->n_batches += nb;
+    stats->kernel_launches += launches;
+    stats->upward_ms += t_up;
+    stats->downward_ms += t_dn;
+    stats->extract_ms += t_ex;
+  }
+  return BF_OK;
+}
+
+}  // namespace bf

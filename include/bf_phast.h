@@ -1,0 +1,244 @@
+/*
+ * bf_phast.h — C ABI of the GB300 K-lane PHAST engine.
+ *
+ * Drop-in device layer for butterfly-route's batched PHAST path: many-to-many
+ * duration matrices and bulk isochrones over a rank-aligned CCH. The entry
+ * points mirror the Rust call surface they replace (paths relative to the
+ * butterfly-osm repository):
+ *
+ *   bf_graph_create        BatchedPhastEngine::new / PhastEngine::new
+ *                          route/src/matrix/batched_phast.rs:89, route/src/range/phast.rs:86
+ *                          (+ the INF-filtering flats UpAdjFlat::build_with, DownAdjFlat::build,
+ *                           DownReverseAdjFlat::build_with, route/src/matrix/bucket_ch.rs:191,282,355)
+ *   bf_graph_info          BatchedPhastEngine::n_nodes  batched_phast.rs:115
+ *   bf_query_batch         BatchedPhastEngine::query_batch          batched_phast.rs:131
+ *                          BatchedPhastEngine::query_batch_bounded  batched_phast.rs:271
+ *   bf_phast_query         PhastEngine::query                        phast.rs:155
+ *   bf_matrix              BatchedPhastEngine::compute_matrix_flat   batched_phast.rs:667
+ *                          (and compute_matrix_flat_soa :756, compute_matrix_block_gated :1223)
+ *   bf_matrix_seeded       table_phast_lopsided                      route/src/matrix/bucket_ch.rs:6717
+ *   bf_phast_bounded_seeded run_phast_bounded_fast_seeded            route/src/server/isochrone_handler.rs:338
+ *   bf_isochrone_bitsets   the PHAST part of isochrone_bulk_handler  isochrone_handler.rs:1668-1709
+ *                          and BatchedIsochroneEngine::query_many    route/src/range/batched_isochrone.rs:216
+ *   bf_server_*            the tiling / admission loop of do_matrix  route/src/server/flight.rs:589,957-1110
+ *
+ * Conventions (as in the reference):
+ *   - node ids are CCH ranks (rank-aligned CCH, node_id == rank);
+ *   - distances are u32 deciseconds (any unit works: arithmetic is exact
+ *     saturating u32 min-plus); 0xFFFFFFFF means unreachable;
+ *   - a weight of 0xFFFFFFFF in the input CSR is an INF edge and is dropped,
+ *     exactly like the reference flats;
+ *   - bounded results are exact for values <= threshold; the engine reports
+ *     every cell / node above the threshold as 0xFFFFFFFF (the server-side
+ *     post-filter of the reference, bucket_ch.rs:6800-6803).
+ *
+ * Ownership: the library owns graph and server handles; callers own every
+ * input and output buffer. A graph is immutable after creation; calls on one
+ * graph from several host threads are serialised internally.
+ *
+ * Errors: every entry point returns a bf_status and never aborts. The
+ * message of the last failure on the calling thread is bf_last_error().
+ * The status style follows dl/include/butterfly.h:66-72 of the reference.
+ */
+#ifndef BF_PHAST_H
+#define BF_PHAST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bf_status {
+  BF_OK = 0,
+  BF_ERR_INVALID = 1,     /* bad argument (null pointer, id out of range, ...)   */
+  BF_ERR_OOM = 2,         /* device or pinned-host allocation failed             */
+  BF_ERR_DEVICE = 3,      /* CUDA error or no usable sm_103 device               */
+  BF_ERR_TIMEOUT = 4,     /* a bounded device wait ran out                       */
+  BF_ERR_CANCELLED = 5,   /* request cancelled                                   */
+  BF_ERR_BUSY = 6,        /* admission refused: HBM budget or queue full         */
+  BF_ERR_UNSUPPORTED = 7  /* option not supported on this graph / build          */
+} bf_status;
+
+#define BF_INF 0xFFFFFFFFu
+
+/* Rank-aligned CCH adjacency: CchTopo + CchWeights of the reference
+ * (route/src/formats/cch_topo.rs:250-284, cch_weights.rs:359). UP edges go
+ * from a node to higher ranks, DOWN edges to lower ranks, both indexed by
+ * source rank. Weights of 0xFFFFFFFF are INF and dropped. */
+typedef struct bf_cch_csr {
+  uint32_t n_nodes;
+  uint32_t reserved;
+  const uint64_t* up_offsets;   /* [n_nodes + 1] */
+  const uint32_t* up_targets;   /* [up_offsets[n_nodes]] */
+  const uint32_t* up_weights;   /* [up_offsets[n_nodes]] */
+  const uint64_t* down_offsets; /* [n_nodes + 1] */
+  const uint32_t* down_targets; /* [down_offsets[n_nodes]] */
+  const uint32_t* down_weights; /* [down_offsets[n_nodes]] */
+} bf_cch_csr;
+
+/* Engines behind bf_matrix / bf_matrix_device. */
+typedef enum bf_engine {
+  BF_ENGINE_AUTO = 0,     /* batched engine (the default)                        */
+  BF_ENGINE_PLAIN = 1,    /* one K=32 batch at a time: upward launch, one sweep
+                             launch per level, one extraction launch             */
+  BF_ENGINE_BATCHED = 2   /* persistent multi-batch kernels, shared-memory
+                             subtrees, CUDA-graph level schedule, autotuned K    */
+} bf_engine;
+
+typedef struct bf_config {
+  int32_t device;             /* CUDA device ordinal                               */
+  uint32_t engine;            /* bf_engine                                         */
+  uint32_t k_lanes;           /* lanes per batch for the batched engine (0 = autotune;
+                                 16, 32, 64 or 128)                                */
+  uint32_t flags;             /* reserved, must be 0                               */
+  uint64_t hbm_budget_bytes;  /* cap on device memory for distance slabs and
+                                 scratch (0 = 85% of free memory at creation)      */
+  uint32_t subtree_nodes;     /* max nodes of a shared-memory subtree (0 = auto)   */
+  uint32_t reserved2;
+} bf_config;
+
+typedef struct bf_graph bf_graph;
+
+typedef struct bf_graph_info {
+  uint32_t n_nodes;
+  uint32_t n_levels;          /* levels of the downward pull DAG                   */
+  uint64_t n_up;              /* finite UP edges                                   */
+  uint64_t n_down;            /* finite DOWN edges                                 */
+  uint32_t max_depth;         /* elimination-tree depth (upward path length - 1)   */
+  uint32_t n_top_nodes;       /* nodes above the shared-memory subtrees            */
+  uint32_t n_subtrees;        /* shared-memory subtrees                            */
+  uint32_t k_lanes;           /* lanes per batch chosen for the batched engine     */
+  uint64_t device_bytes;      /* device memory held by the graph                   */
+} bf_graph_info;
+
+/* Per-call statistics (BatchedPhastStats, batched_phast.rs:67-80). Times are
+ * device times from CUDA events, in milliseconds. */
+typedef struct bf_stats {
+  uint64_t n_sources;
+  uint64_t n_targets;
+  uint64_t n_batches;
+  uint64_t kernel_launches;   /* kernels launched by the call                      */
+  double upward_ms;
+  double downward_ms;
+  double extract_ms;
+  double total_ms;            /* whole call, host clock                            */
+  uint64_t h2d_bytes;
+  uint64_t d2h_bytes;
+} bf_stats;
+
+bf_status bf_graph_create(const bf_cch_csr* csr, const bf_config* cfg, bf_graph** out);
+void bf_graph_destroy(bf_graph* g);
+bf_status bf_graph_info_get(const bf_graph* g, bf_graph_info* out);
+/* Select the engine used by bf_matrix / bf_matrix_device on this graph. */
+bf_status bf_graph_set_engine(bf_graph* g, uint32_t engine, uint32_t k_lanes);
+
+/* Distances from k sources to every node: dist_out[lane * n_nodes + node]
+ * (the AoS Vec<Vec<u32>> of query_batch). threshold == BF_INF is unbounded;
+ * otherwise entries above the threshold are BF_INF. k is at most 128. */
+bf_status bf_query_batch(bf_graph* g, const uint32_t* sources, uint32_t k, uint32_t threshold,
+                         uint32_t* dist_out);
+
+/* Single-source unbounded PHAST (PhastEngine::query). */
+bf_status bf_phast_query(bf_graph* g, uint32_t origin, uint32_t* dist_out);
+
+/* S x T duration matrix, row-major out[s * T + t], host buffers. threshold
+ * == BF_INF is unbounded; otherwise cells above it are BF_INF. st may be
+ * NULL. */
+bf_status bf_matrix(bf_graph* g, const uint32_t* sources, uint64_t n_sources,
+                    const uint32_t* targets, uint64_t n_targets, uint32_t threshold,
+                    uint32_t* out, bf_stats* st);
+
+/* Same as bf_matrix with device pointers (sources, targets and out in device
+ * memory of the graph's device). stream is a cudaStream_t or NULL for the
+ * library's own stream; the call returns after the work completed. */
+bf_status bf_matrix_device(bf_graph* g, const uint32_t* d_sources, uint64_t n_sources,
+                           const uint32_t* d_targets, uint64_t n_targets, uint32_t threshold,
+                           uint32_t* d_out, void* stream, bf_stats* st);
+
+/* Phantom-seeded matrix (table_phast_lopsided, bucket_ch.rs:6717-6852).
+ * Source s has seeds src_seeds[src_off[s] .. src_off[s+1]), each a (rank,
+ * cost) pair entered into the field with that cost; target t's value is
+ * min over its seeds (rank, part) of F[rank] - part (saturating). Cells above
+ * the threshold are BF_INF. */
+typedef struct bf_seed {
+  uint32_t rank;
+  uint32_t cost;
+} bf_seed;
+bf_status bf_matrix_seeded(bf_graph* g, const bf_seed* src_seeds, const uint64_t* src_off,
+                           uint64_t n_sources, const bf_seed* tgt_seeds, const uint64_t* tgt_off,
+                           uint64_t n_targets, uint32_t threshold, uint32_t* out, bf_stats* st);
+
+/* run_phast_bounded_fast_seeded: settled (rank, dist <= threshold) pairs in
+ * ascending rank order. Writes at most cap pairs; *n_out receives the full
+ * count. */
+bf_status bf_phast_bounded_seeded(bf_graph* g, const bf_seed* seeds, uint32_t n_seeds,
+                                  uint32_t threshold, uint32_t* out_rank, uint32_t* out_dist,
+                                  uint64_t cap, uint64_t* n_out);
+
+/* Bulk isochrones: origin i with threshold thresholds[i]; bit r of row i
+ * (rows of ceil(n_nodes / 64) u64 words) is set iff dist(origin_i, r) <=
+ * thresholds[i]; counts_out[i] is the row's popcount. counts_out may be
+ * NULL. */
+bf_status bf_isochrone_bitsets(bf_graph* g, const uint32_t* origins, const uint32_t* thresholds,
+                               uint64_t n_origins, uint64_t* bits_out, uint64_t* counts_out,
+                               bf_stats* st);
+
+/* ---- serving loop (continuous batching of matrix and isochrone requests) ---- */
+
+typedef struct bf_server bf_server;
+
+typedef struct bf_server_cfg {
+  uint64_t hbm_budget_bytes;  /* device memory for in-flight request slabs        */
+  uint32_t max_inflight;      /* requests admitted at once (0 = 64)               */
+  uint32_t max_queue;         /* queued requests before BF_ERR_BUSY (0 = 4096)    */
+  uint32_t timeout_ms;        /* bound on every device wait (0 = 10000)           */
+  uint32_t reserved;
+} bf_server_cfg;
+
+typedef enum bf_request_kind { BF_REQ_MATRIX = 1, BF_REQ_ISOCHRONE = 2 } bf_request_kind;
+
+/* A request. For BF_REQ_MATRIX: sources/targets (n_sources x n_targets) and
+ * out (n_sources * n_targets u32). For BF_REQ_ISOCHRONE: one origin in
+ * sources[0], threshold, and out = bitset words (ceil(n_nodes/64) u64 as u32
+ * pairs, little-endian). Buffers are owned by the caller and must stay valid
+ * until the request completes. */
+typedef struct bf_request {
+  uint32_t kind;
+  uint32_t threshold;
+  const uint32_t* sources;
+  uint64_t n_sources;
+  const uint32_t* targets;
+  uint64_t n_targets;
+  void* out;
+  uint64_t user_tag;
+} bf_request;
+
+typedef struct bf_completion {
+  uint64_t user_tag;
+  uint64_t ticket;
+  int32_t status;            /* bf_status of the request                        */
+  uint32_t reserved;
+  double submit_s;           /* host clock, seconds                             */
+  double admit_s;
+  double done_s;
+} bf_completion;
+
+bf_status bf_server_create(bf_graph* g, const bf_server_cfg* cfg, bf_server** out);
+/* Queue a request; *ticket identifies it. Returns BF_ERR_BUSY when the queue
+ * is full or the request alone exceeds the HBM budget. */
+bf_status bf_server_submit(bf_server* s, const bf_request* req, uint64_t* ticket);
+/* Collect up to cap completions; waits up to wait_ms for the first one. */
+bf_status bf_server_poll(bf_server* s, bf_completion* out, uint32_t cap, uint32_t wait_ms,
+                         uint32_t* n_out);
+bf_status bf_server_cancel(bf_server* s, uint64_t ticket);
+void bf_server_destroy(bf_server* s);
+
+const char* bf_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BF_PHAST_H */

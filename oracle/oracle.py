@@ -1,0 +1,141 @@
+"""ctypes binding of the CPU oracle (phast_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, always as the checker or the timed CPU baseline,
+never as part of the product path.
+
+Parity is pinned by the reference's own known-answer tests (see
+tests/golden/reference_kats.json and tests/test_oracle_kat.py) and by plain
+Dijkstra over the edge-based graph.
+"""
+import ctypes
+import pathlib
+
+import numpy as np
+
+from .build import build_oracle
+
+INF = 0xFFFFFFFF
+_lib = None
+_V = ctypes.c_void_p
+
+
+def load():
+    global _lib
+    if _lib is None:
+        so = build_oracle()
+        lib = ctypes.CDLL(str(so))
+        csr = [ctypes.c_uint32] + [_V] * 6
+        lib.orc_phast_query.argtypes = csr + [ctypes.c_uint32, _V]
+        lib.orc_query_batch.argtypes = csr + [_V, ctypes.c_uint32, _V]
+        lib.orc_query_batch_bounded.argtypes = csr + [_V, ctypes.c_uint32, ctypes.c_uint32, _V]
+        lib.orc_matrix_soa.argtypes = csr + [_V, ctypes.c_uint64, _V, ctypes.c_uint64, _V,
+                                             ctypes.c_int]
+        lib.orc_phast_bounded_seeded.argtypes = csr + [_V, _V, ctypes.c_uint32, ctypes.c_uint32,
+                                                       _V, _V, ctypes.c_uint64]
+        lib.orc_phast_bounded_seeded.restype = ctypes.c_uint64
+        lib.orc_isochrone_bitsets.argtypes = csr + [_V, _V, ctypes.c_uint64, _V, _V, ctypes.c_int]
+        lib.orc_dijkstra_ebg.argtypes = [ctypes.c_uint32, _V, _V, _V, ctypes.c_uint32, _V]
+        lib.orc_phast_reverse.argtypes = csr + [ctypes.c_uint32, _V]
+        _lib = lib
+    return _lib
+
+
+def _a(x, dt):
+    return np.ascontiguousarray(x, dtype=dt)
+
+
+class Cch:
+    """Rank-aligned CCH (up / down CSR by source) held for oracle calls."""
+
+    def __init__(self, n, up_off, up_tgt, up_w, down_off, down_tgt, down_w):
+        self.n = int(n)
+        self.arrs = [_a(up_off, np.uint64), _a(up_tgt, np.uint32), _a(up_w, np.uint32),
+                     _a(down_off, np.uint64), _a(down_tgt, np.uint32), _a(down_w, np.uint32)]
+
+    @classmethod
+    def from_dict(cls, d):
+        return cls(d["n"], d["up_off"], d["up_tgt"], d["up_w"], d["down_off"], d["down_tgt"],
+                   d["down_w"])
+
+    def _csr(self):
+        return [self.n] + [a.ctypes.data for a in self.arrs]
+
+    def phast_query(self, origin):
+        out = np.empty(self.n, dtype=np.uint32)
+        load().orc_phast_query(*self._csr(), int(origin), out.ctypes.data)
+        return out
+
+    def query_batch(self, sources):
+        s = _a(sources, np.uint32)
+        out = np.empty((len(s), self.n), dtype=np.uint32)
+        assert load().orc_query_batch(*self._csr(), s.ctypes.data, len(s), out.ctypes.data) == 0
+        return out
+
+    def query_batch_bounded(self, sources, threshold):
+        s = _a(sources, np.uint32)
+        out = np.empty((len(s), self.n), dtype=np.uint32)
+        assert load().orc_query_batch_bounded(*self._csr(), s.ctypes.data, len(s), threshold,
+                                              out.ctypes.data) == 0
+        return out
+
+    def matrix(self, sources, targets, threads=1):
+        """compute_matrix_flat_soa (K = 8); returns (matrix, threads used)."""
+        s, t = _a(sources, np.uint32), _a(targets, np.uint32)
+        out = np.empty((len(s), len(t)), dtype=np.uint32)
+        used = load().orc_matrix_soa(*self._csr(), s.ctypes.data, len(s), t.ctypes.data, len(t),
+                                     out.ctypes.data, threads)
+        return out, used
+
+    def bounded_seeded(self, seeds, threshold):
+        """run_phast_bounded_fast_seeded: (ranks, dists) with dist <= threshold."""
+        r = _a([x[0] for x in seeds], np.uint32)
+        c = _a([x[1] for x in seeds], np.uint32)
+        rk = np.empty(self.n, dtype=np.uint32)
+        ds = np.empty(self.n, dtype=np.uint32)
+        cnt = load().orc_phast_bounded_seeded(*self._csr(), r.ctypes.data, c.ctypes.data, len(r),
+                                              threshold, rk.ctypes.data, ds.ctypes.data, self.n)
+        return rk[:cnt].copy(), ds[:cnt].copy()
+
+    def isochrone_bitsets(self, origins, thresholds, threads=0):
+        o, t = _a(origins, np.uint32), _a(thresholds, np.uint32)
+        words = (self.n + 63) // 64
+        bits = np.empty((len(o), words), dtype=np.uint64)
+        counts = np.empty(len(o), dtype=np.uint64)
+        load().orc_isochrone_bitsets(*self._csr(), o.ctypes.data, t.ctypes.data, len(o),
+                                     bits.ctypes.data, counts.ctypes.data, threads)
+        return bits, counts
+
+    def reverse(self, target, rev_off, rev_src, rev_w):
+        """query_block_gated_reverse with a caller-built DownReverseAdjFlat."""
+        ro, rs, rw = _a(rev_off, np.uint64), _a(rev_src, np.uint32), _a(rev_w, np.uint32)
+        out = np.empty(self.n, dtype=np.uint32)
+        a = self.arrs
+        load().orc_phast_reverse(self.n, a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data,
+                                 ro.ctypes.data, rs.ctypes.data, rw.ctypes.data, int(target),
+                                 out.ctypes.data)
+        return out
+
+
+def dijkstra_ebg(ebg, origin_state):
+    """Plain Dijkstra over the edge-based graph from one state."""
+    off, dst, w = (_a(ebg["arc_off"], np.uint64), _a(ebg["arc_dst"], np.uint32),
+                   _a(ebg["arc_w"], np.uint32))
+    out = np.empty(ebg["n"], dtype=np.uint32)
+    load().orc_dijkstra_ebg(ebg["n"], off.ctypes.data, dst.ctypes.data, w.ctypes.data,
+                            int(origin_state), out.ctypes.data)
+    return out
+
+
+def down_reverse(cch):
+    """DownReverseAdjFlat::build (bucket_ch.rs:355-418): DOWN edges by target."""
+    n = cch.n
+    doff, dtg, dw = cch.arrs[3], cch.arrs[4], cch.arrs[5]
+    src = np.repeat(np.arange(n, dtype=np.uint32), np.diff(doff.astype(np.int64)))
+    keep = dw != INF
+    src, tgt, w = src[keep], dtg[keep], dw[keep]
+    order = np.argsort(tgt, kind="stable")
+    cnt = np.bincount(tgt, minlength=n)
+    off = np.zeros(n + 1, dtype=np.uint64)
+    off[1:] = np.cumsum(cnt)
+    return off, src[order], w[order]

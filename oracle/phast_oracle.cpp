@@ -1,0 +1,378 @@
+// phast_oracle.cpp — CPU oracle for the K-lane PHAST engine.
+//
+// TEST INFRASTRUCTURE ONLY. This file is a plain restatement of the
+// reference's CPU PHAST code paths. It is used by tests/, by the smoke check
+// and by bench.py's CPU-baseline leg as the checker and as the timed CPU
+// baseline. It is never linked into or called by the product library.
+//
+// Every function cites the reference function it restates (paths relative to
+// the butterfly-osm repository). Arithmetic is u32 with saturating add and
+// u32::MAX (0xFFFFFFFF) as "unreachable", exactly as in the reference.
+
+#include <omp.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <queue>
+#include <vector>
+
+namespace {
+
+using u32 = uint32_t;
+using u64 = uint64_t;
+constexpr u32 INF = 0xFFFFFFFFu;
+
+inline u32 sat_add(u32 a, u32 b) {
+  u64 s = (u64)a + b;
+  return s >= INF ? INF : (u32)s;
+}
+
+struct Csr {
+  const u64* off;
+  const u32* tgt;
+  const u32* w;
+};
+
+using MinHeap = std::priority_queue<std::pair<u32, u32>, std::vector<std::pair<u32, u32>>,
+                                    std::greater<std::pair<u32, u32>>>;
+
+// Upward Dijkstra from one origin writing into dist (stride elements apart);
+// bounded by `threshold` when `bounded` is set (phast.rs:308-315 early stop).
+void upward(const Csr& up, u32 origin, u32* dist, size_t stride, bool bounded, u32 threshold) {
+  MinHeap pq;
+  pq.push({0u, origin});
+  while (!pq.empty()) {
+    auto [d, u] = pq.top();
+    pq.pop();
+    if (bounded && d > threshold) break;
+    if (d > dist[(size_t)u * stride]) continue;
+    for (u64 i = up.off[u]; i < up.off[u + 1]; ++i) {
+      u32 w = up.w[i];
+      if (w == INF) continue;
+      u32 v = up.tgt[i];
+      u32 nd = sat_add(d, w);
+      if (nd < dist[(size_t)v * stride]) {
+        dist[(size_t)v * stride] = nd;
+        pq.push({nd, v});
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// PhastEngine::query — route/src/range/phast.rs:155-263.
+// Unbounded single-source PHAST over the rank-aligned CCH (INF weights are
+// skipped in both phases, phast.rs:191-193 and :238-240).
+void orc_phast_query(u32 n, const u64* up_off, const u32* up_tgt, const u32* up_w,
+                     const u64* dn_off, const u32* dn_tgt, const u32* dn_w, u32 origin,
+                     u32* dist) {
+  std::fill(dist, dist + n, INF);
+  dist[origin] = 0;
+  upward({up_off, up_tgt, up_w}, origin, dist, 1, false, INF);
+  for (u32 r = n; r-- > 0;) {
+    u32 du = dist[r];
+    if (du == INF) continue;
+    for (u64 i = dn_off[r]; i < dn_off[r + 1]; ++i) {
+      u32 w = dn_w[i];
+      if (w == INF) continue;
+      u32 v = dn_tgt[i];
+      u32 nd = sat_add(du, w);
+      if (nd < dist[v]) dist[v] = nd;
+    }
+  }
+}
+
+// BatchedPhastEngine::query_batch — route/src/matrix/batched_phast.rs:131-260.
+// k <= 8 sources; K separate upward heaps, one downward scan that skips a node
+// when every lane is unreachable (:220-223). Output is AoS: dist[lane*n+node].
+int orc_query_batch(u32 n, const u64* up_off, const u32* up_tgt, const u32* up_w,
+                    const u64* dn_off, const u32* dn_tgt, const u32* dn_w, const u32* src,
+                    u32 k, u32* dist) {
+  if (k > 8) return 1;  // batched_phast.rs:132 asserts sources.len() <= K_LANES
+  std::fill(dist, dist + (size_t)k * n, INF);
+  for (u32 l = 0; l < k; ++l) dist[(size_t)l * n + src[l]] = 0;
+  Csr up{up_off, up_tgt, up_w};
+  for (u32 l = 0; l < k; ++l) upward(up, src[l], dist + (size_t)l * n, 1, false, INF);
+  for (u32 r = n; r-- > 0;) {
+    if (dn_off[r] == dn_off[r + 1]) continue;
+    bool any = false;
+    for (u32 l = 0; l < k; ++l) any |= dist[(size_t)l * n + r] != INF;
+    if (!any) continue;
+    for (u64 i = dn_off[r]; i < dn_off[r + 1]; ++i) {
+      u32 w = dn_w[i];
+      if (w == INF) continue;
+      u32 v = dn_tgt[i];
+      for (u32 l = 0; l < k; ++l) {
+        u32 du = dist[(size_t)l * n + r];
+        if (du != INF) {
+          u32 nd = sat_add(du, w);
+          u32& dv = dist[(size_t)l * n + v];
+          if (nd < dv) dv = nd;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+// BatchedPhastEngine::query_batch_bounded — batched_phast.rs:271-445.
+// Per-lane upward early stop at d > T, per-lane active blocks of 512 ranks,
+// downward relaxes only new_dist <= T. Values > T are implementation
+// artefacts in the reference too; only entries <= T are meaningful.
+int orc_query_batch_bounded(u32 n, const u64* up_off, const u32* up_tgt, const u32* up_w,
+                            const u64* dn_off, const u32* dn_tgt, const u32* dn_w,
+                            const u32* src, u32 k, u32 threshold, u32* dist) {
+  if (k > 8) return 1;
+  const u32 BS = 512;
+  u32 nb = (n + BS - 1) / BS;
+  std::vector<std::vector<uint8_t>> active(k, std::vector<uint8_t>(nb, 0));
+  std::fill(dist, dist + (size_t)k * n, INF);
+  for (u32 l = 0; l < k; ++l) {
+    dist[(size_t)l * n + src[l]] = 0;
+    active[l][src[l] / BS] = 1;
+  }
+  for (u32 l = 0; l < k; ++l) {
+    u32* d = dist + (size_t)l * n;
+    MinHeap pq;
+    pq.push({0u, src[l]});
+    while (!pq.empty()) {
+      auto [du, u] = pq.top();
+      pq.pop();
+      if (du > threshold) break;
+      if (du > d[u]) continue;
+      for (u64 i = up_off[u]; i < up_off[u + 1]; ++i) {
+        u32 w = up_w[i];
+        if (w == INF) continue;
+        u32 v = up_tgt[i], nd = sat_add(du, w);
+        if (nd < d[v]) {
+          d[v] = nd;
+          pq.push({nd, v});
+          if (nd <= threshold) active[l][v / BS] = 1;
+        }
+      }
+    }
+  }
+  std::vector<uint8_t> lane_on(k, 0);
+  for (u32 l = 0; l < k; ++l)
+    for (u32 b = 0; b < nb; ++b) lane_on[l] |= active[l][b];
+  for (u32 r = n; r-- > 0;) {
+    if (dn_off[r] == dn_off[r + 1]) continue;
+    u32 blk = r / BS;
+    bool any = false;
+    for (u32 l = 0; l < k; ++l) any |= lane_on[l] && active[l][blk];
+    if (!any) continue;
+    for (u64 i = dn_off[r]; i < dn_off[r + 1]; ++i) {
+      u32 w = dn_w[i];
+      if (w == INF) continue;
+      u32 v = dn_tgt[i];
+      for (u32 l = 0; l < k; ++l) {
+        if (!lane_on[l] || !active[l][blk]) continue;
+        u32 du = dist[(size_t)l * n + r];
+        if (du == INF) continue;
+        u32 nd = sat_add(du, w);
+        u32& dv = dist[(size_t)l * n + v];
+        if (nd <= threshold && nd < dv) {
+          dv = nd;
+          active[l][v / BS] = 1;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+// BatchedPhastEngine::compute_matrix_flat_soa + query_batch_soa_raw —
+// batched_phast.rs:756-917. K = 8 lanes in SoA layout dist[node*8 + lane];
+// sources chunked by 8; the row-major S x T matrix is gathered from the SoA
+// slab. n_threads > 1 runs independent K-batches on worker threads, the
+// rayon shape of bucket_ch.rs:6814-6823. Returns the number of threads used.
+int orc_matrix_soa(u32 n, const u64* up_off, const u32* up_tgt, const u32* up_w,
+                   const u64* dn_off, const u32* dn_tgt, const u32* dn_w, const u32* src,
+                   u64 S, const u32* tgt, u64 T, u32* out, int n_threads) {
+  const u32 K = 8;
+  u64 nbatch = (S + K - 1) / K;
+  if (n_threads <= 0) n_threads = omp_get_max_threads();
+  int used = 1;
+#pragma omp parallel num_threads(n_threads)
+  {
+#pragma omp single
+    used = omp_get_num_threads();
+    std::vector<u32> soa((size_t)n * K);
+    Csr up{up_off, up_tgt, up_w};
+#pragma omp for schedule(dynamic, 1)
+    for (u64 b = 0; b < nbatch; ++b) {
+      u64 s0 = b * K;
+      u32 k = (u32)std::min<u64>(K, S - s0);
+      std::fill(soa.begin(), soa.end(), INF);
+      for (u32 l = 0; l < k; ++l) soa[(size_t)src[s0 + l] * K + l] = 0;
+      for (u32 l = 0; l < k; ++l) upward(up, src[s0 + l], soa.data() + l, K, false, INF);
+      for (u32 r = n; r-- > 0;) {
+        if (dn_off[r] == dn_off[r + 1]) continue;
+        const u32* ur = soa.data() + (size_t)r * K;
+        bool any = false;
+        for (u32 l = 0; l < k; ++l) any |= ur[l] != INF;
+        if (!any) continue;
+        u32 du[K];
+        for (u32 l = 0; l < K; ++l) du[l] = l < k ? ur[l] : INF;
+        for (u64 i = dn_off[r]; i < dn_off[r + 1]; ++i) {
+          u32 w = dn_w[i];
+          if (w == INF) continue;
+          u32* vr = soa.data() + (size_t)dn_tgt[i] * K;
+          for (u32 l = 0; l < k; ++l)
+            if (du[l] != INF) {
+              u32 nd = sat_add(du[l], w);
+              if (nd < vr[l]) vr[l] = nd;
+            }
+        }
+      }
+      for (u32 l = 0; l < k; ++l)
+        for (u64 t = 0; t < T; ++t) out[(s0 + l) * T + t] = soa[(size_t)tgt[t] * K + l];
+    }
+  }
+  return used;
+}
+
+// run_phast_bounded_fast_seeded — route/src/server/isochrone_handler.rs:338-491
+// with PhastState (:132-227). Multi-seed (rank, cost) init, bounded upward
+// heap (break at d > T), block-gated downward scan (4096-rank blocks, skip
+// d_u > T), and the ascending-rank collection of settled (rank, d <= T).
+// Writes up to `cap` pairs; returns the number of settled pairs.
+u64 orc_phast_bounded_seeded(u32 n, const u64* up_off, const u32* up_tgt, const u32* up_w,
+                             const u64* dn_off, const u32* dn_tgt, const u32* dn_w,
+                             const u32* seed_rank, const u32* seed_cost, u32 n_seeds,
+                             u32 threshold, u32* out_rank, u32* out_dist, u64 cap) {
+  const u32 BS = 4096;
+  u32 nb = (n + BS - 1) / BS;
+  // a fresh generation per call: version == 1 marks "set this query"
+  std::vector<u32> dist(n, INF);
+  std::vector<uint8_t> version(n, 0), block(nb, 0);
+  auto get = [&](u32 v) { return version[v] ? dist[v] : INF; };
+  auto set = [&](u32 v, u32 d) {
+    dist[v] = d;
+    version[v] = 1;
+    block[v / BS] = 1;
+  };
+  for (u32 i = 0; i < n_seeds; ++i)
+    if (seed_cost[i] < get(seed_rank[i])) set(seed_rank[i], seed_cost[i]);
+  MinHeap pq;
+  for (u32 i = 0; i < n_seeds; ++i)
+    if (get(seed_rank[i]) == seed_cost[i]) pq.push({seed_cost[i], seed_rank[i]});
+  while (!pq.empty()) {
+    auto [d, u] = pq.top();
+    pq.pop();
+    if (d > threshold) break;
+    if (d > get(u)) continue;
+    for (u64 i = up_off[u]; i < up_off[u + 1]; ++i) {
+      u32 v = up_tgt[i], nd = sat_add(d, up_w[i]);
+      if (nd < get(v)) {
+        set(v, nd);
+        pq.push({nd, v});
+      }
+    }
+  }
+  for (u32 b = nb; b-- > 0;) {
+    if (!block[b]) continue;
+    u32 lo = b * BS, hi = std::min(n, lo + BS);
+    for (u32 r = hi; r-- > lo;) {
+      u32 du = get(r);
+      if (du == INF || du > threshold) continue;
+      for (u64 i = dn_off[r]; i < dn_off[r + 1]; ++i) {
+        u32 v = dn_tgt[i], nd = sat_add(du, dn_w[i]);
+        if (nd < get(v)) set(v, nd);
+      }
+    }
+  }
+  u64 cnt = 0;
+  for (u32 b = 0; b < nb; ++b) {
+    if (!block[b]) continue;
+    u32 lo = b * BS, hi = std::min(n, lo + BS);
+    for (u32 r = lo; r < hi; ++r)
+      if (version[r] && dist[r] <= threshold) {
+        if (cnt < cap) {
+          out_rank[cnt] = r;
+          out_dist[cnt] = dist[r];
+        }
+        ++cnt;
+      }
+  }
+  return cnt;
+}
+
+// Bulk isochrone reachable sets: for origin i, bit r of row i is set iff rank
+// r is settled with d <= T_i by run_phast_bounded_fast_seeded (the
+// `reachable_edges` set of isochrone_handler.rs:1271-1278). Rows are
+// ceil(n/64) u64 words. counts[i] = popcount of row i.
+void orc_isochrone_bitsets(u32 n, const u64* up_off, const u32* up_tgt, const u32* up_w,
+                           const u64* dn_off, const u32* dn_tgt, const u32* dn_w,
+                           const u32* origins, const u32* thresholds, u64 n_orig, u64* bits,
+                           u64* counts, int n_threads) {
+  u64 words = (n + 63) / 64;
+  if (n_threads <= 0) n_threads = omp_get_max_threads();
+#pragma omp parallel num_threads(n_threads)
+  {
+    std::vector<u32> rk(n), ds(n);
+#pragma omp for schedule(dynamic, 1)
+    for (u64 i = 0; i < n_orig; ++i) {
+      u32 zero = 0;
+      u64 c = orc_phast_bounded_seeded(n, up_off, up_tgt, up_w, dn_off, dn_tgt, dn_w,
+                                       &origins[i], &zero, 1, thresholds[i], rk.data(),
+                                       ds.data(), n);
+      u64* row = bits + i * words;
+      std::memset(row, 0, words * 8);
+      for (u64 j = 0; j < c; ++j) row[rk[j] >> 6] |= 1ull << (rk[j] & 63);
+      counts[i] = c;
+    }
+  }
+}
+
+// Plain Dijkstra over the edge-based graph (validate/cch_correctness.rs
+// pattern: an independent ground truth for the CCH pipeline).
+void orc_dijkstra_ebg(u32 n, const u64* arc_off, const u32* arc_dst, const u32* arc_w,
+                      u32 origin, u32* dist) {
+  std::fill(dist, dist + n, INF);
+  dist[origin] = 0;
+  MinHeap pq;
+  pq.push({0u, origin});
+  while (!pq.empty()) {
+    auto [d, u] = pq.top();
+    pq.pop();
+    if (d > dist[u]) continue;
+    for (u64 i = arc_off[u]; i < arc_off[u + 1]; ++i) {
+      u32 v = arc_dst[i], nd = sat_add(d, arc_w[i]);
+      if (nd < dist[v]) {
+        dist[v] = nd;
+        pq.push({nd, v});
+      }
+    }
+  }
+}
+
+// PhastEngine::query_block_gated_reverse (all-to-one) — phast.rs:879-1001.
+// Upward over the DOWN-reverse flat (in-edges of DOWN, bucket_ch.rs:355-418),
+// then a pull over UP edges in descending rank order. rev_off/rev_src/rev_w
+// is the DownReverseAdjFlat; up_* the UpAdjFlat.
+void orc_phast_reverse(u32 n, const u64* up_off, const u32* up_tgt, const u32* up_w,
+                       const u64* rev_off, const u32* rev_src, const u32* rev_w, u32 target,
+                       u32* dist) {
+  std::fill(dist, dist + n, INF);
+  dist[target] = 0;
+  upward({rev_off, rev_src, rev_w}, target, dist, 1, false, INF);
+  for (u32 r = n; r-- > 0;) {
+    u32 best = dist[r];
+    for (u64 i = up_off[r]; i < up_off[r + 1]; ++i) {
+      u32 w = up_w[i];
+      if (w == INF) continue;
+      u32 dv = dist[up_tgt[i]];
+      if (dv == INF) continue;
+      best = std::min(best, sat_add(dv, w));
+    }
+    dist[r] = best;
+  }
+}
+
+}  // extern "C"

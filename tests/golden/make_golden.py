@@ -1,0 +1,105 @@
+"""Writes the golden fixtures under tests/golden/.
+
+reference_kats.json
+    Known-answer vectors transcribed from the reference's own unit tests
+    (paths relative to the butterfly-osm repository):
+      * route/src/range/phast.rs:1180-1250   5-node CCH (build_test_cch) and
+        its forward / reverse results (test_reverse_phast_simple :1255-1390,
+        test_reverse_phast_bounded :1420-1445)
+      * route/src/range/phast.rs:1447-1560   asymmetric 3-node CCH
+        (test_reverse_phast_asymmetric)
+      * route/src/matrix/bucket_ch.rs:4855-4905  4-node CCH with INF entries
+        (make_cch) — 3 finite UP and 3 finite DOWN edges survive the flats
+      * route/src/matrix/bucket_ch.rs:5619-5700  broom graph, closed-form
+        matrix d(s,t) = wu[s] + wd[t] (0 on the diagonal) with the bounded
+        thresholds the tests sweep (:5721-5760)
+
+grid100_matrix.npz
+    The 100 x 100 matrix of the 100 x 100 synthetic grid computed by the CPU
+    oracle (a restatement of compute_matrix_flat_soa) with the seeded
+    sources/targets of workload.sources_targets, plus a fingerprint of the
+    contracted graph so drift of the build pipeline between machines is
+    caught. Regenerate with:  python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import pathlib
+import sys
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT / "butterfly-osm_gb300"))
+sys.path.insert(0, str(ROOT))
+
+INF = 0xFFFFFFFF
+
+
+def kats():
+    broom = {}
+    for n_leaf in (5, 12):
+        wu = [(i + 1) * 10 for i in range(n_leaf)]
+        wd = [i + 1 for i in range(n_leaf)]
+        n = n_leaf + 1
+        up_off = [min(i, n_leaf) for i in range(n + 1)]
+        down_off = [0] * (n_leaf + 1) + [n_leaf]
+        expect = [[0 if s == t else wu[s] + wd[t] for t in range(n_leaf)] for s in range(n_leaf)]
+        broom[str(n_leaf)] = dict(
+            cch=dict(n=n, up_off=up_off, up_tgt=[n_leaf] * n_leaf, up_w=wu, down_off=down_off,
+                     down_tgt=list(range(n_leaf)), down_w=wd),
+            expect=expect,
+            thresholds=[0, 15, 25, 55, 1000] if n_leaf == 5 else [0, 30, 75, 130, 100000])
+    return {
+        "five_node": {
+            "source": "route/src/range/phast.rs:1180-1250",
+            "cch": dict(n=5, up_off=[0, 1, 2, 4, 4, 4], up_tgt=[2, 2, 3, 4], up_w=[10, 3, 7, 5],
+                        down_off=[0, 0, 0, 2, 3, 4], down_tgt=[0, 1, 2, 2],
+                        down_w=[10, 3, 7, 5]),
+            "fwd": {"0": [0, 13, 10, 17, 15]},
+            "rev": {"0": [0, 13, 10, 17, 15]},
+            "rev_bounded_count": {"target": 0, "threshold": 12, "count": 2},
+        },
+        "asym_three_node": {
+            "source": "route/src/range/phast.rs:1447-1560",
+            "cch": dict(n=3, up_off=[0, 1, 2, 2], up_tgt=[2, 2], up_w=[10, 5],
+                        down_off=[0, 0, 0, 2], down_tgt=[0, 1], down_w=[20, 3]),
+            "fwd": {"0": [0, 13, 10], "1": [25, 0, 5], "2": [20, 3, 0]},
+            "rev": {"0": [0, 25, 20]},
+        },
+        "inf_four_node": {
+            "source": "route/src/matrix/bucket_ch.rs:4855-4905",
+            "cch": dict(n=4, up_off=[0, 1, 2, 4, 4], up_tgt=[2, 2, 3, 3], up_w=[10, 3, 7, INF],
+                        down_off=[0, 0, 0, 2, 4], down_tgt=[0, 1, 2, 2],
+                        down_w=[10, 3, 7, INF]),
+            "finite_up": 3,
+            "finite_down": 3,
+        },
+        "broom": {"source": "route/src/matrix/bucket_ch.rs:5619-5760", **broom},
+    }
+
+
+def fingerprint(cch):
+    h = hashlib.sha256()
+    for k in ("up_off", "up_tgt", "up_w", "down_off", "down_tgt", "down_w"):
+        h.update(np.ascontiguousarray(cch[k]).tobytes())
+    return h.hexdigest()
+
+
+def main():
+    (HERE / "reference_kats.json").write_text(json.dumps(kats(), indent=1) + "\n")
+    import cchbuild
+    import workload
+    from oracle import oracle as orc
+    _, cch = cchbuild.build_synthetic(cchbuild.KIND_GRID, 100, 100, seed=42)
+    src, tgt = workload.sources_targets(cch["n"], 100, 100, seed=42)
+    m, _ = orc.Cch.from_dict(cch).matrix(src, tgt, threads=0)
+    np.savez_compressed(HERE / "grid100_matrix.npz", sources=src, targets=tgt, matrix=m,
+                        n=np.uint32(cch["n"]), n_up=np.uint64(len(cch["up_tgt"])),
+                        n_down=np.uint64(len(cch["down_tgt"])),
+                        sha256=np.array(fingerprint(cch)))
+    print("wrote", HERE / "reference_kats.json", HERE / "grid100_matrix.npz")
+
+
+if __name__ == "__main__":
+    main()

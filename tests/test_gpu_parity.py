@@ -1,0 +1,146 @@
+"""GPU engine vs the CPU oracle, through the C ABI. Bit-exact (tolerance 0:
+all arithmetic is u32 saturating min-plus)."""
+import pathlib
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+INF = 0xFFFFFFFF
+GOLDEN = pathlib.Path(__file__).parent / "golden"
+
+
+def _graph(d, **kw):
+    import bfphast
+    return bfphast.Graph(d["n"], d["up_off"], d["up_tgt"], d["up_w"], d["down_off"],
+                         d["down_tgt"], d["down_w"], **kw)
+
+
+ENGINES = ["plain", "batched"]
+
+
+def _engine(g, name):
+    import bfphast
+    g.set_engine(bfphast.ENGINE_PLAIN if name == "plain" else bfphast.ENGINE_BATCHED)
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_kat_five_node_and_asym(built, kats, engine):
+    for key in ("five_node", "asym_three_node"):
+        k = kats[key]
+        g = _graph(k["cch"])
+        _engine(g, engine)
+        for s, want in k["fwd"].items():
+            assert g.phast_query(int(s)).tolist() == want
+        n = k["cch"]["n"]
+        m = g.matrix(np.arange(n), np.arange(n))
+        c = orc.Cch(**{"n": n, **{x: k["cch"][x] for x in ("up_off", "up_tgt", "up_w",
+                                                          "down_off", "down_tgt", "down_w")}})
+        want, _ = c.matrix(np.arange(n), np.arange(n))
+        assert np.array_equal(m, want)
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_kat_inf_four_node(built, kats, engine):
+    g = _graph(kats["inf_four_node"]["cch"])
+    _engine(g, engine)
+    info = g.info()
+    assert info["n_up"] == 3 and info["n_down"] == 3
+    assert g.phast_query(0).tolist() == [0, 13, 10, 17]
+    assert g.phast_query(3).tolist() == [17, 10, 7, 0]
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("n_leaf", ["5", "12"])
+def test_kat_broom_bounded(built, kats, engine, n_leaf):
+    b = kats["broom"][n_leaf]
+    g = _graph(b["cch"])
+    _engine(g, engine)
+    n = int(n_leaf)
+    expect = np.array(b["expect"], dtype=np.uint32)
+    assert np.array_equal(g.matrix(np.arange(n), np.arange(n)), expect)
+    for thr in b["thresholds"]:
+        m = g.matrix(np.arange(n), np.arange(n), threshold=thr)
+        assert np.array_equal(m, np.where(expect <= thr, expect, INF))
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_grid100_matrix_golden(built, grid100, engine):
+    _, cch = grid100
+    gold = np.load(GOLDEN / "grid100_matrix.npz")
+    g = _graph(cch)
+    _engine(g, engine)
+    m = g.matrix(gold["sources"], gold["targets"])
+    assert m.dtype == np.uint32 and np.array_equal(m, gold["matrix"])
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_grid100_query_batch_vs_oracle(built, grid100, engine):
+    _, cch = grid100
+    c = orc.Cch.from_dict(cch)
+    g = _graph(cch)
+    _engine(g, engine)
+    src = np.array([0, 1, 77, 5000, 12345, 20000, 35723, 35000], dtype=np.uint32)
+    assert np.array_equal(g.query_batch(src), c.query_batch(src))
+    # 40 sources: more than one K = 32 batch
+    src40 = np.arange(0, cch["n"], cch["n"] // 40, dtype=np.uint32)[:40]
+    got = g.query_batch(src40)
+    for lane in range(0, 40, 7):
+        assert np.array_equal(got[lane], c.phast_query(src40[lane]))
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_grid100_bounded(built, grid100, engine):
+    _, cch = grid100
+    c = orc.Cch.from_dict(cch)
+    g = _graph(cch)
+    _engine(g, engine)
+    src = np.arange(3, cch["n"], 997, dtype=np.uint32)[:36]
+    full = np.stack([c.phast_query(s) for s in src])
+    tgt = np.arange(0, cch["n"], 3, dtype=np.uint32)
+    for thr in (0, 400, 2500, 9000):
+        m = g.matrix(src, tgt, threshold=thr)
+        want = full[:, tgt]
+        assert np.array_equal(m, np.where(want <= thr, want, INF))
+
+
+def test_country_small_matrix(built, country_small):
+    import workload
+    _, cch = country_small
+    c = orc.Cch.from_dict(cch)
+    g = _graph(cch)
+    src, tgt = workload.sources_targets(cch["n"], 70, 300, seed=5)
+    want, _ = c.matrix(src, tgt)
+    for eng in ENGINES:
+        _engine(g, eng)
+        assert np.array_equal(g.matrix(src, tgt), want)
+
+
+def test_invalid_ids_rejected(built, grid100):
+    import bfphast
+    _, cch = grid100
+    g = _graph(cch)
+    with pytest.raises(bfphast.BfError) as e:
+        g.matrix([0, cch["n"]], [1])
+    assert e.value.status == bfphast.BF_ERR_INVALID
+    # the graph stays usable after a rejected call
+    assert g.phast_query(0)[0] == 0
+
+
+def test_empty_inputs(built, grid100):
+    _, cch = grid100
+    g = _graph(cch)
+    assert g.matrix(np.zeros(0, np.uint32), [1, 2]).shape == (0, 2)
+    assert g.matrix([1, 2], np.zeros(0, np.uint32)).shape == (2, 0)
+
+
+def test_duplicate_sources_and_targets(built, grid100):
+    _, cch = grid100
+    c = orc.Cch.from_dict(cch)
+    g = _graph(cch)
+    src = np.array([9, 9, 9, 100, 9], dtype=np.uint32)
+    tgt = np.array([9, 100, 100, 9], dtype=np.uint32)
+    want, _ = c.matrix(src, tgt)
+    assert np.array_equal(g.matrix(src, tgt), want)
