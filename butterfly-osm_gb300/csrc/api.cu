@@ -67,7 +67,7 @@ bf_status run_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t
                      uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                      bf_stats* stats) {
   bf_status s;
-  if (g->engine == BF_ENGINE_PLAIN || !g->bt.ready) {
+  if (g->engine == BF_ENGINE_PLAIN) {
     DevBuf tpos;
     if ((s = tpos.alloc(T * 4))) return s;
     if ((s = to_positions(g, d_tgt, T, tpos.as<uint32_t>(), st))) return s;
@@ -182,8 +182,6 @@ bf_status bf_graph_info_get(const bf_graph* h, bf_graph_info* o) {
   o->n_up = g.n_up;
   o->n_down = g.n_down;
   o->max_depth = g.max_depth;
-  o->n_top_nodes = g.bt.n_top;
-  o->n_subtrees = g.bt.n_sub;
   o->k_lanes = g.k_lanes;
   o->device_bytes = g.device_bytes;
   return BF_OK;

@@ -35,16 +35,6 @@ constexpr uint32_t PLAIN_K = 32;
 constexpr uint32_t UPWARD_SMEM_PATH = 2048;
 constexpr uint32_t UPWARD_WARPS = 4;
 
-// Shared-memory subtree task of the batched engine.
-struct SubtreeMeta {
-  uint32_t node0;      // first subtree position (positions are contiguous)
-  uint32_t n_nodes;    // nodes in the subtree
-  uint32_t lvl0;       // first entry in the subtree-level table
-  uint32_t n_lvls;     // local levels
-  uint64_t edge0;      // first edge record
-  uint64_t n_edges;    // edge records (internal + boundary)
-};
-
 struct Graph {
   int device = 0;
   uint32_t n = 0;
@@ -81,31 +71,26 @@ struct Graph {
   uint32_t* d_gpath = nullptr;    // global fallback for deep ancestor paths
   uint32_t gpath_stride = 0;      // entries per warp in d_gpath (2 * (max_depth + 1))
 
-  // ---- batched engine (shared-memory subtrees) ----
-  struct Batched {
-    bool ready = false;
-    uint32_t S_max = 0;             // max subtree nodes
-    uint32_t n_top = 0;             // nodes above the subtrees
-    uint32_t n_sub = 0;             // subtrees
-    std::vector<uint32_t> tchunk;   // top schedule: chunk start (top positions), n_chunks + 1
-    std::vector<uint64_t> tchunk_e; // top schedule: chunk edge start, n_chunks + 1
-    std::vector<uint8_t> tchunk_sync; // 1 = a CTA barrier precedes this chunk
-    uint32_t* d_tchunk = nullptr;
-    uint64_t* d_tchunk_e = nullptr;
-    uint8_t* d_tchunk_sync = nullptr;
-    uint32_t n_tchunks = 0;
-    uint4* d_top_rec = nullptr;     // top-tree edges {src top pos, w, dst slot, 0}
-    uint32_t* d_top_of = nullptr;   // [n] rank -> top position or NONE
-    uint32_t* d_sub_of = nullptr;   // [n] rank -> subtree id or NONE
-    uint32_t* d_loc_of = nullptr;   // [n] rank -> position inside its subtree
-    uint32_t* d_top_rank = nullptr; // [n_top] top position -> rank
-    SubtreeMeta* d_sub = nullptr;   // [n_sub]
-    uint32_t* d_slvl = nullptr;     // subtree level table: local level start (local index)
-    uint4* d_sub_rec = nullptr;     // subtree edges {src, w, dst local, is_boundary}
-    uint32_t* d_sub_rank = nullptr; // [n] subtree-ordered rank list (node0 + local)
-    std::vector<SubtreeMeta> sub;
-    uint64_t n_top_edges = 0, n_sub_edges = 0;
-  } bt;
+  // host copies of the pull CSR (target restriction is computed on the host)
+  std::vector<uint64_t> h_in_off;  // [n+1] by slab position
+  std::vector<uint2> h_in_rec;     // {source position, w}
+
+  // ---- batched engine: cached target-restricted schedule ----
+  struct Sched {
+    bool valid = false;
+    uint64_t key = 0;              // hash of the target positions
+    uint32_t n_r = 0;              // restricted nodes
+    uint64_t n_items = 0;
+    std::vector<uint32_t> lvl_item;  // level -> first work item, n_levels + 1
+    uint32_t* d_cidx = nullptr;    // [n] rank -> compact row or NONE
+    uint4* d_item = nullptr;       // {row, edge0, edge1, split flag}
+    uint2* d_erec = nullptr;       // {source row, w}
+    uint32_t* d_trow = nullptr;    // [T] target rows
+    uint64_t T = 0;
+    size_t cap_items = 0, cap_edges = 0, cap_t = 0;
+  } sc;
+  uint32_t* d_slab = nullptr;      // batched distance slab [rows][Kp]
+  size_t slab_bytes = 0;
 };
 
 // graph.cu
@@ -121,9 +106,15 @@ bf_status plain_dist(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t thres
 bf_status to_positions(Graph* g, const uint32_t* d_rank, uint64_t n, uint32_t* d_pos,
                        cudaStream_t st);
 bf_status check_device_error(Graph* g, cudaStream_t st);
+bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t threshold,
+                        const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
+                        cudaStream_t st);
+__global__ void k_extract(const uint32_t* __restrict__ slab, uint32_t slab_stride,
+                          const uint32_t* __restrict__ tpos, uint64_t T, uint32_t k,
+                          uint32_t* __restrict__ out);
 
 // engine_batched.cu
-bf_status batched_prepare(Graph* g, uint32_t S_max);
+bf_status batched_prepare(Graph* g, uint32_t split_edges);
 bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
                          uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                          bf_stats* stats);

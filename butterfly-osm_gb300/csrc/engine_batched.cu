@@ -1,21 +1,301 @@
-// engine_batched.cu — batched engine (shared-memory subtrees). Filled in below.
+// engine_batched.cu — the batched GPU PHAST engine.
+//
+// All sources of a call (up to the HBM budget) run as the lanes of ONE
+// level-synchronous sweep over a [row][lane] u32 slab, instead of the
+// reference's chunks of K_LANES = 8 (batched_phast.rs:33, :667-706):
+//
+//   * target restriction (RPHAST): only rows that reach a requested target
+//     through DOWN edges are swept. They are found by one descending scan of
+//     the level-ordered pull CSR (in-edge sources always sit at lower slab
+//     positions). Their distances at the targets are exactly the unrestricted
+//     ones: every DOWN path into a target stays inside the restricted set.
+//   * upward: the k_upward path walk writes each source's settled ancestors
+//     straight into its lane of the (INF-initialised) slab.
+//   * sweep: one launch per level of the restricted DAG; a work item is a
+//     node (or a slice of at most SPLIT in-edges of a high in-degree node);
+//     a thread owns 4 consecutive lanes, so every gathered source row is a
+//     contiguous, coalesced uint4 stream. Sliced nodes combine with atomicMin.
+//   * extract: target rows -> row-major S x T matrix via a shared-memory
+//     transpose; cells above the threshold become INF.
+
+#include <algorithm>
+#include <cstring>
+
 #include "engine.cuh"
 
 namespace bf {
 
-bf_status batched_prepare(Graph* g, uint32_t S_max) {
-  (void)g;
-  (void)S_max;
+namespace {
+
+constexpr uint32_t SPLIT = 16;  // max in-edges per work item
+
+uint64_t hash_targets(const uint32_t* t, uint64_t T) {
+  uint64_t h = 1469598103934665603ull ^ T;
+  for (uint64_t i = 0; i < T; ++i) {
+    h ^= t[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+template <class T>
+bf_status ensure(T** p, size_t& cap, size_t need, Graph* g) {
+  if (need <= cap && *p) return BF_OK;
+  if (*p) {
+    cudaFree(*p);
+    g->device_bytes -= cap * sizeof(T);
+  }
+  *p = nullptr;
+  cap = 0;
+  size_t n = std::max<size_t>(need, 1);
+  if (cudaMalloc((void**)p, n * sizeof(T)) != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    set_error("cudaMalloc for the restricted schedule failed");
+    return BF_ERR_OOM;
+  }
+  cap = n;
+  g->device_bytes += n * sizeof(T);
+  return BF_OK;
+}
+
+// Build (or reuse) the schedule for a target set given as ranks on the host.
+bf_status build_schedule(Graph* g, const uint32_t* h_tgt, uint64_t T, cudaStream_t st) {
+  Graph::Sched& sc = g->sc;
+  const uint64_t key = hash_targets(h_tgt, T);
+  if (sc.valid && sc.key == key && sc.T == T) return BF_OK;
+  sc.valid = false;
+  const uint32_t n = g->n;
+  std::vector<uint8_t> mark(n, 0);
+  for (uint64_t i = 0; i < T; ++i) mark[g->pos_of[h_tgt[i]]] = 1;
+  uint64_t m_r = 0;
+  for (uint32_t p = n; p-- > 0;) {
+    if (!mark[p]) continue;
+    for (uint64_t k = g->h_in_off[p]; k < g->h_in_off[p + 1]; ++k) mark[g->h_in_rec[k].x] = 1;
+    m_r += g->h_in_off[p + 1] - g->h_in_off[p];
+  }
+  // compact rows in position order (level order is preserved)
+  std::vector<uint32_t> row_of(n, NONE);
+  uint32_t n_r = 0;
+  for (uint32_t p = 0; p < n; ++p)
+    if (mark[p]) row_of[p] = n_r++;
+  std::vector<uint32_t> cidx(n);
+  for (uint32_t r = 0; r < n; ++r) cidx[r] = row_of[g->pos_of[r]];
+  std::vector<uint4> items;
+  std::vector<uint2> erec;
+  erec.reserve(m_r);
+  sc.lvl_item.assign(g->n_levels + 1, 0);
+  for (uint32_t l = 0; l < g->n_levels; ++l) {
+    sc.lvl_item[l] = (uint32_t)items.size();
+    for (uint32_t p = g->lvl_start[l]; p < g->lvl_start[l + 1]; ++p) {
+      if (!mark[p]) continue;
+      uint64_t k0 = g->h_in_off[p], k1 = g->h_in_off[p + 1];
+      if (k0 == k1) continue;  // no in-edges: the row is its seed
+      uint32_t e0 = (uint32_t)erec.size();
+      for (uint64_t k = k0; k < k1; ++k)
+        erec.push_back(make_uint2(row_of[g->h_in_rec[k].x], g->h_in_rec[k].y));
+      uint32_t deg = (uint32_t)(k1 - k0);
+      uint32_t split = deg > SPLIT ? 1u : 0u;
+      for (uint32_t a = 0; a < deg; a += SPLIT)
+        items.push_back(make_uint4(row_of[p], e0 + a, e0 + std::min(deg, a + SPLIT), split));
+    }
+  }
+  sc.lvl_item[g->n_levels] = (uint32_t)items.size();
+  if (erec.size() > 0xFFFFFFFFull) {
+    set_error("restricted edge set exceeds 2^32 edges");
+    return BF_ERR_UNSUPPORTED;
+  }
+  bf_status s;
+  size_t cap_c = sc.d_cidx ? n : 0;
+  if ((s = ensure(&sc.d_cidx, cap_c, n, g))) return s;
+  if ((s = ensure(&sc.d_item, sc.cap_items, items.size(), g))) return s;
+  if ((s = ensure(&sc.d_erec, sc.cap_edges, erec.size(), g))) return s;
+  if ((s = ensure(&sc.d_trow, sc.cap_t, T, g))) return s;
+  std::vector<uint32_t> trow(T);
+  for (uint64_t i = 0; i < T; ++i) trow[i] = row_of[g->pos_of[h_tgt[i]]];
+  BF_CUDA(cudaMemcpyAsync(sc.d_cidx, cidx.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
+  if (!items.empty())
+    BF_CUDA(cudaMemcpyAsync(sc.d_item, items.data(), items.size() * sizeof(uint4),
+                            cudaMemcpyHostToDevice, st));
+  if (!erec.empty())
+    BF_CUDA(cudaMemcpyAsync(sc.d_erec, erec.data(), erec.size() * sizeof(uint2),
+                            cudaMemcpyHostToDevice, st));
+  BF_CUDA(cudaMemcpyAsync(sc.d_trow, trow.data(), T * 4, cudaMemcpyHostToDevice, st));
+  BF_CUDA(cudaStreamSynchronize(st));  // host vectors are freed on return
+  sc.n_r = n_r;
+  sc.n_items = items.size();
+  sc.T = T;
+  sc.key = key;
+  sc.valid = true;
+  return BF_OK;
+}
+
+// One level of the restricted sweep. blockIdx.x = work item, a thread owns
+// 4 consecutive lanes starting at lane; rows are Kp lanes wide (Kp % 4 == 0).
+__global__ void __launch_bounds__(128)
+    k_sweep_items(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
+                  uint32_t* __restrict__ slab, uint32_t Kp) {
+  const uint4 it = item[i0 + blockIdx.x];
+  const uint32_t lane = (blockIdx.y * blockDim.x + threadIdx.x) * 4;
+  if (lane >= Kp) return;
+  uint4 acc = make_uint4(INF, INF, INF, INF);
+  uint32_t e = it.y;
+  for (; e + 2 <= it.z; e += 2) {
+    const uint2 r0 = erec[e], r1 = erec[e + 1];
+    const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r0.x * Kp + lane);
+    const uint4 b = *reinterpret_cast<const uint4*>(slab + (size_t)r1.x * Kp + lane);
+    acc.x = min(acc.x, min(sat_add(a.x, r0.y), sat_add(b.x, r1.y)));
+    acc.y = min(acc.y, min(sat_add(a.y, r0.y), sat_add(b.y, r1.y)));
+    acc.z = min(acc.z, min(sat_add(a.z, r0.y), sat_add(b.z, r1.y)));
+    acc.w = min(acc.w, min(sat_add(a.w, r0.y), sat_add(b.w, r1.y)));
+  }
+  if (e < it.z) {
+    const uint2 r0 = erec[e];
+    const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r0.x * Kp + lane);
+    acc.x = min(acc.x, sat_add(a.x, r0.y));
+    acc.y = min(acc.y, sat_add(a.y, r0.y));
+    acc.z = min(acc.z, sat_add(a.z, r0.y));
+    acc.w = min(acc.w, sat_add(a.w, r0.y));
+  }
+  uint32_t* dst = slab + (size_t)it.x * Kp + lane;
+  if (it.w) {  // one slice of a high in-degree node: combine atomically
+    if (acc.x != INF) atomicMin(dst + 0, acc.x);
+    if (acc.y != INF) atomicMin(dst + 1, acc.y);
+    if (acc.z != INF) atomicMin(dst + 2, acc.z);
+    if (acc.w != INF) atomicMin(dst + 3, acc.w);
+  } else {
+    uint4 c = *reinterpret_cast<const uint4*>(dst);
+    c.x = min(c.x, acc.x);
+    c.y = min(c.y, acc.y);
+    c.z = min(c.z, acc.z);
+    c.w = min(c.w, acc.w);
+    *reinterpret_cast<uint4*>(dst) = c;
+  }
+}
+
+// out[s * T + t] = slab[trow[t]][s] (INF above the threshold); 32 x 32 tiles.
+__global__ void __launch_bounds__(256)
+    k_extract_lanes(const uint32_t* __restrict__ slab, uint32_t Kp,
+                    const uint32_t* __restrict__ trow, uint64_t T, uint32_t S,
+                    uint32_t threshold, uint32_t* __restrict__ out) {
+  __shared__ uint32_t tile[32][33];
+  const uint64_t t0 = (uint64_t)blockIdx.x * 32;
+  const uint32_t l0 = blockIdx.y * 32;
+  for (uint32_t r = threadIdx.y; r < 32; r += 8) {
+    const uint64_t t = t0 + r;
+    const uint32_t l = l0 + threadIdx.x;
+    tile[r][threadIdx.x] = (t < T && l < S) ? slab[(size_t)trow[t] * Kp + l] : INF;
+  }
+  __syncthreads();
+  for (uint32_t r = threadIdx.y; r < 32; r += 8) {
+    const uint32_t l = l0 + r;
+    const uint64_t t = t0 + threadIdx.x;
+    if (l < S && t < T) {
+      const uint32_t v = tile[threadIdx.x][r];
+      out[(uint64_t)l * T + t] = v > threshold ? INF : v;
+    }
+  }
+}
+
+}  // namespace
+
+}  // namespace bf
+
+namespace bf {
+
+bf_status batched_prepare(Graph* g, uint32_t) {
+  g->sc = Graph::Sched();
   return BF_OK;
 }
 
 bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
                          uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                          bf_stats* stats) {
-  (void)g; (void)d_src; (void)S; (void)d_tgt; (void)T; (void)threshold; (void)d_out; (void)st;
-  (void)stats;
-  set_error("batched engine not ready");
-  return BF_ERR_UNSUPPORTED;
+  bf_status s;
+  std::vector<uint32_t> h_tgt(T);
+  BF_CUDA(cudaMemcpyAsync(h_tgt.data(), d_tgt, T * 4, cudaMemcpyDeviceToHost, st));
+  BF_CUDA(cudaStreamSynchronize(st));
+  for (uint64_t i = 0; i < T; ++i)
+    if (h_tgt[i] >= g->n) {
+      set_error("targets[" + std::to_string(i) + "] is not a node of the graph");
+      return BF_ERR_INVALID;
+    }
+  if ((s = build_schedule(g, h_tgt.data(), T, st))) return s;
+  const Graph::Sched& sc = g->sc;
+  const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
+  // lanes per wave: all sources if the slab fits the budget, else waves
+  uint64_t budget = g->hbm_budget > g->device_bytes ? g->hbm_budget - g->device_bytes : 0;
+  budget += g->slab_bytes;  // the current slab is reusable
+  uint64_t max_lanes = budget / (rows * 4);
+  max_lanes = max_lanes >= 32 ? max_lanes & ~31ull : 0;
+  if (max_lanes == 0) {
+    set_error("HBM budget too small for one 32-lane wave of the restricted slab");
+    return BF_ERR_OOM;
+  }
+  const uint64_t wave = std::min<uint64_t>(max_lanes, (S + 3) & ~3ull);
+  const uint32_t Kp = (uint32_t)((wave + 3) & ~3ull);
+  const size_t need = (size_t)rows * Kp * 4;
+  if (need > g->slab_bytes) {
+    if (g->d_slab) {
+      cudaFree(g->d_slab);
+      g->device_bytes -= g->slab_bytes;
+      g->d_slab = nullptr;
+      g->slab_bytes = 0;
+    }
+    if (cudaMalloc(&g->d_slab, need) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cannot allocate the batched distance slab (" + std::to_string(need) + " bytes)");
+      return BF_ERR_OOM;
+    }
+    g->slab_bytes = need;
+    g->device_bytes += need;
+  }
+  uint64_t launches = 0;
+  float t_up = 0, t_dn = 0, t_ex = 0;
+  const unsigned thr_per_blk = std::min<uint32_t>(128, ((Kp / 4 + 31) / 32) * 32);
+  const unsigned lane_blocks = (Kp / 4 + thr_per_blk - 1) / thr_per_blk;
+  for (uint64_t s0 = 0; s0 < S; s0 += wave) {
+    const uint64_t kw = std::min<uint64_t>(wave, S - s0);
+    if (stats) BF_CUDA(cudaEventRecord(g->ev[0], st));
+    BF_CUDA(cudaMemsetAsync(g->d_slab, 0xFF, (size_t)rows * Kp * 4, st));
+    if ((s = launch_upward(g, d_src + s0, kw, INF, sc.d_cidx, g->d_slab, Kp, nullptr, st)))
+      return s;
+    launches += 1;
+    if (stats) BF_CUDA(cudaEventRecord(g->ev[1], st));
+    for (uint32_t l = 0; l < g->n_levels; ++l) {
+      const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
+      if (i1 == i0) continue;
+      dim3 grid(i1 - i0, lane_blocks);
+      k_sweep_items<<<grid, thr_per_blk, 0, st>>>(sc.d_item, i0, sc.d_erec, g->d_slab, Kp);
+      ++launches;
+    }
+    BF_CUDA(cudaGetLastError());
+    if (stats) BF_CUDA(cudaEventRecord(g->ev[2], st));
+    dim3 eg((unsigned)((T + 31) / 32), (unsigned)((kw + 31) / 32)), eb(32, 8);
+    k_extract_lanes<<<eg, eb, 0, st>>>(g->d_slab, Kp, sc.d_trow, T, (uint32_t)kw, threshold,
+                                       d_out + s0 * T);
+    BF_CUDA(cudaGetLastError());
+    ++launches;
+    if (stats) {
+      BF_CUDA(cudaEventRecord(g->ev[3], st));
+      BF_CUDA(cudaEventSynchronize(g->ev[3]));
+      float a, b, c;
+      BF_CUDA(cudaEventElapsedTime(&a, g->ev[0], g->ev[1]));
+      BF_CUDA(cudaEventElapsedTime(&b, g->ev[1], g->ev[2]));
+      BF_CUDA(cudaEventElapsedTime(&c, g->ev[2], g->ev[3]));
+      t_up += a;
+      t_dn += b;
+      t_ex += c;
+    }
+  }
+  if (stats) {
+    stats->n_batches += (S + wave - 1) / wave;
+    stats->kernel_launches += launches;
+    stats->upward_ms += t_up;
+    stats->downward_ms += t_dn;
+    stats->extract_ms += t_ex;
+  }
+  return BF_OK;
 }
 
 }  // namespace bf

@@ -103,8 +103,9 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32)
     if (d == INF || d > threshold) continue;
     uint32_t x = GLOBAL_PATH ? __ldcg(&pn[l]) : pn[l];
     uint32_t p = pos_of[x];
+    if (p == NONE) continue;  // outside the target-restricted rows
     seed[(size_t)p * seed_stride + w] = d;
-    atomicOr(&flag[p >> 5], 1u << (p & 31));
+    if (flag) atomicOr(&flag[p >> 5], 1u << (p & 31));
   }
 }
 
@@ -210,40 +211,53 @@ static bf_status plain_buffers(Graph* g) {
   g->device_bytes += 2 * slab + ((g->n + 31) / 32) * 4;
   BF_CUDA(cudaMemset(g->d_seed, 0xFF, slab));
   BF_CUDA(cudaMemset(g->d_flag, 0, ((g->n + 31) / 32) * 4));
-  if (g->max_depth + 1 > UPWARD_SMEM_PATH) {
-    g->gpath_stride = 2 * (g->max_depth + 1);
-    size_t bytes = (size_t)PLAIN_K * g->gpath_stride * 4;
-    if (cudaMalloc(&g->d_gpath, bytes) != cudaSuccess) {
-      cudaGetLastError();
-      set_error("cannot allocate the ancestor-path scratch");
-      return BF_ERR_OOM;
-    }
-    g->device_bytes += bytes;
-  }
+  return BF_OK;
+}
+
+// Upward pass for k sources: source i writes lane i of row pos_map[x] of
+// `seed` (stride lanes per row) for every settled ancestor x; rows mapped to
+// NONE are skipped. `flag` (optional) receives the seeded-row bits.
+bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t threshold,
+                        const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
+                        cudaStream_t st) {
   static bool attr_set = false;
   if (!attr_set) {
     BF_CUDA(cudaFuncSetAttribute(k_upward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  UPWARD_WARPS * 2 * UPWARD_SMEM_PATH * 4));
     attr_set = true;
   }
-  return BF_OK;
-}
-
-// Launch one upward pass for k <= 32 sources writing into the plain slabs.
-static bf_status plain_upward(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,
-                              cudaStream_t st) {
-  const unsigned blocks = (k + UPWARD_WARPS - 1) / UPWARD_WARPS;
-  if (g->d_gpath) {
-    k_upward<true><<<blocks, UPWARD_WARPS * 32, 0, st>>>(
-        d_src, k, threshold, g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec,
-        g->d_pos_of, g->n, g->d_seed, PLAIN_K, g->d_flag, g->d_gpath, g->gpath_stride, g->d_err);
+  if (g->max_depth + 1 > UPWARD_SMEM_PATH) {
+    // deep trees: ancestor paths live in global scratch, PLAIN_K warps per launch
+    if (!g->d_gpath) {
+      g->gpath_stride = 2 * (g->max_depth + 1);
+      size_t bytes = (size_t)PLAIN_K * g->gpath_stride * 4;
+      if (cudaMalloc(&g->d_gpath, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cannot allocate the ancestor-path scratch");
+        return BF_ERR_OOM;
+      }
+      g->device_bytes += bytes;
+    }
+    for (uint64_t s0 = 0; s0 < k; s0 += PLAIN_K) {
+      uint32_t kk = (uint32_t)std::min<uint64_t>(PLAIN_K, k - s0);
+      k_upward<true><<<(kk + UPWARD_WARPS - 1) / UPWARD_WARPS, UPWARD_WARPS * 32, 0, st>>>(
+          d_src + s0, kk, threshold, g->d_parent, g->d_run_end, g->d_depth, g->d_up_off,
+          g->d_up_rec, pos_map, g->n, seed + s0, stride, flag, g->d_gpath, g->gpath_stride,
+          g->d_err);
+    }
   } else {
-    k_upward<false><<<blocks, UPWARD_WARPS * 32, UPWARD_WARPS * 2 * UPWARD_SMEM_PATH * 4, st>>>(
-        d_src, k, threshold, g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec,
-        g->d_pos_of, g->n, g->d_seed, PLAIN_K, g->d_flag, nullptr, 0, g->d_err);
+    k_upward<false><<<(unsigned)((k + UPWARD_WARPS - 1) / UPWARD_WARPS), UPWARD_WARPS * 32,
+                       UPWARD_WARPS * 2 * UPWARD_SMEM_PATH * 4, st>>>(
+        d_src, (uint32_t)k, threshold, g->d_parent, g->d_run_end, g->d_depth, g->d_up_off,
+        g->d_up_rec, pos_map, g->n, seed, stride, flag, nullptr, 0, g->d_err);
   }
   BF_CUDA(cudaGetLastError());
   return BF_OK;
+}
+
+static bf_status plain_upward(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,
+                              cudaStream_t st) {
+  return launch_upward(g, d_src, k, threshold, g->d_pos_of, g->d_seed, PLAIN_K, g->d_flag, st);
 }
 
 static bf_status plain_sweep(Graph* g, uint32_t threshold, cudaStream_t st, uint64_t* launches) {

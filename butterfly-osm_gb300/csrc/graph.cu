@@ -209,6 +209,8 @@ bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
   if ((s = dev_upload(&g->d_in_rec, in_rec.data(), in_rec.size(), g))) return s;
   uint32_t zero = 0;
   if ((s = dev_upload(&g->d_err, &zero, 1, g))) return s;
+  g->h_in_off = std::move(in_off);
+  g->h_in_rec = std::move(in_rec);
   (void)cfg;
   return BF_OK;
 }
@@ -216,12 +218,10 @@ bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
 void free_graph(Graph* g) {
   if (!g) return;
   cudaSetDevice(g->device);
-  void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec,
-                  g->d_pos_of, g->d_rank_at, g->d_in_off, g->d_in_rec, g->d_dist,
-                  g->d_seed, g->d_flag, g->d_err, g->d_gpath, g->bt.d_tchunk,
-                  g->bt.d_tchunk_e, g->bt.d_tchunk_sync, g->bt.d_top_rec, g->bt.d_top_of,
-                  g->bt.d_sub_of, g->bt.d_loc_of, g->bt.d_top_rank, g->bt.d_sub, g->bt.d_slvl,
-                  g->bt.d_sub_rec, g->bt.d_sub_rank};
+  void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth,  g->d_up_off,    g->d_up_rec,
+                  g->d_pos_of,  g->d_rank_at, g->d_in_off, g->d_in_rec,    g->d_dist,
+                  g->d_seed,    g->d_flag,    g->d_err,    g->d_gpath,     g->sc.d_cidx,
+                  g->sc.d_item, g->sc.d_erec, g->sc.d_trow, g->d_slab};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& e : g->ev)
