@@ -1,0 +1,319 @@
+"""Benchmark: 10k x 10k duration matrix on the country-scale synthetic CCH.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one step): the 10 000 x 10 000 u32 duration matrix, sources and
+targets uniform over the ranks of the 2000 x 2500 lattice road graph with a
+3-level hierarchy (11.94 M edge states after edge-based expansion), contracted
+by the host CCH pipeline. The batched GPU engine computes it; the plain GPU
+sweep (one K = 32 batch per launch sequence) is timed on a slice of the same
+workload for the speed-up, and the CPU restatement of the reference's K = 8
+SoA batched PHAST (compute_matrix_flat_soa) is timed on a bounded sample.
+
+value   cells/s with sources, targets and the output resident in HBM
+        (bf_matrix_device, CUDA events on the launching stream)
+e2e     cells/s through bf_matrix with pinned host buffers: the H2D copy of
+        sources/targets and the D2H copy of the whole matrix are inside the
+        timed region
+Every step overwrites an 11 GB distance slab, far larger than L2 (126 MB).
+
+N > 1 (torchrun): every rank runs the same workload on its own GPU with its own
+seed (weak scaling, no collective on the data path); value = all ranks'
+cells / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "butterfly-osm_gb300"))
+sys.path.insert(0, str(ROOT))
+
+S_CELLS = 10000
+T_CELLS = 10000
+METRIC = "10k x 10k matrix cells/s (bit-exact vs CPU PHAST)"
+UNIT = "cells/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sources", type=int, default=S_CELLS)
+    ap.add_argument("--targets", type=int, default=T_CELLS)
+    ap.add_argument("--rows", type=int, default=2000)
+    ap.add_argument("--cols", type=int, default=2500)
+    ap.add_argument("--cpu-sample-s", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 6:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[2 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def build_workload(args, seed):
+    import cchbuild
+    import workload
+    _, cch = cchbuild.build_synthetic(cchbuild.KIND_COUNTRY, args.rows, args.cols, seed=42)
+    n = cch["n"]
+    src, tgt = workload.sources_targets(n, args.sources, args.targets, seed=seed)
+    return cch, src, tgt
+
+
+def cpu_sample(cch, src, tgt, budget_s, rows=None):
+    """Time the CPU restatement of compute_matrix_flat_soa (K = 8) on a row
+    sample on all host threads. Returns (dict, sample_rows, sample_matrix)."""
+    import numpy as np
+    from oracle import oracle as orc
+    c = orc.Cch.from_dict(cch)
+    threads = os.cpu_count() or 1
+    if rows is None:
+        rows = max(8, min(len(src), (len(src) // 100) or 8))  # a 1% row sample
+    pick = np.linspace(0, len(src) - 1, rows).astype(np.int64)
+    t0 = time.perf_counter()
+    m, used = c.matrix(src[pick], tgt, threads=threads)
+    dt = time.perf_counter() - t0
+    cells = rows * len(tgt)
+    return ({"value": cells / dt, "unit": UNIT, "cores": int(used), "kind": "port",
+             "sample": "%d of %d rows (seeded even spacing) x %d targets, %.1f s"
+                       % (rows, len(src), len(tgt), dt)}, pick, m)
+
+
+def run_ours(args, rank, world, dist):
+    import numpy as np
+    import torch
+    import bfphast
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    cch, src, tgt = build_workload(args, seed=42 + rank)
+    S, T = len(src), len(tgt)
+    g = bfphast.Graph.from_cch(cch, device=dev)
+    stream = torch.cuda.current_stream()
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_tgt = torch.from_numpy(tgt.view(np.int32)).cuda()
+    d_out = torch.empty(S * T, dtype=torch.int32, device="cuda")
+
+    def step():
+        return g.matrix_device(d_src.data_ptr(), S, d_tgt.data_ptr(), T, d_out.data_ptr(),
+                               stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    sync = (lambda: dist.barrier()) if dist else (lambda: None)
+    sync()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            stats.append(step())
+        e1.record(stream)
+        torch.cuda.synchronize()
+    sync()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms_all = ms
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_all = float(t.item())
+    value = world * S * T / (ms_all / 1e3)
+    out_dev = d_out.view(S, T).cpu().numpy().view(np.uint32)
+
+    # e2e: host (pinned) buffers through bf_matrix, copies inside the region
+    h_src = torch.from_numpy(src.view(np.int32)).pin_memory().numpy().view(np.uint32)
+    h_tgt = torch.from_numpy(tgt.view(np.int32)).pin_memory().numpy().view(np.uint32)
+    h_out = torch.empty(S * T, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    h_out = h_out.reshape(S, T)
+    for _ in range(max(1, args.warmup)):
+        g.matrix(h_src, h_tgt, out=h_out)
+    sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        g.matrix(h_src, h_tgt, out=h_out)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_ok = bool(np.array_equal(h_out, out_dev))
+
+    # roofline of the dominant kernel (the restricted downward sweep)
+    st = stats[-1]
+    K, M, N = st["lanes"], st["swept_edges"], st["swept_nodes"]
+    alg_bytes = 8 * M + 4 * (N + 1) + 4 * K * M + 4 * K * N
+    sweep_s = st["downward_ms"] / 1e3
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / sweep_s / 1e9
+    traffic = None
+    prof = ROOT / "profiles" / "sweep_items_country10k.json"
+    if prof.exists():
+        traffic = json.loads(prof.read_text()).get("dram_bytes_per_sweep")
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "peak_kind": peak_kind, "kernel": "k_sweep_items",
+            "alg_bytes_per_sweep": alg_bytes, "sweep_ms": round(st["downward_ms"], 3),
+            "swept_nodes": N, "swept_edges": M, "lanes": K}
+
+    # plain GPU sweep on a slice of the same workload (the >= 10x denominator)
+    g.set_engine(bfphast.ENGINE_PLAIN)
+    ps = 64
+    g.matrix(src[:32], tgt)
+    t0 = time.perf_counter()
+    pm = g.matrix(src[:ps], tgt)
+    plain_s = time.perf_counter() - t0
+    g.set_engine(bfphast.ENGINE_BATCHED)
+    plain_ok = bool(np.array_equal(pm, out_dev[:ps]))
+    plain_cps = ps * T / plain_s
+
+    res = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_all, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+           "data": "synthetic (seeded country-scale lattice road graph, CCH built in-run)",
+           "config": {"workload": "country 2000x2500 lattice, 10k x 10k matrix, batched engine",
+                      "n_nodes": cch["n"], "m_down": int(len(cch["down_tgt"])),
+                      "m_up": int(len(cch["up_tgt"])), "sources": S, "targets": T,
+                      "parallelism": "dp%d" % world if world > 1 else "single",
+                      "l2": "slab of %.1f GB rewritten every step (> L2)"
+                            % (st["lanes"] * max(N, 1) * 4 / 1e9)},
+           "e2e": {"value": round(world * S * T / e2e_s, 1), "unit": UNIT,
+                   "h2d_bytes_per_step": (S + T) * 4, "d2h_bytes_per_step": S * T * 4,
+                   "ms_per_step": round(e2e_s * 1e3, 3), "matches_device_run": e2e_ok},
+           "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+           "roofline": roof,
+           "plain_gpu": {"value": round(plain_cps, 1), "unit": UNIT,
+                         "sample": "%d x %d rows, K=32 per launch sequence" % (ps, T),
+                         "bit_exact_vs_batched": plain_ok,
+                         "speedup_batched_over_plain": round(value / world / plain_cps, 2)},
+           "phases_ms": {"upward": round(st["upward_ms"], 3),
+                         "downward": round(st["downward_ms"], 3),
+                         "extract": round(st["extract_ms"], 3)},
+           "clocks": clk.summary()}
+    return res, cch, src, tgt, out_dev
+
+
+def run_reference(args):
+    """The reference path on the host cores: the CPU restatement of
+    BatchedPhastEngine::compute_matrix_flat_soa (K = 8, rayon-shaped threads),
+    each step a bounded row sample of the same 10k x 10k workload (the Rust
+    reference cannot be compiled here)."""
+    cch, src, tgt = build_workload(args, seed=42)
+    threads = os.cpu_count() or 1
+    rows = 8 * threads  # one K = 8 batch per thread per step
+    for _ in range(args.warmup):
+        cpu_sample(cch, src, tgt, 0, rows=8)
+    vals = []
+    for _ in range(args.steps):
+        d, _, _ = cpu_sample(cch, src, tgt, 0, rows=rows)
+        vals.append(d["value"])
+    value = statistics.median(vals)
+    cb = dict(d)
+    cb["value"] = value
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(rows * len(tgt) / value * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded country-scale lattice road graph, CCH built in-run)",
+            "config": {"workload": "country 2000x2500 lattice, 10k x 10k matrix, row sample",
+                       "n_nodes": cch["n"], "sources": len(src), "targets": len(tgt)},
+            "cpu_baseline": cb,
+            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        tdist.init_process_group("nccl")
+        dist = tdist
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
+    import numpy as np
+    res, cch, src, tgt, out = run_ours(args, rank, world, dist)
+    if rank == 0:
+        if not args.no_cpu:
+            cb, pick, m = cpu_sample(cch, src, tgt, args.cpu_sample_s)
+            res["cpu_baseline"] = cb
+            res["bit_exact_sample"] = {"rows": len(pick), "targets": len(tgt),
+                                       "equal": bool(np.array_equal(out[pick], m))}
+        print(json.dumps(res), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -54,7 +54,9 @@ class Stats(ctypes.Structure):
                 ("n_batches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
                 ("upward_ms", ctypes.c_double), ("downward_ms", ctypes.c_double),
                 ("extract_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
-                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("swept_nodes", ctypes.c_uint64), ("swept_edges", ctypes.c_uint64),
+                ("lanes", ctypes.c_uint64), ("waves", ctypes.c_uint64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -240,14 +240,30 @@ bf_status bf_matrix(bf_graph* h, const uint32_t* src, uint64_t S, const uint32_t
   if (!S || !T) return BF_OK;
   if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
   cudaStream_t s = g->stream;
-  DevBuf ds, dt, dout;
-  if ((rc = ds.alloc(S * 4)) || (rc = dt.alloc(T * 4)) || (rc = dout.alloc(S * T * 4))) return rc;
-  BF_CUDA(cudaMemcpyAsync(ds.p, src, S * 4, cudaMemcpyHostToDevice, s));
-  BF_CUDA(cudaMemcpyAsync(dt.p, tgt, T * 4, cudaMemcpyHostToDevice, s));
-  if ((rc = run_matrix(g, ds.as<uint32_t>(), S, dt.as<uint32_t>(), T, threshold,
-                       dout.as<uint32_t>(), s, st)))
-    return rc;
-  BF_CUDA(cudaMemcpyAsync(out, dout.p, S * T * 4, cudaMemcpyDeviceToHost, s));
+  // graph-owned I/O buffer: [sources | targets | matrix], grown on demand
+  const size_t need = (S + T + S * T) * 4;
+  if (need > g->io_bytes) {
+    if (g->d_io) {
+      cudaFree(g->d_io);
+      g->device_bytes -= g->io_bytes;
+      g->d_io = nullptr;
+      g->io_bytes = 0;
+    }
+    if (cudaMalloc(&g->d_io, need) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc of " + std::to_string(need) + " bytes for matrix I/O failed");
+      return BF_ERR_OOM;
+    }
+    g->io_bytes = need;
+    g->device_bytes += need;
+  }
+  uint32_t* d_src = g->d_io;
+  uint32_t* d_tgt = d_src + S;
+  uint32_t* d_out = d_tgt + T;
+  BF_CUDA(cudaMemcpyAsync(d_src, src, S * 4, cudaMemcpyHostToDevice, s));
+  BF_CUDA(cudaMemcpyAsync(d_tgt, tgt, T * 4, cudaMemcpyHostToDevice, s));
+  if ((rc = run_matrix(g, d_src, S, d_tgt, T, threshold, d_out, s, st))) return rc;
+  BF_CUDA(cudaMemcpyAsync(out, d_out, S * T * 4, cudaMemcpyDeviceToHost, s));
   BF_CUDA(cudaStreamSynchronize(s));
   if (st) {
     st->n_sources = S;

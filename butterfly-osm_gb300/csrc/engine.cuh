@@ -81,6 +81,7 @@ struct Graph {
     uint64_t key = 0;              // hash of the target positions
     uint32_t n_r = 0;              // restricted nodes
     uint64_t n_items = 0;
+    uint64_t n_edges = 0;
     std::vector<uint32_t> lvl_item;  // level -> first work item, n_levels + 1
     uint32_t* d_cidx = nullptr;    // [n] rank -> compact row or NONE
     uint4* d_item = nullptr;       // {row, edge0, edge1, split flag}
@@ -91,6 +92,8 @@ struct Graph {
   } sc;
   uint32_t* d_slab = nullptr;      // batched distance slab [rows][Kp]
   size_t slab_bytes = 0;
+  uint32_t* d_io = nullptr;        // bf_matrix host-call I/O buffer
+  size_t io_bytes = 0;
 };
 
 // graph.cu

@@ -124,6 +124,7 @@ bf_status build_schedule(Graph* g, const uint32_t* h_tgt, uint64_t T, cudaStream
   BF_CUDA(cudaStreamSynchronize(st));  // host vectors are freed on return
   sc.n_r = n_r;
   sc.n_items = items.size();
+  sc.n_edges = erec.size();
   sc.T = T;
   sc.key = key;
   sc.valid = true;
@@ -290,6 +291,10 @@ bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint
   }
   if (stats) {
     stats->n_batches += (S + wave - 1) / wave;
+    stats->waves += (S + wave - 1) / wave;
+    stats->swept_nodes = sc.n_r;
+    stats->swept_edges = sc.n_edges;
+    stats->lanes = Kp;
     stats->kernel_launches += launches;
     stats->upward_ms += t_up;
     stats->downward_ms += t_dn;

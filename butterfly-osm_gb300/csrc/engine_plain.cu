@@ -311,6 +311,10 @@ bf_status plain_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32
   }
   if (stats) {
     stats->n_batches += nb;
+    stats->waves += nb;
+    stats->swept_nodes = g->n;
+    stats->swept_edges = g->n_down;
+    stats->lanes = PLAIN_K;
     stats->kernel_launches += launches;
     stats->upward_ms += t_up;
     stats->downward_ms += t_dn;

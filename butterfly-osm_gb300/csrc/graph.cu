@@ -221,7 +221,7 @@ void free_graph(Graph* g) {
   void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth,  g->d_up_off,    g->d_up_rec,
                   g->d_pos_of,  g->d_rank_at, g->d_in_off, g->d_in_rec,    g->d_dist,
                   g->d_seed,    g->d_flag,    g->d_err,    g->d_gpath,     g->sc.d_cidx,
-                  g->sc.d_item, g->sc.d_erec, g->sc.d_trow, g->d_slab};
+                  g->sc.d_item, g->sc.d_erec, g->sc.d_trow, g->d_slab,  g->d_io};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& e : g->ev)

@@ -126,6 +126,10 @@ typedef struct bf_stats {
   double total_ms;            /* whole call, host clock                            */
   uint64_t h2d_bytes;
   uint64_t d2h_bytes;
+  uint64_t swept_nodes;       /* rows processed by the downward sweep (per wave)  */
+  uint64_t swept_edges;       /* DOWN edges relaxed per lane (per wave)           */
+  uint64_t lanes;             /* lanes (sources) per wave, padded to 4            */
+  uint64_t waves;             /* sweeps run                                       */
 } bf_stats;
 
 bf_status bf_graph_create(const bf_cch_csr* csr, const bf_config* cfg, bf_graph** out);
