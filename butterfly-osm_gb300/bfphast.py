@@ -96,6 +96,8 @@ _SIGNATURES = {
     "bf_query_batch": (ctypes.c_int, [ctypes.c_void_p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
                                       _u32p]),
     "bf_phast_query": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _u32p]),
+    "bf_query_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                              ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p]),
     "bf_matrix": (ctypes.c_int, [ctypes.c_void_p, _u32p, ctypes.c_uint64, _u32p, ctypes.c_uint64,
                                  ctypes.c_uint32, _u32p, ctypes.POINTER(Stats)]),
     "bf_matrix_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,

@@ -301,6 +301,21 @@ bf_status bf_query_batch(bf_graph* h, const uint32_t* src, uint32_t k, uint32_t 
   return BF_OK;
 }
 
+bf_status bf_query_batch_noalloc(bf_graph* h, const uint32_t* d_src, uint32_t k,
+                                 uint32_t threshold, uint32_t* d_out, void* stream) {
+  if (!h || (k && (!d_src || !d_out))) {
+    set_error("bf_query_batch_noalloc: null argument");
+    return BF_ERR_INVALID;
+  }
+  Graph* g = &h->g;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+  bf_status rc = query_batch_noalloc(g, d_src, k, threshold, d_out, s);
+  if (rc != BF_OK) return rc;
+  return check_device_error(g, s);
+}
+
 bf_status bf_phast_query(bf_graph* h, uint32_t origin, uint32_t* dist_out) {
   return bf_query_batch(h, &origin, 1, BF_INF, dist_out);
 }

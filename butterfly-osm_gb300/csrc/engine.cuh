@@ -122,6 +122,10 @@ bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint
                          uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                          bf_stats* stats);
 
+// noalloc.cu
+bf_status query_batch_noalloc(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,
+                              uint32_t* d_out, cudaStream_t st);
+
 // api.cu
 void set_error(const std::string& msg);
 bf_status cuda_status(cudaError_t e, const char* what);

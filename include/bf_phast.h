@@ -144,6 +144,26 @@ bf_status bf_graph_set_engine(bf_graph* g, uint32_t engine, uint32_t k_lanes);
 bf_status bf_query_batch(bf_graph* g, const uint32_t* sources, uint32_t k, uint32_t threshold,
                          uint32_t* dist_out);
 
+/* Fixed size of the device scratch array behind bf_query_batch_noalloc. */
+#define BF_NOALLOC_SCRATCH_BYTES (4u << 20)
+
+/* bf_query_batch for callers that cannot allocate memory. It has no
+ * counterpart in the reference. Callers whose device memory is all reserved
+ * up front by their own pool allocator, or who cannot afford cudaMalloc's
+ * implicit device synchronisation on their hot path, pass device buffers:
+ * d_sources (k ranks) and d_dist_out (k * n_nodes u32, laid out as
+ * bf_query_batch's dist_out). The call allocates nothing: its only scratch
+ * (the upward pass's ancestor paths, 8 * (max_depth + 1) bytes per source) is
+ * a static device array of BF_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library holds until exit. Limits: k <= 32 and k * 8 * (max_depth + 1) <=
+ * BF_NOALLOC_SCRATCH_BYTES, else BF_ERR_INVALID. The first call on a device
+ * resolves the array's device address; make it before any stream capture.
+ * All calls share the array: calls whose work overlaps on the GPU race and
+ * must be serialised by the caller. stream is a cudaStream_t or NULL for the
+ * graph's stream; the call returns after the work completed. */
+bf_status bf_query_batch_noalloc(bf_graph* g, const uint32_t* d_sources, uint32_t k,
+                                 uint32_t threshold, uint32_t* d_dist_out, void* stream);
+
 /* Single-source unbounded PHAST (PhastEngine::query). */
 bf_status bf_phast_query(bf_graph* g, uint32_t origin, uint32_t* dist_out);
 
