@@ -89,6 +89,11 @@ struct Graph {
     uint32_t* d_trow = nullptr;    // [T] target rows
     uint64_t T = 0;
     size_t cap_items = 0, cap_edges = 0, cap_t = 0;
+    uint32_t uses = 0;             // calls that reused this schedule
+    cudaGraphExec_t gexec = nullptr;  // captured level launches
+    uint32_t g_kp = 0, g_lb = 0, g_tpb = 0;
+    uint32_t* g_slab = nullptr;
+    cudaStream_t g_stream = nullptr;
   } sc;
   uint32_t* d_slab = nullptr;      // batched distance slab [rows][Kp]
   size_t slab_bytes = 0;

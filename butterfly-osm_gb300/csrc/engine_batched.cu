@@ -63,8 +63,16 @@ bf_status ensure(T** p, size_t& cap, size_t need, Graph* g) {
 bf_status build_schedule(Graph* g, const uint32_t* h_tgt, uint64_t T, cudaStream_t st) {
   Graph::Sched& sc = g->sc;
   const uint64_t key = hash_targets(h_tgt, T);
-  if (sc.valid && sc.key == key && sc.T == T) return BF_OK;
+  if (sc.valid && sc.key == key && sc.T == T) {
+    ++sc.uses;
+    return BF_OK;
+  }
   sc.valid = false;
+  sc.uses = 0;
+  if (sc.gexec) {
+    cudaGraphExecDestroy(sc.gexec);
+    sc.gexec = nullptr;
+  }
   const uint32_t n = g->n;
   std::vector<uint8_t> mark(n, 0);
   for (uint64_t i = 0; i < T; ++i) mark[g->pos_of[h_tgt[i]]] = 1;
@@ -209,6 +217,63 @@ bf_status batched_prepare(Graph* g, uint32_t) {
   return BF_OK;
 }
 
+// Launch the restricted sweep's level schedule. From the second call on the
+// same schedule and slab geometry the launches are replayed from a captured
+// CUDA graph instead of being issued one by one.
+static bf_status sweep_levels(Graph* g, uint32_t Kp, unsigned lane_blocks, unsigned tpb,
+                              cudaStream_t st, uint64_t* launches) {
+  Graph::Sched& sc = g->sc;
+  auto issue = [&](cudaStream_t s) {
+    for (uint32_t l = 0; l < g->n_levels; ++l) {
+      const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
+      if (i1 == i0) continue;
+      dim3 grid(i1 - i0, lane_blocks);
+      k_sweep_items<<<grid, tpb, 0, s>>>(sc.d_item, i0, sc.d_erec, g->d_slab, Kp);
+      ++*launches;
+    }
+  };
+  const bool geom = sc.g_kp == Kp && sc.g_lb == lane_blocks && sc.g_tpb == tpb &&
+                    sc.g_slab == g->d_slab && sc.g_stream == st;
+  if (sc.gexec && !geom) {
+    cudaGraphExecDestroy(sc.gexec);
+    sc.gexec = nullptr;
+  }
+  if (!sc.gexec && sc.uses >= 1) {
+    cudaStreamCaptureStatus cs;
+    BF_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs == cudaStreamCaptureStatusNone) {
+      uint64_t dummy = 0;
+      cudaGraph_t graph;
+      BF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      for (uint32_t l = 0; l < g->n_levels; ++l) {
+        const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
+        if (i1 == i0) continue;
+        dim3 grid(i1 - i0, lane_blocks);
+        k_sweep_items<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, g->d_slab, Kp);
+        ++dummy;
+      }
+      BF_CUDA(cudaStreamEndCapture(st, &graph));
+      cudaError_t e = cudaGraphInstantiate(&sc.gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate");
+      sc.g_kp = Kp;
+      sc.g_lb = lane_blocks;
+      sc.g_tpb = tpb;
+      sc.g_slab = g->d_slab;
+      sc.g_stream = st;
+    }
+  }
+  if (sc.gexec) {
+    BF_CUDA(cudaGraphLaunch(sc.gexec, st));
+    for (uint32_t l = 0; l < g->n_levels; ++l)
+      if (sc.lvl_item[l + 1] != sc.lvl_item[l]) ++*launches;
+  } else {
+    issue(st);
+  }
+  BF_CUDA(cudaGetLastError());
+  return BF_OK;
+}
+
 bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
                          uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                          bf_stats* stats) {
@@ -263,14 +328,7 @@ bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint
       return s;
     launches += 1;
     if (stats) BF_CUDA(cudaEventRecord(g->ev[1], st));
-    for (uint32_t l = 0; l < g->n_levels; ++l) {
-      const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
-      if (i1 == i0) continue;
-      dim3 grid(i1 - i0, lane_blocks);
-      k_sweep_items<<<grid, thr_per_blk, 0, st>>>(sc.d_item, i0, sc.d_erec, g->d_slab, Kp);
-      ++launches;
-    }
-    BF_CUDA(cudaGetLastError());
+    if ((s = sweep_levels(g, Kp, lane_blocks, thr_per_blk, st, &launches))) return s;
     if (stats) BF_CUDA(cudaEventRecord(g->ev[2], st));
     dim3 eg((unsigned)((T + 31) / 32), (unsigned)((kw + 31) / 32)), eb(32, 8);
     k_extract_lanes<<<eg, eb, 0, st>>>(g->d_slab, Kp, sc.d_trow, T, (uint32_t)kw, threshold,

@@ -109,6 +109,88 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32)
   }
 }
 
+// Upward pass, shared-memory path variant. Each warp keeps its ancestor path
+// (nodes and distances) in dcap-entry shared arrays. The UP-edge ranges of 32
+// path nodes are fetched in one parallel load and broadcast by shuffle, and
+// the first edge record of the next path node is loaded while the current one
+// is relaxed, so a path step costs about one shared-memory round trip instead
+// of two dependent L2 round trips.
+__global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
+    k_upward_fast(const uint32_t* __restrict__ src, uint32_t k, uint32_t threshold,
+                  const uint32_t* __restrict__ parent, const uint32_t* __restrict__ run_end,
+                  const uint32_t* __restrict__ depth, const uint64_t* __restrict__ up_off,
+                  const uint2* __restrict__ up_rec, const uint32_t* __restrict__ pos_of,
+                  uint32_t n, uint32_t* __restrict__ seed, uint32_t seed_stride,
+                  uint32_t* __restrict__ flag, uint32_t dcap, uint32_t* __restrict__ err) {
+  extern __shared__ uint32_t smem[];
+  const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t w = blockIdx.x * UPWARD_WARPS + wib;
+  if (w >= k) return;
+  const uint32_t s = src[w];
+  if (s >= n) {
+    if (lane == 0) atomicOr(err, DEVERR_PATH);
+    return;
+  }
+  const uint32_t D = depth[s] + 1;
+  uint32_t* pd = smem + wib * 2 * dcap;
+  uint32_t* pn = pd + dcap;
+  if (D > dcap || walk_path(s, D, parent, run_end, pn, lane) != D) {
+    if (lane == 0) atomicOr(err, DEVERR_PATH);
+    return;
+  }
+  for (uint32_t l = lane; l < D; l += 32) pd[l] = (l == 0) ? 0u : INF;
+  __syncwarp();
+  const unsigned FULL = 0xFFFFFFFFu;
+  uint64_t cb = 0, ce = 0;  // edge range of path node (chunk base + lane)
+  if (lane < D) {
+    const uint32_t x = pn[lane];
+    cb = up_off[x];
+    ce = up_off[x + 1];
+  }
+  uint64_t b_cur = __shfl_sync(FULL, cb, 0), e_cur = __shfl_sync(FULL, ce, 0);
+  uint2 rec = (b_cur + lane < e_cur) ? up_rec[b_cur + lane] : make_uint2(0, 0);
+  for (uint32_t i = 0; i < D; ++i) {
+    const uint32_t j = i + 1;
+    if ((j & 31) == 0 && j < D) {
+      cb = ce = 0;
+      if (j + lane < D) {
+        const uint32_t x = pn[j + lane];
+        cb = up_off[x];
+        ce = up_off[x + 1];
+      }
+    }
+    const uint64_t b_nx = __shfl_sync(FULL, cb, j & 31), e_nx = __shfl_sync(FULL, ce, j & 31);
+    const uint2 nrec =
+        (j < D && b_nx + lane < e_nx) ? up_rec[b_nx + lane] : make_uint2(0, 0);
+    const uint32_t d = *(const volatile uint32_t*)&pd[i];
+    if (d != INF && d <= threshold) {
+      if (b_cur + lane < e_cur) {
+        const uint32_t t = i + rec.x;
+        if (t < D) atomicMin(&pd[t], sat_add(d, rec.y));
+        else atomicOr(err, DEVERR_EDGE);
+      }
+      for (uint64_t e = b_cur + 32 + lane; e < e_cur; e += 32) {
+        const uint2 r = up_rec[e];
+        const uint32_t t = i + r.x;
+        if (t < D) atomicMin(&pd[t], sat_add(d, r.y));
+        else atomicOr(err, DEVERR_EDGE);
+      }
+    }
+    __syncwarp();
+    rec = nrec;
+    b_cur = b_nx;
+    e_cur = e_nx;
+  }
+  for (uint32_t l = lane; l < D; l += 32) {
+    const uint32_t d = *(const volatile uint32_t*)&pd[l];
+    if (d == INF || d > threshold) continue;
+    const uint32_t p = pos_of[pn[l]];
+    if (p == NONE) continue;
+    seed[(size_t)p * seed_stride + w] = d;
+    if (flag) atomicOr(&flag[p >> 5], 1u << (p & 31));
+  }
+}
+
 // One level of the pull sweep: positions [p0, p1), a warp per node.
 __global__ void __launch_bounds__(256)
     k_sweep_level(uint32_t p0, uint32_t p1, const uint64_t* __restrict__ in_off,
@@ -220,13 +302,20 @@ static bf_status plain_buffers(Graph* g) {
 bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t threshold,
                         const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
                         cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    BF_CUDA(cudaFuncSetAttribute(k_upward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 UPWARD_WARPS * 2 * UPWARD_SMEM_PATH * 4));
-    attr_set = true;
+  const uint32_t dcap = ((g->max_depth + 1) + 31) & ~31u;
+  const size_t fast_smem = (size_t)UPWARD_WARPS * 2 * dcap * 4;
+  const bool fast = fast_smem <= 200 * 1024;
+  if (fast) {
+    BF_CUDA(cudaFuncSetAttribute(k_upward_fast, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fast_smem));
+    k_upward_fast<<<(unsigned)((k + UPWARD_WARPS - 1) / UPWARD_WARPS), UPWARD_WARPS * 32,
+                    fast_smem, st>>>(d_src, (uint32_t)k, threshold, g->d_parent, g->d_run_end,
+                                     g->d_depth, g->d_up_off, g->d_up_rec, pos_map, g->n, seed,
+                                     stride, flag, dcap, g->d_err);
+    BF_CUDA(cudaGetLastError());
+    return BF_OK;
   }
-  if (g->max_depth + 1 > UPWARD_SMEM_PATH) {
+  {
     // deep trees: ancestor paths live in global scratch, PLAIN_K warps per launch
     if (!g->d_gpath) {
       g->gpath_stride = 2 * (g->max_depth + 1);
@@ -245,11 +334,6 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
           g->d_up_rec, pos_map, g->n, seed + s0, stride, flag, g->d_gpath, g->gpath_stride,
           g->d_err);
     }
-  } else {
-    k_upward<false><<<(unsigned)((k + UPWARD_WARPS - 1) / UPWARD_WARPS), UPWARD_WARPS * 32,
-                       UPWARD_WARPS * 2 * UPWARD_SMEM_PATH * 4, st>>>(
-        d_src, (uint32_t)k, threshold, g->d_parent, g->d_run_end, g->d_depth, g->d_up_off,
-        g->d_up_rec, pos_map, g->n, seed, stride, flag, nullptr, 0, g->d_err);
   }
   BF_CUDA(cudaGetLastError());
   return BF_OK;

@@ -226,6 +226,7 @@ void free_graph(Graph* g) {
     if (p) cudaFree(p);
   for (auto& e : g->ev)
     if (e) cudaEventDestroy(e);
+  if (g->sc.gexec) cudaGraphExecDestroy(g->sc.gexec);
   if (g->stream) cudaStreamDestroy(g->stream);
 }
 
