@@ -112,6 +112,10 @@ _SIGNATURES = {
                                                ctypes.c_uint64, _u64p]),
     "bf_isochrone_bitsets": (ctypes.c_int, [ctypes.c_void_p, _u32p, _u32p, ctypes.c_uint64,
                                             _u64p, _u64p, ctypes.POINTER(Stats)]),
+    "bf_isochrone_bitsets_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p,
+                                                   ctypes.c_void_p, ctypes.c_uint64,
+                                                   ctypes.c_void_p, ctypes.c_void_p,
+                                                   ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "bf_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerCfg),
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "bf_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Request), _u64p]),
@@ -273,3 +277,11 @@ class Graph:
         _check(load().bf_isochrone_bitsets(self._h, _ptr(o), _ptr(t), len(o), _ptr(bits, _u64p),
                                            _ptr(counts, _u64p), ctypes.byref(st)))
         return (bits, counts, st.as_dict()) if stats else (bits, counts)
+
+    def isochrone_bitsets_device(self, d_orig, d_thr, n, d_bits, d_counts, stream=None):
+        """Device-pointer variant: d_* are integer device addresses."""
+        st = Stats()
+        _check(load().bf_isochrone_bitsets_device(
+            self._h, ctypes.c_void_p(d_orig), ctypes.c_void_p(d_thr), n, ctypes.c_void_p(d_bits),
+            ctypes.c_void_p(d_counts), ctypes.c_void_p(stream or 0), ctypes.byref(st)))
+        return st.as_dict()

@@ -332,10 +332,89 @@ bf_status bf_phast_bounded_seeded(bf_graph*, const bf_seed*, uint32_t, uint32_t,
   return BF_ERR_UNSUPPORTED;
 }
 
-bf_status bf_isochrone_bitsets(bf_graph*, const uint32_t*, const uint32_t*, uint64_t, uint64_t*,
-                               uint64_t*, bf_stats*) {
-  set_error("bf_isochrone_bitsets: not implemented yet");
-  return BF_ERR_UNSUPPORTED;
+bf_status bf_isochrone_bitsets_device(bf_graph* h, const uint32_t* d_orig, const uint32_t* d_thr,
+                                      uint64_t n, uint64_t* d_bits, uint64_t* d_counts,
+                                      void* stream, bf_stats* st) {
+  if (!h || (n && (!d_orig || !d_thr || !d_bits || !d_counts))) {
+    set_error("bf_isochrone_bitsets_device: null argument");
+    return BF_ERR_INVALID;
+  }
+  double t0 = now_s();
+  Graph* g = &h->g;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
+  if (st) std::memset(st, 0, sizeof(*st));
+  bf_status rc = BF_OK;
+  if (n) rc = isochrone_bitsets(g, d_orig, d_thr, n, d_bits, d_counts, s, st);
+  if (rc == BF_OK) rc = check_device_error(g, s);
+  if (st) {
+    st->n_sources = n;
+    st->n_targets = g->n;
+    st->total_ms = (now_s() - t0) * 1e3;
+  }
+  return rc;
+}
+
+bf_status bf_isochrone_bitsets(bf_graph* h, const uint32_t* orig, const uint32_t* thr, uint64_t n,
+                               uint64_t* bits, uint64_t* counts, bf_stats* st) {
+  if (!h || (n && (!orig || !thr || !bits))) {
+    set_error("bf_isochrone_bitsets: null argument");
+    return BF_ERR_INVALID;
+  }
+  double t0 = now_s();
+  Graph* g = &h->g;
+  bf_status rc;
+  if ((rc = check_ids(orig, n, g->n, "origins"))) return rc;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (!n) return BF_OK;
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t s = g->stream;
+  const uint64_t w64 = (g->n + 63) / 64;
+  // origins per chunk: bitset rows of at most ~8 GB on the device
+  uint64_t chunk = std::max<uint64_t>(32, (8ull << 30) / (w64 * 8));
+  chunk = std::min<uint64_t>(chunk, n);
+  const size_t need = chunk * (4 + 4 + 8) + chunk * w64 * 8;
+  if (need > g->iso_bytes) {
+    if (g->d_iso) {
+      cudaFree(g->d_iso);
+      g->device_bytes -= g->iso_bytes;
+      g->d_iso = nullptr;
+      g->iso_bytes = 0;
+    }
+    if (cudaMalloc(&g->d_iso, need) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc of " + std::to_string(need) + " bytes for isochrone I/O failed");
+      return BF_ERR_OOM;
+    }
+    g->iso_bytes = need;
+    g->device_bytes += need;
+  }
+  uint64_t* d_bits = reinterpret_cast<uint64_t*>(g->d_iso);
+  uint64_t* d_counts = d_bits + chunk * w64;
+  uint32_t* d_orig = reinterpret_cast<uint32_t*>(d_counts + chunk);
+  uint32_t* d_thr = d_orig + chunk;
+  std::vector<uint64_t> tmp_counts;
+  for (uint64_t c0 = 0; c0 < n; c0 += chunk) {
+    const uint64_t m = std::min<uint64_t>(chunk, n - c0);
+    BF_CUDA(cudaMemcpyAsync(d_orig, orig + c0, m * 4, cudaMemcpyHostToDevice, s));
+    BF_CUDA(cudaMemcpyAsync(d_thr, thr + c0, m * 4, cudaMemcpyHostToDevice, s));
+    if ((rc = isochrone_bitsets(g, d_orig, d_thr, m, d_bits, d_counts, s, st))) return rc;
+    BF_CUDA(cudaMemcpyAsync(bits + c0 * w64, d_bits, m * w64 * 8, cudaMemcpyDeviceToHost, s));
+    if (counts)
+      BF_CUDA(cudaMemcpyAsync(counts + c0, d_counts, m * 8, cudaMemcpyDeviceToHost, s));
+    BF_CUDA(cudaStreamSynchronize(s));
+  }
+  if ((rc = check_device_error(g, s))) return rc;
+  if (st) {
+    st->n_sources = n;
+    st->n_targets = g->n;
+    st->h2d_bytes = n * 8;
+    st->d2h_bytes = n * w64 * 8 + (counts ? n * 8 : 0);
+    st->total_ms = (now_s() - t0) * 1e3;
+  }
+  return BF_OK;
 }
 
 bf_status bf_server_create(bf_graph*, const bf_server_cfg*, bf_server** out) {

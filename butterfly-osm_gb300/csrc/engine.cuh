@@ -76,7 +76,7 @@ struct Graph {
   std::vector<uint2> h_in_rec;     // {source position, w}
 
   // ---- batched engine: cached target-restricted schedule ----
-  struct Sched {
+  struct Sched {  // a sweep schedule (target-restricted or full graph)
     bool valid = false;
     uint64_t key = 0;              // hash of the target positions
     uint32_t n_r = 0;              // restricted nodes
@@ -94,11 +94,15 @@ struct Graph {
     uint32_t g_kp = 0, g_lb = 0, g_tpb = 0;
     uint32_t* g_slab = nullptr;
     cudaStream_t g_stream = nullptr;
-  } sc;
+  } sc, full;  // sc: last target-restricted schedule; full: every node
   uint32_t* d_slab = nullptr;      // batched distance slab [rows][Kp]
   size_t slab_bytes = 0;
   uint32_t* d_io = nullptr;        // bf_matrix host-call I/O buffer
   size_t io_bytes = 0;
+  uint8_t* d_iso = nullptr;        // isochrone I/O: origins, thresholds, counts, bits
+  size_t iso_bytes = 0;
+  uint32_t* d_iso_tmp = nullptr;   // isochrone permutation and active-row bitmap
+  size_t iso_tmp_bytes = 0;
 };
 
 // graph.cu
@@ -116,16 +120,29 @@ bf_status to_positions(Graph* g, const uint32_t* d_rank, uint64_t n, uint32_t* d
 bf_status check_device_error(Graph* g, cudaStream_t st);
 bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t threshold,
                         const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
-                        cudaStream_t st);
+                        cudaStream_t st, const uint32_t* lane_thr = nullptr);
 __global__ void k_extract(const uint32_t* __restrict__ slab, uint32_t slab_stride,
                           const uint32_t* __restrict__ tpos, uint64_t T, uint32_t k,
                           uint32_t* __restrict__ out);
 
 // engine_batched.cu
 bf_status batched_prepare(Graph* g, uint32_t split_edges);
+bf_status build_schedule(Graph* g, Graph::Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
+                         cudaStream_t st);
+bf_status sweep_levels(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_blocks,
+                       unsigned tpb, cudaStream_t st, uint64_t* launches);
+bf_status sweep_levels_gated(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_blocks,
+                             unsigned tpb, uint32_t* active, const uint32_t* thr, uint32_t kw,
+                             cudaStream_t st, uint64_t* launches);
+bf_status ensure_slab(Graph* g, size_t bytes);
 bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
                          uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                          bf_stats* stats);
+
+// isochrone.cu
+bf_status isochrone_bitsets(Graph* g, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
+                            uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,
+                            bf_stats* stats);
 
 // noalloc.cu
 bf_status query_batch_noalloc(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,

@@ -59,10 +59,14 @@ bf_status ensure(T** p, size_t& cap, size_t need, Graph* g) {
   return BF_OK;
 }
 
-// Build (or reuse) the schedule for a target set given as ranks on the host.
-bf_status build_schedule(Graph* g, const uint32_t* h_tgt, uint64_t T, cudaStream_t st) {
-  Graph::Sched& sc = g->sc;
-  const uint64_t key = hash_targets(h_tgt, T);
+}  // namespace
+
+// Build (or reuse) a sweep schedule: restricted to the DOWN ancestry of the
+// targets h_tgt[0..T) (ranks, on the host), or over every node when all is
+// set (then h_tgt may be null and T is 0).
+bf_status build_schedule(Graph* g, Graph::Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
+                         cudaStream_t st) {
+  const uint64_t key = all ? 0x9E3779B97F4A7C15ull : hash_targets(h_tgt, T);
   if (sc.valid && sc.key == key && sc.T == T) {
     ++sc.uses;
     return BF_OK;
@@ -74,7 +78,7 @@ bf_status build_schedule(Graph* g, const uint32_t* h_tgt, uint64_t T, cudaStream
     sc.gexec = nullptr;
   }
   const uint32_t n = g->n;
-  std::vector<uint8_t> mark(n, 0);
+  std::vector<uint8_t> mark(n, all ? 1 : 0);
   for (uint64_t i = 0; i < T; ++i) mark[g->pos_of[h_tgt[i]]] = 1;
   uint64_t m_r = 0;
   for (uint32_t p = n; p-- > 0;) {
@@ -128,7 +132,7 @@ bf_status build_schedule(Graph* g, const uint32_t* h_tgt, uint64_t T, cudaStream
   if (!erec.empty())
     BF_CUDA(cudaMemcpyAsync(sc.d_erec, erec.data(), erec.size() * sizeof(uint2),
                             cudaMemcpyHostToDevice, st));
-  BF_CUDA(cudaMemcpyAsync(sc.d_trow, trow.data(), T * 4, cudaMemcpyHostToDevice, st));
+  if (T) BF_CUDA(cudaMemcpyAsync(sc.d_trow, trow.data(), T * 4, cudaMemcpyHostToDevice, st));
   BF_CUDA(cudaStreamSynchronize(st));  // host vectors are freed on return
   sc.n_r = n_r;
   sc.n_items = items.size();
@@ -138,6 +142,8 @@ bf_status build_schedule(Graph* g, const uint32_t* h_tgt, uint64_t T, cudaStream
   sc.valid = true;
   return BF_OK;
 }
+
+namespace {
 
 // One level of the restricted sweep. blockIdx.x = work item, a thread owns
 // 4 consecutive lanes starting at lane; rows are Kp lanes wide (Kp % 4 == 0).
@@ -182,6 +188,60 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// Gated variant for bounded sweeps with a threshold per lane: a row is
+// "active" when some lane holds a value within that lane's threshold (bit in
+// `active`). An item none of whose in-edge sources is active is skipped (its
+// row keeps its seed or INF), and inactive source rows are not gathered: a
+// value above a lane's threshold can only produce values above it, so every
+// distance within the threshold is still exact. This is the GPU form of the
+// reference's block gating (isochrone_handler.rs:419-452, batched_phast.rs:1093-1160).
+__global__ void __launch_bounds__(128)
+    k_sweep_gated(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
+                  uint32_t* __restrict__ slab, uint32_t Kp, uint32_t* __restrict__ active,
+                  const uint32_t* __restrict__ thr, uint32_t kw) {
+  const uint4 it = item[i0 + blockIdx.x];
+  bool any = false;
+  for (uint32_t e = it.y; e < it.z; ++e) {
+    const uint32_t r = erec[e].x;
+    any |= (active[r >> 5] >> (r & 31)) & 1u;
+  }
+  if (!any) return;  // uniform across the block
+  const uint32_t lane = (blockIdx.y * blockDim.x + threadIdx.x) * 4;
+  if (lane >= Kp) return;
+  uint4 acc = make_uint4(INF, INF, INF, INF);
+  for (uint32_t e = it.y; e < it.z; ++e) {
+    const uint2 r = erec[e];
+    if (!((active[r.x >> 5] >> (r.x & 31)) & 1u)) continue;
+    const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r.x * Kp + lane);
+    acc.x = min(acc.x, sat_add(a.x, r.y));
+    acc.y = min(acc.y, sat_add(a.y, r.y));
+    acc.z = min(acc.z, sat_add(a.z, r.y));
+    acc.w = min(acc.w, sat_add(a.w, r.y));
+  }
+  uint32_t* dst = slab + (size_t)it.x * Kp + lane;
+  uint4 v = acc;
+  if (it.w) {
+    if (acc.x != INF) atomicMin(dst + 0, acc.x);
+    if (acc.y != INF) atomicMin(dst + 1, acc.y);
+    if (acc.z != INF) atomicMin(dst + 2, acc.z);
+    if (acc.w != INF) atomicMin(dst + 3, acc.w);
+  } else {
+    v = *reinterpret_cast<const uint4*>(dst);
+    v.x = min(v.x, acc.x);
+    v.y = min(v.y, acc.y);
+    v.z = min(v.z, acc.z);
+    v.w = min(v.w, acc.w);
+    *reinterpret_cast<uint4*>(dst) = v;
+  }
+  const bool act = (lane + 0 < kw && v.x <= thr[lane + 0]) ||
+                   (lane + 1 < kw && v.y <= thr[lane + 1]) ||
+                   (lane + 2 < kw && v.z <= thr[lane + 2]) ||
+                   (lane + 3 < kw && v.w <= thr[lane + 3]);
+  const unsigned m = __ballot_sync(__activemask(), act);
+  if (m && (threadIdx.x & 31) == (unsigned)(__ffs(m) - 1))
+    atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
+}
+
 // out[s * T + t] = slab[trow[t]][s] (INF above the threshold); 32 x 32 tiles.
 __global__ void __launch_bounds__(256)
     k_extract_lanes(const uint32_t* __restrict__ slab, uint32_t Kp,
@@ -212,17 +272,35 @@ __global__ void __launch_bounds__(256)
 
 namespace bf {
 
+// Grow the shared distance slab to at least `need` bytes.
+bf_status ensure_slab(Graph* g, size_t need) {
+  if (need <= g->slab_bytes) return BF_OK;
+  if (g->d_slab) {
+    cudaFree(g->d_slab);
+    g->device_bytes -= g->slab_bytes;
+    g->d_slab = nullptr;
+    g->slab_bytes = 0;
+  }
+  if (cudaMalloc(&g->d_slab, need) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cannot allocate the batched distance slab (" + std::to_string(need) + " bytes)");
+    return BF_ERR_OOM;
+  }
+  g->slab_bytes = need;
+  g->device_bytes += need;
+  return BF_OK;
+}
+
 bf_status batched_prepare(Graph* g, uint32_t) {
-  g->sc = Graph::Sched();
+  (void)g;
   return BF_OK;
 }
 
 // Launch the restricted sweep's level schedule. From the second call on the
 // same schedule and slab geometry the launches are replayed from a captured
 // CUDA graph instead of being issued one by one.
-static bf_status sweep_levels(Graph* g, uint32_t Kp, unsigned lane_blocks, unsigned tpb,
-                              cudaStream_t st, uint64_t* launches) {
-  Graph::Sched& sc = g->sc;
+bf_status sweep_levels(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_blocks,
+                       unsigned tpb, cudaStream_t st, uint64_t* launches) {
   auto issue = [&](cudaStream_t s) {
     for (uint32_t l = 0; l < g->n_levels; ++l) {
       const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
@@ -274,6 +352,22 @@ static bf_status sweep_levels(Graph* g, uint32_t Kp, unsigned lane_blocks, unsig
   return BF_OK;
 }
 
+// Gated level schedule (launched directly: the skip decisions depend on the
+// data of each call).
+bf_status sweep_levels_gated(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_blocks,
+                             unsigned tpb, uint32_t* active, const uint32_t* thr, uint32_t kw,
+                             cudaStream_t st, uint64_t* launches) {
+  for (uint32_t l = 0; l < g->n_levels; ++l) {
+    const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
+    if (i1 == i0) continue;
+    dim3 grid(i1 - i0, lane_blocks);
+    k_sweep_gated<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, g->d_slab, Kp, active, thr, kw);
+    ++*launches;
+  }
+  BF_CUDA(cudaGetLastError());
+  return BF_OK;
+}
+
 bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
                          uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                          bf_stats* stats) {
@@ -286,7 +380,7 @@ bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint
       set_error("targets[" + std::to_string(i) + "] is not a node of the graph");
       return BF_ERR_INVALID;
     }
-  if ((s = build_schedule(g, h_tgt.data(), T, st))) return s;
+  if ((s = build_schedule(g, g->sc, h_tgt.data(), T, false, st))) return s;
   const Graph::Sched& sc = g->sc;
   const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
   // lanes per wave: all sources if the slab fits the budget, else waves
@@ -300,22 +394,7 @@ bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint
   }
   const uint64_t wave = std::min<uint64_t>(max_lanes, (S + 3) & ~3ull);
   const uint32_t Kp = (uint32_t)((wave + 3) & ~3ull);
-  const size_t need = (size_t)rows * Kp * 4;
-  if (need > g->slab_bytes) {
-    if (g->d_slab) {
-      cudaFree(g->d_slab);
-      g->device_bytes -= g->slab_bytes;
-      g->d_slab = nullptr;
-      g->slab_bytes = 0;
-    }
-    if (cudaMalloc(&g->d_slab, need) != cudaSuccess) {
-      cudaGetLastError();
-      set_error("cannot allocate the batched distance slab (" + std::to_string(need) + " bytes)");
-      return BF_ERR_OOM;
-    }
-    g->slab_bytes = need;
-    g->device_bytes += need;
-  }
+  if ((s = ensure_slab(g, (size_t)rows * Kp * 4))) return s;
   uint64_t launches = 0;
   float t_up = 0, t_dn = 0, t_ex = 0;
   const unsigned thr_per_blk = std::min<uint32_t>(128, ((Kp / 4 + 31) / 32) * 32);
@@ -328,7 +407,7 @@ bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint
       return s;
     launches += 1;
     if (stats) BF_CUDA(cudaEventRecord(g->ev[1], st));
-    if ((s = sweep_levels(g, Kp, lane_blocks, thr_per_blk, st, &launches))) return s;
+    if ((s = sweep_levels(g, g->sc, Kp, lane_blocks, thr_per_blk, st, &launches))) return s;
     if (stats) BF_CUDA(cudaEventRecord(g->ev[2], st));
     dim3 eg((unsigned)((T + 31) / 32), (unsigned)((kw + 31) / 32)), eb(32, 8);
     k_extract_lanes<<<eg, eb, 0, st>>>(g->d_slab, Kp, sc.d_trow, T, (uint32_t)kw, threshold,

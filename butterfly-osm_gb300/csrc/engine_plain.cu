@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
                   const uint32_t* __restrict__ depth, const uint64_t* __restrict__ up_off,
                   const uint2* __restrict__ up_rec, const uint32_t* __restrict__ pos_of,
                   uint32_t n, uint32_t* __restrict__ seed, uint32_t seed_stride,
-                  uint32_t* __restrict__ flag, uint32_t dcap, uint32_t* __restrict__ err) {
+                  uint32_t* __restrict__ flag, uint32_t dcap, uint32_t* __restrict__ err,
+                  const uint32_t* __restrict__ lane_thr) {
   extern __shared__ uint32_t smem[];
   const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t w = blockIdx.x * UPWARD_WARPS + wib;
@@ -181,13 +182,16 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
     b_cur = b_nx;
     e_cur = e_nx;
   }
+  // with lane_thr, a seed above this lane's own threshold can never reach a
+  // node within it: it is written but does not mark its row active
+  const uint32_t lt = lane_thr ? lane_thr[w] : threshold;
   for (uint32_t l = lane; l < D; l += 32) {
     const uint32_t d = *(const volatile uint32_t*)&pd[l];
     if (d == INF || d > threshold) continue;
     const uint32_t p = pos_of[pn[l]];
     if (p == NONE) continue;
     seed[(size_t)p * seed_stride + w] = d;
-    if (flag) atomicOr(&flag[p >> 5], 1u << (p & 31));
+    if (flag && d <= lt) atomicOr(&flag[p >> 5], 1u << (p & 31));
   }
 }
 
@@ -301,7 +305,7 @@ static bf_status plain_buffers(Graph* g) {
 // NONE are skipped. `flag` (optional) receives the seeded-row bits.
 bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t threshold,
                         const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
-                        cudaStream_t st) {
+                        cudaStream_t st, const uint32_t* lane_thr) {
   const uint32_t dcap = ((g->max_depth + 1) + 31) & ~31u;
   const size_t fast_smem = (size_t)UPWARD_WARPS * 2 * dcap * 4;
   const bool fast = fast_smem <= 200 * 1024;
@@ -311,7 +315,7 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
     k_upward_fast<<<(unsigned)((k + UPWARD_WARPS - 1) / UPWARD_WARPS), UPWARD_WARPS * 32,
                     fast_smem, st>>>(d_src, (uint32_t)k, threshold, g->d_parent, g->d_run_end,
                                      g->d_depth, g->d_up_off, g->d_up_rec, pos_map, g->n, seed,
-                                     stride, flag, dcap, g->d_err);
+                                     stride, flag, dcap, g->d_err, lane_thr);
     BF_CUDA(cudaGetLastError());
     return BF_OK;
   }
@@ -326,6 +330,10 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
         return BF_ERR_OOM;
       }
       g->device_bytes += bytes;
+    }
+    if (lane_thr) {
+      set_error("per-lane thresholds need the shared-memory upward pass (tree too deep)");
+      return BF_ERR_UNSUPPORTED;
     }
     for (uint64_t s0 = 0; s0 < k; s0 += PLAIN_K) {
       uint32_t kk = (uint32_t)std::min<uint64_t>(PLAIN_K, k - s0);

@@ -221,12 +221,14 @@ void free_graph(Graph* g) {
   void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth,  g->d_up_off,    g->d_up_rec,
                   g->d_pos_of,  g->d_rank_at, g->d_in_off, g->d_in_rec,    g->d_dist,
                   g->d_seed,    g->d_flag,    g->d_err,    g->d_gpath,     g->sc.d_cidx,
-                  g->sc.d_item, g->sc.d_erec, g->sc.d_trow, g->d_slab,  g->d_io};
+                  g->sc.d_item, g->sc.d_erec, g->sc.d_trow, g->d_slab,  g->d_io,
+                  g->full.d_cidx, g->full.d_item, g->full.d_erec, g->full.d_trow, g->d_iso,  g->d_iso_tmp};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& e : g->ev)
     if (e) cudaEventDestroy(e);
   if (g->sc.gexec) cudaGraphExecDestroy(g->sc.gexec);
+  if (g->full.gexec) cudaGraphExecDestroy(g->full.gexec);
   if (g->stream) cudaStreamDestroy(g->stream);
 }
 

@@ -1,0 +1,218 @@
+// isochrone.cu — bulk isochrone reachable sets on the GPU.
+//
+// Restates the PHAST part of the reference's bulk isochrones
+// (isochrone_bulk_handler, route/src/server/isochrone_handler.rs:1668-1709,
+// and BatchedIsochroneEngine::query_many, route/src/range/batched_isochrone.rs:216):
+// for origin i with threshold T_i the reachable set is
+// {rank r : dist(origin_i, r) <= T_i}, the settled set that
+// run_phast_bounded_fast_seeded (isochrone_handler.rs:338-491) returns.
+//
+// Origins are the lanes of a full-graph sweep (every node is a row; waves of
+// as many lanes as the HBM budget allows). Distances are computed unbounded,
+// which is exact, and the threshold is applied when the bitsets are emitted:
+// k_bits stages a 256-rank x 32-lane tile of the slab in shared memory and
+// turns each lane's 256 comparisons into eight ballot words (one 32-byte
+// sector of that origin's bitset row).
+
+#include <algorithm>
+
+#include "engine.cuh"
+
+namespace bf {
+
+namespace {
+
+constexpr uint32_t TILE_R = 256;  // ranks per tile
+constexpr uint32_t TILE_L = 32;   // lanes per tile
+constexpr uint32_t LANE_TILES_PER_BLOCK = 8;
+
+// bits: rows of w32 u32 words; lane l writes output row out_row[l]. A block
+// owns 256 ranks and walks all lane tiles of the wave: the ranks' slab rows
+// and activity are looked up once, inactive rows (no value within any lane's
+// threshold) are never read, and a tile with no active row only writes zeros.
+__global__ void __launch_bounds__(256)
+    k_bits(const uint32_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ cidx,
+           uint32_t n, const uint32_t* __restrict__ thr, uint32_t kw, uint32_t* __restrict__ bits,
+           uint64_t w32, unsigned long long* __restrict__ counts,
+           const uint32_t* __restrict__ active, const uint32_t* __restrict__ out_row) {
+  __shared__ uint32_t tile[TILE_R][TILE_L + 1];
+  __shared__ uint32_t srow[TILE_R];
+  __shared__ int any_active;
+  const uint32_t r0 = blockIdx.x * TILE_R;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) any_active = 0;
+  __syncthreads();
+  {
+    const uint32_t rank = r0 + threadIdx.x;
+    uint32_t row = NONE;
+    if (rank < n) {
+      const uint32_t c = cidx[rank];
+      if ((active[c >> 5] >> (c & 31)) & 1u) row = c;
+    }
+    srow[threadIdx.x] = row;
+    if (__any_sync(0xFFFFFFFFu, row != NONE) && lane == 0) any_active = 1;
+  }
+  __syncthreads();
+  const bool live = any_active != 0;
+  const uint64_t wbase = r0 / 32;
+  const uint32_t lend = min(kw, (blockIdx.y + 1) * TILE_L * LANE_TILES_PER_BLOCK);
+  for (uint32_t l0 = blockIdx.y * TILE_L * LANE_TILES_PER_BLOCK; l0 < lend; l0 += TILE_L) {
+    if (live) {
+      for (uint32_t r = warp; r < TILE_R; r += 8) {
+        const uint32_t row = srow[r], l = l0 + lane;
+        tile[r][lane] = (row != NONE && l < lend) ? slab[(size_t)row * Kp + l] : INF;
+      }
+      __syncthreads();
+    }
+    for (uint32_t q = 0; q < 4; ++q) {
+      const uint32_t li = warp * 4 + q, l = l0 + li;
+      if (l >= lend) continue;  // warp-uniform
+      const uint64_t orow = out_row[l];
+      uint32_t mine = 0;
+      if (live) {
+        const uint32_t t = thr[l];
+        for (uint32_t c = 0; c < TILE_R / 32; ++c) {
+          const uint32_t d = tile[c * 32 + lane][li];
+          const uint32_t word = __ballot_sync(0xFFFFFFFFu, d != INF && d <= t);
+          if (lane == c) mine = word;
+        }
+      }
+      const uint64_t wi = wbase + lane;
+      uint32_t pc = 0;
+      if (lane < TILE_R / 32 && wi < w32) {
+        bits[orow * w32 + wi] = mine;
+        pc = __popc(mine);
+      }
+      if (live) {
+        for (int o = 16; o > 0; o >>= 1) pc += __shfl_down_sync(0xFFFFFFFFu, pc, o);
+        if (lane == 0 && pc) atomicAdd(&counts[orow], (unsigned long long)pc);
+      }
+    }
+    if (live) __syncthreads();
+  }
+}
+
+}  // namespace
+
+// d_bits: n rows of ceil(n_nodes / 64) u64 words; d_counts: n u64.
+// Origins are processed in (threshold, rank) order so that the lanes of a
+// wave share a threshold and lie close together in the nested-dissection
+// order, which keeps the set of active rows of the gated sweep small.
+bf_status isochrone_bitsets(Graph* g, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
+                            uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,
+                            bf_stats* stats) {
+  bf_status s;
+  if ((s = build_schedule(g, g->full, nullptr, 0, true, st))) return s;
+  Graph::Sched& sc = g->full;
+  const uint64_t rows = g->n;
+  const uint64_t w64 = (g->n + 63) / 64;
+  const uint64_t aw = (rows + 31) / 32;  // active-bitmap words
+  // permutation: (threshold, rank) order
+  std::vector<uint32_t> ho(n), ht(n), perm(n);
+  BF_CUDA(cudaMemcpyAsync(ho.data(), d_orig, n * 4, cudaMemcpyDeviceToHost, st));
+  BF_CUDA(cudaMemcpyAsync(ht.data(), d_thr, n * 4, cudaMemcpyDeviceToHost, st));
+  BF_CUDA(cudaStreamSynchronize(st));
+  for (uint64_t i = 0; i < n; ++i)
+    if (ho[i] >= g->n) {
+      set_error("origins[" + std::to_string(i) + "] is not a node of the graph");
+      return BF_ERR_INVALID;
+    }
+  for (uint64_t i = 0; i < n; ++i) perm[i] = (uint32_t)i;
+  std::sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) {
+    return ht[a] != ht[b] ? ht[a] < ht[b] : ho[a] < ho[b];
+  });
+  std::vector<uint32_t> pk(3 * n);
+  for (uint64_t i = 0; i < n; ++i) {
+    pk[i] = ho[perm[i]];
+    pk[n + i] = ht[perm[i]];
+    pk[2 * n + i] = perm[i];
+  }
+  const size_t need = pk.size() * 4 + aw * 4;
+  if (need > g->iso_tmp_bytes) {
+    if (g->d_iso_tmp) {
+      cudaFree(g->d_iso_tmp);
+      g->device_bytes -= g->iso_tmp_bytes;
+      g->d_iso_tmp = nullptr;
+      g->iso_tmp_bytes = 0;
+    }
+    if (cudaMalloc(&g->d_iso_tmp, need) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc for isochrone scratch failed");
+      return BF_ERR_OOM;
+    }
+    g->iso_tmp_bytes = need;
+    g->device_bytes += need;
+  }
+  uint32_t* p_orig = g->d_iso_tmp;
+  uint32_t* p_thr = p_orig + n;
+  uint32_t* p_row = p_thr + n;
+  uint32_t* d_active = p_row + n;
+  BF_CUDA(cudaMemcpyAsync(p_orig, pk.data(), pk.size() * 4, cudaMemcpyHostToDevice, st));
+  // the slab is the only per-lane device memory here
+  uint64_t budget = g->hbm_budget > g->device_bytes ? g->hbm_budget - g->device_bytes : 0;
+  budget += g->slab_bytes;
+  uint64_t max_lanes = budget / (rows * 4);
+  max_lanes = max_lanes >= 32 ? max_lanes & ~31ull : 0;
+  if (!max_lanes) {
+    set_error("HBM budget too small for one 32-lane isochrone wave");
+    return BF_ERR_OOM;
+  }
+  const uint64_t wave = std::min<uint64_t>(max_lanes, (n + 3) & ~3ull);
+  const uint32_t Kp = (uint32_t)((wave + 3) & ~3ull);
+  if ((s = ensure_slab(g, (size_t)rows * Kp * 4))) return s;
+  BF_CUDA(cudaMemsetAsync(d_counts, 0, n * 8, st));
+  const unsigned tpb = std::min<uint32_t>(128, ((Kp / 4 + 31) / 32) * 32);
+  const unsigned lane_blocks = (Kp / 4 + tpb - 1) / tpb;
+  uint64_t launches = 0;
+  float t_up = 0, t_dn = 0, t_ex = 0;
+  for (uint64_t s0 = 0; s0 < n; s0 += wave) {
+    const uint64_t kw = std::min<uint64_t>(wave, n - s0);
+    if (stats) BF_CUDA(cudaEventRecord(g->ev[0], st));
+    BF_CUDA(cudaMemsetAsync(g->d_slab, 0xFF, (size_t)rows * Kp * 4, st));
+    BF_CUDA(cudaMemsetAsync(d_active, 0, aw * 4, st));
+    if ((s = launch_upward(g, p_orig + s0, kw, INF, sc.d_cidx, g->d_slab, Kp, d_active, st,
+                           p_thr + s0)))
+      return s;
+    ++launches;
+    if (stats) BF_CUDA(cudaEventRecord(g->ev[1], st));
+    if ((s = sweep_levels_gated(g, sc, Kp, lane_blocks, tpb, d_active, p_thr + s0,
+                                (uint32_t)kw, st, &launches)))
+      return s;
+    if (stats) BF_CUDA(cudaEventRecord(g->ev[2], st));
+    dim3 bgrid((unsigned)((g->n + TILE_R - 1) / TILE_R),
+               (unsigned)((kw + TILE_L * LANE_TILES_PER_BLOCK - 1) / (TILE_L * LANE_TILES_PER_BLOCK)));
+    k_bits<<<bgrid, 256, 0, st>>>(g->d_slab, Kp, sc.d_cidx, g->n, p_thr + s0, (uint32_t)kw,
+                                 reinterpret_cast<uint32_t*>(d_bits), 2 * w64,
+                                 reinterpret_cast<unsigned long long*>(d_counts), d_active,
+                                 p_row + s0);
+    BF_CUDA(cudaGetLastError());
+    ++launches;
+    if (stats) {
+      BF_CUDA(cudaEventRecord(g->ev[3], st));
+      BF_CUDA(cudaEventSynchronize(g->ev[3]));
+      float a, b, c;
+      BF_CUDA(cudaEventElapsedTime(&a, g->ev[0], g->ev[1]));
+      BF_CUDA(cudaEventElapsedTime(&b, g->ev[1], g->ev[2]));
+      BF_CUDA(cudaEventElapsedTime(&c, g->ev[2], g->ev[3]));
+      t_up += a;
+      t_dn += b;
+      t_ex += c;
+    }
+  }
+  BF_CUDA(cudaStreamSynchronize(st));  // pk / perm host vectors die on return
+  if (stats) {
+    const uint64_t waves = (n + wave - 1) / wave;
+    stats->n_batches += waves;
+    stats->waves += waves;
+    stats->kernel_launches += launches;
+    stats->upward_ms += t_up;
+    stats->downward_ms += t_dn;
+    stats->extract_ms += t_ex;
+    stats->swept_nodes = sc.n_r;
+    stats->swept_edges = sc.n_edges;
+    stats->lanes = Kp;
+  }
+  return BF_OK;
+}
+
+}  // namespace bf

@@ -209,6 +209,14 @@ bf_status bf_isochrone_bitsets(bf_graph* g, const uint32_t* origins, const uint3
                                uint64_t n_origins, uint64_t* bits_out, uint64_t* counts_out,
                                bf_stats* st);
 
+/* bf_isochrone_bitsets with device buffers (d_origins, d_thresholds: n
+ * entries; d_bits: n rows of ceil(n_nodes / 64) u64; d_counts: n u64) on the
+ * given stream (NULL = the graph's stream); returns after completion. */
+bf_status bf_isochrone_bitsets_device(bf_graph* g, const uint32_t* d_origins,
+                                      const uint32_t* d_thresholds, uint64_t n_origins,
+                                      uint64_t* d_bits, uint64_t* d_counts, void* stream,
+                                      bf_stats* st);
+
 /* ---- serving loop (continuous batching of matrix and isochrone requests) ---- */
 
 typedef struct bf_server bf_server;
