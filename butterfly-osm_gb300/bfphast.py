@@ -105,8 +105,8 @@ _SIGNATURES = {
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "bf_matrix_seeded": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Seed), _u64p,
                                         ctypes.c_uint64, ctypes.POINTER(Seed), _u64p,
-                                        ctypes.c_uint64, ctypes.c_uint32, _u32p,
-                                        ctypes.POINTER(Stats)]),
+                                        ctypes.c_uint64, ctypes.c_uint32, _u32p, _u64p,
+                                        ctypes.c_uint64, _u64p, ctypes.POINTER(Stats)]),
     "bf_phast_bounded_seeded": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Seed),
                                                ctypes.c_uint32, ctypes.c_uint32, _u32p, _u32p,
                                                ctypes.c_uint64, _u64p]),
@@ -238,8 +238,9 @@ class Graph:
                                        ctypes.c_void_p(stream or 0), ctypes.byref(st)))
         return st.as_dict()
 
-    def matrix_seeded(self, src_seeds, tgt_seeds, threshold=INF):
-        """src_seeds / tgt_seeds: lists of lists of (rank, cost)."""
+    def matrix_seeded(self, src_seeds, tgt_seeds, threshold=INF, with_conflicts=False):
+        """src_seeds / tgt_seeds: lists of lists of (rank, cost). Returns the
+        matrix (conflict cells INF) and, if asked, the conflict cell indices."""
         def pack(sets):
             off = np.zeros(len(sets) + 1, dtype=np.uint64)
             flat = []
@@ -252,9 +253,15 @@ class Graph:
         ta, to = pack(tgt_seeds)
         out = np.empty((len(src_seeds), len(tgt_seeds)), dtype=np.uint32)
         st = Stats()
+        cap = len(src_seeds) * len(tgt_seeds)
+        conf = np.empty(max(1, cap), dtype=np.uint64)
+        nconf = ctypes.c_uint64()
         _check(load().bf_matrix_seeded(self._h, sa, _ptr(so, _u64p), len(src_seeds), ta,
                                        _ptr(to, _u64p), len(tgt_seeds), threshold, _ptr(out),
+                                       _ptr(conf, _u64p), cap, ctypes.byref(nconf),
                                        ctypes.byref(st)))
+        if with_conflicts:
+            return out, conf[:min(cap, nconf.value)].copy()
         return out
 
     def phast_bounded_seeded(self, seeds, threshold):

@@ -320,16 +320,77 @@ bf_status bf_phast_query(bf_graph* h, uint32_t origin, uint32_t* dist_out) {
   return bf_query_batch(h, &origin, 1, BF_INF, dist_out);
 }
 
-bf_status bf_matrix_seeded(bf_graph*, const bf_seed*, const uint64_t*, uint64_t, const bf_seed*,
-                           const uint64_t*, uint64_t, uint32_t, uint32_t*, bf_stats*) {
-  set_error("bf_matrix_seeded: not implemented yet");
-  return BF_ERR_UNSUPPORTED;
+static bf_status check_seedsets(const bf_seed* seeds, const uint64_t* off, uint64_t m,
+                                uint32_t n, const char* what) {
+  if (!off || off[0] != 0) {
+    set_error(std::string(what) + " offsets must start at 0");
+    return BF_ERR_INVALID;
+  }
+  for (uint64_t i = 0; i < m; ++i)
+    if (off[i + 1] < off[i]) {
+      set_error(std::string(what) + " offsets must be non-decreasing");
+      return BF_ERR_INVALID;
+    }
+  if (off[m] && !seeds) {
+    set_error(std::string(what) + " seeds missing");
+    return BF_ERR_INVALID;
+  }
+  for (uint64_t k = 0; k < off[m]; ++k)
+    if (seeds[k].rank >= n) {
+      set_error(std::string(what) + " seed rank " + std::to_string(seeds[k].rank) +
+                " is not a node of the graph");
+      return BF_ERR_INVALID;
+    }
+  return BF_OK;
 }
 
-bf_status bf_phast_bounded_seeded(bf_graph*, const bf_seed*, uint32_t, uint32_t, uint32_t*,
-                                  uint32_t*, uint64_t, uint64_t*) {
-  set_error("bf_phast_bounded_seeded: not implemented yet");
-  return BF_ERR_UNSUPPORTED;
+bf_status bf_matrix_seeded(bf_graph* h, const bf_seed* src_seeds, const uint64_t* src_off,
+                           uint64_t S, const bf_seed* tgt_seeds, const uint64_t* tgt_off,
+                           uint64_t T, uint32_t threshold, uint32_t* out, uint64_t* conflicts,
+                           uint64_t conflict_cap, uint64_t* n_conflicts, bf_stats* st) {
+  if (!h || (S && T && !out) || (conflict_cap && !conflicts)) {
+    set_error("bf_matrix_seeded: null argument");
+    return BF_ERR_INVALID;
+  }
+  double t0 = now_s();
+  Graph* g = &h->g;
+  bf_status rc;
+  if ((rc = check_seedsets(src_seeds, src_off, S, g->n, "source")) ||
+      (rc = check_seedsets(tgt_seeds, tgt_off, T, g->n, "target")))
+    return rc;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (n_conflicts) *n_conflicts = 0;
+  if (!S || !T) return BF_OK;
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  rc = matrix_seeded(g, src_seeds, src_off, S, tgt_seeds, tgt_off, T, threshold, out, conflicts,
+                     conflict_cap, n_conflicts, st);
+  if (st) {
+    st->n_sources = S;
+    st->n_targets = T;
+    st->total_ms = (now_s() - t0) * 1e3;
+  }
+  return rc;
+}
+
+bf_status bf_phast_bounded_seeded(bf_graph* h, const bf_seed* seeds, uint32_t n_seeds,
+                                  uint32_t threshold, uint32_t* out_rank, uint32_t* out_dist,
+                                  uint64_t cap, uint64_t* n_out) {
+  if (!h || (n_seeds && !seeds) || (cap && (!out_rank || !out_dist))) {
+    set_error("bf_phast_bounded_seeded: null argument");
+    return BF_ERR_INVALID;
+  }
+  Graph* g = &h->g;
+  for (uint32_t i = 0; i < n_seeds; ++i)
+    if (seeds[i].rank >= g->n) {
+      set_error("bf_phast_bounded_seeded: seed rank " + std::to_string(seeds[i].rank) +
+                " is not a node of the graph");
+      return BF_ERR_INVALID;
+    }
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (n_out) *n_out = 0;
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  return bounded_seeded(g, seeds, n_seeds, threshold, out_rank, out_dist, cap, n_out);
 }
 
 bf_status bf_isochrone_bitsets_device(bf_graph* h, const uint32_t* d_orig, const uint32_t* d_thr,

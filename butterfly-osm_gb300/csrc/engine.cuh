@@ -120,7 +120,8 @@ bf_status to_positions(Graph* g, const uint32_t* d_rank, uint64_t n, uint32_t* d
 bf_status check_device_error(Graph* g, cudaStream_t st);
 bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t threshold,
                         const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
-                        cudaStream_t st, const uint32_t* lane_thr = nullptr);
+                        cudaStream_t st, const uint32_t* lane_thr = nullptr,
+                        const uint32_t* unit_cost = nullptr, const uint32_t* unit_lane = nullptr);
 __global__ void k_extract(const uint32_t* __restrict__ slab, uint32_t slab_stride,
                           const uint32_t* __restrict__ tpos, uint64_t T, uint32_t k,
                           uint32_t* __restrict__ out);
@@ -143,6 +144,14 @@ bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint
 bf_status isochrone_bitsets(Graph* g, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
                             uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,
                             bf_stats* stats);
+
+// seeded.cu
+bf_status matrix_seeded(Graph* g, const bf_seed* src_seeds, const uint64_t* src_off, uint64_t S,
+                        const bf_seed* tgt_seeds, const uint64_t* tgt_off, uint64_t T,
+                        uint32_t threshold, uint32_t* out, uint64_t* conflicts,
+                        uint64_t conflict_cap, uint64_t* n_conflicts, bf_stats* st);
+bf_status bounded_seeded(Graph* g, const bf_seed* seeds, uint32_t n_seeds, uint32_t threshold,
+                         uint32_t* out_rank, uint32_t* out_dist, uint64_t cap, uint64_t* n_out);
 
 // noalloc.cu
 bf_status query_batch_noalloc(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,

@@ -122,7 +122,8 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
                   const uint2* __restrict__ up_rec, const uint32_t* __restrict__ pos_of,
                   uint32_t n, uint32_t* __restrict__ seed, uint32_t seed_stride,
                   uint32_t* __restrict__ flag, uint32_t dcap, uint32_t* __restrict__ err,
-                  const uint32_t* __restrict__ lane_thr) {
+                  const uint32_t* __restrict__ lane_thr, const uint32_t* __restrict__ unit_cost,
+                  const uint32_t* __restrict__ unit_lane) {
   extern __shared__ uint32_t smem[];
   const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t w = blockIdx.x * UPWARD_WARPS + wib;
@@ -139,7 +140,10 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
     if (lane == 0) atomicOr(err, DEVERR_PATH);
     return;
   }
-  for (uint32_t l = lane; l < D; l += 32) pd[l] = (l == 0) ? 0u : INF;
+  // a seeded unit starts at its seed cost and writes (min) into its source's lane
+  const uint32_t c0 = unit_cost ? unit_cost[w] : 0u;
+  const uint32_t out_lane = unit_lane ? unit_lane[w] : w;
+  for (uint32_t l = lane; l < D; l += 32) pd[l] = (l == 0) ? c0 : INF;
   __syncwarp();
   const unsigned FULL = 0xFFFFFFFFu;
   uint64_t cb = 0, ce = 0;  // edge range of path node (chunk base + lane)
@@ -184,13 +188,14 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
   }
   // with lane_thr, a seed above this lane's own threshold can never reach a
   // node within it: it is written but does not mark its row active
-  const uint32_t lt = lane_thr ? lane_thr[w] : threshold;
+  const uint32_t lt = lane_thr ? lane_thr[out_lane] : threshold;
   for (uint32_t l = lane; l < D; l += 32) {
     const uint32_t d = *(const volatile uint32_t*)&pd[l];
     if (d == INF || d > threshold) continue;
     const uint32_t p = pos_of[pn[l]];
     if (p == NONE) continue;
-    seed[(size_t)p * seed_stride + w] = d;
+    if (unit_lane) atomicMin(&seed[(size_t)p * seed_stride + out_lane], d);
+    else seed[(size_t)p * seed_stride + w] = d;
     if (flag && d <= lt) atomicOr(&flag[p >> 5], 1u << (p & 31));
   }
 }
@@ -305,7 +310,8 @@ static bf_status plain_buffers(Graph* g) {
 // NONE are skipped. `flag` (optional) receives the seeded-row bits.
 bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t threshold,
                         const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
-                        cudaStream_t st, const uint32_t* lane_thr) {
+                        cudaStream_t st, const uint32_t* lane_thr, const uint32_t* unit_cost,
+                        const uint32_t* unit_lane) {
   const uint32_t dcap = ((g->max_depth + 1) + 31) & ~31u;
   const size_t fast_smem = (size_t)UPWARD_WARPS * 2 * dcap * 4;
   const bool fast = fast_smem <= 200 * 1024;
@@ -315,7 +321,8 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
     k_upward_fast<<<(unsigned)((k + UPWARD_WARPS - 1) / UPWARD_WARPS), UPWARD_WARPS * 32,
                     fast_smem, st>>>(d_src, (uint32_t)k, threshold, g->d_parent, g->d_run_end,
                                      g->d_depth, g->d_up_off, g->d_up_rec, pos_map, g->n, seed,
-                                     stride, flag, dcap, g->d_err, lane_thr);
+                                     stride, flag, dcap, g->d_err, lane_thr, unit_cost,
+                                     unit_lane);
     BF_CUDA(cudaGetLastError());
     return BF_OK;
   }
@@ -331,8 +338,9 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
       }
       g->device_bytes += bytes;
     }
-    if (lane_thr) {
-      set_error("per-lane thresholds need the shared-memory upward pass (tree too deep)");
+    if (lane_thr || unit_cost || unit_lane) {
+      set_error("seeded units and per-lane thresholds need the shared-memory upward pass "
+                "(elimination tree too deep)");
       return BF_ERR_UNSUPPORTED;
     }
     for (uint64_t s0 = 0; s0 < k; s0 += PLAIN_K) {

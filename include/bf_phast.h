@@ -183,16 +183,24 @@ bf_status bf_matrix_device(bf_graph* g, const uint32_t* d_sources, uint64_t n_so
 
 /* Phantom-seeded matrix (table_phast_lopsided, bucket_ch.rs:6717-6852).
  * Source s has seeds src_seeds[src_off[s] .. src_off[s+1]), each a (rank,
- * cost) pair entered into the field with that cost; target t's value is
- * min over its seeds (rank, part) of F[rank] - part (saturating). Cells above
- * the threshold are BF_INF. */
+ * cost) pair entered into its field F_s with that cost (a super-source);
+ * target t's value is min over its seeds (rank, part) of F_s[rank] - part
+ * (saturating, unreachable seeds skipped). Cells above the threshold are
+ * BF_INF. A pair whose source and target share a seed rank (a same-edge
+ * move, which the reference recomputes with its bucket engine,
+ * bucket_ch.rs:6786-6845) is a conflict: its cell is left BF_INF and its
+ * index s * n_targets + t is reported in conflict_cells (ascending, at most
+ * conflict_cap written; *n_conflicts receives the total) for the caller's
+ * bucket path. conflict_cells may be NULL when conflict_cap is 0. */
 typedef struct bf_seed {
   uint32_t rank;
   uint32_t cost;
 } bf_seed;
 bf_status bf_matrix_seeded(bf_graph* g, const bf_seed* src_seeds, const uint64_t* src_off,
                            uint64_t n_sources, const bf_seed* tgt_seeds, const uint64_t* tgt_off,
-                           uint64_t n_targets, uint32_t threshold, uint32_t* out, bf_stats* st);
+                           uint64_t n_targets, uint32_t threshold, uint32_t* out,
+                           uint64_t* conflict_cells, uint64_t conflict_cap,
+                           uint64_t* n_conflicts, bf_stats* st);
 
 /* run_phast_bounded_fast_seeded: settled (rank, dist <= threshold) pairs in
  * ascending rank order. Writes at most cap pairs; *n_out receives the full

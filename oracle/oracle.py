@@ -139,3 +139,42 @@ def down_reverse(cch):
     off = np.zeros(n + 1, dtype=np.uint64)
     off[1:] = np.cumsum(cnt)
     return off, src[order], w[order]
+
+
+def table_phast_lopsided(cch, src_seedsets, tgt_seedsets, threshold):
+    """table_phast_lopsided (route/src/matrix/bucket_ch.rs:6717-6852), field
+    part: per source one run_phast_bounded_fast_seeded field with bound
+    T + max source part + max target part (:6741-6758); per target
+    min over its seeds (rank, part) of F[rank] - part (saturating, :6785-6808);
+    cells above T -> INF (:6800-6803). Pairs sharing a seed rank are the
+    reference's bucket-engine conflicts (:6786-6790, :6826-6845): returned as
+    cell indices with INF in the matrix."""
+    S, T = len(src_seedsets), len(tgt_seedsets)
+    out = np.full((S, T), INF, dtype=np.uint32)
+    max_tgt = max([p for ss in tgt_seedsets for _, p in ss] or [0])
+    conflicts = []
+    for s, seeds in enumerate(src_seedsets):
+        if not seeds:
+            continue
+        if threshold == INF:
+            bound = INF
+        else:
+            bound = min(INF, threshold + max(c for _, c in seeds) + max_tgt)
+        rk, ds = cch.bounded_seeded(seeds, bound)
+        field = dict(zip(rk.tolist(), ds.tolist()))
+        src_ranks = {r for r, _ in seeds}
+        for t, tseeds in enumerate(tgt_seedsets):
+            if not tseeds:
+                continue
+            if any(r in src_ranks for r, _ in tseeds):
+                conflicts.append(s * T + t)
+                continue
+            best = INF
+            for r, part in tseeds:
+                f = field.get(r)
+                if f is not None and f != INF:
+                    best = min(best, f - part if f > part else 0)
+            if threshold != INF and best != INF and best > threshold:
+                best = INF
+            out[s, t] = best
+    return out, np.array(sorted(conflicts), dtype=np.uint64)
