@@ -292,3 +292,60 @@ class Graph:
             self._h, ctypes.c_void_p(d_orig), ctypes.c_void_p(d_thr), n, ctypes.c_void_p(d_bits),
             ctypes.c_void_p(d_counts), ctypes.c_void_p(stream or 0), ctypes.byref(st)))
         return st.as_dict()
+
+
+class Server:
+    """Continuous-batching serving loop (bf_server_*). Output buffers of
+    submitted requests are kept alive here until their completion is polled."""
+
+    def __init__(self, graph, hbm_budget=0, max_inflight=0, max_queue=0, timeout_ms=0):
+        self.graph = graph
+        cfg = ServerCfg(hbm_budget, max_inflight, max_queue, timeout_ms, 0)
+        h = ctypes.c_void_p()
+        _check(load().bf_server_create(graph.handle, ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._live = {}
+
+    def _submit(self, kind, src, tgt, threshold, out, tag):
+        req = Request(kind, threshold, _ptr(src), len(src),
+                      _ptr(tgt) if tgt is not None else None,
+                      len(tgt) if tgt is not None else 0, out.ctypes.data, tag)
+        t = ctypes.c_uint64()
+        _check(load().bf_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)))
+        self._live[t.value] = (src, tgt, out)
+        return t.value
+
+    def submit_matrix(self, sources, targets, threshold=INF, tag=0):
+        s, t = _u32(sources), _u32(targets)
+        out = np.empty((len(s), len(t)), dtype=np.uint32)
+        return self._submit(REQ_MATRIX, s, t, threshold, out, tag), out
+
+    def submit_isochrone(self, origin, threshold, tag=0):
+        s = _u32([origin])
+        out = np.empty((self.graph.n + 63) // 64, dtype=np.uint64)
+        return self._submit(REQ_ISOCHRONE, s, None, threshold, out, tag), out
+
+    def poll(self, wait_ms=100, cap=256):
+        buf = (Completion * cap)()
+        n = ctypes.c_uint32()
+        _check(load().bf_server_poll(self._h, buf, cap, wait_ms, ctypes.byref(n)))
+        res = []
+        for i in range(n.value):
+            c = buf[i]
+            self._live.pop(c.ticket, None)
+            res.append({f: getattr(c, f) for f, _ in c._fields_})
+        return res
+
+    def cancel(self, ticket):
+        return load().bf_server_cancel(self._h, ticket)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bf_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -75,7 +75,7 @@ bf_status run_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t
       return s;
     if (stats) stats->kernel_launches += 1;
   } else {
-    if ((s = batched_matrix(g, d_src, S, d_tgt, T, threshold, d_out, st, stats))) return s;
+    if ((s = batched_matrix(g, g->ctx, d_src, S, d_tgt, T, threshold, d_out, st, stats))) return s;
   }
   return check_device_error(g, st);
 }
@@ -88,6 +88,10 @@ using namespace bf;
 struct bf_graph {
   Graph g;
 };
+
+namespace bf {
+Graph* graph_of(bf_graph* h) { return &h->g; }
+}  // namespace bf
 
 extern "C" {
 
@@ -363,7 +367,7 @@ bf_status bf_matrix_seeded(bf_graph* h, const bf_seed* src_seeds, const uint64_t
   if (n_conflicts) *n_conflicts = 0;
   if (!S || !T) return BF_OK;
   if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
-  rc = matrix_seeded(g, src_seeds, src_off, S, tgt_seeds, tgt_off, T, threshold, out, conflicts,
+  rc = matrix_seeded(g, g->ctx, src_seeds, src_off, S, tgt_seeds, tgt_off, T, threshold, out, conflicts,
                      conflict_cap, n_conflicts, st);
   if (st) {
     st->n_sources = S;
@@ -390,7 +394,7 @@ bf_status bf_phast_bounded_seeded(bf_graph* h, const bf_seed* seeds, uint32_t n_
   std::lock_guard<std::mutex> lk(g->mu);
   if (n_out) *n_out = 0;
   if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
-  return bounded_seeded(g, seeds, n_seeds, threshold, out_rank, out_dist, cap, n_out);
+  return bounded_seeded(g, g->ctx, seeds, n_seeds, threshold, out_rank, out_dist, cap, n_out);
 }
 
 bf_status bf_isochrone_bitsets_device(bf_graph* h, const uint32_t* d_orig, const uint32_t* d_thr,
@@ -407,7 +411,7 @@ bf_status bf_isochrone_bitsets_device(bf_graph* h, const uint32_t* d_orig, const
   cudaStream_t s = stream ? (cudaStream_t)stream : g->stream;
   if (st) std::memset(st, 0, sizeof(*st));
   bf_status rc = BF_OK;
-  if (n) rc = isochrone_bitsets(g, d_orig, d_thr, n, d_bits, d_counts, s, st);
+  if (n) rc = isochrone_bitsets(g, g->ctx, d_orig, d_thr, n, d_bits, d_counts, s, st);
   if (rc == BF_OK) rc = check_device_error(g, s);
   if (st) {
     st->n_sources = n;
@@ -461,7 +465,7 @@ bf_status bf_isochrone_bitsets(bf_graph* h, const uint32_t* orig, const uint32_t
     const uint64_t m = std::min<uint64_t>(chunk, n - c0);
     BF_CUDA(cudaMemcpyAsync(d_orig, orig + c0, m * 4, cudaMemcpyHostToDevice, s));
     BF_CUDA(cudaMemcpyAsync(d_thr, thr + c0, m * 4, cudaMemcpyHostToDevice, s));
-    if ((rc = isochrone_bitsets(g, d_orig, d_thr, m, d_bits, d_counts, s, st))) return rc;
+    if ((rc = isochrone_bitsets(g, g->ctx, d_orig, d_thr, m, d_bits, d_counts, s, st))) return rc;
     BF_CUDA(cudaMemcpyAsync(bits + c0 * w64, d_bits, m * w64 * 8, cudaMemcpyDeviceToHost, s));
     if (counts)
       BF_CUDA(cudaMemcpyAsync(counts + c0, d_counts, m * 8, cudaMemcpyDeviceToHost, s));
@@ -477,26 +481,6 @@ bf_status bf_isochrone_bitsets(bf_graph* h, const uint32_t* orig, const uint32_t
   }
   return BF_OK;
 }
-
-bf_status bf_server_create(bf_graph*, const bf_server_cfg*, bf_server** out) {
-  if (out) *out = nullptr;
-  set_error("bf_server_create: not implemented yet");
-  return BF_ERR_UNSUPPORTED;
-}
-bf_status bf_server_submit(bf_server*, const bf_request*, uint64_t*) {
-  set_error("bf_server_submit: not implemented yet");
-  return BF_ERR_UNSUPPORTED;
-}
-bf_status bf_server_poll(bf_server*, bf_completion*, uint32_t, uint32_t, uint32_t* n_out) {
-  if (n_out) *n_out = 0;
-  set_error("bf_server_poll: not implemented yet");
-  return BF_ERR_UNSUPPORTED;
-}
-bf_status bf_server_cancel(bf_server*, uint64_t) {
-  set_error("bf_server_cancel: not implemented yet");
-  return BF_ERR_UNSUPPORTED;
-}
-void bf_server_destroy(bf_server*) {}
 
 const char* bf_last_error(void) { return t_err.c_str(); }
 

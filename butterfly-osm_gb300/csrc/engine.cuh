@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -35,6 +36,41 @@ constexpr uint32_t PLAIN_K = 32;
 constexpr uint32_t UPWARD_SMEM_PATH = 2048;
 constexpr uint32_t UPWARD_WARPS = 4;
 
+// A sweep schedule (target-restricted or full graph) with its cached CUDA graph.
+struct Sched {
+  bool valid = false;
+  uint64_t key = 0;              // hash of the target positions
+  uint32_t n_r = 0;              // restricted nodes
+  uint64_t n_items = 0;
+  uint64_t n_edges = 0;
+  std::vector<uint32_t> lvl_item;  // level -> first work item, n_levels + 1
+  uint32_t* d_cidx = nullptr;    // [n] rank -> compact row or NONE
+  uint4* d_item = nullptr;       // {row, edge0, edge1, split flag}
+  uint2* d_erec = nullptr;       // {source row, w}
+  uint32_t* d_trow = nullptr;    // [T] target rows
+  uint64_t T = 0;
+  size_t cap_items = 0, cap_edges = 0, cap_t = 0;
+  uint32_t uses = 0;             // calls that reused this schedule
+  cudaGraphExec_t gexec = nullptr;  // captured level launches
+  uint32_t g_kp = 0, g_lb = 0, g_tpb = 0;
+  uint32_t* g_slab = nullptr;
+  cudaStream_t g_stream = nullptr;
+};
+
+// Execution context of the batched engine: schedules, the distance slab and
+// scratch of one in-flight computation. The C-ABI calls use the graph's
+// context; the serving loop runs two contexts on two streams.
+struct Ctx {
+  Sched sc;                        // last target-restricted schedule
+  Sched full;                      // every node (isochrones, seeded fields)
+  uint32_t* d_slab = nullptr;      // distance slab [rows][Kp]
+  size_t slab_bytes = 0;
+  uint32_t* d_iso_tmp = nullptr;   // isochrone permutation and active-row bitmap
+  size_t iso_tmp_bytes = 0;
+  cudaEvent_t ev[4] = {};
+  uint64_t budget = 0;             // slab bytes this context may use (0 = graph budget)
+};
+
 struct Graph {
   int device = 0;
   uint32_t n = 0;
@@ -42,7 +78,7 @@ struct Graph {
   uint32_t n_levels = 0, max_depth = 0;
   uint32_t engine = BF_ENGINE_BATCHED;
   uint32_t k_lanes = 0;
-  uint64_t device_bytes = 0;
+  std::atomic<uint64_t> device_bytes{0};
   uint64_t hbm_budget = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
@@ -75,34 +111,11 @@ struct Graph {
   std::vector<uint64_t> h_in_off;  // [n+1] by slab position
   std::vector<uint2> h_in_rec;     // {source position, w}
 
-  // ---- batched engine: cached target-restricted schedule ----
-  struct Sched {  // a sweep schedule (target-restricted or full graph)
-    bool valid = false;
-    uint64_t key = 0;              // hash of the target positions
-    uint32_t n_r = 0;              // restricted nodes
-    uint64_t n_items = 0;
-    uint64_t n_edges = 0;
-    std::vector<uint32_t> lvl_item;  // level -> first work item, n_levels + 1
-    uint32_t* d_cidx = nullptr;    // [n] rank -> compact row or NONE
-    uint4* d_item = nullptr;       // {row, edge0, edge1, split flag}
-    uint2* d_erec = nullptr;       // {source row, w}
-    uint32_t* d_trow = nullptr;    // [T] target rows
-    uint64_t T = 0;
-    size_t cap_items = 0, cap_edges = 0, cap_t = 0;
-    uint32_t uses = 0;             // calls that reused this schedule
-    cudaGraphExec_t gexec = nullptr;  // captured level launches
-    uint32_t g_kp = 0, g_lb = 0, g_tpb = 0;
-    uint32_t* g_slab = nullptr;
-    cudaStream_t g_stream = nullptr;
-  } sc, full;  // sc: last target-restricted schedule; full: every node
-  uint32_t* d_slab = nullptr;      // batched distance slab [rows][Kp]
-  size_t slab_bytes = 0;
+  Ctx ctx;                         // execution context of the C-ABI calls
   uint32_t* d_io = nullptr;        // bf_matrix host-call I/O buffer
   size_t io_bytes = 0;
   uint8_t* d_iso = nullptr;        // isochrone I/O: origins, thresholds, counts, bits
   size_t iso_bytes = 0;
-  uint32_t* d_iso_tmp = nullptr;   // isochrone permutation and active-row bitmap
-  size_t iso_tmp_bytes = 0;
 };
 
 // graph.cu
@@ -128,36 +141,46 @@ __global__ void k_extract(const uint32_t* __restrict__ slab, uint32_t slab_strid
 
 // engine_batched.cu
 bf_status batched_prepare(Graph* g, uint32_t split_edges);
-bf_status build_schedule(Graph* g, Graph::Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
+bf_status build_schedule(Graph* g, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
                          cudaStream_t st);
-bf_status sweep_levels(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_blocks,
+bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                        unsigned tpb, cudaStream_t st, uint64_t* launches);
-bf_status sweep_levels_gated(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_blocks,
+bf_status sweep_levels_gated(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                              unsigned tpb, uint32_t* active, const uint32_t* thr, uint32_t kw,
                              cudaStream_t st, uint64_t* launches);
-bf_status ensure_slab(Graph* g, size_t bytes);
-bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
+bf_status ensure_slab(Graph* g, Ctx& c, size_t bytes);
+uint64_t ctx_budget(Graph* g, Ctx& c);
+void free_ctx(Ctx& c);
+bf_status init_ctx(Ctx& c);
+bf_status batched_wave(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t kw, uint32_t Kp,
+                       cudaStream_t st, uint64_t* launches, bool timed);
+bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
                          uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                          bf_stats* stats);
 
 // isochrone.cu
-bf_status isochrone_bitsets(Graph* g, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
+bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
                             uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,
                             bf_stats* stats);
 
 // seeded.cu
-bf_status matrix_seeded(Graph* g, const bf_seed* src_seeds, const uint64_t* src_off, uint64_t S,
+bf_status matrix_seeded(Graph* g, Ctx& c, const bf_seed* src_seeds, const uint64_t* src_off, uint64_t S,
                         const bf_seed* tgt_seeds, const uint64_t* tgt_off, uint64_t T,
                         uint32_t threshold, uint32_t* out, uint64_t* conflicts,
                         uint64_t conflict_cap, uint64_t* n_conflicts, bf_stats* st);
-bf_status bounded_seeded(Graph* g, const bf_seed* seeds, uint32_t n_seeds, uint32_t threshold,
+bf_status bounded_seeded(Graph* g, Ctx& c, const bf_seed* seeds, uint32_t n_seeds, uint32_t threshold,
                          uint32_t* out_rank, uint32_t* out_dist, uint64_t cap, uint64_t* n_out);
 
 // noalloc.cu
 bf_status query_batch_noalloc(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,
                               uint32_t* d_out, cudaStream_t st);
 
+// k_extract_lanes (engine_batched.cu): out[s * T + t] = slab[trow[t]][s]
+void launch_extract_lanes(const uint32_t* slab, uint32_t Kp, const uint32_t* trow, uint64_t T,
+                          uint32_t S, uint32_t threshold, uint32_t* out, cudaStream_t st);
+
 // api.cu
+Graph* graph_of(bf_graph* h);
 void set_error(const std::string& msg);
 bf_status cuda_status(cudaError_t e, const char* what);
 

@@ -64,7 +64,7 @@ bf_status ensure(T** p, size_t& cap, size_t need, Graph* g) {
 // Build (or reuse) a sweep schedule: restricted to the DOWN ancestry of the
 // targets h_tgt[0..T) (ranks, on the host), or over every node when all is
 // set (then h_tgt may be null and T is 0).
-bf_status build_schedule(Graph* g, Graph::Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
+bf_status build_schedule(Graph* g, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
                          cudaStream_t st) {
   const uint64_t key = all ? 0x9E3779B97F4A7C15ull : hash_targets(h_tgt, T);
   if (sc.valid && sc.key == key && sc.T == T) {
@@ -272,22 +272,53 @@ __global__ void __launch_bounds__(256)
 
 namespace bf {
 
-// Grow the shared distance slab to at least `need` bytes.
-bf_status ensure_slab(Graph* g, size_t need) {
-  if (need <= g->slab_bytes) return BF_OK;
-  if (g->d_slab) {
-    cudaFree(g->d_slab);
-    g->device_bytes -= g->slab_bytes;
-    g->d_slab = nullptr;
-    g->slab_bytes = 0;
+// Grow the context's distance slab to at least `need` bytes.
+bf_status ensure_slab(Graph* g, Ctx& c, size_t need) {
+  if (need <= c.slab_bytes) return BF_OK;
+  if (c.d_slab) {
+    cudaFree(c.d_slab);
+    g->device_bytes -= c.slab_bytes;
+    c.d_slab = nullptr;
+    c.slab_bytes = 0;
   }
-  if (cudaMalloc(&g->d_slab, need) != cudaSuccess) {
+  if (cudaMalloc(&c.d_slab, need) != cudaSuccess) {
     cudaGetLastError();
     set_error("cannot allocate the batched distance slab (" + std::to_string(need) + " bytes)");
     return BF_ERR_OOM;
   }
-  g->slab_bytes = need;
+  c.slab_bytes = need;
   g->device_bytes += need;
+  return BF_OK;
+}
+
+// Slab bytes available to a context: its own budget, or what the graph's
+// budget leaves (the context's current slab is reusable).
+uint64_t ctx_budget(Graph* g, Ctx& c) {
+  if (c.budget) return c.budget;
+  const uint64_t used = g->device_bytes;
+  return (g->hbm_budget > used ? g->hbm_budget - used : 0) + c.slab_bytes;
+}
+
+static void free_sched(Sched& sc) {
+  void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_trow};
+  for (void* q : p)
+    if (q) cudaFree(q);
+  if (sc.gexec) cudaGraphExecDestroy(sc.gexec);
+  sc = Sched();
+}
+
+void free_ctx(Ctx& c) {
+  free_sched(c.sc);
+  free_sched(c.full);
+  if (c.d_slab) cudaFree(c.d_slab);
+  if (c.d_iso_tmp) cudaFree(c.d_iso_tmp);
+  for (auto& e : c.ev)
+    if (e) cudaEventDestroy(e);
+  c = Ctx();
+}
+
+bf_status init_ctx(Ctx& c) {
+  for (auto& e : c.ev) BF_CUDA(cudaEventCreate(&e));
   return BF_OK;
 }
 
@@ -299,19 +330,19 @@ bf_status batched_prepare(Graph* g, uint32_t) {
 // Launch the restricted sweep's level schedule. From the second call on the
 // same schedule and slab geometry the launches are replayed from a captured
 // CUDA graph instead of being issued one by one.
-bf_status sweep_levels(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_blocks,
+bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                        unsigned tpb, cudaStream_t st, uint64_t* launches) {
   auto issue = [&](cudaStream_t s) {
     for (uint32_t l = 0; l < g->n_levels; ++l) {
       const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
       if (i1 == i0) continue;
       dim3 grid(i1 - i0, lane_blocks);
-      k_sweep_items<<<grid, tpb, 0, s>>>(sc.d_item, i0, sc.d_erec, g->d_slab, Kp);
+      k_sweep_items<<<grid, tpb, 0, s>>>(sc.d_item, i0, sc.d_erec, slab, Kp);
       ++*launches;
     }
   };
   const bool geom = sc.g_kp == Kp && sc.g_lb == lane_blocks && sc.g_tpb == tpb &&
-                    sc.g_slab == g->d_slab && sc.g_stream == st;
+                    sc.g_slab == slab && sc.g_stream == st;
   if (sc.gexec && !geom) {
     cudaGraphExecDestroy(sc.gexec);
     sc.gexec = nullptr;
@@ -327,7 +358,7 @@ bf_status sweep_levels(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_bl
         const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
         if (i1 == i0) continue;
         dim3 grid(i1 - i0, lane_blocks);
-        k_sweep_items<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, g->d_slab, Kp);
+        k_sweep_items<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, slab, Kp);
         ++dummy;
       }
       BF_CUDA(cudaStreamEndCapture(st, &graph));
@@ -337,7 +368,7 @@ bf_status sweep_levels(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_bl
       sc.g_kp = Kp;
       sc.g_lb = lane_blocks;
       sc.g_tpb = tpb;
-      sc.g_slab = g->d_slab;
+      sc.g_slab = slab;
       sc.g_stream = st;
     }
   }
@@ -354,21 +385,45 @@ bf_status sweep_levels(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_bl
 
 // Gated level schedule (launched directly: the skip decisions depend on the
 // data of each call).
-bf_status sweep_levels_gated(Graph* g, Graph::Sched& sc, uint32_t Kp, unsigned lane_blocks,
+bf_status sweep_levels_gated(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                              unsigned tpb, uint32_t* active, const uint32_t* thr, uint32_t kw,
                              cudaStream_t st, uint64_t* launches) {
   for (uint32_t l = 0; l < g->n_levels; ++l) {
     const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
     if (i1 == i0) continue;
     dim3 grid(i1 - i0, lane_blocks);
-    k_sweep_gated<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, g->d_slab, Kp, active, thr, kw);
+    k_sweep_gated<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, slab, Kp, active, thr, kw);
     ++*launches;
   }
   BF_CUDA(cudaGetLastError());
   return BF_OK;
 }
 
-bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
+void launch_extract_lanes(const uint32_t* slab, uint32_t Kp, const uint32_t* trow, uint64_t T,
+                          uint32_t S, uint32_t threshold, uint32_t* out, cudaStream_t st) {
+  dim3 eg((unsigned)((T + 31) / 32), (unsigned)((S + 31) / 32)), eb(32, 8);
+  k_extract_lanes<<<eg, eb, 0, st>>>(slab, Kp, trow, T, S, threshold, out);
+}
+
+// One wave on the context's current target-restricted schedule: reset the
+// slab, upward pass for kw sources, restricted sweep. Records c.ev[0..2]
+// around the phases when `timed`.
+bf_status batched_wave(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t kw, uint32_t Kp,
+                       cudaStream_t st, uint64_t* launches, bool timed) {
+  bf_status s;
+  Sched& sc = c.sc;
+  const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
+  const unsigned tpb = std::min<uint32_t>(128, ((Kp / 4 + 31) / 32) * 32);
+  const unsigned lane_blocks = (Kp / 4 + tpb - 1) / tpb;
+  if (timed) BF_CUDA(cudaEventRecord(c.ev[0], st));
+  BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)rows * Kp * 4, st));
+  if ((s = launch_upward(g, d_src, kw, INF, sc.d_cidx, c.d_slab, Kp, nullptr, st))) return s;
+  ++*launches;
+  if (timed) BF_CUDA(cudaEventRecord(c.ev[1], st));
+  return sweep_levels(g, sc, c.d_slab, Kp, lane_blocks, tpb, st, launches);
+}
+
+bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
                          uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                          bf_stats* stats) {
   bf_status s;
@@ -380,13 +435,11 @@ bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint
       set_error("targets[" + std::to_string(i) + "] is not a node of the graph");
       return BF_ERR_INVALID;
     }
-  if ((s = build_schedule(g, g->sc, h_tgt.data(), T, false, st))) return s;
-  const Graph::Sched& sc = g->sc;
+  if ((s = build_schedule(g, c.sc, h_tgt.data(), T, false, st))) return s;
+  Sched& sc = c.sc;
   const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
   // lanes per wave: all sources if the slab fits the budget, else waves
-  uint64_t budget = g->hbm_budget > g->device_bytes ? g->hbm_budget - g->device_bytes : 0;
-  budget += g->slab_bytes;  // the current slab is reusable
-  uint64_t max_lanes = budget / (rows * 4);
+  uint64_t max_lanes = ctx_budget(g, c) / (rows * 4);
   max_lanes = max_lanes >= 32 ? max_lanes & ~31ull : 0;
   if (max_lanes == 0) {
     set_error("HBM budget too small for one 32-lane wave of the restricted slab");
@@ -394,36 +447,28 @@ bf_status batched_matrix(Graph* g, const uint32_t* d_src, uint64_t S, const uint
   }
   const uint64_t wave = std::min<uint64_t>(max_lanes, (S + 3) & ~3ull);
   const uint32_t Kp = (uint32_t)((wave + 3) & ~3ull);
-  if ((s = ensure_slab(g, (size_t)rows * Kp * 4))) return s;
+  if ((s = ensure_slab(g, c, (size_t)rows * Kp * 4))) return s;
   uint64_t launches = 0;
   float t_up = 0, t_dn = 0, t_ex = 0;
-  const unsigned thr_per_blk = std::min<uint32_t>(128, ((Kp / 4 + 31) / 32) * 32);
-  const unsigned lane_blocks = (Kp / 4 + thr_per_blk - 1) / thr_per_blk;
   for (uint64_t s0 = 0; s0 < S; s0 += wave) {
     const uint64_t kw = std::min<uint64_t>(wave, S - s0);
-    if (stats) BF_CUDA(cudaEventRecord(g->ev[0], st));
-    BF_CUDA(cudaMemsetAsync(g->d_slab, 0xFF, (size_t)rows * Kp * 4, st));
-    if ((s = launch_upward(g, d_src + s0, kw, INF, sc.d_cidx, g->d_slab, Kp, nullptr, st)))
-      return s;
-    launches += 1;
-    if (stats) BF_CUDA(cudaEventRecord(g->ev[1], st));
-    if ((s = sweep_levels(g, g->sc, Kp, lane_blocks, thr_per_blk, st, &launches))) return s;
-    if (stats) BF_CUDA(cudaEventRecord(g->ev[2], st));
+    if ((s = batched_wave(g, c, d_src + s0, kw, Kp, st, &launches, stats != nullptr))) return s;
+    if (stats) BF_CUDA(cudaEventRecord(c.ev[2], st));
     dim3 eg((unsigned)((T + 31) / 32), (unsigned)((kw + 31) / 32)), eb(32, 8);
-    k_extract_lanes<<<eg, eb, 0, st>>>(g->d_slab, Kp, sc.d_trow, T, (uint32_t)kw, threshold,
+    k_extract_lanes<<<eg, eb, 0, st>>>(c.d_slab, Kp, sc.d_trow, T, (uint32_t)kw, threshold,
                                        d_out + s0 * T);
     BF_CUDA(cudaGetLastError());
     ++launches;
     if (stats) {
-      BF_CUDA(cudaEventRecord(g->ev[3], st));
-      BF_CUDA(cudaEventSynchronize(g->ev[3]));
-      float a, b, c;
-      BF_CUDA(cudaEventElapsedTime(&a, g->ev[0], g->ev[1]));
-      BF_CUDA(cudaEventElapsedTime(&b, g->ev[1], g->ev[2]));
-      BF_CUDA(cudaEventElapsedTime(&c, g->ev[2], g->ev[3]));
-      t_up += a;
-      t_dn += b;
-      t_ex += c;
+      BF_CUDA(cudaEventRecord(c.ev[3], st));
+      BF_CUDA(cudaEventSynchronize(c.ev[3]));
+      float ea, eb, ec;
+      BF_CUDA(cudaEventElapsedTime(&ea, c.ev[0], c.ev[1]));
+      BF_CUDA(cudaEventElapsedTime(&eb, c.ev[1], c.ev[2]));
+      BF_CUDA(cudaEventElapsedTime(&ec, c.ev[2], c.ev[3]));
+      t_up += ea;
+      t_dn += eb;
+      t_ex += ec;
     }
   }
   if (stats) {

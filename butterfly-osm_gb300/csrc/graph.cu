@@ -198,6 +198,7 @@ bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
   BF_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
   for (auto& e : g->ev) BF_CUDA(cudaEventCreate(&e));
   bf_status s;
+  if ((s = init_ctx(g->ctx))) return s;
   if ((s = dev_upload(&g->d_parent, parent.data(), n, g))) return s;
   if ((s = dev_upload(&g->d_run_end, run_end.data(), n, g))) return s;
   if ((s = dev_upload(&g->d_depth, depth.data(), n, g))) return s;
@@ -218,17 +219,15 @@ bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
 void free_graph(Graph* g) {
   if (!g) return;
   cudaSetDevice(g->device);
-  void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth,  g->d_up_off,    g->d_up_rec,
-                  g->d_pos_of,  g->d_rank_at, g->d_in_off, g->d_in_rec,    g->d_dist,
-                  g->d_seed,    g->d_flag,    g->d_err,    g->d_gpath,     g->sc.d_cidx,
-                  g->sc.d_item, g->sc.d_erec, g->sc.d_trow, g->d_slab,  g->d_io,
-                  g->full.d_cidx, g->full.d_item, g->full.d_erec, g->full.d_trow, g->d_iso,  g->d_iso_tmp};
+  void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec,
+                  g->d_pos_of,  g->d_rank_at, g->d_in_off, g->d_in_rec, g->d_dist,
+                  g->d_seed,    g->d_flag,    g->d_err,    g->d_gpath,  g->d_io,
+                  g->d_iso};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  free_ctx(g->ctx);
   for (auto& e : g->ev)
     if (e) cudaEventDestroy(e);
-  if (g->sc.gexec) cudaGraphExecDestroy(g->sc.gexec);
-  if (g->full.gexec) cudaGraphExecDestroy(g->full.gexec);
   if (g->stream) cudaStreamDestroy(g->stream);
 }
 

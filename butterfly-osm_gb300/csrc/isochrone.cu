@@ -98,12 +98,12 @@ __global__ void __launch_bounds__(256)
 // Origins are processed in (threshold, rank) order so that the lanes of a
 // wave share a threshold and lie close together in the nested-dissection
 // order, which keeps the set of active rows of the gated sweep small.
-bf_status isochrone_bitsets(Graph* g, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
+bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
                             uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,
                             bf_stats* stats) {
   bf_status s;
-  if ((s = build_schedule(g, g->full, nullptr, 0, true, st))) return s;
-  Graph::Sched& sc = g->full;
+  if ((s = build_schedule(g, c.full, nullptr, 0, true, st))) return s;
+  Sched& sc = c.full;
   const uint64_t rows = g->n;
   const uint64_t w64 = (g->n + 63) / 64;
   const uint64_t aw = (rows + 31) / 32;  // active-bitmap words
@@ -128,30 +128,28 @@ bf_status isochrone_bitsets(Graph* g, const uint32_t* d_orig, const uint32_t* d_
     pk[2 * n + i] = perm[i];
   }
   const size_t need = pk.size() * 4 + aw * 4;
-  if (need > g->iso_tmp_bytes) {
-    if (g->d_iso_tmp) {
-      cudaFree(g->d_iso_tmp);
-      g->device_bytes -= g->iso_tmp_bytes;
-      g->d_iso_tmp = nullptr;
-      g->iso_tmp_bytes = 0;
+  if (need > c.iso_tmp_bytes) {
+    if (c.d_iso_tmp) {
+      cudaFree(c.d_iso_tmp);
+      g->device_bytes -= c.iso_tmp_bytes;
+      c.d_iso_tmp = nullptr;
+      c.iso_tmp_bytes = 0;
     }
-    if (cudaMalloc(&g->d_iso_tmp, need) != cudaSuccess) {
+    if (cudaMalloc(&c.d_iso_tmp, need) != cudaSuccess) {
       cudaGetLastError();
       set_error("cudaMalloc for isochrone scratch failed");
       return BF_ERR_OOM;
     }
-    g->iso_tmp_bytes = need;
+    c.iso_tmp_bytes = need;
     g->device_bytes += need;
   }
-  uint32_t* p_orig = g->d_iso_tmp;
+  uint32_t* p_orig = c.d_iso_tmp;
   uint32_t* p_thr = p_orig + n;
   uint32_t* p_row = p_thr + n;
   uint32_t* d_active = p_row + n;
   BF_CUDA(cudaMemcpyAsync(p_orig, pk.data(), pk.size() * 4, cudaMemcpyHostToDevice, st));
   // the slab is the only per-lane device memory here
-  uint64_t budget = g->hbm_budget > g->device_bytes ? g->hbm_budget - g->device_bytes : 0;
-  budget += g->slab_bytes;
-  uint64_t max_lanes = budget / (rows * 4);
+  uint64_t max_lanes = ctx_budget(g, c) / (rows * 4);
   max_lanes = max_lanes >= 32 ? max_lanes & ~31ull : 0;
   if (!max_lanes) {
     set_error("HBM budget too small for one 32-lane isochrone wave");
@@ -159,7 +157,7 @@ bf_status isochrone_bitsets(Graph* g, const uint32_t* d_orig, const uint32_t* d_
   }
   const uint64_t wave = std::min<uint64_t>(max_lanes, (n + 3) & ~3ull);
   const uint32_t Kp = (uint32_t)((wave + 3) & ~3ull);
-  if ((s = ensure_slab(g, (size_t)rows * Kp * 4))) return s;
+  if ((s = ensure_slab(g, c, (size_t)rows * Kp * 4))) return s;
   BF_CUDA(cudaMemsetAsync(d_counts, 0, n * 8, st));
   const unsigned tpb = std::min<uint32_t>(128, ((Kp / 4 + 31) / 32) * 32);
   const unsigned lane_blocks = (Kp / 4 + tpb - 1) / tpb;
@@ -167,36 +165,36 @@ bf_status isochrone_bitsets(Graph* g, const uint32_t* d_orig, const uint32_t* d_
   float t_up = 0, t_dn = 0, t_ex = 0;
   for (uint64_t s0 = 0; s0 < n; s0 += wave) {
     const uint64_t kw = std::min<uint64_t>(wave, n - s0);
-    if (stats) BF_CUDA(cudaEventRecord(g->ev[0], st));
-    BF_CUDA(cudaMemsetAsync(g->d_slab, 0xFF, (size_t)rows * Kp * 4, st));
+    if (stats) BF_CUDA(cudaEventRecord(c.ev[0], st));
+    BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)rows * Kp * 4, st));
     BF_CUDA(cudaMemsetAsync(d_active, 0, aw * 4, st));
-    if ((s = launch_upward(g, p_orig + s0, kw, INF, sc.d_cidx, g->d_slab, Kp, d_active, st,
+    if ((s = launch_upward(g, p_orig + s0, kw, INF, sc.d_cidx, c.d_slab, Kp, d_active, st,
                            p_thr + s0)))
       return s;
     ++launches;
-    if (stats) BF_CUDA(cudaEventRecord(g->ev[1], st));
-    if ((s = sweep_levels_gated(g, sc, Kp, lane_blocks, tpb, d_active, p_thr + s0,
+    if (stats) BF_CUDA(cudaEventRecord(c.ev[1], st));
+    if ((s = sweep_levels_gated(g, sc, c.d_slab, Kp, lane_blocks, tpb, d_active, p_thr + s0,
                                 (uint32_t)kw, st, &launches)))
       return s;
-    if (stats) BF_CUDA(cudaEventRecord(g->ev[2], st));
+    if (stats) BF_CUDA(cudaEventRecord(c.ev[2], st));
     dim3 bgrid((unsigned)((g->n + TILE_R - 1) / TILE_R),
                (unsigned)((kw + TILE_L * LANE_TILES_PER_BLOCK - 1) / (TILE_L * LANE_TILES_PER_BLOCK)));
-    k_bits<<<bgrid, 256, 0, st>>>(g->d_slab, Kp, sc.d_cidx, g->n, p_thr + s0, (uint32_t)kw,
+    k_bits<<<bgrid, 256, 0, st>>>(c.d_slab, Kp, sc.d_cidx, g->n, p_thr + s0, (uint32_t)kw,
                                  reinterpret_cast<uint32_t*>(d_bits), 2 * w64,
                                  reinterpret_cast<unsigned long long*>(d_counts), d_active,
                                  p_row + s0);
     BF_CUDA(cudaGetLastError());
     ++launches;
     if (stats) {
-      BF_CUDA(cudaEventRecord(g->ev[3], st));
-      BF_CUDA(cudaEventSynchronize(g->ev[3]));
-      float a, b, c;
-      BF_CUDA(cudaEventElapsedTime(&a, g->ev[0], g->ev[1]));
-      BF_CUDA(cudaEventElapsedTime(&b, g->ev[1], g->ev[2]));
-      BF_CUDA(cudaEventElapsedTime(&c, g->ev[2], g->ev[3]));
-      t_up += a;
-      t_dn += b;
-      t_ex += c;
+      BF_CUDA(cudaEventRecord(c.ev[3], st));
+      BF_CUDA(cudaEventSynchronize(c.ev[3]));
+      float ea, eb, ec;
+      BF_CUDA(cudaEventElapsedTime(&ea, c.ev[0], c.ev[1]));
+      BF_CUDA(cudaEventElapsedTime(&eb, c.ev[1], c.ev[2]));
+      BF_CUDA(cudaEventElapsedTime(&ec, c.ev[2], c.ev[3]));
+      t_up += ea;
+      t_dn += eb;
+      t_ex += ec;
     }
   }
   BF_CUDA(cudaStreamSynchronize(st));  // pk / perm host vectors die on return

@@ -131,7 +131,7 @@ struct Dev {
 
 }  // namespace
 
-bf_status matrix_seeded(Graph* g, const bf_seed* src_seeds, const uint64_t* src_off, uint64_t S,
+bf_status matrix_seeded(Graph* g, Ctx& c, const bf_seed* src_seeds, const uint64_t* src_off, uint64_t S,
                         const bf_seed* tgt_seeds, const uint64_t* tgt_off, uint64_t T,
                         uint32_t threshold, uint32_t* out, uint64_t* conflicts,
                         uint64_t conflict_cap, uint64_t* n_conflicts, bf_stats* st) {
@@ -143,12 +143,10 @@ bf_status matrix_seeded(Graph* g, const bf_seed* src_seeds, const uint64_t* src_
   for (uint64_t k = 0; k < nt; ++k) tr[k] = tgt_seeds[k].rank;
   std::sort(tr.begin(), tr.end());
   tr.erase(std::unique(tr.begin(), tr.end()), tr.end());
-  if ((rc = build_schedule(g, g->sc, tr.data(), tr.size(), false, s))) return rc;
-  Graph::Sched& sc = g->sc;
+  if ((rc = build_schedule(g, c.sc, tr.data(), tr.size(), false, s))) return rc;
+  Sched& sc = c.sc;
   const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
-  uint64_t budget = g->hbm_budget > g->device_bytes ? g->hbm_budget - g->device_bytes : 0;
-  budget += g->slab_bytes;
-  uint64_t max_lanes = budget / (rows * 4 + (uint64_t)T * 4 * 2);
+  uint64_t max_lanes = ctx_budget(g, c) / (rows * 4 + (uint64_t)T * 4 * 2);
   max_lanes = max_lanes >= 32 ? max_lanes & ~31ull : 0;
   if (!max_lanes) {
     set_error("HBM budget too small for a 32-lane seeded wave");
@@ -156,7 +154,7 @@ bf_status matrix_seeded(Graph* g, const bf_seed* src_seeds, const uint64_t* src_
   }
   const uint64_t wave = std::min<uint64_t>(max_lanes, (S + 3) & ~3ull);
   const uint32_t Kp = (uint32_t)((wave + 3) & ~3ull);
-  if ((rc = ensure_slab(g, (size_t)rows * Kp * 4))) return rc;
+  if ((rc = ensure_slab(g, c, (size_t)rows * Kp * 4))) return rc;
   // device copies: target seeds {rank, part}, target offsets, units, output
   Dev d_ts, d_to, d_units, d_out;
   if (!d_ts.alloc(nt * 8) || !d_to.alloc((T + 1) * 8) || !d_units.alloc(ns * 12) ||
@@ -181,16 +179,16 @@ bf_status matrix_seeded(Graph* g, const bf_seed* src_seeds, const uint64_t* src_
       }
     uint32_t* du = d_units.as<uint32_t>();
     if (nu) BF_CUDA(cudaMemcpyAsync(du, units.data(), units.size() * 4, cudaMemcpyHostToDevice, s));
-    BF_CUDA(cudaMemsetAsync(g->d_slab, 0xFF, (size_t)rows * Kp * 4, s));
+    BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)rows * Kp * 4, s));
     if (nu) {
-      if ((rc = launch_upward(g, du, nu, INF, sc.d_cidx, g->d_slab, Kp, nullptr, s, nullptr,
+      if ((rc = launch_upward(g, du, nu, INF, sc.d_cidx, c.d_slab, Kp, nullptr, s, nullptr,
                               du + nu, du + 2 * nu)))
         return rc;
       ++launches;
     }
-    if ((rc = sweep_levels(g, sc, Kp, lane_blocks, tpb, s, &launches))) return rc;
+    if ((rc = sweep_levels(g, sc, c.d_slab, Kp, lane_blocks, tpb, s, &launches))) return rc;
     dim3 eg((unsigned)((T + 31) / 32), (unsigned)((kw + 31) / 32)), eb(32, 8);
-    k_seeded_extract<<<eg, eb, 0, s>>>(g->d_slab, Kp, sc.d_cidx, d_to.as<uint64_t>(),
+    k_seeded_extract<<<eg, eb, 0, s>>>(c.d_slab, Kp, sc.d_cidx, d_to.as<uint64_t>(),
                                        d_ts.as<uint2>(), T, (uint32_t)kw, threshold,
                                        d_out.as<uint32_t>());
     BF_CUDA(cudaGetLastError());
@@ -227,15 +225,15 @@ bf_status matrix_seeded(Graph* g, const bf_seed* src_seeds, const uint64_t* src_
   return BF_OK;
 }
 
-bf_status bounded_seeded(Graph* g, const bf_seed* seeds, uint32_t n_seeds, uint32_t threshold,
+bf_status bounded_seeded(Graph* g, Ctx& c, const bf_seed* seeds, uint32_t n_seeds, uint32_t threshold,
                          uint32_t* out_rank, uint32_t* out_dist, uint64_t cap, uint64_t* n_out) {
   cudaStream_t s = g->stream;
   bf_status rc;
-  if ((rc = build_schedule(g, g->full, nullptr, 0, true, s))) return rc;
-  Graph::Sched& sc = g->full;
+  if ((rc = build_schedule(g, c.full, nullptr, 0, true, s))) return rc;
+  Sched& sc = c.full;
   const uint32_t Kp = 4, n = g->n;
   const uint64_t aw = (n + 31) / 32, nb = (n + 1023) / 1024;
-  if ((rc = ensure_slab(g, (size_t)n * Kp * 4))) return rc;
+  if ((rc = ensure_slab(g, c, (size_t)n * Kp * 4))) return rc;
   Dev d_u, d_act, d_cnt, d_off, d_res;
   if (!d_u.alloc((size_t)n_seeds * 12 + 16) || !d_act.alloc(aw * 4) || !d_cnt.alloc(nb * 4) ||
       !d_off.alloc(nb * 8))
@@ -250,16 +248,16 @@ bf_status bounded_seeded(Graph* g, const bf_seed* seeds, uint32_t n_seeds, uint3
   uint32_t* du = d_u.as<uint32_t>();
   BF_CUDA(cudaMemcpyAsync(du, units.data(), units.size() * 4, cudaMemcpyHostToDevice, s));
   const uint32_t* d_thr = du + 3 * (size_t)n_seeds;
-  BF_CUDA(cudaMemsetAsync(g->d_slab, 0xFF, (size_t)n * Kp * 4, s));
+  BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)n * Kp * 4, s));
   BF_CUDA(cudaMemsetAsync(d_act.p, 0, aw * 4, s));
   uint64_t launches = 0;
   if (n_seeds &&
-      (rc = launch_upward(g, du, n_seeds, threshold, sc.d_cidx, g->d_slab, Kp,
+      (rc = launch_upward(g, du, n_seeds, threshold, sc.d_cidx, c.d_slab, Kp,
                           d_act.as<uint32_t>(), s, d_thr, du + n_seeds, du + 2 * (size_t)n_seeds)))
     return rc;
-  if ((rc = sweep_levels_gated(g, sc, Kp, 1, 32, d_act.as<uint32_t>(), d_thr, 1, s, &launches)))
+  if ((rc = sweep_levels_gated(g, sc, c.d_slab, Kp, 1, 32, d_act.as<uint32_t>(), d_thr, 1, s, &launches)))
     return rc;
-  k_rank_count<<<(unsigned)nb, 1024, 0, s>>>(g->d_slab, Kp, sc.d_cidx, d_act.as<uint32_t>(), n,
+  k_rank_count<<<(unsigned)nb, 1024, 0, s>>>(c.d_slab, Kp, sc.d_cidx, d_act.as<uint32_t>(), n,
                                             threshold, d_cnt.as<uint32_t>());
   BF_CUDA(cudaGetLastError());
   std::vector<uint32_t> cnt(nb);
@@ -275,7 +273,7 @@ bf_status bounded_seeded(Graph* g, const bf_seed* seeds, uint32_t n_seeds, uint3
   const uint64_t keep = std::min<uint64_t>(tot, cap);
   if (!d_res.alloc(keep * 8 + 16)) return BF_ERR_OOM;
   BF_CUDA(cudaMemcpyAsync(d_off.p, off.data(), nb * 8, cudaMemcpyHostToDevice, s));
-  k_rank_scatter<<<(unsigned)nb, 1024, 0, s>>>(g->d_slab, Kp, sc.d_cidx, d_act.as<uint32_t>(), n,
+  k_rank_scatter<<<(unsigned)nb, 1024, 0, s>>>(c.d_slab, Kp, sc.d_cidx, d_act.as<uint32_t>(), n,
                                               threshold, d_off.as<uint64_t>(), keep,
                                               d_res.as<uint32_t>(), d_res.as<uint32_t>() + keep);
   BF_CUDA(cudaGetLastError());
