@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--cols", type=int, default=2500)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-s", type=float, default=15.0,
+                    help="seconds of Poisson arrivals for the serving run (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=100.0, help="arrivals per second")
     return ap.parse_args()
 
 
@@ -132,7 +135,8 @@ def cpu_sample(cch, src, tgt, budget_s, rows=None):
     c = orc.Cch.from_dict(cch)
     threads = os.cpu_count() or 1
     if rows is None:
-        rows = max(8, min(len(src), (len(src) // 100) or 8))  # a 1% row sample
+        # at least a 1% row sample; ~10 K=8 batches per host thread
+        rows = max(8, min(len(src), max(len(src) // 100, 80 * threads)))
     pick = np.linspace(0, len(src) - 1, rows).astype(np.int64)
     t0 = time.perf_counter()
     m, used = c.matrix(src[pick], tgt, threads=threads)
@@ -253,7 +257,67 @@ def run_ours(args, rank, world, dist):
                          "downward": round(st["downward_ms"], 3),
                          "extract": round(st["extract_ms"], 3)},
            "clocks": clk.summary()}
+    if args.serve_s > 0 and rank == 0:
+        res["serving"] = run_serving(g, cch["n"], args.serve_s, args.serve_rate)
     return res, cch, src, tgt, out_dev
+
+
+def run_serving(g, n, seconds, rate, seed=7):
+    """Serving mix on the same graph: Poisson arrivals at `rate` req/s for
+    `seconds`; 70% matrices with S and T log-uniform in [10, 5000], 30%
+    isochrones with a threshold uniform in [300, 3600] s. Latency is
+    completion minus submission (server clock)."""
+    import numpy as np
+    import bfphast
+    rng = np.random.default_rng(seed)
+    count = int(rng.poisson(rate * seconds))
+    arrivals = np.sort(rng.uniform(0, seconds, count))
+    specs = []
+    for _ in range(count):
+        if rng.random() < 0.7:
+            S = int(np.exp(rng.uniform(np.log(10), np.log(5000))))
+            T = int(np.exp(rng.uniform(np.log(10), np.log(5000))))
+            specs.append(("m", rng.integers(0, n, S).astype(np.uint32),
+                          rng.integers(0, n, T).astype(np.uint32)))
+        else:
+            specs.append(("i", int(rng.integers(0, n)), int(rng.integers(3000, 36001))))
+    srv = bfphast.Server(g, hbm_budget=60 << 30, max_inflight=64)
+    kinds, done = {}, {}
+    t0 = time.perf_counter()
+    for i, (at, sp) in enumerate(zip(arrivals, specs)):
+        wait = t0 + at - time.perf_counter()
+        if wait > 0:
+            time.sleep(wait)
+        if sp[0] == "m":
+            t, _ = srv.submit_matrix(sp[1], sp[2], tag=i)
+            kinds[t] = ("m", len(sp[1]) * len(sp[2]))
+        else:
+            t, _ = srv.submit_isochrone(sp[1], sp[2], tag=i)
+            kinds[t] = ("i", 0)
+        for c in srv.poll(wait_ms=0):
+            done[c["ticket"]] = c
+    while len(done) < len(kinds) and time.perf_counter() - t0 < seconds + 120:
+        for c in srv.poll(wait_ms=100):
+            done[c["ticket"]] = c
+    elapsed = time.perf_counter() - t0
+    srv.close()
+    lat = {k: [] for k in ("m", "i")}
+    cells = ok = 0
+    for t, c in done.items():
+        if c["status"] == 0:
+            ok += 1
+            kd, cl = kinds[t]
+            lat[kd].append((c["done_s"] - c["submit_s"]) * 1e3)
+            cells += cl
+    alll = lat["m"] + lat["i"]
+    pct = lambda v, q: round(float(np.percentile(v, q)), 2) if v else None
+    return {"requests": count, "completed_ok": ok, "seconds": seconds, "rate_req_s": rate,
+            "p50_ms": pct(alll, 50), "p99_ms": pct(alll, 99),
+            "matrix_p50_ms": pct(lat["m"], 50), "matrix_p99_ms": pct(lat["m"], 99),
+            "isochrone_p50_ms": pct(lat["i"], 50), "isochrone_p99_ms": pct(lat["i"], 99),
+            "cells_per_s": round(cells / elapsed, 1),
+            "isochrones_per_s": round(len(lat["i"]) / elapsed, 1),
+            "mix": "70% matrices S,T log-uniform[10,5000]; 30% isochrones T U[300,3600] s"}
 
 
 def run_reference(args):

@@ -55,6 +55,8 @@ struct Sched {
   uint32_t g_kp = 0, g_lb = 0, g_tpb = 0;
   uint32_t* g_slab = nullptr;
   cudaStream_t g_stream = nullptr;
+  std::vector<uint32_t> ranks;   // ranks whose d_cidx entry is set (reset on rebuild)
+  bool cidx_ready = false;       // d_cidx holds NONE outside `ranks`
 };
 
 // Execution context of the batched engine: schedules, the distance slab and
@@ -69,6 +71,10 @@ struct Ctx {
   size_t iso_tmp_bytes = 0;
   cudaEvent_t ev[4] = {};
   uint64_t budget = 0;             // slab bytes this context may use (0 = graph budget)
+  std::vector<uint8_t> mark;       // host scratch [n], all 0 between builds
+  std::vector<uint32_t> rowmap;    // host scratch [n], all NONE between builds
+  uint32_t* d_pairs = nullptr;     // device scratch for (rank, row) updates
+  size_t cap_pairs = 0;
 };
 
 struct Graph {
@@ -87,6 +93,7 @@ struct Graph {
   // host tables
   std::vector<uint32_t> pos_of;     // rank -> slab position (plain engine)
   std::vector<uint32_t> lvl_start;  // level -> first position, n_levels + 1
+  std::vector<uint32_t> rank_at;    // slab position -> rank
 
   // device: elimination tree / upward
   uint32_t* d_parent = nullptr;   // [n] etree parent rank (NONE at roots)
@@ -141,7 +148,7 @@ __global__ void k_extract(const uint32_t* __restrict__ slab, uint32_t slab_strid
 
 // engine_batched.cu
 bf_status batched_prepare(Graph* g, uint32_t split_edges);
-bf_status build_schedule(Graph* g, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
+bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
                          cudaStream_t st);
 bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                        unsigned tpb, cudaStream_t st, uint64_t* launches);

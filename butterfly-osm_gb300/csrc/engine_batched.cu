@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <queue>
 
 #include "engine.cuh"
 
@@ -61,10 +62,21 @@ bf_status ensure(T** p, size_t& cap, size_t need, Graph* g) {
 
 }  // namespace
 
+__global__ void k_scatter_pairs(const uint2* __restrict__ pr, uint64_t m,
+                                uint32_t* __restrict__ out) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) out[pr[i].x] = pr[i].y;
+}
+
 // Build (or reuse) a sweep schedule: restricted to the DOWN ancestry of the
 // targets h_tgt[0..T) (ranks, on the host), or over every node when all is
-// set (then h_tgt may be null and T is 0).
-bf_status build_schedule(Graph* g, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
+// set (then h_tgt may be null and T is 0). The restricted set is collected by
+// walking in-edges from the targets in descending slab position (a max-heap:
+// in-edge sources always have lower positions), so the cost is proportional
+// to the restricted nodes and edges, not to the graph. The device rank->row
+// map is patched in place: entries of the previous schedule are reset to
+// NONE and the new ones set.
+bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
                          cudaStream_t st) {
   const uint64_t key = all ? 0x9E3779B97F4A7C15ull : hash_targets(h_tgt, T);
   if (sc.valid && sc.key == key && sc.T == T) {
@@ -78,54 +90,98 @@ bf_status build_schedule(Graph* g, Sched& sc, const uint32_t* h_tgt, uint64_t T,
     sc.gexec = nullptr;
   }
   const uint32_t n = g->n;
-  std::vector<uint8_t> mark(n, all ? 1 : 0);
-  for (uint64_t i = 0; i < T; ++i) mark[g->pos_of[h_tgt[i]]] = 1;
-  uint64_t m_r = 0;
-  for (uint32_t p = n; p-- > 0;) {
-    if (!mark[p]) continue;
-    for (uint64_t k = g->h_in_off[p]; k < g->h_in_off[p + 1]; ++k) mark[g->h_in_rec[k].x] = 1;
-    m_r += g->h_in_off[p + 1] - g->h_in_off[p];
+  if (c.mark.size() != n) {
+    c.mark.assign(n, 0);
+    c.rowmap.assign(n, NONE);
   }
-  // compact rows in position order (level order is preserved)
-  std::vector<uint32_t> row_of(n, NONE);
-  uint32_t n_r = 0;
-  for (uint32_t p = 0; p < n; ++p)
-    if (mark[p]) row_of[p] = n_r++;
-  std::vector<uint32_t> cidx(n);
-  for (uint32_t r = 0; r < n; ++r) cidx[r] = row_of[g->pos_of[r]];
+  std::vector<uint32_t> R;  // restricted positions, ascending
+  if (all) {
+    R.resize(n);
+    for (uint32_t p = 0; p < n; ++p) R[p] = p;
+  } else {
+    std::priority_queue<uint32_t> pq;
+    for (uint64_t i = 0; i < T; ++i) {
+      const uint32_t p = g->pos_of[h_tgt[i]];
+      if (!c.mark[p]) {
+        c.mark[p] = 1;
+        pq.push(p);
+      }
+    }
+    while (!pq.empty()) {
+      const uint32_t p = pq.top();
+      pq.pop();
+      R.push_back(p);
+      for (uint64_t k = g->h_in_off[p]; k < g->h_in_off[p + 1]; ++k) {
+        const uint32_t u = g->h_in_rec[k].x;
+        if (!c.mark[u]) {
+          c.mark[u] = 1;
+          pq.push(u);
+        }
+      }
+    }
+    std::reverse(R.begin(), R.end());
+    for (uint32_t p : R) c.mark[p] = 0;
+  }
+  const uint32_t n_r = (uint32_t)R.size();
+  for (uint32_t i = 0; i < n_r; ++i) c.rowmap[R[i]] = i;
   std::vector<uint4> items;
   std::vector<uint2> erec;
-  erec.reserve(m_r);
   sc.lvl_item.assign(g->n_levels + 1, 0);
-  for (uint32_t l = 0; l < g->n_levels; ++l) {
-    sc.lvl_item[l] = (uint32_t)items.size();
-    for (uint32_t p = g->lvl_start[l]; p < g->lvl_start[l + 1]; ++p) {
-      if (!mark[p]) continue;
-      uint64_t k0 = g->h_in_off[p], k1 = g->h_in_off[p + 1];
-      if (k0 == k1) continue;  // no in-edges: the row is its seed
-      uint32_t e0 = (uint32_t)erec.size();
-      for (uint64_t k = k0; k < k1; ++k)
-        erec.push_back(make_uint2(row_of[g->h_in_rec[k].x], g->h_in_rec[k].y));
-      uint32_t deg = (uint32_t)(k1 - k0);
-      uint32_t split = deg > SPLIT ? 1u : 0u;
-      for (uint32_t a = 0; a < deg; a += SPLIT)
-        items.push_back(make_uint4(row_of[p], e0 + a, e0 + std::min(deg, a + SPLIT), split));
-    }
+  uint32_t lvl = 0;
+  for (uint32_t i = 0; i < n_r; ++i) {
+    const uint32_t p = R[i];
+    while (p >= g->lvl_start[lvl + 1]) sc.lvl_item[++lvl] = (uint32_t)items.size();
+    const uint64_t k0 = g->h_in_off[p], k1 = g->h_in_off[p + 1];
+    if (k0 == k1) continue;  // no in-edges: the row is its seed
+    const uint32_t e0 = (uint32_t)erec.size();
+    for (uint64_t k = k0; k < k1; ++k)
+      erec.push_back(make_uint2(c.rowmap[g->h_in_rec[k].x], g->h_in_rec[k].y));
+    const uint32_t deg = (uint32_t)(k1 - k0);
+    const uint32_t split = deg > SPLIT ? 1u : 0u;
+    for (uint32_t a = 0; a < deg; a += SPLIT)
+      items.push_back(make_uint4(i, e0 + a, e0 + std::min(deg, a + SPLIT), split));
   }
-  sc.lvl_item[g->n_levels] = (uint32_t)items.size();
+  while (lvl < g->n_levels) sc.lvl_item[++lvl] = (uint32_t)items.size();
   if (erec.size() > 0xFFFFFFFFull) {
+    for (uint32_t p : R) c.rowmap[p] = NONE;
     set_error("restricted edge set exceeds 2^32 edges");
     return BF_ERR_UNSUPPORTED;
   }
+  std::vector<uint32_t> trow(T);
+  for (uint64_t i = 0; i < T; ++i) trow[i] = c.rowmap[g->pos_of[h_tgt[i]]];
+  // device rank -> row map: reset the previous schedule's entries, set ours
+  std::vector<uint2> pairs;
+  pairs.reserve(sc.ranks.size() + n_r);
+  for (uint32_t r : sc.ranks) pairs.push_back(make_uint2(r, NONE));
+  const size_t n_reset = pairs.size();
+  std::vector<uint32_t> ranks(n_r);
+  for (uint32_t i = 0; i < n_r; ++i) {
+    ranks[i] = g->rank_at[R[i]];
+    pairs.push_back(make_uint2(ranks[i], i));
+  }
+  for (uint32_t p : R) c.rowmap[p] = NONE;
   bf_status s;
   size_t cap_c = sc.d_cidx ? n : 0;
   if ((s = ensure(&sc.d_cidx, cap_c, n, g))) return s;
   if ((s = ensure(&sc.d_item, sc.cap_items, items.size(), g))) return s;
   if ((s = ensure(&sc.d_erec, sc.cap_edges, erec.size(), g))) return s;
   if ((s = ensure(&sc.d_trow, sc.cap_t, T, g))) return s;
-  std::vector<uint32_t> trow(T);
-  for (uint64_t i = 0; i < T; ++i) trow[i] = row_of[g->pos_of[h_tgt[i]]];
-  BF_CUDA(cudaMemcpyAsync(sc.d_cidx, cidx.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
+  if ((s = ensure(&c.d_pairs, c.cap_pairs, pairs.size() * 2, g))) return s;
+  if (!sc.cidx_ready) {
+    BF_CUDA(cudaMemsetAsync(sc.d_cidx, 0xFF, (size_t)n * 4, st));
+    sc.cidx_ready = true;
+  }
+  if (!pairs.empty()) {
+    BF_CUDA(cudaMemcpyAsync(c.d_pairs, pairs.data(), pairs.size() * sizeof(uint2),
+                            cudaMemcpyHostToDevice, st));
+    const uint2* dp = reinterpret_cast<const uint2*>(c.d_pairs);
+    if (n_reset)
+      k_scatter_pairs<<<(unsigned)((n_reset + 255) / 256), 256, 0, st>>>(dp, n_reset, sc.d_cidx);
+    if (n_r)
+      k_scatter_pairs<<<(unsigned)((n_r + 255) / 256), 256, 0, st>>>(dp + n_reset, n_r,
+                                                                      sc.d_cidx);
+    BF_CUDA(cudaGetLastError());
+  }
   if (!items.empty())
     BF_CUDA(cudaMemcpyAsync(sc.d_item, items.data(), items.size() * sizeof(uint4),
                             cudaMemcpyHostToDevice, st));
@@ -134,6 +190,7 @@ bf_status build_schedule(Graph* g, Sched& sc, const uint32_t* h_tgt, uint64_t T,
                             cudaMemcpyHostToDevice, st));
   if (T) BF_CUDA(cudaMemcpyAsync(sc.d_trow, trow.data(), T * 4, cudaMemcpyHostToDevice, st));
   BF_CUDA(cudaStreamSynchronize(st));  // host vectors are freed on return
+  sc.ranks.swap(ranks);
   sc.n_r = n_r;
   sc.n_items = items.size();
   sc.n_edges = erec.size();
@@ -310,6 +367,7 @@ static void free_sched(Sched& sc) {
 void free_ctx(Ctx& c) {
   free_sched(c.sc);
   free_sched(c.full);
+  if (c.d_pairs) cudaFree(c.d_pairs);
   if (c.d_slab) cudaFree(c.d_slab);
   if (c.d_iso_tmp) cudaFree(c.d_iso_tmp);
   for (auto& e : c.ev)
@@ -435,7 +493,7 @@ bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, co
       set_error("targets[" + std::to_string(i) + "] is not a node of the graph");
       return BF_ERR_INVALID;
     }
-  if ((s = build_schedule(g, c.sc, h_tgt.data(), T, false, st))) return s;
+  if ((s = build_schedule(g, c, c.sc, h_tgt.data(), T, false, st))) return s;
   Sched& sc = c.sc;
   const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
   // lanes per wave: all sources if the slab fits the budget, else waves

@@ -210,6 +210,7 @@ bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
   if ((s = dev_upload(&g->d_in_rec, in_rec.data(), in_rec.size(), g))) return s;
   uint32_t zero = 0;
   if ((s = dev_upload(&g->d_err, &zero, 1, g))) return s;
+  g->rank_at = std::move(rank_at);
   g->h_in_off = std::move(in_off);
   g->h_in_rec = std::move(in_rec);
   (void)cfg;

@@ -102,7 +102,7 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
                             uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,
                             bf_stats* stats) {
   bf_status s;
-  if ((s = build_schedule(g, c.full, nullptr, 0, true, st))) return s;
+  if ((s = build_schedule(g, c, c.full, nullptr, 0, true, st))) return s;
   Sched& sc = c.full;
   const uint64_t rows = g->n;
   const uint64_t w64 = (g->n + 63) / 64;

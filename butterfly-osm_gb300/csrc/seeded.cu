@@ -143,7 +143,7 @@ bf_status matrix_seeded(Graph* g, Ctx& c, const bf_seed* src_seeds, const uint64
   for (uint64_t k = 0; k < nt; ++k) tr[k] = tgt_seeds[k].rank;
   std::sort(tr.begin(), tr.end());
   tr.erase(std::unique(tr.begin(), tr.end()), tr.end());
-  if ((rc = build_schedule(g, c.sc, tr.data(), tr.size(), false, s))) return rc;
+  if ((rc = build_schedule(g, c, c.sc, tr.data(), tr.size(), false, s))) return rc;
   Sched& sc = c.sc;
   const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
   uint64_t max_lanes = ctx_budget(g, c) / (rows * 4 + (uint64_t)T * 4 * 2);
@@ -229,7 +229,7 @@ bf_status bounded_seeded(Graph* g, Ctx& c, const bf_seed* seeds, uint32_t n_seed
                          uint32_t* out_rank, uint32_t* out_dist, uint64_t cap, uint64_t* n_out) {
   cudaStream_t s = g->stream;
   bf_status rc;
-  if ((rc = build_schedule(g, c.full, nullptr, 0, true, s))) return rc;
+  if ((rc = build_schedule(g, c, c.full, nullptr, 0, true, s))) return rc;
   Sched& sc = c.full;
   const uint32_t Kp = 4, n = g->n;
   const uint64_t aw = (n + 31) / 32, nb = (n + 1023) / 1024;

@@ -164,7 +164,7 @@ bf_status run_matrix_batch(Server* sv, Slot& sl, std::vector<Job*>& jobs) {
   uint32_t* d_out = d_trow + TT;
   BF_CUDA(cudaMemcpyAsync(d_src, hs.data(), L * 4, cudaMemcpyHostToDevice, st));
   BF_CUDA(cudaMemcpyAsync(d_tgt, ht.data(), TT * 4, cudaMemcpyHostToDevice, st));
-  if ((s = build_schedule(g, c.sc, uni.data(), uni.size(), false, st))) return s;
+  if ((s = build_schedule(g, c, c.sc, uni.data(), uni.size(), false, st))) return s;
   if (TT) k_gather<<<(unsigned)((TT + 255) / 256), 256, 0, st>>>(c.sc.d_cidx, d_tgt, TT, d_trow);
   BF_CUDA(cudaGetLastError());
   if (L == 0) return wait_slot(sl, sv->cfg.timeout_ms);
