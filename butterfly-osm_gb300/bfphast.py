@@ -62,6 +62,16 @@ class Stats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class Tune(ctypes.Structure):
+    _fields_ = [("threads_per_block", ctypes.c_uint32), ("edges_per_item", ctypes.c_uint32),
+                ("graph_capture", ctypes.c_uint32), ("lanes_per_wave", ctypes.c_uint32),
+                ("step_ms", ctypes.c_double), ("tried", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 class Seed(ctypes.Structure):
     _fields_ = [("rank", ctypes.c_uint32), ("cost", ctypes.c_uint32)]
 
@@ -93,6 +103,11 @@ _SIGNATURES = {
     "bf_graph_destroy": (None, [ctypes.c_void_p]),
     "bf_graph_info_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(GraphInfo)]),
     "bf_graph_set_engine": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
+    "bf_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                   ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                   ctypes.POINTER(Tune)]),
+    "bf_set_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tune)]),
+    "bf_get_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tune)]),
     "bf_query_batch": (ctypes.c_int, [ctypes.c_void_p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
                                       _u32p]),
     "bf_phast_query": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _u32p]),
@@ -209,6 +224,23 @@ class Graph:
 
     def set_engine(self, engine, k_lanes=0):
         _check(load().bf_graph_set_engine(self._h, engine, k_lanes))
+
+    def autotune(self, d_src, S, d_tgt, T, reps=2):
+        """Time candidate tunables on a device-resident sample; keeps the best."""
+        t = Tune()
+        _check(load().bf_autotune(self._h, ctypes.c_void_p(d_src), S, ctypes.c_void_p(d_tgt), T,
+                                  reps, ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tune(self, threads_per_block=128, edges_per_item=16, graph_capture=1,
+                 lanes_per_wave=0):
+        t = Tune(threads_per_block, edges_per_item, graph_capture, lanes_per_wave, 0.0, 0, 0)
+        _check(load().bf_set_tune(self._h, ctypes.byref(t)))
+
+    def get_tune(self):
+        t = Tune()
+        _check(load().bf_get_tune(self._h, ctypes.byref(t)))
+        return t.as_dict()
 
     def query_batch(self, sources, threshold=INF):
         s = _u32(sources)

@@ -228,6 +228,96 @@ bf_status bf_matrix_device(bf_graph* h, const uint32_t* d_src, uint64_t S, const
   return rc;
 }
 
+static bf_tune to_c(const Tune& t) {
+  bf_tune o{};
+  o.threads_per_block = t.tpb;
+  o.edges_per_item = t.split;
+  o.graph_capture = t.graphs;
+  o.lanes_per_wave = t.max_lanes;
+  return o;
+}
+
+bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
+  if (!h || !t || (t->threads_per_block != 32 && t->threads_per_block != 64 &&
+                   t->threads_per_block != 128 && t->threads_per_block != 256) ||
+      t->edges_per_item == 0 || t->edges_per_item > 1024 ||
+      (t->lanes_per_wave && t->lanes_per_wave % 32)) {
+    set_error("bf_set_tune: invalid tunables");
+    return BF_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(h->g.mu);
+  h->g.tune.tpb = t->threads_per_block;
+  h->g.tune.split = t->edges_per_item;
+  h->g.tune.graphs = t->graph_capture ? 1 : 0;
+  h->g.tune.max_lanes = t->lanes_per_wave;
+  return BF_OK;
+}
+
+bf_status bf_get_tune(const bf_graph* h, bf_tune* t) {
+  if (!h || !t) {
+    set_error("bf_get_tune: null argument");
+    return BF_ERR_INVALID;
+  }
+  *t = to_c(h->g.tune);
+  return BF_OK;
+}
+
+bf_status bf_autotune(bf_graph* h, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
+                      uint64_t T, uint32_t reps, bf_tune* best) {
+  if (!h || !d_src || !d_tgt || !S || !T || !best) {
+    set_error("bf_autotune: null argument or empty sample");
+    return BF_ERR_INVALID;
+  }
+  Graph* g = &h->g;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  if (reps == 0) reps = 2;
+  cudaStream_t s = g->stream;
+  DevBuf out;
+  bf_status rc;
+  if ((rc = out.alloc(S * T * 4))) return rc;
+  std::vector<Tune> cands;
+  std::vector<uint32_t> lane_opts = {0};
+  if (S >= 256) lane_opts.push_back((uint32_t)(((S / 2) + 31) & ~31ull));
+  for (uint32_t tpb : {64u, 128u, 256u})
+    for (uint32_t split : {8u, 16u, 32u})
+      for (uint32_t lanes : lane_opts) {
+        Tune t;
+        t.tpb = tpb;
+        t.split = split;
+        t.graphs = 1;
+        t.max_lanes = lanes;
+        cands.push_back(t);
+      }
+  const Tune saved = g->tune;
+  double best_ms = 1e300;
+  Tune best_t = saved;
+  for (const Tune& t : cands) {
+    g->tune = t;
+    double sum = 0;
+    for (uint32_t r = 0; r <= reps; ++r) {
+      bf_stats st{};
+      rc = batched_matrix(g, g->ctx, d_src, S, d_tgt, T, BF_INF, out.as<uint32_t>(), s, &st);
+      if (rc == BF_OK) rc = check_device_error(g, s);
+      if (rc != BF_OK) {
+        g->tune = saved;
+        return rc;
+      }
+      if (r) sum += st.upward_ms + st.downward_ms + st.extract_ms;
+    }
+    const double ms = sum / reps;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_t = t;
+    }
+  }
+  g->tune = best_t;
+  *best = to_c(best_t);
+  best->step_ms = best_ms;
+  best->tried = (uint32_t)cands.size();
+  return BF_OK;
+}
+
 bf_status bf_matrix(bf_graph* h, const uint32_t* src, uint64_t S, const uint32_t* tgt, uint64_t T,
                     uint32_t threshold, uint32_t* out, bf_stats* st) {
   if (!h || (S && !src) || (T && !tgt) || (S && T && !out)) {

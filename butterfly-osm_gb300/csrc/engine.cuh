@@ -77,7 +77,16 @@ struct Ctx {
   size_t cap_pairs = 0;
 };
 
+// Tunables of the batched sweep (chosen by bf_autotune).
+struct Tune {
+  uint32_t tpb = 128;        // threads per sweep block (4 lanes each)
+  uint32_t split = 16;       // max in-edges per work item
+  uint32_t graphs = 1;       // replay the level schedule from a CUDA graph
+  uint32_t max_lanes = 0;    // lanes per wave (0 = as many as the budget allows)
+};
+
 struct Graph {
+  Tune tune;
   int device = 0;
   uint32_t n = 0;
   uint64_t n_up = 0, n_down = 0;

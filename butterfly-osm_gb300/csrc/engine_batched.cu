@@ -28,7 +28,6 @@ namespace bf {
 
 namespace {
 
-constexpr uint32_t SPLIT = 16;  // max in-edges per work item
 
 uint64_t hash_targets(const uint32_t* t, uint64_t T) {
   uint64_t h = 1469598103934665603ull ^ T;
@@ -78,7 +77,9 @@ __global__ void k_scatter_pairs(const uint2* __restrict__ pr, uint64_t m,
 // NONE and the new ones set.
 bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
                          cudaStream_t st) {
-  const uint64_t key = all ? 0x9E3779B97F4A7C15ull : hash_targets(h_tgt, T);
+  const uint32_t SPLIT = std::max<uint32_t>(1, g->tune.split);
+  const uint64_t key = (all ? 0x9E3779B97F4A7C15ull : hash_targets(h_tgt, T)) ^
+                       ((uint64_t)SPLIT << 56);
   if (sc.valid && sc.key == key && sc.T == T) {
     ++sc.uses;
     return BF_OK;
@@ -204,7 +205,7 @@ namespace {
 
 // One level of the restricted sweep. blockIdx.x = work item, a thread owns
 // 4 consecutive lanes starting at lane; rows are Kp lanes wide (Kp % 4 == 0).
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
     k_sweep_items(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
                   uint32_t* __restrict__ slab, uint32_t Kp) {
   const uint4 it = item[i0 + blockIdx.x];
@@ -405,7 +406,7 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
     cudaGraphExecDestroy(sc.gexec);
     sc.gexec = nullptr;
   }
-  if (!sc.gexec && sc.uses >= 1) {
+  if (!sc.gexec && sc.uses >= 1 && g->tune.graphs) {
     cudaStreamCaptureStatus cs;
     BF_CUDA(cudaStreamIsCapturing(st, &cs));
     if (cs == cudaStreamCaptureStatusNone) {
@@ -430,7 +431,7 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
       sc.g_stream = st;
     }
   }
-  if (sc.gexec) {
+  if (sc.gexec && g->tune.graphs) {
     BF_CUDA(cudaGraphLaunch(sc.gexec, st));
     for (uint32_t l = 0; l < g->n_levels; ++l)
       if (sc.lvl_item[l + 1] != sc.lvl_item[l]) ++*launches;
@@ -471,7 +472,7 @@ bf_status batched_wave(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t kw, uin
   bf_status s;
   Sched& sc = c.sc;
   const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
-  const unsigned tpb = std::min<uint32_t>(128, ((Kp / 4 + 31) / 32) * 32);
+  const unsigned tpb = std::min<uint32_t>(g->tune.tpb, ((Kp / 4 + 31) / 32) * 32);
   const unsigned lane_blocks = (Kp / 4 + tpb - 1) / tpb;
   if (timed) BF_CUDA(cudaEventRecord(c.ev[0], st));
   BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)rows * Kp * 4, st));
@@ -503,6 +504,7 @@ bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, co
     set_error("HBM budget too small for one 32-lane wave of the restricted slab");
     return BF_ERR_OOM;
   }
+  if (g->tune.max_lanes) max_lanes = std::min<uint64_t>(max_lanes, g->tune.max_lanes);
   const uint64_t wave = std::min<uint64_t>(max_lanes, (S + 3) & ~3ull);
   const uint32_t Kp = (uint32_t)((wave + 3) & ~3ull);
   if ((s = ensure_slab(g, c, (size_t)rows * Kp * 4))) return s;

@@ -138,6 +138,28 @@ bf_status bf_graph_info_get(const bf_graph* g, bf_graph_info* out);
 /* Select the engine used by bf_matrix / bf_matrix_device on this graph. */
 bf_status bf_graph_set_engine(bf_graph* g, uint32_t engine, uint32_t k_lanes);
 
+/* Tunables of the batched engine's sweep. */
+typedef struct bf_tune {
+  uint32_t threads_per_block;  /* sweep block size (each thread owns 4 lanes)    */
+  uint32_t edges_per_item;     /* max in-edges per work item (larger in-degrees
+                                  are split into slices combined by atomicMin)   */
+  uint32_t graph_capture;      /* replay the level schedule from a CUDA graph   */
+  uint32_t lanes_per_wave;     /* 0 = as many lanes as the HBM budget allows     */
+  double step_ms;              /* device time of the sample under this choice    */
+  uint32_t tried;              /* candidates timed by bf_autotune               */
+  uint32_t reserved;
+} bf_tune;
+
+/* Time candidate tunables on a sample matrix (device buffers: d_sources,
+ * d_targets) and keep the fastest for this graph; *best receives it. reps
+ * timed repetitions per candidate (after one warm-up). */
+bf_status bf_autotune(bf_graph* g, const uint32_t* d_sources, uint64_t n_sources,
+                      const uint32_t* d_targets, uint64_t n_targets, uint32_t reps,
+                      bf_tune* best);
+/* Set (e.g. from a cached autotune result) or read back the tunables. */
+bf_status bf_set_tune(bf_graph* g, const bf_tune* t);
+bf_status bf_get_tune(const bf_graph* g, bf_tune* t);
+
 /* Distances from k sources to every node: dist_out[lane * n_nodes + node]
  * (the AoS Vec<Vec<u32>> of query_batch). threshold == BF_INF is unbounded;
  * otherwise entries above the threshold are BF_INF. k is at most 128. */

@@ -144,3 +144,34 @@ def test_duplicate_sources_and_targets(built, grid100):
     tgt = np.array([9, 100, 100, 9], dtype=np.uint32)
     want, _ = c.matrix(src, tgt)
     assert np.array_equal(g.matrix(src, tgt), want)
+
+
+@pytest.mark.parametrize("tune", [dict(threads_per_block=32, edges_per_item=1, graph_capture=0,
+                                       lanes_per_wave=32),
+                                  dict(threads_per_block=256, edges_per_item=64,
+                                       graph_capture=1, lanes_per_wave=0),
+                                  dict(threads_per_block=64, edges_per_item=3, graph_capture=1,
+                                       lanes_per_wave=64)])
+def test_tunables_keep_results_exact(built, grid100, tune):
+    _, cch = grid100
+    gold = np.load(GOLDEN / "grid100_matrix.npz")
+    g = _graph(cch)
+    g.set_tune(**tune)
+    assert g.get_tune()["edges_per_item"] == tune["edges_per_item"]
+    for _ in range(3):  # first call builds the schedule, later ones replay it
+        assert np.array_equal(g.matrix(gold["sources"], gold["targets"]), gold["matrix"])
+
+
+def test_autotune_picks_a_valid_choice(built, grid100):
+    import torch
+    import workload
+    _, cch = grid100
+    g = _graph(cch)
+    src, tgt = workload.sources_targets(cch["n"], 300, 500, seed=77)
+    d_s = torch.from_numpy(src.view(np.int32)).cuda()
+    d_t = torch.from_numpy(tgt.view(np.int32)).cuda()
+    best = g.autotune(d_s.data_ptr(), len(src), d_t.data_ptr(), len(tgt), reps=1)
+    assert best["tried"] >= 9 and best["step_ms"] > 0
+    assert best["threads_per_block"] in (64, 128, 256)
+    gold = np.load(GOLDEN / "grid100_matrix.npz")
+    assert np.array_equal(g.matrix(gold["sources"], gold["targets"]), gold["matrix"])
