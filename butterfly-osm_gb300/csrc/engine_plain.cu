@@ -174,11 +174,22 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
         if (t < D) atomicMin(&pd[t], sat_add(d, rec.y));
         else atomicOr(err, DEVERR_EDGE);
       }
-      for (uint64_t e = b_cur + 32 + lane; e < e_cur; e += 32) {
-        const uint2 r = up_rec[e];
-        const uint32_t t = i + r.x;
-        if (t < D) atomicMin(&pd[t], sat_add(d, r.y));
-        else atomicOr(err, DEVERR_EDGE);
+      // high-degree path nodes (the dense top separators): issue 8 record
+      // loads before the first atomic so their latencies overlap
+      for (uint64_t e0 = b_cur + 32; e0 < e_cur; e0 += 256) {
+        uint2 r[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const uint64_t e = e0 + q * 32 + lane;
+          r[q] = e < e_cur ? up_rec[e] : make_uint2(0xFFFFFFFFu, 0);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          if (r[q].x == 0xFFFFFFFFu) continue;
+          const uint32_t t = i + r[q].x;
+          if (t < D) atomicMin(&pd[t], sat_add(d, r[q].y));
+          else atomicOr(err, DEVERR_EDGE);
+        }
       }
     }
     __syncwarp();
