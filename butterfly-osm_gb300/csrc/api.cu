@@ -234,6 +234,7 @@ static bf_tune to_c(const Tune& t) {
   o.edges_per_item = t.split;
   o.graph_capture = t.graphs;
   o.lanes_per_wave = t.max_lanes;
+  o.isochrone_lanes = t.iso_lanes;
   return o;
 }
 
@@ -241,7 +242,8 @@ bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
   if (!h || !t || (t->threads_per_block != 32 && t->threads_per_block != 64 &&
                    t->threads_per_block != 128 && t->threads_per_block != 256) ||
       t->edges_per_item == 0 || t->edges_per_item > 1024 ||
-      (t->lanes_per_wave && t->lanes_per_wave % 32)) {
+      (t->lanes_per_wave && t->lanes_per_wave % 32) ||
+      (t->isochrone_lanes && t->isochrone_lanes % 32)) {
     set_error("bf_set_tune: invalid tunables");
     return BF_ERR_INVALID;
   }
@@ -250,6 +252,7 @@ bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
   h->g.tune.split = t->edges_per_item;
   h->g.tune.graphs = t->graph_capture ? 1 : 0;
   h->g.tune.max_lanes = t->lanes_per_wave;
+  h->g.tune.iso_lanes = t->isochrone_lanes;
   return BF_OK;
 }
 
@@ -276,6 +279,7 @@ bf_status bf_autotune(bf_graph* h, const uint32_t* d_src, uint64_t S, const uint
   DevBuf out;
   bf_status rc;
   if ((rc = out.alloc(S * T * 4))) return rc;
+  const Tune saved = g->tune;
   std::vector<Tune> cands;
   std::vector<uint32_t> lane_opts = {0};
   if (S >= 256) lane_opts.push_back((uint32_t)(((S / 2) + 31) & ~31ull));
@@ -287,9 +291,9 @@ bf_status bf_autotune(bf_graph* h, const uint32_t* d_src, uint64_t S, const uint
         t.split = split;
         t.graphs = 1;
         t.max_lanes = lanes;
+        t.iso_lanes = saved.iso_lanes;
         cands.push_back(t);
       }
-  const Tune saved = g->tune;
   double best_ms = 1e300;
   Tune best_t = saved;
   for (const Tune& t : cands) {

@@ -48,6 +48,8 @@ struct Sched {
   uint4* d_item = nullptr;       // {row, edge0, edge1, split flag}
   uint2* d_erec = nullptr;       // {source row, w}
   uint32_t* d_trow = nullptr;    // [T] target rows
+  uint32_t* d_split = nullptr;   // [rows / 32] rows whose in-edges are split over items
+  size_t cap_split = 0;
   uint64_t T = 0;
   size_t cap_items = 0, cap_edges = 0, cap_t = 0;
   uint32_t uses = 0;             // calls that reused this schedule
@@ -83,6 +85,7 @@ struct Tune {
   uint32_t split = 16;       // max in-edges per work item
   uint32_t graphs = 1;       // replay the level schedule from a CUDA graph
   uint32_t max_lanes = 0;    // lanes per wave (0 = as many as the budget allows)
+  uint32_t iso_lanes = 1024; // isochrone origins per wave (spatially compact waves)
 };
 
 struct Graph {
@@ -163,7 +166,8 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
                        unsigned tpb, cudaStream_t st, uint64_t* launches);
 bf_status sweep_levels_gated(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                              unsigned tpb, uint32_t* active, const uint32_t* thr, uint32_t kw,
-                             cudaStream_t st, uint64_t* launches);
+                             cudaStream_t st, uint64_t* launches,
+                             const uint32_t* seeded = nullptr);
 bf_status ensure_slab(Graph* g, Ctx& c, size_t bytes);
 uint64_t ctx_budget(Graph* g, Ctx& c);
 void free_ctx(Ctx& c);

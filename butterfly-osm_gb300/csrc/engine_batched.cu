@@ -127,6 +127,7 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   for (uint32_t i = 0; i < n_r; ++i) c.rowmap[R[i]] = i;
   std::vector<uint4> items;
   std::vector<uint2> erec;
+  std::vector<uint32_t> split_bits((n_r + 31) / 32 + 1, 0);
   sc.lvl_item.assign(g->n_levels + 1, 0);
   uint32_t lvl = 0;
   for (uint32_t i = 0; i < n_r; ++i) {
@@ -139,6 +140,7 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
       erec.push_back(make_uint2(c.rowmap[g->h_in_rec[k].x], g->h_in_rec[k].y));
     const uint32_t deg = (uint32_t)(k1 - k0);
     const uint32_t split = deg > SPLIT ? 1u : 0u;
+    if (split) split_bits[i >> 5] |= 1u << (i & 31);
     for (uint32_t a = 0; a < deg; a += SPLIT)
       items.push_back(make_uint4(i, e0 + a, e0 + std::min(deg, a + SPLIT), split));
   }
@@ -168,6 +170,9 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   if ((s = ensure(&sc.d_erec, sc.cap_edges, erec.size(), g))) return s;
   if ((s = ensure(&sc.d_trow, sc.cap_t, T, g))) return s;
   if ((s = ensure(&c.d_pairs, c.cap_pairs, pairs.size() * 2, g))) return s;
+  if ((s = ensure(&sc.d_split, sc.cap_split, split_bits.size(), g))) return s;
+  BF_CUDA(cudaMemcpyAsync(sc.d_split, split_bits.data(), split_bits.size() * 4,
+                          cudaMemcpyHostToDevice, st));
   if (!sc.cidx_ready) {
     BF_CUDA(cudaMemsetAsync(sc.d_cidx, 0xFF, (size_t)n * 4, st));
     sc.cidx_ready = true;
@@ -256,7 +261,8 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(128)
     k_sweep_gated(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
                   uint32_t* __restrict__ slab, uint32_t Kp, uint32_t* __restrict__ active,
-                  const uint32_t* __restrict__ thr, uint32_t kw) {
+                  const uint32_t* __restrict__ thr, uint32_t kw,
+                  const uint32_t* __restrict__ seeded) {
   const uint4 it = item[i0 + blockIdx.x];
   bool any = false;
   for (uint32_t e = it.y; e < it.z; ++e) {
@@ -284,7 +290,9 @@ __global__ void __launch_bounds__(128)
     if (acc.z != INF) atomicMin(dst + 2, acc.z);
     if (acc.w != INF) atomicMin(dst + 3, acc.w);
   } else {
-    v = *reinterpret_cast<const uint4*>(dst);
+    // without a full slab reset only seeded rows hold valid data here
+    const bool valid = !seeded || ((seeded[it.x >> 5] >> (it.x & 31)) & 1u);
+    v = valid ? *reinterpret_cast<const uint4*>(dst) : make_uint4(INF, INF, INF, INF);
     v.x = min(v.x, acc.x);
     v.y = min(v.y, acc.y);
     v.z = min(v.z, acc.z);
@@ -358,7 +366,7 @@ uint64_t ctx_budget(Graph* g, Ctx& c) {
 }
 
 static void free_sched(Sched& sc) {
-  void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_trow};
+  void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_trow, sc.d_split};
   for (void* q : p)
     if (q) cudaFree(q);
   if (sc.gexec) cudaGraphExecDestroy(sc.gexec);
@@ -446,12 +454,13 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
 // data of each call).
 bf_status sweep_levels_gated(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                              unsigned tpb, uint32_t* active, const uint32_t* thr, uint32_t kw,
-                             cudaStream_t st, uint64_t* launches) {
+                             cudaStream_t st, uint64_t* launches, const uint32_t* seeded) {
   for (uint32_t l = 0; l < g->n_levels; ++l) {
     const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
     if (i1 == i0) continue;
     dim3 grid(i1 - i0, lane_blocks);
-    k_sweep_gated<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, slab, Kp, active, thr, kw);
+    k_sweep_gated<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, slab, Kp, active, thr, kw,
+                                        seeded);
     ++*launches;
   }
   BF_CUDA(cudaGetLastError());

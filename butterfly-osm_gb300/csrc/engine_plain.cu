@@ -143,6 +143,9 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
   // a seeded unit starts at its seed cost and writes (min) into its source's lane
   const uint32_t c0 = unit_cost ? unit_cost[w] : 0u;
   const uint32_t out_lane = unit_lane ? unit_lane[w] : w;
+  // a per-lane threshold also bounds the relaxations: values above it can
+  // never lead to a distance within it
+  if (lane_thr) threshold = min(threshold, lane_thr[out_lane]);
   for (uint32_t l = lane; l < D; l += 32) pd[l] = (l == 0) ? c0 : INF;
   __syncwarp();
   const unsigned FULL = 0xFFFFFFFFu;

@@ -147,7 +147,8 @@ typedef struct bf_tune {
   uint32_t lanes_per_wave;     /* 0 = as many lanes as the HBM budget allows     */
   double step_ms;              /* device time of the sample under this choice    */
   uint32_t tried;              /* candidates timed by bf_autotune               */
-  uint32_t reserved;
+  uint32_t isochrone_lanes;    /* origins per isochrone wave (0 = budget-limited;
+                                  small waves keep the gated active set compact) */
 } bf_tune;
 
 /* Time candidate tunables on a sample matrix (device buffers: d_sources,

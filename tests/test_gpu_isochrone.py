@@ -71,3 +71,17 @@ def test_bitsets_empty_and_invalid(built, grid100):
     assert bits.shape[0] == 0 and counts.shape == (0,)
     with pytest.raises(bfphast.BfError):
         g.isochrone_bitsets([cch["n"]], [100])
+
+
+@pytest.mark.parametrize("iso_lanes", [32, 64, 0])
+def test_wave_widths_match_oracle(built, country_small, iso_lanes):
+    import workload
+    _, cch = country_small
+    c = orc.Cch.from_dict(cch)
+    g = _graph(cch)
+    g.set_tune(isochrone_lanes=iso_lanes)
+    origins, thr = workload.isochrone_workload(cch["n"], 150, seed=17)
+    bits, counts = g.isochrone_bitsets(origins, thr)
+    want_bits, want_counts = c.isochrone_bitsets(origins, thr)
+    assert np.array_equal(bits, want_bits)
+    assert np.array_equal(counts, want_counts)
