@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--serve-s", type=float, default=15.0,
                     help="seconds of Poisson arrivals for the serving run (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=100.0, help="arrivals per second")
+    ap.add_argument("--isochrones", type=int, default=100000,
+                    help="bulk isochrone origins (0 = skip)")
     return ap.parse_args()
 
 
@@ -266,6 +268,8 @@ def run_ours(args, rank, world, dist):
                          "downward": round(st["downward_ms"], 3),
                          "extract": round(st["extract_ms"], 3)},
            "clocks": clk.summary()}
+    if args.isochrones > 0:
+        res["isochrones"] = run_isochrones(g, cch, args.isochrones, seed=42 + rank)
     if args.serve_s > 0 and rank == 0:
         res["serving"] = run_serving(g, cch["n"], args.serve_s, args.serve_rate)
     return res, cch, src, tgt, out_dev
@@ -327,6 +331,63 @@ def run_serving(g, n, seconds, rate, seed=7):
             "cells_per_s": round(cells / elapsed, 1),
             "isochrones_per_s": round(len(lat["i"]) / elapsed, 1),
             "mix": "70% matrices S,T log-uniform[10,5000]; 30% isochrones T U[300,3600] s"}
+
+
+def run_isochrones(g, cch, count, seed=42):
+    """Bulk isochrones (configs[3]): `count` origins uniform over ranks,
+    thresholds uniform over {300, 600, 1200, 1800, 3600} s; bitsets written
+    to HBM in chunks of 20 000 origins; a sample is checked bit for bit
+    against the CPU oracle, which is also timed on the host cores."""
+    import numpy as np
+    import torch
+    import workload
+    from oracle import oracle as orc
+    n = cch["n"]
+    w64 = (n + 63) // 64
+    o, t = workload.isochrone_workload(n, count, seed=seed)
+    chunk = min(count, 20000)
+    d_b = torch.empty(chunk * w64, dtype=torch.int64, device="cuda")
+    d_c = torch.empty(chunk, dtype=torch.int64, device="cuda")
+    d_o = torch.from_numpy(o.view(np.int32)).cuda()
+    d_t = torch.from_numpy(t.view(np.int32)).cuda()
+    stream = torch.cuda.current_stream()
+    g.isochrone_bitsets_device(d_o.data_ptr(), d_t.data_ptr(), min(count, 1024),
+                               d_b.data_ptr(), d_c.data_ptr())  # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    counts = np.zeros(count, dtype=np.uint64)
+    last = None
+    e0.record(stream)
+    for c0 in range(0, count, chunk):
+        m = min(chunk, count - c0)
+        st = g.isochrone_bitsets_device(d_o.data_ptr() + 4 * c0, d_t.data_ptr() + 4 * c0, m,
+                                        d_b.data_ptr(), d_c.data_ptr(),
+                                        stream=stream.cuda_stream)
+        launches += st["kernel_launches"]
+        counts[c0:c0 + m] = d_c[:m].cpu().numpy().view(np.uint64)
+        last = (c0, m)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    # bit-exact sample from the last chunk + CPU oracle rate on the host cores
+    c = orc.Cch.from_dict(cch)
+    c0, m = last
+    pick = np.linspace(c0, c0 + m - 1, 32).astype(np.int64)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    wb, wc = c.isochrone_bitsets(o[pick], t[pick], threads=threads)
+    cpu_s = time.perf_counter() - t0
+    got = d_b.view(chunk, w64)[torch.from_numpy(pick - c0)].cpu().numpy().view(np.uint64)
+    exact = bool(np.array_equal(got, wb)) and bool(np.array_equal(counts[pick], wc))
+    return {"origins": count, "value": round(count / sec, 1), "unit": "isochrones/s",
+            "seconds": round(sec, 3), "gpu_launches": int(launches),
+            "mean_reachable_nodes": round(float(counts.mean()), 1),
+            "thresholds_s": list(workload.ISO_THRESHOLDS_S),
+            "bit_exact_sample": {"origins": len(pick), "equal": exact},
+            "cpu_baseline": {"value": round(len(pick) / cpu_s, 2), "unit": "isochrones/s",
+                             "cores": threads, "kind": "port",
+                             "sample": "%d origins of the last chunk, %.1f s" % (len(pick), cpu_s)}}
 
 
 def run_reference(args):
