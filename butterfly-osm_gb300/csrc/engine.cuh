@@ -48,7 +48,8 @@ struct Sched {
   uint4* d_item = nullptr;       // {row, edge0, edge1, split flag}
   uint2* d_erec = nullptr;       // {source row, w}
   uint32_t* d_trow = nullptr;    // [T] target rows
-  uint32_t* d_split = nullptr;   // [rows / 32] rows whose in-edges are split over items
+  uint32_t* d_split = nullptr;   // [rows / 32] rows reset every wave: no in-edges, or
+                                 // in-edges split over items (combined by atomicMin)
   size_t cap_split = 0;
   uint64_t T = 0;
   size_t cap_items = 0, cap_edges = 0, cap_t = 0;
@@ -57,6 +58,7 @@ struct Sched {
   uint32_t g_kp = 0, g_lb = 0, g_tpb = 0;
   uint32_t* g_slab = nullptr;
   cudaStream_t g_stream = nullptr;
+  const uint32_t* g_seeded = nullptr;
   std::vector<uint32_t> ranks;   // ranks whose d_cidx entry is set (reset on rebuild)
   bool cidx_ready = false;       // d_cidx holds NONE outside `ranks`
 };
@@ -77,6 +79,8 @@ struct Ctx {
   std::vector<uint32_t> rowmap;    // host scratch [n], all NONE between builds
   uint32_t* d_pairs = nullptr;     // device scratch for (rank, row) updates
   size_t cap_pairs = 0;
+  uint32_t* d_seeded = nullptr;    // [rows / 32] rows seeded by the current wave
+  size_t cap_seeded = 0;
 };
 
 // Tunables of the batched sweep (chosen by bf_autotune).
@@ -163,7 +167,16 @@ bf_status batched_prepare(Graph* g, uint32_t split_edges);
 bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
                          cudaStream_t st);
 bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
-                       unsigned tpb, cudaStream_t st, uint64_t* launches);
+                       unsigned tpb, cudaStream_t st, uint64_t* launches,
+                       const uint32_t* seeded);
+// Reset the slab for a wave and mark its seeded rows (the ancestor paths of
+// the wave's sources) so the sweep reads a row's old value only when seeded.
+void launch_mark_paths(Graph* g, const uint32_t* d_src, uint64_t k, const uint32_t* cidx,
+                       uint32_t* seeded, cudaStream_t st);
+void launch_init_rows(const uint32_t* seeded, const uint32_t* split, uint32_t words,
+                      uint32_t* slab, uint32_t Kp, cudaStream_t st);
+bf_status prepare_rows(Graph* g, Ctx& c, Sched& sc, const uint32_t* d_src, uint64_t kw,
+                       uint32_t Kp, cudaStream_t st, uint64_t* launches);
 bf_status sweep_levels_gated(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                              unsigned tpb, uint32_t* active, const uint32_t* thr, uint32_t kw,
                              cudaStream_t st, uint64_t* launches,

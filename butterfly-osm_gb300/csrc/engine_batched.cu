@@ -134,7 +134,10 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
     const uint32_t p = R[i];
     while (p >= g->lvl_start[lvl + 1]) sc.lvl_item[++lvl] = (uint32_t)items.size();
     const uint64_t k0 = g->h_in_off[p], k1 = g->h_in_off[p + 1];
-    if (k0 == k1) continue;  // no in-edges: the row is its seed
+    if (k0 == k1) {  // no in-edges: the row is its seed (or INF): reset every wave
+      split_bits[i >> 5] |= 1u << (i & 31);
+      continue;
+    }
     const uint32_t e0 = (uint32_t)erec.size();
     for (uint64_t k = k0; k < k1; ++k)
       erec.push_back(make_uint2(c.rowmap[g->h_in_rec[k].x], g->h_in_rec[k].y));
@@ -212,7 +215,7 @@ namespace {
 // 4 consecutive lanes starting at lane; rows are Kp lanes wide (Kp % 4 == 0).
 __global__ void __launch_bounds__(256)
     k_sweep_items(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
-                  uint32_t* __restrict__ slab, uint32_t Kp) {
+                  uint32_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ seeded) {
   const uint4 it = item[i0 + blockIdx.x];
   const uint32_t lane = (blockIdx.y * blockDim.x + threadIdx.x) * 4;
   if (lane >= Kp) return;
@@ -242,7 +245,10 @@ __global__ void __launch_bounds__(256)
     if (acc.z != INF) atomicMin(dst + 2, acc.z);
     if (acc.w != INF) atomicMin(dst + 3, acc.w);
   } else {
-    uint4 c = *reinterpret_cast<const uint4*>(dst);
+    // rows that got no seed this wave hold stale data: their value is the pull
+    uint4 c = ((seeded[it.x >> 5] >> (it.x & 31)) & 1u)
+                  ? *reinterpret_cast<const uint4*>(dst)
+                  : make_uint4(INF, INF, INF, INF);
     c.x = min(c.x, acc.x);
     c.y = min(c.y, acc.y);
     c.z = min(c.z, acc.z);
@@ -306,6 +312,49 @@ __global__ void __launch_bounds__(128)
   const unsigned m = __ballot_sync(__activemask(), act);
   if (m && (threadIdx.x & 31) == (unsigned)(__ffs(m) - 1))
     atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
+}
+
+// Mark the slab rows of every origin's ancestor path (the rows the upward
+// pass will seed): one warp per origin, whole runs of consecutive ranks at once.
+__global__ void __launch_bounds__(128)
+    k_mark_paths(const uint32_t* __restrict__ orig, uint32_t k, const uint32_t* __restrict__ parent,
+                 const uint32_t* __restrict__ run_end, const uint32_t* __restrict__ cidx,
+                 uint32_t* __restrict__ seeded) {
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= k) return;
+  uint32_t x = orig[w];
+  for (uint32_t guard = 0; x != NONE && guard < (1u << 30); ++guard) {
+    // ancestors are shared: once a run's first node is marked, the warp that
+    // marked it covers the rest of this same path
+    const uint32_t r0 = cidx[x];
+    if (r0 != NONE && ((*(volatile uint32_t*)&seeded[r0 >> 5] >> (r0 & 31)) & 1u)) break;
+    const uint32_t e = run_end[x];
+    for (uint32_t r = x + lane; r <= e; r += 32) {
+      const uint32_t row = cidx[r];
+      if (row != NONE) atomicOr(&seeded[row >> 5], 1u << (row & 31));
+    }
+    __syncwarp();
+    x = parent[e];
+  }
+}
+
+// Reset to INF the rows that are read before being fully written: rows that
+// get seeds (seeded bits), rows without in-edges and rows whose in-edges are
+// split over items (combined by atomicMin). All other rows are fully written
+// by the sweep before anything reads them. One block per 32-row group.
+__global__ void __launch_bounds__(256)
+    k_init_rows(const uint32_t* __restrict__ seeded, const uint32_t* __restrict__ split,
+                uint32_t words, uint32_t* __restrict__ slab, uint32_t Kp) {
+  for (uint32_t gw = blockIdx.x; gw < words; gw += gridDim.x) {
+    uint32_t m = seeded[gw] | split[gw];
+    while (m) {
+      const uint32_t b = __ffs(m) - 1;
+      m &= m - 1;
+      uint32_t* row = slab + (size_t)(gw * 32 + b) * Kp;
+      for (uint32_t l = threadIdx.x * 4; l < Kp; l += blockDim.x * 4)
+        *reinterpret_cast<uint4*>(row + l) = make_uint4(INF, INF, INF, INF);
+    }
+  }
 }
 
 // out[s * T + t] = slab[trow[t]][s] (INF above the threshold); 32 x 32 tiles.
@@ -377,6 +426,7 @@ void free_ctx(Ctx& c) {
   free_sched(c.sc);
   free_sched(c.full);
   if (c.d_pairs) cudaFree(c.d_pairs);
+  if (c.d_seeded) cudaFree(c.d_seeded);
   if (c.d_slab) cudaFree(c.d_slab);
   if (c.d_iso_tmp) cudaFree(c.d_iso_tmp);
   for (auto& e : c.ev)
@@ -398,18 +448,19 @@ bf_status batched_prepare(Graph* g, uint32_t) {
 // same schedule and slab geometry the launches are replayed from a captured
 // CUDA graph instead of being issued one by one.
 bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
-                       unsigned tpb, cudaStream_t st, uint64_t* launches) {
+                       unsigned tpb, cudaStream_t st, uint64_t* launches,
+                       const uint32_t* seeded) {
   auto issue = [&](cudaStream_t s) {
     for (uint32_t l = 0; l < g->n_levels; ++l) {
       const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
       if (i1 == i0) continue;
       dim3 grid(i1 - i0, lane_blocks);
-      k_sweep_items<<<grid, tpb, 0, s>>>(sc.d_item, i0, sc.d_erec, slab, Kp);
+      k_sweep_items<<<grid, tpb, 0, s>>>(sc.d_item, i0, sc.d_erec, slab, Kp, seeded);
       ++*launches;
     }
   };
   const bool geom = sc.g_kp == Kp && sc.g_lb == lane_blocks && sc.g_tpb == tpb &&
-                    sc.g_slab == slab && sc.g_stream == st;
+                    sc.g_slab == slab && sc.g_stream == st && sc.g_seeded == seeded;
   if (sc.gexec && !geom) {
     cudaGraphExecDestroy(sc.gexec);
     sc.gexec = nullptr;
@@ -425,7 +476,7 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
         const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
         if (i1 == i0) continue;
         dim3 grid(i1 - i0, lane_blocks);
-        k_sweep_items<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, slab, Kp);
+        k_sweep_items<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, slab, Kp, seeded);
         ++dummy;
       }
       BF_CUDA(cudaStreamEndCapture(st, &graph));
@@ -437,6 +488,7 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
       sc.g_tpb = tpb;
       sc.g_slab = slab;
       sc.g_stream = st;
+      sc.g_seeded = seeded;
     }
   }
   if (sc.gexec && g->tune.graphs) {
@@ -473,6 +525,36 @@ void launch_extract_lanes(const uint32_t* slab, uint32_t Kp, const uint32_t* tro
   k_extract_lanes<<<eg, eb, 0, st>>>(slab, Kp, trow, T, S, threshold, out);
 }
 
+void launch_mark_paths(Graph* g, const uint32_t* d_src, uint64_t k, const uint32_t* cidx,
+                       uint32_t* seeded, cudaStream_t st) {
+  if (!k) return;
+  k_mark_paths<<<(unsigned)((k + 3) / 4), 128, 0, st>>>(d_src, (uint32_t)k, g->d_parent,
+                                                        g->d_run_end, cidx, seeded);
+}
+
+void launch_init_rows(const uint32_t* seeded, const uint32_t* split, uint32_t words,
+                      uint32_t* slab, uint32_t Kp, cudaStream_t st) {
+  const uint32_t tpb = Kp >= 1024 ? 256 : 64;
+  k_init_rows<<<std::min<uint32_t>(words, 152 * 32), tpb, 0, st>>>(seeded, split, words, slab,
+                                                                   Kp);
+}
+
+bf_status prepare_rows(Graph* g, Ctx& c, Sched& sc, const uint32_t* d_src, uint64_t kw,
+                       uint32_t Kp, cudaStream_t st, uint64_t* launches) {
+  const uint32_t words = (std::max<uint32_t>(sc.n_r, 1) + 31) / 32;
+  bf_status s;
+  if ((s = ensure(&c.d_seeded, c.cap_seeded, words, g))) return s;
+  BF_CUDA(cudaMemsetAsync(c.d_seeded, 0, (size_t)words * 4, st));
+  // the restricted rows are mostly on some source's ancestor path, so one
+  // streaming reset of the slab beats resetting the marked rows one by one;
+  // the seeded bits still let the sweep skip reading unseeded rows
+  BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)std::max<uint32_t>(sc.n_r, 1) * Kp * 4, st));
+  launch_mark_paths(g, d_src, kw, sc.d_cidx, c.d_seeded, st);
+  BF_CUDA(cudaGetLastError());
+  *launches += 1;
+  return BF_OK;
+}
+
 // One wave on the context's current target-restricted schedule: reset the
 // slab, upward pass for kw sources, restricted sweep. Records c.ev[0..2]
 // around the phases when `timed`.
@@ -483,12 +565,13 @@ bf_status batched_wave(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t kw, uin
   const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
   const unsigned tpb = std::min<uint32_t>(g->tune.tpb, ((Kp / 4 + 31) / 32) * 32);
   const unsigned lane_blocks = (Kp / 4 + tpb - 1) / tpb;
+  (void)rows;
   if (timed) BF_CUDA(cudaEventRecord(c.ev[0], st));
-  BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)rows * Kp * 4, st));
+  if ((s = prepare_rows(g, c, sc, d_src, kw, Kp, st, launches))) return s;
   if ((s = launch_upward(g, d_src, kw, INF, sc.d_cidx, c.d_slab, Kp, nullptr, st))) return s;
   ++*launches;
   if (timed) BF_CUDA(cudaEventRecord(c.ev[1], st));
-  return sweep_levels(g, sc, c.d_slab, Kp, lane_blocks, tpb, st, launches);
+  return sweep_levels(g, sc, c.d_slab, Kp, lane_blocks, tpb, st, launches, c.d_seeded);
 }
 
 bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,

@@ -92,46 +92,6 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Mark the slab rows of every origin's ancestor path (the rows the upward
-// pass will seed): one warp per origin, whole runs of consecutive ranks at once.
-__global__ void __launch_bounds__(128)
-    k_mark_paths(const uint32_t* __restrict__ orig, uint32_t k, const uint32_t* __restrict__ parent,
-                 const uint32_t* __restrict__ run_end, const uint32_t* __restrict__ cidx,
-                 uint32_t* __restrict__ seeded) {
-  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (w >= k) return;
-  uint32_t x = orig[w];
-  for (uint32_t guard = 0; x != NONE && guard < (1u << 30); ++guard) {
-    const uint32_t e = run_end[x];
-    for (uint32_t r = x + lane; r <= e; r += 32) {
-      const uint32_t row = cidx[r];
-      if (row != NONE) atomicOr(&seeded[row >> 5], 1u << (row & 31));
-    }
-    x = parent[e];
-  }
-}
-
-// Reset to INF the rows that are read before being fully written: rows that
-// get seeds (seeded bits) and rows whose in-edges are split over items
-// (combined by atomicMin). All other rows are only read once marked active,
-// i.e. after the sweep wrote them. One warp per 32-row group.
-__global__ void __launch_bounds__(256)
-    k_init_rows(const uint32_t* __restrict__ seeded, const uint32_t* __restrict__ split,
-                uint32_t words, uint32_t* __restrict__ slab, uint32_t Kp) {
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gw < words; gw += nw) {
-    uint32_t m = seeded[gw] | split[gw];
-    while (m) {
-      const uint32_t b = __ffs(m) - 1;
-      m &= m - 1;
-      uint32_t* row = slab + (size_t)(gw * 32 + b) * Kp;
-      for (uint32_t l = lane * 4; l < Kp; l += 128)
-        *reinterpret_cast<uint4*>(row + l) = make_uint4(INF, INF, INF, INF);
-    }
-  }
-}
-
 }  // namespace
 
 // d_bits: n rows of ceil(n_nodes / 64) u64 words; d_counts: n u64.
@@ -209,9 +169,8 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
     const uint64_t kw = std::min<uint64_t>(wave, n - s0);
     if (stats) BF_CUDA(cudaEventRecord(c.ev[0], st));
     BF_CUDA(cudaMemsetAsync(d_active, 0, 2 * aw * 4, st));  // active + seeded bitmaps
-    k_mark_paths<<<(unsigned)((kw + 3) / 4), 128, 0, st>>>(p_orig + s0, (uint32_t)kw, g->d_parent,
-                                                         g->d_run_end, sc.d_cidx, d_seeded);
-    k_init_rows<<<152 * 8, 256, 0, st>>>(d_seeded, sc.d_split, (uint32_t)aw, c.d_slab, Kp);
+    launch_mark_paths(g, p_orig + s0, kw, sc.d_cidx, d_seeded, st);
+    launch_init_rows(d_seeded, sc.d_split, (uint32_t)aw, c.d_slab, Kp, st);
     launches += 2;
     if ((s = launch_upward(g, p_orig + s0, kw, INF, sc.d_cidx, c.d_slab, Kp, d_active, st,
                            p_thr + s0)))

@@ -179,14 +179,15 @@ bf_status matrix_seeded(Graph* g, Ctx& c, const bf_seed* src_seeds, const uint64
       }
     uint32_t* du = d_units.as<uint32_t>();
     if (nu) BF_CUDA(cudaMemcpyAsync(du, units.data(), units.size() * 4, cudaMemcpyHostToDevice, s));
-    BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)rows * Kp * 4, s));
+    if ((rc = prepare_rows(g, c, sc, du, nu, Kp, s, &launches))) return rc;
     if (nu) {
       if ((rc = launch_upward(g, du, nu, INF, sc.d_cidx, c.d_slab, Kp, nullptr, s, nullptr,
                               du + nu, du + 2 * nu)))
         return rc;
       ++launches;
     }
-    if ((rc = sweep_levels(g, sc, c.d_slab, Kp, lane_blocks, tpb, s, &launches))) return rc;
+    if ((rc = sweep_levels(g, sc, c.d_slab, Kp, lane_blocks, tpb, s, &launches, c.d_seeded)))
+      return rc;
     dim3 eg((unsigned)((T + 31) / 32), (unsigned)((kw + 31) / 32)), eb(32, 8);
     k_seeded_extract<<<eg, eb, 0, s>>>(c.d_slab, Kp, sc.d_cidx, d_to.as<uint64_t>(),
                                        d_ts.as<uint2>(), T, (uint32_t)kw, threshold,
