@@ -22,6 +22,7 @@ INF = 0xFFFFFFFF
 BF_OK, BF_ERR_INVALID, BF_ERR_OOM, BF_ERR_DEVICE, BF_ERR_TIMEOUT, BF_ERR_CANCELLED, BF_ERR_BUSY, \
     BF_ERR_UNSUPPORTED = range(8)
 ENGINE_AUTO, ENGINE_PLAIN, ENGINE_BATCHED = 0, 1, 2
+FLAG_REVERSE = 1
 REQ_MATRIX, REQ_ISOCHRONE = 1, 2
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
@@ -182,7 +183,7 @@ class Graph:
     """A CCH resident on the GPU (owns a bf_graph handle)."""
 
     def __init__(self, n_nodes, up_off, up_tgt, up_w, down_off, down_tgt, down_w, device=0,
-                 engine=ENGINE_AUTO, k_lanes=0, subtree_nodes=0, hbm_budget=0):
+                 engine=ENGINE_AUTO, k_lanes=0, subtree_nodes=0, hbm_budget=0, reverse=False):
         lib = load()
         self._keep = [np.ascontiguousarray(up_off, dtype=np.uint64), _u32(up_tgt), _u32(up_w),
                       np.ascontiguousarray(down_off, dtype=np.uint64), _u32(down_tgt),
@@ -190,7 +191,8 @@ class Graph:
         uo, ut, uw, do, dt, dw = self._keep
         csr = CchCsr(n_nodes, 0, _ptr(uo, _u64p), _ptr(ut), _ptr(uw), _ptr(do, _u64p), _ptr(dt),
                      _ptr(dw))
-        cfg = Config(device, engine, k_lanes, 0, hbm_budget, subtree_nodes, 0)
+        cfg = Config(device, engine, k_lanes, FLAG_REVERSE if reverse else 0, hbm_budget,
+                     subtree_nodes, 0)
         h = ctypes.c_void_p()
         _check(lib.bf_graph_create(ctypes.byref(csr), ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h

@@ -108,9 +108,9 @@ bf_status bf_graph_create(const bf_cch_csr* csr, const bf_config* cfg, bf_graph*
   }
   bf_config c{};
   if (cfg) c = *cfg;
-  if (c.engine > BF_ENGINE_BATCHED || (c.k_lanes && c.k_lanes != 16 && c.k_lanes != 32 &&
-                                       c.k_lanes != 64 && c.k_lanes != 128)) {
-    set_error("bf_graph_create: invalid engine or k_lanes");
+  if (c.engine > BF_ENGINE_BATCHED || (c.flags & ~BF_FLAG_REVERSE) ||
+      (c.k_lanes && c.k_lanes != 16 && c.k_lanes != 32 && c.k_lanes != 64 && c.k_lanes != 128)) {
+    set_error("bf_graph_create: invalid engine, flags or k_lanes");
     return BF_ERR_INVALID;
   }
   int ndev = 0;

@@ -47,7 +47,73 @@ bf_status dev_upload(T** dptr, const T* src, size_t count, Graph* g) {
 
 }  // namespace
 
+static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, Graph* g);
+
+// The CCH of the transposed graph: UP'(x) = {(y, w) : DOWN edge y -> x},
+// DOWN'(y) = {(x, w) : UP edge x -> y}. Distances from t in it are the
+// distances to t in the original (the reference's reverse PHAST runs its
+// upward phase over DownReverseAdjFlat and pulls over UpAdjFlat,
+// route/src/range/phast.rs:879-1001).
 bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
+  if (!(cfg && (cfg->flags & BF_FLAG_REVERSE))) return build_graph_impl(csr, cfg, g);
+  const uint32_t n = csr->n_nodes;
+  const uint64_t* uo = csr->up_offsets;
+  const uint64_t* dno = csr->down_offsets;
+  for (uint32_t u = 0; u < n; ++u)
+    if (uo[u + 1] < uo[u] || dno[u + 1] < dno[u]) {
+      set_error("CSR offsets must be non-decreasing");
+      return BF_ERR_INVALID;
+    }
+  std::vector<uint64_t> ro(n + 1, 0), rdo(n + 1, 0);
+  for (uint32_t y = 0; y < n; ++y)
+    for (uint64_t k = dno[y]; k < dno[y + 1]; ++k) {
+      const uint32_t x = csr->down_targets[k];
+      if (x >= y) {
+        set_error("DOWN edge does not go to a lower rank");
+        return BF_ERR_INVALID;
+      }
+      ro[x + 1]++;
+    }
+  for (uint32_t x = 0; x < n; ++x)
+    for (uint64_t k = uo[x]; k < uo[x + 1]; ++k) {
+      const uint32_t y = csr->up_targets[k];
+      if (y >= n || y <= x) {
+        set_error("UP edge does not go to a higher rank");
+        return BF_ERR_INVALID;
+      }
+      rdo[y + 1]++;
+    }
+  for (uint32_t v = 0; v < n; ++v) {
+    ro[v + 1] += ro[v];
+    rdo[v + 1] += rdo[v];
+  }
+  std::vector<uint32_t> rt(ro[n]), rw(ro[n]), rdt(rdo[n]), rdw(rdo[n]);
+  {
+    std::vector<uint64_t> f(ro.begin(), ro.end() - 1), fd(rdo.begin(), rdo.end() - 1);
+    for (uint32_t y = 0; y < n; ++y)
+      for (uint64_t k = dno[y]; k < dno[y + 1]; ++k) {
+        const uint32_t x = csr->down_targets[k];
+        rt[f[x]] = y;
+        rw[f[x]++] = csr->down_weights[k];
+      }
+    for (uint32_t x = 0; x < n; ++x)
+      for (uint64_t k = uo[x]; k < uo[x + 1]; ++k) {
+        const uint32_t y = csr->up_targets[k];
+        rdt[fd[y]] = x;
+        rdw[fd[y]++] = csr->up_weights[k];
+      }
+  }
+  bf_cch_csr t = *csr;
+  t.up_offsets = ro.data();
+  t.up_targets = rt.data();
+  t.up_weights = rw.data();
+  t.down_offsets = rdo.data();
+  t.down_targets = rdt.data();
+  t.down_weights = rdw.data();
+  return build_graph_impl(&t, cfg, g);
+}
+
+static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
   const uint32_t n = csr->n_nodes;
   g->n = n;
   const uint64_t* uo = csr->up_offsets;

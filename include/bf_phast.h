@@ -92,12 +92,20 @@ typedef struct bf_config {
   uint32_t engine;            /* bf_engine                                         */
   uint32_t k_lanes;           /* lanes per batch for the batched engine (0 = autotune;
                                  16, 32, 64 or 128)                                */
-  uint32_t flags;             /* reserved, must be 0                               */
+  uint32_t flags;             /* BF_FLAG_* bits                                    */
   uint64_t hbm_budget_bytes;  /* cap on device memory for distance slabs and
                                  scratch (0 = 85% of free memory at creation)      */
   uint32_t subtree_nodes;     /* max nodes of a shared-memory subtree (0 = auto)   */
   uint32_t reserved2;
 } bf_config;
+
+/* bf_config.flags: build the CCH of the transposed graph. Every entry point
+ * then answers the all-to-one (arrive-by) question: bf_phast_query(g, t) is
+ * PhastEngine::query_block_gated_reverse (route/src/range/phast.rs:879), the
+ * isochrones are the reverse isochrones of run_phast_bounded_fast_reverse_seeded
+ * (route/src/server/isochrone_handler.rs:657-780), and bf_matrix(g, T, S)
+ * is the transpose of the forward S x T matrix. */
+#define BF_FLAG_REVERSE 1u
 
 typedef struct bf_graph bf_graph;
 
