@@ -77,6 +77,10 @@ class Seed(ctypes.Structure):
     _fields_ = [("rank", ctypes.c_uint32), ("cost", ctypes.c_uint32)]
 
 
+class Seed2(ctypes.Structure):
+    _fields_ = [("rank", ctypes.c_uint32), ("cost", ctypes.c_uint32), ("len", ctypes.c_uint32)]
+
+
 class ServerCfg(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
                 ("max_queue", ctypes.c_uint32), ("timeout_ms", ctypes.c_uint32),
@@ -101,6 +105,9 @@ class Completion(ctypes.Structure):
 _SIGNATURES = {
     "bf_graph_create": (ctypes.c_int, [ctypes.POINTER(CchCsr), ctypes.POINTER(Config),
                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "bf_graph_create_2ch": (ctypes.c_int, [ctypes.POINTER(CchCsr), _u32p, _u32p,
+                                           ctypes.POINTER(Config),
+                                           ctypes.POINTER(ctypes.c_void_p)]),
     "bf_graph_destroy": (None, [ctypes.c_void_p]),
     "bf_graph_info_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(GraphInfo)]),
     "bf_graph_set_engine": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]),
@@ -126,6 +133,13 @@ _SIGNATURES = {
     "bf_phast_bounded_seeded": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Seed),
                                                ctypes.c_uint32, ctypes.c_uint32, _u32p, _u32p,
                                                ctypes.c_uint64, _u64p]),
+    "bf_matrix_seeded_2ch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Seed2), _u64p,
+                                            ctypes.c_uint64, ctypes.POINTER(Seed2), _u64p,
+                                            ctypes.c_uint64, ctypes.c_uint32, _u32p, _u32p, _u64p,
+                                            ctypes.c_uint64, _u64p, ctypes.POINTER(Stats)]),
+    "bf_phast_bounded_seeded_2ch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Seed2),
+                                                   ctypes.c_uint32, ctypes.c_uint32, _u32p,
+                                                   _u32p, _u32p, ctypes.c_uint64, _u64p]),
     "bf_isochrone_bitsets": (ctypes.c_int, [ctypes.c_void_p, _u32p, _u32p, ctypes.c_uint64,
                                             _u64p, _u64p, ctypes.POINTER(Stats)]),
     "bf_isochrone_bitsets_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p,
@@ -183,7 +197,10 @@ class Graph:
     """A CCH resident on the GPU (owns a bf_graph handle)."""
 
     def __init__(self, n_nodes, up_off, up_tgt, up_w, down_off, down_tgt, down_w, device=0,
-                 engine=ENGINE_AUTO, k_lanes=0, subtree_nodes=0, hbm_budget=0, reverse=False):
+                 engine=ENGINE_AUTO, k_lanes=0, subtree_nodes=0, hbm_budget=0, reverse=False,
+                 up_len=None, down_len=None):
+        """up_len / down_len (optional): length-along-time weight per CCH edge,
+        INF exactly where the time weight is; they make a two-channel graph."""
         lib = load()
         self._keep = [np.ascontiguousarray(up_off, dtype=np.uint64), _u32(up_tgt), _u32(up_w),
                       np.ascontiguousarray(down_off, dtype=np.uint64), _u32(down_tgt),
@@ -194,7 +211,13 @@ class Graph:
         cfg = Config(device, engine, k_lanes, FLAG_REVERSE if reverse else 0, hbm_budget,
                      subtree_nodes, 0)
         h = ctypes.c_void_p()
-        _check(lib.bf_graph_create(ctypes.byref(csr), ctypes.byref(cfg), ctypes.byref(h)))
+        if up_len is not None or down_len is not None:
+            ul, dl = _u32(up_len if up_len is not None else []), _u32(
+                down_len if down_len is not None else [])
+            _check(lib.bf_graph_create_2ch(ctypes.byref(csr), _ptr(ul), _ptr(dl),
+                                           ctypes.byref(cfg), ctypes.byref(h)))
+        else:
+            _check(lib.bf_graph_create(ctypes.byref(csr), ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
         self._keep = None  # the library copied what it needs
         self.n = n_nodes
@@ -309,6 +332,48 @@ class Graph:
                                               _ptr(ds), cap, ctypes.byref(cnt)))
         c = cnt.value
         return rk[:c].copy(), ds[:c].copy()
+
+    @staticmethod
+    def _pack2(sets):
+        off = np.zeros(len(sets) + 1, dtype=np.uint64)
+        flat = []
+        for i, ss in enumerate(sets):
+            flat.extend(ss)
+            off[i + 1] = len(flat)
+        arr = (Seed2 * max(1, len(flat)))(*[Seed2(int(r), int(c), int(ln)) for r, c, ln in flat])
+        return arr, off
+
+    def matrix_seeded_2ch(self, src_seeds, tgt_seeds, threshold=INF, with_conflicts=False):
+        """Seed sets of (rank, cost, len). Returns (time, length) matrices
+        (conflict cells INF) and, if asked, the conflict cell indices."""
+        sa, so = self._pack2(src_seeds)
+        ta, to = self._pack2(tgt_seeds)
+        S, T = len(src_seeds), len(tgt_seeds)
+        ot = np.empty((S, T), dtype=np.uint32)
+        ol = np.empty((S, T), dtype=np.uint32)
+        st = Stats()
+        cap = S * T
+        conf = np.empty(max(1, cap), dtype=np.uint64)
+        nconf = ctypes.c_uint64()
+        _check(load().bf_matrix_seeded_2ch(self._h, sa, _ptr(so, _u64p), S, ta, _ptr(to, _u64p),
+                                           T, threshold, _ptr(ot), _ptr(ol), _ptr(conf, _u64p),
+                                           cap, ctypes.byref(nconf), ctypes.byref(st)))
+        if with_conflicts:
+            return ot, ol, conf[:min(cap, nconf.value)].copy()
+        return ot, ol
+
+    def phast_bounded_seeded_2ch(self, seeds, threshold):
+        """Settled (ranks, times, lengths) with time <= threshold, ascending rank."""
+        arr, _ = self._pack2([seeds])
+        cap = self.n
+        rk = np.empty(cap, dtype=np.uint32)
+        tm = np.empty(cap, dtype=np.uint32)
+        ln = np.empty(cap, dtype=np.uint32)
+        cnt = ctypes.c_uint64()
+        _check(load().bf_phast_bounded_seeded_2ch(self._h, arr, len(seeds), threshold, _ptr(rk),
+                                                  _ptr(tm), _ptr(ln), cap, ctypes.byref(cnt)))
+        c = cnt.value
+        return rk[:c].copy(), tm[:c].copy(), ln[:c].copy()
 
     def isochrone_bitsets(self, origins, thresholds, stats=False):
         o, t = _u32(origins), _u32(thresholds)

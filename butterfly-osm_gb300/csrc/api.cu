@@ -95,7 +95,8 @@ Graph* graph_of(bf_graph* h) { return &h->g; }
 
 extern "C" {
 
-bf_status bf_graph_create(const bf_cch_csr* csr, const bf_config* cfg, bf_graph** out) {
+static bf_status graph_create(const bf_cch_csr* csr, const uint32_t* up_len,
+                              const uint32_t* down_len, const bf_config* cfg, bf_graph** out) {
   if (out) *out = nullptr;
   if (!csr || !out || !csr->up_offsets || !csr->down_offsets || csr->n_nodes == 0) {
     set_error("bf_graph_create: null argument or empty graph");
@@ -153,7 +154,7 @@ bf_status bf_graph_create(const bf_cch_csr* csr, const bf_config* cfg, bf_graph*
   g->hbm_budget = c.hbm_budget_bytes ? c.hbm_budget_bytes : (uint64_t)(fr * 0.85);
   bf_status s;
   try {
-    s = build_graph(csr, &c, g);
+    s = build_graph(csr, &c, g, up_len, down_len);
     if (s == BF_OK) s = batched_prepare(g, c.subtree_nodes);
   } catch (const std::bad_alloc&) {
     set_error("out of host memory");
@@ -166,6 +167,26 @@ bf_status bf_graph_create(const bf_cch_csr* csr, const bf_config* cfg, bf_graph*
   }
   *out = h;
   return BF_OK;
+}
+
+bf_status bf_graph_create(const bf_cch_csr* csr, const bf_config* cfg, bf_graph** out) {
+  return graph_create(csr, nullptr, nullptr, cfg, out);
+}
+
+bf_status bf_graph_create_2ch(const bf_cch_csr* csr, const uint32_t* up_len_weights,
+                              const uint32_t* down_len_weights, const bf_config* cfg,
+                              bf_graph** out) {
+  if (out) *out = nullptr;
+  if (csr && csr->up_offsets && csr->down_offsets && csr->n_nodes &&
+      ((csr->up_offsets[csr->n_nodes] && !up_len_weights) ||
+       (csr->down_offsets[csr->n_nodes] && !down_len_weights))) {
+    set_error("bf_graph_create_2ch: length weights missing");
+    return BF_ERR_INVALID;
+  }
+  // an edgeless direction still marks the graph as two-channel
+  static const uint32_t none = 0;
+  return graph_create(csr, up_len_weights ? up_len_weights : &none,
+                      down_len_weights ? down_len_weights : &none, cfg, out);
 }
 
 void bf_graph_destroy(bf_graph* h) {
@@ -489,6 +510,99 @@ bf_status bf_phast_bounded_seeded(bf_graph* h, const bf_seed* seeds, uint32_t n_
   if (n_out) *n_out = 0;
   if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
   return bounded_seeded(g, g->ctx, seeds, n_seeds, threshold, out_rank, out_dist, cap, n_out);
+}
+
+static bf_status check_seedsets2(const bf_seed2* seeds, const uint64_t* off, uint64_t m,
+                                 uint32_t n, const char* what) {
+  if (!off || off[0] != 0) {
+    set_error(std::string(what) + " offsets must start at 0");
+    return BF_ERR_INVALID;
+  }
+  for (uint64_t i = 0; i < m; ++i)
+    if (off[i + 1] < off[i]) {
+      set_error(std::string(what) + " offsets must be non-decreasing");
+      return BF_ERR_INVALID;
+    }
+  if (off[m] && !seeds) {
+    set_error(std::string(what) + " seeds missing");
+    return BF_ERR_INVALID;
+  }
+  for (uint64_t k = 0; k < off[m]; ++k)
+    if (seeds[k].rank >= n) {
+      set_error(std::string(what) + " seed rank " + std::to_string(seeds[k].rank) +
+                " is not a node of the graph");
+      return BF_ERR_INVALID;
+    }
+  return BF_OK;
+}
+
+bf_status bf_matrix_seeded_2ch(bf_graph* h, const bf_seed2* src_seeds, const uint64_t* src_off,
+                               uint64_t S, const bf_seed2* tgt_seeds, const uint64_t* tgt_off,
+                               uint64_t T, uint32_t threshold, uint32_t* out_time,
+                               uint32_t* out_len, uint64_t* conflicts, uint64_t conflict_cap,
+                               uint64_t* n_conflicts, bf_stats* st) {
+  if (!h || (S && T && (!out_time || !out_len)) || (conflict_cap && !conflicts)) {
+    set_error("bf_matrix_seeded_2ch: null argument");
+    return BF_ERR_INVALID;
+  }
+  double t0 = now_s();
+  Graph* g = &h->g;
+  if (!g->has_len) {
+    set_error("bf_matrix_seeded_2ch: the graph has no length weights (use bf_graph_create_2ch)");
+    return BF_ERR_UNSUPPORTED;
+  }
+  bf_status rc;
+  if ((rc = check_seedsets2(src_seeds, src_off, S, g->n, "source")) ||
+      (rc = check_seedsets2(tgt_seeds, tgt_off, T, g->n, "target")))
+    return rc;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (n_conflicts) *n_conflicts = 0;
+  if (!S || !T) return BF_OK;
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  try {
+    rc = matrix_seeded_2ch(g, g->ctx, src_seeds, src_off, S, tgt_seeds, tgt_off, T, threshold,
+                           out_time, out_len, conflicts, conflict_cap, n_conflicts, st);
+  } catch (const std::bad_alloc&) {
+    set_error("out of host memory");
+    rc = BF_ERR_OOM;
+  }
+  if (st) {
+    st->n_sources = S;
+    st->n_targets = T;
+    st->total_ms = (now_s() - t0) * 1e3;
+  }
+  return rc;
+}
+
+bf_status bf_phast_bounded_seeded_2ch(bf_graph* h, const bf_seed2* seeds, uint32_t n_seeds,
+                                      uint32_t threshold, uint32_t* out_rank, uint32_t* out_time,
+                                      uint32_t* out_len, uint64_t cap, uint64_t* n_out) {
+  if (!h || (n_seeds && !seeds) || (cap && (!out_rank || !out_time || !out_len))) {
+    set_error("bf_phast_bounded_seeded_2ch: null argument");
+    return BF_ERR_INVALID;
+  }
+  Graph* g = &h->g;
+  if (!g->has_len) {
+    set_error("bf_phast_bounded_seeded_2ch: the graph has no length weights");
+    return BF_ERR_UNSUPPORTED;
+  }
+  for (uint32_t i = 0; i < n_seeds; ++i)
+    if (seeds[i].rank >= g->n) {
+      set_error("bf_phast_bounded_seeded_2ch: seed rank " + std::to_string(seeds[i].rank) +
+                " is not a node of the graph");
+      return BF_ERR_INVALID;
+    }
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (n_out) *n_out = 0;
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  try {
+    return bounded_seeded_2ch(g, g->ctx, seeds, n_seeds, threshold, out_rank, out_time, out_len,
+                              cap, n_out);
+  } catch (const std::bad_alloc&) {
+    set_error("out of host memory");
+    return BF_ERR_OOM;
+  }
 }
 
 bf_status bf_isochrone_bitsets_device(bf_graph* h, const uint32_t* d_orig, const uint32_t* d_thr,

@@ -30,6 +30,24 @@ __host__ __device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) {
   return (s < a) ? INF : s;  // wraps only on overflow; INF + x also saturates
 }
 
+// Ancestor path of `s` written into pn[0 .. D): runs of consecutive ranks are
+// emitted by the whole warp at once. Returns D (or 0 on inconsistency).
+__device__ __forceinline__ uint32_t walk_path(uint32_t s, uint32_t D,
+                                              const uint32_t* __restrict__ parent,
+                                              const uint32_t* __restrict__ run_end, uint32_t* pn,
+                                              uint32_t lane) {
+  uint32_t i = 0, x = s;
+  while (x != 0xFFFFFFFFu) {
+    const uint32_t e = run_end[x];
+    const uint32_t len = e - x + 1;
+    if (i + len > D) return 0;
+    for (uint32_t l = lane; l < len; l += 32) pn[i + l] = x + l;
+    i += len;
+    x = parent[e];
+  }
+  return i == D ? D : 0;
+}
+
 // Lanes per batch of the plain engine (one warp lane per source).
 constexpr uint32_t PLAIN_K = 32;
 // Ancestor-path entries a warp keeps in shared memory during the upward pass.
@@ -47,6 +65,8 @@ struct Sched {
   uint32_t* d_cidx = nullptr;    // [n] rank -> compact row or NONE
   uint4* d_item = nullptr;       // {row, edge0, edge1, split flag}
   uint2* d_erec = nullptr;       // {source row, w}
+  uint32_t* d_elen = nullptr;    // length weight per edge of d_erec (two-channel graphs)
+  size_t cap_elen = 0;
   uint32_t* d_trow = nullptr;    // [T] target rows
   uint32_t* d_split = nullptr;   // [rows / 32] rows reset every wave: no in-edges, or
                                  // in-edges split over items (combined by atomicMin)
@@ -117,6 +137,8 @@ struct Graph {
   uint32_t* d_depth = nullptr;    // [n] etree depth
   uint64_t* d_up_off = nullptr;   // [n+1] finite UP edges by source rank
   uint2* d_up_rec = nullptr;      // {depth(src) - depth(dst), w}
+  uint32_t* d_up_len = nullptr;   // length weight per UP record (two-channel graphs)
+  bool has_len = false;           // created with length-along-time weights
   uint32_t* d_pos_of = nullptr;   // [n] rank -> plain slab position
   uint32_t* d_rank_at = nullptr;  // [n] plain slab position -> rank
   // device: level-ordered pull CSR (plain engine)
@@ -133,6 +155,7 @@ struct Graph {
   // host copies of the pull CSR (target restriction is computed on the host)
   std::vector<uint64_t> h_in_off;  // [n+1] by slab position
   std::vector<uint2> h_in_rec;     // {source position, w}
+  std::vector<uint32_t> h_in_len;  // length weight per h_in_rec entry (two-channel graphs)
 
   Ctx ctx;                         // execution context of the C-ABI calls
   uint32_t* d_io = nullptr;        // bf_matrix host-call I/O buffer
@@ -142,7 +165,8 @@ struct Graph {
 };
 
 // graph.cu
-bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g);
+bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g,
+                      const uint32_t* up_len = nullptr, const uint32_t* down_len = nullptr);
 void free_graph(Graph* g);
 
 // engine_plain.cu
@@ -203,6 +227,16 @@ bf_status matrix_seeded(Graph* g, Ctx& c, const bf_seed* src_seeds, const uint64
                         uint64_t conflict_cap, uint64_t* n_conflicts, bf_stats* st);
 bf_status bounded_seeded(Graph* g, Ctx& c, const bf_seed* seeds, uint32_t n_seeds, uint32_t threshold,
                          uint32_t* out_rank, uint32_t* out_dist, uint64_t cap, uint64_t* n_out);
+
+// twochannel.cu
+bf_status matrix_seeded_2ch(Graph* g, Ctx& c, const bf_seed2* src_seeds, const uint64_t* src_off,
+                            uint64_t S, const bf_seed2* tgt_seeds, const uint64_t* tgt_off,
+                            uint64_t T, uint32_t threshold, uint32_t* out_time, uint32_t* out_len,
+                            uint64_t* conflicts, uint64_t conflict_cap, uint64_t* n_conflicts,
+                            bf_stats* st);
+bf_status bounded_seeded_2ch(Graph* g, Ctx& c, const bf_seed2* seeds, uint32_t n_seeds,
+                             uint32_t threshold, uint32_t* out_rank, uint32_t* out_time,
+                             uint32_t* out_len, uint64_t cap, uint64_t* n_out);
 
 // noalloc.cu
 bf_status query_batch_noalloc(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,

@@ -127,6 +127,8 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   for (uint32_t i = 0; i < n_r; ++i) c.rowmap[R[i]] = i;
   std::vector<uint4> items;
   std::vector<uint2> erec;
+  std::vector<uint32_t> elen;  // two-channel graphs: length weight per erec entry
+  const bool two = g->has_len;
   std::vector<uint32_t> split_bits((n_r + 31) / 32 + 1, 0);
   sc.lvl_item.assign(g->n_levels + 1, 0);
   uint32_t lvl = 0;
@@ -139,8 +141,10 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
       continue;
     }
     const uint32_t e0 = (uint32_t)erec.size();
-    for (uint64_t k = k0; k < k1; ++k)
+    for (uint64_t k = k0; k < k1; ++k) {
       erec.push_back(make_uint2(c.rowmap[g->h_in_rec[k].x], g->h_in_rec[k].y));
+      if (two) elen.push_back(g->h_in_len[k]);
+    }
     const uint32_t deg = (uint32_t)(k1 - k0);
     const uint32_t split = deg > SPLIT ? 1u : 0u;
     if (split) split_bits[i >> 5] |= 1u << (i & 31);
@@ -171,6 +175,7 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   if ((s = ensure(&sc.d_cidx, cap_c, n, g))) return s;
   if ((s = ensure(&sc.d_item, sc.cap_items, items.size(), g))) return s;
   if ((s = ensure(&sc.d_erec, sc.cap_edges, erec.size(), g))) return s;
+  if (two && (s = ensure(&sc.d_elen, sc.cap_elen, elen.size(), g))) return s;
   if ((s = ensure(&sc.d_trow, sc.cap_t, T, g))) return s;
   if ((s = ensure(&c.d_pairs, c.cap_pairs, pairs.size() * 2, g))) return s;
   if ((s = ensure(&sc.d_split, sc.cap_split, split_bits.size(), g))) return s;
@@ -197,6 +202,8 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   if (!erec.empty())
     BF_CUDA(cudaMemcpyAsync(sc.d_erec, erec.data(), erec.size() * sizeof(uint2),
                             cudaMemcpyHostToDevice, st));
+  if (!elen.empty())
+    BF_CUDA(cudaMemcpyAsync(sc.d_elen, elen.data(), elen.size() * 4, cudaMemcpyHostToDevice, st));
   if (T) BF_CUDA(cudaMemcpyAsync(sc.d_trow, trow.data(), T * 4, cudaMemcpyHostToDevice, st));
   BF_CUDA(cudaStreamSynchronize(st));  // host vectors are freed on return
   sc.ranks.swap(ranks);
@@ -415,7 +422,7 @@ uint64_t ctx_budget(Graph* g, Ctx& c) {
 }
 
 static void free_sched(Sched& sc) {
-  void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_trow, sc.d_split};
+  void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_elen, sc.d_trow, sc.d_split};
   for (void* q : p)
     if (q) cudaFree(q);
   if (sc.gexec) cudaGraphExecDestroy(sc.gexec);

@@ -21,22 +21,6 @@ namespace bf {
 
 namespace {
 
-// Ancestor path of `s` written into pn[0 .. D): runs of consecutive ranks are
-// emitted by the whole warp at once. Returns D (or 0 on inconsistency).
-__device__ uint32_t walk_path(uint32_t s, uint32_t D, const uint32_t* __restrict__ parent,
-                              const uint32_t* __restrict__ run_end, uint32_t* pn, uint32_t lane) {
-  uint32_t i = 0, x = s;
-  while (x != NONE) {
-    uint32_t e = run_end[x];
-    uint32_t len = e - x + 1;
-    if (i + len > D) return 0;
-    for (uint32_t l = lane; l < len; l += 32) pn[i + l] = x + l;
-    i += len;
-    x = parent[e];
-  }
-  return i == D ? D : 0;
-}
-
 template <bool GLOBAL_PATH>
 __device__ __forceinline__ uint32_t pd_load(const uint32_t* p) {
   if (GLOBAL_PATH) return __ldcg(p);

@@ -47,15 +47,21 @@ bf_status dev_upload(T** dptr, const T* src, size_t count, Graph* g) {
 
 }  // namespace
 
-static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, Graph* g);
+static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, Graph* g,
+                                  bool two, const uint32_t* up_len, const uint32_t* down_len);
 
 // The CCH of the transposed graph: UP'(x) = {(y, w) : DOWN edge y -> x},
 // DOWN'(y) = {(x, w) : UP edge x -> y}. Distances from t in it are the
 // distances to t in the original (the reference's reverse PHAST runs its
 // upward phase over DownReverseAdjFlat and pulls over UpAdjFlat,
 // route/src/range/phast.rs:879-1001).
-bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
-  if (!(cfg && (cfg->flags & BF_FLAG_REVERSE))) return build_graph_impl(csr, cfg, g);
+//
+// Length weights (two-channel graphs) travel with their edges.
+bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g,
+                      const uint32_t* up_len, const uint32_t* down_len) {
+  const bool two = up_len != nullptr;
+  if (!(cfg && (cfg->flags & BF_FLAG_REVERSE)))
+    return build_graph_impl(csr, cfg, g, two, up_len, down_len);
   const uint32_t n = csr->n_nodes;
   const uint64_t* uo = csr->up_offsets;
   const uint64_t* dno = csr->down_offsets;
@@ -88,18 +94,21 @@ bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
     rdo[v + 1] += rdo[v];
   }
   std::vector<uint32_t> rt(ro[n]), rw(ro[n]), rdt(rdo[n]), rdw(rdo[n]);
+  std::vector<uint32_t> rl(two ? ro[n] : 0), rdl(two ? rdo[n] : 0);
   {
     std::vector<uint64_t> f(ro.begin(), ro.end() - 1), fd(rdo.begin(), rdo.end() - 1);
     for (uint32_t y = 0; y < n; ++y)
       for (uint64_t k = dno[y]; k < dno[y + 1]; ++k) {
         const uint32_t x = csr->down_targets[k];
         rt[f[x]] = y;
+        if (two) rl[f[x]] = down_len[k];
         rw[f[x]++] = csr->down_weights[k];
       }
     for (uint32_t x = 0; x < n; ++x)
       for (uint64_t k = uo[x]; k < uo[x + 1]; ++k) {
         const uint32_t y = csr->up_targets[k];
         rdt[fd[y]] = x;
+        if (two) rdl[fd[y]] = up_len[k];
         rdw[fd[y]++] = csr->up_weights[k];
       }
   }
@@ -110,10 +119,11 @@ bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
   t.down_offsets = rdo.data();
   t.down_targets = rdt.data();
   t.down_weights = rdw.data();
-  return build_graph_impl(&t, cfg, g);
+  return build_graph_impl(&t, cfg, g, two, rl.data(), rdl.data());
 }
 
-static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, Graph* g) {
+static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, Graph* g,
+                                  bool two, const uint32_t* up_len, const uint32_t* down_len) {
   const uint32_t n = csr->n_nodes;
   g->n = n;
   const uint64_t* uo = csr->up_offsets;
@@ -123,6 +133,22 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
       set_error("CSR offsets must be non-decreasing");
       return BF_ERR_INVALID;
     }
+  if (two) {
+    // the reference indexes its length flats as aligned with the time flats,
+    // which holds only when both drop the same INF edges
+    for (uint64_t k = 0; k < uo[n]; ++k)
+      if ((csr->up_weights[k] == INF) != (up_len[k] == INF)) {
+        set_error("UP length weight " + std::to_string(k) +
+                  " is INF where the time weight is not (or the reverse)");
+        return BF_ERR_INVALID;
+      }
+    for (uint64_t k = 0; k < dno[n]; ++k)
+      if ((csr->down_weights[k] == INF) != (down_len[k] == INF)) {
+        set_error("DOWN length weight " + std::to_string(k) +
+                  " is INF where the time weight is not (or the reverse)");
+        return BF_ERR_INVALID;
+      }
+  }
   // finite UP / DOWN edges, validated
   std::vector<uint64_t> up_off(n + 1, 0), dn_cnt(n + 1, 0);
   for (uint32_t u = 0; u < n; ++u) {
@@ -152,7 +178,7 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
   std::vector<uint64_t> in_off_r(n + 1, 0);
   for (uint32_t v = 0; v < n; ++v) in_off_r[v + 1] = in_off_r[v] + dn_cnt[v + 1];
   g->n_down = in_off_r[n];
-  std::vector<uint32_t> in_src_r(g->n_down), in_w_r(g->n_down);
+  std::vector<uint32_t> in_src_r(g->n_down), in_w_r(g->n_down), in_l_r(two ? g->n_down : 0);
   {
     std::vector<uint64_t> f(in_off_r.begin(), in_off_r.end() - 1);
     for (uint32_t u = 0; u < n; ++u)
@@ -161,6 +187,7 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
         if (w == INF) continue;
         uint32_t t = csr->down_targets[k];
         in_src_r[f[t]] = u;
+        if (two) in_l_r[f[t]] = down_len[k];
         in_w_r[f[t]++] = w;
       }
   }
@@ -211,12 +238,14 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
   g->max_depth = maxd;
   // UP records
   std::vector<uint2> up_rec(g->n_up);
+  std::vector<uint32_t> up_l(two ? g->n_up : 0);
   for (uint32_t u = 0; u < n; ++u) {
     uint64_t p = up_off[u];
     for (uint64_t k = uo[u]; k < uo[u + 1]; ++k) {
       uint32_t w = csr->up_weights[k];
       if (w == INF) continue;
       uint32_t v = csr->up_targets[k];
+      if (two) up_l[p] = up_len[k];
       up_rec[p++] = make_uint2(depth[u] - depth[v], w);
     }
   }
@@ -250,13 +279,22 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
     in_off[p + 1] = in_off[p] + (in_off_r[v + 1] - in_off_r[v]);
   }
   std::vector<uint2> in_rec(g->n_down);
+  std::vector<uint32_t> in_len(two ? g->n_down : 0);
+  std::vector<uint64_t> ord;
   for (uint32_t p = 0; p < n; ++p) {
     uint32_t v = rank_at[p];
+    const uint64_t k0 = in_off_r[v], k1 = in_off_r[v + 1];
+    // sources in ascending position; the sort key carries the edge index so
+    // the length weight follows its edge
+    ord.clear();
+    for (uint64_t k = k0; k < k1; ++k) ord.push_back(((uint64_t)g->pos_of[in_src_r[k]] << 32) | (k - k0));
+    std::sort(ord.begin(), ord.end());
     uint64_t q = in_off[p];
-    for (uint64_t k = in_off_r[v]; k < in_off_r[v + 1]; ++k)
-      in_rec[q++] = make_uint2(g->pos_of[in_src_r[k]], in_w_r[k]);
-    std::sort(in_rec.begin() + in_off[p], in_rec.begin() + in_off[p + 1],
-              [](const uint2& a, const uint2& b) { return a.x < b.x; });
+    for (uint64_t o : ord) {
+      const uint64_t k = k0 + (uint32_t)o;
+      if (two) in_len[q] = in_l_r[k];
+      in_rec[q++] = make_uint2((uint32_t)(o >> 32), in_w_r[k]);
+    }
   }
 
   // device
@@ -270,6 +308,7 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
   if ((s = dev_upload(&g->d_depth, depth.data(), n, g))) return s;
   if ((s = dev_upload(&g->d_up_off, up_off.data(), n + 1, g))) return s;
   if ((s = dev_upload(&g->d_up_rec, up_rec.data(), up_rec.size(), g))) return s;
+  if (two && (s = dev_upload(&g->d_up_len, up_l.data(), up_l.size(), g))) return s;
   if ((s = dev_upload(&g->d_pos_of, g->pos_of.data(), n, g))) return s;
   if ((s = dev_upload(&g->d_rank_at, rank_at.data(), n, g))) return s;
   if ((s = dev_upload(&g->d_in_off, in_off.data(), n + 1, g))) return s;
@@ -279,6 +318,8 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
   g->rank_at = std::move(rank_at);
   g->h_in_off = std::move(in_off);
   g->h_in_rec = std::move(in_rec);
+  g->h_in_len = std::move(in_len);
+  g->has_len = two;
   (void)cfg;
   return BF_OK;
 }
@@ -286,7 +327,7 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
 void free_graph(Graph* g) {
   if (!g) return;
   cudaSetDevice(g->device);
-  void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec,
+  void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec, g->d_up_len,
                   g->d_pos_of,  g->d_rank_at, g->d_in_off, g->d_in_rec, g->d_dist,
                   g->d_seed,    g->d_flag,    g->d_err,    g->d_gpath,  g->d_io,
                   g->d_iso};

@@ -18,6 +18,9 @@
  *                          (and compute_matrix_flat_soa :756, compute_matrix_block_gated :1223)
  *   bf_matrix_seeded       table_phast_lopsided                      route/src/matrix/bucket_ch.rs:6717
  *   bf_phast_bounded_seeded run_phast_bounded_fast_seeded            route/src/server/isochrone_handler.rs:338
+ *   bf_graph_create_2ch    the optional len-along-time flats         route/src/server/state.rs:2962
+ *   bf_matrix_seeded_2ch   table_phast_lopsided_2ch                  bucket_ch.rs:6381-6521
+ *   bf_phast_bounded_seeded_2ch run_phast_bounded_fast_seeded_2ch    isochrone_handler.rs:500-625
  *   bf_isochrone_bitsets   the PHAST part of isochrone_bulk_handler  isochrone_handler.rs:1668-1709
  *                          and BatchedIsochroneEngine::query_many    route/src/range/batched_isochrone.rs:216
  *   bf_server_*            the tiling / admission loop of do_matrix  route/src/server/flight.rs:589,957-1110
@@ -239,6 +242,46 @@ bf_status bf_matrix_seeded(bf_graph* g, const bf_seed* src_seeds, const uint64_t
 bf_status bf_phast_bounded_seeded(bf_graph* g, const bf_seed* seeds, uint32_t n_seeds,
                                   uint32_t threshold, uint32_t* out_rank, uint32_t* out_dist,
                                   uint64_t cap, uint64_t* n_out);
+
+/* ---- two channels: time and length along the time-optimal path ----------
+ * A graph created with bf_graph_create_2ch also carries a length weight per
+ * CCH edge (the reference's cch_weights_len_along_time, same indexing as the
+ * time weights). Both channels follow the same path: labels are compared by
+ * time, ties by length (the reference's lexicographic tie-break,
+ * isochrone_handler.rs:543-571, :599-611). The length weights must be
+ * 0xFFFFFFFF exactly where the time weights are (the reference's length flats
+ * drop INF edges independently and index them as aligned with the time
+ * flats); otherwise BF_ERR_INVALID. The 2ch calls return BF_ERR_UNSUPPORTED
+ * on a graph created without lengths. */
+bf_status bf_graph_create_2ch(const bf_cch_csr* csr, const uint32_t* up_len_weights,
+                              const uint32_t* down_len_weights, const bf_config* cfg,
+                              bf_graph** out);
+
+/* A two-channel seed: (rank, time cost, length cost), the reference's
+ * EngineSeed (rank, part_time, part_len) (bucket_ch.rs:6039). */
+typedef struct bf_seed2 {
+  uint32_t rank;
+  uint32_t cost;
+  uint32_t len;
+} bf_seed2;
+
+/* table_phast_lopsided_2ch: out_time as bf_matrix_seeded; out_len[s*T + t] is
+ * F_len[rank] - part_len of the first target seed (in the given order) that
+ * attains the cell's time, BF_INF where the time cell is BF_INF. Several
+ * seeds of one source on the same rank keep the first with the smallest
+ * cost (isochrone_handler.rs:527-531). Conflicts as in bf_matrix_seeded; both
+ * cells stay BF_INF there. */
+bf_status bf_matrix_seeded_2ch(bf_graph* g, const bf_seed2* src_seeds, const uint64_t* src_off,
+                               uint64_t n_sources, const bf_seed2* tgt_seeds,
+                               const uint64_t* tgt_off, uint64_t n_targets, uint32_t threshold,
+                               uint32_t* out_time, uint32_t* out_len, uint64_t* conflict_cells,
+                               uint64_t conflict_cap, uint64_t* n_conflicts, bf_stats* st);
+
+/* run_phast_bounded_fast_seeded_2ch: settled (rank, time <= threshold, len)
+ * triples in ascending rank order; at most cap written, *n_out = total. */
+bf_status bf_phast_bounded_seeded_2ch(bf_graph* g, const bf_seed2* seeds, uint32_t n_seeds,
+                                      uint32_t threshold, uint32_t* out_rank, uint32_t* out_time,
+                                      uint32_t* out_len, uint64_t cap, uint64_t* n_out);
 
 /* Bulk isochrones: origin i with threshold thresholds[i]; bit r of row i
  * (rows of ceil(n_nodes / 64) u64 words) is set iff dist(origin_i, r) <=

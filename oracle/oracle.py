@@ -34,6 +34,10 @@ def load():
         lib.orc_phast_bounded_seeded.argtypes = csr + [_V, _V, ctypes.c_uint32, ctypes.c_uint32,
                                                        _V, _V, ctypes.c_uint64]
         lib.orc_phast_bounded_seeded.restype = ctypes.c_uint64
+        lib.orc_phast_bounded_seeded_2ch.argtypes = csr + [_V, _V, _V, _V, _V, ctypes.c_uint32,
+                                                           ctypes.c_uint32, _V, _V, _V,
+                                                           ctypes.c_uint64]
+        lib.orc_phast_bounded_seeded_2ch.restype = ctypes.c_uint64
         lib.orc_isochrone_bitsets.argtypes = csr + [_V, _V, ctypes.c_uint64, _V, _V, ctypes.c_int]
         lib.orc_dijkstra_ebg.argtypes = [ctypes.c_uint32, _V, _V, _V, ctypes.c_uint32, _V]
         lib.orc_phast_reverse.argtypes = csr + [ctypes.c_uint32, _V]
@@ -96,6 +100,22 @@ class Cch:
         cnt = load().orc_phast_bounded_seeded(*self._csr(), r.ctypes.data, c.ctypes.data, len(r),
                                               threshold, rk.ctypes.data, ds.ctypes.data, self.n)
         return rk[:cnt].copy(), ds[:cnt].copy()
+
+    def bounded_seeded_2ch(self, seeds, threshold, up_len, down_len):
+        """run_phast_bounded_fast_seeded_2ch: (ranks, times, lengths) with
+        time <= threshold; seeds are (rank, time cost, length cost)."""
+        r = _a([x[0] for x in seeds], np.uint32)
+        c = _a([x[1] for x in seeds], np.uint32)
+        ln = _a([x[2] for x in seeds], np.uint32)
+        ul, dl = _a(up_len, np.uint32), _a(down_len, np.uint32)
+        rk = np.empty(self.n, dtype=np.uint32)
+        tm = np.empty(self.n, dtype=np.uint32)
+        lo = np.empty(self.n, dtype=np.uint32)
+        cnt = load().orc_phast_bounded_seeded_2ch(*self._csr(), ul.ctypes.data, dl.ctypes.data,
+                                                  r.ctypes.data, c.ctypes.data, ln.ctypes.data,
+                                                  len(r), threshold, rk.ctypes.data,
+                                                  tm.ctypes.data, lo.ctypes.data, self.n)
+        return rk[:cnt].copy(), tm[:cnt].copy(), lo[:cnt].copy()
 
     def isochrone_bitsets(self, origins, thresholds, threads=0):
         o, t = _a(origins, np.uint32), _a(thresholds, np.uint32)
@@ -178,3 +198,46 @@ def table_phast_lopsided(cch, src_seedsets, tgt_seedsets, threshold):
                 best = INF
             out[s, t] = best
     return out, np.array(sorted(conflicts), dtype=np.uint64)
+
+
+def table_phast_lopsided_2ch(cch, src_seedsets, tgt_seedsets, threshold, up_len, down_len):
+    """table_phast_lopsided_2ch (route/src/matrix/bucket_ch.rs:6381-6521): per
+    source one run_phast_bounded_fast_seeded_2ch field (bound as in the
+    one-channel form, :6409-6418, from the seeds' time parts); per target,
+    over its seeds in order, the first with the strictly smallest
+    F_t[rank] - part_t (saturating) also gives F_l[rank] - part_l (:6452-6466);
+    time cells above T -> INF in both channels (:6467-6470). Same-rank pairs
+    are conflicts (:6460-6463), INF in both matrices."""
+    S, T = len(src_seedsets), len(tgt_seedsets)
+    out_t = np.full((S, T), INF, dtype=np.uint32)
+    out_l = np.full((S, T), INF, dtype=np.uint32)
+    max_tgt = max([p for ss in tgt_seedsets for _, p, _ in ss] or [0])
+    conflicts = []
+    for s, seeds in enumerate(src_seedsets):
+        if not seeds:
+            continue
+        if threshold == INF:
+            bound = INF
+        else:
+            bound = min(INF, threshold + max(c for _, c, _ in seeds) + max_tgt)
+        rk, tm, ln = cch.bounded_seeded_2ch(seeds, bound, up_len, down_len)
+        field = {int(r): (int(a), int(b)) for r, a, b in zip(rk, tm, ln)}
+        src_ranks = {r for r, _, _ in seeds}
+        for t, tseeds in enumerate(tgt_seedsets):
+            if not tseeds:
+                continue
+            if any(r in src_ranks for r, _, _ in tseeds):
+                conflicts.append(s * T + t)
+                continue
+            bt, bl = INF, INF
+            for r, pt, pl in tseeds:
+                f = field.get(r)
+                if f is not None and f[0] != INF:
+                    at = f[0] - pt if f[0] > pt else 0
+                    if at < bt:
+                        bt = at
+                        bl = f[1] - pl if f[1] > pl else 0
+            if threshold != INF and bt != INF and bt > threshold:
+                bt, bl = INF, INF
+            out_t[s, t], out_l[s, t] = bt, bl
+    return out_t, out_l, np.array(sorted(conflicts), dtype=np.uint64)

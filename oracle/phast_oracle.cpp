@@ -303,6 +303,96 @@ u64 orc_phast_bounded_seeded(u32 n, const u64* up_off, const u32* up_tgt, const 
   return cnt;
 }
 
+// run_phast_bounded_fast_seeded_2ch — route/src/server/isochrone_handler.rs:500-625.
+// As orc_phast_bounded_seeded with a length-along-time channel carried in
+// lockstep: seeds (rank, time, len) enter only when their time is below the
+// rank's current time (:527-531); relaxations adopt a strictly smaller time,
+// or an equal finite time with a strictly shorter length, and re-push in the
+// upward phase (:543-571, lazy lexicographic tie-break); the downward scan
+// applies the same rule without re-push (:592-612). up_l / dn_l are the
+// length weights aligned with up_w / dn_w; edges with time INF are absent
+// from the reference flats and skipped here. Writes up to `cap` triples in
+// ascending rank; returns the number of settled nodes (time <= threshold).
+u64 orc_phast_bounded_seeded_2ch(u32 n, const u64* up_off, const u32* up_tgt, const u32* up_w,
+                                 const u64* dn_off, const u32* dn_tgt, const u32* dn_w,
+                                 const u32* up_l, const u32* dn_l, const u32* seed_rank,
+                                 const u32* seed_cost, const u32* seed_len, u32 n_seeds,
+                                 u32 threshold, u32* out_rank, u32* out_time, u32* out_len,
+                                 u64 cap) {
+  const u32 BS = 4096;
+  u32 nb = (n + BS - 1) / BS;
+  std::vector<u32> dist(n, INF), len(n, INF);
+  std::vector<uint8_t> version(n, 0), block(nb, 0);
+  auto get = [&](u32 v) { return version[v] ? dist[v] : INF; };
+  auto get_len = [&](u32 v) { return version[v] ? len[v] : INF; };
+  auto set = [&](u32 v, u32 d, u32 l) {
+    dist[v] = d;
+    len[v] = l;
+    version[v] = 1;
+    block[v / BS] = 1;
+  };
+  for (u32 i = 0; i < n_seeds; ++i)
+    if (seed_cost[i] < get(seed_rank[i])) set(seed_rank[i], seed_cost[i], seed_len[i]);
+  MinHeap pq;
+  for (u32 i = 0; i < n_seeds; ++i)
+    if (get(seed_rank[i]) == seed_cost[i]) pq.push({seed_cost[i], seed_rank[i]});
+  while (!pq.empty()) {
+    auto [d, u] = pq.top();
+    pq.pop();
+    if (d > threshold) break;
+    if (d > get(u)) continue;
+    const u32 lu = get_len(u);
+    for (u64 i = up_off[u]; i < up_off[u + 1]; ++i) {
+      if (up_w[i] == INF) continue;
+      const u32 v = up_tgt[i], nt = sat_add(d, up_w[i]), ct = get(v);
+      if (nt < ct) {
+        set(v, nt, sat_add(lu, up_l[i]));
+        pq.push({nt, v});
+      } else if (nt == ct && ct != INF) {
+        const u32 nl = sat_add(lu, up_l[i]);
+        if (nl < get_len(v)) {
+          set(v, nt, nl);
+          pq.push({nt, v});
+        }
+      }
+    }
+  }
+  for (u32 b = nb; b-- > 0;) {
+    if (!block[b]) continue;
+    u32 lo = b * BS, hi = std::min(n, lo + BS);
+    for (u32 r = hi; r-- > lo;) {
+      const u32 du = get(r);
+      if (du == INF || du > threshold) continue;
+      const u32 lu = get_len(r);
+      for (u64 i = dn_off[r]; i < dn_off[r + 1]; ++i) {
+        if (dn_w[i] == INF) continue;
+        const u32 v = dn_tgt[i], nt = sat_add(du, dn_w[i]), ct = get(v);
+        if (nt < ct) {
+          set(v, nt, sat_add(lu, dn_l[i]));
+        } else if (nt == ct && ct != INF) {
+          const u32 nl = sat_add(lu, dn_l[i]);
+          if (nl < get_len(v)) set(v, nt, nl);
+        }
+      }
+    }
+  }
+  u64 cnt = 0;
+  for (u32 b = 0; b < nb; ++b) {
+    if (!block[b]) continue;
+    u32 lo = b * BS, hi = std::min(n, lo + BS);
+    for (u32 r = lo; r < hi; ++r)
+      if (version[r] && dist[r] <= threshold) {
+        if (cnt < cap) {
+          out_rank[cnt] = r;
+          out_time[cnt] = dist[r];
+          out_len[cnt] = len[r];
+        }
+        ++cnt;
+      }
+  }
+  return cnt;
+}
+
 // Bulk isochrone reachable sets: for origin i, bit r of row i is set iff rank
 // r is settled with d <= T_i by run_phast_bounded_fast_seeded (the
 // `reachable_edges` set of isochrone_handler.rs:1271-1278). Rows are

@@ -13,6 +13,9 @@ reference_kats.json
       * route/src/matrix/bucket_ch.rs:5619-5700  broom graph, closed-form
         matrix d(s,t) = wu[s] + wd[t] (0 on the diagonal) with the bounded
         thresholds the tests sweep (:5721-5760)
+      * route/src/server/isochrone_handler.rs:1806-1869  two-channel
+        lexicographic tie (phast_2ch_lex_tests): two equal-time paths to node
+        3, the shorter length must win whichever path pops first
 
 grid100_matrix.npz
     The 100 x 100 matrix of the 100 x 100 synthetic grid computed by the CPU
@@ -76,6 +79,21 @@ def kats():
             "finite_down": 3,
         },
         "broom": {"source": "route/src/matrix/bucket_ch.rs:5619-5760", **broom},
+        "two_channel_tie": {
+            "source": "route/src/server/isochrone_handler.rs:1806-1869",
+            "cases": [
+                # shorter length arrives second (:1806-1845)
+                dict(cch=dict(n=4, up_off=[0, 2, 3, 4, 4], up_tgt=[1, 2, 3, 3], up_w=[3, 5, 7, 5],
+                              down_off=[0, 0, 0, 0, 0], down_tgt=[], down_w=[]),
+                     up_len=[100, 1, 100, 1], down_len=[], seeds=[[0, 0, 0]], threshold=1000,
+                     node=3, time=10, len=2),
+                # shorter length arrives first (:1847-1868)
+                dict(cch=dict(n=4, up_off=[0, 2, 3, 4, 4], up_tgt=[1, 2, 3, 3], up_w=[5, 3, 5, 7],
+                              down_off=[0, 0, 0, 0, 0], down_tgt=[], down_w=[]),
+                     up_len=[100, 1, 100, 1], down_len=[], seeds=[[0, 0, 0]], threshold=1000,
+                     node=3, time=10, len=2),
+            ],
+        },
     }
 
 

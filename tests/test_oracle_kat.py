@@ -144,3 +144,28 @@ def test_grid100_golden_matches_oracle(built, grid100):
     _, cch = grid100
     m, _ = orc.Cch.from_dict(cch).matrix(g["sources"], g["targets"], threads=2)
     assert np.array_equal(m, g["matrix"])
+
+
+def test_two_channel_lexicographic_tie(built, kats):
+    # route/src/server/isochrone_handler.rs:1806-1869 (phast_2ch_lex_tests):
+    # node 3 has two time-10 paths; the shorter length (2) wins in both pop orders
+    for case in kats["two_channel_tie"]["cases"]:
+        c = _cch(case["cch"])
+        rk, tm, ln = c.bounded_seeded_2ch([tuple(x) for x in case["seeds"]], case["threshold"],
+                                          case["up_len"], case["down_len"])
+        i = rk.tolist().index(case["node"])
+        assert (tm[i], ln[i]) == (case["time"], case["len"])
+
+
+def test_two_channel_time_matches_one_channel(built, grid100):
+    # the time channel of the 2-channel field is the 1-channel field
+    # (isochrone_handler.rs:500-506: "Mirrors run_phast_bounded_fast_seeded
+    # exactly on the time side"); with length == time both channels agree
+    _, cch = grid100
+    c = orc.Cch.from_dict(cch)
+    seeds = [(17, 0, 0), (4000, 35, 35), (4000, 20, 20)]
+    for thr in (900, 5000, INF):
+        rk1, d1 = c.bounded_seeded([(r, t) for r, t, _ in seeds], thr)
+        rk2, tm, ln = c.bounded_seeded_2ch(seeds, thr, cch["up_w"], cch["down_w"])
+        assert np.array_equal(rk1, rk2) and np.array_equal(d1, tm)
+        assert np.array_equal(tm, ln)
