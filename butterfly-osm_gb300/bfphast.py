@@ -81,6 +81,14 @@ class Seed2(ctypes.Structure):
     _fields_ = [("rank", ctypes.c_uint32), ("cost", ctypes.c_uint32), ("len", ctypes.c_uint32)]
 
 
+class Router(ctypes.Structure):
+    _fields_ = [("sweep_ns", ctypes.c_uint64), ("scan_ns", ctypes.c_uint64)]
+
+
+COST_SWEEP, COST_SCAN = 0, 1
+ROUTE_AUTO, ROUTE_BUCKET, ROUTE_PHAST = 0, 1, 2
+
+
 class ServerCfg(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
                 ("max_queue", ctypes.c_uint32), ("timeout_ms", ctypes.c_uint32),
@@ -140,6 +148,10 @@ _SIGNATURES = {
     "bf_phast_bounded_seeded_2ch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Seed2),
                                                    ctypes.c_uint32, ctypes.c_uint32, _u32p,
                                                    _u32p, _u32p, ctypes.c_uint64, _u64p]),
+    "bf_router_observe": (None, [ctypes.POINTER(Router), ctypes.c_uint32, ctypes.c_uint64]),
+    "bf_router_observe_stats": (None, [ctypes.POINTER(Router), ctypes.POINTER(Stats)]),
+    "bf_router_phast_wins": (ctypes.c_int, [ctypes.POINTER(Router), ctypes.c_uint64,
+                                            ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32]),
     "bf_isochrone_bitsets": (ctypes.c_int, [ctypes.c_void_p, _u32p, _u32p, ctypes.c_uint64,
                                             _u64p, _u64p, ctypes.POINTER(Stats)]),
     "bf_isochrone_bitsets_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p,

@@ -605,6 +605,49 @@ bf_status bf_phast_bounded_seeded_2ch(bf_graph* h, const bf_seed2* seeds, uint32
   }
 }
 
+// update_cost_ewma (bucket_ch.rs:6663-6671): the first sample is taken as is,
+// later ones move the estimate by a quarter; never below 1.
+void bf_router_observe(bf_router* r, uint32_t which, uint64_t sample_ns) {
+  if (!r || which > BF_COST_SCAN) return;
+  uint64_t* cell = which == BF_COST_SWEEP ? &r->sweep_ns : &r->scan_ns;
+  uint64_t prev = __atomic_load_n(cell, __ATOMIC_RELAXED);
+  for (;;) {
+    uint64_t next = prev == 0 ? sample_ns : prev - prev / 4 + sample_ns / 4;
+    if (next < 1) next = 1;
+    if (__atomic_compare_exchange_n(cell, &prev, next, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED))
+      return;
+  }
+}
+
+// The GPU computes every source's field in one call: its per-source share of
+// the call is the scan cost the router compares against bucket sweeps.
+void bf_router_observe_stats(bf_router* r, const bf_stats* st) {
+  if (!r || !st || st->n_sources == 0 || !(st->total_ms > 0)) return;
+  const double ns = st->total_ms * 1e6 / (double)st->n_sources;
+  bf_router_observe(r, BF_COST_SCAN, ns < 1.0 ? 1 : (uint64_t)ns);
+}
+
+// phast_wins (bucket_ch.rs:6677-6712).
+int bf_router_phast_wins(const bf_router* r, uint64_t n_sources, uint64_t n_targets,
+                         uint64_t n_nodes, uint32_t force) {
+  if (force == BF_ROUTE_BUCKET) return 0;
+  if (force == BF_ROUTE_PHAST) return n_sources <= n_targets;
+  if (n_sources > n_targets) return 0;
+  const uint64_t sweep = r ? __atomic_load_n(&r->sweep_ns, __ATOMIC_RELAXED) : 0;
+  const uint64_t scan = r ? __atomic_load_n(&r->scan_ns, __ATOMIC_RELAXED) : 0;
+  unsigned __int128 scan_cost, sweep_cost;
+  if (sweep > 0 && scan > 0) {
+    scan_cost = scan;
+    sweep_cost = sweep;
+  } else {
+    scan_cost = n_nodes;
+    sweep_cost = std::min<uint64_t>(std::max<uint64_t>(n_nodes / 400, 500), 20000);
+  }
+  const unsigned __int128 phast = (unsigned __int128)n_sources * scan_cost;
+  const unsigned __int128 bucket = (unsigned __int128)(n_sources + n_targets) * sweep_cost;
+  return phast < bucket ? 1 : 0;
+}
+
 bf_status bf_isochrone_bitsets_device(bf_graph* h, const uint32_t* d_orig, const uint32_t* d_thr,
                                       uint64_t n, uint64_t* d_bits, uint64_t* d_counts,
                                       void* stream, bf_stats* st) {

@@ -19,6 +19,7 @@
  *   bf_matrix_seeded       table_phast_lopsided                      route/src/matrix/bucket_ch.rs:6717
  *   bf_phast_bounded_seeded run_phast_bounded_fast_seeded            route/src/server/isochrone_handler.rs:338
  *   bf_graph_create_2ch    the optional len-along-time flats         route/src/server/state.rs:2962
+ *   bf_router_*            phast_wins / update_cost_ewma             bucket_ch.rs:6655-6712
  *   bf_matrix_seeded_2ch   table_phast_lopsided_2ch                  bucket_ch.rs:6381-6521
  *   bf_phast_bounded_seeded_2ch run_phast_bounded_fast_seeded_2ch    isochrone_handler.rs:500-625
  *   bf_isochrone_bitsets   the PHAST part of isochrone_bulk_handler  isochrone_handler.rs:1668-1709
@@ -282,6 +283,28 @@ bf_status bf_matrix_seeded_2ch(bf_graph* g, const bf_seed2* src_seeds, const uin
 bf_status bf_phast_bounded_seeded_2ch(bf_graph* g, const bf_seed2* seeds, uint32_t n_seeds,
                                       uint32_t threshold, uint32_t* out_rank, uint32_t* out_time,
                                       uint32_t* out_len, uint64_t cap, uint64_t* n_out);
+
+/* ---- router cost model (phast_wins, bucket_ch.rs:6655-6712) ---------------
+ * Chooses between the seeded PHAST matrix and the caller's bucket engine:
+ * PHAST iff n_sources <= n_targets and n_sources * scan < (n_sources +
+ * n_targets) * sweep, with scan / sweep the EWMA (alpha 1/4) of measured
+ * per-field and per-sweep nanoseconds, or before both are measured the
+ * structural bound scan = n_nodes, sweep = clamp(n_nodes / 400, 500, 20000).
+ * One bf_router per process replaces the reference's two static atomics;
+ * updates and reads are atomic. Feed the GPU's cost with
+ * bf_router_observe_stats (the per-source share of a bf_matrix_seeded call)
+ * and the bucket engine's with BF_COST_SWEEP samples. `force` carries the
+ * caller's BUTTERFLY_MATRIX_ALGO override. Returns 1 for PHAST, 0 for bucket. */
+typedef struct bf_router {
+  uint64_t sweep_ns;  /* 0 = not measured yet */
+  uint64_t scan_ns;
+} bf_router;
+enum { BF_COST_SWEEP = 0, BF_COST_SCAN = 1 };
+enum { BF_ROUTE_AUTO = 0, BF_ROUTE_BUCKET = 1, BF_ROUTE_PHAST = 2 };
+void bf_router_observe(bf_router* r, uint32_t which, uint64_t sample_ns);
+void bf_router_observe_stats(bf_router* r, const bf_stats* st);
+int bf_router_phast_wins(const bf_router* r, uint64_t n_sources, uint64_t n_targets,
+                         uint64_t n_nodes, uint32_t force);
 
 /* Bulk isochrones: origin i with threshold thresholds[i]; bit r of row i
  * (rows of ceil(n_nodes / 64) u64 words) is set iff dist(origin_i, r) <=
