@@ -67,7 +67,8 @@ class Tune(ctypes.Structure):
     _fields_ = [("threads_per_block", ctypes.c_uint32), ("edges_per_item", ctypes.c_uint32),
                 ("graph_capture", ctypes.c_uint32), ("lanes_per_wave", ctypes.c_uint32),
                 ("step_ms", ctypes.c_double), ("tried", ctypes.c_uint32),
-                ("isochrone_lanes", ctypes.c_uint32)]
+                ("isochrone_lanes", ctypes.c_uint32), ("small_level_rows", ctypes.c_uint32),
+                ("small_level_edges", ctypes.c_uint32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -270,9 +271,10 @@ class Graph:
         return t.as_dict()
 
     def set_tune(self, threads_per_block=128, edges_per_item=16, graph_capture=1,
-                 lanes_per_wave=0, isochrone_lanes=1024):
+                 lanes_per_wave=0, isochrone_lanes=1024, small_level_rows=0,
+                 small_level_edges=4):
         t = Tune(threads_per_block, edges_per_item, graph_capture, lanes_per_wave, 0.0, 0,
-                 isochrone_lanes)
+                 isochrone_lanes, small_level_rows, small_level_edges)
         _check(load().bf_set_tune(self._h, ctypes.byref(t)))
 
     def get_tune(self):

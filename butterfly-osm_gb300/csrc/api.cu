@@ -256,6 +256,8 @@ static bf_tune to_c(const Tune& t) {
   o.graph_capture = t.graphs;
   o.lanes_per_wave = t.max_lanes;
   o.isochrone_lanes = t.iso_lanes;
+  o.small_level_rows = t.small_rows;
+  o.small_level_edges = t.small_split;
   return o;
 }
 
@@ -264,7 +266,8 @@ bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
                    t->threads_per_block != 128 && t->threads_per_block != 256) ||
       t->edges_per_item == 0 || t->edges_per_item > 1024 ||
       (t->lanes_per_wave && t->lanes_per_wave % 32) ||
-      (t->isochrone_lanes && t->isochrone_lanes % 32)) {
+      (t->isochrone_lanes && t->isochrone_lanes % 32) ||
+      (t->small_level_rows && (t->small_level_edges == 0 || t->small_level_edges > 1024))) {
     set_error("bf_set_tune: invalid tunables");
     return BF_ERR_INVALID;
   }
@@ -274,6 +277,8 @@ bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
   h->g.tune.graphs = t->graph_capture ? 1 : 0;
   h->g.tune.max_lanes = t->lanes_per_wave;
   h->g.tune.iso_lanes = t->isochrone_lanes;
+  h->g.tune.small_rows = t->small_level_rows;
+  h->g.tune.small_split = t->small_level_rows ? t->small_level_edges : 4;
   return BF_OK;
 }
 
@@ -336,10 +341,34 @@ bf_status bf_autotune(bf_graph* h, const uint32_t* d_src, uint64_t S, const uint
       best_t = t;
     }
   }
+  // second stage: short work items on the small top levels, on the winner
+  uint32_t tried = (uint32_t)cands.size();
+  for (uint32_t rows : {64u, 1024u}) {
+    Tune t = best_t;
+    t.small_rows = rows;
+    t.small_split = 8;
+    g->tune = t;
+    double sum = 0;
+    for (uint32_t r = 0; r <= reps; ++r) {
+      bf_stats st{};
+      rc = batched_matrix(g, g->ctx, d_src, S, d_tgt, T, BF_INF, out.as<uint32_t>(), s, &st);
+      if (rc == BF_OK) rc = check_device_error(g, s);
+      if (rc != BF_OK) {
+        g->tune = saved;
+        return rc;
+      }
+      if (r) sum += st.upward_ms + st.downward_ms + st.extract_ms;
+    }
+    ++tried;
+    if (sum / reps < best_ms) {
+      best_ms = sum / reps;
+      best_t = t;
+    }
+  }
   g->tune = best_t;
   *best = to_c(best_t);
   best->step_ms = best_ms;
-  best->tried = (uint32_t)cands.size();
+  best->tried = tried;
   return BF_OK;
 }
 

@@ -110,6 +110,8 @@ struct Tune {
   uint32_t graphs = 1;       // replay the level schedule from a CUDA graph
   uint32_t max_lanes = 0;    // lanes per wave (0 = as many as the budget allows)
   uint32_t iso_lanes = 1024; // isochrone origins per wave (spatially compact waves)
+  uint32_t small_rows = 0;   // levels with fewer rows use small_split edges per item
+  uint32_t small_split = 4;
 };
 
 struct Graph {

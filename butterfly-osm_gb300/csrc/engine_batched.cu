@@ -78,8 +78,11 @@ __global__ void k_scatter_pairs(const uint2* __restrict__ pr, uint64_t m,
 bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
                          cudaStream_t st) {
   const uint32_t SPLIT = std::max<uint32_t>(1, g->tune.split);
+  const uint32_t SMALL_ROWS = g->tune.small_rows;
+  const uint32_t SMALL_SPLIT = std::max<uint32_t>(1, std::min(SPLIT, g->tune.small_split));
   const uint64_t key = (all ? 0x9E3779B97F4A7C15ull : hash_targets(h_tgt, T)) ^
-                       ((uint64_t)SPLIT << 56);
+                       ((uint64_t)SPLIT << 56) ^ ((uint64_t)SMALL_SPLIT << 48) ^
+                       ((uint64_t)SMALL_ROWS << 20);
   if (sc.valid && sc.key == key && sc.T == T) {
     ++sc.uses;
     return BF_OK;
@@ -131,10 +134,29 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   const bool two = g->has_len;
   std::vector<uint32_t> split_bits((n_r + 31) / 32 + 1, 0);
   sc.lvl_item.assign(g->n_levels + 1, 0);
+  // rows per level of the restricted set: small levels get short work items
+  std::vector<uint32_t> lvl_rows(g->n_levels + 1, 0);
+  {
+    uint32_t l = 0;
+    for (uint32_t i = 0; i < n_r; ++i) {
+      while (R[i] >= g->lvl_start[l + 1]) ++l;
+      ++lvl_rows[l];
+    }
+  }
+  // items of a level, heaviest first, so the level's last blocks are short
+  auto close_level = [&](uint32_t l) {
+    std::stable_sort(items.begin() + sc.lvl_item[l], items.end(),
+                     [](const uint4& a, const uint4& b) { return a.z - a.y > b.z - b.y; });
+  };
   uint32_t lvl = 0;
+  uint32_t split_l = lvl_rows[0] < SMALL_ROWS ? SMALL_SPLIT : SPLIT;
   for (uint32_t i = 0; i < n_r; ++i) {
     const uint32_t p = R[i];
-    while (p >= g->lvl_start[lvl + 1]) sc.lvl_item[++lvl] = (uint32_t)items.size();
+    while (p >= g->lvl_start[lvl + 1]) {
+      close_level(lvl);
+      sc.lvl_item[++lvl] = (uint32_t)items.size();
+      split_l = lvl_rows[lvl] < SMALL_ROWS ? SMALL_SPLIT : SPLIT;
+    }
     const uint64_t k0 = g->h_in_off[p], k1 = g->h_in_off[p + 1];
     if (k0 == k1) {  // no in-edges: the row is its seed (or INF): reset every wave
       split_bits[i >> 5] |= 1u << (i & 31);
@@ -146,11 +168,12 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
       if (two) elen.push_back(g->h_in_len[k]);
     }
     const uint32_t deg = (uint32_t)(k1 - k0);
-    const uint32_t split = deg > SPLIT ? 1u : 0u;
+    const uint32_t split = deg > split_l ? 1u : 0u;
     if (split) split_bits[i >> 5] |= 1u << (i & 31);
-    for (uint32_t a = 0; a < deg; a += SPLIT)
-      items.push_back(make_uint4(i, e0 + a, e0 + std::min(deg, a + SPLIT), split));
+    for (uint32_t a = 0; a < deg; a += split_l)
+      items.push_back(make_uint4(i, e0 + a, e0 + std::min(deg, a + split_l), split));
   }
+  close_level(lvl);
   while (lvl < g->n_levels) sc.lvl_item[++lvl] = (uint32_t)items.size();
   if (erec.size() > 0xFFFFFFFFull) {
     for (uint32_t p : R) c.rowmap[p] = NONE;
@@ -218,6 +241,24 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
 
 namespace {
 
+// min-combine one warp's 128 lanes (thread t holds lanes 4t..4t+3 of the
+// group starting at wbase) into a row with atomicMin, transposed through the
+// warp's 512-byte shared-memory slice so that atomic instruction j covers the
+// 32 consecutive lanes wbase + 32j .. +31: one 128-byte line per instruction
+// instead of 16 sectors. Every thread of the warp must call it.
+__device__ __forceinline__ void atomic_min_lanes(uint32_t* row, uint32_t wbase, uint4 acc,
+                                                 uint32_t Kp, uint32_t* wbuf) {
+  const uint32_t t = threadIdx.x & 31;
+  reinterpret_cast<uint4*>(wbuf)[t] = acc;
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t v = wbuf[32 * j + t];
+    const uint32_t L = wbase + 32 * j + t;
+    if (L < Kp && v != INF) atomicMin(row + L, v);
+  }
+}
+
 // One level of the restricted sweep. blockIdx.x = work item, a thread owns
 // 4 consecutive lanes starting at lane; rows are Kp lanes wide (Kp % 4 == 0).
 __global__ void __launch_bounds__(256)
@@ -225,42 +266,44 @@ __global__ void __launch_bounds__(256)
                   uint32_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ seeded) {
   const uint4 it = item[i0 + blockIdx.x];
   const uint32_t lane = (blockIdx.y * blockDim.x + threadIdx.x) * 4;
-  if (lane >= Kp) return;
+  const uint32_t wbase = lane - 4 * (threadIdx.x & 31);
+  if (wbase >= Kp) return;  // the whole warp is past the last lane
+  const bool live = lane < Kp;
   uint4 acc = make_uint4(INF, INF, INF, INF);
-  uint32_t e = it.y;
-  for (; e + 2 <= it.z; e += 2) {
-    const uint2 r0 = erec[e], r1 = erec[e + 1];
-    const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r0.x * Kp + lane);
-    const uint4 b = *reinterpret_cast<const uint4*>(slab + (size_t)r1.x * Kp + lane);
-    acc.x = min(acc.x, min(sat_add(a.x, r0.y), sat_add(b.x, r1.y)));
-    acc.y = min(acc.y, min(sat_add(a.y, r0.y), sat_add(b.y, r1.y)));
-    acc.z = min(acc.z, min(sat_add(a.z, r0.y), sat_add(b.z, r1.y)));
-    acc.w = min(acc.w, min(sat_add(a.w, r0.y), sat_add(b.w, r1.y)));
+  if (live) {
+    uint32_t e = it.y;
+    for (; e + 2 <= it.z; e += 2) {
+      const uint2 r0 = erec[e], r1 = erec[e + 1];
+      const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r0.x * Kp + lane);
+      const uint4 b = *reinterpret_cast<const uint4*>(slab + (size_t)r1.x * Kp + lane);
+      acc.x = min(acc.x, min(sat_add(a.x, r0.y), sat_add(b.x, r1.y)));
+      acc.y = min(acc.y, min(sat_add(a.y, r0.y), sat_add(b.y, r1.y)));
+      acc.z = min(acc.z, min(sat_add(a.z, r0.y), sat_add(b.z, r1.y)));
+      acc.w = min(acc.w, min(sat_add(a.w, r0.y), sat_add(b.w, r1.y)));
+    }
+    if (e < it.z) {
+      const uint2 r0 = erec[e];
+      const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r0.x * Kp + lane);
+      acc.x = min(acc.x, sat_add(a.x, r0.y));
+      acc.y = min(acc.y, sat_add(a.y, r0.y));
+      acc.z = min(acc.z, sat_add(a.z, r0.y));
+      acc.w = min(acc.w, sat_add(a.w, r0.y));
+    }
   }
-  if (e < it.z) {
-    const uint2 r0 = erec[e];
-    const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r0.x * Kp + lane);
-    acc.x = min(acc.x, sat_add(a.x, r0.y));
-    acc.y = min(acc.y, sat_add(a.y, r0.y));
-    acc.z = min(acc.z, sat_add(a.z, r0.y));
-    acc.w = min(acc.w, sat_add(a.w, r0.y));
-  }
-  uint32_t* dst = slab + (size_t)it.x * Kp + lane;
+  uint32_t* row = slab + (size_t)it.x * Kp;
   if (it.w) {  // one slice of a high in-degree node: combine atomically
-    if (acc.x != INF) atomicMin(dst + 0, acc.x);
-    if (acc.y != INF) atomicMin(dst + 1, acc.y);
-    if (acc.z != INF) atomicMin(dst + 2, acc.z);
-    if (acc.w != INF) atomicMin(dst + 3, acc.w);
-  } else {
+    __shared__ __align__(16) uint32_t sbuf[256 * 4];
+    atomic_min_lanes(row, wbase, acc, Kp, sbuf + (threadIdx.x & ~31u) * 4);
+  } else if (live) {
     // rows that got no seed this wave hold stale data: their value is the pull
     uint4 c = ((seeded[it.x >> 5] >> (it.x & 31)) & 1u)
-                  ? *reinterpret_cast<const uint4*>(dst)
+                  ? *reinterpret_cast<const uint4*>(row + lane)
                   : make_uint4(INF, INF, INF, INF);
     c.x = min(c.x, acc.x);
     c.y = min(c.y, acc.y);
     c.z = min(c.z, acc.z);
     c.w = min(c.w, acc.w);
-    *reinterpret_cast<uint4*>(dst) = c;
+    *reinterpret_cast<uint4*>(row + lane) = c;
   }
 }
 
@@ -284,39 +327,40 @@ __global__ void __launch_bounds__(128)
   }
   if (!any) return;  // uniform across the block
   const uint32_t lane = (blockIdx.y * blockDim.x + threadIdx.x) * 4;
-  if (lane >= Kp) return;
+  const uint32_t wbase = lane - 4 * (threadIdx.x & 31);
+  if (wbase >= Kp) return;  // the whole warp is past the last lane
+  const bool live = lane < Kp;
   uint4 acc = make_uint4(INF, INF, INF, INF);
-  for (uint32_t e = it.y; e < it.z; ++e) {
-    const uint2 r = erec[e];
-    if (!((active[r.x >> 5] >> (r.x & 31)) & 1u)) continue;
-    const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r.x * Kp + lane);
-    acc.x = min(acc.x, sat_add(a.x, r.y));
-    acc.y = min(acc.y, sat_add(a.y, r.y));
-    acc.z = min(acc.z, sat_add(a.z, r.y));
-    acc.w = min(acc.w, sat_add(a.w, r.y));
-  }
-  uint32_t* dst = slab + (size_t)it.x * Kp + lane;
+  if (live)
+    for (uint32_t e = it.y; e < it.z; ++e) {
+      const uint2 r = erec[e];
+      if (!((active[r.x >> 5] >> (r.x & 31)) & 1u)) continue;
+      const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r.x * Kp + lane);
+      acc.x = min(acc.x, sat_add(a.x, r.y));
+      acc.y = min(acc.y, sat_add(a.y, r.y));
+      acc.z = min(acc.z, sat_add(a.z, r.y));
+      acc.w = min(acc.w, sat_add(a.w, r.y));
+    }
+  uint32_t* row = slab + (size_t)it.x * Kp;
   uint4 v = acc;
   if (it.w) {
-    if (acc.x != INF) atomicMin(dst + 0, acc.x);
-    if (acc.y != INF) atomicMin(dst + 1, acc.y);
-    if (acc.z != INF) atomicMin(dst + 2, acc.z);
-    if (acc.w != INF) atomicMin(dst + 3, acc.w);
-  } else {
+    __shared__ __align__(16) uint32_t sbuf[128 * 4];
+    atomic_min_lanes(row, wbase, acc, Kp, sbuf + (threadIdx.x & ~31u) * 4);
+  } else if (live) {
     // without a full slab reset only seeded rows hold valid data here
     const bool valid = !seeded || ((seeded[it.x >> 5] >> (it.x & 31)) & 1u);
-    v = valid ? *reinterpret_cast<const uint4*>(dst) : make_uint4(INF, INF, INF, INF);
+    v = valid ? *reinterpret_cast<const uint4*>(row + lane) : make_uint4(INF, INF, INF, INF);
     v.x = min(v.x, acc.x);
     v.y = min(v.y, acc.y);
     v.z = min(v.z, acc.z);
     v.w = min(v.w, acc.w);
-    *reinterpret_cast<uint4*>(dst) = v;
+    *reinterpret_cast<uint4*>(row + lane) = v;
   }
-  const bool act = (lane + 0 < kw && v.x <= thr[lane + 0]) ||
-                   (lane + 1 < kw && v.y <= thr[lane + 1]) ||
-                   (lane + 2 < kw && v.z <= thr[lane + 2]) ||
-                   (lane + 3 < kw && v.w <= thr[lane + 3]);
-  const unsigned m = __ballot_sync(__activemask(), act);
+  const bool act = live && ((lane + 0 < kw && v.x <= thr[lane + 0]) ||
+                            (lane + 1 < kw && v.y <= thr[lane + 1]) ||
+                            (lane + 2 < kw && v.z <= thr[lane + 2]) ||
+                            (lane + 3 < kw && v.w <= thr[lane + 3]));
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, act);
   if (m && (threadIdx.x & 31) == (unsigned)(__ffs(m) - 1))
     atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
 }

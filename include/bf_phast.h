@@ -161,6 +161,10 @@ typedef struct bf_tune {
   uint32_t tried;              /* candidates timed by bf_autotune               */
   uint32_t isochrone_lanes;    /* origins per isochrone wave (0 = budget-limited;
                                   small waves keep the gated active set compact) */
+  uint32_t small_level_rows;   /* levels with fewer rows than this use ...        */
+  uint32_t small_level_edges;  /* ... at most this many in-edges per work item:
+                                  short dependent load chains where a level is
+                                  too small to hide latency (0 = off)           */
 } bf_tune;
 
 /* Time candidate tunables on a sample matrix (device buffers: d_sources,
