@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--cols", type=int, default=2500)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the library's default tunables (short profiling runs)")
     ap.add_argument("--serve-s", type=float, default=15.0,
                     help="seconds of Poisson arrivals for the serving run (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=100.0, help="arrivals per second")
@@ -172,7 +174,10 @@ def run_ours(args, rank, world, dist):
     ts, tt = workload.sources_targets(cch["n"], S, T, seed=1042 + rank)
     d_ts = torch.from_numpy(ts.view(np.int32)).cuda()
     d_tt = torch.from_numpy(tt.view(np.int32)).cuda()
-    tune = g.autotune(d_ts.data_ptr(), S, d_tt.data_ptr(), T, reps=2)
+    if args.no_autotune:
+        tune = dict(g.get_tune(), autotuned=False)
+    else:
+        tune = g.autotune(d_ts.data_ptr(), S, d_tt.data_ptr(), T, reps=2)
     del d_ts, d_tt
 
     for _ in range(args.warmup):

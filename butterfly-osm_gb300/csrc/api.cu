@@ -258,6 +258,7 @@ static bf_tune to_c(const Tune& t) {
   o.isochrone_lanes = t.iso_lanes;
   o.small_level_rows = t.small_rows;
   o.small_level_edges = t.small_split;
+  o.overlap_levels = t.pdl;
   return o;
 }
 
@@ -278,7 +279,8 @@ bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
   h->g.tune.max_lanes = t->lanes_per_wave;
   h->g.tune.iso_lanes = t->isochrone_lanes;
   h->g.tune.small_rows = t->small_level_rows;
-  h->g.tune.small_split = t->small_level_rows ? t->small_level_edges : 4;
+  h->g.tune.small_split = t->small_level_rows ? t->small_level_edges : 8;
+  h->g.tune.pdl = t->overlap_levels ? 1 : 0;
   return BF_OK;
 }
 
@@ -343,7 +345,7 @@ bf_status bf_autotune(bf_graph* h, const uint32_t* d_src, uint64_t S, const uint
   }
   // second stage: short work items on the small top levels, on the winner
   uint32_t tried = (uint32_t)cands.size();
-  for (uint32_t rows : {64u, 1024u}) {
+  for (uint32_t rows : {0u, 1024u}) {
     Tune t = best_t;
     t.small_rows = rows;
     t.small_split = 8;

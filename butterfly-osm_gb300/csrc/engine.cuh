@@ -79,6 +79,7 @@ struct Sched {
   uint32_t* g_slab = nullptr;
   cudaStream_t g_stream = nullptr;
   const uint32_t* g_seeded = nullptr;
+  bool g_pdl = false;
   std::vector<uint32_t> ranks;   // ranks whose d_cidx entry is set (reset on rebuild)
   bool cidx_ready = false;       // d_cidx holds NONE outside `ranks`
 };
@@ -110,8 +111,9 @@ struct Tune {
   uint32_t graphs = 1;       // replay the level schedule from a CUDA graph
   uint32_t max_lanes = 0;    // lanes per wave (0 = as many as the budget allows)
   uint32_t iso_lanes = 1024; // isochrone origins per wave (spatially compact waves)
-  uint32_t small_rows = 0;   // levels with fewer rows use small_split edges per item
-  uint32_t small_split = 4;
+  uint32_t small_rows = 64;  // levels with fewer rows use small_split edges per item
+  uint32_t small_split = 8;
+  uint32_t pdl = 1;          // level launches as programmatic dependents
 };
 
 struct Graph {

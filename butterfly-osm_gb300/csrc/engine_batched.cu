@@ -264,11 +264,16 @@ __device__ __forceinline__ void atomic_min_lanes(uint32_t* row, uint32_t wbase, 
 __global__ void __launch_bounds__(256)
     k_sweep_items(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
                   uint32_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ seeded) {
+  // launched as a programmatic dependent of the previous level: let the next
+  // level's blocks get scheduled, read the static schedule, then wait for the
+  // previous level's rows (no-ops for a plain launch)
+  asm volatile("griddepcontrol.launch_dependents;");
   const uint4 it = item[i0 + blockIdx.x];
   const uint32_t lane = (blockIdx.y * blockDim.x + threadIdx.x) * 4;
   const uint32_t wbase = lane - 4 * (threadIdx.x & 31);
   if (wbase >= Kp) return;  // the whole warp is past the last lane
   const bool live = lane < Kp;
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   uint4 acc = make_uint4(INF, INF, INF, INF);
   if (live) {
     uint32_t e = it.y;
@@ -319,7 +324,9 @@ __global__ void __launch_bounds__(128)
                   uint32_t* __restrict__ slab, uint32_t Kp, uint32_t* __restrict__ active,
                   const uint32_t* __restrict__ thr, uint32_t kw,
                   const uint32_t* __restrict__ seeded) {
+  asm volatile("griddepcontrol.launch_dependents;");
   const uint4 it = item[i0 + blockIdx.x];
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   bool any = false;
   for (uint32_t e = it.y; e < it.z; ++e) {
     const uint32_t r = erec[e].x;
@@ -495,23 +502,46 @@ bf_status batched_prepare(Graph* g, uint32_t) {
   return BF_OK;
 }
 
+// One level launch; with `pdl` it is a programmatic dependent of the
+// previous launch on the stream (the kernels wait before reading rows).
+template <class... P, class... A>
+static cudaError_t launch_level(void (*kern)(P...), dim3 grid, unsigned tpb, bool pdl,
+                                cudaStream_t s, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(tpb);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // Launch the restricted sweep's level schedule. From the second call on the
 // same schedule and slab geometry the launches are replayed from a captured
 // CUDA graph instead of being issued one by one.
 bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                        unsigned tpb, cudaStream_t st, uint64_t* launches,
                        const uint32_t* seeded) {
-  auto issue = [&](cudaStream_t s) {
+  const bool pdl = g->tune.pdl != 0;
+  auto issue = [&](cudaStream_t s, uint64_t* count) -> cudaError_t {
     for (uint32_t l = 0; l < g->n_levels; ++l) {
       const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
       if (i1 == i0) continue;
-      dim3 grid(i1 - i0, lane_blocks);
-      k_sweep_items<<<grid, tpb, 0, s>>>(sc.d_item, i0, sc.d_erec, slab, Kp, seeded);
-      ++*launches;
+      cudaError_t e = launch_level(k_sweep_items, dim3(i1 - i0, lane_blocks), tpb, pdl, s,
+                                   (const uint4*)sc.d_item, i0, (const uint2*)sc.d_erec, slab, Kp,
+                                   seeded);
+      if (e != cudaSuccess) return e;
+      ++*count;
     }
+    return cudaSuccess;
   };
   const bool geom = sc.g_kp == Kp && sc.g_lb == lane_blocks && sc.g_tpb == tpb &&
-                    sc.g_slab == slab && sc.g_stream == st && sc.g_seeded == seeded;
+                    sc.g_slab == slab && sc.g_stream == st && sc.g_seeded == seeded &&
+                    sc.g_pdl == pdl;
   if (sc.gexec && !geom) {
     cudaGraphExecDestroy(sc.gexec);
     sc.gexec = nullptr;
@@ -523,14 +553,13 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
       uint64_t dummy = 0;
       cudaGraph_t graph;
       BF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      for (uint32_t l = 0; l < g->n_levels; ++l) {
-        const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
-        if (i1 == i0) continue;
-        dim3 grid(i1 - i0, lane_blocks);
-        k_sweep_items<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, slab, Kp, seeded);
-        ++dummy;
+      const cudaError_t le = issue(st, &dummy);
+      const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+      if (le != cudaSuccess) {
+        if (ce == cudaSuccess) cudaGraphDestroy(graph);
+        return cuda_status(le, "level launch during capture");
       }
-      BF_CUDA(cudaStreamEndCapture(st, &graph));
+      if (ce != cudaSuccess) return cuda_status(ce, "cudaStreamEndCapture");
       cudaError_t e = cudaGraphInstantiate(&sc.gexec, graph, 0);
       cudaGraphDestroy(graph);
       if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate");
@@ -540,6 +569,7 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
       sc.g_slab = slab;
       sc.g_stream = st;
       sc.g_seeded = seeded;
+      sc.g_pdl = pdl;
     }
   }
   if (sc.gexec && g->tune.graphs) {
@@ -547,7 +577,7 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
     for (uint32_t l = 0; l < g->n_levels; ++l)
       if (sc.lvl_item[l + 1] != sc.lvl_item[l]) ++*launches;
   } else {
-    issue(st);
+    BF_CUDA(issue(st, launches));
   }
   BF_CUDA(cudaGetLastError());
   return BF_OK;
@@ -558,12 +588,13 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
 bf_status sweep_levels_gated(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                              unsigned tpb, uint32_t* active, const uint32_t* thr, uint32_t kw,
                              cudaStream_t st, uint64_t* launches, const uint32_t* seeded) {
+  const bool pdl = g->tune.pdl != 0;
   for (uint32_t l = 0; l < g->n_levels; ++l) {
     const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
     if (i1 == i0) continue;
-    dim3 grid(i1 - i0, lane_blocks);
-    k_sweep_gated<<<grid, tpb, 0, st>>>(sc.d_item, i0, sc.d_erec, slab, Kp, active, thr, kw,
-                                        seeded);
+    BF_CUDA(launch_level(k_sweep_gated, dim3(i1 - i0, lane_blocks), tpb, pdl, st,
+                         (const uint4*)sc.d_item, i0, (const uint2*)sc.d_erec, slab, Kp, active,
+                         thr, kw, seeded));
     ++*launches;
   }
   BF_CUDA(cudaGetLastError());

@@ -165,6 +165,9 @@ typedef struct bf_tune {
   uint32_t small_level_edges;  /* ... at most this many in-edges per work item:
                                   short dependent load chains where a level is
                                   too small to hide latency (0 = off)           */
+  uint32_t overlap_levels;     /* 1: launch each level as a programmatic
+                                  dependent of the previous one, so its blocks
+                                  are scheduled while that level drains        */
 } bf_tune;
 
 /* Time candidate tunables on a sample matrix (device buffers: d_sources,
