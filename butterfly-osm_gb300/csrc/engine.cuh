@@ -114,6 +114,7 @@ struct Tune {
   uint32_t small_rows = 64;  // levels with fewer rows use small_split edges per item
   uint32_t small_split = 8;
   uint32_t pdl = 1;          // level launches as programmatic dependents
+  uint32_t iso_half = 1;     // 16-bit isochrone lanes when all thresholds fit
 };
 
 struct Graph {
@@ -168,6 +169,24 @@ struct Graph {
   size_t iso_bytes = 0;
 };
 
+// One level launch; with `pdl` it is a programmatic dependent of the
+// previous launch on the stream (the kernels wait before reading rows).
+template <class... P, class... A>
+inline cudaError_t launch_level(void (*kern)(P...), dim3 grid, unsigned tpb, bool pdl,
+                                cudaStream_t s, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(tpb);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // graph.cu
 bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g,
                       const uint32_t* up_len = nullptr, const uint32_t* down_len = nullptr);
@@ -185,7 +204,8 @@ bf_status check_device_error(Graph* g, cudaStream_t st);
 bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t threshold,
                         const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
                         cudaStream_t st, const uint32_t* lane_thr = nullptr,
-                        const uint32_t* unit_cost = nullptr, const uint32_t* unit_lane = nullptr);
+                        const uint32_t* unit_cost = nullptr, const uint32_t* unit_lane = nullptr,
+                        bool half = false);
 __global__ void k_extract(const uint32_t* __restrict__ slab, uint32_t slab_stride,
                           const uint32_t* __restrict__ tpos, uint64_t T, uint32_t k,
                           uint32_t* __restrict__ out);

@@ -502,24 +502,6 @@ bf_status batched_prepare(Graph* g, uint32_t) {
   return BF_OK;
 }
 
-// One level launch; with `pdl` it is a programmatic dependent of the
-// previous launch on the stream (the kernels wait before reading rows).
-template <class... P, class... A>
-static cudaError_t launch_level(void (*kern)(P...), dim3 grid, unsigned tpb, bool pdl,
-                                cudaStream_t s, A... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = dim3(tpb);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, kern, args...);
-}
-
 // Launch the restricted sweep's level schedule. From the second call on the
 // same schedule and slab geometry the launches are replayed from a captured
 // CUDA graph instead of being issued one by one.

@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
                   uint32_t n, uint32_t* __restrict__ seed, uint32_t seed_stride,
                   uint32_t* __restrict__ flag, uint32_t dcap, uint32_t* __restrict__ err,
                   const uint32_t* __restrict__ lane_thr, const uint32_t* __restrict__ unit_cost,
-                  const uint32_t* __restrict__ unit_lane) {
+                  const uint32_t* __restrict__ unit_lane, uint32_t half) {
   extern __shared__ uint32_t smem[];
   const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t w = blockIdx.x * UPWARD_WARPS + wib;
@@ -193,6 +193,8 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
     const uint32_t p = pos_of[pn[l]];
     if (p == NONE) continue;
     if (unit_lane) atomicMin(&seed[(size_t)p * seed_stride + out_lane], d);
+    else if (half)  // 16-bit lanes: every stored d is within its lane threshold (< 0xFFFF)
+      reinterpret_cast<uint16_t*>(seed)[(size_t)p * seed_stride + w] = (uint16_t)d;
     else seed[(size_t)p * seed_stride + w] = d;
     if (flag && d <= lt) atomicOr(&flag[p >> 5], 1u << (p & 31));
   }
@@ -309,7 +311,11 @@ static bf_status plain_buffers(Graph* g) {
 bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t threshold,
                         const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
                         cudaStream_t st, const uint32_t* lane_thr, const uint32_t* unit_cost,
-                        const uint32_t* unit_lane) {
+                        const uint32_t* unit_lane, bool half) {
+  if (half && (!lane_thr || unit_lane)) {
+    set_error("16-bit seed lanes need per-lane thresholds below 0xFFFF");
+    return BF_ERR_UNSUPPORTED;
+  }
   const uint32_t dcap = ((g->max_depth + 1) + 31) & ~31u;
   const size_t fast_smem = (size_t)UPWARD_WARPS * 2 * dcap * 4;
   const bool fast = fast_smem <= 200 * 1024;
@@ -320,7 +326,7 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
                     fast_smem, st>>>(d_src, (uint32_t)k, threshold, g->d_parent, g->d_run_end,
                                      g->d_depth, g->d_up_off, g->d_up_rec, pos_map, g->n, seed,
                                      stride, flag, dcap, g->d_err, lane_thr, unit_cost,
-                                     unit_lane);
+                                     unit_lane, half ? 1u : 0u);
     BF_CUDA(cudaGetLastError());
     return BF_OK;
   }

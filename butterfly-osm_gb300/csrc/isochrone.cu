@@ -26,12 +26,105 @@ constexpr uint32_t TILE_R = 256;  // ranks per tile
 constexpr uint32_t TILE_L = 32;   // lanes per tile
 constexpr uint32_t LANE_TILES_PER_BLOCK = 8;
 
+// min of the two halfwords of *p and v, one lane per halfword, by
+// compare-and-swap (there is no 16-bit atomicMin). Lock-free: a failed swap
+// means another thread lowered the word; the loop is bounded all the same.
+__device__ __forceinline__ void atomic_min_u16x2(uint32_t* p, uint32_t v, uint32_t* err) {
+  uint32_t old = *(volatile uint32_t*)p;
+  for (uint32_t guard = 0; guard < (1u << 20); ++guard) {
+    const uint32_t nv = __vminu2(old, v);
+    if (nv == old) return;
+    const uint32_t seen = atomicCAS(p, old, nv);
+    if (seen == old) return;
+    old = seen;
+  }
+  atomicOr(err, DEVERR_TIMEOUT);
+}
+
+// Gated sweep with 16-bit lanes, for isochrone waves whose thresholds are all
+// below 0xFFFF. A lane holds its distance while it is within the lane's
+// threshold and 0xFFFF otherwise: a value above a threshold only leads to
+// values above it, so the clamp keeps every distance within the threshold
+// exact and halves the bytes of every gather and row write. A thread owns 8
+// lanes (one 16-byte load per gathered row), adds with halfword saturation and
+// clamps once per item. Gating as in the 32-bit form: items with no active
+// source are skipped, inactive sources are not gathered, and a row becomes
+// active when any lane is within its threshold.
+__global__ void __launch_bounds__(128)
+    k_sweep_gated16(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
+                    uint16_t* __restrict__ slab, uint32_t Kp, uint32_t* __restrict__ active,
+                    const uint32_t* __restrict__ thr, uint32_t kw,
+                    const uint32_t* __restrict__ seeded, uint32_t* __restrict__ err) {
+  asm volatile("griddepcontrol.launch_dependents;");
+  const uint4 it = item[i0 + blockIdx.x];
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  bool any = false;
+  for (uint32_t e = it.y; e < it.z; ++e) {
+    const uint32_t r = erec[e].x;
+    any |= (active[r >> 5] >> (r & 31)) & 1u;
+  }
+  if (!any) return;  // uniform across the block
+  const uint32_t lane = (blockIdx.y * blockDim.x + threadIdx.x) * 8;
+  const uint32_t wbase = lane - 8 * (threadIdx.x & 31);
+  if (wbase >= Kp) return;  // the whole warp is past the last lane
+  const bool live = lane < Kp;
+  uint4 acc = make_uint4(~0u, ~0u, ~0u, ~0u);
+  if (live) {
+    for (uint32_t e = it.y; e < it.z; ++e) {
+      const uint2 r = erec[e];
+      if (!((active[r.x >> 5] >> (r.x & 31)) & 1u)) continue;
+      const uint32_t w16 = min(r.y, 0xFFFFu), ww = w16 | (w16 << 16);
+      const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r.x * Kp + lane);
+      acc.x = __vminu2(acc.x, __vaddus2(a.x, ww));
+      acc.y = __vminu2(acc.y, __vaddus2(a.y, ww));
+      acc.z = __vminu2(acc.z, __vaddus2(a.z, ww));
+      acc.w = __vminu2(acc.w, __vaddus2(a.w, ww));
+    }
+    // clamp each lane to its threshold (lanes past the wave stay 0xFFFF)
+    uint32_t* w = &acc.x;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t l = lane + 2 * q;
+      uint32_t lo = w[q] & 0xFFFFu, hi = w[q] >> 16;
+      if (l >= kw || lo > thr[l]) lo = 0xFFFFu;
+      if (l + 1 >= kw || hi > thr[l + 1]) hi = 0xFFFFu;
+      w[q] = lo | (hi << 16);
+    }
+  }
+  uint16_t* row = slab + (size_t)it.x * Kp;
+  uint4 v = acc;
+  if (live) {
+    uint32_t* dst = reinterpret_cast<uint32_t*>(row + lane);
+    if (it.w) {
+      atomic_min_u16x2(dst + 0, acc.x, err);
+      atomic_min_u16x2(dst + 1, acc.y, err);
+      atomic_min_u16x2(dst + 2, acc.z, err);
+      atomic_min_u16x2(dst + 3, acc.w, err);
+    } else {
+      // without a full slab reset only seeded rows hold valid data here
+      const bool valid = (seeded[it.x >> 5] >> (it.x & 31)) & 1u;
+      const uint4 c = valid ? *reinterpret_cast<const uint4*>(dst) : make_uint4(~0u, ~0u, ~0u, ~0u);
+      v.x = __vminu2(c.x, acc.x);
+      v.y = __vminu2(c.y, acc.y);
+      v.z = __vminu2(c.z, acc.z);
+      v.w = __vminu2(c.w, acc.w);
+      *reinterpret_cast<uint4*>(dst) = v;
+    }
+  }
+  const bool act = live && (acc.x & acc.y & acc.z & acc.w) != ~0u;
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, act);
+  if (m && (threadIdx.x & 31) == (unsigned)(__ffs(m) - 1))
+    atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
+}
+
 // bits: rows of w32 u32 words; lane l writes output row out_row[l]. A block
 // owns 256 ranks and walks all lane tiles of the wave: the ranks' slab rows
 // and activity are looked up once, inactive rows (no value within any lane's
 // threshold) are never read, and a tile with no active row only writes zeros.
+// L is the lane type: uint32_t, or uint16_t for clamped 16-bit waves.
+template <class L>
 __global__ void __launch_bounds__(256)
-    k_bits(const uint32_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ cidx,
+    k_bits(const L* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ cidx,
            uint32_t n, const uint32_t* __restrict__ thr, uint32_t kw, uint32_t* __restrict__ bits,
            uint64_t w32, unsigned long long* __restrict__ counts,
            const uint32_t* __restrict__ active, const uint32_t* __restrict__ out_row) {
@@ -60,7 +153,8 @@ __global__ void __launch_bounds__(256)
     if (live) {
       for (uint32_t r = warp; r < TILE_R; r += 8) {
         const uint32_t row = srow[r], l = l0 + lane;
-        tile[r][lane] = (row != NONE && l < lend) ? slab[(size_t)row * Kp + l] : INF;
+        const uint32_t d = (row != NONE && l < lend) ? (uint32_t)slab[(size_t)row * Kp + l] : INF;
+        tile[r][lane] = d == (uint32_t)(L)~0u ? INF : d;
       }
       __syncthreads();
     }
@@ -149,20 +243,28 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
   uint32_t* d_active = p_row + n;
   uint32_t* d_seeded = d_active + aw;
   BF_CUDA(cudaMemcpyAsync(p_orig, pk.data(), pk.size() * 4, cudaMemcpyHostToDevice, st));
+  // 16-bit lanes when every threshold fits below 0xFFFF (the clamp keeps
+  // distances within the thresholds exact and halves the bytes moved)
+  uint32_t tmax = 0;
+  for (uint64_t i = 0; i < n; ++i) tmax = std::max(tmax, ht[i]);
+  const bool half = g->tune.iso_half && tmax < 0xFFFFu;
+  const uint32_t lb = half ? 2 : 4;      // bytes per lane
+  const uint32_t lq = half ? 8 : 4;      // lanes per thread (one 16-byte load)
   // the slab is the only per-lane device memory here
-  uint64_t max_lanes = ctx_budget(g, c) / (rows * 4);
+  uint64_t max_lanes = ctx_budget(g, c) / (rows * lb);
   max_lanes = max_lanes >= 32 ? max_lanes & ~31ull : 0;
   if (!max_lanes) {
     set_error("HBM budget too small for one 32-lane isochrone wave");
     return BF_ERR_OOM;
   }
   if (g->tune.iso_lanes) max_lanes = std::min<uint64_t>(max_lanes, g->tune.iso_lanes);
-  const uint64_t wave = std::min<uint64_t>(max_lanes, (n + 3) & ~3ull);
-  const uint32_t Kp = (uint32_t)((wave + 3) & ~3ull);
-  if ((s = ensure_slab(g, c, (size_t)rows * Kp * 4))) return s;
+  const uint64_t wave = std::min<uint64_t>(max_lanes, (n + lq - 1) & ~(uint64_t)(lq - 1));
+  const uint32_t Kp = (uint32_t)((wave + lq - 1) & ~(uint64_t)(lq - 1));
+  if ((s = ensure_slab(g, c, (size_t)rows * Kp * lb))) return s;
   BF_CUDA(cudaMemsetAsync(d_counts, 0, n * 8, st));
-  const unsigned tpb = std::min<uint32_t>(128, ((Kp / 4 + 31) / 32) * 32);
-  const unsigned lane_blocks = (Kp / 4 + tpb - 1) / tpb;
+  const unsigned tpb = std::min<uint32_t>(128, ((Kp / lq + 31) / 32) * 32);
+  const unsigned lane_blocks = (Kp / lq + tpb - 1) / tpb;
+  uint16_t* slab16 = reinterpret_cast<uint16_t*>(c.d_slab);
   uint64_t launches = 0;
   float t_up = 0, t_dn = 0, t_ex = 0;
   for (uint64_t s0 = 0; s0 < n; s0 += wave) {
@@ -170,23 +272,44 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
     if (stats) BF_CUDA(cudaEventRecord(c.ev[0], st));
     BF_CUDA(cudaMemsetAsync(d_active, 0, 2 * aw * 4, st));  // active + seeded bitmaps
     launch_mark_paths(g, p_orig + s0, kw, sc.d_cidx, d_seeded, st);
-    launch_init_rows(d_seeded, sc.d_split, (uint32_t)aw, c.d_slab, Kp, st);
+    // rows are Kp * lb bytes = Kp * lb / 4 words
+    launch_init_rows(d_seeded, sc.d_split, (uint32_t)aw, c.d_slab, Kp * lb / 4, st);
     launches += 2;
     if ((s = launch_upward(g, p_orig + s0, kw, INF, sc.d_cidx, c.d_slab, Kp, d_active, st,
-                           p_thr + s0)))
+                           p_thr + s0, nullptr, nullptr, half)))
       return s;
     ++launches;
     if (stats) BF_CUDA(cudaEventRecord(c.ev[1], st));
-    if ((s = sweep_levels_gated(g, sc, c.d_slab, Kp, lane_blocks, tpb, d_active, p_thr + s0,
-                                (uint32_t)kw, st, &launches, d_seeded)))
+    if (half) {
+      const bool pdl = g->tune.pdl != 0;
+      for (uint32_t l = 0; l < g->n_levels; ++l) {
+        const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
+        if (i1 == i0) continue;
+        BF_CUDA(launch_level(k_sweep_gated16, dim3(i1 - i0, lane_blocks), tpb, pdl, st,
+                             (const uint4*)sc.d_item, i0, (const uint2*)sc.d_erec, slab16, Kp,
+                             d_active, (const uint32_t*)(p_thr + s0), (uint32_t)kw,
+                             (const uint32_t*)d_seeded, g->d_err));
+        ++launches;
+      }
+    } else if ((s = sweep_levels_gated(g, sc, c.d_slab, Kp, lane_blocks, tpb, d_active,
+                                       p_thr + s0, (uint32_t)kw, st, &launches, d_seeded))) {
       return s;
+    }
     if (stats) BF_CUDA(cudaEventRecord(c.ev[2], st));
     dim3 bgrid((unsigned)((g->n + TILE_R - 1) / TILE_R),
                (unsigned)((kw + TILE_L * LANE_TILES_PER_BLOCK - 1) / (TILE_L * LANE_TILES_PER_BLOCK)));
-    k_bits<<<bgrid, 256, 0, st>>>(c.d_slab, Kp, sc.d_cidx, g->n, p_thr + s0, (uint32_t)kw,
-                                 reinterpret_cast<uint32_t*>(d_bits), 2 * w64,
-                                 reinterpret_cast<unsigned long long*>(d_counts), d_active,
-                                 p_row + s0);
+    if (half)
+      k_bits<uint16_t><<<bgrid, 256, 0, st>>>(slab16, Kp, sc.d_cidx, g->n, p_thr + s0,
+                                              (uint32_t)kw, reinterpret_cast<uint32_t*>(d_bits),
+                                              2 * w64,
+                                              reinterpret_cast<unsigned long long*>(d_counts),
+                                              d_active, p_row + s0);
+    else
+      k_bits<uint32_t><<<bgrid, 256, 0, st>>>(c.d_slab, Kp, sc.d_cidx, g->n, p_thr + s0,
+                                              (uint32_t)kw, reinterpret_cast<uint32_t*>(d_bits),
+                                              2 * w64,
+                                              reinterpret_cast<unsigned long long*>(d_counts),
+                                              d_active, p_row + s0);
     BF_CUDA(cudaGetLastError());
     ++launches;
     if (stats) {

@@ -168,6 +168,9 @@ typedef struct bf_tune {
   uint32_t overlap_levels;     /* 1: launch each level as a programmatic
                                   dependent of the previous one, so its blocks
                                   are scheduled while that level drains        */
+  uint32_t isochrone_16bit;    /* 1: isochrone calls whose thresholds are all
+                                  below 0xFFFF keep 16-bit lanes clamped at the
+                                  threshold (exact, half the bytes)             */
 } bf_tune;
 
 /* Time candidate tunables on a sample matrix (device buffers: d_sources,

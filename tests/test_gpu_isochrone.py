@@ -85,3 +85,33 @@ def test_wave_widths_match_oracle(built, country_small, iso_lanes):
     want_bits, want_counts = c.isochrone_bitsets(origins, thr)
     assert np.array_equal(bits, want_bits)
     assert np.array_equal(counts, want_counts)
+
+
+@pytest.mark.parametrize("half", [1, 0])
+def test_16bit_and_32bit_lanes_match_oracle(built, country_small, half):
+    # thresholds below 0xFFFF take the clamped 16-bit lanes unless disabled
+    import workload
+    _, cch = country_small
+    c = orc.Cch.from_dict(cch)
+    g = _graph(cch)
+    g.set_tune(isochrone_lanes=64, isochrone_16bit=half)
+    origins, thr = workload.isochrone_workload(cch["n"], 130, seed=23)
+    bits, counts = g.isochrone_bitsets(origins, thr)
+    want_bits, want_counts = c.isochrone_bitsets(origins, thr)
+    assert np.array_equal(bits, want_bits)
+    assert np.array_equal(counts, want_counts)
+
+
+def test_16bit_boundary_thresholds(built, grid100):
+    # 0xFFFE is the largest threshold the 16-bit lanes hold; 0xFFFF and above
+    # run on 32-bit lanes. Both must agree with the oracle.
+    _, cch = grid100
+    c = orc.Cch.from_dict(cch)
+    g = _graph(cch)
+    origins = np.array([3, 400, 9000, 22222, 35000, 7], dtype=np.uint32)
+    for t in (0xFFFE, 0xFFFF, 0x10000):
+        thr = np.full(len(origins), t, dtype=np.uint32)
+        thr[0] = 50
+        bits, counts = g.isochrone_bitsets(origins, thr)
+        want_bits, want_counts = c.isochrone_bitsets(origins, thr)
+        assert np.array_equal(bits, want_bits) and np.array_equal(counts, want_counts)
