@@ -121,10 +121,8 @@ __global__ void __launch_bounds__(128)
 // owns 256 ranks and walks all lane tiles of the wave: the ranks' slab rows
 // and activity are looked up once, inactive rows (no value within any lane's
 // threshold) are never read, and a tile with no active row only writes zeros.
-// L is the lane type: uint32_t, or uint16_t for clamped 16-bit waves.
-template <class L>
 __global__ void __launch_bounds__(256)
-    k_bits(const L* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ cidx,
+    k_bits(const uint32_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ cidx,
            uint32_t n, const uint32_t* __restrict__ thr, uint32_t kw, uint32_t* __restrict__ bits,
            uint64_t w32, unsigned long long* __restrict__ counts,
            const uint32_t* __restrict__ active, const uint32_t* __restrict__ out_row) {
@@ -153,8 +151,7 @@ __global__ void __launch_bounds__(256)
     if (live) {
       for (uint32_t r = warp; r < TILE_R; r += 8) {
         const uint32_t row = srow[r], l = l0 + lane;
-        const uint32_t d = (row != NONE && l < lend) ? (uint32_t)slab[(size_t)row * Kp + l] : INF;
-        tile[r][lane] = d == (uint32_t)(L)~0u ? INF : d;
+        tile[r][lane] = (row != NONE && l < lend) ? slab[(size_t)row * Kp + l] : INF;
       }
       __syncthreads();
     }
@@ -168,6 +165,76 @@ __global__ void __launch_bounds__(256)
         for (uint32_t c = 0; c < TILE_R / 32; ++c) {
           const uint32_t d = tile[c * 32 + lane][li];
           const uint32_t word = __ballot_sync(0xFFFFFFFFu, d != INF && d <= t);
+          if (lane == c) mine = word;
+        }
+      }
+      const uint64_t wi = wbase + lane;
+      uint32_t pc = 0;
+      if (lane < TILE_R / 32 && wi < w32) {
+        bits[orow * w32 + wi] = mine;
+        pc = __popc(mine);
+      }
+      if (live) {
+        for (int o = 16; o > 0; o >>= 1) pc += __shfl_down_sync(0xFFFFFFFFu, pc, o);
+        if (lane == 0 && pc) atomicAdd(&counts[orow], (unsigned long long)pc);
+      }
+    }
+    if (live) __syncthreads();
+  }
+}
+
+// 16-bit form of k_bits: lane tiles of 64, a thread loads two lanes, so a
+// warp reads one 128-byte line per slab row. Lanes hold 0xFFFF beyond their
+// threshold (the sweep and the upward pass clamp), so a bit is just
+// "not 0xFFFF" on an active row.
+constexpr uint32_t TILE_L16 = 64;
+
+__global__ void __launch_bounds__(256)
+    k_bits16(const uint16_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ cidx,
+             uint32_t n, uint32_t kw, uint32_t* __restrict__ bits, uint64_t w32,
+             unsigned long long* __restrict__ counts, const uint32_t* __restrict__ active,
+             const uint32_t* __restrict__ out_row) {
+  __shared__ uint32_t tile[TILE_R][TILE_L16 / 2 + 1];  // two lanes per word
+  __shared__ uint32_t srow[TILE_R];
+  __shared__ int any_active;
+  const uint32_t r0 = blockIdx.x * TILE_R;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) any_active = 0;
+  __syncthreads();
+  {
+    const uint32_t rank = r0 + threadIdx.x;
+    uint32_t row = NONE;
+    if (rank < n) {
+      const uint32_t c = cidx[rank];
+      if ((active[c >> 5] >> (c & 31)) & 1u) row = c;
+    }
+    srow[threadIdx.x] = row;
+    if (__any_sync(0xFFFFFFFFu, row != NONE) && lane == 0) any_active = 1;
+  }
+  __syncthreads();
+  const bool live = any_active != 0;
+  const uint64_t wbase = r0 / 32;
+  const uint32_t lend = min(kw, (blockIdx.y + 1) * TILE_L16 * LANE_TILES_PER_BLOCK);
+  for (uint32_t l0 = blockIdx.y * TILE_L16 * LANE_TILES_PER_BLOCK; l0 < lend; l0 += TILE_L16) {
+    if (live) {
+      for (uint32_t r = warp; r < TILE_R; r += 8) {
+        const uint32_t row = srow[r], l = l0 + 2 * lane;  // even: 4-byte aligned
+        tile[r][lane] = (row != NONE && l < lend)
+                            ? *reinterpret_cast<const uint32_t*>(slab + (size_t)row * Kp + l)
+                            : 0xFFFFFFFFu;
+      }
+      __syncthreads();
+    }
+    for (uint32_t q = 0; q < 8; ++q) {
+      const uint32_t li = warp * 8 + q, l = l0 + li;
+      if (l >= lend) continue;  // warp-uniform
+      const uint64_t orow = out_row[l];
+      uint32_t mine = 0;
+      if (live) {
+        for (uint32_t c = 0; c < TILE_R / 32; ++c) {
+          const uint32_t wd = tile[c * 32 + lane][li >> 1];
+          const uint32_t d = (li & 1) ? (wd >> 16) : (wd & 0xFFFFu);
+          const uint32_t word = __ballot_sync(0xFFFFFFFFu, d != 0xFFFFu);
           if (lane == c) mine = word;
         }
       }
@@ -298,14 +365,15 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
     if (stats) BF_CUDA(cudaEventRecord(c.ev[2], st));
     dim3 bgrid((unsigned)((g->n + TILE_R - 1) / TILE_R),
                (unsigned)((kw + TILE_L * LANE_TILES_PER_BLOCK - 1) / (TILE_L * LANE_TILES_PER_BLOCK)));
-    if (half)
-      k_bits<uint16_t><<<bgrid, 256, 0, st>>>(slab16, Kp, sc.d_cidx, g->n, p_thr + s0,
-                                              (uint32_t)kw, reinterpret_cast<uint32_t*>(d_bits),
-                                              2 * w64,
-                                              reinterpret_cast<unsigned long long*>(d_counts),
-                                              d_active, p_row + s0);
-    else
-      k_bits<uint32_t><<<bgrid, 256, 0, st>>>(c.d_slab, Kp, sc.d_cidx, g->n, p_thr + s0,
+    if (half) {
+      dim3 bg16(bgrid.x, (unsigned)((kw + TILE_L16 * LANE_TILES_PER_BLOCK - 1) /
+                                    (TILE_L16 * LANE_TILES_PER_BLOCK)));
+      k_bits16<<<bg16, 256, 0, st>>>(slab16, Kp, sc.d_cidx, g->n, (uint32_t)kw,
+                                     reinterpret_cast<uint32_t*>(d_bits), 2 * w64,
+                                     reinterpret_cast<unsigned long long*>(d_counts), d_active,
+                                     p_row + s0);
+    } else
+      k_bits<<<bgrid, 256, 0, st>>>(c.d_slab, Kp, sc.d_cidx, g->n, p_thr + s0,
                                               (uint32_t)kw, reinterpret_cast<uint32_t*>(d_bits),
                                               2 * w64,
                                               reinterpret_cast<unsigned long long*>(d_counts),
