@@ -58,28 +58,72 @@ __global__ void __launch_bounds__(128)
   asm volatile("griddepcontrol.launch_dependents;");
   const uint4 it = item[i0 + blockIdx.x];
   asm volatile("griddepcontrol.wait;" ::: "memory");
+  const unsigned FULL = 0xFFFFFFFFu;
+  const uint32_t t = threadIdx.x & 31;
+  // every warp evaluates the item's in-edges 32 at a time: warp lane t holds
+  // edge base + t, and a ballot gives the edges whose source row is active
+  // (the same mask in every warp, so the skip below is block-uniform)
   bool any = false;
-  for (uint32_t e = it.y; e < it.z; ++e) {
-    const uint32_t r = erec[e].x;
-    any |= (active[r >> 5] >> (r & 31)) & 1u;
+  for (uint32_t base = it.y; base < it.z && !any; base += 32) {
+    const uint32_t e = base + t;
+    bool a = false;
+    if (e < it.z) {
+      const uint32_t r = erec[e].x;
+      a = (active[r >> 5] >> (r & 31)) & 1u;
+    }
+    any = __ballot_sync(FULL, a) != 0;
   }
-  if (!any) return;  // uniform across the block
+  if (!any) return;
   const uint32_t lane = (blockIdx.y * blockDim.x + threadIdx.x) * 8;
-  const uint32_t wbase = lane - 8 * (threadIdx.x & 31);
+  const uint32_t wbase = lane - 8 * t;
   if (wbase >= Kp) return;  // the whole warp is past the last lane
   const bool live = lane < Kp;
   uint4 acc = make_uint4(~0u, ~0u, ~0u, ~0u);
-  if (live) {
-    for (uint32_t e = it.y; e < it.z; ++e) {
-      const uint2 r = erec[e];
-      if (!((active[r.x >> 5] >> (r.x & 31)) & 1u)) continue;
-      const uint32_t w16 = min(r.y, 0xFFFFu), ww = w16 | (w16 << 16);
-      const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r.x * Kp + lane);
-      acc.x = __vminu2(acc.x, __vaddus2(a.x, ww));
-      acc.y = __vminu2(acc.y, __vaddus2(a.y, ww));
-      acc.z = __vminu2(acc.z, __vaddus2(a.z, ww));
-      acc.w = __vminu2(acc.w, __vaddus2(a.w, ww));
+  auto relax = [&](const uint4& a, uint32_t w) {
+    const uint32_t w16 = min(w, 0xFFFFu), ww = w16 | (w16 << 16);
+    acc.x = __vminu2(acc.x, __vaddus2(a.x, ww));
+    acc.y = __vminu2(acc.y, __vaddus2(a.y, ww));
+    acc.z = __vminu2(acc.z, __vaddus2(a.z, ww));
+    acc.w = __vminu2(acc.w, __vaddus2(a.w, ww));
+  };
+  for (uint32_t base = it.y; base < it.z; base += 32) {
+    const uint32_t e = base + t;
+    uint2 r = make_uint2(0, 0);
+    bool a = false;
+    if (e < it.z) {
+      r = erec[e];
+      a = (active[r.x >> 5] >> (r.x & 31)) & 1u;
     }
+    uint32_t m = __ballot_sync(FULL, a);
+    // gather the active sources four at a time (loads in flight together)
+    while (m) {
+      uint32_t j[4], k = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        j[q] = m ? (uint32_t)(__ffs(m) - 1) : 32u;
+        if (m) {
+          m &= m - 1;
+          ++k;
+        }
+      }
+      uint32_t src[4], w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        src[q] = __shfl_sync(FULL, r.x, j[q] & 31);
+        w[q] = __shfl_sync(FULL, r.y, j[q] & 31);
+      }
+      if (live) {
+        uint4 v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          v[q] = q < (int)k ? *reinterpret_cast<const uint4*>(slab + (size_t)src[q] * Kp + lane)
+                            : make_uint4(~0u, ~0u, ~0u, ~0u);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) relax(v[q], w[q]);
+      }
+    }
+  }
+  if (live) {
     // clamp each lane to its threshold (lanes past the wave stay 0xFFFF)
     uint32_t* w = &acc.x;
 #pragma unroll
