@@ -25,6 +25,9 @@ namespace {
 constexpr uint32_t TILE_R = 256;  // ranks per tile
 constexpr uint32_t TILE_L = 32;   // lanes per tile
 constexpr uint32_t LANE_TILES_PER_BLOCK = 8;
+// blocks of the 16-bit gated sweep per level: 16 resident 128-thread blocks
+// on each of the 152 SMs
+constexpr uint32_t GATED16_BLOCKS = 152 * 16;
 
 // min of the two halfwords of *p and v, one lane per halfword, by
 // compare-and-swap (there is no 16-bit atomicMin). Lock-free: a failed swap
@@ -50,115 +53,111 @@ __device__ __forceinline__ void atomic_min_u16x2(uint32_t* p, uint32_t v, uint32
 // clamps once per item. Gating as in the 32-bit form: items with no active
 // source are skipped, inactive sources are not gathered, and a row becomes
 // active when any lane is within its threshold.
-__global__ void __launch_bounds__(128)
-    k_sweep_gated16(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
-                    uint16_t* __restrict__ slab, uint32_t Kp, uint32_t* __restrict__ active,
-                    const uint32_t* __restrict__ thr, uint32_t kw,
+//
+// A full-graph wave has millions of small items, most of them inactive, so a
+// block does not own one item: the level's items [i0, i1) are dealt out
+// block-stride over a grid sized to the GPU, and a skipped item costs one
+// warp ballot instead of a block launch.
+__global__ void __launch_bounds__(128, 16)
+    k_sweep_gated16(const uint4* __restrict__ item, uint32_t i0, uint32_t i1,
+                    const uint2* __restrict__ erec, uint16_t* __restrict__ slab, uint32_t Kp,
+                    uint32_t* __restrict__ active, const uint32_t* __restrict__ thr, uint32_t kw,
                     const uint32_t* __restrict__ seeded, uint32_t* __restrict__ err) {
   asm volatile("griddepcontrol.launch_dependents;");
-  const uint4 it = item[i0 + blockIdx.x];
-  asm volatile("griddepcontrol.wait;" ::: "memory");
   const unsigned FULL = 0xFFFFFFFFu;
   const uint32_t t = threadIdx.x & 31;
-  // every warp evaluates the item's in-edges 32 at a time: warp lane t holds
-  // edge base + t, and a ballot gives the edges whose source row is active
-  // (the same mask in every warp, so the skip below is block-uniform)
-  bool any = false;
-  for (uint32_t base = it.y; base < it.z && !any; base += 32) {
-    const uint32_t e = base + t;
-    bool a = false;
-    if (e < it.z) {
-      const uint32_t r = erec[e].x;
-      a = (active[r >> 5] >> (r & 31)) & 1u;
-    }
-    any = __ballot_sync(FULL, a) != 0;
-  }
-  if (!any) return;
   const uint32_t lane = (blockIdx.y * blockDim.x + threadIdx.x) * 8;
   const uint32_t wbase = lane - 8 * t;
   if (wbase >= Kp) return;  // the whole warp is past the last lane
   const bool live = lane < Kp;
-  uint4 acc = make_uint4(~0u, ~0u, ~0u, ~0u);
-  auto relax = [&](const uint4& a, uint32_t w) {
-    const uint32_t w16 = min(w, 0xFFFFu), ww = w16 | (w16 << 16);
-    acc.x = __vminu2(acc.x, __vaddus2(a.x, ww));
-    acc.y = __vminu2(acc.y, __vaddus2(a.y, ww));
-    acc.z = __vminu2(acc.z, __vaddus2(a.z, ww));
-    acc.w = __vminu2(acc.w, __vaddus2(a.w, ww));
-  };
-  for (uint32_t base = it.y; base < it.z; base += 32) {
-    const uint32_t e = base + t;
-    uint2 r = make_uint2(0, 0);
-    bool a = false;
-    if (e < it.z) {
-      r = erec[e];
-      a = (active[r.x >> 5] >> (r.x & 31)) & 1u;
-    }
-    uint32_t m = __ballot_sync(FULL, a);
-    // gather the active sources four at a time (loads in flight together)
-    while (m) {
-      uint32_t j[4], k = 0;
+  // lanes of this thread inside the wave (the rest clamp to 0xFFFF)
+  const uint32_t valid_lanes = live ? min(8u, kw > lane ? kw - lane : 0u) : 0u;
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  for (uint32_t ii = i0 + blockIdx.x; ii < i1; ii += gridDim.x) {
+    const uint4 it = item[ii];
+    // every warp evaluates the item's in-edges 32 at a time: warp lane t holds
+    // edge base + t, and a ballot gives the edges whose source row is active
+    // (the same masks in every warp)
+    uint4 acc = make_uint4(~0u, ~0u, ~0u, ~0u);
+    bool any = false;
+    for (uint32_t base = it.y; base < it.z; base += 32) {
+      const uint32_t e = base + t;
+      uint2 r = make_uint2(0, 0);
+      bool a = false;
+      if (e < it.z) {
+        r = erec[e];
+        a = (active[r.x >> 5] >> (r.x & 31)) & 1u;
+      }
+      uint32_t m = __ballot_sync(FULL, a);
+      any |= m != 0;
+      // gather the active sources four at a time (loads in flight together)
+      while (m) {
+        uint32_t j[4], k = 0;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        j[q] = m ? (uint32_t)(__ffs(m) - 1) : 32u;
-        if (m) {
-          m &= m - 1;
-          ++k;
+        for (int q = 0; q < 4; ++q) {
+          j[q] = m ? (uint32_t)(__ffs(m) - 1) : 0u;
+          if (m) {
+            m &= m - 1;
+            ++k;
+          }
+        }
+        uint32_t src[4], w[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          src[q] = __shfl_sync(FULL, r.x, j[q]);
+          w[q] = __shfl_sync(FULL, r.y, j[q]);
+        }
+        if (live) {
+          uint4 v[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            v[q] = q < (int)k ? *reinterpret_cast<const uint4*>(slab + (size_t)src[q] * Kp + lane)
+                              : make_uint4(~0u, ~0u, ~0u, ~0u);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const uint32_t w16 = min(w[q], 0xFFFFu), ww = w16 | (w16 << 16);
+            acc.x = __vminu2(acc.x, __vaddus2(v[q].x, ww));
+            acc.y = __vminu2(acc.y, __vaddus2(v[q].y, ww));
+            acc.z = __vminu2(acc.z, __vaddus2(v[q].z, ww));
+            acc.w = __vminu2(acc.w, __vaddus2(v[q].w, ww));
+          }
         }
       }
-      uint32_t src[4], w[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        src[q] = __shfl_sync(FULL, r.x, j[q] & 31);
-        w[q] = __shfl_sync(FULL, r.y, j[q] & 31);
-      }
-      if (live) {
-        uint4 v[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-          v[q] = q < (int)k ? *reinterpret_cast<const uint4*>(slab + (size_t)src[q] * Kp + lane)
-                            : make_uint4(~0u, ~0u, ~0u, ~0u);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) relax(v[q], w[q]);
-      }
     }
-  }
-  if (live) {
-    // clamp each lane to its threshold (lanes past the wave stay 0xFFFF)
-    uint32_t* w = &acc.x;
+    if (!any) continue;  // uniform across the block: the row keeps its seed or INF
+    // clamp each lane to its threshold
+    uint32_t* aw = &acc.x;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const uint32_t l = lane + 2 * q;
-      uint32_t lo = w[q] & 0xFFFFu, hi = w[q] >> 16;
-      if (l >= kw || lo > thr[l]) lo = 0xFFFFu;
-      if (l + 1 >= kw || hi > thr[l + 1]) hi = 0xFFFFu;
-      w[q] = lo | (hi << 16);
+      uint32_t lo = aw[q] & 0xFFFFu, hi = aw[q] >> 16;
+      if (2 * q >= (int)valid_lanes || lo > thr[lane + 2 * q]) lo = 0xFFFFu;
+      if (2 * q + 1 >= (int)valid_lanes || hi > thr[lane + 2 * q + 1]) hi = 0xFFFFu;
+      aw[q] = lo | (hi << 16);
     }
-  }
-  uint16_t* row = slab + (size_t)it.x * Kp;
-  uint4 v = acc;
-  if (live) {
-    uint32_t* dst = reinterpret_cast<uint32_t*>(row + lane);
-    if (it.w) {
-      atomic_min_u16x2(dst + 0, acc.x, err);
-      atomic_min_u16x2(dst + 1, acc.y, err);
-      atomic_min_u16x2(dst + 2, acc.z, err);
-      atomic_min_u16x2(dst + 3, acc.w, err);
-    } else {
-      // without a full slab reset only seeded rows hold valid data here
-      const bool valid = (seeded[it.x >> 5] >> (it.x & 31)) & 1u;
-      const uint4 c = valid ? *reinterpret_cast<const uint4*>(dst) : make_uint4(~0u, ~0u, ~0u, ~0u);
-      v.x = __vminu2(c.x, acc.x);
-      v.y = __vminu2(c.y, acc.y);
-      v.z = __vminu2(c.z, acc.z);
-      v.w = __vminu2(c.w, acc.w);
-      *reinterpret_cast<uint4*>(dst) = v;
+    if (live) {
+      uint32_t* dst = reinterpret_cast<uint32_t*>(slab + (size_t)it.x * Kp + lane);
+      if (it.w) {
+        atomic_min_u16x2(dst + 0, acc.x, err);
+        atomic_min_u16x2(dst + 1, acc.y, err);
+        atomic_min_u16x2(dst + 2, acc.z, err);
+        atomic_min_u16x2(dst + 3, acc.w, err);
+      } else {
+        // without a full slab reset only seeded rows hold valid data here
+        const bool valid = (seeded[it.x >> 5] >> (it.x & 31)) & 1u;
+        const uint4 c =
+            valid ? *reinterpret_cast<const uint4*>(dst) : make_uint4(~0u, ~0u, ~0u, ~0u);
+        uint4 v;
+        v.x = __vminu2(c.x, acc.x);
+        v.y = __vminu2(c.y, acc.y);
+        v.z = __vminu2(c.z, acc.z);
+        v.w = __vminu2(c.w, acc.w);
+        *reinterpret_cast<uint4*>(dst) = v;
+      }
     }
+    const bool act = live && (acc.x & acc.y & acc.z & acc.w) != ~0u;
+    const unsigned am = __ballot_sync(FULL, act);
+    if (am && t == (unsigned)(__ffs(am) - 1)) atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
   }
-  const bool act = live && (acc.x & acc.y & acc.z & acc.w) != ~0u;
-  const unsigned m = __ballot_sync(0xFFFFFFFFu, act);
-  if (m && (threadIdx.x & 31) == (unsigned)(__ffs(m) - 1))
-    atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
 }
 
 // bits: rows of w32 u32 words; lane l writes output row out_row[l]. A block
@@ -396,9 +395,10 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
       for (uint32_t l = 0; l < g->n_levels; ++l) {
         const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
         if (i1 == i0) continue;
-        BF_CUDA(launch_level(k_sweep_gated16, dim3(i1 - i0, lane_blocks), tpb, pdl, st,
-                             (const uint4*)sc.d_item, i0, (const uint2*)sc.d_erec, slab16, Kp,
-                             d_active, (const uint32_t*)(p_thr + s0), (uint32_t)kw,
+        const uint32_t blocks = std::min<uint32_t>(i1 - i0, GATED16_BLOCKS);
+        BF_CUDA(launch_level(k_sweep_gated16, dim3(blocks, lane_blocks), tpb, pdl, st,
+                             (const uint4*)sc.d_item, i0, i1, (const uint2*)sc.d_erec, slab16,
+                             Kp, d_active, (const uint32_t*)(p_thr + s0), (uint32_t)kw,
                              (const uint32_t*)d_seeded, g->d_err));
         ++launches;
       }
