@@ -313,6 +313,16 @@ bf_status bf_server_create(bf_graph* gh, const bf_server_cfg* cfg, bf_server** o
     if (rc == BF_OK && (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
                         cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess))
       rc = cuda_status(cudaGetLastError(), "stream/event create");
+    // the full-graph schedule isochrone batches sweep is built here, once per
+    // slot, so that no request waits for it
+    if (rc == BF_OK) {
+      try {
+        rc = build_schedule(g, sl.ctx, sl.ctx.full, nullptr, 0, true, sl.stream);
+      } catch (const std::bad_alloc&) {
+        set_error("out of host memory");
+        rc = BF_ERR_OOM;
+      }
+    }
     if (rc != BF_OK) {
       bf_server_destroy(h);
       return rc;
