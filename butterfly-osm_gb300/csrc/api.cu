@@ -260,6 +260,7 @@ static bf_tune to_c(const Tune& t) {
   o.small_level_edges = t.small_split;
   o.overlap_levels = t.pdl;
   o.isochrone_16bit = t.iso_half;
+  o.overlap_upward = t.overlap_up;
   return o;
 }
 
@@ -283,6 +284,7 @@ bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
   h->g.tune.small_split = t->small_level_rows ? t->small_level_edges : 8;
   h->g.tune.pdl = t->overlap_levels ? 1 : 0;
   h->g.tune.iso_half = t->isochrone_16bit ? 1 : 0;
+  h->g.tune.overlap_up = t->overlap_upward ? 1 : 0;
   return BF_OK;
 }
 

@@ -102,6 +102,10 @@ struct Ctx {
   size_t cap_pairs = 0;
   uint32_t* d_seeded = nullptr;    // [rows / 32] rows seeded by the current wave
   size_t cap_seeded = 0;
+  cudaStream_t aux = nullptr;      // side stream: upward pass overlapping the slab reset
+  cudaEvent_t fork = nullptr, join = nullptr;
+  uint2* d_cseed = nullptr;        // compact upward output [depth from root][source]
+  size_t cap_cseed = 0;
 };
 
 // Tunables of the batched sweep (chosen by bf_autotune).
@@ -115,6 +119,7 @@ struct Tune {
   uint32_t small_split = 8;
   uint32_t pdl = 1;          // level launches as programmatic dependents
   uint32_t iso_half = 1;     // 16-bit isochrone lanes when all thresholds fit
+  uint32_t overlap_up = 1;   // upward pass on a side stream during the slab reset
 };
 
 struct Graph {
@@ -205,7 +210,14 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
                         const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
                         cudaStream_t st, const uint32_t* lane_thr = nullptr,
                         const uint32_t* unit_cost = nullptr, const uint32_t* unit_lane = nullptr,
-                        bool half = false);
+                        uint32_t mode = 0);
+// Output of the upward pass: the u32 slab, a 16-bit slab (isochrone lanes), or
+// a compact per-source buffer of k x (max_depth + 1) {row, dist} entries that
+// launch_scatter_seeds writes into the slab later (so the pass can overlap
+// the slab reset).
+enum : uint32_t { UPWARD_OUT_SLAB32 = 0, UPWARD_OUT_SLAB16 = 1, UPWARD_OUT_COMPACT = 2 };
+bf_status launch_scatter_seeds(Graph* g, const void* cseed, uint64_t k, const uint32_t* d_src,
+                               uint32_t* slab, uint32_t Kp, cudaStream_t st);
 __global__ void k_extract(const uint32_t* __restrict__ slab, uint32_t slab_stride,
                           const uint32_t* __restrict__ tpos, uint64_t T, uint32_t k,
                           uint32_t* __restrict__ out);

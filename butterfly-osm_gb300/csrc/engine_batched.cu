@@ -487,13 +487,20 @@ void free_ctx(Ctx& c) {
   if (c.d_seeded) cudaFree(c.d_seeded);
   if (c.d_slab) cudaFree(c.d_slab);
   if (c.d_iso_tmp) cudaFree(c.d_iso_tmp);
+  if (c.d_cseed) cudaFree(c.d_cseed);
   for (auto& e : c.ev)
     if (e) cudaEventDestroy(e);
+  if (c.fork) cudaEventDestroy(c.fork);
+  if (c.join) cudaEventDestroy(c.join);
+  if (c.aux) cudaStreamDestroy(c.aux);
   c = Ctx();
 }
 
 bf_status init_ctx(Ctx& c) {
   for (auto& e : c.ev) BF_CUDA(cudaEventCreate(&e));
+  BF_CUDA(cudaStreamCreateWithFlags(&c.aux, cudaStreamNonBlocking));
+  BF_CUDA(cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming));
+  BF_CUDA(cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming));
   return BF_OK;
 }
 
@@ -631,9 +638,33 @@ bf_status batched_wave(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t kw, uin
   const unsigned lane_blocks = (Kp / 4 + tpb - 1) / tpb;
   (void)rows;
   if (timed) BF_CUDA(cudaEventRecord(c.ev[0], st));
-  if ((s = prepare_rows(g, c, sc, d_src, kw, Kp, st, launches))) return s;
-  if ((s = launch_upward(g, d_src, kw, INF, sc.d_cidx, c.d_slab, Kp, nullptr, st))) return s;
-  ++*launches;
+  // the upward pass is latency-bound and the slab reset bandwidth-bound: with
+  // a shallow enough tree the pass runs on the side stream into a compact
+  // buffer while the reset runs here, and a scatter joins them
+  const uint32_t dcap = ((g->max_depth + 1) + 31) & ~31u;
+  const bool overlap = g->tune.overlap_up && c.aux && (size_t)UPWARD_WARPS * 2 * dcap * 4 <= 200 * 1024;
+  if (overlap) {
+    const uint32_t words = (std::max<uint32_t>(sc.n_r, 1) + 31) / 32;
+    if ((s = ensure(&c.d_seeded, c.cap_seeded, words, g))) return s;
+    if ((s = ensure(&c.d_cseed, c.cap_cseed, kw * (g->max_depth + 1), g))) return s;
+    BF_CUDA(cudaMemsetAsync(c.d_seeded, 0, (size_t)words * 4, st));
+    launch_mark_paths(g, d_src, kw, sc.d_cidx, c.d_seeded, st);
+    BF_CUDA(cudaEventRecord(c.fork, st));
+    BF_CUDA(cudaStreamWaitEvent(c.aux, c.fork, 0));
+    if ((s = launch_upward(g, d_src, kw, INF, sc.d_cidx, reinterpret_cast<uint32_t*>(c.d_cseed),
+                           (uint32_t)kw, nullptr, c.aux, nullptr, nullptr, nullptr,
+                           UPWARD_OUT_COMPACT)))
+      return s;
+    BF_CUDA(cudaEventRecord(c.join, c.aux));
+    BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)std::max<uint32_t>(sc.n_r, 1) * Kp * 4, st));
+    BF_CUDA(cudaStreamWaitEvent(st, c.join, 0));
+    if ((s = launch_scatter_seeds(g, c.d_cseed, kw, d_src, c.d_slab, Kp, st))) return s;
+    *launches += 3;
+  } else {
+    if ((s = prepare_rows(g, c, sc, d_src, kw, Kp, st, launches))) return s;
+    if ((s = launch_upward(g, d_src, kw, INF, sc.d_cidx, c.d_slab, Kp, nullptr, st))) return s;
+    ++*launches;
+  }
   if (timed) BF_CUDA(cudaEventRecord(c.ev[1], st));
   return sweep_levels(g, sc, c.d_slab, Kp, lane_blocks, tpb, st, launches, c.d_seeded);
 }

@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
                   uint32_t n, uint32_t* __restrict__ seed, uint32_t seed_stride,
                   uint32_t* __restrict__ flag, uint32_t dcap, uint32_t* __restrict__ err,
                   const uint32_t* __restrict__ lane_thr, const uint32_t* __restrict__ unit_cost,
-                  const uint32_t* __restrict__ unit_lane, uint32_t half) {
+                  const uint32_t* __restrict__ unit_lane, uint32_t mode) {
   extern __shared__ uint32_t smem[];
   const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t w = blockIdx.x * UPWARD_WARPS + wib;
@@ -187,17 +187,41 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
   // with lane_thr, a seed above this lane's own threshold can never reach a
   // node within it: it is written but does not mark its row active
   const uint32_t lt = lane_thr ? lane_thr[out_lane] : threshold;
+  if (mode == UPWARD_OUT_COMPACT) {
+    // entry (D-1-l) * seed_stride + w: indexed from the root, so entries of
+    // different sources at one index mostly name the same top-of-tree row
+    uint2* out = reinterpret_cast<uint2*>(seed);
+    for (uint32_t l = lane; l < D; l += 32) {
+      const uint32_t d = *(const volatile uint32_t*)&pd[l];
+      const uint32_t p = (d == INF || d > threshold) ? NONE : pos_of[pn[l]];
+      out[(size_t)(D - 1 - l) * seed_stride + w] = make_uint2(p, d);
+    }
+    return;
+  }
   for (uint32_t l = lane; l < D; l += 32) {
     const uint32_t d = *(const volatile uint32_t*)&pd[l];
     if (d == INF || d > threshold) continue;
     const uint32_t p = pos_of[pn[l]];
     if (p == NONE) continue;
     if (unit_lane) atomicMin(&seed[(size_t)p * seed_stride + out_lane], d);
-    else if (half)  // 16-bit lanes: every stored d is within its lane threshold (< 0xFFFF)
+    else if (mode == UPWARD_OUT_SLAB16)  // every stored d is within its lane threshold (< 0xFFFF)
       reinterpret_cast<uint16_t*>(seed)[(size_t)p * seed_stride + w] = (uint16_t)d;
     else seed[(size_t)p * seed_stride + w] = d;
     if (flag && d <= lt) atomicOr(&flag[p >> 5], 1u << (p & 31));
   }
+}
+
+// Compact upward output -> slab: thread (w, i) writes entry i (counted from
+// the root) of source w's ancestor path into lane w of its row. Consecutive
+// threads are consecutive lanes, and near the root their rows coincide, so
+// those writes are whole lines.
+__global__ void __launch_bounds__(256)
+    k_scatter_seeds(const uint2* __restrict__ cseed, uint32_t k, const uint32_t* __restrict__ src,
+                    const uint32_t* __restrict__ depth, uint32_t* __restrict__ slab, uint32_t Kp) {
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+  if (w >= k || i > depth[src[w]]) return;
+  const uint2 e = cseed[(size_t)i * k + w];
+  if (e.x != NONE) slab[(size_t)e.x * Kp + w] = e.y;
 }
 
 // One level of the pull sweep: positions [p0, p1), a warp per node.
@@ -305,14 +329,24 @@ static bf_status plain_buffers(Graph* g) {
   return BF_OK;
 }
 
+bf_status launch_scatter_seeds(Graph* g, const void* cseed, uint64_t k, const uint32_t* d_src,
+                               uint32_t* slab, uint32_t Kp, cudaStream_t st) {
+  if (!k) return BF_OK;
+  dim3 grid((unsigned)((k + 255) / 256), g->max_depth + 1);
+  k_scatter_seeds<<<grid, 256, 0, st>>>(reinterpret_cast<const uint2*>(cseed), (uint32_t)k, d_src,
+                                       g->d_depth, slab, Kp);
+  BF_CUDA(cudaGetLastError());
+  return BF_OK;
+}
+
 // Upward pass for k sources: source i writes lane i of row pos_map[x] of
 // `seed` (stride lanes per row) for every settled ancestor x; rows mapped to
 // NONE are skipped. `flag` (optional) receives the seeded-row bits.
 bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t threshold,
                         const uint32_t* pos_map, uint32_t* seed, uint32_t stride, uint32_t* flag,
                         cudaStream_t st, const uint32_t* lane_thr, const uint32_t* unit_cost,
-                        const uint32_t* unit_lane, bool half) {
-  if (half && (!lane_thr || unit_lane)) {
+                        const uint32_t* unit_lane, uint32_t mode) {
+  if (mode == UPWARD_OUT_SLAB16 && (!lane_thr || unit_lane)) {
     set_error("16-bit seed lanes need per-lane thresholds below 0xFFFF");
     return BF_ERR_UNSUPPORTED;
   }
@@ -326,7 +360,7 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
                     fast_smem, st>>>(d_src, (uint32_t)k, threshold, g->d_parent, g->d_run_end,
                                      g->d_depth, g->d_up_off, g->d_up_rec, pos_map, g->n, seed,
                                      stride, flag, dcap, g->d_err, lane_thr, unit_cost,
-                                     unit_lane, half ? 1u : 0u);
+                                     unit_lane, mode);
     BF_CUDA(cudaGetLastError());
     return BF_OK;
   }
@@ -342,7 +376,7 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
       }
       g->device_bytes += bytes;
     }
-    if (lane_thr || unit_cost || unit_lane) {
+    if (lane_thr || unit_cost || unit_lane || mode != UPWARD_OUT_SLAB32) {
       set_error("seeded units and per-lane thresholds need the shared-memory upward pass "
                 "(elimination tree too deep)");
       return BF_ERR_UNSUPPORTED;

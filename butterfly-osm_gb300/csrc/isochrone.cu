@@ -386,7 +386,8 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
     launch_init_rows(d_seeded, sc.d_split, (uint32_t)aw, c.d_slab, Kp * lb / 4, st);
     launches += 2;
     if ((s = launch_upward(g, p_orig + s0, kw, INF, sc.d_cidx, c.d_slab, Kp, d_active, st,
-                           p_thr + s0, nullptr, nullptr, half)))
+                           p_thr + s0, nullptr, nullptr,
+                           half ? UPWARD_OUT_SLAB16 : UPWARD_OUT_SLAB32)))
       return s;
     ++launches;
     if (stats) BF_CUDA(cudaEventRecord(c.ev[1], st));

@@ -171,6 +171,8 @@ typedef struct bf_tune {
   uint32_t isochrone_16bit;    /* 1: isochrone calls whose thresholds are all
                                   below 0xFFFF keep 16-bit lanes clamped at the
                                   threshold (exact, half the bytes)             */
+  uint32_t overlap_upward;     /* 1: matrix waves run the upward pass on a side
+                                  stream while the slab is reset               */
 } bf_tune;
 
 /* Time candidate tunables on a sample matrix (device buffers: d_sources,

@@ -151,7 +151,7 @@ def test_duplicate_sources_and_targets(built, grid100):
                                   dict(threads_per_block=256, edges_per_item=64,
                                        graph_capture=1, lanes_per_wave=0),
                                   dict(threads_per_block=64, edges_per_item=3, graph_capture=1,
-                                       lanes_per_wave=64),
+                                       lanes_per_wave=64, overlap_upward=0),
                                   dict(threads_per_block=128, edges_per_item=16, graph_capture=1,
                                        lanes_per_wave=0, small_level_rows=4096,
                                        small_level_edges=2)])
