@@ -57,7 +57,8 @@ class Stats(ctypes.Structure):
                 ("extract_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("swept_nodes", ctypes.c_uint64), ("swept_edges", ctypes.c_uint64),
-                ("lanes", ctypes.c_uint64), ("waves", ctypes.c_uint64)]
+                ("lanes", ctypes.c_uint64), ("waves", ctypes.c_uint64),
+                ("schedule_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

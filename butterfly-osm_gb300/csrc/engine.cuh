@@ -96,8 +96,9 @@ struct Ctx {
   size_t iso_tmp_bytes = 0;
   cudaEvent_t ev[4] = {};
   uint64_t budget = 0;             // slab bytes this context may use (0 = graph budget)
-  std::vector<uint8_t> mark;       // host scratch [n], all 0 between builds
   std::vector<uint32_t> rowmap;    // host scratch [n], all NONE between builds
+  std::vector<uint64_t> markbits;  // host scratch [n bits], all 0 between builds
+  std::vector<std::vector<uint32_t>> buckets;  // host scratch per level, empty between builds
   uint32_t* d_pairs = nullptr;     // device scratch for (rank, row) updates
   size_t cap_pairs = 0;
   uint32_t* d_seeded = nullptr;    // [rows / 32] rows seeded by the current wave

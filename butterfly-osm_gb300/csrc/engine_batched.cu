@@ -19,8 +19,10 @@
 //     transpose; cells above the threshold become INF.
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <queue>
+#include <thread>
 
 #include "engine.cuh"
 
@@ -59,6 +61,26 @@ bf_status ensure(T** p, size_t& cap, size_t need, Graph* g) {
   return BF_OK;
 }
 
+// Run f(b, e) over [0, n) split into contiguous chunks on host threads
+// (single-threaded below `grain` units per thread).
+template <class F>
+void parallel_chunks(uint64_t n, uint64_t grain, F f) {
+  uint64_t nt = std::min<uint64_t>(std::max(1u, std::thread::hardware_concurrency()), 16);
+  nt = std::min<uint64_t>(nt, std::max<uint64_t>(1, n / std::max<uint64_t>(grain, 1)));
+  if (nt <= 1) {
+    f(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const uint64_t step = (n + nt - 1) / nt;
+  for (uint64_t t = 1; t < nt; ++t) {
+    const uint64_t b = std::min(n, t * step), e = std::min(n, (t + 1) * step);
+    th.emplace_back([&f, b, e] { f(b, e); });
+  }
+  f(0, std::min(n, step));
+  for (auto& x : th) x.join();
+}
+
 }  // namespace
 
 __global__ void k_scatter_pairs(const uint2* __restrict__ pr, uint64_t m,
@@ -94,92 +116,114 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
     sc.gexec = nullptr;
   }
   const uint32_t n = g->n;
-  if (c.mark.size() != n) {
-    c.mark.assign(n, 0);
-    c.rowmap.assign(n, NONE);
-  }
-  std::vector<uint32_t> R;  // restricted positions, ascending
+  if (c.rowmap.size() != n) c.rowmap.assign(n, NONE);
+  // restricted positions grouped by level, levels ascending (the order inside
+  // a level does not matter: no edge joins two rows of one level)
+  std::vector<uint32_t> R;
   if (all) {
     R.resize(n);
     for (uint32_t p = 0; p < n; ++p) R[p] = p;
   } else {
-    std::priority_queue<uint32_t> pq;
-    for (uint64_t i = 0; i < T; ++i) {
-      const uint32_t p = g->pos_of[h_tgt[i]];
-      if (!c.mark[p]) {
-        c.mark[p] = 1;
-        pq.push(p);
+    // walk in-edges from the targets one level at a time, deepest level
+    // first: in-edge sources always sit in lower levels, so a level's bucket
+    // is complete when it is reached. Marks are a bitmap (n bits), small
+    // enough to stay in the host caches.
+    const uint32_t L = g->n_levels;
+    auto level_of = [&](uint32_t p) {
+      return (uint32_t)(std::upper_bound(g->lvl_start.begin(), g->lvl_start.end(), p) -
+                        g->lvl_start.begin() - 1);
+    };
+    if (c.markbits.size() != (n + 63) / 64) c.markbits.assign((n + 63) / 64, 0);
+    if (c.buckets.size() != L) c.buckets.assign(L, {});
+    uint64_t* mb = c.markbits.data();
+    auto mark = [&](uint32_t p) {
+      uint64_t& w = mb[p >> 6];
+      const uint64_t b = 1ull << (p & 63);
+      if (w & b) return;
+      w |= b;
+      c.buckets[level_of(p)].push_back(p);
+    };
+    for (uint64_t i = 0; i < T; ++i) mark(g->pos_of[h_tgt[i]]);
+    for (uint32_t l = L; l-- > 0;)
+      for (size_t j = 0; j < c.buckets[l].size(); ++j) {
+        const uint32_t p = c.buckets[l][j];
+        for (uint64_t k = g->h_in_off[p]; k < g->h_in_off[p + 1]; ++k) mark(g->h_in_rec[k].x);
       }
+    size_t tot = 0;
+    for (auto& b : c.buckets) tot += b.size();
+    R.reserve(tot);
+    for (auto& b : c.buckets) {
+      R.insert(R.end(), b.begin(), b.end());
+      b.clear();
     }
-    while (!pq.empty()) {
-      const uint32_t p = pq.top();
-      pq.pop();
-      R.push_back(p);
-      for (uint64_t k = g->h_in_off[p]; k < g->h_in_off[p + 1]; ++k) {
-        const uint32_t u = g->h_in_rec[k].x;
-        if (!c.mark[u]) {
-          c.mark[u] = 1;
-          pq.push(u);
-        }
-      }
-    }
-    std::reverse(R.begin(), R.end());
-    for (uint32_t p : R) c.mark[p] = 0;
+    for (uint32_t p : R) mb[p >> 6] = 0;
   }
   const uint32_t n_r = (uint32_t)R.size();
   for (uint32_t i = 0; i < n_r; ++i) c.rowmap[R[i]] = i;
-  std::vector<uint4> items;
-  std::vector<uint2> erec;
-  std::vector<uint32_t> elen;  // two-channel graphs: length weight per erec entry
   const bool two = g->has_len;
-  std::vector<uint32_t> split_bits((n_r + 31) / 32 + 1, 0);
-  sc.lvl_item.assign(g->n_levels + 1, 0);
-  // rows per level of the restricted set: small levels get short work items
-  std::vector<uint32_t> lvl_rows(g->n_levels + 1, 0);
+  // rows per level; small levels get short work items
+  std::vector<uint32_t> row_lvl(g->n_levels + 1, 0);
   {
     uint32_t l = 0;
     for (uint32_t i = 0; i < n_r; ++i) {
-      while (R[i] >= g->lvl_start[l + 1]) ++l;
-      ++lvl_rows[l];
+      while (R[i] >= g->lvl_start[l + 1]) row_lvl[++l] = i;
+    }
+    while (l < g->n_levels) row_lvl[++l] = n_r;
+  }
+  // per row: edge and item offsets (prefix sums), then a parallel fill
+  std::vector<uint64_t> eoff(n_r + 1, 0), ioff(n_r + 1, 0);
+  std::vector<uint32_t> split_of(n_r);
+  for (uint32_t l = 0; l < g->n_levels; ++l) {
+    const uint32_t rows_l = row_lvl[l + 1] - row_lvl[l];
+    const uint32_t split_l = rows_l < SMALL_ROWS ? SMALL_SPLIT : SPLIT;
+    for (uint32_t i = row_lvl[l]; i < row_lvl[l + 1]; ++i) {
+      const uint32_t p = R[i];
+      const uint64_t deg = g->h_in_off[p + 1] - g->h_in_off[p];
+      split_of[i] = split_l;
+      eoff[i + 1] = eoff[i] + deg;
+      ioff[i + 1] = ioff[i] + (deg + split_l - 1) / split_l;
     }
   }
-  // items of a level, heaviest first, so the level's last blocks are short
-  auto close_level = [&](uint32_t l) {
-    std::stable_sort(items.begin() + sc.lvl_item[l], items.end(),
-                     [](const uint4& a, const uint4& b) { return a.z - a.y > b.z - b.y; });
-  };
-  uint32_t lvl = 0;
-  uint32_t split_l = lvl_rows[0] < SMALL_ROWS ? SMALL_SPLIT : SPLIT;
-  for (uint32_t i = 0; i < n_r; ++i) {
-    const uint32_t p = R[i];
-    while (p >= g->lvl_start[lvl + 1]) {
-      close_level(lvl);
-      sc.lvl_item[++lvl] = (uint32_t)items.size();
-      split_l = lvl_rows[lvl] < SMALL_ROWS ? SMALL_SPLIT : SPLIT;
-    }
-    const uint64_t k0 = g->h_in_off[p], k1 = g->h_in_off[p + 1];
-    if (k0 == k1) {  // no in-edges: the row is its seed (or INF): reset every wave
-      split_bits[i >> 5] |= 1u << (i & 31);
-      continue;
-    }
-    const uint32_t e0 = (uint32_t)erec.size();
-    for (uint64_t k = k0; k < k1; ++k) {
-      erec.push_back(make_uint2(c.rowmap[g->h_in_rec[k].x], g->h_in_rec[k].y));
-      if (two) elen.push_back(g->h_in_len[k]);
-    }
-    const uint32_t deg = (uint32_t)(k1 - k0);
-    const uint32_t split = deg > split_l ? 1u : 0u;
-    if (split) split_bits[i >> 5] |= 1u << (i & 31);
-    for (uint32_t a = 0; a < deg; a += split_l)
-      items.push_back(make_uint4(i, e0 + a, e0 + std::min(deg, a + split_l), split));
-  }
-  close_level(lvl);
-  while (lvl < g->n_levels) sc.lvl_item[++lvl] = (uint32_t)items.size();
-  if (erec.size() > 0xFFFFFFFFull) {
+  if (eoff[n_r] > 0xFFFFFFFFull) {
     for (uint32_t p : R) c.rowmap[p] = NONE;
     set_error("restricted edge set exceeds 2^32 edges");
     return BF_ERR_UNSUPPORTED;
   }
+  std::vector<uint2> erec(eoff[n_r]);
+  std::vector<uint32_t> elen(two ? eoff[n_r] : 0);  // length weight per erec entry
+  std::vector<uint4> items(ioff[n_r]);
+  std::vector<uint32_t> split_bits((n_r + 31) / 32 + 1, 0);
+  // chunks of whole 32-row groups, so no two threads share a split_bits word
+  parallel_chunks((n_r + 31) / 32, 256, [&](uint64_t w0, uint64_t w1) {
+    const uint32_t i1 = (uint32_t)std::min<uint64_t>(n_r, w1 * 32);
+    for (uint32_t i = (uint32_t)(w0 * 32); i < i1; ++i) {
+      const uint32_t p = R[i];
+      const uint64_t k0 = g->h_in_off[p], k1 = g->h_in_off[p + 1];
+      if (k0 == k1) {  // no in-edges: the row is its seed (or INF): reset every wave
+        split_bits[i >> 5] |= 1u << (i & 31);
+        continue;
+      }
+      const uint32_t e0 = (uint32_t)eoff[i];
+      for (uint64_t k = k0; k < k1; ++k) {
+        erec[e0 + (k - k0)] = make_uint2(c.rowmap[g->h_in_rec[k].x], g->h_in_rec[k].y);
+        if (two) elen[e0 + (k - k0)] = g->h_in_len[k];
+      }
+      const uint32_t deg = (uint32_t)(k1 - k0), sp = split_of[i];
+      const uint32_t split = deg > sp ? 1u : 0u;
+      if (split) split_bits[i >> 5] |= 1u << (i & 31);
+      uint64_t it = ioff[i];
+      for (uint32_t a = 0; a < deg; a += sp)
+        items[it++] = make_uint4(i, e0 + a, e0 + std::min(deg, a + sp), split);
+    }
+  });
+  sc.lvl_item.assign(g->n_levels + 1, 0);
+  for (uint32_t l = 0; l <= g->n_levels; ++l) sc.lvl_item[l] = (uint32_t)ioff[row_lvl[l]];
+  // items of a level, heaviest first, so the level's last blocks are short
+  parallel_chunks(g->n_levels, 16, [&](uint64_t l0, uint64_t l1) {
+    for (uint64_t l = l0; l < l1; ++l)
+      std::stable_sort(items.begin() + sc.lvl_item[l], items.begin() + sc.lvl_item[l + 1],
+                       [](const uint4& a, const uint4& b) { return a.z - a.y > b.z - b.y; });
+  });
   std::vector<uint32_t> trow(T);
   for (uint64_t i = 0; i < T; ++i) trow[i] = c.rowmap[g->pos_of[h_tgt[i]]];
   // device rank -> row map: reset the previous schedule's entries, set ours
@@ -681,7 +725,11 @@ bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, co
       set_error("targets[" + std::to_string(i) + "] is not a node of the graph");
       return BF_ERR_INVALID;
     }
+  const auto tb = std::chrono::steady_clock::now();
   if ((s = build_schedule(g, c, c.sc, h_tgt.data(), T, false, st))) return s;
+  if (stats)
+    stats->schedule_ms +=
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();
   Sched& sc = c.sc;
   const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
   // lanes per wave: all sources if the slab fits the budget, else waves

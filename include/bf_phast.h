@@ -142,6 +142,7 @@ typedef struct bf_stats {
   uint64_t swept_edges;       /* DOWN edges relaxed per lane (per wave)           */
   uint64_t lanes;             /* lanes (sources) per wave, padded to 4            */
   uint64_t waves;             /* sweeps run                                       */
+  double schedule_ms;         /* host time building sweep schedules (0 on reuse)  */
 } bf_stats;
 
 bf_status bf_graph_create(const bf_cch_csr* csr, const bf_config* cfg, bf_graph** out);
