@@ -58,6 +58,31 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// One level of the gated single-lane sweep (one bounded query): a thread per
+// work item. A source row takes part only when its bit in `active` is set (a
+// distance within the threshold); a row whose new distance is within the
+// threshold sets its own bit. The slab is one INF-initialised u32 per row.
+__global__ void __launch_bounds__(128)
+    k_sweep_one(const uint4* __restrict__ item, uint32_t i0, uint32_t i1,
+                const uint2* __restrict__ erec, uint32_t* __restrict__ slab,
+                uint32_t* __restrict__ active, uint32_t threshold) {
+  asm volatile("griddepcontrol.launch_dependents;");
+  const uint32_t i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (i >= i1) return;
+  const uint4 it = item[i];
+  uint32_t acc = INF;
+  for (uint32_t e = it.y; e < it.z; ++e) {
+    const uint2 r = erec[e];
+    if (!((active[r.x >> 5] >> (r.x & 31)) & 1u)) continue;
+    acc = min(acc, sat_add(slab[r.x], r.y));
+  }
+  if (acc > threshold) return;  // cannot lead to a distance within the threshold
+  if (it.w) atomicMin(&slab[it.x], acc);
+  else if (acc < slab[it.x]) slab[it.x] = acc;
+  atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
+}
+
 // Settled-set compaction for one lane (lane 0): ranks in blocks of 1024.
 __device__ __forceinline__ bool settled(const uint32_t* slab, uint32_t Kp, const uint32_t* cidx,
                                         const uint32_t* active, uint32_t rank, uint32_t n,
@@ -232,7 +257,7 @@ bf_status bounded_seeded(Graph* g, Ctx& c, const bf_seed* seeds, uint32_t n_seed
   bf_status rc;
   if ((rc = build_schedule(g, c, c.full, nullptr, 0, true, s))) return rc;
   Sched& sc = c.full;
-  const uint32_t Kp = 4, n = g->n;
+  const uint32_t Kp = 1, n = g->n;
   const uint64_t aw = (n + 31) / 32, nb = (n + 1023) / 1024;
   if ((rc = ensure_slab(g, c, (size_t)n * Kp * 4))) return rc;
   Dev d_u, d_act, d_cnt, d_off, d_res;
@@ -256,8 +281,14 @@ bf_status bounded_seeded(Graph* g, Ctx& c, const bf_seed* seeds, uint32_t n_seed
       (rc = launch_upward(g, du, n_seeds, threshold, sc.d_cidx, c.d_slab, Kp,
                           d_act.as<uint32_t>(), s, d_thr, du + n_seeds, du + 2 * (size_t)n_seeds)))
     return rc;
-  if ((rc = sweep_levels_gated(g, sc, c.d_slab, Kp, 1, 32, d_act.as<uint32_t>(), d_thr, 1, s, &launches)))
-    return rc;
+  for (uint32_t l = 0; l < g->n_levels; ++l) {
+    const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
+    if (i1 == i0) continue;
+    BF_CUDA(launch_level(k_sweep_one, dim3((i1 - i0 + 127) / 128), 128, g->tune.pdl != 0, s,
+                         (const uint4*)sc.d_item, i0, i1, (const uint2*)sc.d_erec, c.d_slab,
+                         d_act.as<uint32_t>(), threshold));
+    ++launches;
+  }
   k_rank_count<<<(unsigned)nb, 1024, 0, s>>>(c.d_slab, Kp, sc.d_cidx, d_act.as<uint32_t>(), n,
                                             threshold, d_cnt.as<uint32_t>());
   BF_CUDA(cudaGetLastError());

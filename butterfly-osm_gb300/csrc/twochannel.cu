@@ -177,7 +177,9 @@ __global__ void __launch_bounds__(128)
                     const uint2* __restrict__ erec, const uint32_t* __restrict__ elen,
                     uint64_t* __restrict__ slab, uint32_t* __restrict__ active,
                     uint32_t threshold) {
+  asm volatile("griddepcontrol.launch_dependents;");
   const uint32_t i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   if (i >= i1) return;
   const uint4 it = item[i];
   uint64_t acc = LINF;
@@ -532,8 +534,9 @@ bf_status bounded_seeded_2ch(Graph* g, Ctx& c, const bf_seed2* seeds, uint32_t n
   for (uint32_t l = 0; l < g->n_levels; ++l) {
     const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
     if (i1 == i0) continue;
-    k_sweep_one_2ch<<<(i1 - i0 + 127) / 128, 128, 0, s>>>(sc.d_item, i0, i1, sc.d_erec, sc.d_elen,
-                                                         slab, act, threshold);
+    BF_CUDA(launch_level(k_sweep_one_2ch, dim3((i1 - i0 + 127) / 128), 128, g->tune.pdl != 0, s,
+                         (const uint4*)sc.d_item, i0, i1, (const uint2*)sc.d_erec,
+                         (const uint32_t*)sc.d_elen, slab, act, threshold));
   }
   BF_CUDA(cudaGetLastError());
   k_count_2ch<<<(unsigned)nb, 1024, 0, s>>>(slab, sc.d_cidx, act, n, threshold,
