@@ -80,6 +80,11 @@ struct Sched {
   cudaStream_t g_stream = nullptr;
   const uint32_t* g_seeded = nullptr;
   bool g_pdl = false;
+  // captured single-lane bounded sweep (full schedule), with its geometry
+  cudaGraphExec_t one_exec = nullptr;
+  const void* one_slab = nullptr;
+  const void* one_state = nullptr;
+  bool one_pdl = false;
   std::vector<uint32_t> ranks;   // ranks whose d_cidx entry is set (reset on rebuild)
   bool cidx_ready = false;       // d_cidx holds NONE outside `ranks`
 };
@@ -107,6 +112,8 @@ struct Ctx {
   cudaEvent_t fork = nullptr, join = nullptr;
   uint2* d_cseed = nullptr;        // compact upward output [depth from root][source]
   size_t cap_cseed = 0;
+  uint32_t* d_one = nullptr;       // bounded-query state: active bitmap, then the threshold
+  size_t cap_one = 0;
 };
 
 // Tunables of the batched sweep (chosen by bf_autotune).

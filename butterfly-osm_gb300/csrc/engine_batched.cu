@@ -115,6 +115,10 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
     cudaGraphExecDestroy(sc.gexec);
     sc.gexec = nullptr;
   }
+  if (sc.one_exec) {
+    cudaGraphExecDestroy(sc.one_exec);
+    sc.one_exec = nullptr;
+  }
   const uint32_t n = g->n;
   if (c.rowmap.size() != n) c.rowmap.assign(n, NONE);
   // restricted positions grouped by level, levels ascending (the order inside
@@ -521,6 +525,7 @@ static void free_sched(Sched& sc) {
   for (void* q : p)
     if (q) cudaFree(q);
   if (sc.gexec) cudaGraphExecDestroy(sc.gexec);
+  if (sc.one_exec) cudaGraphExecDestroy(sc.one_exec);
   sc = Sched();
 }
 
@@ -532,6 +537,7 @@ void free_ctx(Ctx& c) {
   if (c.d_slab) cudaFree(c.d_slab);
   if (c.d_iso_tmp) cudaFree(c.d_iso_tmp);
   if (c.d_cseed) cudaFree(c.d_cseed);
+  if (c.d_one) cudaFree(c.d_one);
   for (auto& e : c.ev)
     if (e) cudaEventDestroy(e);
   if (c.fork) cudaEventDestroy(c.fork);

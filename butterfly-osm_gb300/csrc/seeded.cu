@@ -65,11 +65,12 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(128)
     k_sweep_one(const uint4* __restrict__ item, uint32_t i0, uint32_t i1,
                 const uint2* __restrict__ erec, uint32_t* __restrict__ slab,
-                uint32_t* __restrict__ active, uint32_t threshold) {
+                uint32_t* __restrict__ active, const uint32_t* __restrict__ thr) {
   asm volatile("griddepcontrol.launch_dependents;");
   const uint32_t i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
   asm volatile("griddepcontrol.wait;" ::: "memory");
   if (i >= i1) return;
+  const uint32_t threshold = *thr;
   const uint4 it = item[i];
   uint32_t acc = INF;
   for (uint32_t e = it.y; e < it.z; ++e) {
@@ -260,9 +261,27 @@ bf_status bounded_seeded(Graph* g, Ctx& c, const bf_seed* seeds, uint32_t n_seed
   const uint32_t Kp = 1, n = g->n;
   const uint64_t aw = (n + 31) / 32, nb = (n + 1023) / 1024;
   if ((rc = ensure_slab(g, c, (size_t)n * Kp * 4))) return rc;
-  Dev d_u, d_act, d_cnt, d_off, d_res;
-  if (!d_u.alloc((size_t)n_seeds * 12 + 16) || !d_act.alloc(aw * 4) || !d_cnt.alloc(nb * 4) ||
-      !d_off.alloc(nb * 8))
+  // persistent query state (active bitmap + threshold word) so that the level
+  // launches can be replayed from a captured graph
+  if (c.cap_one < aw + 4) {
+    if (c.d_one) {
+      cudaFree(c.d_one);
+      g->device_bytes -= c.cap_one * 4;
+      c.d_one = nullptr;
+      c.cap_one = 0;
+    }
+    if (cudaMalloc(&c.d_one, (aw + 4) * 4) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc for the bounded-query state failed");
+      return BF_ERR_OOM;
+    }
+    c.cap_one = aw + 4;
+    g->device_bytes += c.cap_one * 4;
+  }
+  uint32_t* act = c.d_one;
+  uint32_t* d_thr = c.d_one + aw;
+  Dev d_u, d_cnt, d_off, d_res;
+  if (!d_u.alloc((size_t)n_seeds * 12 + 16) || !d_cnt.alloc(nb * 4) || !d_off.alloc(nb * 8))
     return BF_ERR_OOM;
   std::vector<uint32_t> units(3 * (size_t)n_seeds + 4, 0);
   for (uint32_t i = 0; i < n_seeds; ++i) {
@@ -270,26 +289,60 @@ bf_status bounded_seeded(Graph* g, Ctx& c, const bf_seed* seeds, uint32_t n_seed
     units[n_seeds + i] = seeds[i].cost;
     units[2 * (size_t)n_seeds + i] = 0;
   }
-  units[3 * (size_t)n_seeds] = threshold;  // lane 0's threshold
   uint32_t* du = d_u.as<uint32_t>();
   BF_CUDA(cudaMemcpyAsync(du, units.data(), units.size() * 4, cudaMemcpyHostToDevice, s));
-  const uint32_t* d_thr = du + 3 * (size_t)n_seeds;
+  BF_CUDA(cudaMemcpyAsync(d_thr, &threshold, 4, cudaMemcpyHostToDevice, s));  // lane 0's threshold
   BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)n * Kp * 4, s));
-  BF_CUDA(cudaMemsetAsync(d_act.p, 0, aw * 4, s));
+  BF_CUDA(cudaMemsetAsync(act, 0, aw * 4, s));
   uint64_t launches = 0;
-  if (n_seeds &&
-      (rc = launch_upward(g, du, n_seeds, threshold, sc.d_cidx, c.d_slab, Kp,
-                          d_act.as<uint32_t>(), s, d_thr, du + n_seeds, du + 2 * (size_t)n_seeds)))
+  if (n_seeds && (rc = launch_upward(g, du, n_seeds, threshold, sc.d_cidx, c.d_slab, Kp, act, s,
+                                     d_thr, du + n_seeds, du + 2 * (size_t)n_seeds)))
     return rc;
-  for (uint32_t l = 0; l < g->n_levels; ++l) {
-    const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
-    if (i1 == i0) continue;
-    BF_CUDA(launch_level(k_sweep_one, dim3((i1 - i0 + 127) / 128), 128, g->tune.pdl != 0, s,
-                         (const uint4*)sc.d_item, i0, i1, (const uint2*)sc.d_erec, c.d_slab,
-                         d_act.as<uint32_t>(), threshold));
-    ++launches;
+  const bool pdl = g->tune.pdl != 0;
+  auto issue = [&](cudaStream_t st) -> cudaError_t {
+    for (uint32_t l = 0; l < g->n_levels; ++l) {
+      const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
+      if (i1 == i0) continue;
+      cudaError_t e = launch_level(k_sweep_one, dim3((i1 - i0 + 127) / 128), 128, pdl, st,
+                                   (const uint4*)sc.d_item, i0, i1, (const uint2*)sc.d_erec,
+                                   c.d_slab, act, (const uint32_t*)d_thr);
+      if (e != cudaSuccess) return e;
+      ++launches;
+    }
+    return cudaSuccess;
+  };
+  // the schedule is static: from its second use the level launches are
+  // captured once and replayed (geometry: slab, state, launch mode)
+  if (sc.one_exec && (sc.one_slab != c.d_slab || sc.one_state != c.d_one || sc.one_pdl != pdl)) {
+    cudaGraphExecDestroy(sc.one_exec);
+    sc.one_exec = nullptr;
   }
-  k_rank_count<<<(unsigned)nb, 1024, 0, s>>>(c.d_slab, Kp, sc.d_cidx, d_act.as<uint32_t>(), n,
+  if (!sc.one_exec && sc.uses >= 1 && g->tune.graphs) {
+    cudaGraph_t graph;
+    uint64_t before = launches;
+    BF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t le = issue(s);
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    launches = before;
+    if (le != cudaSuccess) {
+      if (ce == cudaSuccess) cudaGraphDestroy(graph);
+      return cuda_status(le, "level launch during capture");
+    }
+    if (ce != cudaSuccess) return cuda_status(ce, "cudaStreamEndCapture");
+    const cudaError_t ie = cudaGraphInstantiate(&sc.one_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return cuda_status(ie, "cudaGraphInstantiate");
+    sc.one_slab = c.d_slab;
+    sc.one_state = c.d_one;
+    sc.one_pdl = pdl;
+  }
+  if (sc.one_exec && g->tune.graphs) {
+    BF_CUDA(cudaGraphLaunch(sc.one_exec, s));
+  } else {
+    BF_CUDA(issue(s));
+  }
+  BF_CUDA(cudaGetLastError());
+  k_rank_count<<<(unsigned)nb, 1024, 0, s>>>(c.d_slab, Kp, sc.d_cidx, act, n,
                                             threshold, d_cnt.as<uint32_t>());
   BF_CUDA(cudaGetLastError());
   std::vector<uint32_t> cnt(nb);
@@ -305,7 +358,7 @@ bf_status bounded_seeded(Graph* g, Ctx& c, const bf_seed* seeds, uint32_t n_seed
   const uint64_t keep = std::min<uint64_t>(tot, cap);
   if (!d_res.alloc(keep * 8 + 16)) return BF_ERR_OOM;
   BF_CUDA(cudaMemcpyAsync(d_off.p, off.data(), nb * 8, cudaMemcpyHostToDevice, s));
-  k_rank_scatter<<<(unsigned)nb, 1024, 0, s>>>(c.d_slab, Kp, sc.d_cidx, d_act.as<uint32_t>(), n,
+  k_rank_scatter<<<(unsigned)nb, 1024, 0, s>>>(c.d_slab, Kp, sc.d_cidx, act, n,
                                               threshold, d_off.as<uint64_t>(), keep,
                                               d_res.as<uint32_t>(), d_res.as<uint32_t>() + keep);
   BF_CUDA(cudaGetLastError());
