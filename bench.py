@@ -139,8 +139,14 @@ def cpu_sample(cch, src, tgt, budget_s, rows=None):
     c = orc.Cch.from_dict(cch)
     threads = os.cpu_count() or 1
     if rows is None:
-        # at least a 1% row sample; ~10 K=8 batches per host thread
-        rows = max(8, min(len(src), max(len(src) // 100, 80 * threads)))
+        # calibrate on 2 K=8 batches per host thread, then size the sample to
+        # about budget_s seconds of CPU work (at least a 1% row sample)
+        cal = max(8, min(len(src), 16 * threads))
+        t0 = time.perf_counter()
+        c.matrix(src[np.linspace(0, len(src) - 1, cal).astype(np.int64)], tgt, threads=threads)
+        per_row = (time.perf_counter() - t0) / cal
+        rows = int(budget_s / max(per_row, 1e-9))
+        rows = max(8, min(len(src), max(rows, len(src) // 100)))
     pick = np.linspace(0, len(src) - 1, rows).astype(np.int64)
     t0 = time.perf_counter()
     m, used = c.matrix(src[pick], tgt, threads=threads)
