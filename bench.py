@@ -161,6 +161,7 @@ def run_ours(args, rank, world, dist):
     import numpy as np
     import torch
     import bfphast
+    import replicas
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     cch, src, tgt = build_workload(args, seed=42 + rank)
@@ -201,12 +202,8 @@ def run_ours(args, rank, world, dist):
         torch.cuda.synchronize()
     sync()
     ms = e0.elapsed_time(e1) / args.steps
-    ms_all = ms
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_all = float(t.item())
-    value = world * S * T / (ms_all / 1e3)
+    ms_all = replicas.max_over_ranks(ms, dist, device="cuda")
+    value = replicas.whole_job_rate(S * T, world, ms_all / 1e3)
     out_dev = d_out.view(S, T).cpu().numpy().view(np.uint32)
 
     # e2e: host (pinned) buffers through bf_matrix, copies inside the region
@@ -220,11 +217,7 @@ def run_ours(args, rank, world, dist):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         g.matrix(h_src, h_tgt, out=h_out)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / args.steps, dist, device="cuda")
     e2e_ok = bool(np.array_equal(h_out, out_dev))
 
     # roofline of the dominant kernel (the restricted downward sweep)
@@ -266,7 +259,7 @@ def run_ours(args, rank, world, dist):
                       "l2": "slab of %.1f GB rewritten every step (> L2)"
                             % (st["lanes"] * max(N, 1) * 4 / 1e9),
                       "tune": tune},
-           "e2e": {"value": round(world * S * T / e2e_s, 1), "unit": UNIT,
+           "e2e": {"value": round(replicas.whole_job_rate(S * T, world, e2e_s), 1), "unit": UNIT,
                    "h2d_bytes_per_step": (S + T) * 4, "d2h_bytes_per_step": S * T * 4,
                    "ms_per_step": round(e2e_s * 1e3, 3), "matches_device_run": e2e_ok},
            "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
