@@ -261,6 +261,7 @@ static bf_tune to_c(const Tune& t) {
   o.overlap_levels = t.pdl;
   o.isochrone_16bit = t.iso_half;
   o.overlap_upward = t.overlap_up;
+  o.mapped_output = t.mapped_out;
   return o;
 }
 
@@ -285,6 +286,7 @@ bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
   h->g.tune.pdl = t->overlap_levels ? 1 : 0;
   h->g.tune.iso_half = t->isochrone_16bit ? 1 : 0;
   h->g.tune.overlap_up = t->overlap_upward ? 1 : 0;
+  h->g.tune.mapped_out = t->mapped_output ? 1 : 0;
   return BF_OK;
 }
 
@@ -394,8 +396,21 @@ bf_status bf_matrix(bf_graph* h, const uint32_t* src, uint64_t S, const uint32_t
   if (!S || !T) return BF_OK;
   if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
   cudaStream_t s = g->stream;
+  // A page-locked output buffer is written by the extraction kernel directly
+  // (over the CPU-GPU link), which saves the device copy and the separate
+  // device-to-host transfer; any other buffer gets the copy.
+  uint32_t* d_direct = nullptr;
+  {
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, out) == cudaSuccess) {
+      if (pa.type == cudaMemoryTypeHost && pa.devicePointer && g->tune.mapped_out)
+        d_direct = static_cast<uint32_t*>(pa.devicePointer);
+    } else {
+      cudaGetLastError();
+    }
+  }
   // graph-owned I/O buffer: [sources | targets | matrix], grown on demand
-  const size_t need = (S + T + S * T) * 4;
+  const size_t need = (S + T + (d_direct ? 0 : S * T)) * 4;
   if (need > g->io_bytes) {
     if (g->d_io) {
       cudaFree(g->d_io);
@@ -413,11 +428,11 @@ bf_status bf_matrix(bf_graph* h, const uint32_t* src, uint64_t S, const uint32_t
   }
   uint32_t* d_src = g->d_io;
   uint32_t* d_tgt = d_src + S;
-  uint32_t* d_out = d_tgt + T;
+  uint32_t* d_out = d_direct ? d_direct : d_tgt + T;
   BF_CUDA(cudaMemcpyAsync(d_src, src, S * 4, cudaMemcpyHostToDevice, s));
   BF_CUDA(cudaMemcpyAsync(d_tgt, tgt, T * 4, cudaMemcpyHostToDevice, s));
   if ((rc = run_matrix(g, d_src, S, d_tgt, T, threshold, d_out, s, st))) return rc;
-  BF_CUDA(cudaMemcpyAsync(out, d_out, S * T * 4, cudaMemcpyDeviceToHost, s));
+  if (!d_direct) BF_CUDA(cudaMemcpyAsync(out, d_out, S * T * 4, cudaMemcpyDeviceToHost, s));
   BF_CUDA(cudaStreamSynchronize(s));
   if (st) {
     st->n_sources = S;

@@ -128,6 +128,7 @@ struct Tune {
   uint32_t pdl = 1;          // level launches as programmatic dependents
   uint32_t iso_half = 1;     // 16-bit isochrone lanes when all thresholds fit
   uint32_t overlap_up = 1;   // upward pass on a side stream during the slab reset
+  uint32_t mapped_out = 1;   // bf_matrix writes a page-locked output buffer directly
 };
 
 struct Graph {

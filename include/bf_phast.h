@@ -174,6 +174,8 @@ typedef struct bf_tune {
                                   threshold (exact, half the bytes)             */
   uint32_t overlap_upward;     /* 1: matrix waves run the upward pass on a side
                                   stream while the slab is reset               */
+  uint32_t mapped_output;      /* 1: bf_matrix into page-locked host memory is
+                                  written by the extraction kernel directly     */
 } bf_tune;
 
 /* Time candidate tunables on a sample matrix (device buffers: d_sources,

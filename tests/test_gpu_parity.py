@@ -178,3 +178,20 @@ def test_autotune_picks_a_valid_choice(built, grid100):
     assert best["threads_per_block"] in (64, 128, 256)
     gold = np.load(GOLDEN / "grid100_matrix.npz")
     assert np.array_equal(g.matrix(gold["sources"], gold["targets"]), gold["matrix"])
+
+
+@pytest.mark.parametrize("mapped", [1, 0])
+def test_page_locked_output(built, grid100, mapped):
+    # a page-locked output buffer is written by the extraction kernel directly
+    import torch
+    _, cch = grid100
+    gold = np.load(GOLDEN / "grid100_matrix.npz")
+    g = _graph(cch)
+    g.set_tune(mapped_output=mapped)
+    S, T = len(gold["sources"]), len(gold["targets"])
+    out = torch.full((S * T,), -1, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    out = out.reshape(S, T)
+    for _ in range(2):
+        m = g.matrix(gold["sources"], gold["targets"], out=out)
+        assert m is out or np.shares_memory(m, out)
+        assert np.array_equal(out, gold["matrix"])
