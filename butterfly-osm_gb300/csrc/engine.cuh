@@ -80,11 +80,16 @@ struct Sched {
   cudaStream_t g_stream = nullptr;
   const uint32_t* g_seeded = nullptr;
   bool g_pdl = false;
+  const uint32_t* g_hub = nullptr;
   // captured single-lane bounded sweep (full schedule), with its geometry
   cudaGraphExec_t one_exec = nullptr;
   const void* one_slab = nullptr;
   const void* one_state = nullptr;
   bool one_pdl = false;
+  std::vector<uint32_t> hub_order;  // rows by descending gather count (most-used first)
+  uint32_t* d_hub = nullptr;     // [rows / 32] hub rows (kept in L2 by cache hints)
+  size_t cap_hub = 0;
+  uint32_t hub_rows = 0;         // rows set in d_hub
   std::vector<uint32_t> ranks;   // ranks whose d_cidx entry is set (reset on rebuild)
   bool cidx_ready = false;       // d_cidx holds NONE outside `ranks`
 };
@@ -128,6 +133,7 @@ struct Tune {
   uint32_t pdl = 1;          // level launches as programmatic dependents
   uint32_t iso_half = 1;     // 16-bit isochrone lanes when all thresholds fit
   uint32_t overlap_up = 1;   // upward pass on a side stream during the slab reset
+  uint32_t hub_mb = 48;      // L2 megabytes the most-gathered rows may keep (0 = off)
   uint32_t mapped_out = 1;   // bf_matrix writes a page-locked output buffer directly
 };
 

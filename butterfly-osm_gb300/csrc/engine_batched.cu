@@ -222,6 +222,21 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   });
   sc.lvl_item.assign(g->n_levels + 1, 0);
   for (uint32_t l = 0; l <= g->n_levels; ++l) sc.lvl_item[l] = (uint32_t)ioff[row_lvl[l]];
+  // rows by gather count, most-used first (up to 65536 of them): the sweep
+  // keeps the head of this list in L2
+  {
+    std::vector<uint32_t> uses(n_r, 0);
+    for (const uint2& e : erec) ++uses[e.x];
+    std::vector<uint32_t> ord(n_r);
+    for (uint32_t i = 0; i < n_r; ++i) ord[i] = i;
+    const uint32_t keep = std::min<uint32_t>(n_r, 65536);
+    std::partial_sort(ord.begin(), ord.begin() + keep, ord.end(), [&](uint32_t a, uint32_t b) {
+      return uses[a] != uses[b] ? uses[a] > uses[b] : a < b;
+    });
+    ord.resize(keep);
+    sc.hub_order.swap(ord);
+    sc.hub_rows = NONE;  // bitmap to be (re)built for this schedule
+  }
   // items of a level, heaviest first, so the level's last blocks are short
   parallel_chunks(g->n_levels, 16, [&](uint64_t l0, uint64_t l1) {
     for (uint64_t l = l0; l < l1; ++l)
@@ -309,9 +324,36 @@ __device__ __forceinline__ void atomic_min_lanes(uint32_t* row, uint32_t wbase, 
 
 // One level of the restricted sweep. blockIdx.x = work item, a thread owns
 // 4 consecutive lanes starting at lane; rows are Kp lanes wide (Kp % 4 == 0).
+__device__ __forceinline__ uint64_t l2_policy_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint4 ld_hint(const uint32_t* a, uint64_t pol) {
+  uint4 v;
+  asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_hint(uint32_t* a, uint4 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(a), "r"(v.x),
+               "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ bool is_hub(const uint32_t* hub, uint32_t r) {
+  return hub && ((hub[r >> 5] >> (r & 31)) & 1u);
+}
+
 __global__ void __launch_bounds__(256)
     k_sweep_items(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
-                  uint32_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ seeded) {
+                  uint32_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ seeded,
+                  const uint32_t* __restrict__ hub) {
   // launched as a programmatic dependent of the previous level: let the next
   // level's blocks get scheduled, read the static schedule, then wait for the
   // previous level's rows (no-ops for a plain launch)
@@ -321,14 +363,17 @@ __global__ void __launch_bounds__(256)
   const uint32_t wbase = lane - 4 * (threadIdx.x & 31);
   if (wbase >= Kp) return;  // the whole warp is past the last lane
   const bool live = lane < Kp;
+  // rows gathered most often (hub rows) stay in L2: their loads and stores
+  // carry an evict-last policy, every other row evict-first
+  const uint64_t pl = l2_policy_last(), pf = l2_policy_first();
   asm volatile("griddepcontrol.wait;" ::: "memory");
   uint4 acc = make_uint4(INF, INF, INF, INF);
   if (live) {
     uint32_t e = it.y;
     for (; e + 2 <= it.z; e += 2) {
       const uint2 r0 = erec[e], r1 = erec[e + 1];
-      const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r0.x * Kp + lane);
-      const uint4 b = *reinterpret_cast<const uint4*>(slab + (size_t)r1.x * Kp + lane);
+      const uint4 a = ld_hint(slab + (size_t)r0.x * Kp + lane, is_hub(hub, r0.x) ? pl : pf);
+      const uint4 b = ld_hint(slab + (size_t)r1.x * Kp + lane, is_hub(hub, r1.x) ? pl : pf);
       acc.x = min(acc.x, min(sat_add(a.x, r0.y), sat_add(b.x, r1.y)));
       acc.y = min(acc.y, min(sat_add(a.y, r0.y), sat_add(b.y, r1.y)));
       acc.z = min(acc.z, min(sat_add(a.z, r0.y), sat_add(b.z, r1.y)));
@@ -336,7 +381,7 @@ __global__ void __launch_bounds__(256)
     }
     if (e < it.z) {
       const uint2 r0 = erec[e];
-      const uint4 a = *reinterpret_cast<const uint4*>(slab + (size_t)r0.x * Kp + lane);
+      const uint4 a = ld_hint(slab + (size_t)r0.x * Kp + lane, is_hub(hub, r0.x) ? pl : pf);
       acc.x = min(acc.x, sat_add(a.x, r0.y));
       acc.y = min(acc.y, sat_add(a.y, r0.y));
       acc.z = min(acc.z, sat_add(a.z, r0.y));
@@ -348,15 +393,15 @@ __global__ void __launch_bounds__(256)
     __shared__ __align__(16) uint32_t sbuf[256 * 4];
     atomic_min_lanes(row, wbase, acc, Kp, sbuf + (threadIdx.x & ~31u) * 4);
   } else if (live) {
+    const uint64_t pw = is_hub(hub, it.x) ? pl : pf;
     // rows that got no seed this wave hold stale data: their value is the pull
-    uint4 c = ((seeded[it.x >> 5] >> (it.x & 31)) & 1u)
-                  ? *reinterpret_cast<const uint4*>(row + lane)
-                  : make_uint4(INF, INF, INF, INF);
+    uint4 c = ((seeded[it.x >> 5] >> (it.x & 31)) & 1u) ? ld_hint(row + lane, pf)
+                                                        : make_uint4(INF, INF, INF, INF);
     c.x = min(c.x, acc.x);
     c.y = min(c.y, acc.y);
     c.z = min(c.z, acc.z);
     c.w = min(c.w, acc.w);
-    *reinterpret_cast<uint4*>(row + lane) = c;
+    st_hint(row + lane, c, pw);
   }
 }
 
@@ -521,7 +566,7 @@ uint64_t ctx_budget(Graph* g, Ctx& c) {
 }
 
 static void free_sched(Sched& sc) {
-  void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_elen, sc.d_trow, sc.d_split};
+  void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_elen, sc.d_trow, sc.d_split, sc.d_hub};
   for (void* q : p)
     if (q) cudaFree(q);
   if (sc.gexec) cudaGraphExecDestroy(sc.gexec);
@@ -566,13 +611,27 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
                        unsigned tpb, cudaStream_t st, uint64_t* launches,
                        const uint32_t* seeded) {
   const bool pdl = g->tune.pdl != 0;
+  // hub rows: as many of the most-gathered rows as fit the L2 share
+  uint32_t H = 0;
+  if (g->tune.hub_mb && Kp)
+    H = (uint32_t)std::min<uint64_t>(sc.hub_order.size(),
+                                     ((uint64_t)g->tune.hub_mb << 20) / ((uint64_t)Kp * 4));
+  if (H && H != sc.hub_rows) {
+    std::vector<uint32_t> bits((std::max<uint32_t>(sc.n_r, 1) + 31) / 32, 0);
+    for (uint32_t i = 0; i < H; ++i) bits[sc.hub_order[i] >> 5] |= 1u << (sc.hub_order[i] & 31);
+    bf_status hs;
+    if ((hs = ensure(&sc.d_hub, sc.cap_hub, bits.size(), g))) return hs;
+    BF_CUDA(cudaMemcpyAsync(sc.d_hub, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice, st));
+    sc.hub_rows = H;
+  }
+  const uint32_t* hub = H ? sc.d_hub : nullptr;
   auto issue = [&](cudaStream_t s, uint64_t* count) -> cudaError_t {
     for (uint32_t l = 0; l < g->n_levels; ++l) {
       const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
       if (i1 == i0) continue;
       cudaError_t e = launch_level(k_sweep_items, dim3(i1 - i0, lane_blocks), tpb, pdl, s,
                                    (const uint4*)sc.d_item, i0, (const uint2*)sc.d_erec, slab, Kp,
-                                   seeded);
+                                   seeded, hub);
       if (e != cudaSuccess) return e;
       ++*count;
     }
@@ -580,7 +639,7 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
   };
   const bool geom = sc.g_kp == Kp && sc.g_lb == lane_blocks && sc.g_tpb == tpb &&
                     sc.g_slab == slab && sc.g_stream == st && sc.g_seeded == seeded &&
-                    sc.g_pdl == pdl;
+                    sc.g_pdl == pdl && sc.g_hub == hub;
   if (sc.gexec && !geom) {
     cudaGraphExecDestroy(sc.gexec);
     sc.gexec = nullptr;
@@ -609,6 +668,7 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
       sc.g_stream = st;
       sc.g_seeded = seeded;
       sc.g_pdl = pdl;
+      sc.g_hub = hub;
     }
   }
   if (sc.gexec && g->tune.graphs) {

@@ -176,6 +176,8 @@ typedef struct bf_tune {
                                   stream while the slab is reset               */
   uint32_t mapped_output;      /* 1: bf_matrix into page-locked host memory is
                                   written by the extraction kernel directly     */
+  uint32_t hub_l2_mb;          /* L2 megabytes kept for the most-gathered rows
+                                  (evict-last cache hints; 0 = no hints)         */
 } bf_tune;
 
 /* Time candidate tunables on a sample matrix (device buffers: d_sources,
