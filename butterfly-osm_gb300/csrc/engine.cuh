@@ -48,6 +48,33 @@ __device__ __forceinline__ uint32_t walk_path(uint32_t s, uint32_t D,
   return i == D ? D : 0;
 }
 
+// L2 eviction-priority policies and cache-hinted 16-byte global loads/stores.
+__device__ __forceinline__ uint64_t l2_policy_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint4 ld_hint(const uint32_t* a, uint64_t pol) {
+  uint4 v;
+  asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_hint(uint32_t* a, uint4 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(a), "r"(v.x),
+               "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ bool is_hub(const uint32_t* hub, uint32_t r) {
+  return hub && ((hub[r >> 5] >> (r & 31)) & 1u);
+}
+
 // Lanes per batch of the plain engine (one warp lane per source).
 constexpr uint32_t PLAIN_K = 32;
 // Ancestor-path entries a warp keeps in shared memory during the upward pass.
@@ -257,6 +284,7 @@ bf_status sweep_levels_gated(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, u
                              cudaStream_t st, uint64_t* launches,
                              const uint32_t* seeded = nullptr);
 bf_status ensure_slab(Graph* g, Ctx& c, size_t bytes);
+bf_status hub_rows(Graph* g, Sched& sc, uint64_t row_bytes, cudaStream_t st, const uint32_t** hub);
 uint64_t ctx_budget(Graph* g, Ctx& c);
 void free_ctx(Ctx& c);
 bf_status init_ctx(Ctx& c);

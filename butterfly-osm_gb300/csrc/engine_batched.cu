@@ -324,32 +324,6 @@ __device__ __forceinline__ void atomic_min_lanes(uint32_t* row, uint32_t wbase, 
 
 // One level of the restricted sweep. blockIdx.x = work item, a thread owns
 // 4 consecutive lanes starting at lane; rows are Kp lanes wide (Kp % 4 == 0).
-__device__ __forceinline__ uint64_t l2_policy_last() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t l2_policy_first() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint4 ld_hint(const uint32_t* a, uint64_t pol) {
-  uint4 v;
-  asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
-               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-               : "l"(a), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ void st_hint(uint32_t* a, uint4 v, uint64_t pol) {
-  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(a), "r"(v.x),
-               "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol)
-               : "memory");
-}
-__device__ __forceinline__ bool is_hub(const uint32_t* hub, uint32_t r) {
-  return hub && ((hub[r >> 5] >> (r & 31)) & 1u);
-}
-
 __global__ void __launch_bounds__(256)
     k_sweep_items(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
                   uint32_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ seeded,
@@ -604,6 +578,27 @@ bf_status batched_prepare(Graph* g, uint32_t) {
   return BF_OK;
 }
 
+// Hub rows of a schedule for rows of row_bytes: as many of the most-gathered
+// rows as fit the tune's L2 share, as a device bitmap (*hub = null when off).
+bf_status hub_rows(Graph* g, Sched& sc, uint64_t row_bytes, cudaStream_t st, const uint32_t** hub) {
+  *hub = nullptr;
+  uint32_t H = 0;
+  if (g->tune.hub_mb && row_bytes)
+    H = (uint32_t)std::min<uint64_t>(sc.hub_order.size(),
+                                     ((uint64_t)g->tune.hub_mb << 20) / row_bytes);
+  if (!H) return BF_OK;
+  if (H != sc.hub_rows) {
+    std::vector<uint32_t> bits((std::max<uint32_t>(sc.n_r, 1) + 31) / 32, 0);
+    for (uint32_t i = 0; i < H; ++i) bits[sc.hub_order[i] >> 5] |= 1u << (sc.hub_order[i] & 31);
+    bf_status s;
+    if ((s = ensure(&sc.d_hub, sc.cap_hub, bits.size(), g))) return s;
+    BF_CUDA(cudaMemcpyAsync(sc.d_hub, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice, st));
+    sc.hub_rows = H;
+  }
+  *hub = sc.d_hub;
+  return BF_OK;
+}
+
 // Launch the restricted sweep's level schedule. From the second call on the
 // same schedule and slab geometry the launches are replayed from a captured
 // CUDA graph instead of being issued one by one.
@@ -611,20 +606,9 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
                        unsigned tpb, cudaStream_t st, uint64_t* launches,
                        const uint32_t* seeded) {
   const bool pdl = g->tune.pdl != 0;
-  // hub rows: as many of the most-gathered rows as fit the L2 share
-  uint32_t H = 0;
-  if (g->tune.hub_mb && Kp)
-    H = (uint32_t)std::min<uint64_t>(sc.hub_order.size(),
-                                     ((uint64_t)g->tune.hub_mb << 20) / ((uint64_t)Kp * 4));
-  if (H && H != sc.hub_rows) {
-    std::vector<uint32_t> bits((std::max<uint32_t>(sc.n_r, 1) + 31) / 32, 0);
-    for (uint32_t i = 0; i < H; ++i) bits[sc.hub_order[i] >> 5] |= 1u << (sc.hub_order[i] & 31);
-    bf_status hs;
-    if ((hs = ensure(&sc.d_hub, sc.cap_hub, bits.size(), g))) return hs;
-    BF_CUDA(cudaMemcpyAsync(sc.d_hub, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice, st));
-    sc.hub_rows = H;
-  }
-  const uint32_t* hub = H ? sc.d_hub : nullptr;
+  const uint32_t* hub = nullptr;
+  bf_status hs;
+  if ((hs = hub_rows(g, sc, (uint64_t)Kp * 4, st, &hub))) return hs;
   auto issue = [&](cudaStream_t s, uint64_t* count) -> cudaError_t {
     for (uint32_t l = 0; l < g->n_levels; ++l) {
       const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
