@@ -1,0 +1,73 @@
+"""Deep elimination trees: a chain CCH whose ancestor path (depth n - 1) is
+longer than the upward pass keeps in shared memory, so the upward pass runs
+with per-warp global scratch. Results against the CPU oracle (bit-exact);
+calls that need the shared-memory pass report BF_ERR_UNSUPPORTED and leave
+the graph usable."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+INF = 0xFFFFFFFF
+
+
+def _chain(n):
+    """Ranks 0..n-1 in a line: UP edge i -> i+1, DOWN edge i+1 -> i."""
+    up_off = np.minimum(np.arange(n + 1), n - 1).astype(np.uint64)
+    up_tgt = np.arange(1, n, dtype=np.uint32)
+    up_w = (1 + np.arange(n - 1) % 7).astype(np.uint32)
+    down_off = np.concatenate([[0], np.arange(n)]).astype(np.uint64)
+    down_tgt = np.arange(0, n - 1, dtype=np.uint32)
+    down_w = (2 + np.arange(n - 1) % 5).astype(np.uint32)
+    return dict(n=n, up_off=up_off, up_tgt=up_tgt, up_w=up_w, down_off=down_off,
+                down_tgt=down_tgt, down_w=down_w)
+
+
+N = 7000  # ancestor path of rank 0: 7000 entries, past the shared-memory capacity
+
+
+def test_deep_chain_matrix_both_engines(built):
+    import bfphast
+    cch = _chain(N)
+    c = orc.Cch.from_dict(cch)
+    g = bfphast.Graph.from_cch(cch)
+    assert g.info()["max_depth"] == N - 1
+    src = np.array([0, 1, 17, 3333, N - 2, N - 1, 0], dtype=np.uint32)
+    tgt = np.array([N - 1, 0, 5, 4000, 6999, 12], dtype=np.uint32)
+    want, _ = c.matrix(src, tgt)
+    for eng in (bfphast.ENGINE_BATCHED, bfphast.ENGINE_PLAIN):
+        g.set_engine(eng)
+        assert np.array_equal(g.matrix(src, tgt), want)
+        assert np.array_equal(g.matrix(src, tgt, threshold=5000),
+                              np.where(want <= 5000, want, INF))
+    assert np.array_equal(g.phast_query(0), c.phast_query(0))
+
+
+def test_deep_chain_two_channel_global_path(built):
+    import bfphast
+    cch = _chain(5000)  # 1-channel path fits shared memory, the 2-channel one does not
+    c = orc.Cch.from_dict(cch)
+    up_l = (cch["up_w"] * 3).astype(np.uint32)
+    dn_l = (cch["down_w"] * 5).astype(np.uint32)
+    g = bfphast.Graph.from_cch(cch, up_len=up_l, down_len=dn_l)
+    for seeds, thr in (([(0, 0, 0)], 4000), ([(2500, 3, 7), (10, 0, 1)], INF)):
+        got = g.phast_bounded_seeded_2ch(seeds, thr)
+        want = c.bounded_seeded_2ch(seeds, thr, up_l, dn_l)
+        for a, b in zip(got, want):
+            assert np.array_equal(a, b)
+
+
+def test_deep_chain_threshold_calls_unsupported(built):
+    import bfphast
+    cch = _chain(N)
+    g = bfphast.Graph.from_cch(cch)
+    with pytest.raises(bfphast.BfError) as e:
+        g.isochrone_bitsets([0, 10], [100, 200])
+    assert e.value.status == bfphast.BF_ERR_UNSUPPORTED
+    with pytest.raises(bfphast.BfError) as e:
+        g.phast_bounded_seeded([(0, 0)], 100)
+    assert e.value.status == bfphast.BF_ERR_UNSUPPORTED
+    # the graph stays usable
+    c = orc.Cch.from_dict(cch)
+    assert np.array_equal(g.phast_query(N - 1), c.phast_query(N - 1))
