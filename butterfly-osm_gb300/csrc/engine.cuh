@@ -201,8 +201,6 @@ struct Graph {
   uint32_t* d_seed = nullptr;     // [n][32], all INF between calls
   uint32_t* d_flag = nullptr;     // [ceil(n/32)] seeded-row bits, all 0 between calls
   uint32_t* d_err = nullptr;      // device error word
-  uint32_t* d_gpath = nullptr;    // global fallback for deep ancestor paths
-  uint32_t gpath_stride = 0;      // entries per warp in d_gpath (2 * (max_depth + 1))
 
   // host copies of the pull CSR (target restriction is computed on the host)
   std::vector<uint64_t> h_in_off;  // [n+1] by slab position

@@ -29,76 +29,18 @@ __device__ __forceinline__ uint32_t pd_load(const uint32_t* p) {
 
 }  // namespace
 
-// Upward pass for one batch. Warp w handles source src[w] (w < k) and writes
-// its settled pairs into seed[pos * K + lane_base + w] (+ the seeded bit).
-template <bool GLOBAL_PATH>
-__global__ void __launch_bounds__(UPWARD_WARPS * 32)
-    k_upward(const uint32_t* __restrict__ src, uint32_t k, uint32_t threshold,
-             const uint32_t* __restrict__ parent, const uint32_t* __restrict__ run_end,
-             const uint32_t* __restrict__ depth, const uint64_t* __restrict__ up_off,
-             const uint2* __restrict__ up_rec, const uint32_t* __restrict__ pos_of, uint32_t n,
-             uint32_t* __restrict__ seed, uint32_t seed_stride, uint32_t* __restrict__ flag,
-             uint32_t* __restrict__ gpath, uint32_t gpath_stride, uint32_t* __restrict__ err) {
-  extern __shared__ uint32_t smem[];
-  const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t w = blockIdx.x * UPWARD_WARPS + wib;
-  if (w >= k) return;
-  const uint32_t s = src[w];
-  if (s >= n) {
-    if (lane == 0) atomicOr(err, DEVERR_PATH);
-    return;
-  }
-  const uint32_t D = depth[s] + 1;
-  uint32_t *pd, *pn;
-  if (GLOBAL_PATH) {
-    pd = gpath + (size_t)w * gpath_stride;
-    pn = pd + gpath_stride / 2;
-  } else {
-    pd = smem + wib * 2 * UPWARD_SMEM_PATH;
-    pn = pd + UPWARD_SMEM_PATH;
-  }
-  if (walk_path(s, D, parent, run_end, pn, lane) != D) {
-    if (lane == 0) atomicOr(err, DEVERR_PATH);
-    return;
-  }
-  for (uint32_t l = lane; l < D; l += 32) pd[l] = (l == 0) ? 0u : INF;
-  if (GLOBAL_PATH) __threadfence_block();
-  __syncwarp();
-  for (uint32_t i = 0; i < D; ++i) {
-    uint32_t d = pd_load<GLOBAL_PATH>(&pd[i]);
-    if (d == INF || d > threshold) continue;
-    uint32_t x = GLOBAL_PATH ? __ldcg(&pn[i]) : pn[i];
-    uint64_t e1 = up_off[x + 1];
-    for (uint64_t e = up_off[x] + lane; e < e1; e += 32) {
-      uint2 r = up_rec[e];
-      uint32_t j = i + r.x;
-      if (j >= D) {
-        atomicOr(err, DEVERR_EDGE);
-        continue;
-      }
-      atomicMin(&pd[j], sat_add(d, r.y));
-    }
-    __syncwarp();
-  }
-  if (GLOBAL_PATH) __threadfence_block();
-  __syncwarp();
-  for (uint32_t l = lane; l < D; l += 32) {
-    uint32_t d = pd_load<GLOBAL_PATH>(&pd[l]);
-    if (d == INF || d > threshold) continue;
-    uint32_t x = GLOBAL_PATH ? __ldcg(&pn[l]) : pn[l];
-    uint32_t p = pos_of[x];
-    if (p == NONE) continue;  // outside the target-restricted rows
-    seed[(size_t)p * seed_stride + w] = d;
-    if (flag) atomicOr(&flag[p >> 5], 1u << (p & 31));
-  }
-}
-
-// Upward pass, shared-memory path variant. Each warp keeps its ancestor path
-// (nodes and distances) in dcap-entry shared arrays. The UP-edge ranges of 32
+// Upward pass: warp w walks source (or seed unit) w's ancestor path in
+// increasing rank order (replaces the per-lane BinaryHeap Dijkstra of
+// batched_phast.rs:156-189; ranks are a topological order of the UP DAG, so a
+// node's distance is final once every lower path node has pushed). Each warp
+// keeps its path (nodes and distances) in dcap-entry arrays: shared memory
+// (GLOBAL = false), or for elimination trees too deep for it a per-warp slot
+// of global scratch (warps w0 .. w0 + launch size). The UP-edge ranges of 32
 // path nodes are fetched in one parallel load and broadcast by shuffle, and
 // the first edge record of the next path node is loaded while the current one
-// is relaxed, so a path step costs about one shared-memory round trip instead
-// of two dependent L2 round trips.
+// is relaxed, so a path step costs about one memory round trip instead of two
+// dependent ones.
+template <bool GLOBAL>
 __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
     k_upward_fast(const uint32_t* __restrict__ src, uint32_t k, uint32_t threshold,
                   const uint32_t* __restrict__ parent, const uint32_t* __restrict__ run_end,
@@ -107,10 +49,12 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
                   uint32_t n, uint32_t* __restrict__ seed, uint32_t seed_stride,
                   uint32_t* __restrict__ flag, uint32_t dcap, uint32_t* __restrict__ err,
                   const uint32_t* __restrict__ lane_thr, const uint32_t* __restrict__ unit_cost,
-                  const uint32_t* __restrict__ unit_lane, uint32_t mode) {
+                  const uint32_t* __restrict__ unit_lane, uint32_t mode, uint32_t w0,
+                  uint32_t* __restrict__ gscratch) {
   extern __shared__ uint32_t smem[];
   const uint32_t wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t w = blockIdx.x * UPWARD_WARPS + wib;
+  const uint32_t slot = blockIdx.x * UPWARD_WARPS + wib;
+  const uint32_t w = w0 + slot;
   if (w >= k) return;
   const uint32_t s = src[w];
   if (s >= n) {
@@ -118,8 +62,9 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
     return;
   }
   const uint32_t D = depth[s] + 1;
-  uint32_t* pd = smem + wib * 2 * dcap;
+  uint32_t* pd = GLOBAL ? gscratch + (size_t)slot * 2 * dcap : smem + wib * 2 * dcap;
   uint32_t* pn = pd + dcap;
+#define PN(x) (GLOBAL ? __ldcg(&pn[(x)]) : pn[(x)])
   if (D > dcap || walk_path(s, D, parent, run_end, pn, lane) != D) {
     if (lane == 0) atomicOr(err, DEVERR_PATH);
     return;
@@ -131,11 +76,12 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
   // never lead to a distance within it
   if (lane_thr) threshold = min(threshold, lane_thr[out_lane]);
   for (uint32_t l = lane; l < D; l += 32) pd[l] = (l == 0) ? c0 : INF;
+  if (GLOBAL) __threadfence_block();
   __syncwarp();
   const unsigned FULL = 0xFFFFFFFFu;
   uint64_t cb = 0, ce = 0;  // edge range of path node (chunk base + lane)
   if (lane < D) {
-    const uint32_t x = pn[lane];
+    const uint32_t x = PN(lane);
     cb = up_off[x];
     ce = up_off[x + 1];
   }
@@ -146,7 +92,7 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
     if ((j & 31) == 0 && j < D) {
       cb = ce = 0;
       if (j + lane < D) {
-        const uint32_t x = pn[j + lane];
+        const uint32_t x = PN(j + lane);
         cb = up_off[x];
         ce = up_off[x + 1];
       }
@@ -154,7 +100,7 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
     const uint64_t b_nx = __shfl_sync(FULL, cb, j & 31), e_nx = __shfl_sync(FULL, ce, j & 31);
     const uint2 nrec =
         (j < D && b_nx + lane < e_nx) ? up_rec[b_nx + lane] : make_uint2(0, 0);
-    const uint32_t d = *(const volatile uint32_t*)&pd[i];
+    const uint32_t d = pd_load<GLOBAL>(&pd[i]);
     if (d != INF && d <= threshold) {
       if (b_cur + lane < e_cur) {
         const uint32_t t = i + rec.x;
@@ -179,6 +125,7 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
         }
       }
     }
+    if (GLOBAL) __threadfence_block();
     __syncwarp();
     rec = nrec;
     b_cur = b_nx;
@@ -192,16 +139,16 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
     // different sources at one index mostly name the same top-of-tree row
     uint2* out = reinterpret_cast<uint2*>(seed);
     for (uint32_t l = lane; l < D; l += 32) {
-      const uint32_t d = *(const volatile uint32_t*)&pd[l];
-      const uint32_t p = (d == INF || d > threshold) ? NONE : pos_of[pn[l]];
+      const uint32_t d = pd_load<GLOBAL>(&pd[l]);
+      const uint32_t p = (d == INF || d > threshold) ? NONE : pos_of[PN(l)];
       out[(size_t)(D - 1 - l) * seed_stride + w] = make_uint2(p, d);
     }
     return;
   }
   for (uint32_t l = lane; l < D; l += 32) {
-    const uint32_t d = *(const volatile uint32_t*)&pd[l];
+    const uint32_t d = pd_load<GLOBAL>(&pd[l]);
     if (d == INF || d > threshold) continue;
-    const uint32_t p = pos_of[pn[l]];
+    const uint32_t p = pos_of[PN(l)];
     if (p == NONE) continue;
     if (unit_lane) atomicMin(&seed[(size_t)p * seed_stride + out_lane], d);
     else if (mode == UPWARD_OUT_SLAB16)  // every stored d is within its lane threshold (< 0xFFFF)
@@ -210,6 +157,7 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
     if (flag && d <= lt) atomicOr(&flag[p >> 5], 1u << (p & 31));
   }
 }
+#undef PN
 
 // Compact upward output -> slab: thread (w, i) writes entry i (counted from
 // the root) of source w's ancestor path into lane w of its row. Consecutive
@@ -352,43 +300,43 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
   }
   const uint32_t dcap = ((g->max_depth + 1) + 31) & ~31u;
   const size_t fast_smem = (size_t)UPWARD_WARPS * 2 * dcap * 4;
-  const bool fast = fast_smem <= 200 * 1024;
-  if (fast) {
-    BF_CUDA(cudaFuncSetAttribute(k_upward_fast, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (fast_smem <= 200 * 1024) {
+    BF_CUDA(cudaFuncSetAttribute(k_upward_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)fast_smem));
-    k_upward_fast<<<(unsigned)((k + UPWARD_WARPS - 1) / UPWARD_WARPS), UPWARD_WARPS * 32,
-                    fast_smem, st>>>(d_src, (uint32_t)k, threshold, g->d_parent, g->d_run_end,
-                                     g->d_depth, g->d_up_off, g->d_up_rec, pos_map, g->n, seed,
-                                     stride, flag, dcap, g->d_err, lane_thr, unit_cost,
-                                     unit_lane, mode);
+    k_upward_fast<false><<<(unsigned)((k + UPWARD_WARPS - 1) / UPWARD_WARPS), UPWARD_WARPS * 32,
+                           fast_smem, st>>>(d_src, (uint32_t)k, threshold, g->d_parent,
+                                            g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec,
+                                            pos_map, g->n, seed, stride, flag, dcap, g->d_err,
+                                            lane_thr, unit_cost, unit_lane, mode, 0u, nullptr);
     BF_CUDA(cudaGetLastError());
     return BF_OK;
   }
-  {
-    // deep trees: ancestor paths live in global scratch, PLAIN_K warps per launch
-    if (!g->d_gpath) {
-      g->gpath_stride = 2 * (g->max_depth + 1);
-      size_t bytes = (size_t)PLAIN_K * g->gpath_stride * 4;
-      if (cudaMalloc(&g->d_gpath, bytes) != cudaSuccess) {
-        cudaGetLastError();
-        set_error("cannot allocate the ancestor-path scratch");
-        return BF_ERR_OOM;
-      }
-      g->device_bytes += bytes;
-    }
-    if (lane_thr || unit_cost || unit_lane || mode != UPWARD_OUT_SLAB32) {
-      set_error("seeded units and per-lane thresholds need the shared-memory upward pass "
-                "(elimination tree too deep)");
-      return BF_ERR_UNSUPPORTED;
-    }
-    for (uint64_t s0 = 0; s0 < k; s0 += PLAIN_K) {
-      uint32_t kk = (uint32_t)std::min<uint64_t>(PLAIN_K, k - s0);
-      k_upward<true><<<(kk + UPWARD_WARPS - 1) / UPWARD_WARPS, UPWARD_WARPS * 32, 0, st>>>(
-          d_src + s0, kk, threshold, g->d_parent, g->d_run_end, g->d_depth, g->d_up_off,
-          g->d_up_rec, pos_map, g->n, seed + s0, stride, flag, g->d_gpath, g->gpath_stride,
-          g->d_err);
-    }
+  // deep trees: ancestor paths in a per-call global scratch, a bounded
+  // number of warps per launch
+  const size_t per = (size_t)dcap * 2 * 4;
+  uint64_t chunk = std::max<uint64_t>(UPWARD_WARPS, ((256ull << 20) / per) & ~(uint64_t)(UPWARD_WARPS - 1));
+  chunk = std::min<uint64_t>(chunk, (k + UPWARD_WARPS - 1) & ~(uint64_t)(UPWARD_WARPS - 1));
+  void* scratch = nullptr;
+  if (cudaMalloc(&scratch, chunk * per) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cannot allocate the ancestor-path scratch");
+    return BF_ERR_OOM;
   }
+  cudaError_t le = cudaSuccess;
+  for (uint64_t w0 = 0; w0 < k && le == cudaSuccess; w0 += chunk) {
+    const uint64_t m = std::min<uint64_t>(chunk, k - w0);
+    k_upward_fast<true><<<(unsigned)((m + UPWARD_WARPS - 1) / UPWARD_WARPS), UPWARD_WARPS * 32, 0,
+                          st>>>(d_src, (uint32_t)k, threshold, g->d_parent, g->d_run_end,
+                                g->d_depth, g->d_up_off, g->d_up_rec, pos_map, g->n, seed, stride,
+                                flag, dcap, g->d_err, lane_thr, unit_cost, unit_lane, mode,
+                                (uint32_t)w0, static_cast<uint32_t*>(scratch));
+    le = cudaGetLastError();
+  }
+  // the scratch is freed once the launches that use it have finished
+  const cudaError_t se = cudaStreamSynchronize(st);
+  cudaFree(scratch);
+  if (le != cudaSuccess) return cuda_status(le, "deep-tree upward launch");
+  if (se != cudaSuccess) return cuda_status(se, "cudaStreamSynchronize");
   BF_CUDA(cudaGetLastError());
   return BF_OK;
 }

@@ -329,7 +329,7 @@ void free_graph(Graph* g) {
   cudaSetDevice(g->device);
   void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec, g->d_up_len,
                   g->d_pos_of,  g->d_rank_at, g->d_in_off, g->d_in_rec, g->d_dist,
-                  g->d_seed,    g->d_flag,    g->d_err,    g->d_gpath,  g->d_io,
+                  g->d_seed,    g->d_flag,    g->d_err,    g->d_io,
                   g->d_iso};
   for (void* p : ptrs)
     if (p) cudaFree(p);

@@ -1,8 +1,7 @@
 """Deep elimination trees: a chain CCH whose ancestor path (depth n - 1) is
 longer than the upward pass keeps in shared memory, so the upward pass runs
-with per-warp global scratch. Results against the CPU oracle (bit-exact);
-calls that need the shared-memory pass report BF_ERR_UNSUPPORTED and leave
-the graph usable."""
+with per-warp global scratch. Every entry point against the CPU oracle
+(bit-exact)."""
 import numpy as np
 import pytest
 
@@ -58,16 +57,21 @@ def test_deep_chain_two_channel_global_path(built):
             assert np.array_equal(a, b)
 
 
-def test_deep_chain_threshold_calls_unsupported(built):
+def test_deep_chain_threshold_calls(built):
+    # per-lane thresholds and seeded units also run on the global-scratch pass
     import bfphast
     cch = _chain(N)
-    g = bfphast.Graph.from_cch(cch)
-    with pytest.raises(bfphast.BfError) as e:
-        g.isochrone_bitsets([0, 10], [100, 200])
-    assert e.value.status == bfphast.BF_ERR_UNSUPPORTED
-    with pytest.raises(bfphast.BfError) as e:
-        g.phast_bounded_seeded([(0, 0)], 100)
-    assert e.value.status == bfphast.BF_ERR_UNSUPPORTED
-    # the graph stays usable
     c = orc.Cch.from_dict(cch)
-    assert np.array_equal(g.phast_query(N - 1), c.phast_query(N - 1))
+    g = bfphast.Graph.from_cch(cch)
+    origins = np.array([0, 10, 3500, N - 1], dtype=np.uint32)
+    thr = np.array([100, 2000, 9000, 50], dtype=np.uint32)
+    bits, counts = g.isochrone_bitsets(origins, thr)
+    want_bits, want_counts = c.isochrone_bitsets(origins, thr)
+    assert np.array_equal(bits, want_bits) and np.array_equal(counts, want_counts)
+    for seeds, t in (([(0, 0)], 100), ([(10, 5), (6000, 0)], 4000)):
+        rk, ds = g.phast_bounded_seeded(seeds, t)
+        wr, wd = c.bounded_seeded(seeds, t)
+        assert np.array_equal(rk, wr) and np.array_equal(ds, wd)
+    src = [[(0, 0)], [(100, 3), (200, 1)]]
+    tgt = [[(N - 1, 0)], [(50, 2)], [(3000, 0), (3001, 4)]]
+    assert np.array_equal(g.matrix_seeded(src, tgt), orc.table_phast_lopsided(c, src, tgt, INF)[0])
