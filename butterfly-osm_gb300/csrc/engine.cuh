@@ -135,7 +135,6 @@ struct Ctx {
   uint64_t budget = 0;             // slab bytes this context may use (0 = graph budget)
   std::vector<uint32_t> rowmap;    // host scratch [n], all NONE between builds
   std::vector<uint64_t> markbits;  // host scratch [n bits], all 0 between builds
-  std::vector<std::vector<uint32_t>> buckets;  // host scratch per level, empty between builds
   uint32_t* d_pairs = nullptr;     // device scratch for (rank, row) updates
   size_t cap_pairs = 0;
   uint32_t* d_seeded = nullptr;    // [rows / 32] rows seeded by the current wave

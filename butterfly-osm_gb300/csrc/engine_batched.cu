@@ -63,9 +63,22 @@ bf_status ensure(T** p, size_t& cap, size_t need, Graph* g) {
 
 // Run f(b, e) over [0, n) split into contiguous chunks on host threads
 // (single-threaded below `grain` units per thread).
+// f(t, b, e) for nt equal contiguous slices of [0, n), slice t on thread t.
 template <class F>
-void parallel_chunks(uint64_t n, uint64_t grain, F f) {
-  uint64_t nt = std::min<uint64_t>(std::max(1u, std::thread::hardware_concurrency()), 16);
+void parallel_slices(uint64_t n, uint32_t nt, F f) {
+  const uint64_t step = (n + nt - 1) / nt;
+  std::vector<std::thread> th;
+  for (uint32_t t = 1; t < nt; ++t) {
+    const uint64_t b = std::min(n, t * step), e = std::min(n, (t + 1) * step);
+    th.emplace_back([&f, t, b, e] { f(t, b, e); });
+  }
+  f(0, 0, std::min(n, step));
+  for (auto& x : th) x.join();
+}
+
+template <class F>
+void parallel_chunks(uint64_t n, uint64_t grain, F f, uint64_t max_threads = 16) {
+  uint64_t nt = std::min<uint64_t>(std::max(1u, std::thread::hardware_concurrency()), max_threads);
   nt = std::min<uint64_t>(nt, std::max<uint64_t>(1, n / std::max<uint64_t>(grain, 1)));
   if (nt <= 1) {
     f(0, n);
@@ -128,37 +141,64 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
     R.resize(n);
     for (uint32_t p = 0; p < n; ++p) R[p] = p;
   } else {
-    // walk in-edges from the targets one level at a time, deepest level
-    // first: in-edge sources always sit in lower levels, so a level's bucket
-    // is complete when it is reached. Marks are a bitmap (n bits), small
-    // enough to stay in the host caches.
-    const uint32_t L = g->n_levels;
-    auto level_of = [&](uint32_t p) {
-      return (uint32_t)(std::upper_bound(g->lvl_start.begin(), g->lvl_start.end(), p) -
-                        g->lvl_start.begin() - 1);
-    };
+    // The restricted set is everything that reaches a target along in-edges.
+    // Host threads each walk (depth first) from their share of the targets; a
+    // node is expanded by the thread that claims it (atomic OR on a bitmap of
+    // n bits, small enough to stay in the host caches), so every node is
+    // expanded once. The claimed nodes are then grouped by level.
     if (c.markbits.size() != (n + 63) / 64) c.markbits.assign((n + 63) / 64, 0);
-    if (c.buckets.size() != L) c.buckets.assign(L, {});
     uint64_t* mb = c.markbits.data();
-    auto mark = [&](uint32_t p) {
-      uint64_t& w = mb[p >> 6];
-      const uint64_t b = 1ull << (p & 63);
-      if (w & b) return;
-      w |= b;
-      c.buckets[level_of(p)].push_back(p);
+    auto claim = [mb](uint32_t u) {
+      const uint64_t bit = 1ull << (u & 63);
+      if (__atomic_load_n(&mb[u >> 6], __ATOMIC_RELAXED) & bit) return false;
+      return (__atomic_fetch_or(&mb[u >> 6], bit, __ATOMIC_RELAXED) & bit) == 0;
     };
-    for (uint64_t i = 0; i < T; ++i) mark(g->pos_of[h_tgt[i]]);
-    for (uint32_t l = L; l-- > 0;)
-      for (size_t j = 0; j < c.buckets[l].size(); ++j) {
-        const uint32_t p = c.buckets[l][j];
-        for (uint64_t k = g->h_in_off[p]; k < g->h_in_off[p + 1]; ++k) mark(g->h_in_rec[k].x);
+    const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const uint32_t nth = T >= 512 ? std::min(16u, hw) : 1u;
+    std::vector<std::vector<uint32_t>> found(nth);
+    parallel_slices(T, nth, [&](uint32_t t, uint64_t b, uint64_t e) {
+      std::vector<uint32_t>& out = found[t];
+      std::vector<uint32_t> stack;
+      for (uint64_t i = b; i < e; ++i) {
+        const uint32_t p0 = g->pos_of[h_tgt[i]];
+        if (!claim(p0)) continue;
+        out.push_back(p0);
+        stack.push_back(p0);
+        while (!stack.empty()) {
+          const uint32_t p = stack.back();
+          stack.pop_back();
+          for (uint64_t k = g->h_in_off[p]; k < g->h_in_off[p + 1]; ++k) {
+            const uint32_t u = g->h_in_rec[k].x;
+            if (claim(u)) {
+              out.push_back(u);
+              stack.push_back(u);
+            }
+          }
+        }
       }
+    });
+    // group by level, levels ascending (a counting sort on the level index)
+    const uint32_t L = g->n_levels;
+    std::vector<uint32_t> lvl_cnt(L + 1, 0);
     size_t tot = 0;
-    for (auto& b : c.buckets) tot += b.size();
-    R.reserve(tot);
-    for (auto& b : c.buckets) {
-      R.insert(R.end(), b.begin(), b.end());
-      b.clear();
+    for (auto& f : found) tot += f.size();
+    std::vector<uint32_t> lv(tot);
+    {
+      size_t j = 0;
+      for (auto& f : found)
+        for (uint32_t p : f) {
+          const uint32_t l = (uint32_t)(std::upper_bound(g->lvl_start.begin(), g->lvl_start.end(), p) -
+                                        g->lvl_start.begin() - 1);
+          lv[j++] = l;
+          ++lvl_cnt[l + 1];
+        }
+    }
+    for (uint32_t l = 0; l < L; ++l) lvl_cnt[l + 1] += lvl_cnt[l];
+    R.resize(tot);
+    {
+      size_t j = 0;
+      for (auto& f : found)
+        for (uint32_t p : f) R[lvl_cnt[lv[j++]]++] = p;
     }
     for (uint32_t p : R) mb[p >> 6] = 0;
   }
@@ -222,20 +262,30 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   });
   sc.lvl_item.assign(g->n_levels + 1, 0);
   for (uint32_t l = 0; l <= g->n_levels; ++l) sc.lvl_item[l] = (uint32_t)ioff[row_lvl[l]];
-  // rows by gather count, most-used first (up to 65536 of them): the sweep
-  // keeps the head of this list in L2
-  {
+  // rows by gather count, most-used first (up to 65536 of them): the matrix
+  // sweep keeps the head of this list in L2. A counting sort by count; the
+  // full-graph schedule (isochrones, bounded queries) does not use it.
+  sc.hub_order.clear();
+  sc.hub_rows = NONE;  // bitmap to be (re)built for this schedule
+  if (!all && n_r) {
     std::vector<uint32_t> uses(n_r, 0);
     for (const uint2& e : erec) ++uses[e.x];
-    std::vector<uint32_t> ord(n_r);
-    for (uint32_t i = 0; i < n_r; ++i) ord[i] = i;
+    uint32_t top = 0;
+    for (uint32_t u : uses) top = std::max(top, u);
+    std::vector<uint32_t> at(top + 2, 0);  // rows per count, then start offsets (descending)
+    for (uint32_t u : uses) ++at[u];
     const uint32_t keep = std::min<uint32_t>(n_r, 65536);
-    std::partial_sort(ord.begin(), ord.begin() + keep, ord.end(), [&](uint32_t a, uint32_t b) {
-      return uses[a] != uses[b] ? uses[a] > uses[b] : a < b;
-    });
-    ord.resize(keep);
-    sc.hub_order.swap(ord);
-    sc.hub_rows = NONE;  // bitmap to be (re)built for this schedule
+    uint32_t acc = 0;
+    for (uint32_t u = top + 1; u-- > 0;) {
+      const uint32_t c = at[u];
+      at[u] = acc;
+      acc += c;
+    }
+    sc.hub_order.assign(keep, 0);
+    for (uint32_t i = 0; i < n_r; ++i) {
+      const uint32_t slot = at[uses[i]]++;
+      if (slot < keep) sc.hub_order[slot] = i;
+    }
   }
   // items of a level, heaviest first, so the level's last blocks are short
   parallel_chunks(g->n_levels, 16, [&](uint64_t l0, uint64_t l1) {
