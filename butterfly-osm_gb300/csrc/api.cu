@@ -130,6 +130,7 @@ static bf_status graph_create(const bf_cch_csr* csr, const uint32_t* up_len,
     set_error("cudaGetDeviceProperties failed");
     return BF_ERR_DEVICE;
   }
+  const uint64_t l2_bytes = (uint64_t)prop.l2CacheSize;
   if (prop.major != 10 || prop.minor != 3) {
     set_error(std::string("this library is built for sm_103 (GB300); device is ") + prop.name);
     return BF_ERR_DEVICE;
@@ -141,6 +142,7 @@ static bf_status graph_create(const bf_cch_csr* csr, const uint32_t* up_len,
   }
   Graph* g = &h->g;
   g->device = c.device;
+  g->l2_bytes = l2_bytes;
   g->engine = c.engine == BF_ENGINE_AUTO ? BF_ENGINE_BATCHED : c.engine;
   g->k_lanes = c.k_lanes;
   if (cudaSetDevice(c.device) != cudaSuccess) {

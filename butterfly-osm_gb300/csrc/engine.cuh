@@ -54,6 +54,11 @@ __device__ __forceinline__ uint64_t l2_policy_last() {
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
   return p;
 }
+__device__ __forceinline__ uint64_t l2_policy_normal() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
 __device__ __forceinline__ uint64_t l2_policy_first() {
   uint64_t p;
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
@@ -108,6 +113,7 @@ struct Sched {
   const uint32_t* g_seeded = nullptr;
   bool g_pdl = false;
   const uint32_t* g_hub = nullptr;
+  bool g_hinted = false;
   // captured single-lane bounded sweep (full schedule), with its geometry
   cudaGraphExec_t one_exec = nullptr;
   const void* one_slab = nullptr;
@@ -145,6 +151,8 @@ struct Ctx {
   size_t cap_cseed = 0;
   uint32_t* d_one = nullptr;       // bounded-query state: active bitmap, then the threshold
   size_t cap_one = 0;
+  void* h_stage = nullptr;         // page-locked staging arena for schedule uploads
+  size_t stage_bytes = 0;
 };
 
 // Tunables of the batched sweep (chosen by bf_autotune).
@@ -173,6 +181,7 @@ struct Graph {
   uint32_t k_lanes = 0;
   std::atomic<uint64_t> device_bytes{0};
   uint64_t hbm_budget = 0;
+  uint64_t l2_bytes = 0;          // L2 size of the device (cache-hint decisions)
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
   std::mutex mu;

@@ -233,9 +233,27 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
     set_error("restricted edge set exceeds 2^32 edges");
     return BF_ERR_UNSUPPORTED;
   }
-  std::vector<uint2> erec(eoff[n_r]);
-  std::vector<uint32_t> elen(two ? eoff[n_r] : 0);  // length weight per erec entry
-  std::vector<uint4> items(ioff[n_r]);
+  // items, edge records (and length weights) are filled in place in the
+  // context's page-locked staging arena, so their upload is a plain DMA
+  const size_t n_e = eoff[n_r], n_i = ioff[n_r];
+  {
+    const size_t need = n_i * sizeof(uint4) + n_e * sizeof(uint2) + (two ? n_e * 4 : 0) + 64;
+    if (need > c.stage_bytes) {
+      if (c.h_stage) cudaFreeHost(c.h_stage);
+      c.h_stage = nullptr;
+      c.stage_bytes = 0;
+      if (cudaHostAlloc(&c.h_stage, need, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        for (uint32_t p : R) c.rowmap[p] = NONE;
+        set_error("cannot allocate the page-locked schedule staging buffer");
+        return BF_ERR_OOM;
+      }
+      c.stage_bytes = need;
+    }
+  }
+  uint4* items = static_cast<uint4*>(c.h_stage);
+  uint2* erec = reinterpret_cast<uint2*>(items + n_i);
+  uint32_t* elen = reinterpret_cast<uint32_t*>(erec + n_e);  // length weight per erec entry
   std::vector<uint32_t> split_bits((n_r + 31) / 32 + 1, 0);
   // chunks of whole 32-row groups, so no two threads share a split_bits word
   parallel_chunks((n_r + 31) / 32, 256, [&](uint64_t w0, uint64_t w1) {
@@ -269,7 +287,7 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   sc.hub_rows = NONE;  // bitmap to be (re)built for this schedule
   if (!all && n_r) {
     std::vector<uint32_t> uses(n_r, 0);
-    for (const uint2& e : erec) ++uses[e.x];
+    for (size_t k = 0; k < n_e; ++k) ++uses[erec[k].x];
     uint32_t top = 0;
     for (uint32_t u : uses) top = std::max(top, u);
     std::vector<uint32_t> at(top + 2, 0);  // rows per count, then start offsets (descending)
@@ -290,7 +308,7 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   // items of a level, heaviest first, so the level's last blocks are short
   parallel_chunks(g->n_levels, 16, [&](uint64_t l0, uint64_t l1) {
     for (uint64_t l = l0; l < l1; ++l)
-      std::stable_sort(items.begin() + sc.lvl_item[l], items.begin() + sc.lvl_item[l + 1],
+      std::stable_sort(items + sc.lvl_item[l], items + sc.lvl_item[l + 1],
                        [](const uint4& a, const uint4& b) { return a.z - a.y > b.z - b.y; });
   });
   std::vector<uint32_t> trow(T);
@@ -309,9 +327,9 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   bf_status s;
   size_t cap_c = sc.d_cidx ? n : 0;
   if ((s = ensure(&sc.d_cidx, cap_c, n, g))) return s;
-  if ((s = ensure(&sc.d_item, sc.cap_items, items.size(), g))) return s;
-  if ((s = ensure(&sc.d_erec, sc.cap_edges, erec.size(), g))) return s;
-  if (two && (s = ensure(&sc.d_elen, sc.cap_elen, elen.size(), g))) return s;
+  if ((s = ensure(&sc.d_item, sc.cap_items, n_i, g))) return s;
+  if ((s = ensure(&sc.d_erec, sc.cap_edges, n_e, g))) return s;
+  if (two && (s = ensure(&sc.d_elen, sc.cap_elen, n_e, g))) return s;
   if ((s = ensure(&sc.d_trow, sc.cap_t, T, g))) return s;
   if ((s = ensure(&c.d_pairs, c.cap_pairs, pairs.size() * 2, g))) return s;
   if ((s = ensure(&sc.d_split, sc.cap_split, split_bits.size(), g))) return s;
@@ -332,20 +350,18 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
                                                                       sc.d_cidx);
     BF_CUDA(cudaGetLastError());
   }
-  if (!items.empty())
-    BF_CUDA(cudaMemcpyAsync(sc.d_item, items.data(), items.size() * sizeof(uint4),
-                            cudaMemcpyHostToDevice, st));
-  if (!erec.empty())
-    BF_CUDA(cudaMemcpyAsync(sc.d_erec, erec.data(), erec.size() * sizeof(uint2),
-                            cudaMemcpyHostToDevice, st));
-  if (!elen.empty())
-    BF_CUDA(cudaMemcpyAsync(sc.d_elen, elen.data(), elen.size() * 4, cudaMemcpyHostToDevice, st));
+  if (n_i)
+    BF_CUDA(cudaMemcpyAsync(sc.d_item, items, n_i * sizeof(uint4), cudaMemcpyHostToDevice, st));
+  if (n_e)
+    BF_CUDA(cudaMemcpyAsync(sc.d_erec, erec, n_e * sizeof(uint2), cudaMemcpyHostToDevice, st));
+  if (two && n_e)
+    BF_CUDA(cudaMemcpyAsync(sc.d_elen, elen, n_e * 4, cudaMemcpyHostToDevice, st));
   if (T) BF_CUDA(cudaMemcpyAsync(sc.d_trow, trow.data(), T * 4, cudaMemcpyHostToDevice, st));
   BF_CUDA(cudaStreamSynchronize(st));  // host vectors are freed on return
   sc.ranks.swap(ranks);
   sc.n_r = n_r;
-  sc.n_items = items.size();
-  sc.n_edges = erec.size();
+  sc.n_items = n_i;
+  sc.n_edges = n_e;
   sc.T = T;
   sc.key = key;
   sc.valid = true;
@@ -377,7 +393,7 @@ __device__ __forceinline__ void atomic_min_lanes(uint32_t* row, uint32_t wbase, 
 __global__ void __launch_bounds__(256)
     k_sweep_items(const uint4* __restrict__ item, uint32_t i0, const uint2* __restrict__ erec,
                   uint32_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ seeded,
-                  const uint32_t* __restrict__ hub) {
+                  const uint32_t* __restrict__ hub, uint32_t hinted) {
   // launched as a programmatic dependent of the previous level: let the next
   // level's blocks get scheduled, read the static schedule, then wait for the
   // previous level's rows (no-ops for a plain launch)
@@ -387,9 +403,10 @@ __global__ void __launch_bounds__(256)
   const uint32_t wbase = lane - 4 * (threadIdx.x & 31);
   if (wbase >= Kp) return;  // the whole warp is past the last lane
   const bool live = lane < Kp;
-  // rows gathered most often (hub rows) stay in L2: their loads and stores
-  // carry an evict-last policy, every other row evict-first
-  const uint64_t pl = l2_policy_last(), pf = l2_policy_first();
+  // when the slab is much larger than L2, rows gathered most often (hub
+  // rows) stay in L2: their loads and stores carry an evict-last policy,
+  // every other row evict-first; a slab of L2 scale keeps normal eviction
+  const uint64_t pl = l2_policy_last(), pf = hinted ? l2_policy_first() : l2_policy_normal();
   asm volatile("griddepcontrol.wait;" ::: "memory");
   uint4 acc = make_uint4(INF, INF, INF, INF);
   if (live) {
@@ -607,6 +624,7 @@ void free_ctx(Ctx& c) {
   if (c.d_iso_tmp) cudaFree(c.d_iso_tmp);
   if (c.d_cseed) cudaFree(c.d_cseed);
   if (c.d_one) cudaFree(c.d_one);
+  if (c.h_stage) cudaFreeHost(c.h_stage);
   for (auto& e : c.ev)
     if (e) cudaEventDestroy(e);
   if (c.fork) cudaEventDestroy(c.fork);
@@ -656,16 +674,19 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
                        unsigned tpb, cudaStream_t st, uint64_t* launches,
                        const uint32_t* seeded) {
   const bool pdl = g->tune.pdl != 0;
+  // cache hints only pay when the slab is well beyond L2 (otherwise
+  // evict-first would drop lines that the sweep reads again)
+  const bool hinted = (uint64_t)std::max<uint32_t>(sc.n_r, 1) * Kp * 4 > 4 * g->l2_bytes;
   const uint32_t* hub = nullptr;
   bf_status hs;
-  if ((hs = hub_rows(g, sc, (uint64_t)Kp * 4, st, &hub))) return hs;
+  if (hinted && (hs = hub_rows(g, sc, (uint64_t)Kp * 4, st, &hub))) return hs;
   auto issue = [&](cudaStream_t s, uint64_t* count) -> cudaError_t {
     for (uint32_t l = 0; l < g->n_levels; ++l) {
       const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
       if (i1 == i0) continue;
       cudaError_t e = launch_level(k_sweep_items, dim3(i1 - i0, lane_blocks), tpb, pdl, s,
                                    (const uint4*)sc.d_item, i0, (const uint2*)sc.d_erec, slab, Kp,
-                                   seeded, hub);
+                                   seeded, hub, hinted ? 1u : 0u);
       if (e != cudaSuccess) return e;
       ++*count;
     }
@@ -673,7 +694,7 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
   };
   const bool geom = sc.g_kp == Kp && sc.g_lb == lane_blocks && sc.g_tpb == tpb &&
                     sc.g_slab == slab && sc.g_stream == st && sc.g_seeded == seeded &&
-                    sc.g_pdl == pdl && sc.g_hub == hub;
+                    sc.g_pdl == pdl && sc.g_hub == hub && sc.g_hinted == hinted;
   if (sc.gexec && !geom) {
     cudaGraphExecDestroy(sc.gexec);
     sc.gexec = nullptr;
@@ -703,6 +724,7 @@ bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigne
       sc.g_seeded = seeded;
       sc.g_pdl = pdl;
       sc.g_hub = hub;
+      sc.g_hinted = hinted;
     }
   }
   if (sc.gexec && g->tune.graphs) {
