@@ -338,7 +338,7 @@ def run_serving(g, n, seconds, rate, seed=7):
 
 
 def run_isochrones(g, cch, count, seed=42):
-    """Bulk isochrones (configs[3]): `count` origins uniform over ranks,
+    """Bulk isochrones: `count` origins uniform over ranks,
     thresholds uniform over {300, 600, 1200, 1800, 3600} s; bitsets written
     to HBM in chunks of 20 000 origins; a sample is checked bit for bit
     against the CPU oracle, which is also timed on the host cores."""

@@ -124,7 +124,7 @@ void make_intersections(bfc_graph& g, u32 rows, u32 cols, u32 sp, u32 jit, Rng& 
     }
 }
 
-// configs[0]: 4-neighbour grid; 5% of roads removed, 10% one-way; speed
+// Grid workload (100 x 100 in the tests): 4-neighbour grid; 5% of roads removed, 10% one-way; speed
 // classes 30/50/90 km/h at 80/15/5 %.
 std::vector<Road> roads_grid(u32 rows, u32 cols, Rng& rng) {
   std::vector<Road> roads;
@@ -148,7 +148,7 @@ std::vector<Road> roads_grid(u32 rows, u32 cols, Rng& rng) {
   return kept;
 }
 
-// configs[1]: lattice with arterial lines every 10 rows/cols (70 km/h),
+// Country-scale workload: lattice with arterial lines every 10 rows/cols (70 km/h),
 // motorway lines every 80 (120 km/h), and 9x9 local-street cells. Inside a
 // cell the streets are a random spanning tree plus ~30% of the remaining
 // lattice edges as loops (30-50 km/h); each cell joins the arterial on its
