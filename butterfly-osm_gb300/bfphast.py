@@ -6,6 +6,9 @@ This mirrors the reference engine's call surface for tests and benchmarks:
   Graph.query_batch(src, T)  query_batch / query_batch_bounded  batched_phast.rs:131, :271
   Graph.phast_query(o)       PhastEngine::query           route/src/range/phast.rs:155
   Graph.matrix(src, tgt, T)  compute_matrix_flat          batched_phast.rs:667
+  Cch(topo).customize(...)   customize_cch_time_in_memory route/src/customization.rs:571
+  Cch.relax / relax_lex      triangle_relax[_lex]_parallel customization.rs:1083, :1253
+  Cch.bottom_up(...)         bottom_up_with_external_middles customization.rs:953
 
 The native library is mandatory: importing this module raises if
 lib/libbf_phast.so is missing. There is no CPU fallback.
@@ -113,6 +116,23 @@ class Completion(ctypes.Structure):
                 ("done_s", ctypes.c_double)]
 
 
+class CchTopo(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("up_offsets", _u64p), ("up_targets", _u32p),
+                ("up_is_shortcut", ctypes.c_void_p), ("up_middle", _u32p),
+                ("down_offsets", _u64p), ("down_targets", _u32p),
+                ("down_is_shortcut", ctypes.c_void_p), ("down_middle", _u32p)]
+
+
+class CchStats(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_uint32), ("levels", ctypes.c_uint32),
+                ("up_edges", ctypes.c_uint64), ("down_edges", ctypes.c_uint64),
+                ("triangles", ctypes.c_uint64), ("bottom_up_shortcuts", ctypes.c_uint64),
+                ("apexes", ctypes.c_uint32), ("etree_levels", ctypes.c_uint32),
+                ("plan_ms", ctypes.c_double), ("last_device_ms", ctypes.c_double),
+                ("last_total_ms", ctypes.c_double)]
+
+
 # Every symbol include/bf_phast.h declares, with its ctypes signature.
 _SIGNATURES = {
     "bf_graph_create": (ctypes.c_int, [ctypes.POINTER(CchCsr), ctypes.POINTER(Config),
@@ -169,6 +189,17 @@ _SIGNATURES = {
                                       ctypes.c_uint32, ctypes.c_uint32, _u32p]),
     "bf_server_cancel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "bf_server_destroy": (None, [ctypes.c_void_p]),
+    "bf_cch_create": (ctypes.c_int, [ctypes.POINTER(CchTopo), ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_void_p)]),
+    "bf_cch_destroy": (None, [ctypes.c_void_p]),
+    "bf_cch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CchStats)]),
+    "bf_cch_relax": (ctypes.c_int, [ctypes.c_void_p, _u32p, _u32p, _u32p, _u32p]),
+    "bf_cch_customize": (ctypes.c_int, [ctypes.c_void_p, _u32p, _u32p, _u32p, _u32p, _u32p,
+                                        _u32p]),
+    "bf_cch_relax_lex": (ctypes.c_int, [ctypes.c_void_p, _u32p, _u32p, _u32p, _u32p, _u32p,
+                                        _u32p]),
+    "bf_cch_bottom_up": (ctypes.c_int, [ctypes.c_void_p, _u32p, _u32p, _u32p, _u32p, _u32p,
+                                        _u32p]),
     "bf_last_error": (ctypes.c_char_p, []),
 }
 
@@ -468,3 +499,91 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+class Cch:
+    """A rank-space CCH topology on the GPU for customization (owns a bf_cch).
+
+    Mirrors the reference's CchTopo (formats/cch_topo.rs:250-290): UP edges
+    u -> v (v > u) and DOWN edges u -> v (v < u) as two CSRs with targets
+    ascending per node, optional shortcut flags and contraction middles."""
+
+    def __init__(self, n_nodes, up_off, up_tgt, down_off, down_tgt, up_short=None,
+                 down_short=None, up_mid=None, down_mid=None, device=0):
+        lib = load()
+        self._keep = [np.ascontiguousarray(up_off, dtype=np.uint64), _u32(up_tgt),
+                      np.ascontiguousarray(down_off, dtype=np.uint64), _u32(down_tgt)]
+        self.nu, self.nd = len(self._keep[1]), len(self._keep[3])
+        t = CchTopo(n_nodes=int(n_nodes))
+        t.up_offsets, t.up_targets = _ptr(self._keep[0], _u64p), _ptr(self._keep[1])
+        t.down_offsets, t.down_targets = _ptr(self._keep[2], _u64p), _ptr(self._keep[3])
+        for name, arr, dt in (("up_is_shortcut", up_short, np.uint8),
+                              ("down_is_shortcut", down_short, np.uint8),
+                              ("up_middle", up_mid, np.uint32),
+                              ("down_middle", down_mid, np.uint32)):
+            if arr is not None:
+                a = np.ascontiguousarray(arr, dtype=dt)
+                self._keep.append(a)
+                setattr(t, name, a.ctypes.data if dt == np.uint8 else _ptr(a))
+        h = ctypes.c_void_p()
+        _check(lib.bf_cch_create(ctypes.byref(t), int(device), ctypes.byref(h)))
+        self._h = h
+
+    @classmethod
+    def from_oracle_topo(cls, t, with_short=True, device=0):
+        """From an oracle.CchTopo (same field meaning)."""
+        return cls(t.n, t.up_off, t.up_tgt, t.down_off, t.down_tgt,
+                   t.up_short if with_short else None, t.down_short if with_short else None,
+                   t.up_mid, t.down_mid, device=device)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bf_cch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        st = CchStats()
+        _check(load().bf_cch_info(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in CchStats._fields_}
+
+    def relax(self, up_w, down_w, up_mid, down_mid):
+        """triangle_relax_parallel: returns (up_w, down_w, up_mid, down_mid)."""
+        uw, dw, um, dm = (_u32(x).copy() for x in (up_w, down_w, up_mid, down_mid))
+        _check(load().bf_cch_relax(self._h, _ptr(uw), _ptr(dw), _ptr(um), _ptr(dm)))
+        return uw, dw, um, dm
+
+    def customize(self, orig_up, orig_down):
+        """bottom_up_customize + triangle_relax_parallel: returns
+        (up_w, down_w, up_mid, down_mid)."""
+        ou, od = _u32(orig_up), _u32(orig_down)
+        uw, dw = np.empty(self.nu, np.uint32), np.empty(self.nd, np.uint32)
+        um, dm = np.empty(self.nu, np.uint32), np.empty(self.nd, np.uint32)
+        _check(load().bf_cch_customize(self._h, _ptr(ou), _ptr(od), _ptr(uw), _ptr(dw), _ptr(um),
+                                       _ptr(dm)))
+        return uw, dw, um, dm
+
+    def relax_lex(self, up_t, down_t, up_len, down_len, up_mid, down_mid):
+        """triangle_relax_lex_parallel: returns (up_t, down_t, up_mid, down_mid)."""
+        ut, dt, um, dm = (_u32(x).copy() for x in (up_t, down_t, up_mid, down_mid))
+        ul, dl = _u32(up_len), _u32(down_len)
+        _check(load().bf_cch_relax_lex(self._h, _ptr(ut), _ptr(dt), _ptr(ul), _ptr(dl), _ptr(um),
+                                       _ptr(dm)))
+        return ut, dt, um, dm
+
+    def bottom_up(self, orig_up, orig_down, up_mid=None, down_mid=None):
+        """bottom_up_with_external_middles (the topology's middles when None):
+        returns (up_w, down_w)."""
+        ou, od = _u32(orig_up), _u32(orig_down)
+        um = None if up_mid is None else _u32(up_mid)
+        dm = None if down_mid is None else _u32(down_mid)
+        uw, dw = np.empty(self.nu, np.uint32), np.empty(self.nd, np.uint32)
+        _check(load().bf_cch_bottom_up(self._h, _ptr(ou), _ptr(od),
+                                       None if um is None else _ptr(um),
+                                       None if dm is None else _ptr(dm), _ptr(uw), _ptr(dw)))
+        return uw, dw

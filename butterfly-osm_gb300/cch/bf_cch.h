@@ -98,6 +98,22 @@ typedef struct bfc_cch_view {
   double t_customize_s;
 } bfc_cch_view;
 
+/* The chordal completion behind the flats, in upper-neighbour form: edge e of
+ * rank j joins j and tgt[e] (> j); orig_up[e] / orig_down[e] are the original
+ * arc weights of j -> tgt[e] / tgt[e] -> j (INF: no arc), cust_* the weights
+ * after this library's customization (INF edges are the ones the flats drop). */
+typedef struct bfc_topo_view {
+  uint32_t n_nodes;
+  uint32_t reserved;
+  uint64_t n_edges;
+  const uint64_t* off;          /* [n_nodes + 1]                                     */
+  const uint32_t* tgt;          /* [n_edges]                                         */
+  const uint32_t* orig_up;      /* [n_edges]                                         */
+  const uint32_t* orig_down;    /* [n_edges]                                         */
+  const uint32_t* cust_up;      /* [n_edges]                                         */
+  const uint32_t* cust_down;    /* [n_edges]                                         */
+} bfc_topo_view;
+
 /* Build a synthetic road graph, its EBG and its CCH. n_threads <= 0 uses all
  * hardware threads. Returns 0 on success; on failure *out is NULL and
  * bfc_last_error() describes the problem. */
@@ -112,6 +128,7 @@ int bfc_build_from_arcs(uint32_t n_states, uint64_t n_arcs, const uint32_t* arc_
 void bfc_free(bfc_graph* g);
 void bfc_ebg(const bfc_graph* g, bfc_ebg_view* out);
 void bfc_cch(const bfc_graph* g, bfc_cch_view* out);
+void bfc_topo(const bfc_graph* g, bfc_topo_view* out);
 const char* bfc_last_error(void);
 
 #ifdef __cplusplus

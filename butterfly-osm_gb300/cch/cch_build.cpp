@@ -101,6 +101,11 @@ struct bfc_graph {
   u64 n_chordal = 0;
   std::vector<u64> up_off, dn_off;
   std::vector<u32> up_tgt, up_w, dn_tgt, dn_w;
+  // chordal completion in upper-neighbour form (kept for customization tests)
+  std::vector<u64> topo_off;           // [n + 1]
+  std::vector<u32> topo_tgt;           // upper neighbours of each rank, ascending
+  std::vector<u32> orig_up, orig_dn;   // original arc weights per edge (INF: none)
+  std::vector<u32> cust_up, cust_dn;   // weights after this library's customization
   double t_gen = 0, t_order = 0, t_contract = 0, t_custom = 0;
 };
 
@@ -720,6 +725,8 @@ void build_cch(bfc_graph& g, int n_threads) {
       }
     }
   }
+  g.orig_up = wup;
+  g.orig_dn = wdn;
   // etree heights (children before parents)
   std::vector<u32> height(n, 0);
   u32 max_h = 0;
@@ -761,6 +768,10 @@ void build_cch(bfc_graph& g, int n_threads) {
   }
   double t3 = now_s();
   g.t_custom = t3 - t2;
+  g.topo_off = Uoff;
+  g.topo_tgt = Ut;
+  g.cust_up = wup;
+  g.cust_dn = wdn;
   rowj.clear();
   rowj.shrink_to_fit();
   rowslot.clear();
@@ -924,6 +935,18 @@ void bfc_ebg(const bfc_graph* g, bfc_ebg_view* o) {
   o->state_class = g->scls.data();
   o->ix = g->ix.data();
   o->iy = g->iy.data();
+}
+
+void bfc_topo(const bfc_graph* g, bfc_topo_view* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->n_nodes = g->n;
+  o->n_edges = g->topo_tgt.size();
+  o->off = g->topo_off.data();
+  o->tgt = g->topo_tgt.data();
+  o->orig_up = g->orig_up.data();
+  o->orig_down = g->orig_dn.data();
+  o->cust_up = g->cust_up.data();
+  o->cust_down = g->cust_dn.data();
 }
 
 void bfc_cch(const bfc_graph* g, bfc_cch_view* o) {

@@ -50,6 +50,13 @@ class _Cch(ctypes.Structure):
                 ("t_contract_s", ctypes.c_double), ("t_customize_s", ctypes.c_double)]
 
 
+class _Topo(ctypes.Structure):
+    _fields_ = [("n_nodes", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("n_edges", ctypes.c_uint64), ("off", ctypes.c_void_p), ("tgt", ctypes.c_void_p),
+                ("orig_up", ctypes.c_void_p), ("orig_down", ctypes.c_void_p),
+                ("cust_up", ctypes.c_void_p), ("cust_down", ctypes.c_void_p)]
+
+
 _lib = None
 
 
@@ -66,6 +73,7 @@ def load():
         lib.bfc_free.argtypes = [ctypes.c_void_p]
         lib.bfc_ebg.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Ebg)]
         lib.bfc_cch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Cch)]
+        lib.bfc_topo.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Topo)]
         lib.bfc_last_error.restype = ctypes.c_char_p
         _lib = lib
     return _lib
@@ -78,7 +86,7 @@ def _copy(ptr, count, dtype):
     return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ct)), shape=(count,)).copy()
 
 
-def _extract(lib, h):
+def _extract(lib, h, with_topo=False):
     e, c = _Ebg(), _Cch()
     lib.bfc_ebg(h, ctypes.byref(e))
     lib.bfc_cch(h, ctypes.byref(c))
@@ -104,18 +112,29 @@ def _extract(lib, h):
                state_to_rank=_copy(c.state_to_rank, n, np.uint32),
                times=dict(generate_s=c.t_generate_s, order_s=c.t_order_s,
                           contract_s=c.t_contract_s, customize_s=c.t_customize_s))
+    if with_topo:
+        t = _Topo()
+        lib.bfc_topo(h, ctypes.byref(t))
+        m = t.n_edges
+        cch["topo"] = dict(off=_copy(t.off, n + 1, np.uint64), tgt=_copy(t.tgt, m, np.uint32),
+                           orig_up=_copy(t.orig_up, m, np.uint32),
+                           orig_down=_copy(t.orig_down, m, np.uint32),
+                           cust_up=_copy(t.cust_up, m, np.uint32),
+                           cust_down=_copy(t.cust_down, m, np.uint32))
     return ebg, cch
 
 
-def build_synthetic(kind, rows, cols, seed=42, threads=0):
-    """Build a synthetic road graph and its CCH; returns (ebg, cch) dicts."""
+def build_synthetic(kind, rows, cols, seed=42, threads=0, with_topo=False):
+    """Build a synthetic road graph and its CCH; returns (ebg, cch) dicts.
+    with_topo adds cch["topo"]: the chordal completion in upper-neighbour form
+    with original and customized weights (for customization tests)."""
     lib = load()
     p = _Params(kind, rows, cols, 0, 0, 0, seed)
     h = ctypes.c_void_p()
     if lib.bfc_build_synthetic(ctypes.byref(p), threads, ctypes.byref(h)) != 0:
         raise RuntimeError("bfc_build_synthetic: " + lib.bfc_last_error().decode())
     try:
-        return _extract(lib, h)
+        return _extract(lib, h, with_topo)
     finally:
         lib.bfc_free(h)
 

@@ -389,6 +389,89 @@ bf_status bf_server_poll(bf_server* s, bf_completion* out, uint32_t cap, uint32_
 bf_status bf_server_cancel(bf_server* s, uint64_t ticket);
 void bf_server_destroy(bf_server* s);
 
+/* ---- CCH customization (route/src/customization.rs:953-1436) ---------------
+ * A bf_cch holds one rank-space CCH topology on the device (the reference's
+ * CchTopo, formats/cch_topo.rs:250-290): UP edges u -> v (v > u) and DOWN
+ * edges u -> v (v < u) as two CSRs, targets strictly ascending per node,
+ * optional per-edge shortcut flags and contraction middles (u32::MAX on an
+ * original arc). Every call keeps the reference's array layout: one u32 per
+ * UP edge and one per DOWN edge, u32::MAX = no edge / unreachable.
+ *
+ * The relaxation's result is, for every edge, the smaller of its seed and
+ * the minimum over its lower triangles x -> m -> y of
+ * (w(x -> m) + w(m -> y), m), packed weight-major with the apex as
+ * tie-break, sums saturating, legs of weight u32::MAX skipped. That value is
+ * unique, so one pass in elimination-tree order returns bit for bit what the
+ * reference's passes-until-stable return, middles included. */
+typedef struct bf_cch bf_cch;
+
+typedef struct bf_cch_topo {
+  uint32_t n_nodes;
+  uint32_t reserved;
+  const uint64_t* up_offsets;       /* [n_nodes + 1]                                */
+  const uint32_t* up_targets;
+  const uint8_t* up_is_shortcut;    /* 0/1 per UP edge; NULL = no shortcuts        */
+  const uint32_t* up_middle;        /* per UP edge; NULL = all u32::MAX            */
+  const uint64_t* down_offsets;     /* [n_nodes + 1]                                */
+  const uint32_t* down_targets;
+  const uint8_t* down_is_shortcut;
+  const uint32_t* down_middle;
+} bf_cch_topo;
+
+typedef struct bf_cch_stats {
+  uint32_t n_nodes;
+  uint32_t levels;                /* elimination-tree levels                        */
+  uint64_t up_edges;
+  uint64_t down_edges;
+  uint64_t triangles;             /* (DOWN x -> m, UP m -> y) pairs, x == y included */
+  uint64_t bottom_up_shortcuts;
+  uint32_t apexes;                /* nodes with at least one triangle               */
+  uint32_t etree_levels;          /* 1: heights of the elimination tree, 0: longest path */
+  double plan_ms;                 /* bf_cch_create                                  */
+  double last_device_ms;          /* last call: device time without host copies     */
+  double last_total_ms;           /* last call: wall time with host copies          */
+} bf_cch_stats;
+
+/* Uploads the topology and builds the level plan (reverse DOWN adjacency,
+ * elimination-tree levels, triangle prefix). Replaces
+ * build_reverse_down_adj_for_relax (customization.rs:832-875) and the
+ * topology load before customize_cch / customize_cch_time_in_memory. */
+bf_status bf_cch_create(const bf_cch_topo* topo, int device, bf_cch** out);
+void bf_cch_destroy(bf_cch* c);
+bf_status bf_cch_info(const bf_cch* c, bf_cch_stats* out);
+
+/* triangle_relax_parallel (customization.rs:1083-1200): seeds in, converged
+ * weights and middles out, in place. */
+bf_status bf_cch_relax(bf_cch* c, uint32_t* up_w, uint32_t* down_w, uint32_t* up_mid,
+                       uint32_t* down_mid);
+
+/* bottom_up_customize + triangle_relax_parallel (customization.rs:571-650,
+ * customize_cch_time_in_memory): original arc weights in (entries of
+ * shortcut edges ignored), customized weights and middles out. A shortcut's
+ * bottom-up seed is dominated by the triangle through its own contraction
+ * middle, so the relaxation is seeded with u32::MAX there: same result. */
+bf_status bf_cch_customize(bf_cch* c, const uint32_t* orig_up, const uint32_t* orig_down,
+                           uint32_t* up_w, uint32_t* down_w, uint32_t* up_mid,
+                           uint32_t* down_mid);
+
+/* triangle_relax_lex_parallel (customization.rs:1253-1436): (time, length)
+ * seeds, compared time first; times and middles updated in place. Each
+ * shortcut elects the smallest apex whose (time, length) sum equals its
+ * converged pair; original edges and shortcuts without such an apex keep the
+ * given middle. Needs the topology's shortcut flags. */
+bf_status bf_cch_relax_lex(bf_cch* c, uint32_t* up_t, uint32_t* down_t, const uint32_t* up_len,
+                           const uint32_t* down_len, uint32_t* up_mid, uint32_t* down_mid);
+
+/* bottom_up_with_external_middles / bottom_up_customize
+ * (customization.rs:953-1052): an original edge takes its original weight,
+ * a shortcut u -> v with middle m takes w(u -> m) + w(m -> v) (saturating; a
+ * missing leg, or a middle not below both endpoints, reads u32::MAX). Middles
+ * NULL = the topology's. BF_ERR_INVALID when a shortcut's middle is not a
+ * rank (the reference indexes out of bounds there). */
+bf_status bf_cch_bottom_up(bf_cch* c, const uint32_t* orig_up, const uint32_t* orig_down,
+                           const uint32_t* up_mid, const uint32_t* down_mid, uint32_t* up_w,
+                           uint32_t* down_w);
+
 const char* bf_last_error(void);
 
 #ifdef __cplusplus

@@ -41,6 +41,12 @@ def load():
         lib.orc_isochrone_bitsets.argtypes = csr + [_V, _V, ctypes.c_uint64, _V, _V, ctypes.c_int]
         lib.orc_dijkstra_ebg.argtypes = [ctypes.c_uint32, _V, _V, _V, ctypes.c_uint32, _V]
         lib.orc_phast_reverse.argtypes = csr + [ctypes.c_uint32, _V]
+        lib.orc_cch_relax.argtypes = [ctypes.c_uint32] + [_V] * 8
+        lib.orc_cch_relax.restype = ctypes.c_uint32
+        lib.orc_cch_relax_lex.argtypes = [ctypes.c_uint32] + [_V] * 12
+        lib.orc_cch_relax_lex.restype = ctypes.c_uint32
+        lib.orc_cch_bottom_up.argtypes = [ctypes.c_uint32] + [_V] * 12
+        lib.orc_cch_bottom_up.restype = ctypes.c_uint32
         _lib = lib
     return _lib
 
@@ -241,3 +247,84 @@ def table_phast_lopsided_2ch(cch, src_seedsets, tgt_seedsets, threshold, up_len,
                 bt, bl = INF, INF
             out_t[s, t], out_l[s, t] = bt, bl
     return out_t, out_l, np.array(sorted(conflicts), dtype=np.uint64)
+
+
+
+class CchTopo:
+    """The reference's rank-space CCH topology (formats/cch_topo.rs:250-290):
+    UP edges u -> v (v > u) and DOWN edges u -> v (v < u) as two CSRs with
+    targets ascending per node, shortcut flags and middles (u32::MAX on an
+    original arc)."""
+
+    def __init__(self, n, up_off, up_tgt, down_off, down_tgt, up_short=None, down_short=None,
+                 up_mid=None, down_mid=None):
+        self.n = int(n)
+        self.up_off, self.up_tgt = _a(up_off, np.uint64), _a(up_tgt, np.uint32)
+        self.down_off, self.down_tgt = _a(down_off, np.uint64), _a(down_tgt, np.uint32)
+        nu, nd = len(self.up_tgt), len(self.down_tgt)
+        self.up_short = _a(np.zeros(nu, np.uint8) if up_short is None else up_short, np.uint8)
+        self.down_short = _a(np.zeros(nd, np.uint8) if down_short is None else down_short, np.uint8)
+        self.up_mid = _a(np.full(nu, INF, np.uint32) if up_mid is None else up_mid, np.uint32)
+        self.down_mid = _a(np.full(nd, INF, np.uint32) if down_mid is None else down_mid, np.uint32)
+
+    def _csr(self):
+        return (self.n, self.up_off.ctypes.data, self.up_tgt.ctypes.data,
+                self.down_off.ctypes.data, self.down_tgt.ctypes.data)
+
+    @classmethod
+    def from_upper(cls, topo):
+        """Directed form of a chordal topology given in upper-neighbour form
+        (edge e of rank j joins j and tgt[e] > j): every pair becomes an UP
+        edge j -> tgt[e] and a DOWN edge tgt[e] -> j. Returns the topology and
+        the per-edge weights (orig_up, orig_down) mapped onto it."""
+        off, tgt = _a(topo["off"], np.uint64), _a(topo["tgt"], np.uint32)
+        n = len(off) - 1
+        low = np.repeat(np.arange(n, dtype=np.uint32), np.diff(off).astype(np.int64))
+        order = np.lexsort((low, tgt))
+        down_off = np.zeros(n + 1, np.uint64)
+        down_off[1:] = np.cumsum(np.bincount(tgt, minlength=n))
+        t = cls(n, off, tgt, down_off, low[order])
+        return t, order
+
+    def relax(self, up_w, down_w, up_mid=None, down_mid=None):
+        """triangle_relax_parallel (customization.rs:1083-1200) from the given
+        seeds; returns (up_w, down_w, up_mid, down_mid, passes)."""
+        uw, dw = _a(up_w, np.uint32).copy(), _a(down_w, np.uint32).copy()
+        um = (self.up_mid if up_mid is None else _a(up_mid, np.uint32)).copy()
+        dm = (self.down_mid if down_mid is None else _a(down_mid, np.uint32)).copy()
+        passes = load().orc_cch_relax(*self._csr(), uw.ctypes.data, dw.ctypes.data,
+                                      um.ctypes.data, dm.ctypes.data)
+        if passes == 0:
+            raise RuntimeError("triangle relaxation did not converge in 100 passes")
+        return uw, dw, um, dm, passes
+
+    def relax_lex(self, up_t, down_t, up_l, down_l, up_mid=None, down_mid=None):
+        """triangle_relax_lex_parallel (customization.rs:1253-1436); returns
+        (up_t, down_t, up_mid, down_mid, passes)."""
+        ut, dt = _a(up_t, np.uint32).copy(), _a(down_t, np.uint32).copy()
+        ul, dl = _a(up_l, np.uint32), _a(down_l, np.uint32)
+        um = (self.up_mid if up_mid is None else _a(up_mid, np.uint32)).copy()
+        dm = (self.down_mid if down_mid is None else _a(down_mid, np.uint32)).copy()
+        passes = load().orc_cch_relax_lex(*self._csr(), self.up_short.ctypes.data,
+                                          self.down_short.ctypes.data, ut.ctypes.data,
+                                          dt.ctypes.data, ul.ctypes.data, dl.ctypes.data,
+                                          um.ctypes.data, dm.ctypes.data)
+        if passes == 0:
+            raise RuntimeError("lexicographic relaxation did not converge in 100 passes")
+        return ut, dt, um, dm, passes
+
+    def bottom_up(self, orig_up, orig_down, up_mid=None, down_mid=None):
+        """bottom_up_customize / bottom_up_with_external_middles
+        (customization.rs:953-1052); returns (up_w, down_w)."""
+        um = self.up_mid if up_mid is None else _a(up_mid, np.uint32)
+        dm = self.down_mid if down_mid is None else _a(down_mid, np.uint32)
+        ou, od = _a(orig_up, np.uint32), _a(orig_down, np.uint32)
+        uw = np.empty(len(self.up_tgt), np.uint32)
+        dw = np.empty(len(self.down_tgt), np.uint32)
+        rc = load().orc_cch_bottom_up(*self._csr(), self.up_short.ctypes.data,
+                                      self.down_short.ctypes.data, um.ctypes.data, dm.ctypes.data,
+                                      ou.ctypes.data, od.ctypes.data, uw.ctypes.data,
+                                      dw.ctypes.data)
+        if rc:
+            raise IndexError("shortcut middle is not a rank")
+        return uw, dw

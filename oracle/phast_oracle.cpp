@@ -466,3 +466,217 @@ void orc_phast_reverse(u32 n, const u64* up_off, const u32* up_tgt, const u32* u
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// CCH customization on the reference's directed rank-space topology
+// (formats/cch_topo.rs:250-290, CchTopo): UP edges u -> v (v > u) and DOWN
+// edges u -> v (v < u) as two CSRs, targets ascending within each node.
+// Middle u32::MAX marks an original arc (cch_topo.rs:268).
+
+namespace {
+struct CTopo {
+  u32 n;
+  const u64* uo;
+  const u32* ut;
+  const u64* dof;
+  const u32* dt;
+};
+
+// find_edge_index (customization.rs:1507-1521): binary search for target v
+// in u's list; ~0 when absent.
+u64 c_find(const u64* off, const u32* tgt, u32 u, u32 v) {
+  const u32* lo = tgt + off[u];
+  const u32* hi = tgt + off[u + 1];
+  const u32* it = std::lower_bound(lo, hi, v);
+  return (it != hi && *it == v) ? (u64)(it - tgt) : ~0ull;
+}
+
+// build_reverse_down_adj_for_relax (customization.rs:832-875): for every m
+// the DOWN edges x -> m, sources in ascending x.
+struct RevDown {
+  std::vector<u64> off;
+  std::vector<u32> src;
+  std::vector<u64> eid;
+};
+RevDown c_rev_down(const CTopo& t) {
+  RevDown r;
+  r.off.assign((size_t)t.n + 1, 0);
+  for (u64 i = 0; i < t.dof[t.n]; ++i) r.off[t.dt[i] + 1]++;
+  for (u32 m = 0; m < t.n; ++m) r.off[m + 1] += r.off[m];
+  r.src.resize(t.dof[t.n]);
+  r.eid.resize(t.dof[t.n]);
+  std::vector<u64> pos(r.off.begin(), r.off.end() - 1);
+  for (u32 u = 0; u < t.n; ++u)
+    for (u64 i = t.dof[u]; i < t.dof[u + 1]; ++i) {
+      const u64 p = pos[t.dt[i]]++;
+      r.src[p] = u;
+      r.eid[p] = i;
+    }
+  return r;
+}
+
+// One apex-ordered pass over every triangle x -> m -> y (customization.rs
+// :1110-1170): calls f(x, y, m, down edge x->m, up edge m->y, target edge,
+// target is UP) for each pair with both legs present and y != x.
+template <class F>
+void c_triangles(const CTopo& t, const RevDown& r, F&& f) {
+  for (u32 m = 0; m < t.n; ++m)
+    for (u64 ir = r.off[m]; ir < r.off[m + 1]; ++ir) {
+      const u32 x = r.src[ir];
+      for (u64 j = t.uo[m]; j < t.uo[m + 1]; ++j) {
+        const u32 y = t.ut[j];
+        if (y == x) continue;
+        if (y > x) {
+          const u64 e = c_find(t.uo, t.ut, x, y);
+          if (e != ~0ull) f(m, r.eid[ir], j, e, true);
+        } else {
+          const u64 e = c_find(t.dof, t.dt, x, y);
+          if (e != ~0ull) f(m, r.eid[ir], j, e, false);
+        }
+      }
+    }
+}
+}  // namespace
+
+extern "C" {
+// triangle_relax_parallel (customization.rs:1083-1200): packed
+// (weight << 32 | middle) per edge, seeded from the given weights and
+// middles; every pass offers each triangle's (w(x->m) + w(m->y), m) to edge
+// x -> y (legs with weight u32::MAX skipped, the sum saturating) and keeps
+// the smaller packed value; passes repeat until one changes nothing. The
+// weight and middle arrays are updated in place. Returns the number of
+// passes, 0 when 100 passes did not converge (the reference panics there).
+u32 orc_cch_relax(u32 n, const u64* uo, const u32* ut, const u64* dof, const u32* dt, u32* up_w,
+                  u32* dn_w, u32* up_mid, u32* dn_mid) {
+  const CTopo t{n, uo, ut, dof, dt};
+  const RevDown r = c_rev_down(t);
+  const u64 nu = uo[n], nd = dof[n];
+  std::vector<u64> pu(nu), pd(nd);
+  for (u64 e = 0; e < nu; ++e) pu[e] = ((u64)up_w[e] << 32) | up_mid[e];
+  for (u64 e = 0; e < nd; ++e) pd[e] = ((u64)dn_w[e] << 32) | dn_mid[e];
+  u32 passes = 0;
+  for (;;) {
+    ++passes;
+    u64 updates = 0;
+    c_triangles(t, r, [&](u32 m, u64 exm, u64 emy, u64 e, bool up) {
+      const u32 wxm = (u32)(pd[exm] >> 32), wmy = (u32)(pu[emy] >> 32);
+      if (wxm == INF || wmy == INF) return;
+      const u64 np = ((u64)sat_add(wxm, wmy) << 32) | m;
+      u64& slot = up ? pu[e] : pd[e];
+      if (np < slot) {
+        slot = np;
+        ++updates;
+      }
+    });
+    if (!updates) break;
+    if (passes >= 100) return 0;
+  }
+  for (u64 e = 0; e < nu; ++e) {
+    up_w[e] = (u32)(pu[e] >> 32);
+    up_mid[e] = (u32)pu[e];
+  }
+  for (u64 e = 0; e < nd; ++e) {
+    dn_w[e] = (u32)(pd[e] >> 32);
+    dn_mid[e] = (u32)pd[e];
+  }
+  return passes;
+}
+
+// triangle_relax_lex_parallel (customization.rs:1253-1436): packed
+// (time << 32 | length) per edge, both components summed separately with
+// saturation and compared as one u64 (time first, then length), passes until
+// no update. Then, on the converged values, every SHORTCUT edge elects the
+// smallest apex whose triangle sum equals its packed value; a shortcut with
+// no such apex, and every original edge, keeps the given middle. Times and
+// middles are updated in place; lengths are read only.
+u32 orc_cch_relax_lex(u32 n, const u64* uo, const u32* ut, const u64* dof, const u32* dt,
+                      const uint8_t* up_short, const uint8_t* dn_short, u32* up_t, u32* dn_t,
+                      const u32* up_l, const u32* dn_l, u32* up_mid, u32* dn_mid) {
+  const CTopo t{n, uo, ut, dof, dt};
+  const RevDown r = c_rev_down(t);
+  const u64 nu = uo[n], nd = dof[n];
+  std::vector<u64> pu(nu), pd(nd);
+  for (u64 e = 0; e < nu; ++e) pu[e] = ((u64)up_t[e] << 32) | up_l[e];
+  for (u64 e = 0; e < nd; ++e) pd[e] = ((u64)dn_t[e] << 32) | dn_l[e];
+  auto cand = [](u64 a, u64 b) {
+    return ((u64)sat_add((u32)(a >> 32), (u32)(b >> 32)) << 32) | sat_add((u32)a, (u32)b);
+  };
+  u32 passes = 0;
+  for (;;) {
+    ++passes;
+    u64 updates = 0;
+    c_triangles(t, r, [&](u32, u64 exm, u64 emy, u64 e, bool up) {
+      if ((u32)(pd[exm] >> 32) == INF || (u32)(pu[emy] >> 32) == INF) return;
+      const u64 np = cand(pd[exm], pu[emy]);
+      u64& slot = up ? pu[e] : pd[e];
+      if (np < slot) {
+        slot = np;
+        ++updates;
+      }
+    });
+    if (!updates) break;
+    if (passes >= 100) return 0;
+  }
+  std::vector<u32> mu(nu, INF), md(nd, INF);
+  c_triangles(t, r, [&](u32 m, u64 exm, u64 emy, u64 e, bool up) {
+    if ((u32)(pd[exm] >> 32) == INF || (u32)(pu[emy] >> 32) == INF) return;
+    const u64 np = cand(pd[exm], pu[emy]);
+    if (up) {
+      if (up_short[e] && np == pu[e]) mu[e] = std::min(mu[e], m);
+    } else {
+      if (dn_short[e] && np == pd[e]) md[e] = std::min(md[e], m);
+    }
+  });
+  for (u64 e = 0; e < nu; ++e) {
+    up_t[e] = (u32)(pu[e] >> 32);
+    if (mu[e] != INF) up_mid[e] = mu[e];
+  }
+  for (u64 e = 0; e < nd; ++e) {
+    dn_t[e] = (u32)(pd[e] >> 32);
+    if (md[e] != INF) dn_mid[e] = md[e];
+  }
+  return passes;
+}
+
+// bottom_up_customize / bottom_up_with_external_middles
+// (customization.rs:953-1052): ranks ascending; within a rank its DOWN edges
+// by ascending target, then its UP edges. An original edge takes its
+// original weight; a shortcut u -> v with middle m takes
+// w(u -> m) + w(m -> v) (saturating), a missing leg reading u32::MAX. Every
+// weight starts at u32::MAX, so a leg not yet computed in this order reads
+// u32::MAX as well. Returns 0, or 1 when a shortcut's middle is not a rank
+// (the reference indexes out of bounds there).
+u32 orc_cch_bottom_up(u32 n, const u64* uo, const u32* ut, const u64* dof, const u32* dt,
+                      const uint8_t* up_short, const uint8_t* dn_short, const u32* up_mid,
+                      const u32* dn_mid, const u32* orig_up, const u32* orig_dn, u32* out_up,
+                      u32* out_dn) {
+  const u64 nu = uo[n], nd = dof[n];
+  std::fill(out_up, out_up + nu, INF);
+  std::fill(out_dn, out_dn + nd, INF);
+  auto leg = [&](const u64* off, const u32* tgt, const u32* w, u32 a, u32 b) {
+    const u64 e = c_find(off, tgt, a, b);
+    return e == ~0ull ? INF : w[e];
+  };
+  for (u32 u = 0; u < n; ++u) {
+    for (u64 i = dof[u]; i < dof[u + 1]; ++i) {  // targets ascend: already sorted
+      if (!dn_short[i]) {
+        out_dn[i] = orig_dn[i];
+        continue;
+      }
+      const u32 m = dn_mid[i];
+      if (m >= n) return 1;
+      out_dn[i] = sat_add(leg(dof, dt, out_dn, u, m), leg(uo, ut, out_up, m, dt[i]));
+    }
+    for (u64 i = uo[u]; i < uo[u + 1]; ++i) {
+      if (!up_short[i]) {
+        out_up[i] = orig_up[i];
+        continue;
+      }
+      const u32 m = up_mid[i];
+      if (m >= n) return 1;
+      out_up[i] = sat_add(leg(dof, dt, out_dn, u, m), leg(uo, ut, out_up, m, ut[i]));
+    }
+  }
+  return 0;
+}
+}

@@ -16,6 +16,11 @@ reference_kats.json
       * route/src/server/isochrone_handler.rs:1806-1869  two-channel
         lexicographic tie (phast_2ch_lex_tests): two equal-time paths to node
         3, the shorter length must win whichever path pops first
+      * route/src/customization.rs:2269-2487  CCH customization on a
+        4-node directed topology (topo_4node): a shortcut 2 -> 3 expanded
+        through external middle 0 or 1 (lengths 13 and 105), the packed
+        (weight, middle) order, and the three (time, length) lexicographic
+        middle elections
 
 grid100_matrix.npz
     The 100 x 100 matrix of the 100 x 100 synthetic grid computed by the CPU
@@ -53,7 +58,32 @@ def kats():
                      down_tgt=list(range(n_leaf)), down_w=wd),
             expect=expect,
             thresholds=[0, 15, 25, 55, 1000] if n_leaf == 5 else [0, 30, 75, 130, 100000])
+    four = dict(n=4, up_off=[0, 1, 2, 3, 3], up_tgt=[3, 3, 3], up_short=[0, 0, 1],
+                up_mid=[INF, INF, 0], down_off=[0, 0, 0, 2, 2], down_tgt=[0, 1],
+                down_short=[0, 0], down_mid=[INF, INF])
+    customize = {
+        "source": "route/src/customization.rs:2269-2487",
+        "topo": four,
+        # shortcut_len_along_time_follows_the_time_optimal_middle (:2302-2350):
+        # original lengths 0->3 = 10, 1->3 = 100, 2->0 = 3, 2->1 = 5
+        "bottom_up": [dict(orig_up=[10, 100, 0], orig_down=[3, 5], up_mid=[INF, INF, m],
+                           down_mid=[INF, INF], up=[10, 100, want], down=[3, 5])
+                      for m, want in ((0, 13), (1, 105))],
+        # pack_wm_is_a_bijection_and_orders_by_weight_then_middle (:2352-2371)
+        "pack_order": [[[10, INF], [11, 0]], [[10, 3], [10, 4]]],
+        # lex_election_* (:2420-2487): seeds (time, length) per edge, the
+        # shortcut's converged time and elected middle
+        "lex": [
+            dict(up_t=[7, 5, 10], down_t=[3, 5], up_l=[10, 100, 105], down_l=[3, 5],
+                 time=10, middle=0),
+            dict(up_t=[5, 5, 10], down_t=[5, 5], up_l=[100, 10, 999], down_l=[5, 3],
+                 time=10, middle=1),
+            dict(up_t=[7, 5, 999], down_t=[3, 5], up_l=[6, 6, 999], down_l=[4, 4],
+                 time=10, middle=0),
+        ],
+    }
     return {
+        "cch_customize": customize,
         "five_node": {
             "source": "route/src/range/phast.rs:1180-1250",
             "cch": dict(n=5, up_off=[0, 1, 2, 4, 4, 4], up_tgt=[2, 2, 3, 4], up_w=[10, 3, 7, 5],

@@ -62,3 +62,23 @@ def test_missing_library_fails_loudly(tmp_path):
             bfphast.load(tmp_path / "nope.so")
         finally:
             bfphast._lib = None
+
+
+def test_cch_create_rejects_bad_topology(built):
+    # host-side validation runs before any device call: targets must ascend
+    # strictly, UP targets above their node and DOWN targets below it
+    import ctypes
+    import numpy as np
+    import bfphast
+    lib = bfphast.load()
+    for up_tgt, down_tgt in (([2, 1], [0]), ([1, 1], [0]), ([0, 2], [0]), ([1, 2], [2])):
+        keep = [np.array([0, 2, 2, 2], np.uint64), np.array(up_tgt, np.uint32),
+                np.array([0, 0, 1, 1], np.uint64), np.array(down_tgt, np.uint32)]
+        t = bfphast.CchTopo(n_nodes=3)
+        t.up_offsets = keep[0].ctypes.data_as(bfphast._u64p)
+        t.up_targets = keep[1].ctypes.data_as(bfphast._u32p)
+        t.down_offsets = keep[2].ctypes.data_as(bfphast._u64p)
+        t.down_targets = keep[3].ctypes.data_as(bfphast._u32p)
+        h = ctypes.c_void_p()
+        assert lib.bf_cch_create(ctypes.byref(t), 0, ctypes.byref(h)) == bfphast.BF_ERR_INVALID
+        assert not h.value
