@@ -26,6 +26,7 @@ BF_OK, BF_ERR_INVALID, BF_ERR_OOM, BF_ERR_DEVICE, BF_ERR_TIMEOUT, BF_ERR_CANCELL
     BF_ERR_UNSUPPORTED = range(8)
 ENGINE_AUTO, ENGINE_PLAIN, ENGINE_BATCHED = 0, 1, 2
 FLAG_REVERSE = 1
+CCH_SEARCH_TARGETS = 1
 REQ_MATRIX, REQ_ISOCHRONE = 1, 2
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
@@ -33,7 +34,7 @@ _u64p = ctypes.POINTER(ctypes.c_uint64)
 
 
 class CchCsr(ctypes.Structure):
-    _fields_ = [("n_nodes", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+    _fields_ = [("n_nodes", ctypes.c_uint32), ("flags", ctypes.c_uint32),
                 ("up_offsets", _u64p), ("up_targets", _u32p), ("up_weights", _u32p),
                 ("down_offsets", _u64p), ("down_targets", _u32p), ("down_weights", _u32p)]
 
@@ -117,7 +118,7 @@ class Completion(ctypes.Structure):
 
 
 class CchTopo(ctypes.Structure):
-    _fields_ = [("n_nodes", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+    _fields_ = [("n_nodes", ctypes.c_uint32), ("flags", ctypes.c_uint32),
                 ("up_offsets", _u64p), ("up_targets", _u32p),
                 ("up_is_shortcut", ctypes.c_void_p), ("up_middle", _u32p),
                 ("down_offsets", _u64p), ("down_targets", _u32p),
@@ -129,6 +130,7 @@ class CchStats(ctypes.Structure):
                 ("up_edges", ctypes.c_uint64), ("down_edges", ctypes.c_uint64),
                 ("triangles", ctypes.c_uint64), ("bottom_up_shortcuts", ctypes.c_uint64),
                 ("apexes", ctypes.c_uint32), ("etree_levels", ctypes.c_uint32),
+                ("target_index", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
                 ("plan_ms", ctypes.c_double), ("last_device_ms", ctypes.c_double),
                 ("last_total_ms", ctypes.c_double)]
 
@@ -509,12 +511,12 @@ class Cch:
     ascending per node, optional shortcut flags and contraction middles."""
 
     def __init__(self, n_nodes, up_off, up_tgt, down_off, down_tgt, up_short=None,
-                 down_short=None, up_mid=None, down_mid=None, device=0):
+                 down_short=None, up_mid=None, down_mid=None, device=0, search_targets=False):
         lib = load()
         self._keep = [np.ascontiguousarray(up_off, dtype=np.uint64), _u32(up_tgt),
                       np.ascontiguousarray(down_off, dtype=np.uint64), _u32(down_tgt)]
         self.nu, self.nd = len(self._keep[1]), len(self._keep[3])
-        t = CchTopo(n_nodes=int(n_nodes))
+        t = CchTopo(n_nodes=int(n_nodes), flags=CCH_SEARCH_TARGETS if search_targets else 0)
         t.up_offsets, t.up_targets = _ptr(self._keep[0], _u64p), _ptr(self._keep[1])
         t.down_offsets, t.down_targets = _ptr(self._keep[2], _u64p), _ptr(self._keep[3])
         for name, arr, dt in (("up_is_shortcut", up_short, np.uint8),
@@ -530,11 +532,11 @@ class Cch:
         self._h = h
 
     @classmethod
-    def from_oracle_topo(cls, t, with_short=True, device=0):
+    def from_oracle_topo(cls, t, with_short=True, device=0, search_targets=False):
         """From an oracle.CchTopo (same field meaning)."""
         return cls(t.n, t.up_off, t.up_tgt, t.down_off, t.down_tgt,
                    t.up_short if with_short else None, t.down_short if with_short else None,
-                   t.up_mid, t.down_mid, device=device)
+                   t.up_mid, t.down_mid, device=device, search_targets=search_targets)
 
     def close(self):
         if getattr(self, "_h", None):

@@ -91,126 +91,132 @@ __device__ __forceinline__ bool candidate(uint64_t pxm, uint64_t pmy, uint32_t m
   return true;
 }
 
-// Block-level load-balanced search: the block's candidate range [cb, ce)
-// spans apexes [k0, k0 + na) of the level; their prefix values, ranks, UP
-// offsets, UP counts and reverse-DOWN offsets are staged in shared memory.
-struct Stage {
-  uint64_t pre[RC + 1];
-  uint64_t uoff[RC];
-  uint64_t roff[RC];
-  uint32_t m[RC];
-  uint32_t nu[RC];
-  uint32_t k0, na;
+// One block of RC consecutive candidates of a level, computed when the plan
+// is built: its first candidate, the apexes [k0, k0 + na) it touches and its
+// candidate count.
+struct Blk {
+  uint64_t cb;
+  uint32_t k0;
+  uint16_t na;
+  uint16_t cnt;
 };
 
-__device__ uint32_t upper_apex(const uint64_t* __restrict__ cpre, uint32_t a0, uint32_t a1,
-                               uint64_t c) {
-  // last k in [a0, a1) with cpre[k] <= c
-  uint32_t lo = a0, hi = a1;
-  while (hi - lo > 1) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (__ldg(cpre + mid) <= c)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
-}
+// Block-level load-balanced search: the apexes of the block's candidates are
+// staged in shared memory (prefix relative to the block's first apex, UP
+// offset, UP count, reverse-DOWN offset, rank). Edge ids fit 31 bits.
+struct Stage {
+  uint32_t pre[RC + 1];
+  uint32_t uoff[RC];
+  uint32_t roff[RC];
+  uint32_t m[RC];
+  uint32_t nu[RC];
+};
 
-__device__ void stage_block(const PlanDev& p, uint32_t a0, uint32_t a1, uint64_t cb, uint64_t ce,
-                            Stage& st) {
-  if (threadIdx.x == 0) {
-    const uint32_t k0 = upper_apex(p.cpre, a0, a1, cb);
-    const uint32_t k1 = upper_apex(p.cpre, k0, a1, ce - 1);
-    st.k0 = k0;
-    st.na = k1 - k0 + 1;
-  }
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i <= st.na; i += blockDim.x) st.pre[i] = __ldg(p.cpre + st.k0 + i);
-  for (uint32_t i = threadIdx.x; i < st.na; i += blockDim.x) {
-    const uint32_t m = __ldg(p.apex + st.k0 + i);
+// Stages block `b` (plan arrays only, so it may run before the previous
+// level has finished); returns the block's descriptor.
+__device__ __forceinline__ Blk stage_block(const PlanDev& p, const Blk* __restrict__ blk,
+                                           uint64_t b, Stage& st) {
+  const Blk d = blk[b];
+  const uint64_t base = __ldg(p.cpre + d.k0);
+  for (uint32_t i = threadIdx.x; i <= d.na; i += blockDim.x)
+    st.pre[i] = (uint32_t)(__ldg(p.cpre + d.k0 + i) - base);
+  for (uint32_t i = threadIdx.x; i < d.na; i += blockDim.x) {
+    const uint32_t m = __ldg(p.apex + d.k0 + i);
     const uint64_t u0 = __ldg(p.uo + m);
     st.m[i] = m;
-    st.uoff[i] = u0;
+    st.uoff[i] = (uint32_t)u0;
     st.nu[i] = (uint32_t)(__ldg(p.uo + m + 1) - u0);
-    st.roff[i] = __ldg(p.ro + m);
+    st.roff[i] = (uint32_t)__ldg(p.ro + m);
   }
   __syncthreads();
+  return d;
 }
 
-// Locates candidate c of the staged range: apex index k (local) and the
-// (reverse-DOWN entry, UP edge) pair it denotes.
-__device__ __forceinline__ void locate(const Stage& st, uint64_t c, uint32_t* k, uint64_t* ir,
-                                       uint64_t* ey) {
-  uint32_t lo = 0, hi = st.na;
+// Locates the candidate at offset q from the block's first apex: local apex
+// index k and the (reverse-DOWN entry, UP edge) pair it denotes.
+__device__ __forceinline__ void locate(const Stage& st, uint32_t na, uint32_t q, uint32_t* k,
+                                       uint32_t* ir, uint32_t* ey) {
+  uint32_t lo = 0, hi = na;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
-    if (st.pre[mid] <= c)
+    if (st.pre[mid] <= q)
       lo = mid;
     else
       hi = mid;
   }
-  const uint32_t q = (uint32_t)(c - st.pre[lo]);
+  const uint32_t r = q - st.pre[lo];
   const uint32_t nu = st.nu[lo];
-  const uint32_t i = q / nu;
+  const uint32_t i = r / nu;
   *k = lo;
   *ir = st.roff[lo] + i;
-  *ey = st.uoff[lo] + (q - i * nu);
+  *ey = st.uoff[lo] + (r - i * nu);
 }
 
-// Target edge x -> y of a triangle: the UP edge in x's UP list when y > x,
-// else the DOWN edge in x's DOWN list (customization.rs:1140-1165).
-__device__ __forceinline__ uint64_t* target_slot(const PlanDev& p, uint32_t x, uint32_t y,
-                                                 uint64_t* pu, uint64_t* pd, uint64_t* eidx,
-                                                 bool* up) {
+constexpr uint32_t NO_TARGET = 0xFFFFFFFFu;
+
+// Target edge of a candidate as an edge id with DIR_DOWN set for a DOWN
+// edge, NO_TARGET when y == x or the edge is absent; read from the plan's
+// precomputed index or searched in x's list.
+template <bool TIDX>
+__device__ __forceinline__ uint32_t target_of(const PlanDev& p, const uint32_t* __restrict__ tidx,
+                                              uint64_t c, uint32_t ir, uint32_t ey) {
+  if (TIDX) return __ldcs(tidx + c);  // read once per call: streaming
+  const uint32_t x = __ldg(p.rs + ir);
+  const uint32_t y = __ldg(p.ut + ey);
+  if (y == x) return NO_TARGET;
   if (y > x) {
     const uint64_t e = find_edge(p.uo, p.ut, x, y);
-    *eidx = e;
-    *up = true;
-    return e == ~0ull ? nullptr : pu + e;
+    return e == ~0ull ? NO_TARGET : (uint32_t)e;
   }
   const uint64_t e = find_edge(p.dof, p.dt, x, y);
-  *eidx = e;
-  *up = false;
-  return e == ~0ull ? nullptr : pd + e;
+  return e == ~0ull ? NO_TARGET : ((uint32_t)e | DIR_DOWN);
 }
 
-// One level of the relaxation: every candidate of apexes [a0, a1)
-// (candidates [c0, c1)) is offered to its target edge with a 64-bit
-// atomicMin on the packed value. A fresh L2 read first drops candidates that
-// cannot win (values only decrease, so the read is an upper bound).
-template <bool LEX>
-__global__ void __launch_bounds__(RT) k_relax(PlanDev p, uint32_t a0, uint32_t a1, uint64_t c0,
-                                              uint64_t c1, uint64_t* __restrict__ pu,
+// The target index of every candidate, once per plan.
+__global__ void __launch_bounds__(RT) k_tidx(PlanDev p, const Blk* __restrict__ blk,
+                                             uint32_t* __restrict__ tidx) {
+  __shared__ Stage st;
+  const Blk d = stage_block(p, blk, blockIdx.x, st);
+  const uint32_t q0 = (uint32_t)(d.cb - __ldg(p.cpre + d.k0));
+  for (uint32_t r = threadIdx.x; r < d.cnt; r += RT) {
+    uint32_t k, ir, ey;
+    locate(st, d.na, q0 + r, &k, &ir, &ey);
+    tidx[d.cb + r] = target_of<false>(p, nullptr, 0, ir, ey);
+  }
+}
+
+// One level of the relaxation: every candidate of the level's blocks is
+// offered to its target edge with a 64-bit atomicMin on the packed value. A
+// fresh L2 read first drops candidates that cannot win (values only
+// decrease, so the read is an upper bound).
+template <bool LEX, bool TIDX>
+__global__ void __launch_bounds__(RT) k_relax(PlanDev p, const Blk* __restrict__ blk, uint64_t b0,
+                                              const uint32_t* __restrict__ tidx,
+                                              uint64_t* __restrict__ pu,
                                               uint64_t* __restrict__ pd) {
   __shared__ Stage st;
-  const uint64_t cb = c0 + (uint64_t)blockIdx.x * RC;
-  const uint64_t ce = min(c1, cb + RC);
-  stage_block(p, a0, a1, cb, ce, st);  // plan arrays only: overlaps the previous level
+  const Blk d = stage_block(p, blk, b0 + blockIdx.x, st);  // overlaps the previous level
   pdl_launch();
   pdl_wait();
-  for (int r = 0; r < RI; ++r) {
-    const uint64_t c = cb + (uint64_t)r * RT + threadIdx.x;
-    if (c >= ce) break;
-    uint32_t k;
-    uint64_t ir, ey;
-    locate(st, c, &k, &ir, &ey);
-    const uint32_t x = __ldg(p.rs + ir);
-    const uint32_t y = __ldg(p.ut + ey);
-    if (y == x) continue;
+  const uint32_t q0 = (uint32_t)(d.cb - __ldg(p.cpre + d.k0));
+  for (uint32_t r = threadIdx.x; r < d.cnt; r += RT) {
+    uint32_t k, ir, ey;
+    locate(st, d.na, q0 + r, &k, &ir, &ey);
+    const uint32_t t = target_of<TIDX>(p, tidx, d.cb + r, ir, ey);
+    if (t == NO_TARGET) continue;
     uint64_t cand;
     if (!candidate<LEX>(__ldcg(pd + __ldg(p.re + ir)), __ldcg(pu + ey), st.m[k], &cand)) continue;
-    uint64_t e;
-    bool up;
-    uint64_t* slot = target_slot(p, x, y, pu, pd, &e, &up);
-    if (slot && cand < __ldcg(slot)) atomicMin((unsigned long long*)slot, (unsigned long long)cand);
+    uint64_t* slot = (t & DIR_DOWN ? pd : pu) + (t & ~DIR_DOWN);
+    if (cand < __ldcg(slot)) atomicMin((unsigned long long*)slot, (unsigned long long)cand);
   }
 }
 
 // Middle election of the lexicographic relaxation on converged values
 // (customization.rs:1340-1400): the smallest apex whose candidate equals a
 // SHORTCUT edge's packed value.
-__global__ void __launch_bounds__(RT) k_recover(PlanDev p, uint32_t a1, uint64_t c1,
+template <bool TIDX>
+__global__ void __launch_bounds__(RT) k_recover(PlanDev p, const Blk* __restrict__ blk,
+                                                const uint32_t* __restrict__ tidx,
                                                 const uint64_t* __restrict__ pu,
                                                 const uint64_t* __restrict__ pd,
                                                 const uint8_t* __restrict__ us,
@@ -218,26 +224,20 @@ __global__ void __launch_bounds__(RT) k_recover(PlanDev p, uint32_t a1, uint64_t
                                                 uint32_t* __restrict__ mu,
                                                 uint32_t* __restrict__ md) {
   __shared__ Stage st;
-  const uint64_t cb = (uint64_t)blockIdx.x * RC;
-  const uint64_t ce = min(c1, cb + RC);
-  stage_block(p, 0, a1, cb, ce, st);
-  for (int r = 0; r < RI; ++r) {
-    const uint64_t c = cb + (uint64_t)r * RT + threadIdx.x;
-    if (c >= ce) break;
-    uint32_t k;
-    uint64_t ir, ey;
-    locate(st, c, &k, &ir, &ey);
-    const uint32_t x = __ldg(p.rs + ir);
-    const uint32_t y = __ldg(p.ut + ey);
-    if (y == x) continue;
+  const Blk d = stage_block(p, blk, blockIdx.x, st);
+  const uint32_t q0 = (uint32_t)(d.cb - __ldg(p.cpre + d.k0));
+  for (uint32_t r = threadIdx.x; r < d.cnt; r += RT) {
+    uint32_t k, ir, ey;
+    locate(st, d.na, q0 + r, &k, &ir, &ey);
+    const uint32_t t = target_of<TIDX>(p, tidx, d.cb + r, ir, ey);
+    if (t == NO_TARGET) continue;
+    const bool down = t & DIR_DOWN;
+    const uint32_t e = t & ~DIR_DOWN;
+    if (!(down ? ds[e] : us[e])) continue;
     uint64_t cand;
     if (!candidate<true>(__ldg(pd + __ldg(p.re + ir)), __ldg(pu + ey), 0, &cand)) continue;
-    uint64_t e;
-    bool up;
-    const uint64_t* slot = target_slot(p, x, y, const_cast<uint64_t*>(pu),
-                                       const_cast<uint64_t*>(pd), &e, &up);
-    if (!slot || !(up ? us[e] : ds[e]) || __ldg(slot) != cand) continue;
-    atomicMin(up ? mu + e : md + e, st.m[k]);
+    if (__ldg((down ? pd : pu) + e) != cand) continue;
+    atomicMin((down ? md : mu) + e, st.m[k]);
   }
 }
 
@@ -346,6 +346,9 @@ struct bf_cch {
   uint8_t *d_us = nullptr, *d_ds = nullptr;  // shortcut flags (null: none given)
   uint32_t *d_mu0 = nullptr, *d_md0 = nullptr;  // topology middles (null: all u32::MAX)
   uint32_t *d_btail = nullptr, *d_bedge = nullptr;  // bottom-up lists by level
+  Blk* d_blk = nullptr;                               // relaxation blocks, level after level
+  uint32_t* d_tidx = nullptr;                         // target edge per candidate (or null)
+  std::vector<uint64_t> lv_blk;                       // [levels + 1] first block per level
   // relaxation levels: apex ranges and candidate ranges
   std::vector<uint32_t> lv_apex;   // [levels + 1]
   std::vector<uint64_t> lv_cand;   // [levels + 1]
@@ -376,7 +379,7 @@ void free_plan(bf_cch* c) {
     if (g) cudaGraphExecDestroy(g);
   if (c->g_bu) cudaGraphExecDestroy(c->g_bu);
   void* ptrs[] = {c->d_uo, c->d_do, c->d_ro, c->d_cpre, c->d_ut, c->d_dt, c->d_rs, c->d_re,
-                  c->d_apex, c->d_us, c->d_ds, c->d_mu0, c->d_md0, c->d_btail, c->d_bedge,
+                  c->d_apex, c->d_us, c->d_ds, c->d_mu0, c->d_md0, c->d_btail, c->d_bedge, c->d_blk, c->d_tidx,
                   c->d_pu, c->d_pd, c->d_w[0], c->d_w[1], c->d_w[2], c->d_w[3], c->d_l[0],
                   c->d_l[1], c->d_err};
   for (void* p : ptrs)
@@ -473,8 +476,8 @@ bf_status build_plan(bf_cch* c, const bf_cch_topo* t) {
       const uint32_t m = order[i];
       const uint64_t k = (ro[m + 1] - ro[m]) * (t->up_offsets[m + 1] - t->up_offsets[m]);
       if (!k) continue;
-      if (k >= (1ull << 32)) {
-        set_error("bf_cch_create: a node has 2^32 or more triangles");
+      if (k >= (1ull << 30)) {
+        set_error("bf_cch_create: a node has 2^30 or more triangles");
         return BF_ERR_INVALID;
       }
       apex.push_back(m);
@@ -485,6 +488,21 @@ bf_status build_plan(bf_cch* c, const bf_cch_topo* t) {
   }
   c->napex = (uint32_t)apex.size();
   c->ncand = cpre.back();
+  // relaxation blocks: RC consecutive candidates of one level each
+  std::vector<Blk> blks;
+  c->lv_blk.assign((size_t)L + 1, 0);
+  for (uint32_t l = 0; l < L; ++l) {
+    uint32_t k = c->lv_apex[l];
+    const uint32_t a1 = c->lv_apex[l + 1];
+    for (uint64_t cb = c->lv_cand[l]; cb < c->lv_cand[l + 1]; cb += RC) {
+      const uint64_t ce = std::min<uint64_t>(cb + RC, c->lv_cand[l + 1]);
+      while (k + 1 < a1 && cpre[k + 1] <= cb) ++k;
+      uint32_t k1 = k;
+      while (k1 + 1 < a1 && cpre[k1 + 1] < ce) ++k1;
+      blks.push_back(Blk{cb, k, (uint16_t)(k1 - k + 1), (uint16_t)(ce - cb)});
+    }
+    c->lv_blk[l + 1] = blks.size();
+  }
   // bottom-up lists: shortcuts by the level of their lower endpoint
   std::vector<uint32_t> btail, bedge;
   c->lv_bu.assign((size_t)L + 1, 0);
@@ -523,6 +541,7 @@ bf_status build_plan(bf_cch* c, const bf_cch_topo* t) {
   if (t->up_middle) BF_CUDA(upload(&c->d_mu0, t->up_middle, nu));
   if (t->down_middle) BF_CUDA(upload(&c->d_md0, t->down_middle, nd));
   BF_CUDA(upload(&c->d_btail, btail.data(), btail.size()));
+  BF_CUDA(upload(&c->d_blk, blks.data(), blks.size()));
   BF_CUDA(upload(&c->d_bedge, bedge.data(), bedge.size()));
   const uint64_t nmax = std::max<uint64_t>(1, std::max(nu, nd));
   BF_CUDA(cudaMalloc(&c->d_pu, std::max<uint64_t>(1, nu) * 8));
@@ -530,6 +549,15 @@ bf_status build_plan(bf_cch* c, const bf_cch_topo* t) {
   for (int i = 0; i < 4; ++i) BF_CUDA(cudaMalloc(&c->d_w[i], nmax * 4));
   for (int i = 0; i < 2; ++i) BF_CUDA(cudaMalloc(&c->d_l[i], nmax * 4));
   BF_CUDA(cudaMalloc(&c->d_err, 4));
+  // target index: 4 bytes per candidate while that fits a quarter of free HBM
+  size_t fr = 0, tot = 0;
+  BF_CUDA(cudaMemGetInfo(&fr, &tot));
+  if (!(t->flags & BF_CCH_SEARCH_TARGETS) && c->ncand && c->ncand * 4 <= fr / 4) {
+    BF_CUDA(cudaMalloc(&c->d_tidx, c->ncand * 4));
+    k_tidx<<<(unsigned)blks.size(), RT, 0, c->s>>>(c->dev(), c->d_blk, c->d_tidx);
+    BF_CUDA(cudaGetLastError());
+    BF_CUDA(cudaStreamSynchronize(c->s));
+  }
   return BF_OK;
 }
 
@@ -542,14 +570,22 @@ bf_status run_relax(bf_cch* c, bool lex) {
     cudaError_t err = cudaSuccess;
     bool first = true;
     const PlanDev p = c->dev();
-    for (size_t l = 0; l + 1 < c->lv_cand.size() && err == cudaSuccess; ++l) {
-      const uint64_t c0 = c->lv_cand[l], c1 = c->lv_cand[l + 1];
-      if (c1 == c0) continue;
-      const unsigned blocks = (unsigned)((c1 - c0 + RC - 1) / RC);
-      err = lex ? launch_level(k_relax<true>, dim3(blocks), RT, !first, c->s, p, c->lv_apex[l],
-                               c->lv_apex[l + 1], c0, c1, c->d_pu, c->d_pd)
-                : launch_level(k_relax<false>, dim3(blocks), RT, !first, c->s, p, c->lv_apex[l],
-                               c->lv_apex[l + 1], c0, c1, c->d_pu, c->d_pd);
+    for (size_t l = 0; l + 1 < c->lv_blk.size() && err == cudaSuccess; ++l) {
+      const uint64_t b0 = c->lv_blk[l], b1 = c->lv_blk[l + 1];
+      if (b1 == b0) continue;
+      const Blk* blk = c->d_blk;
+      const uint32_t* ti = c->d_tidx;
+      const dim3 grid((unsigned)(b1 - b0));
+      if (ti)
+        err = lex ? launch_level(k_relax<true, true>, grid, RT, !first, c->s, p, blk, b0, ti,
+                                 c->d_pu, c->d_pd)
+                  : launch_level(k_relax<false, true>, grid, RT, !first, c->s, p, blk, b0, ti,
+                                 c->d_pu, c->d_pd);
+      else
+        err = lex ? launch_level(k_relax<true, false>, grid, RT, !first, c->s, p, blk, b0, ti,
+                                 c->d_pu, c->d_pd)
+                  : launch_level(k_relax<false, false>, grid, RT, !first, c->s, p, blk, b0, ti,
+                                 c->d_pu, c->d_pd);
       first = false;
     }
     cudaError_t e2 = cudaStreamEndCapture(c->s, &g);
@@ -623,6 +659,10 @@ bf_status bf_cch_create(const bf_cch_topo* t, int device, bf_cch** out) {
   if (out) *out = nullptr;
   if (!t || !out || !t->up_offsets || !t->down_offsets || t->n_nodes == 0) {
     set_error("bf_cch_create: null argument or empty topology");
+    return BF_ERR_INVALID;
+  }
+  if (t->flags & ~BF_CCH_SEARCH_TARGETS) {
+    set_error("bf_cch_create: unknown flags");
     return BF_ERR_INVALID;
   }
   const uint32_t n = t->n_nodes;
@@ -711,6 +751,7 @@ bf_status bf_cch_info(const bf_cch* c, bf_cch_stats* info) {
   info->down_edges = c->nd;
   info->apexes = c->napex;
   info->etree_levels = c->etree_levels ? 1 : 0;
+  info->target_index = c->d_tidx ? 1 : 0;
   info->triangles = c->ncand;
   info->bottom_up_shortcuts = c->lv_bu.empty() ? 0 : c->lv_bu.back();
   info->plan_ms = c->plan_ms;
@@ -799,9 +840,15 @@ bf_status bf_cch_relax_lex(bf_cch* c, uint32_t* up_t, uint32_t* down_t, const ui
   if (c->nu) BF_CUDA(cudaMemsetAsync(c->d_l[0], 0xFF, c->nu * 4, c->s));
   if (c->nd) BF_CUDA(cudaMemsetAsync(c->d_l[1], 0xFF, c->nd * 4, c->s));
   if (c->ncand) {
-    const uint64_t blocks = (c->ncand + RC - 1) / RC;
-    k_recover<<<(unsigned)blocks, RT, 0, c->s>>>(c->dev(), c->napex, c->ncand, c->d_pu, c->d_pd,
-                                                 c->d_us, c->d_ds, c->d_l[0], c->d_l[1]);
+    const uint64_t blocks = c->lv_blk.back();
+    if (c->d_tidx)
+      k_recover<true><<<(unsigned)blocks, RT, 0, c->s>>>(c->dev(), c->d_blk, c->d_tidx, c->d_pu,
+                                                         c->d_pd, c->d_us, c->d_ds, c->d_l[0],
+                                                         c->d_l[1]);
+    else
+      k_recover<false><<<(unsigned)blocks, RT, 0, c->s>>>(c->dev(), c->d_blk, nullptr, c->d_pu,
+                                                          c->d_pd, c->d_us, c->d_ds, c->d_l[0],
+                                                          c->d_l[1]);
     BF_CUDA(cudaGetLastError());
   }
   if (c->nu) k_unpack<<<pack_grid(c->nu), 256, 0, c->s>>>(c->nu, c->d_pu, c->d_w[0], c->d_w[2], c->d_l[0]);

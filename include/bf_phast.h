@@ -25,6 +25,9 @@
  *   bf_isochrone_bitsets   the PHAST part of isochrone_bulk_handler  isochrone_handler.rs:1668-1709
  *                          and BatchedIsochroneEngine::query_many    route/src/range/batched_isochrone.rs:216
  *   bf_server_*            the tiling / admission loop of do_matrix  route/src/server/flight.rs:589,957-1110
+ *   bf_cch_customize       customize_cch_time_in_memory (weights)    route/src/customization.rs:571
+ *   bf_cch_relax[_lex]     triangle_relax_parallel / _lex_parallel   customization.rs:1083, :1253
+ *   bf_cch_bottom_up       bottom_up_customize / _with_external_middles  customization.rs:1005, :953
  *
  * Conventions (as in the reference):
  *   - node ids are CCH ranks (rank-aligned CCH, node_id == rank);
@@ -405,9 +408,14 @@ void bf_server_destroy(bf_server* s);
  * reference's passes-until-stable return, middles included. */
 typedef struct bf_cch bf_cch;
 
+/* bf_cch_topo.flags: search each triangle's target edge in every call
+ * instead of precomputing it (4 bytes per triangle, taken when that fits a
+ * quarter of the free device memory). */
+#define BF_CCH_SEARCH_TARGETS 1u
+
 typedef struct bf_cch_topo {
   uint32_t n_nodes;
-  uint32_t reserved;
+  uint32_t flags;                   /* BF_CCH_* */
   const uint64_t* up_offsets;       /* [n_nodes + 1]                                */
   const uint32_t* up_targets;
   const uint8_t* up_is_shortcut;    /* 0/1 per UP edge; NULL = no shortcuts        */
@@ -427,6 +435,8 @@ typedef struct bf_cch_stats {
   uint64_t bottom_up_shortcuts;
   uint32_t apexes;                /* nodes with at least one triangle               */
   uint32_t etree_levels;          /* 1: heights of the elimination tree, 0: longest path */
+  uint32_t target_index;          /* 1: target edges precomputed per triangle        */
+  uint32_t reserved;
   double plan_ms;                 /* bf_cch_create                                  */
   double last_device_ms;          /* last call: device time without host copies     */
   double last_total_ms;           /* last call: wall time with host copies          */

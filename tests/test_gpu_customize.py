@@ -43,9 +43,11 @@ def test_reference_four_node(built, kats):
 @pytest.mark.parametrize("rows,cols,seed,order,w_max", [
     (12, 14, 1, "nd", 60), (15, 15, 2, "nd", 6), (9, 10, 3, "random", 40),
     (20, 24, 4, "nd", 1000), (6, 40, 5, "nd", 3)])
-def test_directed_topologies(built, rows, cols, seed, order, w_max):
+@pytest.mark.parametrize("search", [False, True])
+def test_directed_topologies(built, rows, cols, seed, order, w_max, search):
     t, ou, od = cchgen.grid_topology(rows, cols, seed, order=order, w_max=w_max, diagonals=0.2)
-    g = _gpu(t)
+    g = _gpu(t, search_targets=search)
+    assert g.info()["target_index"] == (0 if search else 1)
     # the union of a directed elimination need not be chordal (two
     # in-neighbours of a node are not joined), so either level kind occurs
     assert g.info()["levels"] > 1
@@ -66,12 +68,13 @@ def test_directed_topologies(built, rows, cols, seed, order, w_max):
     _eq(g.bottom_up(lu, ld, um, dm), t.bottom_up(lu, ld, um, dm))
 
 
-def test_arbitrary_and_saturating_seeds(built):
+@pytest.mark.parametrize("search", [False, True])
+def test_arbitrary_and_saturating_seeds(built, search):
     # the reference's fixed point from any seeds: below-optimal seeds,
     # u32::MAX seeds with middles, and legs whose sums saturate (a candidate
     # (u32::MAX, apex) can still lower the middle of a u32::MAX edge)
     t, ou, od = cchgen.grid_topology(11, 13, 9, w_max=30)
-    g = _gpu(t)
+    g = _gpu(t, search_targets=search)
     rng = np.random.default_rng(9)
     for trial in range(4):
         su = rng.integers(0, 200, len(ou)).astype(np.uint32)
@@ -106,11 +109,12 @@ def test_unclosed_topology_uses_longest_path_levels(built):
     uo, ut = csr(up)
     do, dt = csr(dn)
     t = orc.CchTopo(n, uo, ut, do, dt)
-    g = _gpu(t, with_short=False)
-    assert g.info()["etree_levels"] == 0
     su = rng.integers(0, 1000, len(up)).astype(np.uint32)
     sd = rng.integers(0, 1000, len(dn)).astype(np.uint32)
-    _eq(g.relax(su, sd, t.up_mid, t.down_mid), t.relax(su, sd)[:4])
+    for search in (False, True):
+        g = _gpu(t, with_short=False, search_targets=search)
+        assert g.info()["etree_levels"] == 0
+        _eq(g.relax(su, sd, t.up_mid, t.down_mid), t.relax(su, sd)[:4])
 
 
 def test_bottom_up_middle_edge_cases(built):
