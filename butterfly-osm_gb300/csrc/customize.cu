@@ -188,26 +188,49 @@ __global__ void __launch_bounds__(RT) k_tidx(PlanDev p, const Blk* __restrict__ 
 // One level of the relaxation: every candidate of the level's blocks is
 // offered to its target edge with a 64-bit atomicMin on the packed value. A
 // fresh L2 read first drops candidates that cannot win (values only
-// decrease, so the read is an upper bound).
+// decrease, so the read is an upper bound). Everything that depends on the
+// plan alone (apex staging, target edge, DOWN leg id) is fetched before the
+// wait on the previous level; after it, each candidate issues its three
+// state loads at once, for all of the thread's candidates together.
 template <bool LEX, bool TIDX>
 __global__ void __launch_bounds__(RT) k_relax(PlanDev p, const Blk* __restrict__ blk, uint64_t b0,
                                               const uint32_t* __restrict__ tidx,
                                               uint64_t* __restrict__ pu,
                                               uint64_t* __restrict__ pd) {
   __shared__ Stage st;
-  const Blk d = stage_block(p, blk, b0 + blockIdx.x, st);  // overlaps the previous level
+  const Blk d = stage_block(p, blk, b0 + blockIdx.x, st);
   pdl_launch();
-  pdl_wait();
   const uint32_t q0 = (uint32_t)(d.cb - __ldg(p.cpre + d.k0));
-  for (uint32_t r = threadIdx.x; r < d.cnt; r += RT) {
-    uint32_t k, ir, ey;
-    locate(st, d.na, q0 + r, &k, &ir, &ey);
-    const uint32_t t = target_of<TIDX>(p, tidx, d.cb + r, ir, ey);
-    if (t == NO_TARGET) continue;
+  uint32_t tg[RI], lx[RI], ly[RI], am[RI];
+#pragma unroll
+  for (int i = 0; i < RI; ++i) {
+    const uint32_t r = threadIdx.x + i * RT;
+    tg[i] = NO_TARGET;
+    if (r < d.cnt) {
+      uint32_t k, ir, ey;
+      locate(st, d.na, q0 + r, &k, &ir, &ey);
+      tg[i] = target_of<TIDX>(p, tidx, d.cb + r, ir, ey);
+      lx[i] = __ldg(p.re + ir);
+      ly[i] = ey;
+      am[i] = st.m[k];
+    }
+  }
+  pdl_wait();
+  uint64_t a[RI], b[RI], cur[RI];
+#pragma unroll
+  for (int i = 0; i < RI; ++i) {
+    if (tg[i] == NO_TARGET) continue;
+    a[i] = __ldcg(pd + lx[i]);
+    b[i] = __ldcg(pu + ly[i]);
+    cur[i] = __ldcg((tg[i] & DIR_DOWN ? pd : pu) + (tg[i] & ~DIR_DOWN));
+  }
+#pragma unroll
+  for (int i = 0; i < RI; ++i) {
+    if (tg[i] == NO_TARGET) continue;
     uint64_t cand;
-    if (!candidate<LEX>(__ldcg(pd + __ldg(p.re + ir)), __ldcg(pu + ey), st.m[k], &cand)) continue;
-    uint64_t* slot = (t & DIR_DOWN ? pd : pu) + (t & ~DIR_DOWN);
-    if (cand < __ldcg(slot)) atomicMin((unsigned long long*)slot, (unsigned long long)cand);
+    if (!candidate<LEX>(a[i], b[i], am[i], &cand) || !(cand < cur[i])) continue;
+    atomicMin((unsigned long long*)((tg[i] & DIR_DOWN ? pd : pu) + (tg[i] & ~DIR_DOWN)),
+              (unsigned long long)cand);
   }
 }
 
