@@ -43,6 +43,8 @@ def load():
         lib.orc_phast_reverse.argtypes = csr + [ctypes.c_uint32, _V]
         lib.orc_cch_relax.argtypes = [ctypes.c_uint32] + [_V] * 8
         lib.orc_cch_relax.restype = ctypes.c_uint32
+        lib.orc_cch_relax_par.argtypes = [ctypes.c_uint32] + [_V] * 8 + [ctypes.c_int, _V]
+        lib.orc_cch_relax_par.restype = ctypes.c_uint32
         lib.orc_cch_relax_lex.argtypes = [ctypes.c_uint32] + [_V] * 12
         lib.orc_cch_relax_lex.restype = ctypes.c_uint32
         lib.orc_cch_bottom_up.argtypes = [ctypes.c_uint32] + [_V] * 12
@@ -280,20 +282,28 @@ class CchTopo:
         off, tgt = _a(topo["off"], np.uint64), _a(topo["tgt"], np.uint32)
         n = len(off) - 1
         low = np.repeat(np.arange(n, dtype=np.uint32), np.diff(off).astype(np.int64))
-        order = np.lexsort((low, tgt))
+        order = np.argsort(tgt, kind="stable")  # (target, source): sources already ascend
         down_off = np.zeros(n + 1, np.uint64)
         down_off[1:] = np.cumsum(np.bincount(tgt, minlength=n))
         t = cls(n, off, tgt, down_off, low[order])
         return t, order
 
-    def relax(self, up_w, down_w, up_mid=None, down_mid=None):
+    def relax(self, up_w, down_w, up_mid=None, down_mid=None, threads=1):
         """triangle_relax_parallel (customization.rs:1083-1200) from the given
-        seeds; returns (up_w, down_w, up_mid, down_mid, passes)."""
+        seeds; returns (up_w, down_w, up_mid, down_mid, passes). threads > 1
+        (or 0 = all cores) runs the apex-parallel atomic form."""
         uw, dw = _a(up_w, np.uint32).copy(), _a(down_w, np.uint32).copy()
         um = (self.up_mid if up_mid is None else _a(up_mid, np.uint32)).copy()
         dm = (self.down_mid if down_mid is None else _a(down_mid, np.uint32)).copy()
-        passes = load().orc_cch_relax(*self._csr(), uw.ctypes.data, dw.ctypes.data,
-                                      um.ctypes.data, dm.ctypes.data)
+        if threads == 1:
+            passes = load().orc_cch_relax(*self._csr(), uw.ctypes.data, dw.ctypes.data,
+                                          um.ctypes.data, dm.ctypes.data)
+        else:
+            used = ctypes.c_int(0)
+            passes = load().orc_cch_relax_par(*self._csr(), uw.ctypes.data, dw.ctypes.data,
+                                              um.ctypes.data, dm.ctypes.data, int(threads),
+                                              ctypes.byref(used))
+            self.threads_used = used.value
         if passes == 0:
             raise RuntimeError("triangle relaxation did not converge in 100 passes")
         return uw, dw, um, dm, passes

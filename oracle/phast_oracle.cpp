@@ -12,6 +12,7 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <functional>
@@ -578,6 +579,78 @@ u32 orc_cch_relax(u32 n, const u64* uo, const u32* ut, const u64* dof, const u32
   for (u64 e = 0; e < nd; ++e) {
     dn_w[e] = (u32)(pd[e] >> 32);
     dn_mid[e] = (u32)pd[e];
+  }
+  return passes;
+}
+
+// triangle_relax_parallel as the reference runs it (customization.rs:1083-1200):
+// each pass spreads the apexes over n_threads host threads (rayon's
+// into_par_iter), every candidate lowers its target with an atomic fetch_min
+// on the packed value, and passes repeat until one changes nothing. The
+// fixed point is the same as orc_cch_relax's; this is the timed CPU
+// baseline. Returns the number of passes (0: no convergence in 100).
+u32 orc_cch_relax_par(u32 n, const u64* uo, const u32* ut, const u64* dof, const u32* dt,
+                      u32* up_w, u32* dn_w, u32* up_mid, u32* dn_mid, int n_threads,
+                      int* threads_used) {
+  const CTopo t{n, uo, ut, dof, dt};
+  const RevDown r = c_rev_down(t);
+  const u64 nu = uo[n], nd = dof[n];
+  std::vector<std::atomic<u64>> pu(nu), pd(nd);
+  for (u64 e = 0; e < nu; ++e) pu[e].store(((u64)up_w[e] << 32) | up_mid[e], std::memory_order_relaxed);
+  for (u64 e = 0; e < nd; ++e) pd[e].store(((u64)dn_w[e] << 32) | dn_mid[e], std::memory_order_relaxed);
+  if (n_threads <= 0) n_threads = omp_get_max_threads();
+  auto fetch_min = [](std::atomic<u64>& a, u64 v) {
+    u64 cur = a.load(std::memory_order_relaxed);
+    while (v < cur && !a.compare_exchange_weak(cur, v, std::memory_order_relaxed)) {
+    }
+    return v < cur;
+  };
+  u32 passes = 0;
+  int used = 1;
+  for (;;) {
+    ++passes;
+    u64 updates = 0;
+#pragma omp parallel num_threads(n_threads) reduction(+ : updates)
+    {
+#pragma omp single
+      used = omp_get_num_threads();
+#pragma omp for schedule(dynamic, 256)
+      for (long long mm = 0; mm < (long long)n; ++mm) {
+        const u32 m = (u32)mm;
+        for (u64 ir = r.off[m]; ir < r.off[m + 1]; ++ir) {
+          const u32 x = r.src[ir];
+          const u32 wxm = (u32)(pd[r.eid[ir]].load(std::memory_order_relaxed) >> 32);
+          if (wxm == INF) continue;
+          for (u64 j = uo[m]; j < uo[m + 1]; ++j) {
+            const u32 y = ut[j];
+            if (y == x) continue;
+            const u32 wmy = (u32)(pu[j].load(std::memory_order_relaxed) >> 32);
+            if (wmy == INF) continue;
+            const u64 np = ((u64)sat_add(wxm, wmy) << 32) | m;
+            if (y > x) {
+              const u64 e = c_find(uo, ut, x, y);
+              if (e != ~0ull && fetch_min(pu[e], np)) ++updates;
+            } else {
+              const u64 e = c_find(dof, dt, x, y);
+              if (e != ~0ull && fetch_min(pd[e], np)) ++updates;
+            }
+          }
+        }
+      }
+    }
+    if (!updates) break;
+    if (passes >= 100) return 0;
+  }
+  if (threads_used) *threads_used = used;
+  for (u64 e = 0; e < nu; ++e) {
+    const u64 v = pu[e].load(std::memory_order_relaxed);
+    up_w[e] = (u32)(v >> 32);
+    up_mid[e] = (u32)v;
+  }
+  for (u64 e = 0; e < nd; ++e) {
+    const u64 v = pd[e].load(std::memory_order_relaxed);
+    dn_w[e] = (u32)(v >> 32);
+    dn_mid[e] = (u32)v;
   }
   return passes;
 }

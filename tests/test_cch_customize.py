@@ -97,3 +97,15 @@ def test_directed_topology_is_closed(built):
             for y in ys:
                 if x != y:
                     assert ((x, y) in up) if y > x else ((x, y) in dn)
+
+
+def test_parallel_relaxation_matches_sequential(built):
+    # the apex-parallel atomic form (the reference's own) reaches the same
+    # fixed point, middles included
+    for seed in (1, 2):
+        t, ou, od = cchgen.grid_topology(14, 14, seed, w_max=5)
+        bu, bd = t.bottom_up(ou, od)
+        a = t.relax(bu, bd)
+        b = t.relax(bu, bd, threads=4)
+        for x, y in zip(a[:4], b[:4]):
+            assert np.array_equal(x, y)
