@@ -425,10 +425,13 @@ def run_customize(cch, steps, warmup, with_cpu):
         dev.append(inf["last_device_ms"])
         tot.append(inf["last_total_ms"])
     dev_ms, tot_ms = statistics.median(dev), statistics.median(tot)
-    T, E = info["triangles"], info["up_edges"] + info["down_edges"]
+    T, E, P = info["triangles"], info["up_edges"] + info["down_edges"], info["pairs"]
     exact = bool(np.array_equal(got[0], u["cust_up"])) and \
         bool(np.array_equal(got[1], u["cust_down"][order]))
-    algo = 12 * T + 28 * E  # index + target per triangle; seed, unpack per edge
+    # per pair candidate (two directed triangles): 4 B target index + 16 B
+    # target slot; per pair: 16 B slot written + 2 x 4 B edge ids + 2 x 8 B
+    # inputs; per edge: 4 B slot id + 8 B slot word + 8 B outputs
+    algo = 10 * T + 40 * P + 20 * E
     peak, peak_src = measured_peak()
     roof = {"bound": "hbm", "achieved": round(algo / (dev_ms / 1e3) / 1e9, 1), "peak": peak,
             "unit": "GB/s", "frac": round(algo / (dev_ms / 1e3) / 1e9 / peak, 3),
@@ -438,7 +441,7 @@ def run_customize(cch, steps, warmup, with_cpu):
                        % (info["n_nodes"], info["up_edges"], info["down_edges"], T),
            "metric": "customization time", "value": round(dev_ms, 3), "unit": "ms",
            "higher_is_better": False, "triangles_per_s": round(T / (dev_ms / 1e3), 1),
-           "levels": info["levels"], "plan_ms": round(info["plan_ms"], 1),
+           "levels": info["levels"], "pairs": P, "plan_ms": round(info["plan_ms"], 1),
            "target_index": info["target_index"], "steps": steps,
            "e2e": {"value": round(tot_ms, 3), "unit": "ms", "h2d_bytes_per_step": 4 * E,
                    "d2h_bytes_per_step": 16 * E},

@@ -130,7 +130,7 @@ class CchStats(ctypes.Structure):
                 ("up_edges", ctypes.c_uint64), ("down_edges", ctypes.c_uint64),
                 ("triangles", ctypes.c_uint64), ("bottom_up_shortcuts", ctypes.c_uint64),
                 ("apexes", ctypes.c_uint32), ("etree_levels", ctypes.c_uint32),
-                ("target_index", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("target_index", ctypes.c_uint32), ("pairs", ctypes.c_uint32),
                 ("plan_ms", ctypes.c_double), ("last_device_ms", ctypes.c_double),
                 ("last_total_ms", ctypes.c_double)]
 

@@ -431,12 +431,12 @@ typedef struct bf_cch_stats {
   uint32_t levels;                /* elimination-tree levels                        */
   uint64_t up_edges;
   uint64_t down_edges;
-  uint64_t triangles;             /* (DOWN x -> m, UP m -> y) pairs, x == y included */
+  uint64_t triangles;             /* x -> m -> y with x != y over the pair rows      */
   uint64_t bottom_up_shortcuts;
   uint32_t apexes;                /* nodes with at least one triangle               */
   uint32_t etree_levels;          /* 1: heights of the elimination tree, 0: longest path */
-  uint32_t target_index;          /* 1: target edges precomputed per triangle        */
-  uint32_t reserved;
+  uint32_t target_index;          /* 1: target slots precomputed per pair candidate  */
+  uint32_t pairs;                 /* unordered node pairs (one 16-byte slot each)     */
   double plan_ms;                 /* bf_cch_create                                  */
   double last_device_ms;          /* last call: device time without host copies     */
   double last_total_ms;           /* last call: wall time with host copies          */
