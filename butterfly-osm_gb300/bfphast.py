@@ -560,12 +560,19 @@ class Cch:
         _check(load().bf_cch_relax(self._h, _ptr(uw), _ptr(dw), _ptr(um), _ptr(dm)))
         return uw, dw, um, dm
 
-    def customize(self, orig_up, orig_down):
+    def customize(self, orig_up, orig_down, out=None):
         """bottom_up_customize + triangle_relax_parallel: returns
-        (up_w, down_w, up_mid, down_mid)."""
+        (up_w, down_w, up_mid, down_mid), written into `out` (four u32 arrays
+        of the UP, DOWN, UP, DOWN edge counts) when given."""
         ou, od = _u32(orig_up), _u32(orig_down)
-        uw, dw = np.empty(self.nu, np.uint32), np.empty(self.nd, np.uint32)
-        um, dm = np.empty(self.nu, np.uint32), np.empty(self.nd, np.uint32)
+        if out is None:
+            uw, dw = np.empty(self.nu, np.uint32), np.empty(self.nd, np.uint32)
+            um, dm = np.empty(self.nu, np.uint32), np.empty(self.nd, np.uint32)
+        else:
+            uw, dw, um, dm = out
+            for a, k in zip(out, (self.nu, self.nd, self.nu, self.nd)):
+                if a.dtype != np.uint32 or len(a) != k or not a.flags.c_contiguous:
+                    raise ValueError("out: four contiguous u32 arrays of the edge counts")
         _check(load().bf_cch_customize(self._h, _ptr(ou), _ptr(od), _ptr(uw), _ptr(dw), _ptr(um),
                                        _ptr(dm)))
         return uw, dw, um, dm
