@@ -44,7 +44,8 @@ def _nd_order(rows, cols):
 
 def grid_topology(rows, cols, seed, one_way=0.25, w_max=60, p_inf=0.05, order="nd",
                   diagonals=0.0):
-    """Returns (oracle.CchTopo with flags and middles, orig_up, orig_down)."""
+    """Returns (oracle.CchTopo with flags and middles, orig_up, orig_down);
+    the topology's `arcs` attribute holds the original arcs as a CSR."""
     rng = np.random.default_rng(seed)
     n = rows * cols
     pairs = []
@@ -105,4 +106,11 @@ def grid_topology(rows, cols, seed, one_way=0.25, w_max=60, p_inf=0.05, order="n
     uo, ut, us, um, ou = csr(up)
     do, dt, ds, dm, od = csr(dn)
     topo = orc.CchTopo(n, uo, ut, do, dt, up_short=us, down_short=ds, up_mid=um, down_mid=dm)
+    # the original arcs in rank space (finite weights), as a CSR for Dijkstra
+    fin = sorted((u, v, w) for (u, v), (w, m) in edges.items() if m == INF and w != INF)
+    arc_off = np.zeros(n + 1, np.uint64)
+    if fin:
+        arc_off[1:] = np.cumsum(np.bincount([u for u, _, _ in fin], minlength=n))
+    topo.arcs = {"n": n, "arc_off": arc_off, "arc_dst": np.array([v for _, v, _ in fin], np.uint32),
+                 "arc_w": np.array([w for _, _, w in fin], np.uint32)}
     return topo, ou, od

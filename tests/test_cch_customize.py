@@ -109,3 +109,15 @@ def test_parallel_relaxation_matches_sequential(built):
         b = t.relax(bu, bd, threads=4)
         for x, y in zip(a[:4], b[:4]):
             assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("seed,order", [(21, "nd"), (23, "random")])
+def test_customized_cch_answers_exact_distances(built, seed, order):
+    # after customization the CCH's PHAST matrix is the shortest-path matrix
+    # of the original directed arcs (plain Dijkstra)
+    t, ou, od = cchgen.grid_topology(10, 11, seed, order=order, one_way=0.3)
+    uw, dw, _, _, _ = t.relax(ou, od)
+    c = orc.Cch(t.n, t.up_off, t.up_tgt, uw, t.down_off, t.down_tgt, dw)
+    allr = np.arange(t.n, dtype=np.uint32)
+    m, _ = c.matrix(allr, allr)
+    assert np.array_equal(m, np.stack([orc.dijkstra_ebg(t.arcs, s) for s in range(t.n)]))

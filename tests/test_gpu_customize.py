@@ -157,3 +157,58 @@ def test_fixture_graphs(built):
         assert np.array_equal(uw, u["cust_up"]) and np.array_equal(dw, u["cust_down"][order])
         if kind == cchbuild.KIND_GRID:
             _eq((uw, dw, um, dm), d.relax(u["orig_up"], u["orig_down"][order])[:4])
+
+
+def _csr_weights(t, up_w, down_w):
+    return dict(n=t.n, up_off=t.up_off, up_tgt=t.up_tgt, up_w=up_w, down_off=t.down_off,
+                down_tgt=t.down_tgt, down_w=down_w)
+
+
+@pytest.mark.parametrize("seed,order", [(21, "nd"), (22, "random")])
+def test_customized_weights_answer_queries(built, seed, order):
+    # customize on the GPU, build the PHAST engine on the result, and compare
+    # the all-pairs matrix with plain Dijkstra on the original arcs
+    import bfphast
+    t, ou, od = cchgen.grid_topology(12, 13, seed, order=order, one_way=0.3)
+    uw, dw, _, _ = _gpu(t).customize(ou, od)
+    g = bfphast.Graph.from_cch(_csr_weights(t, uw, dw))
+    allr = np.arange(t.n, dtype=np.uint32)
+    got = g.matrix(allr, allr)
+    want = np.stack([orc.dijkstra_ebg(t.arcs, s) for s in range(t.n)])
+    assert np.array_equal(got, want)
+
+
+def test_two_channel_chain(built):
+    # time customization with the (time, length) middle election, then the
+    # length along the elected middles, then the 2-channel engine: every stage
+    # against the oracle's same chain, and the time channel against Dijkstra
+    import bfphast
+    t, ou, od = cchgen.grid_topology(11, 12, 31, w_max=4)  # many equal times
+    rng = np.random.default_rng(31)
+    # a physical length for every arc, also where the time is u32::MAX: a
+    # triangle can give such an arc a finite time, and as an original edge it
+    # keeps its own length
+    lu = rng.integers(1, 90, len(ou)).astype(np.uint32)
+    ld = rng.integers(1, 90, len(od)).astype(np.uint32)
+    g = _gpu(t)
+    bu, bd = g.bottom_up(ou, od)
+    lbu, lbd = g.bottom_up(lu, ld)
+    tu, td, mu, md = g.relax_lex(bu, bd, lbu, lbd, t.up_mid, t.down_mid)
+    wtu, wtd, wmu, wmd, _ = t.relax_lex(*t.bottom_up(ou, od), *t.bottom_up(lu, ld))
+    _eq((tu, td, mu, md), (wtu, wtd, wmu, wmd))
+    latu, latd = g.bottom_up(lu, ld, mu, md)
+    _eq((latu, latd), t.bottom_up(lu, ld, mu, md))
+    # the engine takes length weights only where the time weight is finite
+    latu = np.where(tu == INF, INF, latu).astype(np.uint32)
+    latd = np.where(td == INF, INF, latd).astype(np.uint32)
+    cch = _csr_weights(t, tu, td)
+    g2 = bfphast.Graph.from_cch(cch, up_len=latu, down_len=latd)
+    c = orc.Cch.from_dict(cch)
+    for origin in (0, t.n // 3, t.n - 1):
+        got = g2.phast_bounded_seeded_2ch([(origin, 0, 0)], INF)
+        want = c.bounded_seeded_2ch([(origin, 0, 0)], INF, latu, latd)
+        for a, b in zip(got, want):
+            assert np.array_equal(a, b)
+        dj = orc.dijkstra_ebg(t.arcs, origin)
+        rk, tm = got[0], got[1]
+        assert np.array_equal(tm, dj[rk])
