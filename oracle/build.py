@@ -1,7 +1,9 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles phast_oracle.cpp into oracle/_build/liboracle.so. Only tests/,
-__graft_entry__.smoke() and bench.py's CPU-baseline leg load it.
+Compiles phast_oracle.cpp and contour_oracle.cpp into
+oracle/_build/liboracle.so (no floating-point contraction, so every step
+rounds as written). Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg load it.
 """
 import pathlib
 import subprocess
@@ -12,11 +14,12 @@ OUT = HERE / "_build"
 
 def build_oracle():
     OUT.mkdir(exist_ok=True)
-    src = HERE / "phast_oracle.cpp"
+    srcs = [HERE / "phast_oracle.cpp", HERE / "contour_oracle.cpp"]
     so = OUT / "liboracle.so"
-    if not so.exists() or so.stat().st_mtime < src.stat().st_mtime:
-        r = subprocess.run(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", str(src),
-                            "-o", str(so)], capture_output=True, text=True)
+    if not so.exists() or any(so.stat().st_mtime < s.stat().st_mtime for s in srcs):
+        r = subprocess.run(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
+                            "-ffp-contract=off", *map(str, srcs), "-o", str(so)],
+                           capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
     return so

@@ -43,6 +43,21 @@ def load():
         lib.orc_phast_reverse.argtypes = csr + [ctypes.c_uint32, _V]
         lib.orc_cch_relax.argtypes = [ctypes.c_uint32] + [_V] * 8
         lib.orc_cch_relax.restype = ctypes.c_uint32
+        lib.orc_contour_cells.argtypes = [ctypes.c_uint64, _V, ctypes.c_int, ctypes.c_double,
+                                          ctypes.c_double, _V, ctypes.c_uint64]
+        lib.orc_contour_cells.restype = ctypes.c_uint64
+        lib.orc_sparse_contour.argtypes = [ctypes.c_uint32, _V, _V, ctypes.c_double, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                           ctypes.c_int32, ctypes.c_int32, _V, ctypes.c_uint64]
+        lib.orc_sparse_contour.restype = ctypes.c_uint64
+        lib.orc_contour_config.argtypes = [ctypes.c_int, ctypes.c_uint32] + [_V] * 4
+        lib.orc_mercator.argtypes = [ctypes.c_uint64] + [_V] * 4
+        lib.orc_inverse_mercator.argtypes = [ctypes.c_uint64] + [_V] * 4
+        lib.orc_isochrone_geometry.argtypes = [ctypes.c_uint64, _V, _V, ctypes.c_uint32,
+                                               ctypes.c_uint32, _V, _V, _V, ctypes.c_int,
+                                               ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                               _V, ctypes.c_uint64, _V, ctypes.c_uint64, _V, _V]
+        lib.orc_isochrone_geometry.restype = ctypes.c_uint64
         lib.orc_cch_relax_par.argtypes = [ctypes.c_uint32] + [_V] * 8 + [ctypes.c_int, _V]
         lib.orc_cch_relax_par.restype = ctypes.c_uint32
         lib.orc_cch_relax_lex.argtypes = [ctypes.c_uint32] + [_V] * 12
@@ -338,3 +353,96 @@ class CchTopo:
         if rc:
             raise IndexError("shortcut middle is not a rank")
         return uw, dw
+
+
+# ---------------------------------------------------------------------------
+# Isochrone geometry (server/geometry.rs:281-418, range/sparse_contour.rs)
+
+MODES = {"car": 0, "bike": 1, "foot": 2}
+
+
+def _ring(fn, cap=1 << 16):
+    """Calls fn(out, cap) -> n until the (x, y) ring fits."""
+    while True:
+        out = np.empty(2 * cap, np.float64)
+        n = fn(out.ctypes.data, cap)
+        if n <= cap:
+            return out[:2 * n].reshape(-1, 2)
+        cap = int(n)
+
+
+def contour_cells(cells, anchor=None):
+    """extract_contour_sparse on unit cells [(col, row), ...]: the ring of
+    cell-centre vertices, (x, y) rows."""
+    c = np.ascontiguousarray(np.asarray(cells, np.int32).reshape(-1, 2))
+    ax, ay = anchor if anchor is not None else (0.0, 0.0)
+    return _ring(lambda o, k: load().orc_contour_cells(len(c), c.ctypes.data,
+                                                       int(anchor is not None), ax, ay, o, k))
+
+
+def _segments(segments):
+    off = np.zeros(len(segments) + 1, np.uint64)
+    off[1:] = np.cumsum([len(s) for s in segments])
+    pts = np.ascontiguousarray(np.asarray([p for s in segments for p in s], np.int32).reshape(-1, 2))
+    return off, pts
+
+
+def sparse_contour(segments, cell_m, dilation, erosion, simplify_m, anchor=None):
+    """generate_sparse_contour_anchored: segments of (lat_e7, lon_e7) points;
+    the outer ring as (lon, lat) rows."""
+    if not segments:
+        return np.empty((0, 2))
+    off, pts = _segments(segments)
+    a_lat, a_lon = anchor if anchor is not None else (0, 0)
+    return _ring(lambda o, k: load().orc_sparse_contour(
+        len(segments), off.ctypes.data, pts.ctypes.data, cell_m, dilation, erosion, simplify_m,
+        int(anchor is not None), int(a_lat), int(a_lon), o, k))
+
+
+def contour_config(mode, threshold_s):
+    """SparseContourConfig::for_mode_name_with_threshold:
+    (cell_m, dilation_rounds, erosion_rounds, simplify_m)."""
+    c, s = ctypes.c_double(), ctypes.c_double()
+    d, e = ctypes.c_int(), ctypes.c_int()
+    load().orc_contour_config(MODES.get(mode, 0), int(threshold_s), ctypes.byref(c), ctypes.byref(d),
+                              ctypes.byref(e), ctypes.byref(s))
+    return c.value, d.value, e.value, s.value
+
+
+def mercator(lat, lon):
+    lat, lon = _a(np.atleast_1d(lat), np.float64), _a(np.atleast_1d(lon), np.float64)
+    x, y = np.empty(len(lat)), np.empty(len(lat))
+    load().orc_mercator(len(lat), lat.ctypes.data, lon.ctypes.data, x.ctypes.data, y.ctypes.data)
+    return x, y
+
+
+def inverse_mercator(x, y):
+    x, y = _a(np.atleast_1d(x), np.float64), _a(np.atleast_1d(y), np.float64)
+    lon, lat = np.empty(len(x)), np.empty(len(x))
+    load().orc_inverse_mercator(len(x), x.ctypes.data, y.ctypes.data, lon.ctypes.data,
+                                lat.ctypes.data)
+    return lon, lat
+
+
+def isochrone_geometry(nodes, dists, max_t, node_w, poly_off, poly, mode="car", origin=None):
+    """build_isochrone_geometry_sparse: settled (node, dist) pairs, per-node
+    weights and (lat_e7, lon_e7) polylines; returns (ring (lon, lat) rows,
+    closed cells (col, row) rows ascending by row then column, grid origin
+    (min_x, min_y) in Mercator metres)."""
+    nodes, dists = _a(nodes, np.uint32), _a(dists, np.uint32)
+    node_w, poly_off = _a(node_w, np.uint32), _a(poly_off, np.uint64)
+    poly = np.ascontiguousarray(np.asarray(poly, np.int32).reshape(-1, 2))
+    o_lon, o_lat = origin if origin is not None else (0.0, 0.0)
+    cap_c = 1 << 20
+    while True:
+        cells = np.empty(2 * cap_c, np.int32)
+        nc = ctypes.c_uint64(0)
+        grid = np.zeros(2)
+        ring = _ring(lambda o, k: load().orc_isochrone_geometry(
+            len(nodes), nodes.ctypes.data, dists.ctypes.data, int(max_t), len(node_w),
+            node_w.ctypes.data, poly_off.ctypes.data, poly.ctypes.data, MODES.get(mode, 0),
+            int(origin is not None), o_lon, o_lat, o, k, cells.ctypes.data, cap_c,
+            ctypes.byref(nc), grid.ctypes.data))
+        if nc.value <= cap_c:
+            return ring, cells[:2 * nc.value].reshape(-1, 2), grid
+        cap_c = int(nc.value)

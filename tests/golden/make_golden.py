@@ -21,6 +21,10 @@ reference_kats.json
         through external middle 0 or 1 (lengths 13 and 105), the packed
         (weight, middle) order, and the three (time, length) lexicographic
         middle elections
+      * route/src/range/sparse_contour.rs:1187-1672  isochrone contour:
+        cell-centre rings of a 3x3 block and an L-shape, anchored component
+        selection, the largest component without an anchor, and the
+        threshold tiers of SparseContourConfig
 
 grid100_matrix.npz
     The 100 x 100 matrix of the 100 x 100 synthetic grid computed by the CPU
@@ -82,7 +86,30 @@ def kats():
                  time=10, middle=0),
         ],
     }
+    block3 = [[c, r] for r in range(3) for c in range(3)]
+    strip = [[0, 0], [1, 0], [0, 1], [1, 1]] + [[c, r] for c in range(10, 40) for r in range(10, 13)]
+    contour = {
+        "source": "route/src/range/sparse_contour.rs:1187-1672",
+        # test_center_emission_square_block (:1453-1481): half-cell units
+        "block3": {"cells": block3, "ring_half_cells": [[1, 1], [3, 1], [5, 1], [5, 3], [5, 5],
+                                                        [3, 5], [1, 5], [1, 3]]},
+        # test_center_emission_l_shape_dedup (:1505-1528)
+        "l_shape": {"cells": [[0, 0], [1, 0], [0, 1]], "ring_half_cells": [[1, 1], [3, 1], [1, 3]]},
+        # anchored_extraction_prefers_origin_component (:1421-1451)
+        "anchored": {"cells": strip, "origin": [1.0, 1.0], "inside_big": [20.0, 11.5],
+                     "outside": [100.0, 100.0]},
+        # test_largest_component_wins (:1555-1576)
+        "largest": {"cells": [[c, r] for r in range(5) for c in range(5)]
+                    + [[300, 300], [301, 300], [300, 301], [301, 301]], "bbox": [0.0, 5.0]},
+        # test_adaptive_* (:1243-1380): (mode, threshold_s) -> cell and
+        # simplification multipliers of the mode's base config
+        "tiers": [["car", 300, 1.0, 1.0], ["car", 600, 1.0, 1.0], ["car", 601, 2.0, 2.0],
+                  ["car", 1800, 2.0, 2.0], ["car", 3600, 4.0, 4.0], ["car", 7200, 6.67, 8.0]],
+        "base": {"car": [30.0, 2, 2, 30.0], "bike": [40.0, 3, 3, 40.0], "foot": [25.0, 3, 3, 25.0],
+                 "truck": [30.0, 2, 2, 30.0]},
+    }
     return {
+        "sparse_contour": contour,
         "cch_customize": customize,
         "five_node": {
             "source": "route/src/range/phast.rs:1180-1250",
