@@ -135,6 +135,13 @@ class CchStats(ctypes.Structure):
                 ("last_total_ms", ctypes.c_double)]
 
 
+class Raster(ctypes.Structure):
+    _fields_ = [("col0", ctypes.c_int32), ("row0", ctypes.c_int32),
+                ("width_words", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("word_offset", ctypes.c_uint64), ("origin_x", ctypes.c_double),
+                ("origin_y", ctypes.c_double)]
+
+
 # Every symbol include/bf_phast.h declares, with its ctypes signature.
 _SIGNATURES = {
     "bf_graph_create": (ctypes.c_int, [ctypes.POINTER(CchCsr), ctypes.POINTER(Config),
@@ -202,6 +209,10 @@ _SIGNATURES = {
                                         _u32p]),
     "bf_cch_bottom_up": (ctypes.c_int, [ctypes.c_void_p, _u32p, _u32p, _u32p, _u32p, _u32p,
                                         _u32p]),
+    "bf_contour_rasters": (ctypes.c_int, [ctypes.c_void_p, _u64p, _u64p, ctypes.c_uint32,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                          ctypes.POINTER(Raster), _u64p, ctypes.c_uint64, _u64p]),
     "bf_last_error": (ctypes.c_char_p, []),
 }
 
@@ -596,3 +607,46 @@ class Cch:
                                        None if um is None else _ptr(um),
                                        None if dm is None else _ptr(dm), _ptr(uw), _ptr(dw)))
         return uw, dw
+
+
+def contour_rasters(isochrones, dilation, erosion, device=0):
+    """bf_contour_rasters for a list of isochrones, each a dict with
+    "segments" (list of (n, 2) float64 arrays of Mercator x, y), "cell_m" and
+    optionally "anchor" (x, y). Returns per isochrone (cells, origin): the
+    closed cells as (col, row) rows ascending by row then column, and the
+    grid origin (x, y)."""
+    lib = load()
+    pts, seg_pt, iso_seg = [], [0], [0]
+    for iso in isochrones:
+        for seg in iso["segments"]:
+            a = np.asarray(seg, np.float64).reshape(-1, 2)
+            pts.append(a)
+            seg_pt.append(seg_pt[-1] + len(a))
+        iso_seg.append(len(seg_pt) - 1)
+    xy = np.ascontiguousarray(np.concatenate(pts) if pts else np.zeros((0, 2)))
+    seg_pt = np.asarray(seg_pt, np.uint64)
+    iso_seg = np.asarray(iso_seg, np.uint64)
+    n = len(isochrones)
+    cell = np.asarray([i["cell_m"] for i in isochrones], np.float64)
+    has = np.asarray([i.get("anchor") is not None for i in isochrones], np.uint8)
+    anc = np.asarray([i.get("anchor") or (0.0, 0.0) for i in isochrones], np.float64).reshape(-1, 2)
+    ras = (Raster * max(n, 1))()
+    nw = ctypes.c_uint64(0)
+    args = [xy.ctypes.data, _ptr(seg_pt, _u64p), _ptr(iso_seg, _u64p), n, cell.ctypes.data,
+            has.ctypes.data, anc.ctypes.data, int(dilation), int(erosion), int(device), ras]
+    _check(lib.bf_contour_rasters(*args, None, 0, ctypes.byref(nw)))
+    words = np.zeros(max(int(nw.value), 1), np.uint64)
+    _check(lib.bf_contour_rasters(*args, _ptr(words, _u64p), int(nw.value), ctypes.byref(nw)))
+    out = []
+    for k in range(n):
+        r = ras[k]
+        if r.height == 0:
+            out.append((np.zeros((0, 2), np.int32), (r.origin_x, r.origin_y)))
+            continue
+        w = words[r.word_offset:r.word_offset + r.height * r.width_words].reshape(r.height,
+                                                                                   r.width_words)
+        bits = np.unpackbits(w.view(np.uint8).reshape(r.height, -1), axis=1, bitorder="little")
+        rr, cc = np.nonzero(bits)
+        cells = np.stack([cc + r.col0, rr + r.row0], axis=1).astype(np.int32)
+        out.append((cells, (r.origin_x, r.origin_y)))
+    return out

@@ -28,6 +28,7 @@
  *   bf_cch_customize       customize_cch_time_in_memory (weights)    route/src/customization.rs:571
  *   bf_cch_relax[_lex]     triangle_relax_parallel / _lex_parallel   customization.rs:1083, :1253
  *   bf_cch_bottom_up       bottom_up_customize / _with_external_middles  customization.rs:1005, :953
+ *   bf_contour_rasters     generate_sparse_contour_anchored, steps 1-3  route/src/range/sparse_contour.rs:650
  *
  * Conventions (as in the reference):
  *   - node ids are CCH ranks (rank-aligned CCH, node_id == rank);
@@ -481,6 +482,37 @@ bf_status bf_cch_relax_lex(bf_cch* c, uint32_t* up_t, uint32_t* down_t, const ui
 bf_status bf_cch_bottom_up(bf_cch* c, const uint32_t* orig_up, const uint32_t* orig_down,
                            const uint32_t* up_mid, const uint32_t* down_mid, uint32_t* up_w,
                            uint32_t* down_w);
+
+/* ---- isochrone contour rasters (range/sparse_contour.rs:650-770) ----------
+ * Steps 1-3 of the reference's contour pipeline for a batch of isochrones:
+ * stamp each isochrone's reachable segments (Bresenham between the cells of
+ * consecutive points, then every point, stamp_line :112-144), the anchor's
+ * 3x3 disk, then `dilation` 3x3 dilations and `erosion` 3x3 erosions.
+ * Points are Web-Mercator (x, y) metres as the reference's to_mercator gives
+ * them (:441-445; project once per static polyline vertex, with the libm the
+ * rest of the caller uses). Isochrone k owns segments [iso_seg[k],
+ * iso_seg[k + 1]), segment s owns points [seg_pt[s], seg_pt[s + 1]) of xy
+ * (x, y pairs); its grid origin is (min x - 3 cells, min y - 3 cells) over
+ * its points, cell size cell_m[k]; has_anchor / anchor_xy (x, y per
+ * isochrone) may be NULL. Cell (c, r) is set in isochrone k's raster iff
+ * the reference's closed tile map holds it: bit (c - col0) % 64 of word
+ * word_offset + (r - row0) * width_words + (c - col0) / 64.
+ * Rasters are described in `rasters` (n_iso entries) on every call; the
+ * words are written when `words` has room for *n_words (else only the
+ * layout is filled: call again with a larger buffer). */
+typedef struct bf_raster {
+  int32_t col0, row0;       /* grid cell of bit 0 of the raster's first word   */
+  uint32_t width_words;     /* 64-cell words per row                            */
+  uint32_t height;          /* rows                                              */
+  uint64_t word_offset;     /* first word of this raster in `words`              */
+  double origin_x, origin_y; /* grid origin in Mercator metres                   */
+} bf_raster;
+
+bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uint64_t* iso_seg,
+                             uint32_t n_iso, const double* cell_m, const uint8_t* has_anchor,
+                             const double* anchor_xy, uint32_t dilation, uint32_t erosion,
+                             int device, bf_raster* rasters, uint64_t* words, uint64_t cap_words,
+                             uint64_t* n_words);
 
 const char* bf_last_error(void);
 

@@ -457,6 +457,34 @@ uint64_t orc_sparse_contour(uint32_t n_seg, const uint64_t* off, const int32_t* 
   return emit(contour_of(cl, cfg), out, cap);
 }
 
+// Steps 1-3 of generate_sparse_contour_anchored only: the closed cell set of
+// the segments, (col, row) pairs ascending by row then column (up to
+// cell_cap), and the grid origin (min_x, min_y) in Mercator metres. Returns
+// the number of closed cells.
+uint64_t orc_sparse_closed(uint32_t n_seg, const uint64_t* off, const int32_t* pts,
+                           double cell_m, int dil, int ero, int has_anchor, int32_t a_lat,
+                           int32_t a_lon, int32_t* cells, uint64_t cell_cap,
+                           double* grid_origin) {
+  if (n_seg == 0) return 0;
+  const Config cfg{cell_m, dil, ero, 0.0};
+  const std::pair<int32_t, int32_t> a{a_lat, a_lon};
+  const Closed cl = stamp_and_close(read_segs(n_seg, off, pts), cfg, has_anchor ? &a : nullptr);
+  grid_origin[0] = cl.min_x;
+  grid_origin[1] = cl.min_y;
+  std::vector<std::pair<int32_t, int32_t>> set;
+  for (const auto& kv : cl.map.tiles)
+    for (int lr = 0; lr < TILE; ++lr)
+      for (int lc = 0; lc < TILE; ++lc)
+        if ((kv.second[lr] >> lc) & 1)
+          set.emplace_back(ty_of(kv.first) * TILE + lr, tx_of(kv.first) * TILE + lc);
+  std::sort(set.begin(), set.end());
+  for (uint64_t i = 0; i < set.size() && i < cell_cap; ++i) {
+    cells[2 * i] = set[i].second;
+    cells[2 * i + 1] = set[i].first;
+  }
+  return set.size();
+}
+
 // SparseContourConfig::for_mode_name_with_threshold: mode 0 car, 1 bike,
 // 2 foot (anything else: car).
 void orc_contour_config(int mode, uint32_t threshold_s, double* cell_m, int* dil, int* ero,

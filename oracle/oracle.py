@@ -50,6 +50,10 @@ def load():
                                            ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                            ctypes.c_int32, ctypes.c_int32, _V, ctypes.c_uint64]
         lib.orc_sparse_contour.restype = ctypes.c_uint64
+        lib.orc_sparse_closed.argtypes = [ctypes.c_uint32, _V, _V, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_int32,
+                                          ctypes.c_int32, _V, ctypes.c_uint64, _V]
+        lib.orc_sparse_closed.restype = ctypes.c_uint64
         lib.orc_contour_config.argtypes = [ctypes.c_int, ctypes.c_uint32] + [_V] * 4
         lib.orc_mercator.argtypes = [ctypes.c_uint64] + [_V] * 4
         lib.orc_inverse_mercator.argtypes = [ctypes.c_uint64] + [_V] * 4
@@ -446,3 +450,20 @@ def isochrone_geometry(nodes, dists, max_t, node_w, poly_off, poly, mode="car", 
         if nc.value <= cap_c:
             return ring, cells[:2 * nc.value].reshape(-1, 2), grid
         cap_c = int(nc.value)
+
+
+def sparse_closed(segments, cell_m, dilation, erosion, anchor=None):
+    """Stamped and closed cells of generate_sparse_contour_anchored's
+    segments: ((col, row) rows ascending by row then column, grid origin)."""
+    off, pts = _segments(segments)
+    a_lat, a_lon = anchor if anchor is not None else (0, 0)
+    cap = 1 << 20
+    while True:
+        cells = np.empty(2 * cap, np.int32)
+        grid = np.zeros(2)
+        n = load().orc_sparse_closed(len(segments), off.ctypes.data, pts.ctypes.data, cell_m,
+                                     dilation, erosion, int(anchor is not None), int(a_lat),
+                                     int(a_lon), cells.ctypes.data, cap, grid.ctypes.data)
+        if n <= cap:
+            return cells[:2 * n].reshape(-1, 2), grid
+        cap = int(n)

@@ -82,3 +82,32 @@ def test_cch_create_rejects_bad_topology(built):
         h = ctypes.c_void_p()
         assert lib.bf_cch_create(ctypes.byref(t), 0, ctypes.byref(h)) == bfphast.BF_ERR_INVALID
         assert not h.value
+
+
+def test_contour_layout_without_device(built):
+    # the layout pass of bf_contour_rasters runs on the host: grid origins
+    # are the oracle's (minimum corner less three cells) with no device call
+    import ctypes
+    import sys
+    import numpy as np
+    import bfphast
+    sys.path.insert(0, str(__import__("pathlib").Path(__file__).parent))
+    import contourgen
+    from oracle import oracle as orc
+    rng = np.random.default_rng(2)
+    segs, _ = contourgen.isochrone(rng, 50)
+    m = contourgen.mercator_segments(segs)
+    xy = np.ascontiguousarray(np.concatenate(m))
+    seg_pt = np.asarray([0] + list(np.cumsum([len(a) for a in m])), np.uint64)
+    iso_seg = np.asarray([0, len(m)], np.uint64)
+    cell = np.asarray([30.0])
+    ras = (bfphast.Raster * 1)()
+    nw = ctypes.c_uint64(0)
+    rc = bfphast.load().bf_contour_rasters(xy.ctypes.data, seg_pt.ctypes.data_as(bfphast._u64p),
+                                           iso_seg.ctypes.data_as(bfphast._u64p), 1,
+                                           cell.ctypes.data, None, None, 2, 2, 0, ras, None, 0,
+                                           ctypes.byref(nw))
+    assert rc == bfphast.BF_OK and nw.value > 0
+    _, grid = orc.sparse_closed(segs, 30.0, 2, 2)
+    assert (ras[0].origin_x, ras[0].origin_y) == tuple(grid)
+    assert ras[0].width_words * ras[0].height == nw.value
