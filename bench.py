@@ -62,6 +62,8 @@ def parse():
                     help="bulk isochrone origins (0 = skip)")
     ap.add_argument("--no-customize", action="store_true",
                     help="skip the CCH customization leg")
+    ap.add_argument("--contours", type=int, default=64,
+                    help="isochrone contour rasters in one batch (0 = skip)")
     return ap.parse_args()
 
 
@@ -127,8 +129,11 @@ class ClockSampler:
 def build_workload(args, seed):
     import cchbuild
     import workload
-    _, cch = cchbuild.build_synthetic(cchbuild.KIND_COUNTRY, args.rows, args.cols, seed=42,
+    e, cch = cchbuild.build_synthetic(cchbuild.KIND_COUNTRY, args.rows, args.cols, seed=42,
                                       with_topo=not getattr(args, "no_customize", True))
+    if getattr(args, "contours", 0):
+        cch["geo"] = {k: e[k] for k in ("n_intersections", "state_tail", "state_head",
+                                        "node_weight")}
     n = cch["n"]
     src, tgt = workload.sources_targets(n, args.sources, args.targets, seed=seed)
     return cch, src, tgt
@@ -279,6 +284,8 @@ def run_ours(args, rank, world, dist):
         res["isochrones"] = run_isochrones(g, cch, args.isochrones, seed=42 + rank)
     if args.serve_s > 0 and rank == 0:
         res["serving"] = run_serving(g, cch["n"], args.serve_s, args.serve_rate)
+    if args.contours > 0 and rank == 0:
+        res["contours"] = run_contours(g, cch, args.contours, args.cols)
     if not args.no_customize and rank == 0:
         res["customize"] = run_customize(cch, args.steps, args.warmup, not args.no_cpu)
     return res, cch, src, tgt, out_dev
@@ -397,6 +404,93 @@ def run_isochrones(g, cch, count, seed=42):
             "cpu_baseline": {"value": round(len(pick) / cpu_s, 2), "unit": "isochrones/s",
                              "cores": threads, "kind": "port",
                              "sample": "%d origins of the last chunk, %.1f s" % (len(pick), cpu_s)}}
+
+
+def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
+    """Isochrone contour rasters, steps 1-3 of the reference's contour
+    pipeline, for `count` origins in one bf_contour_rasters call: settled
+    sets from bf_phast_bounded_seeded, reachable road segments whole or cut
+    at the threshold as build_isochrone_geometry_sparse does (f32 cut
+    fraction), on synthetic lattice coordinates (about 100 m spacing, each
+    road a straight tail -> head polyline; intersections projected once, cut
+    points per query). Distances are deciseconds (the graph's unit); the
+    contour tier comes from the threshold in seconds. A sample of isochrones
+    is checked cell for cell against the oracle, which is timed as the CPU
+    baseline."""
+    import numpy as np
+    import bfphast
+    from oracle import oracle as orc
+    geo = cch.pop("geo")
+    tail, head, nw = geo["state_tail"], geo["state_head"], geo["node_weight"]
+    ii = np.arange(geo["n_intersections"], dtype=np.int64)
+    lat_e7 = (500_000_000 + (ii // cols) * 9000).astype(np.int64)
+    lon_e7 = (30_000_000 + (ii % cols) * 14000).astype(np.int64)
+    ix, iy = orc.mercator(lat_e7 / 1e7, lon_e7 / 1e7)
+    r2s = cch["rank_to_state"]
+    origins = np.random.default_rng(seed).integers(0, cch["n"], count)
+    threshold = 10 * threshold_s
+    cell, dil, ero, _ = orc.contour_config("car", threshold_s)
+    xy_parts, len_parts, iso_seg, anchors, e7 = [], [], [0], [], []
+    t_query = 0.0
+    for o in origins:
+        t0 = time.perf_counter()
+        rk, ds = g.phast_bounded_seeded([(int(o), 0)], threshold)
+        t_query += time.perf_counter() - t0
+        st = r2s[rk]
+        w = nw[st].astype(np.int64)
+        keep = (w != 0) & (w != 0xFFFFFFFF)
+        st, d, w = st[keep], ds[keep].astype(np.int64), w[keep]
+        a, b = tail[st], head[st]
+        i0 = int(np.argmin(d))  # first minimum in settled (rank) order
+        anchors.append((ix[a[i0]], iy[a[i0]]))
+        frac = (threshold - d).astype(np.float32) / w.astype(np.float32)
+        whole = (d + w <= threshold) | (frac >= np.float32(1.0))
+        cut = ~whole & (frac > np.float32(0.0))
+        clat = lat_e7[a[cut]] + np.trunc((lat_e7[b[cut]] - lat_e7[a[cut]]).astype(np.float32)
+                                         * frac[cut]).astype(np.int64)
+        clon = lon_e7[a[cut]] + np.trunc((lon_e7[b[cut]] - lon_e7[a[cut]]).astype(np.float32)
+                                         * frac[cut]).astype(np.int64)
+        cx, cy = orc.mercator(clat / 1e7, clon / 1e7)
+        wa, wb, ca = a[whole], b[whole], a[cut]
+        pts = np.empty((2 * (len(wa) + len(ca)), 2))
+        pts[0:2 * len(wa):2] = np.stack([ix[wa], iy[wa]], 1)
+        pts[1:2 * len(wa):2] = np.stack([ix[wb], iy[wb]], 1)
+        pts[2 * len(wa)::2] = np.stack([ix[ca], iy[ca]], 1)
+        pts[2 * len(wa) + 1::2] = np.stack([cx, cy], 1)
+        xy_parts.append(pts)
+        len_parts.append(np.full(len(wa) + len(ca), 2, np.uint64))
+        iso_seg.append(iso_seg[-1] + len(wa) + len(ca))
+        e7.append((lat_e7, lon_e7, wa, wb, ca, clat, clon, a[i0]))
+    xy = np.concatenate(xy_parts)
+    seg_pt = np.concatenate([[0], np.cumsum(np.concatenate(len_parts))]).astype(np.uint64)
+    bfphast.contour_rasters_flat(xy[:2], seg_pt[:2], [0, 1], [cell], dil, ero)  # warm-up
+    t0 = time.perf_counter()
+    ras, words = bfphast.contour_rasters_flat(xy, seg_pt, iso_seg, [cell] * count, dil, ero,
+                                              np.ones(count, np.uint8), np.asarray(anchors))
+    gpu_s = time.perf_counter() - t0
+    # oracle on a sample: the same segments in (lat_e7, lon_e7)
+    pick = [0, count // 2, count - 1][:count]
+    exact, cpu_s = True, 0.0
+    for k in pick:
+        la, lo, wa, wb, ca, clat, clon, a0 = e7[k]
+        segs = [[(int(la[p]), int(lo[p])), (int(la[q]), int(lo[q]))] for p, q in zip(wa, wb)]
+        segs += [[(int(la[p]), int(lo[p])), (int(y), int(x))] for p, y, x in zip(ca, clat, clon)]
+        t0 = time.perf_counter()
+        want, _ = orc.sparse_closed(segs, cell, dil, ero, (int(la[a0]), int(lo[a0])))
+        cpu_s += time.perf_counter() - t0
+        exact = exact and bool(np.array_equal(bfphast.raster_cells(ras[k], words), want))
+    n_seg = int(iso_seg[-1])
+    return {"isochrones": count, "threshold_s": threshold_s, "cell_m": cell,
+            "morphology": [dil, ero], "segments": n_seg,
+            "raster_words": int(len(words)), "value": round(count / gpu_s, 1),
+            "unit": "rasters/s", "ms": round(gpu_s * 1e3, 2),
+            "segments_per_s": round(n_seg / gpu_s, 1),
+            "settled_sets_ms": round(t_query * 1e3, 1),
+            "bit_exact_sample": {"isochrones": len(pick), "equal": exact},
+            "cpu_baseline": {"value": round(len(pick) / cpu_s, 3), "unit": "rasters/s",
+                             "cores": 1, "kind": "port",
+                             "sample": "%d isochrones of the batch, %.1f s" % (len(pick), cpu_s)},
+            "data": "synthetic lattice coordinates, straight tail -> head road polylines"}
 
 
 def run_customize(cch, steps, warmup, with_cpu):

@@ -212,7 +212,8 @@ _SIGNATURES = {
     "bf_contour_rasters": (ctypes.c_int, [ctypes.c_void_p, _u64p, _u64p, ctypes.c_uint32,
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
-                                          ctypes.POINTER(Raster), _u64p, ctypes.c_uint64, _u64p]),
+                                          ctypes.POINTER(Raster), ctypes.POINTER(_u64p), _u64p]),
+    "bf_contour_free": (None, [_u64p]),
     "bf_last_error": (ctypes.c_char_p, []),
 }
 
@@ -609,13 +610,53 @@ class Cch:
         return uw, dw
 
 
+def contour_rasters_flat(xy, seg_pt, iso_seg, cell_m, dilation, erosion, has_anchor=None,
+                         anchor_xy=None, device=0):
+    """bf_contour_rasters on flat arrays: xy (n, 2) Mercator points, seg_pt
+    (segments + 1) and iso_seg (isochrones + 1) offsets, cell_m per isochrone,
+    optional has_anchor (u8) and anchor_xy (isochrones, 2). Returns
+    (rasters, words)."""
+    lib = load()
+    xy = np.ascontiguousarray(xy, np.float64)
+    seg_pt = np.ascontiguousarray(seg_pt, np.uint64)
+    iso_seg = np.ascontiguousarray(iso_seg, np.uint64)
+    n = len(iso_seg) - 1
+    cell = np.ascontiguousarray(cell_m, np.float64)
+    has = None if has_anchor is None else np.ascontiguousarray(has_anchor, np.uint8)
+    anc = None if anchor_xy is None else np.ascontiguousarray(anchor_xy, np.float64)
+    ras = (Raster * max(n, 1))()
+    nw = ctypes.c_uint64(0)
+    out = _u64p()
+    _check(lib.bf_contour_rasters(xy.ctypes.data, _ptr(seg_pt, _u64p), _ptr(iso_seg, _u64p), n,
+                                  cell.ctypes.data, None if has is None else has.ctypes.data,
+                                  None if anc is None else anc.ctypes.data, int(dilation),
+                                  int(erosion), int(device), ras, ctypes.byref(out),
+                                  ctypes.byref(nw)))
+    try:
+        words = np.ctypeslib.as_array(out, shape=(max(int(nw.value), 1),)).copy() if nw.value \
+            else np.zeros(1, np.uint64)
+    finally:
+        lib.bf_contour_free(out)
+    return [ras[k] for k in range(n)], words
+
+
+def raster_cells(r, words):
+    """The set cells of one raster as (col, row) rows ascending by row, col."""
+    if r.height == 0:
+        return np.zeros((0, 2), np.int32)
+    w = words[r.word_offset:r.word_offset + r.height * r.width_words].reshape(r.height,
+                                                                               r.width_words)
+    bits = np.unpackbits(w.view(np.uint8).reshape(r.height, -1), axis=1, bitorder="little")
+    rr, cc = np.nonzero(bits)
+    return np.stack([cc + r.col0, rr + r.row0], axis=1).astype(np.int32)
+
+
 def contour_rasters(isochrones, dilation, erosion, device=0):
     """bf_contour_rasters for a list of isochrones, each a dict with
     "segments" (list of (n, 2) float64 arrays of Mercator x, y), "cell_m" and
     optionally "anchor" (x, y). Returns per isochrone (cells, origin): the
     closed cells as (col, row) rows ascending by row then column, and the
     grid origin (x, y)."""
-    lib = load()
     pts, seg_pt, iso_seg = [], [0], [0]
     for iso in isochrones:
         for seg in iso["segments"]:
@@ -623,30 +664,9 @@ def contour_rasters(isochrones, dilation, erosion, device=0):
             pts.append(a)
             seg_pt.append(seg_pt[-1] + len(a))
         iso_seg.append(len(seg_pt) - 1)
-    xy = np.ascontiguousarray(np.concatenate(pts) if pts else np.zeros((0, 2)))
-    seg_pt = np.asarray(seg_pt, np.uint64)
-    iso_seg = np.asarray(iso_seg, np.uint64)
-    n = len(isochrones)
-    cell = np.asarray([i["cell_m"] for i in isochrones], np.float64)
+    xy = np.concatenate(pts) if pts else np.zeros((0, 2))
     has = np.asarray([i.get("anchor") is not None for i in isochrones], np.uint8)
     anc = np.asarray([i.get("anchor") or (0.0, 0.0) for i in isochrones], np.float64).reshape(-1, 2)
-    ras = (Raster * max(n, 1))()
-    nw = ctypes.c_uint64(0)
-    args = [xy.ctypes.data, _ptr(seg_pt, _u64p), _ptr(iso_seg, _u64p), n, cell.ctypes.data,
-            has.ctypes.data, anc.ctypes.data, int(dilation), int(erosion), int(device), ras]
-    _check(lib.bf_contour_rasters(*args, None, 0, ctypes.byref(nw)))
-    words = np.zeros(max(int(nw.value), 1), np.uint64)
-    _check(lib.bf_contour_rasters(*args, _ptr(words, _u64p), int(nw.value), ctypes.byref(nw)))
-    out = []
-    for k in range(n):
-        r = ras[k]
-        if r.height == 0:
-            out.append((np.zeros((0, 2), np.int32), (r.origin_x, r.origin_y)))
-            continue
-        w = words[r.word_offset:r.word_offset + r.height * r.width_words].reshape(r.height,
-                                                                                   r.width_words)
-        bits = np.unpackbits(w.view(np.uint8).reshape(r.height, -1), axis=1, bitorder="little")
-        rr, cc = np.nonzero(bits)
-        cells = np.stack([cc + r.col0, rr + r.row0], axis=1).astype(np.int32)
-        out.append((cells, (r.origin_x, r.origin_y)))
-    return out
+    ras, words = contour_rasters_flat(xy, seg_pt, iso_seg, [i["cell_m"] for i in isochrones],
+                                      dilation, erosion, has, anc, device)
+    return [(raster_cells(r, words), (r.origin_x, r.origin_y)) for r in ras]

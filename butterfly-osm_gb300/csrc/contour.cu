@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
+#include <cstdlib>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -138,6 +140,106 @@ __global__ void k_morph(uint32_t n_iso, const IsoDev* __restrict__ iso, uint64_t
   }
 }
 
+// Per isochrone (one block each): the minimum point corner, then the grid
+// origin (minimum less three cells, as the reference) and the extreme cells
+// of its points and anchor disk; also tags every segment with its isochrone.
+struct Extent {
+  double ox, oy;
+  int32_t c0, r0, c1, r1;
+  uint32_t has_points, pad;
+};
+
+__device__ __forceinline__ double block_min(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : INFINITY;
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    if (threadIdx.x == 0) red[0] = v;
+  }
+  __syncthreads();
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ int block_minmax_i(int v, bool is_max, int* red) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const int w = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    v = is_max ? max(v, w) : min(v, w);
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : (is_max ? INT_MIN : INT_MAX);
+    for (int o = 16; o > 0; o >>= 1) {
+      const int w = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+      v = is_max ? max(v, w) : min(v, w);
+    }
+    if (threadIdx.x == 0) red[0] = v;
+  }
+  __syncthreads();
+  const int r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(256) k_extent(const double2* __restrict__ xy,
+                                                const uint64_t* __restrict__ seg_pt,
+                                                const uint64_t* __restrict__ iso_seg,
+                                                const double* __restrict__ cell_m,
+                                                const uint8_t* __restrict__ has_anchor,
+                                                const double2* __restrict__ anchor,
+                                                uint32_t* __restrict__ seg_iso,
+                                                Extent* __restrict__ ext) {
+  __shared__ double dred[8];
+  __shared__ int ired[8];
+  const uint32_t k = blockIdx.x;
+  const uint64_t s0 = iso_seg[k], s1 = iso_seg[k + 1];
+  for (uint64_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) seg_iso[s] = k;
+  const uint64_t p0 = seg_pt[s0], p1 = seg_pt[s1];
+  double mx = INFINITY, my = INFINITY;
+  for (uint64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+    mx = fmin(mx, xy[p].x);
+    my = fmin(my, xy[p].y);
+  }
+  mx = block_min(mx, dred);
+  my = block_min(my, dred);
+  Extent e{};
+  if (p1 == p0) {
+    if (threadIdx.x == 0) ext[k] = e;
+    return;
+  }
+  const double cell = cell_m[k];
+  IsoDev g{};
+  g.ox = __dsub_rn(mx, __dmul_rn(cell, 3.0));
+  g.oy = __dsub_rn(my, __dmul_rn(cell, 3.0));
+  g.cell = cell;
+  int c0 = INT_MAX, r0 = INT_MAX, c1 = INT_MIN, r1 = INT_MIN;
+  for (uint64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+    int32_t c, r;
+    cell_of(g, xy[p].x, xy[p].y, &c, &r);
+    c0 = min(c0, c);
+    r0 = min(r0, r);
+    c1 = max(c1, c);
+    r1 = max(r1, r);
+  }
+  if (threadIdx.x == 0 && has_anchor && has_anchor[k]) {
+    int32_t c, r;
+    cell_of(g, anchor[k].x, anchor[k].y, &c, &r);
+    c0 = min(c0, c - 1);
+    r0 = min(r0, r - 1);
+    c1 = max(c1, c + 1);
+    r1 = max(r1, r + 1);
+  }
+  c0 = block_minmax_i(c0, false, ired);
+  r0 = block_minmax_i(r0, false, ired);
+  c1 = block_minmax_i(c1, true, ired);
+  r1 = block_minmax_i(r1, true, ired);
+  if (threadIdx.x == 0) ext[k] = Extent{g.ox, g.oy, c0, r0, c1, r1, 1u, 0u};
+}
+
 unsigned grid_of(uint64_t n) {
   return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 152ull * 16));
 }
@@ -206,6 +308,42 @@ bool layout(const double* xy, const uint64_t* seg_pt, const uint64_t* iso_seg, u
   return true;
 }
 
+// Raster layout from the per-isochrone extents: one more cell than the
+// dilations can grow on every side; word offsets in isochrone order.
+bool place(uint32_t n_iso, const Extent* ext, const double* cell_m, uint32_t dilation,
+           bf_raster* ras, std::vector<IsoDev>& dev, uint64_t* total) {
+  uint64_t woff = 0;
+  dev.assign(n_iso, IsoDev{});
+  for (uint32_t k = 0; k < n_iso; ++k) {
+    bf_raster& R = ras[k];
+    R = bf_raster{};
+    IsoDev& g = dev[k];
+    g.woff = woff;
+    R.word_offset = woff;
+    if (!ext[k].has_points) continue;
+    const int64_t grow = (int64_t)dilation + 1;
+    const int64_t c0 = (int64_t)ext[k].c0 - grow, r0 = (int64_t)ext[k].r0 - grow;
+    const int64_t c1 = (int64_t)ext[k].c1 + grow, r1 = (int64_t)ext[k].r1 + grow;
+    if (c0 < INT32_MIN || r0 < INT32_MIN || c1 > INT32_MAX || r1 > INT32_MAX) return false;
+    g.ox = ext[k].ox;
+    g.oy = ext[k].oy;
+    g.cell = cell_m[k];
+    g.col0 = (int32_t)c0;
+    g.row0 = (int32_t)r0;
+    g.wpr = (uint32_t)((c1 - c0 + 1 + 63) / 64);
+    g.height = (uint32_t)(r1 - r0 + 1);
+    R.col0 = g.col0;
+    R.row0 = g.row0;
+    R.width_words = g.wpr;
+    R.height = g.height;
+    R.origin_x = g.ox;
+    R.origin_y = g.oy;
+    woff += (uint64_t)g.wpr * g.height;
+  }
+  *total = woff;
+  return true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -213,10 +351,10 @@ extern "C" {
 bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uint64_t* iso_seg,
                              uint32_t n_iso, const double* cell_m, const uint8_t* has_anchor,
                              const double* anchor_xy, uint32_t dilation, uint32_t erosion,
-                             int device, bf_raster* rasters, uint64_t* words, uint64_t cap_words,
+                             int device, bf_raster* rasters, uint64_t** words,
                              uint64_t* n_words) {
-  if (!seg_pt || !iso_seg || !cell_m || !rasters || !n_words || (n_iso && !xy) ||
-      (has_anchor && !anchor_xy)) {
+  if (words) *words = nullptr;
+  if (!seg_pt || !iso_seg || !cell_m || !rasters || !n_words || (has_anchor && !anchor_xy)) {
     set_error("bf_contour_rasters: null argument");
     return BF_ERR_INVALID;
   }
@@ -231,99 +369,133 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
       set_error("bf_contour_rasters: seg_pt must be non-decreasing");
       return BF_ERR_INVALID;
     }
-  std::vector<IsoDev> iso;
-  uint64_t total = 0;
-  if (!layout(xy, seg_pt, iso_seg, n_iso, cell_m, has_anchor, anchor_xy, dilation, rasters, iso,
-              &total)) {
-    set_error("bf_contour_rasters: a raster extends beyond 32-bit cell coordinates");
+  const uint64_t n_pts = seg_pt[n_seg];
+  if (n_pts && !xy) {
+    set_error("bf_contour_rasters: null points");
     return BF_ERR_INVALID;
   }
-  *n_words = total;
-  if (!words || cap_words < total || total == 0) {
-    if (words && total) std::fill(words, words + std::min(cap_words, total), 0ull);
-    return BF_OK;  // layout only: call again with room for *n_words words
+  std::vector<IsoDev> iso;
+  uint64_t total = 0;
+  if (!words) {  // layout only, on the host
+    if (!layout(xy, seg_pt, iso_seg, n_iso, cell_m, has_anchor, anchor_xy, dilation, rasters, iso,
+                &total)) {
+      set_error("bf_contour_rasters: a raster extends beyond 32-bit cell coordinates");
+      return BF_ERR_INVALID;
+    }
+    *n_words = total;
+    return BF_OK;
   }
   if (cudaSetDevice(device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
-  const uint64_t n_pts = seg_pt[n_seg];
-  std::vector<uint32_t> seg_iso(n_seg);
-  for (uint32_t k = 0; k < n_iso; ++k)
-    for (uint64_t s = iso_seg[k]; s < iso_seg[k + 1]; ++s) seg_iso[s] = k;
   cudaStream_t st = nullptr;
   BF_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  void* buf[8] = {};
-  auto cleanup = [&]() {
-    for (void* p : buf)
-      if (p) cudaFree(p);
-    cudaStreamDestroy(st);
-  };
-  double2* d_xy = nullptr;
-  uint64_t* d_seg = nullptr;
-  uint32_t *d_siso = nullptr, *d_err = nullptr;
-  IsoDev* d_iso = nullptr;
-  uint8_t* d_has = nullptr;
-  double2* d_anchor = nullptr;
-  unsigned long long *d_a = nullptr, *d_b = nullptr;
+  std::vector<void*> bufs;
   cudaError_t e = cudaSuccess;
-  auto alloc = [&](void** p, size_t bytes, int slot) {
-    if (e == cudaSuccess) e = cudaMalloc(p, std::max<size_t>(bytes, 16));
-    if (e == cudaSuccess) buf[slot] = *p;
+  auto alloc = [&](auto** p, size_t bytes) {
+    if (e != cudaSuccess) return;
+    e = cudaMalloc((void**)p, std::max<size_t>(bytes, 16));
+    if (e == cudaSuccess) bufs.push_back(*p);
   };
-  alloc((void**)&d_xy, n_pts * sizeof(double2), 0);
-  alloc((void**)&d_seg, (n_seg + 1) * 8, 1);
-  alloc((void**)&d_siso, n_seg * 4 + 4, 2);
-  alloc((void**)&d_iso, n_iso * sizeof(IsoDev), 3);
-  alloc((void**)&d_a, total * 8, 4);
-  alloc((void**)&d_b, total * 8, 5);
-  alloc((void**)&d_err, 4, 6);
+  auto done = [&](bf_status rc) {
+    for (void* p : bufs) cudaFree(p);
+    cudaStreamDestroy(st);
+    return rc;
+  };
+  double2 *d_xy = nullptr, *d_anchor = nullptr;
+  uint64_t *d_seg = nullptr, *d_iseg = nullptr;
+  uint32_t *d_siso = nullptr, *d_err = nullptr;
+  double* d_cell = nullptr;
+  uint8_t* d_has = nullptr;
+  Extent* d_ext = nullptr;
+  IsoDev* d_iso = nullptr;
+  alloc(&d_xy, n_pts * sizeof(double2));
+  alloc(&d_seg, (n_seg + 1) * 8);
+  alloc(&d_iseg, ((uint64_t)n_iso + 1) * 8);
+  alloc(&d_siso, n_seg * 4);
+  alloc(&d_cell, (uint64_t)n_iso * 8);
+  alloc(&d_ext, (uint64_t)n_iso * sizeof(Extent));
+  alloc(&d_iso, (uint64_t)n_iso * sizeof(IsoDev));
+  alloc(&d_err, 4);
   if (has_anchor) {
-    alloc((void**)&d_has, n_iso, 7);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&d_anchor, std::max<size_t>(n_iso * 16, 16));
+    alloc(&d_has, n_iso);
+    alloc(&d_anchor, (uint64_t)n_iso * 16);
   }
-  if (e != cudaSuccess) {
-    if (d_anchor) cudaFree(d_anchor);
-    cleanup();
-    return cuda_status(e, "bf_contour_rasters: device memory");
-  }
-  auto run = [&]() -> cudaError_t {
+  if (e != cudaSuccess) return done(cuda_status(e, "bf_contour_rasters: device memory"));
+  std::vector<Extent> ext(n_iso);
+  auto stage1 = [&]() -> cudaError_t {
     cudaError_t r;
-    if ((r = cudaMemcpyAsync(d_xy, xy, n_pts * 16, cudaMemcpyHostToDevice, st))) return r;
+    if (n_pts && (r = cudaMemcpyAsync(d_xy, xy, n_pts * 16, cudaMemcpyHostToDevice, st))) return r;
     if ((r = cudaMemcpyAsync(d_seg, seg_pt, (n_seg + 1) * 8, cudaMemcpyHostToDevice, st))) return r;
-    if (n_seg && (r = cudaMemcpyAsync(d_siso, seg_iso.data(), n_seg * 4, cudaMemcpyHostToDevice, st)))
+    if ((r = cudaMemcpyAsync(d_iseg, iso_seg, ((uint64_t)n_iso + 1) * 8, cudaMemcpyHostToDevice, st)))
       return r;
-    if ((r = cudaMemcpyAsync(d_iso, iso.data(), n_iso * sizeof(IsoDev), cudaMemcpyHostToDevice, st)))
+    if (n_iso && (r = cudaMemcpyAsync(d_cell, cell_m, (uint64_t)n_iso * 8, cudaMemcpyHostToDevice, st)))
       return r;
-    if ((r = cudaMemsetAsync(d_a, 0, total * 8, st))) return r;
+    if (has_anchor && n_iso) {
+      if ((r = cudaMemcpyAsync(d_has, has_anchor, n_iso, cudaMemcpyHostToDevice, st))) return r;
+      if ((r = cudaMemcpyAsync(d_anchor, anchor_xy, (uint64_t)n_iso * 16, cudaMemcpyHostToDevice, st)))
+        return r;
+    }
+    if (n_iso)
+      k_extent<<<n_iso, 256, 0, st>>>(d_xy, d_seg, d_iseg, d_cell, d_has, d_anchor, d_siso, d_ext);
+    if ((r = cudaGetLastError())) return r;
+    if (n_iso && (r = cudaMemcpyAsync(ext.data(), d_ext, (uint64_t)n_iso * sizeof(Extent),
+                                      cudaMemcpyDeviceToHost, st)))
+      return r;
+    return cudaStreamSynchronize(st);
+  };
+  if ((e = stage1()) != cudaSuccess) return done(cuda_status(e, "bf_contour_rasters: extents"));
+  if (!place(n_iso, ext.data(), cell_m, dilation, rasters, iso, &total)) {
+    set_error("bf_contour_rasters: a raster extends beyond 32-bit cell coordinates");
+    return done(BF_ERR_INVALID);
+  }
+  *n_words = total;
+  uint64_t* h_words = (uint64_t*)std::malloc(std::max<uint64_t>(total, 1) * 8);
+  if (!h_words) {
+    set_error("out of host memory");
+    return done(BF_ERR_OOM);
+  }
+  unsigned long long *d_a = nullptr, *d_b = nullptr;
+  alloc(&d_a, total * 8);
+  alloc(&d_b, total * 8);
+  if (e != cudaSuccess) {
+    std::free(h_words);
+    return done(cuda_status(e, "bf_contour_rasters: raster memory"));
+  }
+  auto stage2 = [&]() -> cudaError_t {
+    cudaError_t r;
+    if (n_iso && (r = cudaMemcpyAsync(d_iso, iso.data(), (uint64_t)n_iso * sizeof(IsoDev),
+                                      cudaMemcpyHostToDevice, st)))
+      return r;
+    if ((r = cudaMemsetAsync(d_a, 0, std::max<uint64_t>(total, 1) * 8, st))) return r;
     if ((r = cudaMemsetAsync(d_err, 0, 4, st))) return r;
     if (n_seg) k_stamp<<<grid_of(n_seg), 256, 0, st>>>(n_seg, d_xy, d_seg, d_siso, d_iso, d_a, d_err);
-    if (has_anchor) {
-      if ((r = cudaMemcpyAsync(d_has, has_anchor, n_iso, cudaMemcpyHostToDevice, st))) return r;
-      if ((r = cudaMemcpyAsync(d_anchor, anchor_xy, n_iso * 16, cudaMemcpyHostToDevice, st))) return r;
+    if (has_anchor && n_iso)
       k_anchor<<<(n_iso + 127) / 128, 128, 0, st>>>(n_iso, d_iso, d_has, d_anchor, d_a, d_err);
-    }
     unsigned long long *cur = d_a, *nxt = d_b;
-    for (uint32_t i = 0; i < dilation; ++i) {
+    for (uint32_t i = 0; i < dilation && total; ++i) {
       k_morph<true><<<grid_of(total), 256, 0, st>>>(n_iso, d_iso, total, cur, nxt);
       std::swap(cur, nxt);
     }
-    for (uint32_t i = 0; i < erosion; ++i) {
+    for (uint32_t i = 0; i < erosion && total; ++i) {
       k_morph<false><<<grid_of(total), 256, 0, st>>>(n_iso, d_iso, total, cur, nxt);
       std::swap(cur, nxt);
     }
     if ((r = cudaGetLastError())) return r;
-    if ((r = cudaMemcpyAsync(words, cur, total * 8, cudaMemcpyDeviceToHost, st))) return r;
+    if (total && (r = cudaMemcpyAsync(h_words, cur, total * 8, cudaMemcpyDeviceToHost, st))) return r;
     return cudaStreamSynchronize(st);
   };
-  e = run();
+  e = stage2();
   uint32_t err = 0;
   if (e == cudaSuccess) e = cudaMemcpy(&err, d_err, 4, cudaMemcpyDeviceToHost);
-  if (d_anchor) cudaFree(d_anchor);
-  cleanup();
-  if (e != cudaSuccess) return cuda_status(e, "bf_contour_rasters");
-  if (err) {
+  if (e != cudaSuccess || err) {
+    std::free(h_words);
+    if (e != cudaSuccess) return done(cuda_status(e, "bf_contour_rasters"));
     set_error("bf_contour_rasters: a stamped cell fell outside its raster");
-    return BF_ERR_DEVICE;
+    return done(BF_ERR_DEVICE);
   }
-  return BF_OK;
+  *words = h_words;
+  return done(BF_OK);
 }
+
+void bf_contour_free(uint64_t* words) { std::free(words); }
 
 }  // extern "C"

@@ -497,9 +497,9 @@ bf_status bf_cch_bottom_up(bf_cch* c, const uint32_t* orig_up, const uint32_t* o
  * isochrone) may be NULL. Cell (c, r) is set in isochrone k's raster iff
  * the reference's closed tile map holds it: bit (c - col0) % 64 of word
  * word_offset + (r - row0) * width_words + (c - col0) / 64.
- * Rasters are described in `rasters` (n_iso entries) on every call; the
- * words are written when `words` has room for *n_words (else only the
- * layout is filled: call again with a larger buffer). */
+ * Rasters are described in `rasters` (n_iso entries); *words receives a
+ * buffer of *n_words words that the caller releases with bf_contour_free.
+ * With words == NULL only the layout is computed, on the host. */
 typedef struct bf_raster {
   int32_t col0, row0;       /* grid cell of bit 0 of the raster's first word   */
   uint32_t width_words;     /* 64-cell words per row                            */
@@ -511,8 +511,8 @@ typedef struct bf_raster {
 bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uint64_t* iso_seg,
                              uint32_t n_iso, const double* cell_m, const uint8_t* has_anchor,
                              const double* anchor_xy, uint32_t dilation, uint32_t erosion,
-                             int device, bf_raster* rasters, uint64_t* words, uint64_t cap_words,
-                             uint64_t* n_words);
+                             int device, bf_raster* rasters, uint64_t** words, uint64_t* n_words);
+void bf_contour_free(uint64_t* words);
 
 const char* bf_last_error(void);
 

@@ -105,7 +105,7 @@ def test_contour_layout_without_device(built):
     nw = ctypes.c_uint64(0)
     rc = bfphast.load().bf_contour_rasters(xy.ctypes.data, seg_pt.ctypes.data_as(bfphast._u64p),
                                            iso_seg.ctypes.data_as(bfphast._u64p), 1,
-                                           cell.ctypes.data, None, None, 2, 2, 0, ras, None, 0,
+                                           cell.ctypes.data, None, None, 2, 2, 0, ras, None,
                                            ctypes.byref(nw))
     assert rc == bfphast.BF_OK and nw.value > 0
     _, grid = orc.sparse_closed(segs, 30.0, 2, 2)
