@@ -407,8 +407,9 @@ def run_isochrones(g, cch, count, seed=42):
 
 
 def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
-    """Isochrone contour rasters, steps 1-3 of the reference's contour
-    pipeline, for `count` origins in one bf_contour_rasters call: settled
+    """Isochrone polygons for `count` origins: the contour rasters (steps
+    1-3 of the reference's contour pipeline) in one bf_contour_rasters call,
+    then tracing and simplification in one bf_contour_polygons call: settled
     sets from bf_phast_bounded_seeded, reachable road segments whole or cut
     at the threshold as build_isochrone_geometry_sparse does (f32 cut
     fraction), on synthetic lattice coordinates (about 100 m spacing, each
@@ -429,7 +430,7 @@ def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
     r2s = cch["rank_to_state"]
     origins = np.random.default_rng(seed).integers(0, cch["n"], count)
     threshold = 10 * threshold_s
-    cell, dil, ero, _ = orc.contour_config("car", threshold_s)
+    cell, dil, ero, simp = orc.contour_config("car", threshold_s)
     xy_parts, len_parts, iso_seg, anchors, e7 = [], [], [0], [], []
     t_query = 0.0
     for o in origins:
@@ -464,10 +465,14 @@ def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
     xy = np.concatenate(xy_parts)
     seg_pt = np.concatenate([[0], np.cumsum(np.concatenate(len_parts))]).astype(np.uint64)
     bfphast.contour_rasters_flat(xy[:2], seg_pt[:2], [0, 1], [cell], dil, ero)  # warm-up
+    has, anc = np.ones(count, np.uint8), np.asarray(anchors)
     t0 = time.perf_counter()
     ras, words = bfphast.contour_rasters_flat(xy, seg_pt, iso_seg, [cell] * count, dil, ero,
-                                              np.ones(count, np.uint8), np.asarray(anchors))
+                                              has, anc)
     gpu_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    rings = bfphast.contour_polygons(ras, words, [cell] * count, [simp] * count, has, anc)
+    poly_s = time.perf_counter() - t0
     # oracle on a sample: the same segments in (lat_e7, lon_e7)
     pick = [0, count // 2, count - 1][:count]
     exact, cpu_s = True, 0.0
@@ -475,19 +480,23 @@ def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
         la, lo, wa, wb, ca, clat, clon, a0 = e7[k]
         segs = [[(int(la[p]), int(lo[p])), (int(la[q]), int(lo[q]))] for p, q in zip(wa, wb)]
         segs += [[(int(la[p]), int(lo[p])), (int(y), int(x))] for p, y, x in zip(ca, clat, clon)]
-        t0 = time.perf_counter()
         want, _ = orc.sparse_closed(segs, cell, dil, ero, (int(la[a0]), int(lo[a0])))
-        cpu_s += time.perf_counter() - t0
         exact = exact and bool(np.array_equal(bfphast.raster_cells(ras[k], words), want))
+        t0 = time.perf_counter()
+        ring = orc.sparse_contour(segs, cell, dil, ero, simp, (int(la[a0]), int(lo[a0])))
+        cpu_s += time.perf_counter() - t0
+        exact = exact and bool(np.array_equal(rings[k], ring))
     n_seg = int(iso_seg[-1])
     return {"isochrones": count, "threshold_s": threshold_s, "cell_m": cell,
             "morphology": [dil, ero], "segments": n_seg,
-            "raster_words": int(len(words)), "value": round(count / gpu_s, 1),
-            "unit": "rasters/s", "ms": round(gpu_s * 1e3, 2),
+            "raster_words": int(len(words)), "value": round(count / (gpu_s + poly_s), 1),
+            "unit": "polygons/s", "ms": round((gpu_s + poly_s) * 1e3, 2),
+            "rasters_ms": round(gpu_s * 1e3, 2), "polygons_ms": round(poly_s * 1e3, 2),
             "segments_per_s": round(n_seg / gpu_s, 1),
+            "mean_ring_vertices": round(float(np.mean([len(r) for r in rings])), 1),
             "settled_sets_ms": round(t_query * 1e3, 1),
             "bit_exact_sample": {"isochrones": len(pick), "equal": exact},
-            "cpu_baseline": {"value": round(len(pick) / cpu_s, 3), "unit": "rasters/s",
+            "cpu_baseline": {"value": round(len(pick) / cpu_s, 3), "unit": "polygons/s",
                              "cores": 1, "kind": "port",
                              "sample": "%d isochrones of the batch, %.1f s" % (len(pick), cpu_s)},
             "data": "synthetic lattice coordinates, straight tail -> head road polylines"}

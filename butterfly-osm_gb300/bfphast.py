@@ -214,6 +214,11 @@ _SIGNATURES = {
                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                                           ctypes.POINTER(Raster), ctypes.POINTER(_u64p), _u64p]),
     "bf_contour_free": (None, [_u64p]),
+    "bf_contour_polygons": (ctypes.c_int, [ctypes.POINTER(Raster), _u64p, ctypes.c_uint32,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, _u64p,
+                                           ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]),
+    "bf_contour_free_polygons": (None, [ctypes.POINTER(ctypes.c_double)]),
     "bf_last_error": (ctypes.c_char_p, []),
 }
 
@@ -670,3 +675,28 @@ def contour_rasters(isochrones, dilation, erosion, device=0):
     ras, words = contour_rasters_flat(xy, seg_pt, iso_seg, [i["cell_m"] for i in isochrones],
                                       dilation, erosion, has, anc, device)
     return [(raster_cells(r, words), (r.origin_x, r.origin_y)) for r in ras]
+
+
+def contour_polygons(rasters, words, cell_m, simplify_m, has_anchor=None, anchor_xy=None):
+    """bf_contour_polygons on the output of contour_rasters_flat: one
+    (lon, lat) ring per isochrone."""
+    lib = load()
+    n = len(rasters)
+    ras = (Raster * max(n, 1))(*rasters)
+    words = np.ascontiguousarray(words, np.uint64)
+    cell = np.ascontiguousarray(cell_m, np.float64)
+    simp = np.ascontiguousarray(simplify_m, np.float64)
+    has = None if has_anchor is None else np.ascontiguousarray(has_anchor, np.uint8)
+    anc = None if anchor_xy is None else np.ascontiguousarray(anchor_xy, np.float64)
+    off = np.zeros(n + 1, np.uint64)
+    out = ctypes.POINTER(ctypes.c_double)()
+    _check(lib.bf_contour_polygons(ras, _ptr(words, _u64p), n, cell.ctypes.data, simp.ctypes.data,
+                                   None if has is None else has.ctypes.data,
+                                   None if anc is None else anc.ctypes.data, _ptr(off, _u64p),
+                                   ctypes.byref(out)))
+    try:
+        total = int(off[-1])
+        flat = np.ctypeslib.as_array(out, shape=(max(2 * total, 1),))[:2 * total].copy()
+    finally:
+        lib.bf_contour_free_polygons(out)
+    return [flat[2 * int(off[k]):2 * int(off[k + 1])].reshape(-1, 2) for k in range(n)]

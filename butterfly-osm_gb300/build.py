@@ -49,7 +49,8 @@ def build_engine(verbose=False):
         objs.append(obj)
         if _stale(obj, [src] + headers):
             jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "-Xcompiler", "-O3", "-Xptxas", "-v", "-c", str(src), "-o", str(obj)])
+                         "-Xcompiler", "-O3", "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v",
+                         "-c", str(src), "-o", str(obj)])
     with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         logs = list(ex.map(_run, jobs))
     if verbose:

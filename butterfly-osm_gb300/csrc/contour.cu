@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <tuple>
 #include <cstdlib>
 #include <cmath>
 #include <string>
@@ -497,5 +498,252 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
 }
 
 void bf_contour_free(uint64_t* words) { std::free(words); }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Steps 4-5 on the host, per isochrone in parallel: Moore boundary tracing of
+// the closed raster with cell-centre vertices, the ring containing the anchor
+// (else the largest, the last of equal length), Web-Mercator back-projection
+// and Douglas-Peucker (sparse_contour.rs:770-1183). Sequential per ring.
+
+#include <atomic>
+#include <thread>
+#include <unordered_set>
+
+namespace {
+
+constexpr double EARTH_R = 6378137.0;
+constexpr double PI_D = 3.14159265358979323846264338;
+
+struct RasterView {
+  const bf_raster* r;
+  const uint64_t* w;
+  bool get(int32_t c, int32_t row) const {
+    const int64_t lc = (int64_t)c - r->col0, lr = (int64_t)row - r->row0;
+    if (lc < 0 || lr < 0 || lc >= (int64_t)r->width_words * 64 || lr >= (int64_t)r->height) return false;
+    return (w[r->word_offset + (uint64_t)lr * r->width_words + (uint64_t)(lc >> 6)] >> (lc & 63)) & 1;
+  }
+};
+
+using PtD = std::pair<double, double>;
+
+struct Tracer {
+  RasterView v;
+  std::vector<uint8_t> seen;  // 4 bits per cell: visited edges
+  uint64_t cols = 0;
+  bool visited(int32_t c, int32_t r, uint8_t e) const {
+    return (seen[(uint64_t)(r - v.r->row0) * cols + (uint64_t)(c - v.r->col0)] >> e) & 1;
+  }
+  void mark(int32_t c, int32_t r, uint8_t e) {
+    seen[(uint64_t)(r - v.r->row0) * cols + (uint64_t)(c - v.r->col0)] |= (uint8_t)(1u << e);
+  }
+  void next(int32_t c, int32_t r, uint8_t e, int32_t* nc, int32_t* nr, uint8_t* ne) const {
+    switch (e) {  // next_boundary_edge, sparse_contour.rs:1049-1130
+      case 0:
+        if (v.get(c + 1, r - 1)) { *nc = c + 1; *nr = r - 1; *ne = 3; }
+        else if (v.get(c + 1, r)) { *nc = c + 1; *nr = r; *ne = 0; }
+        else { *nc = c; *nr = r; *ne = 1; }
+        return;
+      case 1:
+        if (v.get(c + 1, r + 1)) { *nc = c + 1; *nr = r + 1; *ne = 0; }
+        else if (v.get(c, r + 1)) { *nc = c; *nr = r + 1; *ne = 1; }
+        else { *nc = c; *nr = r; *ne = 2; }
+        return;
+      case 2:
+        if (v.get(c - 1, r + 1)) { *nc = c - 1; *nr = r + 1; *ne = 1; }
+        else if (v.get(c - 1, r)) { *nc = c - 1; *nr = r; *ne = 2; }
+        else { *nc = c; *nr = r; *ne = 3; }
+        return;
+      default:
+        if (v.get(c - 1, r - 1)) { *nc = c - 1; *nr = r - 1; *ne = 2; }
+        else if (v.get(c, r - 1)) { *nc = c; *nr = r - 1; *ne = 3; }
+        else { *nc = c; *nr = r; *ne = 0; }
+    }
+  }
+};
+
+bool in_ring(PtD p, const std::vector<PtD>& ring) {
+  bool inside = false;
+  const size_t n = ring.size();
+  for (size_t i = 0; i < n; ++i) {
+    const PtD a = ring[i], b = ring[(i + 1) % n];
+    if ((a.second > p.second) != (b.second > p.second) &&
+        p.first < (b.first - a.first) * (p.second - a.second) / (b.second - a.second) + a.first)
+      inside = !inside;
+  }
+  return inside;
+}
+
+bool near_ring(PtD p, const std::vector<PtD>& ring, double tol) {
+  const size_t n = ring.size();
+  for (size_t i = 0; i < n; ++i) {
+    const PtD a = ring[i], b = ring[(i + 1) % n];
+    const double dx = b.first - a.first, dy = b.second - a.second;
+    const double len2 = dx * dx + dy * dy;
+    double t = 0.0;
+    if (len2 > 0.0)
+      t = std::min(std::max(((p.first - a.first) * dx + (p.second - a.second) * dy) / len2, 0.0), 1.0);
+    const double cx = a.first + t * dx, cy = a.second + t * dy;
+    if ((p.first - cx) * (p.first - cx) + (p.second - cy) * (p.second - cy) <= tol * tol) return true;
+  }
+  return false;
+}
+
+double seg_dist(PtD p, PtD s, PtD e) {
+  const double dx = e.first - s.first, dy = e.second - s.second;
+  const double len_sq = dx * dx + dy * dy;
+  if (len_sq < 1e-12) {
+    const double pdx = p.first - s.first, pdy = p.second - s.second;
+    return std::sqrt(pdx * pdx + pdy * pdy);
+  }
+  double t = ((p.first - s.first) * dx + (p.second - s.second) * dy) / len_sq;
+  t = std::min(std::max(t, 0.0), 1.0);
+  const double px = s.first + t * dx, py = s.second + t * dy;
+  const double pdx = p.first - px, pdy = p.second - py;
+  return std::sqrt(pdx * pdx + pdy * pdy);
+}
+
+std::vector<PtD> simplify(const std::vector<PtD>& pts, double tol) {
+  if (pts.size() <= 2) return pts;
+  double max_d = 0.0;
+  size_t max_i = 0;
+  for (size_t i = 1; i + 1 < pts.size(); ++i) {
+    const double d = seg_dist(pts[i], pts.front(), pts.back());
+    if (d > max_d) {
+      max_d = d;
+      max_i = i;
+    }
+  }
+  if (max_d > tol) {
+    std::vector<PtD> left = simplify(std::vector<PtD>(pts.begin(), pts.begin() + max_i + 1), tol);
+    std::vector<PtD> right = simplify(std::vector<PtD>(pts.begin() + max_i, pts.end()), tol);
+    left.pop_back();
+    left.insert(left.end(), right.begin(), right.end());
+    return left;
+  }
+  return {pts.front(), pts.back()};
+}
+
+// The outer ring of one closed raster, as (lon, lat).
+std::vector<PtD> polygon_of(const bf_raster& R, const uint64_t* words, double cell,
+                            double simplify_m, const PtD* anchor_xy) {
+  if (R.height == 0) return {};
+  Tracer t{RasterView{&R, words}, {}, (uint64_t)R.width_words * 64};
+  // boundary starts in (col, row) order, one per boundary cell; the
+  // reference's iteration cap counts its non-empty 64x64 tiles
+  std::vector<std::tuple<int32_t, int32_t, uint8_t>> starts;
+  std::unordered_set<uint64_t> tiles;
+  for (uint32_t lr = 0; lr < R.height; ++lr)
+    for (uint32_t j = 0; j < R.width_words; ++j) {
+      uint64_t bits = words[R.word_offset + (uint64_t)lr * R.width_words + j];
+      while (bits) {
+        const int b = __builtin_ctzll(bits);
+        bits &= bits - 1;
+        const int32_t c = R.col0 + (int32_t)(j * 64 + b), r = R.row0 + (int32_t)lr;
+        tiles.insert(((uint64_t)(uint32_t)(c >> 6) << 32) | (uint32_t)(r >> 6));
+        if (!t.v.get(c, r - 1))
+          starts.emplace_back(c, r, 0);
+        else if (!t.v.get(c - 1, r))
+          starts.emplace_back(c, r, 3);
+        else if (!t.v.get(c + 1, r))
+          starts.emplace_back(c, r, 1);
+        else if (!t.v.get(c, r + 1))
+          starts.emplace_back(c, r, 2);
+      }
+    }
+  if (tiles.empty()) return {};
+  std::sort(starts.begin(), starts.end());
+  t.seen.assign(t.cols * R.height, 0);
+  const uint64_t max_iter = (uint64_t)tiles.size() * 64 * 64 * 4;
+  std::vector<std::vector<PtD>> rings;
+  for (const auto& s : starts) {
+    const int32_t sc = std::get<0>(s), sr = std::get<1>(s);
+    const uint8_t se = std::get<2>(s);
+    if (t.visited(sc, sr, se)) continue;
+    std::vector<PtD> ring;
+    int32_t c = sc, r = sr;
+    uint8_t e = se;
+    for (uint64_t it = 1;; ++it) {
+      if (it > max_iter) break;
+      t.mark(c, r, e);
+      const PtD v{(double)c + 0.5, (double)r + 0.5};
+      if (ring.empty() || ring.back() != v) ring.push_back(v);
+      int32_t nc, nr;
+      uint8_t ne;
+      t.next(c, r, e, &nc, &nr, &ne);
+      if (nc == sc && nr == sr && ne == se) break;
+      c = nc;
+      r = nr;
+      e = ne;
+    }
+    while (ring.size() > 1 && ring.back() == ring.front()) ring.pop_back();
+    if (ring.size() >= 3) rings.push_back(std::move(ring));
+  }
+  const std::vector<PtD>* best = nullptr;
+  if (anchor_xy) {
+    const PtD a{(anchor_xy->first - R.origin_x) / cell, (anchor_xy->second - R.origin_y) / cell};
+    for (const auto& rg : rings)
+      if ((in_ring(a, rg) || near_ring(a, rg, 1.0)) && (!best || rg.size() > best->size())) best = &rg;
+  }
+  if (!best)
+    for (const auto& rg : rings)
+      if (!best || rg.size() >= best->size()) best = &rg;
+  if (!best) return {};
+  std::vector<PtD> wgs;
+  wgs.reserve(best->size());
+  for (const PtD& p : *best) {
+    const double x = R.origin_x + p.first * cell, y = R.origin_y + p.second * cell;
+    const double lon = (x / EARTH_R) * (180.0 / PI_D);
+    const double lat = (2.0 * std::atan(std::exp(y / EARTH_R)) - PI_D / 2.0) * (180.0 / PI_D);
+    wgs.emplace_back(lon, lat);
+  }
+  return simplify(wgs, simplify_m / 111000.0);
+}
+
+}  // namespace
+
+extern "C" {
+
+bf_status bf_contour_polygons(const bf_raster* rasters, const uint64_t* words, uint32_t n_iso,
+                              const double* cell_m, const double* simplify_m,
+                              const uint8_t* has_anchor, const double* anchor_xy,
+                              uint64_t* ring_off, double** lonlat) {
+  if (lonlat) *lonlat = nullptr;
+  if (!rasters || !cell_m || !simplify_m || !ring_off || !lonlat || (has_anchor && !anchor_xy)) {
+    set_error("bf_contour_polygons: null argument");
+    return BF_ERR_INVALID;
+  }
+  std::vector<std::vector<PtD>> rings(n_iso);
+  std::atomic<uint32_t> next{0};
+  auto work = [&]() {
+    for (uint32_t k; (k = next.fetch_add(1)) < n_iso;) {
+      const PtD a = has_anchor ? PtD{anchor_xy[2 * k], anchor_xy[2 * k + 1]} : PtD{0, 0};
+      rings[k] = polygon_of(rasters[k], words, cell_m[k], simplify_m[k],
+                            (has_anchor && has_anchor[k]) ? &a : nullptr);
+    }
+  };
+  const unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), n_iso));
+  std::vector<std::thread> pool;
+  for (unsigned i = 1; i < nt; ++i) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+  ring_off[0] = 0;
+  for (uint32_t k = 0; k < n_iso; ++k) ring_off[k + 1] = ring_off[k] + rings[k].size();
+  double* out = (double*)std::malloc(std::max<uint64_t>(ring_off[n_iso], 1) * 16);
+  if (!out) {
+    set_error("out of host memory");
+    return BF_ERR_OOM;
+  }
+  for (uint32_t k = 0; k < n_iso; ++k)
+    for (size_t i = 0; i < rings[k].size(); ++i) {
+      out[2 * (ring_off[k] + i)] = rings[k][i].first;
+      out[2 * (ring_off[k] + i) + 1] = rings[k][i].second;
+    }
+  *lonlat = out;
+  return BF_OK;
+}
+
+void bf_contour_free_polygons(double* lonlat) { std::free(lonlat); }
 
 }  // extern "C"

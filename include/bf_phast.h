@@ -29,6 +29,7 @@
  *   bf_cch_relax[_lex]     triangle_relax_parallel / _lex_parallel   customization.rs:1083, :1253
  *   bf_cch_bottom_up       bottom_up_customize / _with_external_middles  customization.rs:1005, :953
  *   bf_contour_rasters     generate_sparse_contour_anchored, steps 1-3  route/src/range/sparse_contour.rs:650
+ *   bf_contour_polygons    generate_sparse_contour_anchored, steps 4-5  sparse_contour.rs:770
  *
  * Conventions (as in the reference):
  *   - node ids are CCH ranks (rank-aligned CCH, node_id == rank);
@@ -513,6 +514,20 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
                              const double* anchor_xy, uint32_t dilation, uint32_t erosion,
                              int device, bf_raster* rasters, uint64_t** words, uint64_t* n_words);
 void bf_contour_free(uint64_t* words);
+
+/* Steps 4-5 of generate_sparse_contour_anchored (sparse_contour.rs:770-830,
+ * 831-1183) on the rasters of bf_contour_rasters, one host thread per
+ * isochrone: Moore boundary tracing with cell-centre vertices, the ring
+ * containing the anchor (Mercator x, y; else the ring with the most
+ * vertices, the last of equal length), back-projection to (lon, lat) and
+ * Douglas-Peucker with tolerance simplify_m[k] / 111000 degrees. Ring k is
+ * points [ring_off[k], ring_off[k + 1]) of *lonlat (n_iso + 1 offsets), a
+ * buffer released with bf_contour_free_polygons. */
+bf_status bf_contour_polygons(const bf_raster* rasters, const uint64_t* words, uint32_t n_iso,
+                              const double* cell_m, const double* simplify_m,
+                              const uint8_t* has_anchor, const double* anchor_xy,
+                              uint64_t* ring_off, double** lonlat);
+void bf_contour_free_polygons(double* lonlat);
 
 const char* bf_last_error(void);
 

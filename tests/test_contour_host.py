@@ -1,0 +1,45 @@
+"""bf_contour_polygons (host tracing, anchored ring, back-projection,
+Douglas-Peucker) on rasters built from the oracle's closed cells, against the
+oracle's whole contour pipeline (route/src/range/sparse_contour.rs:770-1183).
+CPU only."""
+import numpy as np
+
+import contourgen
+from oracle import oracle as orc
+
+
+def _raster(cells, grid, off):
+    import bfphast
+    c0, r0 = int(cells[:, 0].min()) - 1, int(cells[:, 1].min()) - 1
+    c1, r1 = int(cells[:, 0].max()) + 1, int(cells[:, 1].max()) + 1
+    wpr, h = (c1 - c0 + 1 + 63) // 64, r1 - r0 + 1
+    words = np.zeros(wpr * h, np.uint64)
+    lc, lr = cells[:, 0] - c0, cells[:, 1] - r0
+    np.bitwise_or.at(words, lr * wpr + lc // 64, np.left_shift(np.uint64(1), (lc % 64).astype(np.uint64)))
+    r = bfphast.Raster(col0=c0, row0=r0, width_words=wpr, height=h, word_offset=off,
+                       origin_x=grid[0], origin_y=grid[1])
+    return r, words
+
+
+def test_host_polygons_match_oracle(built):
+    import bfphast
+    rng = np.random.default_rng(9)
+    rasters, words, cfg, anchors, want = [], [], [], [], []
+    off = 0
+    for k in range(8):
+        segs, anchor = contourgen.isochrone(rng, int(rng.integers(5, 300)), spread=0.01)
+        cell, dil, ero, simp = orc.contour_config(("car", "bike", "foot")[k % 3], 600 + 900 * k)
+        cells, grid = orc.sparse_closed(segs, cell, dil, ero, anchor)
+        r, w = _raster(cells, grid, off)
+        off += len(w)
+        rasters.append(r)
+        words.append(w)
+        cfg.append((cell, simp))
+        anchors.append(contourgen.mercator_point(anchor) if anchor else None)
+        want.append(orc.sparse_contour(segs, cell, dil, ero, simp, anchor))
+    has = np.array([a is not None for a in anchors], np.uint8)
+    anc = np.array([a or (0.0, 0.0) for a in anchors])
+    rings = bfphast.contour_polygons(rasters, np.concatenate(words), [c[0] for c in cfg],
+                                     [c[1] for c in cfg], has, anc)
+    for got, w in zip(rings, want):
+        assert len(w) >= 3 and np.array_equal(got, w)

@@ -41,3 +41,37 @@ def test_empty_and_single_point_isochrones(built):
     for (gc, _), s, cell in zip(got[1:], (one, segs), (30.0, 60.0)):
         wc, _ = orc.sparse_closed(s, cell, 2, 2)
         assert np.array_equal(gc, wc)
+
+
+def test_polygons_match_oracle(built):
+    # the whole pipeline: GPU rasters, then tracing, anchored ring,
+    # back-projection and simplification, against the oracle's rings
+    import bfphast
+    rng = np.random.default_rng(77)
+    segs_all, isos, cfgs = [], [], []
+    for k in range(10):
+        segs, anchor = contourgen.isochrone(rng, int(rng.integers(20, 600)), spread=0.01)
+        mode = ("car", "bike", "foot")[k % 3]
+        cell, dil, ero, simp = orc.contour_config(mode, (300, 1200, 3000, 7200)[k % 4])
+        segs_all.append((segs, anchor))
+        isos.append({"segments": contourgen.mercator_segments(segs), "cell_m": cell,
+                     "anchor": contourgen.mercator_point(anchor) if anchor else None})
+        cfgs.append((cell, dil, ero, simp))
+    for dil, ero in {(c[1], c[2]) for c in cfgs}:
+        idx = [k for k, c in enumerate(cfgs) if (c[1], c[2]) == (dil, ero)]
+        pts, seg_pt, iso_seg = [], [0], [0]
+        for k in idx:
+            for a in isos[k]["segments"]:
+                pts.append(a)
+                seg_pt.append(seg_pt[-1] + len(a))
+            iso_seg.append(len(seg_pt) - 1)
+        has = np.array([isos[k]["anchor"] is not None for k in idx], np.uint8)
+        anc = np.array([isos[k]["anchor"] or (0.0, 0.0) for k in idx])
+        ras, words = bfphast.contour_rasters_flat(np.concatenate(pts), seg_pt, iso_seg,
+                                                  [cfgs[k][0] for k in idx], dil, ero, has, anc)
+        rings = bfphast.contour_polygons(ras, words, [cfgs[k][0] for k in idx],
+                                         [cfgs[k][3] for k in idx], has, anc)
+        for k, ring in zip(idx, rings):
+            segs, anchor = segs_all[k]
+            want = orc.sparse_contour(segs, cfgs[k][0], dil, ero, cfgs[k][3], anchor)
+            assert np.array_equal(ring, want)
