@@ -462,7 +462,10 @@ def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
         len_parts.append(np.full(len(wa) + len(ca), 2, np.uint64))
         iso_seg.append(iso_seg[-1] + len(wa) + len(ca))
         e7.append((lat_e7, lon_e7, wa, wb, ca, clat, clon, a[i0]))
-    xy = np.concatenate(xy_parts)
+    import torch
+    n_pts = sum(len(p) for p in xy_parts)
+    xy = torch.empty((n_pts, 2), dtype=torch.float64, pin_memory=True).numpy()  # page-locked
+    np.concatenate(xy_parts, out=xy)
     seg_pt = np.concatenate([[0], np.cumsum(np.concatenate(len_parts))]).astype(np.uint64)
     bfphast.contour_rasters_flat(xy[:2], seg_pt[:2], [0, 1], [cell], dil, ero)  # warm-up
     has, anc = np.ones(count, np.uint8), np.asarray(anchors)

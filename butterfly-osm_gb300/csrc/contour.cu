@@ -52,41 +52,44 @@ __device__ __forceinline__ void set_cell(const IsoDev& g, int32_t c, int32_t r,
 }
 
 // stamp_line (sparse_contour.rs:112-144) over every consecutive point pair
-// of a segment, then every point of it: one thread per segment.
-__global__ void k_stamp(uint64_t n_seg, const double2* __restrict__ xy,
+// of a segment, and every point of it: one thread per segment, each point's
+// cell computed once (two IEEE double divisions), the line drawn from the
+// previous point's cell. Point ranges are clamped to the points given.
+__global__ void k_stamp(uint64_t n_seg, uint64_t n_pts, const double2* __restrict__ xy,
                         const uint64_t* __restrict__ seg_pt, const uint32_t* __restrict__ seg_iso,
                         const IsoDev* __restrict__ iso, unsigned long long* __restrict__ words,
                         uint32_t* err) {
   for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n_seg;
        s += (uint64_t)gridDim.x * blockDim.x) {
     const IsoDev g = iso[seg_iso[s]];
-    const uint64_t p0 = seg_pt[s], p1 = seg_pt[s + 1];
-    for (uint64_t p = p0; p + 1 < p1; ++p) {
-      int32_t c0, r0, c1, r1;
-      const double2 a = xy[p], b = xy[p + 1];
-      cell_of(g, a.x, a.y, &c0, &r0);
-      cell_of(g, b.x, b.y, &c1, &r1);
-      const int32_t dx = abs(c1 - c0), dy = abs(r1 - r0);
-      const int32_t sx = c0 < c1 ? 1 : -1, sy = r0 < r1 ? 1 : -1;
-      int32_t e = dx - dy, c = c0, r = r0;
-      for (int64_t guard = 0; guard <= (int64_t)dx + dy; ++guard) {  // dx + dy + 1 cells at most
-        set_cell(g, c, r, words, err);
-        if (c == c1 && r == r1) break;
-        const int32_t e2 = 2 * e;
-        if (e2 > -dy) {
-          e -= dy;
-          c += sx;
-        }
-        if (e2 < dx) {
-          e += dx;
-          r += sy;
+    const uint64_t p1 = min(seg_pt[s + 1], n_pts), p0 = min(seg_pt[s], p1);
+    int32_t pc = 0, pr = 0;
+    for (uint64_t p = p0; p < p1; ++p) {
+      int32_t c1, r1;
+      const double2 q = xy[p];
+      cell_of(g, q.x, q.y, &c1, &r1);
+      set_cell(g, c1, r1, words, err);
+      if (p > p0) {
+        const int32_t c0 = pc, r0 = pr;
+        const int32_t dx = abs(c1 - c0), dy = abs(r1 - r0);
+        const int32_t sx = c0 < c1 ? 1 : -1, sy = r0 < r1 ? 1 : -1;
+        int32_t e = dx - dy, c = c0, r = r0;
+        for (int64_t guard = 0; guard <= (int64_t)dx + dy; ++guard) {  // dx + dy + 1 cells at most
+          set_cell(g, c, r, words, err);
+          if (c == c1 && r == r1) break;
+          const int32_t e2 = 2 * e;
+          if (e2 > -dy) {
+            e -= dy;
+            c += sx;
+          }
+          if (e2 < dx) {
+            e += dx;
+            r += sy;
+          }
         }
       }
-    }
-    for (uint64_t p = p0; p < p1; ++p) {
-      int32_t c, r;
-      cell_of(g, xy[p].x, xy[p].y, &c, &r);
-      set_cell(g, c, r, words, err);
+      pc = c1;
+      pr = r1;
     }
   }
 }
@@ -141,92 +144,100 @@ __global__ void k_morph(uint32_t n_iso, const IsoDev* __restrict__ iso, uint64_t
   }
 }
 
-// Per isochrone (one block each): the minimum point corner, then the grid
-// origin (minimum less three cells, as the reference) and the extreme cells
-// of its points and anchor disk; also tags every segment with its isochrone.
+// Extents: the grid origin is each isochrone's minimum corner less three
+// cells (as the reference); cell indices floor((x - origin) / cell) are
+// monotone in x and y, so the extreme cells are those of the extreme
+// coordinates. Chunked min / max partials first (EXT_CHUNKS blocks per
+// isochrone, which also tag segments with their isochrone and check the
+// segment offsets), then one thread per isochrone.
+constexpr uint32_t EXT_CHUNKS = 32;
+
+struct MinMax {
+  double x0, y0, x1, y1;  // minimum and maximum coordinates
+};
+
 struct Extent {
   double ox, oy;
   int32_t c0, r0, c1, r1;
   uint32_t has_points, pad;
 };
 
-__device__ __forceinline__ double block_min(double v, double* red) {
+__device__ __forceinline__ double warp_min(double v) {
   for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : INFINITY;
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
-    if (threadIdx.x == 0) red[0] = v;
-  }
-  __syncthreads();
-  const double r = red[0];
-  __syncthreads();
-  return r;
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  return v;
 }
 
-__device__ __forceinline__ int block_minmax_i(int v, bool is_max, int* red) {
-  for (int o = 16; o > 0; o >>= 1) {
-    const int w = __shfl_xor_sync(0xFFFFFFFFu, v, o);
-    v = is_max ? max(v, w) : min(v, w);
-  }
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : (is_max ? INT_MIN : INT_MAX);
-    for (int o = 16; o > 0; o >>= 1) {
-      const int w = __shfl_xor_sync(0xFFFFFFFFu, v, o);
-      v = is_max ? max(v, w) : min(v, w);
-    }
-    if (threadIdx.x == 0) red[0] = v;
-  }
-  __syncthreads();
-  const int r = red[0];
-  __syncthreads();
-  return r;
-}
-
-__global__ void __launch_bounds__(256) k_extent(const double2* __restrict__ xy,
+__global__ void __launch_bounds__(256) k_minmax(uint64_t n_pts, const double2* __restrict__ xy,
                                                 const uint64_t* __restrict__ seg_pt,
                                                 const uint64_t* __restrict__ iso_seg,
-                                                const double* __restrict__ cell_m,
-                                                const uint8_t* __restrict__ has_anchor,
-                                                const double2* __restrict__ anchor,
                                                 uint32_t* __restrict__ seg_iso,
-                                                Extent* __restrict__ ext) {
-  __shared__ double dred[8];
-  __shared__ int ired[8];
-  const uint32_t k = blockIdx.x;
+                                                MinMax* __restrict__ part, uint32_t* err) {
+  __shared__ MinMax red[8];
+  const uint32_t k = blockIdx.x / EXT_CHUNKS, ch = blockIdx.x % EXT_CHUNKS;
   const uint64_t s0 = iso_seg[k], s1 = iso_seg[k + 1];
-  for (uint64_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) seg_iso[s] = k;
-  const uint64_t p0 = seg_pt[s0], p1 = seg_pt[s1];
-  double mx = INFINITY, my = INFINITY;
-  for (uint64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-    mx = fmin(mx, xy[p].x);
-    my = fmin(my, xy[p].y);
+  const uint64_t sa = s0 + (s1 - s0) * ch / EXT_CHUNKS, sb = s0 + (s1 - s0) * (ch + 1) / EXT_CHUNKS;
+  for (uint64_t s = sa + threadIdx.x; s < sb; s += blockDim.x) {
+    seg_iso[s] = k;
+    if (seg_pt[s + 1] < seg_pt[s] || seg_pt[s + 1] > n_pts) atomicOr(err, 2u);
   }
-  mx = block_min(mx, dred);
-  my = block_min(my, dred);
+  const uint64_t q1 = min(seg_pt[s1], n_pts), q0 = min(seg_pt[s0], q1);
+  const uint64_t pa = q0 + (q1 - q0) * ch / EXT_CHUNKS, pb = q0 + (q1 - q0) * (ch + 1) / EXT_CHUNKS;
+  double mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+  for (uint64_t p = pa + threadIdx.x; p < pb; p += blockDim.x) {
+    const double2 q = xy[p];
+    mnx = fmin(mnx, q.x);
+    mny = fmin(mny, q.y);
+    mxx = fmax(mxx, q.x);
+    mxy = fmax(mxy, q.y);
+  }
+  mnx = warp_min(mnx);
+  mny = warp_min(mny);
+  mxx = warp_max(mxx);
+  mxy = warp_max(mxy);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = MinMax{mnx, mny, mxx, mxy};
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    MinMax r = red[0];
+    for (uint32_t w = 1; w < (blockDim.x >> 5); ++w) {
+      r.x0 = fmin(r.x0, red[w].x0);
+      r.y0 = fmin(r.y0, red[w].y0);
+      r.x1 = fmax(r.x1, red[w].x1);
+      r.y1 = fmax(r.y1, red[w].y1);
+    }
+    part[blockIdx.x] = r;
+  }
+}
+
+__global__ void k_extent(uint32_t n_iso, const MinMax* __restrict__ part,
+                         const double* __restrict__ cell_m, const uint8_t* __restrict__ has_anchor,
+                         const double2* __restrict__ anchor, Extent* __restrict__ ext) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_iso) return;
+  MinMax m = part[(uint64_t)k * EXT_CHUNKS];
+  for (uint32_t c = 1; c < EXT_CHUNKS; ++c) {
+    const MinMax q = part[(uint64_t)k * EXT_CHUNKS + c];
+    m.x0 = fmin(m.x0, q.x0);
+    m.y0 = fmin(m.y0, q.y0);
+    m.x1 = fmax(m.x1, q.x1);
+    m.y1 = fmax(m.y1, q.y1);
+  }
   Extent e{};
-  if (p1 == p0) {
-    if (threadIdx.x == 0) ext[k] = e;
+  if (isinf(m.x0)) {
+    ext[k] = e;
     return;
   }
-  const double cell = cell_m[k];
   IsoDev g{};
-  g.ox = __dsub_rn(mx, __dmul_rn(cell, 3.0));
-  g.oy = __dsub_rn(my, __dmul_rn(cell, 3.0));
-  g.cell = cell;
-  int c0 = INT_MAX, r0 = INT_MAX, c1 = INT_MIN, r1 = INT_MIN;
-  for (uint64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-    int32_t c, r;
-    cell_of(g, xy[p].x, xy[p].y, &c, &r);
-    c0 = min(c0, c);
-    r0 = min(r0, r);
-    c1 = max(c1, c);
-    r1 = max(r1, r);
-  }
-  if (threadIdx.x == 0 && has_anchor && has_anchor[k]) {
+  g.cell = cell_m[k];
+  g.ox = __dsub_rn(m.x0, __dmul_rn(g.cell, 3.0));
+  g.oy = __dsub_rn(m.y0, __dmul_rn(g.cell, 3.0));
+  int32_t c0, r0, c1, r1;
+  cell_of(g, m.x0, m.y0, &c0, &r0);
+  cell_of(g, m.x1, m.y1, &c1, &r1);
+  if (has_anchor && has_anchor[k]) {
     int32_t c, r;
     cell_of(g, anchor[k].x, anchor[k].y, &c, &r);
     c0 = min(c0, c - 1);
@@ -234,11 +245,7 @@ __global__ void __launch_bounds__(256) k_extent(const double2* __restrict__ xy,
     c1 = max(c1, c + 1);
     r1 = max(r1, r + 1);
   }
-  c0 = block_minmax_i(c0, false, ired);
-  r0 = block_minmax_i(r0, false, ired);
-  c1 = block_minmax_i(c1, true, ired);
-  r1 = block_minmax_i(r1, true, ired);
-  if (threadIdx.x == 0) ext[k] = Extent{g.ox, g.oy, c0, r0, c1, r1, 1u, 0u};
+  ext[k] = Extent{g.ox, g.oy, c0, r0, c1, r1, 1u, 0u};
 }
 
 unsigned grid_of(uint64_t n) {
@@ -365,12 +372,7 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
       return BF_ERR_INVALID;
     }
   const uint64_t n_seg = iso_seg[n_iso];
-  for (uint64_t s = 0; s < n_seg; ++s)
-    if (seg_pt[s + 1] < seg_pt[s]) {
-      set_error("bf_contour_rasters: seg_pt must be non-decreasing");
-      return BF_ERR_INVALID;
-    }
-  const uint64_t n_pts = seg_pt[n_seg];
+  const uint64_t n_pts = seg_pt[n_seg];  // segment offsets are checked with the extents
   if (n_pts && !xy) {
     set_error("bf_contour_rasters: null points");
     return BF_ERR_INVALID;
@@ -378,6 +380,11 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
   std::vector<IsoDev> iso;
   uint64_t total = 0;
   if (!words) {  // layout only, on the host
+    for (uint64_t s = 0; s < n_seg; ++s)
+      if (seg_pt[s + 1] < seg_pt[s]) {
+        set_error("bf_contour_rasters: seg_pt must be non-decreasing");
+        return BF_ERR_INVALID;
+      }
     if (!layout(xy, seg_pt, iso_seg, n_iso, cell_m, has_anchor, anchor_xy, dilation, rasters, iso,
                 &total)) {
       set_error("bf_contour_rasters: a raster extends beyond 32-bit cell coordinates");
@@ -408,12 +415,14 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
   uint8_t* d_has = nullptr;
   Extent* d_ext = nullptr;
   IsoDev* d_iso = nullptr;
+  MinMax* d_part = nullptr;
   alloc(&d_xy, n_pts * sizeof(double2));
   alloc(&d_seg, (n_seg + 1) * 8);
   alloc(&d_iseg, ((uint64_t)n_iso + 1) * 8);
   alloc(&d_siso, n_seg * 4);
   alloc(&d_cell, (uint64_t)n_iso * 8);
   alloc(&d_ext, (uint64_t)n_iso * sizeof(Extent));
+  alloc(&d_part, (uint64_t)n_iso * EXT_CHUNKS * sizeof(MinMax));
   alloc(&d_iso, (uint64_t)n_iso * sizeof(IsoDev));
   alloc(&d_err, 4);
   if (has_anchor) {
@@ -435,8 +444,11 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
       if ((r = cudaMemcpyAsync(d_anchor, anchor_xy, (uint64_t)n_iso * 16, cudaMemcpyHostToDevice, st)))
         return r;
     }
-    if (n_iso)
-      k_extent<<<n_iso, 256, 0, st>>>(d_xy, d_seg, d_iseg, d_cell, d_has, d_anchor, d_siso, d_ext);
+    if ((r = cudaMemsetAsync(d_err, 0, 4, st))) return r;
+    if (n_iso) {
+      k_minmax<<<n_iso * EXT_CHUNKS, 256, 0, st>>>(n_pts, d_xy, d_seg, d_iseg, d_siso, d_part, d_err);
+      k_extent<<<(n_iso + 127) / 128, 128, 0, st>>>(n_iso, d_part, d_cell, d_has, d_anchor, d_ext);
+    }
     if ((r = cudaGetLastError())) return r;
     if (n_iso && (r = cudaMemcpyAsync(ext.data(), d_ext, (uint64_t)n_iso * sizeof(Extent),
                                       cudaMemcpyDeviceToHost, st)))
@@ -444,6 +456,15 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
     return cudaStreamSynchronize(st);
   };
   if ((e = stage1()) != cudaSuccess) return done(cuda_status(e, "bf_contour_rasters: extents"));
+  {
+    uint32_t verr = 0;
+    if ((e = cudaMemcpy(&verr, d_err, 4, cudaMemcpyDeviceToHost)) != cudaSuccess)
+      return done(cuda_status(e, "bf_contour_rasters: extents"));
+    if (verr & 2u) {
+      set_error("bf_contour_rasters: seg_pt must be non-decreasing");
+      return done(BF_ERR_INVALID);
+    }
+  }
   if (!place(n_iso, ext.data(), cell_m, dilation, rasters, iso, &total)) {
     set_error("bf_contour_rasters: a raster extends beyond 32-bit cell coordinates");
     return done(BF_ERR_INVALID);
@@ -468,7 +489,8 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
       return r;
     if ((r = cudaMemsetAsync(d_a, 0, std::max<uint64_t>(total, 1) * 8, st))) return r;
     if ((r = cudaMemsetAsync(d_err, 0, 4, st))) return r;
-    if (n_seg) k_stamp<<<grid_of(n_seg), 256, 0, st>>>(n_seg, d_xy, d_seg, d_siso, d_iso, d_a, d_err);
+    if (n_seg)
+      k_stamp<<<grid_of(n_seg), 256, 0, st>>>(n_seg, n_pts, d_xy, d_seg, d_siso, d_iso, d_a, d_err);
     if (has_anchor && n_iso)
       k_anchor<<<(n_iso + 127) / 128, 128, 0, st>>>(n_iso, d_iso, d_has, d_anchor, d_a, d_err);
     unsigned long long *cur = d_a, *nxt = d_b;
@@ -630,32 +652,54 @@ std::vector<PtD> polygon_of(const bf_raster& R, const uint64_t* words, double ce
                             double simplify_m, const PtD* anchor_xy) {
   if (R.height == 0) return {};
   Tracer t{RasterView{&R, words}, {}, (uint64_t)R.width_words * 64};
-  // boundary starts in (col, row) order, one per boundary cell; the
-  // reference's iteration cap counts its non-empty 64x64 tiles
+  // boundary starts in (col, row) order, one per boundary cell, found with
+  // word masks in the reference's edge priority (N, W, E, S); the iteration
+  // cap counts the reference's non-empty 64x64 tiles (aligned at multiples
+  // of 64 in grid cells), marked per word from its lowest and highest bits
   std::vector<std::tuple<int32_t, int32_t, uint8_t>> starts;
-  std::unordered_set<uint64_t> tiles;
+  const int32_t tx0 = R.col0 >> 6, ty0 = R.row0 >> 6;
+  const int32_t tx1 = (R.col0 + (int32_t)(R.width_words * 64) - 1) >> 6;
+  const int32_t ty1 = (R.row0 + (int32_t)R.height - 1) >> 6;
+  const uint64_t ntx = (uint64_t)(tx1 - tx0 + 1);
+  std::vector<uint8_t> tile_set(ntx * (uint64_t)(ty1 - ty0 + 1), 0);
+  auto W = [&](int64_t lr, int64_t j) -> uint64_t {
+    if (lr < 0 || lr >= (int64_t)R.height || j < 0 || j >= (int64_t)R.width_words) return 0;
+    return words[R.word_offset + (uint64_t)lr * R.width_words + (uint64_t)j];
+  };
+  uint64_t n_tiles = 0;
   for (uint32_t lr = 0; lr < R.height; ++lr)
     for (uint32_t j = 0; j < R.width_words; ++j) {
-      uint64_t bits = words[R.word_offset + (uint64_t)lr * R.width_words + j];
-      while (bits) {
-        const int b = __builtin_ctzll(bits);
-        bits &= bits - 1;
-        const int32_t c = R.col0 + (int32_t)(j * 64 + b), r = R.row0 + (int32_t)lr;
-        tiles.insert(((uint64_t)(uint32_t)(c >> 6) << 32) | (uint32_t)(r >> 6));
-        if (!t.v.get(c, r - 1))
-          starts.emplace_back(c, r, 0);
-        else if (!t.v.get(c - 1, r))
-          starts.emplace_back(c, r, 3);
-        else if (!t.v.get(c + 1, r))
-          starts.emplace_back(c, r, 1);
-        else if (!t.v.get(c, r + 1))
-          starts.emplace_back(c, r, 2);
+      const uint64_t cur = W(lr, j);
+      if (!cur) continue;
+      const int32_t r = R.row0 + (int32_t)lr, cb = R.col0 + (int32_t)(j * 64);
+      for (int32_t c : {cb + __builtin_ctzll(cur), cb + 63 - __builtin_clzll(cur)}) {
+        uint8_t& t = tile_set[(uint64_t)((r >> 6) - ty0) * ntx + (uint64_t)((c >> 6) - tx0)];
+        if (!t) {
+          t = 1;
+          ++n_tiles;
+        }
+      }
+      const uint64_t north = W((int64_t)lr - 1, j), south = W((int64_t)lr + 1, j);
+      const uint64_t west = (cur << 1) | (W(lr, (int64_t)j - 1) >> 63);
+      const uint64_t east = (cur >> 1) | (W(lr, (int64_t)j + 1) << 63);
+      // edge 0 (N), then 3 (W), then 1 (E), then 2 (S)
+      const uint64_t mn = cur & ~north;
+      const uint64_t mw = cur & north & ~west;
+      const uint64_t me = cur & north & west & ~east;
+      const uint64_t ms = cur & north & west & east & ~south;
+      const uint64_t any = mn | mw | me | ms;
+      for (uint64_t b = any; b;) {
+        const int i = __builtin_ctzll(b);
+        b &= b - 1;
+        const uint64_t bit = 1ull << i;
+        const uint8_t e = (mn & bit) ? 0 : (mw & bit) ? 3 : (me & bit) ? 1 : 2;
+        starts.emplace_back(cb + i, r, e);
       }
     }
-  if (tiles.empty()) return {};
+  if (n_tiles == 0) return {};
   std::sort(starts.begin(), starts.end());
   t.seen.assign(t.cols * R.height, 0);
-  const uint64_t max_iter = (uint64_t)tiles.size() * 64 * 64 * 4;
+  const uint64_t max_iter = n_tiles * 64 * 64 * 4;
   std::vector<std::vector<PtD>> rings;
   for (const auto& s : starts) {
     const int32_t sc = std::get<0>(s), sr = std::get<1>(s);
