@@ -467,8 +467,9 @@ def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
     xy = torch.empty((n_pts, 2), dtype=torch.float64, pin_memory=True).numpy()  # page-locked
     np.concatenate(xy_parts, out=xy)
     seg_pt = np.concatenate([[0], np.cumsum(np.concatenate(len_parts))]).astype(np.uint64)
-    bfphast.contour_rasters_flat(xy[:2], seg_pt[:2], [0, 1], [cell], dil, ero)  # warm-up
     has, anc = np.ones(count, np.uint8), np.asarray(anchors)
+    warm = bfphast.contour_rasters_flat(xy, seg_pt, iso_seg, [cell] * count, dil, ero, has, anc)
+    bfphast.contour_polygons(*warm, [cell] * count, [simp] * count, has, anc)  # warm-up
     t0 = time.perf_counter()
     ras, words = bfphast.contour_rasters_flat(xy, seg_pt, iso_seg, [cell] * count, dil, ero,
                                               has, anc)

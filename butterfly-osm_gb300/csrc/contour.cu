@@ -19,7 +19,9 @@
 #include <tuple>
 #include <cstdlib>
 #include <cmath>
+#include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "engine.cuh"
@@ -248,6 +250,19 @@ __global__ void k_extent(uint32_t n_iso, const MinMax* __restrict__ part,
   ext[k] = Extent{g.ox, g.oy, c0, r0, c1, r1, 1u, 0u};
 }
 
+// Device buffers and stream of bf_contour_rasters, kept per device across
+// calls (grow-only; calls on one device are serialised by the mutex).
+struct Workspace {
+  std::mutex mu;
+  cudaStream_t st = nullptr;
+  void* buf[16] = {};
+  size_t cap[16] = {};
+};
+Workspace& workspace(int device) {
+  static Workspace ws[64];
+  return ws[device];
+}
+
 unsigned grid_of(uint64_t n) {
   return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 152ull * 16));
 }
@@ -394,20 +409,35 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
     return BF_OK;
   }
   if (cudaSetDevice(device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
-  cudaStream_t st = nullptr;
-  BF_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  std::vector<void*> bufs;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev || device >= 64) {
+    cudaGetLastError();
+    set_error("bf_contour_rasters: no such device");
+    return BF_ERR_INVALID;
+  }
+  // per-device workspace kept across calls: one stream, grow-only buffers
+  Workspace& ws = workspace(device);
+  std::lock_guard<std::mutex> lk(ws.mu);
+  if (!ws.st) BF_CUDA(cudaStreamCreateWithFlags(&ws.st, cudaStreamNonBlocking));
+  cudaStream_t st = ws.st;
   cudaError_t e = cudaSuccess;
+  int slot = 0;
   auto alloc = [&](auto** p, size_t bytes) {
+    const int i = slot++;
     if (e != cudaSuccess) return;
-    e = cudaMalloc((void**)p, std::max<size_t>(bytes, 16));
-    if (e == cudaSuccess) bufs.push_back(*p);
+    bytes = std::max<size_t>(bytes, 16);
+    if (ws.cap[i] < bytes) {
+      if (ws.buf[i]) cudaFree(ws.buf[i]);
+      ws.buf[i] = nullptr;
+      ws.cap[i] = 0;
+      const size_t want = bytes + bytes / 4;
+      e = cudaMalloc(&ws.buf[i], want);
+      if (e != cudaSuccess) return;
+      ws.cap[i] = want;
+    }
+    *p = reinterpret_cast<std::remove_reference_t<decltype(*p)>>(ws.buf[i]);
   };
-  auto done = [&](bf_status rc) {
-    for (void* p : bufs) cudaFree(p);
-    cudaStreamDestroy(st);
-    return rc;
-  };
+  auto done = [&](bf_status rc) { return rc; };
   double2 *d_xy = nullptr, *d_anchor = nullptr;
   uint64_t *d_seg = nullptr, *d_iseg = nullptr;
   uint32_t *d_siso = nullptr, *d_err = nullptr;
@@ -425,10 +455,8 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
   alloc(&d_part, (uint64_t)n_iso * EXT_CHUNKS * sizeof(MinMax));
   alloc(&d_iso, (uint64_t)n_iso * sizeof(IsoDev));
   alloc(&d_err, 4);
-  if (has_anchor) {
-    alloc(&d_has, n_iso);
-    alloc(&d_anchor, (uint64_t)n_iso * 16);
-  }
+  alloc(&d_has, n_iso);  // always, so every buffer keeps its workspace slot
+  alloc(&d_anchor, (uint64_t)n_iso * 16);
   if (e != cudaSuccess) return done(cuda_status(e, "bf_contour_rasters: device memory"));
   std::vector<Extent> ext(n_iso);
   auto stage1 = [&]() -> cudaError_t {
