@@ -111,3 +111,35 @@ def test_contour_layout_without_device(built):
     _, grid = orc.sparse_closed(segs, 30.0, 2, 2)
     assert (ras[0].origin_x, ras[0].origin_y) == tuple(grid)
     assert ras[0].width_words * ras[0].height == nw.value
+
+
+def test_contour_and_customization_input_errors(built):
+    # host-side validation: bad offsets, non-positive cell sizes, unknown
+    # topology flags are BF_ERR_INVALID without touching a device
+    import ctypes
+    import numpy as np
+    import bfphast
+    lib = bfphast.load()
+    xy = np.zeros((4, 2))
+    ras = (bfphast.Raster * 2)()
+    nw = ctypes.c_uint64(0)
+    for seg_pt, iso_seg, cell in (([0, 2, 1, 4], [0, 3], [30.0]),   # decreasing seg_pt
+                                  ([0, 2, 4], [0, 2, 1], [30.0, 30.0]),  # decreasing iso_seg
+                                  ([0, 2, 4], [0, 2], [0.0])):       # cell size 0
+        sp = np.asarray(seg_pt, np.uint64)
+        isg = np.asarray(iso_seg, np.uint64)
+        c = np.asarray(cell)
+        rc = lib.bf_contour_rasters(xy.ctypes.data, sp.ctypes.data_as(bfphast._u64p),
+                                    isg.ctypes.data_as(bfphast._u64p), len(isg) - 1,
+                                    c.ctypes.data, None, None, 2, 2, 0, ras, None,
+                                    ctypes.byref(nw))
+        assert rc == bfphast.BF_ERR_INVALID
+    keep = [np.array([0, 1, 1], np.uint64), np.array([1], np.uint32),
+            np.array([0, 0, 1], np.uint64), np.array([0], np.uint32)]
+    t = bfphast.CchTopo(n_nodes=2, flags=8)
+    t.up_offsets = keep[0].ctypes.data_as(bfphast._u64p)
+    t.up_targets = keep[1].ctypes.data_as(bfphast._u32p)
+    t.down_offsets = keep[2].ctypes.data_as(bfphast._u64p)
+    t.down_targets = keep[3].ctypes.data_as(bfphast._u32p)
+    h = ctypes.c_void_p()
+    assert lib.bf_cch_create(ctypes.byref(t), 0, ctypes.byref(h)) == bfphast.BF_ERR_INVALID
