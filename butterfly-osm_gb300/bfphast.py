@@ -214,6 +214,7 @@ _SIGNATURES = {
                                           ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                                           ctypes.POINTER(Raster), ctypes.POINTER(_u64p), _u64p]),
     "bf_contour_free": (None, [_u64p]),
+    "bf_contour_release": (None, [ctypes.c_int]),
     "bf_contour_polygons": (ctypes.c_int, [ctypes.POINTER(Raster), _u64p, ctypes.c_uint32,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p, _u64p,

@@ -549,6 +549,24 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
 
 void bf_contour_free(uint64_t* words) { std::free(words); }
 
+void bf_contour_release(int device) {
+  if (device < 0 || device >= 64) return;
+  Workspace& ws = workspace(device);
+  std::lock_guard<std::mutex> lk(ws.mu);
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  if (ws.st) cudaStreamSynchronize(ws.st);
+  for (int i = 0; i < 16; ++i) {
+    if (ws.buf[i]) cudaFree(ws.buf[i]);
+    ws.buf[i] = nullptr;
+    ws.cap[i] = 0;
+  }
+  if (ws.st) cudaStreamDestroy(ws.st);
+  ws.st = nullptr;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -514,6 +514,9 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
                              const double* anchor_xy, uint32_t dilation, uint32_t erosion,
                              int device, bf_raster* rasters, uint64_t** words, uint64_t* n_words);
 void bf_contour_free(uint64_t* words);
+/* bf_contour_rasters keeps its device buffers and stream per device between
+ * calls (they only grow); this releases them. */
+void bf_contour_release(int device);
 
 /* Steps 4-5 of generate_sparse_contour_anchored (sparse_contour.rs:770-830,
  * 831-1183) on the rasters of bf_contour_rasters, one host thread per

@@ -26,6 +26,11 @@ def test_rasters_match_oracle(built, dil, ero):
     for (gc, go), (wc, wo) in zip(got, want):
         assert go == tuple(wo)
         assert np.array_equal(gc, wc)
+    # a call after releasing the kept buffers allocates them again
+    bfphast.load().bf_contour_release(0)
+    again = bfphast.contour_rasters(isos[:3], dil, ero)
+    for (gc, _), (wc, _) in zip(again, want[:3]):
+        assert np.array_equal(gc, wc)
 
 
 def test_empty_and_single_point_isochrones(built):
