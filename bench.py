@@ -407,102 +407,63 @@ def run_isochrones(g, cch, count, seed=42):
 
 
 def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
-    """Isochrone polygons for `count` origins: the contour rasters (steps
-    1-3 of the reference's contour pipeline) in one bf_contour_rasters call,
-    then tracing and simplification in one bf_contour_polygons call: settled
-    sets from bf_phast_bounded_seeded, reachable road segments whole or cut
-    at the threshold as build_isochrone_geometry_sparse does (f32 cut
-    fraction), on synthetic lattice coordinates (about 100 m spacing, each
-    road a straight tail -> head polyline; intersections projected once, cut
-    points per query). Distances are deciseconds (the graph's unit); the
-    contour tier comes from the threshold in seconds. A sample of isochrones
-    is checked cell for cell against the oracle, which is timed as the CPU
-    baseline."""
+    """Isochrone polygons for `count` origins through bf_isochrone_polygons:
+    settled sets in bulk, each reachable road whole or cut at the threshold
+    (the reference's f32 cut), contour rasters on the GPU, tracing and
+    simplification on host threads. Road geometry: synthetic lattice
+    coordinates (about 100 m spacing), each road a straight tail -> head
+    polyline, the fixture's node weights. Distances are deciseconds (the
+    graph's unit); the contour tier comes from the threshold in seconds. The
+    whole call runs once as warm-up, then is timed. A sample of origins is
+    checked ring for ring against the oracle's pipeline from the origin
+    (bounded query, then build_isochrone_geometry_sparse), which is timed on
+    one host thread as the CPU baseline."""
     import numpy as np
     import bfphast
     from oracle import oracle as orc
     geo = cch.pop("geo")
-    tail, head, nw = geo["state_tail"], geo["state_head"], geo["node_weight"]
-    ii = np.arange(geo["n_intersections"], dtype=np.int64)
-    lat_e7 = (500_000_000 + (ii // cols) * 9000).astype(np.int64)
-    lon_e7 = (30_000_000 + (ii % cols) * 14000).astype(np.int64)
-    ix, iy = orc.mercator(lat_e7 / 1e7, lon_e7 / 1e7)
     r2s = cch["rank_to_state"]
-    origins = np.random.default_rng(seed).integers(0, cch["n"], count)
-    threshold = 10 * threshold_s
-    cell, dil, ero, simp = orc.contour_config("car", threshold_s)
-    xy_parts, len_parts, iso_seg, anchors, e7 = [], [], [0], [], []
-    t_query = 0.0
-    for o in origins:
-        t0 = time.perf_counter()
-        rk, ds = g.phast_bounded_seeded([(int(o), 0)], threshold)
-        t_query += time.perf_counter() - t0
-        st = r2s[rk]
-        w = nw[st].astype(np.int64)
-        keep = (w != 0) & (w != 0xFFFFFFFF)
-        st, d, w = st[keep], ds[keep].astype(np.int64), w[keep]
-        a, b = tail[st], head[st]
-        i0 = int(np.argmin(d))  # first minimum in settled (rank) order
-        anchors.append((ix[a[i0]], iy[a[i0]]))
-        frac = (threshold - d).astype(np.float32) / w.astype(np.float32)
-        whole = (d + w <= threshold) | (frac >= np.float32(1.0))
-        cut = ~whole & (frac > np.float32(0.0))
-        clat = lat_e7[a[cut]] + np.trunc((lat_e7[b[cut]] - lat_e7[a[cut]]).astype(np.float32)
-                                         * frac[cut]).astype(np.int64)
-        clon = lon_e7[a[cut]] + np.trunc((lon_e7[b[cut]] - lon_e7[a[cut]]).astype(np.float32)
-                                         * frac[cut]).astype(np.int64)
-        cx, cy = orc.mercator(clat / 1e7, clon / 1e7)
-        wa, wb, ca = a[whole], b[whole], a[cut]
-        pts = np.empty((2 * (len(wa) + len(ca)), 2))
-        pts[0:2 * len(wa):2] = np.stack([ix[wa], iy[wa]], 1)
-        pts[1:2 * len(wa):2] = np.stack([ix[wb], iy[wb]], 1)
-        pts[2 * len(wa)::2] = np.stack([ix[ca], iy[ca]], 1)
-        pts[2 * len(wa) + 1::2] = np.stack([cx, cy], 1)
-        xy_parts.append(pts)
-        len_parts.append(np.full(len(wa) + len(ca), 2, np.uint64))
-        iso_seg.append(iso_seg[-1] + len(wa) + len(ca))
-        e7.append((lat_e7, lon_e7, wa, wb, ca, clat, clon, a[i0]))
-    import torch
-    n_pts = sum(len(p) for p in xy_parts)
-    xy = torch.empty((n_pts, 2), dtype=torch.float64, pin_memory=True).numpy()  # page-locked
-    np.concatenate(xy_parts, out=xy)
-    seg_pt = np.concatenate([[0], np.cumsum(np.concatenate(len_parts))]).astype(np.uint64)
-    has, anc = np.ones(count, np.uint8), np.asarray(anchors)
-    warm = bfphast.contour_rasters_flat(xy, seg_pt, iso_seg, [cell] * count, dil, ero, has, anc)
-    bfphast.contour_polygons(*warm, [cell] * count, [simp] * count, has, anc)  # warm-up
+    ii = np.arange(geo["n_intersections"], dtype=np.int64)
+    lat = (500_000_000 + (ii // cols) * 9000).astype(np.int32)
+    lon = (30_000_000 + (ii % cols) * 14000).astype(np.int32)
+    tail, head = geo["state_tail"][r2s], geo["state_head"][r2s]
+    poly = np.stack([np.stack([lat[tail], lon[tail]], 1), np.stack([lat[head], lon[head]], 1)],
+                    1).reshape(-1, 2)
+    off = np.arange(0, 2 * len(r2s) + 1, 2, dtype=np.uint64)
+    w = np.ascontiguousarray(geo["node_weight"][r2s], np.uint32)
     t0 = time.perf_counter()
-    ras, words = bfphast.contour_rasters_flat(xy, seg_pt, iso_seg, [cell] * count, dil, ero,
-                                              has, anc)
-    gpu_s = time.perf_counter() - t0
+    gm = bfphast.Geometry(off, poly, w)
+    geo_ms = (time.perf_counter() - t0) * 1e3
+    origins = np.random.default_rng(seed).integers(0, cch["n"], count).astype(np.uint32)
+    thr = np.full(count, 10 * threshold_s, np.uint32)
+    tiers = np.full(count, threshold_s, np.uint32)
+    bfphast.isochrone_polygons(g, gm, origins, thr, tiers)  # warm-up
     t0 = time.perf_counter()
-    rings = bfphast.contour_polygons(ras, words, [cell] * count, [simp] * count, has, anc)
-    poly_s = time.perf_counter() - t0
-    # oracle on a sample: the same segments in (lat_e7, lon_e7)
+    rings, ph = bfphast.isochrone_polygons(g, gm, origins, thr, tiers)
+    sec = time.perf_counter() - t0
+    c = orc.Cch.from_dict(cch)
     pick = [0, count // 2, count - 1][:count]
     exact, cpu_s = True, 0.0
     for k in pick:
-        la, lo, wa, wb, ca, clat, clon, a0 = e7[k]
-        segs = [[(int(la[p]), int(lo[p])), (int(la[q]), int(lo[q]))] for p, q in zip(wa, wb)]
-        segs += [[(int(la[p]), int(lo[p])), (int(y), int(x))] for p, y, x in zip(ca, clat, clon)]
-        want, _ = orc.sparse_closed(segs, cell, dil, ero, (int(la[a0]), int(lo[a0])))
-        exact = exact and bool(np.array_equal(bfphast.raster_cells(ras[k], words), want))
         t0 = time.perf_counter()
-        ring = orc.sparse_contour(segs, cell, dil, ero, simp, (int(la[a0]), int(lo[a0])))
+        rk, ds = c.bounded_seeded([(int(origins[k]), 0)], int(thr[k]))
+        want, _, _ = orc.isochrone_geometry(rk, ds, int(thr[k]), w, off, poly,
+                                            "car", tier=threshold_s)
         cpu_s += time.perf_counter() - t0
-        exact = exact and bool(np.array_equal(rings[k], ring))
-    n_seg = int(iso_seg[-1])
+        exact = exact and bool(np.array_equal(rings[k], want))
+    cell, dil, ero, simp = bfphast.contour_config(bfphast.MODE_CAR, threshold_s)
     return {"isochrones": count, "threshold_s": threshold_s, "cell_m": cell,
-            "morphology": [dil, ero], "segments": n_seg,
-            "raster_words": int(len(words)), "value": round(count / (gpu_s + poly_s), 1),
-            "unit": "polygons/s", "ms": round((gpu_s + poly_s) * 1e3, 2),
-            "rasters_ms": round(gpu_s * 1e3, 2), "polygons_ms": round(poly_s * 1e3, 2),
-            "segments_per_s": round(n_seg / gpu_s, 1),
+            "morphology": [dil, ero], "value": round(count / sec, 1), "unit": "polygons/s",
+            "ms": round(sec * 1e3, 2),
+            "phases_ms": {"settled_sets": round(ph[0], 2), "segments": round(ph[1], 2),
+                          "rasters": round(ph[2], 2), "polygons": round(ph[3], 2)},
             "mean_ring_vertices": round(float(np.mean([len(r) for r in rings])), 1),
-            "settled_sets_ms": round(t_query * 1e3, 1),
+            "geometry_create_ms": round(geo_ms, 1),
             "bit_exact_sample": {"isochrones": len(pick), "equal": exact},
             "cpu_baseline": {"value": round(len(pick) / cpu_s, 3), "unit": "polygons/s",
                              "cores": 1, "kind": "port",
-                             "sample": "%d isochrones of the batch, %.1f s" % (len(pick), cpu_s)},
+                             "sample": "%d origins of the batch from the origin (bounded query "
+                                       "and geometry), %.1f s" % (len(pick), cpu_s)},
             "data": "synthetic lattice coordinates, straight tail -> head road polylines"}
 
 

@@ -27,6 +27,7 @@ BF_OK, BF_ERR_INVALID, BF_ERR_OOM, BF_ERR_DEVICE, BF_ERR_TIMEOUT, BF_ERR_CANCELL
 ENGINE_AUTO, ENGINE_PLAIN, ENGINE_BATCHED = 0, 1, 2
 FLAG_REVERSE = 1
 CCH_SEARCH_TARGETS = 1
+MODE_CAR, MODE_BIKE, MODE_FOOT = 0, 1, 2
 REQ_MATRIX, REQ_ISOCHRONE = 1, 2
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
@@ -191,6 +192,10 @@ _SIGNATURES = {
                                                    ctypes.c_void_p, ctypes.c_uint64,
                                                    ctypes.c_void_p, ctypes.c_void_p,
                                                    ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "bf_isochrone_settled": (ctypes.c_int, [ctypes.c_void_p, _u32p, _u32p, ctypes.c_uint64, _u64p,
+                                            ctypes.POINTER(_u32p), ctypes.POINTER(_u32p),
+                                            ctypes.POINTER(Stats)]),
+    "bf_settled_free": (None, [_u32p]),
     "bf_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerCfg),
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "bf_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Request), _u64p]),
@@ -220,6 +225,17 @@ _SIGNATURES = {
                                            ctypes.c_void_p, _u64p,
                                            ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]),
     "bf_contour_free_polygons": (None, [ctypes.POINTER(ctypes.c_double)]),
+    "bf_contour_config": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.POINTER(ctypes.c_double), _u32p, _u32p,
+                                         ctypes.POINTER(ctypes.c_double)]),
+    "bf_mercator": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]),
+    "bf_geometry_create": (ctypes.c_int, [ctypes.c_uint32, _u64p, ctypes.c_void_p, _u32p,
+                                          ctypes.POINTER(ctypes.c_void_p)]),
+    "bf_geometry_destroy": (None, [ctypes.c_void_p]),
+    "bf_isochrone_polygons": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _u32p, _u32p,
+                                             ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                             _u64p, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
+                                             ctypes.c_void_p]),
     "bf_last_error": (ctypes.c_char_p, []),
 }
 
@@ -444,6 +460,25 @@ class Graph:
                                                   _ptr(tm), _ptr(ln), cap, ctypes.byref(cnt)))
         c = cnt.value
         return rk[:c].copy(), tm[:c].copy(), ln[:c].copy()
+
+    def isochrone_settled(self, origins, thresholds, stats=False):
+        """bf_isochrone_settled: per origin (ranks, dists) within its
+        threshold, ranks ascending (the bounded single query's output)."""
+        o, t = _u32(origins), _u32(thresholds)
+        off = np.zeros(len(o) + 1, np.uint64)
+        r, d = _u32p(), _u32p()
+        st = Stats()
+        _check(load().bf_isochrone_settled(self._h, _ptr(o), _ptr(t), len(o), _ptr(off, _u64p),
+                                           ctypes.byref(r), ctypes.byref(d), ctypes.byref(st)))
+        try:
+            total = int(off[-1])
+            ranks = np.ctypeslib.as_array(r, shape=(max(total, 1),))[:total].copy()
+            dists = np.ctypeslib.as_array(d, shape=(max(total, 1),))[:total].copy()
+        finally:
+            load().bf_settled_free(r)
+            load().bf_settled_free(d)
+        out = [(ranks[off[i]:off[i + 1]], dists[off[i]:off[i + 1]]) for i in range(len(o))]
+        return (out, st.as_dict()) if stats else out
 
     def isochrone_bitsets(self, origins, thresholds, stats=False):
         o, t = _u32(origins), _u32(thresholds)
@@ -701,3 +736,64 @@ def contour_polygons(rasters, words, cell_m, simplify_m, has_anchor=None, anchor
     finally:
         lib.bf_contour_free_polygons(out)
     return [flat[2 * int(off[k]):2 * int(off[k + 1])].reshape(-1, 2) for k in range(n)]
+
+
+def contour_config(mode, threshold_s):
+    """bf_contour_config: (cell_m, dilation, erosion, simplify_m)."""
+    c, s = ctypes.c_double(), ctypes.c_double()
+    d, e = ctypes.c_uint32(), ctypes.c_uint32()
+    _check(load().bf_contour_config(int(mode), int(threshold_s), ctypes.byref(c), ctypes.byref(d),
+                                    ctypes.byref(e), ctypes.byref(s)))
+    return c.value, d.value, e.value, s.value
+
+
+def mercator(lat_lon_e7):
+    """bf_mercator: (n, 2) (lat_e7, lon_e7) -> (n, 2) (x, y) metres."""
+    p = np.ascontiguousarray(lat_lon_e7, np.int32).reshape(-1, 2)
+    out = np.empty((len(p), 2), np.float64)
+    _check(load().bf_mercator(len(p), p.ctypes.data, out.ctypes.data))
+    return out
+
+
+class Geometry:
+    """Road polylines per rank for bf_isochrone_polygons (owns a bf_geometry)."""
+
+    def __init__(self, poly_off, poly_e7, node_w):
+        off = np.ascontiguousarray(poly_off, np.uint64)
+        pts = np.ascontiguousarray(poly_e7, np.int32).reshape(-1, 2)
+        w = _u32(node_w)
+        h = ctypes.c_void_p()
+        _check(load().bf_geometry_create(len(off) - 1, _ptr(off, _u64p), pts.ctypes.data, _ptr(w),
+                                         ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bf_geometry_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def isochrone_polygons(graph, geometry, origins, thresholds, tier_thresholds=None, mode=MODE_CAR):
+    """bf_isochrone_polygons: one (lon, lat) ring per origin and the phase
+    times (settled, segments, rasters, polygons) in ms."""
+    lib = load()
+    o, t = _u32(origins), _u32(thresholds)
+    tt = None if tier_thresholds is None else _u32(tier_thresholds)
+    off = np.zeros(len(o) + 1, np.uint64)
+    out = ctypes.POINTER(ctypes.c_double)()
+    ph = np.zeros(4)
+    _check(lib.bf_isochrone_polygons(graph._h, geometry._h, _ptr(o), _ptr(t),
+                                     None if tt is None else tt.ctypes.data, len(o), int(mode),
+                                     _ptr(off, _u64p), ctypes.byref(out), ph.ctypes.data))
+    try:
+        total = int(off[-1])
+        flat = np.ctypeslib.as_array(out, shape=(max(2 * total, 1),))[:2 * total].copy()
+    finally:
+        lib.bf_contour_free_polygons(out)
+    return [flat[2 * int(off[k]):2 * int(off[k + 1])].reshape(-1, 2) for k in range(len(o))], ph

@@ -787,6 +787,97 @@ bf_status bf_isochrone_bitsets(bf_graph* h, const uint32_t* orig, const uint32_t
   return BF_OK;
 }
 
+bf_status bf_isochrone_settled(bf_graph* h, const uint32_t* orig, const uint32_t* thr, uint64_t n,
+                               uint64_t* offsets, uint32_t** ranks, uint32_t** dists,
+                               bf_stats* st) {
+  if (ranks) *ranks = nullptr;
+  if (dists) *dists = nullptr;
+  if (!h || !offsets || !ranks || !dists || (n && (!orig || !thr))) {
+    set_error("bf_isochrone_settled: null argument");
+    return BF_ERR_INVALID;
+  }
+  double t0 = now_s();
+  Graph* g = &h->g;
+  bf_status rc;
+  if ((rc = check_ids(orig, n, g->n, "origins"))) return rc;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t s = g->stream;
+  const uint64_t w64 = (g->n + 63) / 64;
+  uint64_t chunk = std::max<uint64_t>(32, (8ull << 30) / (w64 * 8));
+  chunk = std::min<uint64_t>(chunk, std::max<uint64_t>(n, 1));
+  const size_t need = chunk * (4 + 4 + 8) + chunk * w64 * 8;
+  if (need > g->iso_bytes) {
+    if (g->d_iso) {
+      cudaFree(g->d_iso);
+      g->device_bytes -= g->iso_bytes;
+      g->d_iso = nullptr;
+      g->iso_bytes = 0;
+    }
+    if (cudaMalloc(&g->d_iso, need) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc of " + std::to_string(need) + " bytes for isochrone I/O failed");
+      return BF_ERR_OOM;
+    }
+    g->iso_bytes = need;
+    g->device_bytes += need;
+  }
+  uint64_t* d_bits = reinterpret_cast<uint64_t*>(g->d_iso);
+  uint64_t* d_counts = d_bits + chunk * w64;
+  uint32_t* d_orig = reinterpret_cast<uint32_t*>(d_counts + chunk);
+  uint32_t* d_thr = d_orig + chunk;
+  std::vector<std::vector<uint32_t>> all_r(n), all_d(n);
+  for (uint64_t c0 = 0; c0 < n; c0 += chunk) {
+    const uint64_t m = std::min<uint64_t>(chunk, n - c0);
+    SettledSink sink;
+    sink.ranks.resize(m);
+    sink.dists.resize(m);
+    BF_CUDA(cudaMemcpyAsync(d_orig, orig + c0, m * 4, cudaMemcpyHostToDevice, s));
+    BF_CUDA(cudaMemcpyAsync(d_thr, thr + c0, m * 4, cudaMemcpyHostToDevice, s));
+    try {
+      if ((rc = isochrone_bitsets(g, g->ctx, d_orig, d_thr, m, d_bits, d_counts, s, st, &sink)))
+        return rc;
+    } catch (const std::bad_alloc&) {
+      set_error("out of host memory");
+      return BF_ERR_OOM;
+    }
+    for (uint64_t i = 0; i < m; ++i) {
+      all_r[c0 + i].swap(sink.ranks[i]);
+      all_d[c0 + i].swap(sink.dists[i]);
+    }
+  }
+  if ((rc = check_device_error(g, s))) return rc;
+  offsets[0] = 0;
+  for (uint64_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + all_r[i].size();
+  const uint64_t total = offsets[n];
+  uint32_t* r = (uint32_t*)std::malloc(std::max<uint64_t>(total, 1) * 4);
+  uint32_t* d = (uint32_t*)std::malloc(std::max<uint64_t>(total, 1) * 4);
+  if (!r || !d) {
+    std::free(r);
+    std::free(d);
+    set_error("out of host memory");
+    return BF_ERR_OOM;
+  }
+  for (uint64_t i = 0; i < n; ++i) {
+    if (all_r[i].empty()) continue;
+    std::memcpy(r + offsets[i], all_r[i].data(), all_r[i].size() * 4);
+    std::memcpy(d + offsets[i], all_d[i].data(), all_d[i].size() * 4);
+  }
+  *ranks = r;
+  *dists = d;
+  if (st) {
+    st->n_sources = n;
+    st->n_targets = g->n;
+    st->h2d_bytes = n * 8;
+    st->d2h_bytes = total * 8;
+    st->total_ms = (now_s() - t0) * 1e3;
+  }
+  return BF_OK;
+}
+
+void bf_settled_free(uint32_t* p) { std::free(p); }
+
 const char* bf_last_error(void) { return t_err.c_str(); }
 
 }  // extern "C"

@@ -18,6 +18,7 @@
 #include <climits>
 #include <tuple>
 #include <cstdlib>
+#include <cstring>
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -835,5 +836,296 @@ bf_status bf_contour_polygons(const bf_raster* rasters, const uint64_t* words, u
 }
 
 void bf_contour_free_polygons(double* lonlat) { std::free(lonlat); }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Isochrone polygons end to end: settled sets of every origin (bulk waves),
+// the reachable road segments of each (whole, or cut at the threshold, as
+// build_isochrone_geometry_sparse does, server/geometry.rs:281-418), the
+// contour rasters on the GPU, tracing and simplification on host threads.
+
+#include <chrono>
+
+struct bf_geometry {
+  uint32_t n = 0;
+  std::vector<uint64_t> off;   // polyline of rank r: points [off[r], off[r + 1])
+  std::vector<int32_t> e7;     // (lat_e7, lon_e7) per point
+  std::vector<double> xy;      // Web-Mercator (x, y) per point
+  std::vector<uint32_t> w;     // traversal weight per rank
+};
+
+namespace {
+
+// to_mercator (sparse_contour.rs:441-445): to_radians is x * (PI / 180).
+void mercator_e7(int32_t lat_e7, int32_t lon_e7, double* x, double* y) {
+  const double lat = (double)lat_e7 / 1e7, lon = (double)lon_e7 / 1e7;
+  *x = lon * (PI_D / 180.0) * EARTH_R;
+  *y = std::log(std::tan(lat * (PI_D / 180.0) / 2.0 + PI_D / 4.0)) * EARTH_R;
+}
+
+template <class F>
+void parallel_for(uint64_t n, F&& f) {
+  const unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(),
+                                                      (unsigned)std::min<uint64_t>(n, 64)));
+  std::atomic<uint64_t> next{0};
+  auto work = [&]() {
+    for (uint64_t i; (i = next.fetch_add(1)) < n;) f(i);
+  };
+  std::vector<std::thread> pool;
+  for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+// SparseContourConfig::for_mode_name_with_threshold (sparse_contour.rs:476-546).
+bf_status bf_contour_config(uint32_t mode, uint32_t threshold_s, double* cell_m,
+                            uint32_t* dilation, uint32_t* erosion, double* simplify_m) {
+  if (!cell_m || !dilation || !erosion || !simplify_m) {
+    set_error("bf_contour_config: null argument");
+    return BF_ERR_INVALID;
+  }
+  double cell = 30.0, simp = 30.0;
+  uint32_t d = 2, e = 2;
+  if (mode == BF_MODE_BIKE) {
+    cell = simp = 40.0;
+    d = e = 3;
+  } else if (mode == BF_MODE_FOOT) {
+    cell = simp = 25.0;
+    d = e = 3;
+  }
+  double cm = 1.0, sm = 1.0;
+  if (threshold_s > 3600) {
+    cm = 6.67;
+    sm = 8.0;
+  } else if (threshold_s > 1800) {
+    cm = sm = 4.0;
+  } else if (threshold_s > 600) {
+    cm = sm = 2.0;
+  }
+  *cell_m = cell * cm;
+  *simplify_m = simp * sm;
+  *dilation = d;
+  *erosion = e;
+  return BF_OK;
+}
+
+bf_status bf_mercator(uint64_t n, const int32_t* lat_lon_e7, double* xy) {
+  if (n && (!lat_lon_e7 || !xy)) {
+    set_error("bf_mercator: null argument");
+    return BF_ERR_INVALID;
+  }
+  parallel_for((n + 65535) / 65536, [&](uint64_t b) {
+    for (uint64_t i = b * 65536; i < std::min<uint64_t>(n, (b + 1) * 65536); ++i)
+      mercator_e7(lat_lon_e7[2 * i], lat_lon_e7[2 * i + 1], xy + 2 * i, xy + 2 * i + 1);
+  });
+  return BF_OK;
+}
+
+bf_status bf_geometry_create(uint32_t n_nodes, const uint64_t* poly_off, const int32_t* poly_e7,
+                             const uint32_t* node_w, bf_geometry** out) {
+  if (out) *out = nullptr;
+  if (!poly_off || !node_w || !out || (poly_off[n_nodes] && !poly_e7)) {
+    set_error("bf_geometry_create: null argument");
+    return BF_ERR_INVALID;
+  }
+  for (uint32_t r = 0; r < n_nodes; ++r)
+    if (poly_off[r + 1] < poly_off[r]) {
+      set_error("bf_geometry_create: polyline offsets must be non-decreasing");
+      return BF_ERR_INVALID;
+    }
+  bf_geometry* geo = new (std::nothrow) bf_geometry();
+  if (!geo) {
+    set_error("out of host memory");
+    return BF_ERR_OOM;
+  }
+  try {
+    const uint64_t np = poly_off[n_nodes];
+    geo->n = n_nodes;
+    geo->off.assign(poly_off, poly_off + n_nodes + 1);
+    geo->e7.assign(poly_e7, poly_e7 + 2 * np);
+    geo->w.assign(node_w, node_w + n_nodes);
+    geo->xy.resize(2 * np);
+    bf_mercator(np, poly_e7, geo->xy.data());  // static vertices: projected once
+  } catch (const std::bad_alloc&) {
+    delete geo;
+    set_error("out of host memory");
+    return BF_ERR_OOM;
+  }
+  *out = geo;
+  return BF_OK;
+}
+
+void bf_geometry_destroy(bf_geometry* geo) { delete geo; }
+
+bf_status bf_isochrone_polygons(bf_graph* g, const bf_geometry* geo, const uint32_t* origins,
+                                const uint32_t* thresholds, const uint32_t* tier_thresholds,
+                                uint64_t n, uint32_t mode, uint64_t* ring_off, double** lonlat,
+                                double* phase_ms) {
+  if (lonlat) *lonlat = nullptr;
+  if (!g || !geo || !ring_off || !lonlat || (n && (!origins || !thresholds))) {
+    set_error("bf_isochrone_polygons: null argument");
+    return BF_ERR_INVALID;
+  }
+  Graph* gr = graph_of(g);
+  if (geo->n != gr->n) {
+    set_error("bf_isochrone_polygons: the geometry has a polyline per rank of another graph");
+    return BF_ERR_INVALID;
+  }
+  if (n > 0xFFFFFFFFull) {
+    set_error("bf_isochrone_polygons: too many origins in one call");
+    return BF_ERR_INVALID;
+  }
+  using clk = std::chrono::steady_clock;
+  auto ms = [](clk::time_point a) {
+    return std::chrono::duration<double, std::milli>(clk::now() - a).count();
+  };
+  double ph[4] = {0, 0, 0, 0};
+  auto t0 = clk::now();
+  // 1. settled sets of every origin
+  std::vector<uint64_t> soff(n + 1, 0);
+  uint32_t *sr = nullptr, *sd = nullptr;
+  bf_status rc = bf_isochrone_settled(g, origins, thresholds, n, soff.data(), &sr, &sd, nullptr);
+  if (rc) return rc;
+  ph[0] = ms(t0);
+  t0 = clk::now();
+  // 2. reachable segments (host threads): one walk per isochrone counts,
+  // a second writes the points straight into a page-locked buffer kept
+  // across calls (it is also the rasters' upload source)
+  std::vector<double> cell(n), simp(n);
+  uint32_t dil = 0, ero = 0;
+  for (uint64_t k = 0; k < n; ++k)
+    bf_contour_config(mode, tier_thresholds ? tier_thresholds[k] : thresholds[k], &cell[k], &dil,
+                      &ero, &simp[k]);
+  std::vector<uint64_t> nseg(n, 0), npts(n, 0);
+  std::vector<uint8_t> has(n, 0);
+  std::vector<double> anc(2 * n, 0.0);
+  // walk(k, f): f(p0, take, cut, clat, clon) for every stamped road of isochrone k
+  auto walk = [&](uint64_t k, auto&& f) {
+    const uint32_t T = thresholds[k];
+    uint32_t best = 0xFFFFFFFFu;
+    for (uint64_t i = soff[k]; i < soff[k + 1]; ++i) {
+      const uint32_t r = sr[i], d = sd[i];
+      if (d > T) continue;
+      const uint32_t w = geo->w[r];
+      if (w == 0 || w == 0xFFFFFFFFu) continue;
+      const uint64_t p0 = geo->off[r], np = geo->off[r + 1] - p0;
+      if (np == 0) continue;
+      if (d < best) {
+        best = d;
+        has[k] = 1;
+        anc[2 * k] = geo->xy[2 * p0];
+        anc[2 * k + 1] = geo->xy[2 * p0 + 1];
+      }
+      const uint32_t d_end = (d + w < d) ? 0xFFFFFFFFu : d + w;
+      uint64_t take = np;  // whole polyline
+      bool cut = false;
+      int32_t clat = 0, clon = 0;
+      if (d_end > T) {  // frontier road: the reference's f32 cut
+        const float frac = (float)(T - d) / (float)w;
+        if (frac <= 0.0f) continue;
+        if (np > 1 && frac < 1.0f) {
+          const uint64_t nsg = np - 1;
+          const float sf = frac * (float)nsg;
+          const uint64_t si = std::min<uint64_t>((uint64_t)std::floor(sf), nsg - 1);
+          const float lf = sf - (float)si;
+          take = si + 1;
+          if (lf > 0.0f && si + 1 < np) {
+            const int32_t* a = &geo->e7[2 * (p0 + si)];
+            const int32_t* b = a + 2;
+            clat = a[0] + (int32_t)((float)(b[0] - a[0]) * lf);
+            clon = a[1] + (int32_t)((float)(b[1] - a[1]) * lf);
+            cut = true;
+          }
+        } else if (np == 1) {
+          take = 1;
+        }
+      }
+      f(p0, take, cut, clat, clon);
+    }
+  };
+  parallel_for(n, [&](uint64_t k) {
+    walk(k, [&](uint64_t, uint64_t take, bool cut, int32_t, int32_t) {
+      ++nseg[k];
+      npts[k] += take + (cut ? 1 : 0);
+    });
+  });
+  std::vector<uint64_t> iso_seg(n + 1, 0), pt_base(n + 1, 0);
+  for (uint64_t k = 0; k < n; ++k) {
+    iso_seg[k + 1] = iso_seg[k] + nseg[k];
+    pt_base[k + 1] = pt_base[k] + npts[k];
+  }
+  const uint64_t n_pts = pt_base[n];
+  static std::mutex stage_mu;  // the page-locked staging of this entry point
+  static double* stage_xy = nullptr;
+  static uint64_t stage_cap = 0;
+  static std::vector<uint64_t> seg_pt;
+  std::lock_guard<std::mutex> stage_lk(stage_mu);
+  if (stage_cap < n_pts) {
+    if (stage_xy) cudaFreeHost(stage_xy);
+    stage_xy = nullptr;
+    stage_cap = 0;
+    const uint64_t want = n_pts + n_pts / 4;
+    if (cudaHostAlloc((void**)&stage_xy, std::max<uint64_t>(want, 1) * 16, cudaHostAllocDefault) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      bf_settled_free(sr);
+      bf_settled_free(sd);
+      set_error("bf_isochrone_polygons: page-locked staging allocation failed");
+      return BF_ERR_OOM;
+    }
+    stage_cap = want;
+  }
+  try {
+    seg_pt.resize(iso_seg[n] + 1);
+  } catch (const std::bad_alloc&) {
+    bf_settled_free(sr);
+    bf_settled_free(sd);
+    set_error("out of host memory");
+    return BF_ERR_OOM;
+  }
+  seg_pt[0] = 0;
+  parallel_for(n, [&](uint64_t k) {
+    uint64_t s = iso_seg[k], p = pt_base[k];
+    walk(k, [&](uint64_t p0, uint64_t take, bool cut, int32_t clat, int32_t clon) {
+      std::memcpy(stage_xy + 2 * p, geo->xy.data() + 2 * p0, take * 16);
+      p += take;
+      if (cut) {
+        mercator_e7(clat, clon, stage_xy + 2 * p, stage_xy + 2 * p + 1);
+        ++p;
+      }
+      seg_pt[++s] = p;
+    });
+  });
+  bf_settled_free(sr);
+  bf_settled_free(sd);
+  for (uint64_t k = 0; k < n; ++k)
+    if (!nseg[k]) has[k] = 0;  // no segment: the reference returns no contour
+  const double* xy = stage_xy;
+  ph[1] = ms(t0);
+  t0 = clk::now();
+  // 3. rasters (GPU)
+  std::vector<bf_raster> ras(std::max<uint64_t>(n, 1));
+  uint64_t* words = nullptr;
+  uint64_t n_words = 0;
+  if ((rc = bf_contour_rasters(xy, seg_pt.data(), iso_seg.data(), (uint32_t)n, cell.data(),
+                               has.data(), anc.data(), dil, ero, gr->device, ras.data(), &words,
+                               &n_words)))
+    return rc;
+  ph[2] = ms(t0);
+  t0 = clk::now();
+  // 4. polygons (host threads)
+  rc = bf_contour_polygons(ras.data(), words, (uint32_t)n, cell.data(), simp.data(), has.data(),
+                           anc.data(), ring_off, lonlat);
+  bf_contour_free(words);
+  ph[3] = ms(t0);
+  if (phase_ms)
+    for (int i = 0; i < 4; ++i) phase_ms[i] = ph[i];
+  return rc;
+}
 
 }  // extern "C"

@@ -301,9 +301,25 @@ bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, co
                          bf_stats* stats);
 
 // isochrone.cu
+// Settled (rank, distance) lists of bulk isochrones, filled wave by wave:
+// per origin of the call (its index in the call), ranks ascending.
+struct SettledSink {
+  std::vector<std::vector<uint32_t>> ranks, dists;
+  uint32_t* d_pre = nullptr;   // per lane, exclusive popcount prefix of its bitset words
+  size_t pre_bytes = 0;
+  uint32_t* d_out = nullptr;   // a wave's ranks, then its distances
+  size_t out_bytes = 0;
+  uint64_t* d_off = nullptr;   // a wave's lane offsets
+  size_t off_bytes = 0;
+  ~SettledSink() {
+    if (d_pre) cudaFree(d_pre);
+    if (d_out) cudaFree(d_out);
+    if (d_off) cudaFree(d_off);
+  }
+};
 bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
                             uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,
-                            bf_stats* stats);
+                            bf_stats* stats, SettledSink* sink = nullptr);
 
 // seeded.cu
 bf_status matrix_seeded(Graph* g, Ctx& c, const bf_seed* src_seeds, const uint64_t* src_off, uint64_t S,

@@ -296,6 +296,110 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Settled lists of a wave. Lane l's bitset (row lane_row[l] of `bits`, w32
+// words, ranks ascending) gives its settled ranks; k_lane_prefix turns word
+// popcounts into each word's first output position, k_emit writes
+// (rank, distance) pairs from the slab in rank order.
+__global__ void __launch_bounds__(1024)
+    k_lane_prefix(const uint32_t* __restrict__ bits, uint64_t w32,
+                  const uint32_t* __restrict__ lane_row, uint32_t* __restrict__ pre) {
+  __shared__ uint32_t wsum[32];
+  const uint32_t l = blockIdx.x;
+  const uint32_t* b = bits + (uint64_t)lane_row[l] * w32;
+  uint32_t* o = pre + (uint64_t)l * w32;
+  uint32_t carry = 0;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint64_t w0 = 0; w0 < w32; w0 += blockDim.x) {
+    const uint64_t w = w0 + threadIdx.x;
+    const uint32_t v = w < w32 ? __popc(b[w]) : 0;
+    uint32_t x = v;  // inclusive warp scan
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t s = lane < (blockDim.x >> 5) ? wsum[lane] : 0;
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, d);
+        if (lane >= d) s += y;
+      }
+      wsum[lane] = s;  // inclusive over warps
+    }
+    __syncthreads();
+    const uint32_t before = (warp ? wsum[warp - 1] : 0) + x - v;
+    if (w < w32) o[w] = carry + before;
+    carry += wsum[(blockDim.x >> 5) - 1];
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_emit(const T* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ cidx, uint32_t n,
+           const uint32_t* __restrict__ bits, uint64_t w32, const uint32_t* __restrict__ lane_row,
+           const uint32_t* __restrict__ pre, const uint64_t* __restrict__ lane_off,
+           uint64_t total, uint32_t* __restrict__ out_rank, uint32_t* __restrict__ out_dist) {
+  const uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint32_t l = blockIdx.y;
+  if (w >= w32) return;
+  uint32_t m = bits[(uint64_t)lane_row[l] * w32 + w];
+  if (!m) return;
+  uint64_t pos = lane_off[l] + pre[(uint64_t)l * w32 + w];
+  while (m) {
+    const uint32_t bit = __ffs(m) - 1;
+    m &= m - 1;
+    const uint32_t rank = (uint32_t)(w * 32 + bit);
+    if (rank < n && pos < total) {
+      out_rank[pos] = rank;
+      out_dist[pos] = (uint32_t)slab[(size_t)cidx[rank] * Kp + l];
+    }
+    ++pos;
+  }
+}
+
+template <typename T>
+bf_status emit_settled(const T* slab, uint32_t Kp, Graph* g, Sched& sc, const uint32_t* bits,
+                       uint64_t w32, const uint32_t* d_lane_row, const uint32_t* h_lane_row,
+                       uint32_t kw, const uint64_t* d_counts, uint64_t n_all, SettledSink* sink,
+                       cudaStream_t st) {
+  std::vector<uint64_t> cnt(n_all);
+  BF_CUDA(cudaMemcpyAsync(cnt.data(), d_counts, n_all * 8, cudaMemcpyDeviceToHost, st));
+  BF_CUDA(cudaStreamSynchronize(st));
+  std::vector<uint64_t> off(kw + 1, 0);
+  for (uint32_t l = 0; l < kw; ++l) off[l + 1] = off[l] + cnt[h_lane_row[l]];
+  const uint64_t total = off[kw];
+  auto grow = [&](auto** p, size_t& cap, size_t need) -> cudaError_t {
+    if (cap >= need) return cudaSuccess;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc((void**)p, need);
+    if (e == cudaSuccess) cap = need;
+    return e;
+  };
+  BF_CUDA(grow(&sink->d_pre, sink->pre_bytes, std::max<size_t>(16, (size_t)kw * w32 * 4)));
+  BF_CUDA(grow(&sink->d_out, sink->out_bytes, std::max<size_t>(16, (size_t)total * 8)));
+  BF_CUDA(grow(&sink->d_off, sink->off_bytes, (size_t)(kw + 1) * 8));
+  BF_CUDA(cudaMemcpyAsync(sink->d_off, off.data(), (kw + 1) * 8, cudaMemcpyHostToDevice, st));
+  k_lane_prefix<<<kw, 1024, 0, st>>>(bits, w32, d_lane_row, sink->d_pre);
+  dim3 eg((unsigned)((w32 + 255) / 256), kw);
+  k_emit<T><<<eg, 256, 0, st>>>(slab, Kp, sc.d_cidx, g->n, bits, w32, d_lane_row, sink->d_pre,
+                                sink->d_off, total, sink->d_out, sink->d_out + total);
+  BF_CUDA(cudaGetLastError());
+  std::vector<uint32_t> h(2 * total);
+  if (total)
+    BF_CUDA(cudaMemcpyAsync(h.data(), sink->d_out, total * 8, cudaMemcpyDeviceToHost, st));
+  BF_CUDA(cudaStreamSynchronize(st));
+  for (uint32_t l = 0; l < kw; ++l) {
+    const uint32_t o = h_lane_row[l];
+    sink->ranks[o].assign(h.begin() + off[l], h.begin() + off[l + 1]);
+    sink->dists[o].assign(h.begin() + total + off[l], h.begin() + total + off[l + 1]);
+  }
+  return BF_OK;
+}
+
 }  // namespace
 
 // d_bits: n rows of ceil(n_nodes / 64) u64 words; d_counts: n u64.
@@ -304,7 +408,7 @@ __global__ void __launch_bounds__(256)
 // order, which keeps the set of active rows of the gated sweep small.
 bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
                             uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,
-                            bf_stats* stats) {
+                            bf_stats* stats, SettledSink* sink) {
   bf_status s;
   if ((s = build_schedule(g, c, c.full, nullptr, 0, true, st))) return s;
   Sched& sc = c.full;
@@ -425,6 +529,16 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
                                               d_active, p_row + s0);
     BF_CUDA(cudaGetLastError());
     ++launches;
+    if (sink) {
+      const uint32_t* h_rows = pk.data() + 2 * n + s0;
+      const uint32_t* bits32 = reinterpret_cast<const uint32_t*>(d_bits);
+      bf_status es = half ? emit_settled(slab16, Kp, g, sc, bits32, 2 * w64, p_row + s0, h_rows,
+                                         (uint32_t)kw, d_counts, n, sink, st)
+                          : emit_settled(c.d_slab, Kp, g, sc, bits32, 2 * w64, p_row + s0, h_rows,
+                                         (uint32_t)kw, d_counts, n, sink, st);
+      if (es) return es;
+      launches += 2;
+    }
     if (stats) {
       BF_CUDA(cudaEventRecord(c.ev[3], st));
       BF_CUDA(cudaEventSynchronize(c.ev[3]));

@@ -23,6 +23,7 @@
  *   bf_matrix_seeded_2ch   table_phast_lopsided_2ch                  bucket_ch.rs:6381-6521
  *   bf_phast_bounded_seeded_2ch run_phast_bounded_fast_seeded_2ch    isochrone_handler.rs:500-625
  *   bf_isochrone_bitsets   the PHAST part of isochrone_bulk_handler  isochrone_handler.rs:1668-1709
+ *   bf_isochrone_settled   run_phast_bounded_fast_seeded for many origins  isochrone_handler.rs:338
  *                          and BatchedIsochroneEngine::query_many    route/src/range/batched_isochrone.rs:216
  *   bf_server_*            the tiling / admission loop of do_matrix  route/src/server/flight.rs:589,957-1110
  *   bf_cch_customize       customize_cch_time_in_memory (weights)    route/src/customization.rs:571
@@ -30,6 +31,7 @@
  *   bf_cch_bottom_up       bottom_up_customize / _with_external_middles  customization.rs:1005, :953
  *   bf_contour_rasters     generate_sparse_contour_anchored, steps 1-3  route/src/range/sparse_contour.rs:650
  *   bf_contour_polygons    generate_sparse_contour_anchored, steps 4-5  sparse_contour.rs:770
+ *   bf_isochrone_polygons  build_isochrone_geometry for many origins  route/src/server/geometry.rs:239
  *
  * Conventions (as in the reference):
  *   - node ids are CCH ranks (rank-aligned CCH, node_id == rank);
@@ -344,6 +346,17 @@ bf_status bf_isochrone_bitsets_device(bf_graph* g, const uint32_t* d_origins,
                                       uint64_t* d_bits, uint64_t* d_counts, void* stream,
                                       bf_stats* st);
 
+/* Settled sets of bulk isochrones: for origin i, the ranks r with
+ * dist(origin_i, r) <= thresholds[i], ascending, and their distances — the
+ * run_phast_bounded_fast_seeded output (isochrone_handler.rs:338-491) of
+ * every origin, computed with the same waves as bf_isochrone_bitsets.
+ * Origin i owns entries [offsets[i], offsets[i + 1]) (n + 1 offsets) of
+ * *ranks and *dists, buffers released with bf_settled_free. */
+bf_status bf_isochrone_settled(bf_graph* g, const uint32_t* origins, const uint32_t* thresholds,
+                               uint64_t n_origins, uint64_t* offsets, uint32_t** ranks,
+                               uint32_t** dists, bf_stats* st);
+void bf_settled_free(uint32_t* p);
+
 /* ---- serving loop (continuous batching of matrix and isochrone requests) ---- */
 
 typedef struct bf_server bf_server;
@@ -531,6 +544,42 @@ bf_status bf_contour_polygons(const bf_raster* rasters, const uint64_t* words, u
                               const uint8_t* has_anchor, const double* anchor_xy,
                               uint64_t* ring_off, double** lonlat);
 void bf_contour_free_polygons(double* lonlat);
+
+/* ---- isochrone polygons end to end (server/geometry.rs:239-368) -----------
+ * Travel modes of SparseContourConfig (sparse_contour.rs:476-546). */
+enum { BF_MODE_CAR = 0, BF_MODE_BIKE = 1, BF_MODE_FOOT = 2 };
+
+/* SparseContourConfig::for_mode_name_with_threshold: cell size, closing
+ * rounds and simplification tolerance for a travel mode and threshold. */
+bf_status bf_contour_config(uint32_t mode, uint32_t threshold_s, double* cell_m,
+                            uint32_t* dilation, uint32_t* erosion, double* simplify_m);
+
+/* to_mercator (sparse_contour.rs:441-445) of n (lat_e7, lon_e7) points into
+ * (x, y) metres, on host threads with the host libm. */
+bf_status bf_mercator(uint64_t n, const int32_t* lat_lon_e7, double* xy);
+
+/* Road geometry per graph rank: rank r's polyline is points
+ * [poly_off[r], poly_off[r + 1]) of poly_e7 ((lat_e7, lon_e7) pairs), its
+ * traversal weight node_w[r] (the reference's node_weights: 0 or u32::MAX =
+ * not stamped). Vertices are projected once here. */
+typedef struct bf_geometry bf_geometry;
+bf_status bf_geometry_create(uint32_t n_nodes, const uint64_t* poly_off, const int32_t* poly_e7,
+                             const uint32_t* node_w, bf_geometry** out);
+void bf_geometry_destroy(bf_geometry* geo);
+
+/* build_isochrone_geometry for n origins: settled sets (bf_isochrone_settled),
+ * each settled road stamped whole or cut at the threshold with the
+ * reference's f32 fraction, the minimum-distance road's first vertex as the
+ * anchor, contour rasters (bf_contour_rasters) and polygons
+ * (bf_contour_polygons) with the configuration of `mode` at
+ * tier_thresholds[i] (NULL = thresholds, when both are in seconds). Ring i
+ * is points [ring_off[i], ring_off[i + 1]) of *lonlat, released with
+ * bf_contour_free_polygons. phase_ms (4 entries, may be NULL): settled sets,
+ * segments, rasters, polygons. */
+bf_status bf_isochrone_polygons(bf_graph* g, const bf_geometry* geo, const uint32_t* origins,
+                                const uint32_t* thresholds, const uint32_t* tier_thresholds,
+                                uint64_t n, uint32_t mode, uint64_t* ring_off, double** lonlat,
+                                double* phase_ms);
 
 const char* bf_last_error(void);
 

@@ -514,14 +514,17 @@ void orc_inverse_mercator(uint64_t n, const double* x, const double* y, double* 
 // (node i = points [poly_off[i], poly_off[i + 1])), the travel mode and an
 // optional snapped origin (lon, lat). Also returns the closed cell set
 // (col, row pairs, ascending by row then column, up to cell_cap) with the
-// grid origin, for checking the rasterisation stage on its own.
+// grid origin, for checking the rasterisation stage on its own. `tier` is
+// the threshold that selects the contour configuration.
 uint64_t orc_isochrone_geometry(uint64_t n_settled, const uint32_t* node, const uint32_t* dist,
                                 uint32_t max_t, uint32_t n_nodes, const uint32_t* node_w,
                                 const uint64_t* poly_off, const int32_t* poly, int mode,
                                 int has_origin, double o_lon, double o_lat, double* out,
                                 uint64_t cap, int32_t* cells, uint64_t cell_cap,
-                                uint64_t* n_cells, double* grid_origin) {
-  const Config cfg = config_for(mode, max_t);
+                                uint64_t* n_cells, double* grid_origin, uint32_t tier) {
+  // the contour tier of `tier` (the reference passes its threshold; a
+  // caller whose distances are not in seconds passes the seconds here)
+  const Config cfg = config_for(mode, tier);
   Segs segs;
   bool have_anchor = false;
   std::pair<int32_t, int32_t> anchor{0, 0};

@@ -60,7 +60,8 @@ def load():
         lib.orc_isochrone_geometry.argtypes = [ctypes.c_uint64, _V, _V, ctypes.c_uint32,
                                                ctypes.c_uint32, _V, _V, _V, ctypes.c_int,
                                                ctypes.c_int, ctypes.c_double, ctypes.c_double,
-                                               _V, ctypes.c_uint64, _V, ctypes.c_uint64, _V, _V]
+                                               _V, ctypes.c_uint64, _V, ctypes.c_uint64, _V, _V,
+                                               ctypes.c_uint32]
         lib.orc_isochrone_geometry.restype = ctypes.c_uint64
         lib.orc_cch_relax_par.argtypes = [ctypes.c_uint32] + [_V] * 8 + [ctypes.c_int, _V]
         lib.orc_cch_relax_par.restype = ctypes.c_uint32
@@ -428,11 +429,13 @@ def inverse_mercator(x, y):
     return lon, lat
 
 
-def isochrone_geometry(nodes, dists, max_t, node_w, poly_off, poly, mode="car", origin=None):
+def isochrone_geometry(nodes, dists, max_t, node_w, poly_off, poly, mode="car", origin=None,
+                       tier=None):
     """build_isochrone_geometry_sparse: settled (node, dist) pairs, per-node
     weights and (lat_e7, lon_e7) polylines; returns (ring (lon, lat) rows,
     closed cells (col, row) rows ascending by row then column, grid origin
-    (min_x, min_y) in Mercator metres)."""
+    (min_x, min_y) in Mercator metres). `tier` (default max_t) selects the
+    contour configuration."""
     nodes, dists = _a(nodes, np.uint32), _a(dists, np.uint32)
     node_w, poly_off = _a(node_w, np.uint32), _a(poly_off, np.uint64)
     poly = np.ascontiguousarray(np.asarray(poly, np.int32).reshape(-1, 2))
@@ -446,7 +449,7 @@ def isochrone_geometry(nodes, dists, max_t, node_w, poly_off, poly, mode="car", 
             len(nodes), nodes.ctypes.data, dists.ctypes.data, int(max_t), len(node_w),
             node_w.ctypes.data, poly_off.ctypes.data, poly.ctypes.data, MODES.get(mode, 0),
             int(origin is not None), o_lon, o_lat, o, k, cells.ctypes.data, cap_c,
-            ctypes.byref(nc), grid.ctypes.data))
+            ctypes.byref(nc), grid.ctypes.data, int(max_t if tier is None else tier)))
         if nc.value <= cap_c:
             return ring, cells[:2 * nc.value].reshape(-1, 2), grid
         cap_c = int(nc.value)

@@ -43,3 +43,18 @@ def test_host_polygons_match_oracle(built):
                                      [c[1] for c in cfg], has, anc)
     for got, w in zip(rings, want):
         assert len(w) >= 3 and np.array_equal(got, w)
+
+
+def test_projection_and_tiers_match_oracle(built):
+    # the library's to_mercator and SparseContourConfig restatements agree
+    # with the oracle's bit for bit (same host libm)
+    import bfphast
+    rng = np.random.default_rng(4)
+    pts = np.stack([rng.integers(480_000_000, 520_000_000, 5000),
+                    rng.integers(20_000_000, 60_000_000, 5000)], 1).astype(np.int32)
+    xy = bfphast.mercator(pts)
+    x, y = orc.mercator(pts[:, 0] / 1e7, pts[:, 1] / 1e7)
+    assert np.array_equal(xy[:, 0], x) and np.array_equal(xy[:, 1], y)
+    for mode, name in ((0, "car"), (1, "bike"), (2, "foot")):
+        for t in (0, 300, 600, 601, 1800, 1801, 3600, 3601, 7200):
+            assert bfphast.contour_config(mode, t) == orc.contour_config(name, t)

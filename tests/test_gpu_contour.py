@@ -80,3 +80,59 @@ def test_polygons_match_oracle(built):
             segs, anchor = segs_all[k]
             want = orc.sparse_contour(segs, cfgs[k][0], dil, ero, cfgs[k][3], anchor)
             assert np.array_equal(ring, want)
+
+
+def test_isochrone_polygons_end_to_end(built, country_small):
+    # bf_isochrone_polygons from origins to rings against the oracle's
+    # handler restatement on the oracle's settled sets
+    import bfphast
+    e, cch = country_small
+    rows, cols = 200, 250
+    ii = np.arange(e["n_intersections"], dtype=np.int64)
+    lat = (500_000_000 + (ii // cols) * 9000).astype(np.int32)
+    lon = (30_000_000 + (ii % cols) * 14000).astype(np.int32)
+    st = cch["rank_to_state"]
+    tail, head = e["state_tail"][st], e["state_head"][st]
+    poly = np.stack([np.stack([lat[tail], lon[tail]], 1), np.stack([lat[head], lon[head]], 1)],
+                    1).reshape(-1, 2)
+    off = np.arange(0, 2 * cch["n"] + 1, 2, dtype=np.uint64)
+    w = e["node_weight"][st]
+    geo = bfphast.Geometry(off, poly, w)
+    g = bfphast.Graph.from_cch(cch)
+    c = orc.Cch.from_dict(cch)
+    origins = np.array([5, 1234, 40000, 77777 % cch["n"]], np.uint32)
+    thr = np.array([3000, 18000, 6000, 36000], np.uint32)
+    tiers = thr // 10
+    for mode, name in ((bfphast.MODE_CAR, "car"), (bfphast.MODE_FOOT, "foot")):
+        rings, ph = bfphast.isochrone_polygons(g, geo, origins, thr, tiers, mode)
+        for i, o in enumerate(origins):
+            rk, ds = c.bounded_seeded([(int(o), 0)], int(thr[i]))
+            # the oracle's tier comes from the threshold it is given
+            want = _oracle_ring(rk, ds, int(thr[i]), int(tiers[i]), w, off, poly, name)
+            assert len(rings[i]) >= 3 and np.array_equal(rings[i], want)
+
+
+def _oracle_ring(rk, ds, thr, tier, w, off, poly, mode):
+    # build_isochrone_geometry_sparse with the contour tier of `tier`
+    cell, dil, ero, simp = orc.contour_config(mode, tier)
+    segs, anchor, best = [], None, 0xFFFFFFFF
+    for r, d in zip(rk, ds):
+        wr = int(w[r])
+        if d > thr or wr == 0 or wr == 0xFFFFFFFF:
+            continue
+        a, b = poly[off[r]], poly[off[r] + 1]
+        if d < best:
+            best, anchor = d, (int(a[0]), int(a[1]))
+        if d + wr <= thr:
+            segs.append([(int(a[0]), int(a[1])), (int(b[0]), int(b[1]))])
+            continue
+        frac = np.float32(thr - d) / np.float32(wr)
+        if frac <= 0:
+            continue
+        if frac >= 1:
+            segs.append([(int(a[0]), int(a[1])), (int(b[0]), int(b[1]))])
+            continue
+        cl = int(a[0]) + int(np.trunc(np.float32(int(b[0]) - int(a[0])) * frac))
+        cn = int(a[1]) + int(np.trunc(np.float32(int(b[1]) - int(a[1])) * frac))
+        segs.append([(int(a[0]), int(a[1])), (cl, cn)])
+    return orc.sparse_contour(segs, cell, dil, ero, simp, anchor)
