@@ -827,12 +827,18 @@ bf_status bf_isochrone_settled(bf_graph* h, const uint32_t* orig, const uint32_t
   uint64_t* d_counts = d_bits + chunk * w64;
   uint32_t* d_orig = reinterpret_cast<uint32_t*>(d_counts + chunk);
   uint32_t* d_thr = d_orig + chunk;
-  std::vector<std::vector<uint32_t>> all_r(n), all_d(n);
+  SettledSink sink;
+  try {
+    sink.r_at.assign(n, 0);
+    sink.d_at.assign(n, 0);
+    sink.cnt.assign(n, 0);
+  } catch (const std::bad_alloc&) {
+    set_error("out of host memory");
+    return BF_ERR_OOM;
+  }
   for (uint64_t c0 = 0; c0 < n; c0 += chunk) {
     const uint64_t m = std::min<uint64_t>(chunk, n - c0);
-    SettledSink sink;
-    sink.ranks.resize(m);
-    sink.dists.resize(m);
+    sink.base = c0;
     BF_CUDA(cudaMemcpyAsync(d_orig, orig + c0, m * 4, cudaMemcpyHostToDevice, s));
     BF_CUDA(cudaMemcpyAsync(d_thr, thr + c0, m * 4, cudaMemcpyHostToDevice, s));
     try {
@@ -842,14 +848,10 @@ bf_status bf_isochrone_settled(bf_graph* h, const uint32_t* orig, const uint32_t
       set_error("out of host memory");
       return BF_ERR_OOM;
     }
-    for (uint64_t i = 0; i < m; ++i) {
-      all_r[c0 + i].swap(sink.ranks[i]);
-      all_d[c0 + i].swap(sink.dists[i]);
-    }
   }
   if ((rc = check_device_error(g, s))) return rc;
   offsets[0] = 0;
-  for (uint64_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + all_r[i].size();
+  for (uint64_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + sink.cnt[i];
   const uint64_t total = offsets[n];
   uint32_t* r = (uint32_t*)std::malloc(std::max<uint64_t>(total, 1) * 4);
   uint32_t* d = (uint32_t*)std::malloc(std::max<uint64_t>(total, 1) * 4);
@@ -859,11 +861,21 @@ bf_status bf_isochrone_settled(bf_graph* h, const uint32_t* orig, const uint32_t
     set_error("out of host memory");
     return BF_ERR_OOM;
   }
-  for (uint64_t i = 0; i < n; ++i) {
-    if (all_r[i].empty()) continue;
-    std::memcpy(r + offsets[i], all_r[i].data(), all_r[i].size() * 4);
-    std::memcpy(d + offsets[i], all_d[i].data(), all_d[i].size() * 4);
-  }
+  // staging (wave order) -> output (input order), in pieces of 256 Ki entries
+  const uint64_t piece = 1ull << 18;
+  const uint32_t* stage = g->h_set_stage;
+  parallel_for((total + piece - 1) / piece, [&](uint64_t p) {
+    uint64_t a = p * piece;
+    const uint64_t e = std::min(total, a + piece);
+    uint64_t i = (uint64_t)(std::upper_bound(offsets, offsets + n + 1, a) - offsets) - 1;
+    for (; a < e; ++i) {
+      const uint64_t b = std::min(e, offsets[i + 1]);
+      const uint64_t k = a - offsets[i];
+      std::memcpy(r + a, stage + sink.r_at[i] + k, (b - a) * 4);
+      std::memcpy(d + a, stage + sink.d_at[i] + k, (b - a) * 4);
+      a = b;
+    }
+  });
   *ranks = r;
   *dists = d;
   if (st) {

@@ -864,20 +864,6 @@ void mercator_e7(int32_t lat_e7, int32_t lon_e7, double* x, double* y) {
   *y = std::log(std::tan(lat * (PI_D / 180.0) / 2.0 + PI_D / 4.0)) * EARTH_R;
 }
 
-template <class F>
-void parallel_for(uint64_t n, F&& f) {
-  const unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(),
-                                                      (unsigned)std::min<uint64_t>(n, 64)));
-  std::atomic<uint64_t> next{0};
-  auto work = [&]() {
-    for (uint64_t i; (i = next.fetch_add(1)) < n;) f(i);
-  };
-  std::vector<std::thread> pool;
-  for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
-  work();
-  for (auto& th : pool) th.join();
-}
-
 }  // namespace
 
 extern "C" {

@@ -4,8 +4,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -220,7 +222,32 @@ struct Graph {
   size_t io_bytes = 0;
   uint8_t* d_iso = nullptr;        // isochrone I/O: origins, thresholds, counts, bits
   size_t iso_bytes = 0;
+  // bulk settled sets: per-lane popcount prefixes, a wave's output and lane
+  // offsets on the device, and the page-locked staging of a call's output
+  uint32_t* d_set_pre = nullptr;
+  size_t set_pre_bytes = 0;
+  uint32_t* d_set_out = nullptr;
+  size_t set_out_bytes = 0;
+  uint64_t* d_set_off = nullptr;
+  size_t set_off_bytes = 0;
+  uint32_t* h_set_stage = nullptr;
+  uint64_t set_stage_cap = 0;      // u32 entries
 };
+
+// f(i) for i in [0, n) on up to 64 host threads (dynamic assignment).
+template <class F>
+inline void parallel_for(uint64_t n, F&& f) {
+  const unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(),
+                                                      (unsigned)std::min<uint64_t>(n, 64)));
+  std::atomic<uint64_t> next{0};
+  auto work = [&]() {
+    for (uint64_t i; (i = next.fetch_add(1)) < n;) f(i);
+  };
+  std::vector<std::thread> pool;
+  for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+}
 
 // One level launch; with `pdl` it is a programmatic dependent of the
 // previous launch on the stream (the kernels wait before reading rows).
@@ -303,19 +330,12 @@ bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, co
 // isochrone.cu
 // Settled (rank, distance) lists of bulk isochrones, filled wave by wave:
 // per origin of the call (its index in the call), ranks ascending.
+// Where the bulk settled sets land: the graph's page-locked staging buffer
+// (appended wave by wave) and each origin's place in it.
 struct SettledSink {
-  std::vector<std::vector<uint32_t>> ranks, dists;
-  uint32_t* d_pre = nullptr;   // per lane, exclusive popcount prefix of its bitset words
-  size_t pre_bytes = 0;
-  uint32_t* d_out = nullptr;   // a wave's ranks, then its distances
-  size_t out_bytes = 0;
-  uint64_t* d_off = nullptr;   // a wave's lane offsets
-  size_t off_bytes = 0;
-  ~SettledSink() {
-    if (d_pre) cudaFree(d_pre);
-    if (d_out) cudaFree(d_out);
-    if (d_off) cudaFree(d_off);
-  }
+  uint64_t base = 0;                     // input index of the chunk's first origin
+  uint64_t used = 0;                     // u32 entries of the staging buffer in use
+  std::vector<uint64_t> r_at, d_at, cnt;  // per origin: ranks, distances, entries
 };
 bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
                             uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,

@@ -15,6 +15,7 @@
 // sector of that origin's bitset row).
 
 #include <algorithm>
+#include <cstring>
 
 #include "engine.cuh"
 
@@ -373,30 +374,47 @@ bf_status emit_settled(const T* slab, uint32_t Kp, Graph* g, Sched& sc, const ui
   auto grow = [&](auto** p, size_t& cap, size_t need) -> cudaError_t {
     if (cap >= need) return cudaSuccess;
     if (*p) cudaFree(*p);
+    g->device_bytes -= cap;
     *p = nullptr;
     cap = 0;
     cudaError_t e = cudaMalloc((void**)p, need);
-    if (e == cudaSuccess) cap = need;
+    if (e == cudaSuccess) {
+      cap = need;
+      g->device_bytes += need;
+    }
     return e;
   };
-  BF_CUDA(grow(&sink->d_pre, sink->pre_bytes, std::max<size_t>(16, (size_t)kw * w32 * 4)));
-  BF_CUDA(grow(&sink->d_out, sink->out_bytes, std::max<size_t>(16, (size_t)total * 8)));
-  BF_CUDA(grow(&sink->d_off, sink->off_bytes, (size_t)(kw + 1) * 8));
-  BF_CUDA(cudaMemcpyAsync(sink->d_off, off.data(), (kw + 1) * 8, cudaMemcpyHostToDevice, st));
-  k_lane_prefix<<<kw, 1024, 0, st>>>(bits, w32, d_lane_row, sink->d_pre);
+  BF_CUDA(grow(&g->d_set_pre, g->set_pre_bytes, std::max<size_t>(16, (size_t)kw * w32 * 4)));
+  BF_CUDA(grow(&g->d_set_out, g->set_out_bytes, std::max<size_t>(16, (size_t)total * 8)));
+  BF_CUDA(grow(&g->d_set_off, g->set_off_bytes, (size_t)(kw + 1) * 8));
+  BF_CUDA(cudaMemcpyAsync(g->d_set_off, off.data(), (kw + 1) * 8, cudaMemcpyHostToDevice, st));
+  k_lane_prefix<<<kw, 1024, 0, st>>>(bits, w32, d_lane_row, g->d_set_pre);
   dim3 eg((unsigned)((w32 + 255) / 256), kw);
-  k_emit<T><<<eg, 256, 0, st>>>(slab, Kp, sc.d_cidx, g->n, bits, w32, d_lane_row, sink->d_pre,
-                                sink->d_off, total, sink->d_out, sink->d_out + total);
+  k_emit<T><<<eg, 256, 0, st>>>(slab, Kp, sc.d_cidx, g->n, bits, w32, d_lane_row, g->d_set_pre,
+                                g->d_set_off, total, g->d_set_out, g->d_set_out + total);
   BF_CUDA(cudaGetLastError());
-  std::vector<uint32_t> h(2 * total);
+  // the wave's ranks then distances, appended to the page-locked staging
+  const uint64_t need = sink->used + 2 * total;
+  if (need > g->set_stage_cap) {
+    const uint64_t cap = need + need / 4;
+    uint32_t* p = nullptr;
+    BF_CUDA(cudaHostAlloc((void**)&p, cap * 4, cudaHostAllocDefault));
+    if (sink->used) std::memcpy(p, g->h_set_stage, sink->used * 4);
+    if (g->h_set_stage) cudaFreeHost(g->h_set_stage);
+    g->h_set_stage = p;
+    g->set_stage_cap = cap;
+  }
   if (total)
-    BF_CUDA(cudaMemcpyAsync(h.data(), sink->d_out, total * 8, cudaMemcpyDeviceToHost, st));
+    BF_CUDA(cudaMemcpyAsync(g->h_set_stage + sink->used, g->d_set_out, total * 8,
+                            cudaMemcpyDeviceToHost, st));
   BF_CUDA(cudaStreamSynchronize(st));
   for (uint32_t l = 0; l < kw; ++l) {
-    const uint32_t o = h_lane_row[l];
-    sink->ranks[o].assign(h.begin() + off[l], h.begin() + off[l + 1]);
-    sink->dists[o].assign(h.begin() + total + off[l], h.begin() + total + off[l + 1]);
+    const uint64_t o = sink->base + h_lane_row[l];
+    sink->r_at[o] = sink->used + off[l];
+    sink->d_at[o] = sink->used + total + off[l];
+    sink->cnt[o] = off[l + 1] - off[l];
   }
+  sink->used = need;
   return BF_OK;
 }
 
