@@ -736,7 +736,6 @@ bf_status bf_isochrone_bitsets(bf_graph* h, const uint32_t* orig, const uint32_t
   Graph* g = &h->g;
   bf_status rc;
   if ((rc = check_ids(orig, n, g->n, "origins"))) return rc;
-  std::lock_guard<std::mutex> lk(g->mu);
   if (st) std::memset(st, 0, sizeof(*st));
   if (!n) return BF_OK;
   if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
@@ -787,20 +786,14 @@ bf_status bf_isochrone_bitsets(bf_graph* h, const uint32_t* orig, const uint32_t
   return BF_OK;
 }
 
-bf_status bf_isochrone_settled(bf_graph* h, const uint32_t* orig, const uint32_t* thr, uint64_t n,
-                               uint64_t* offsets, uint32_t** ranks, uint32_t** dists,
-                               bf_stats* st) {
-  if (ranks) *ranks = nullptr;
-  if (dists) *dists = nullptr;
-  if (!h || !offsets || !ranks || !dists || (n && (!orig || !thr))) {
-    set_error("bf_isochrone_settled: null argument");
-    return BF_ERR_INVALID;
-  }
-  double t0 = now_s();
-  Graph* g = &h->g;
+}  // extern "C"
+
+namespace bf {
+
+bf_status settled_waves(Graph* g, const uint32_t* orig, const uint32_t* thr, uint64_t n,
+                        SettledSink& sink, bf_stats* st) {
   bf_status rc;
   if ((rc = check_ids(orig, n, g->n, "origins"))) return rc;
-  std::lock_guard<std::mutex> lk(g->mu);
   if (st) std::memset(st, 0, sizeof(*st));
   if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
   cudaStream_t s = g->stream;
@@ -827,15 +820,6 @@ bf_status bf_isochrone_settled(bf_graph* h, const uint32_t* orig, const uint32_t
   uint64_t* d_counts = d_bits + chunk * w64;
   uint32_t* d_orig = reinterpret_cast<uint32_t*>(d_counts + chunk);
   uint32_t* d_thr = d_orig + chunk;
-  SettledSink sink;
-  try {
-    sink.r_at.assign(n, 0);
-    sink.d_at.assign(n, 0);
-    sink.cnt.assign(n, 0);
-  } catch (const std::bad_alloc&) {
-    set_error("out of host memory");
-    return BF_ERR_OOM;
-  }
   for (uint64_t c0 = 0; c0 < n; c0 += chunk) {
     const uint64_t m = std::min<uint64_t>(chunk, n - c0);
     sink.base = c0;
@@ -849,7 +833,36 @@ bf_status bf_isochrone_settled(bf_graph* h, const uint32_t* orig, const uint32_t
       return BF_ERR_OOM;
     }
   }
-  if ((rc = check_device_error(g, s))) return rc;
+  return check_device_error(g, s);
+}
+
+}  // namespace bf
+
+extern "C" {
+
+bf_status bf_isochrone_settled(bf_graph* h, const uint32_t* orig, const uint32_t* thr, uint64_t n,
+                               uint64_t* offsets, uint32_t** ranks, uint32_t** dists,
+                               bf_stats* st) {
+  if (ranks) *ranks = nullptr;
+  if (dists) *dists = nullptr;
+  if (!h || !offsets || !ranks || !dists || (n && (!orig || !thr))) {
+    set_error("bf_isochrone_settled: null argument");
+    return BF_ERR_INVALID;
+  }
+  double t0 = now_s();
+  Graph* g = &h->g;
+  bf_status rc;
+  std::lock_guard<std::mutex> lk(g->mu);  // the staging is the graph's until the copy ends
+  SettledSink sink;
+  try {
+    sink.r_at.assign(n, 0);
+    sink.d_at.assign(n, 0);
+    sink.cnt.assign(n, 0);
+  } catch (const std::bad_alloc&) {
+    set_error("out of host memory");
+    return BF_ERR_OOM;
+  }
+  if ((rc = settled_waves(g, orig, thr, n, sink, st))) return rc;
   offsets[0] = 0;
   for (uint64_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + sink.cnt[i];
   const uint64_t total = offsets[n];

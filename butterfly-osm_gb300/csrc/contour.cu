@@ -253,15 +253,37 @@ __global__ void k_extent(uint32_t n_iso, const MinMax* __restrict__ part,
 
 // Device buffers and stream of bf_contour_rasters, kept per device across
 // calls (grow-only; calls on one device are serialised by the mutex).
+enum Slot {
+  S_XY, S_SEG, S_ISEG, S_SISO, S_CELL, S_EXT, S_PART, S_ISO, S_ERR, S_HAS, S_ANCH, S_A, S_B,
+  S_BLK, S_LANE, S_CUT, S_CUTXY, S_THR, N_SLOTS
+};
 struct Workspace {
   std::mutex mu;
   cudaStream_t st = nullptr;
-  void* buf[16] = {};
-  size_t cap[16] = {};
+  void* buf[N_SLOTS] = {};
+  size_t cap[N_SLOTS] = {};
 };
 Workspace& workspace(int device) {
   static Workspace ws[64];
   return ws[device];
+}
+
+// Slot i of the workspace with room for `bytes` (grown by a quarter when it
+// has to grow).
+template <class T>
+cudaError_t ws_get(Workspace& ws, int i, size_t bytes, T** p) {
+  bytes = std::max<size_t>(bytes, 16);
+  if (ws.cap[i] < bytes) {
+    if (ws.buf[i]) cudaFree(ws.buf[i]);
+    ws.buf[i] = nullptr;
+    ws.cap[i] = 0;
+    const size_t want = bytes + bytes / 4;
+    const cudaError_t e = cudaMalloc(&ws.buf[i], want);
+    if (e != cudaSuccess) return e;
+    ws.cap[i] = want;
+  }
+  *p = reinterpret_cast<T*>(ws.buf[i]);
+  return cudaSuccess;
 }
 
 unsigned grid_of(uint64_t n) {
@@ -370,102 +392,40 @@ bool place(uint32_t n_iso, const Extent* ext, const double* cell_m, uint32_t dil
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uint64_t* iso_seg,
-                             uint32_t n_iso, const double* cell_m, const uint8_t* has_anchor,
-                             const double* anchor_xy, uint32_t dilation, uint32_t erosion,
-                             int device, bf_raster* rasters, uint64_t** words,
-                             uint64_t* n_words) {
-  if (words) *words = nullptr;
-  if (!seg_pt || !iso_seg || !cell_m || !rasters || !n_words || (has_anchor && !anchor_xy)) {
-    set_error("bf_contour_rasters: null argument");
-    return BF_ERR_INVALID;
-  }
-  for (uint32_t k = 0; k < n_iso; ++k)
-    if (iso_seg[k + 1] < iso_seg[k] || !(cell_m[k] > 0) || std::isinf(cell_m[k])) {
-      set_error("bf_contour_rasters: iso_seg must be non-decreasing and cell sizes positive");
-      return BF_ERR_INVALID;
-    }
-  const uint64_t n_seg = iso_seg[n_iso];
-  const uint64_t n_pts = seg_pt[n_seg];  // segment offsets are checked with the extents
-  if (n_pts && !xy) {
-    set_error("bf_contour_rasters: null points");
-    return BF_ERR_INVALID;
-  }
-  std::vector<IsoDev> iso;
-  uint64_t total = 0;
-  if (!words) {  // layout only, on the host
-    for (uint64_t s = 0; s < n_seg; ++s)
-      if (seg_pt[s + 1] < seg_pt[s]) {
-        set_error("bf_contour_rasters: seg_pt must be non-decreasing");
-        return BF_ERR_INVALID;
-      }
-    if (!layout(xy, seg_pt, iso_seg, n_iso, cell_m, has_anchor, anchor_xy, dilation, rasters, iso,
-                &total)) {
-      set_error("bf_contour_rasters: a raster extends beyond 32-bit cell coordinates");
-      return BF_ERR_INVALID;
-    }
-    *n_words = total;
-    return BF_OK;
-  }
-  if (cudaSetDevice(device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev || device >= 64) {
-    cudaGetLastError();
-    set_error("bf_contour_rasters: no such device");
-    return BF_ERR_INVALID;
-  }
-  // per-device workspace kept across calls: one stream, grow-only buffers
-  Workspace& ws = workspace(device);
-  std::lock_guard<std::mutex> lk(ws.mu);
-  if (!ws.st) BF_CUDA(cudaStreamCreateWithFlags(&ws.st, cudaStreamNonBlocking));
-  cudaStream_t st = ws.st;
+// Extents, layout, stamping, closing and download for a batch whose points,
+// segment offsets and per-isochrone segment offsets are on the device
+// (d_xy, d_seg, d_iseg); host arrays for the rest. The caller holds the
+// workspace's lock; everything runs on `st`.
+bf_status rasters_core(Workspace& ws, cudaStream_t st, const double2* d_xy, const uint64_t* d_seg,
+                       const uint64_t* d_iseg, uint64_t n_seg, uint64_t n_pts, uint32_t n_iso,
+                       const double* cell_m, const uint8_t* has_anchor, const double* anchor_xy,
+                       uint32_t dilation, uint32_t erosion, bf_raster* rasters, uint64_t** words,
+                       uint64_t* n_words) {
   cudaError_t e = cudaSuccess;
-  int slot = 0;
-  auto alloc = [&](auto** p, size_t bytes) {
-    const int i = slot++;
-    if (e != cudaSuccess) return;
-    bytes = std::max<size_t>(bytes, 16);
-    if (ws.cap[i] < bytes) {
-      if (ws.buf[i]) cudaFree(ws.buf[i]);
-      ws.buf[i] = nullptr;
-      ws.cap[i] = 0;
-      const size_t want = bytes + bytes / 4;
-      e = cudaMalloc(&ws.buf[i], want);
-      if (e != cudaSuccess) return;
-      ws.cap[i] = want;
-    }
-    *p = reinterpret_cast<std::remove_reference_t<decltype(*p)>>(ws.buf[i]);
-  };
-  auto done = [&](bf_status rc) { return rc; };
-  double2 *d_xy = nullptr, *d_anchor = nullptr;
-  uint64_t *d_seg = nullptr, *d_iseg = nullptr;
   uint32_t *d_siso = nullptr, *d_err = nullptr;
   double* d_cell = nullptr;
   uint8_t* d_has = nullptr;
+  double2* d_anchor = nullptr;
   Extent* d_ext = nullptr;
   IsoDev* d_iso = nullptr;
   MinMax* d_part = nullptr;
-  alloc(&d_xy, n_pts * sizeof(double2));
-  alloc(&d_seg, (n_seg + 1) * 8);
-  alloc(&d_iseg, ((uint64_t)n_iso + 1) * 8);
-  alloc(&d_siso, n_seg * 4);
-  alloc(&d_cell, (uint64_t)n_iso * 8);
-  alloc(&d_ext, (uint64_t)n_iso * sizeof(Extent));
-  alloc(&d_part, (uint64_t)n_iso * EXT_CHUNKS * sizeof(MinMax));
-  alloc(&d_iso, (uint64_t)n_iso * sizeof(IsoDev));
-  alloc(&d_err, 4);
-  alloc(&d_has, n_iso);  // always, so every buffer keeps its workspace slot
-  alloc(&d_anchor, (uint64_t)n_iso * 16);
-  if (e != cudaSuccess) return done(cuda_status(e, "bf_contour_rasters: device memory"));
+  auto get = [&](int i, size_t bytes, auto** p) {
+    if (e == cudaSuccess) e = ws_get(ws, i, bytes, p);
+  };
+  get(S_SISO, n_seg * 4, &d_siso);
+  get(S_CELL, (uint64_t)n_iso * 8, &d_cell);
+  get(S_EXT, (uint64_t)n_iso * sizeof(Extent), &d_ext);
+  get(S_PART, (uint64_t)n_iso * EXT_CHUNKS * sizeof(MinMax), &d_part);
+  get(S_ISO, (uint64_t)n_iso * sizeof(IsoDev), &d_iso);
+  get(S_ERR, 4, &d_err);
+  get(S_HAS, n_iso, &d_has);
+  get(S_ANCH, (uint64_t)n_iso * 16, &d_anchor);
+  if (e != cudaSuccess) return cuda_status(e, "bf_contour_rasters: device memory");
   std::vector<Extent> ext(n_iso);
   auto stage1 = [&]() -> cudaError_t {
     cudaError_t r;
-    if (n_pts && (r = cudaMemcpyAsync(d_xy, xy, n_pts * 16, cudaMemcpyHostToDevice, st))) return r;
-    if ((r = cudaMemcpyAsync(d_seg, seg_pt, (n_seg + 1) * 8, cudaMemcpyHostToDevice, st))) return r;
-    if ((r = cudaMemcpyAsync(d_iseg, iso_seg, ((uint64_t)n_iso + 1) * 8, cudaMemcpyHostToDevice, st)))
-      return r;
     if (n_iso && (r = cudaMemcpyAsync(d_cell, cell_m, (uint64_t)n_iso * 8, cudaMemcpyHostToDevice, st)))
       return r;
     if (has_anchor && n_iso) {
@@ -476,7 +436,8 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
     if ((r = cudaMemsetAsync(d_err, 0, 4, st))) return r;
     if (n_iso) {
       k_minmax<<<n_iso * EXT_CHUNKS, 256, 0, st>>>(n_pts, d_xy, d_seg, d_iseg, d_siso, d_part, d_err);
-      k_extent<<<(n_iso + 127) / 128, 128, 0, st>>>(n_iso, d_part, d_cell, d_has, d_anchor, d_ext);
+      k_extent<<<(n_iso + 127) / 128, 128, 0, st>>>(n_iso, d_part, d_cell,
+                                                     has_anchor ? d_has : nullptr, d_anchor, d_ext);
     }
     if ((r = cudaGetLastError())) return r;
     if (n_iso && (r = cudaMemcpyAsync(ext.data(), d_ext, (uint64_t)n_iso * sizeof(Extent),
@@ -484,32 +445,34 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
       return r;
     return cudaStreamSynchronize(st);
   };
-  if ((e = stage1()) != cudaSuccess) return done(cuda_status(e, "bf_contour_rasters: extents"));
+  if ((e = stage1()) != cudaSuccess) return cuda_status(e, "bf_contour_rasters: extents");
   {
     uint32_t verr = 0;
     if ((e = cudaMemcpy(&verr, d_err, 4, cudaMemcpyDeviceToHost)) != cudaSuccess)
-      return done(cuda_status(e, "bf_contour_rasters: extents"));
+      return cuda_status(e, "bf_contour_rasters: extents");
     if (verr & 2u) {
       set_error("bf_contour_rasters: seg_pt must be non-decreasing");
-      return done(BF_ERR_INVALID);
+      return BF_ERR_INVALID;
     }
   }
+  std::vector<IsoDev> iso;
+  uint64_t total = 0;
   if (!place(n_iso, ext.data(), cell_m, dilation, rasters, iso, &total)) {
     set_error("bf_contour_rasters: a raster extends beyond 32-bit cell coordinates");
-    return done(BF_ERR_INVALID);
+    return BF_ERR_INVALID;
   }
   *n_words = total;
   uint64_t* h_words = (uint64_t*)std::malloc(std::max<uint64_t>(total, 1) * 8);
   if (!h_words) {
     set_error("out of host memory");
-    return done(BF_ERR_OOM);
+    return BF_ERR_OOM;
   }
   unsigned long long *d_a = nullptr, *d_b = nullptr;
-  alloc(&d_a, total * 8);
-  alloc(&d_b, total * 8);
+  get(S_A, total * 8, &d_a);
+  get(S_B, total * 8, &d_b);
   if (e != cudaSuccess) {
     std::free(h_words);
-    return done(cuda_status(e, "bf_contour_rasters: raster memory"));
+    return cuda_status(e, "bf_contour_rasters: raster memory");
   }
   auto stage2 = [&]() -> cudaError_t {
     cudaError_t r;
@@ -540,12 +503,79 @@ bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uin
   if (e == cudaSuccess) e = cudaMemcpy(&err, d_err, 4, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess || err) {
     std::free(h_words);
-    if (e != cudaSuccess) return done(cuda_status(e, "bf_contour_rasters"));
+    if (e != cudaSuccess) return cuda_status(e, "bf_contour_rasters");
     set_error("bf_contour_rasters: a stamped cell fell outside its raster");
-    return done(BF_ERR_DEVICE);
+    return BF_ERR_DEVICE;
   }
   *words = h_words;
-  return done(BF_OK);
+  return BF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+bf_status bf_contour_rasters(const double* xy, const uint64_t* seg_pt, const uint64_t* iso_seg,
+                             uint32_t n_iso, const double* cell_m, const uint8_t* has_anchor,
+                             const double* anchor_xy, uint32_t dilation, uint32_t erosion,
+                             int device, bf_raster* rasters, uint64_t** words,
+                             uint64_t* n_words) {
+  if (words) *words = nullptr;
+  if (!seg_pt || !iso_seg || !cell_m || !rasters || !n_words || (has_anchor && !anchor_xy)) {
+    set_error("bf_contour_rasters: null argument");
+    return BF_ERR_INVALID;
+  }
+  for (uint32_t k = 0; k < n_iso; ++k)
+    if (iso_seg[k + 1] < iso_seg[k] || !(cell_m[k] > 0) || std::isinf(cell_m[k])) {
+      set_error("bf_contour_rasters: iso_seg must be non-decreasing and cell sizes positive");
+      return BF_ERR_INVALID;
+    }
+  const uint64_t n_seg = iso_seg[n_iso];
+  const uint64_t n_pts = seg_pt[n_seg];  // segment offsets are checked with the extents
+  if (n_pts && !xy) {
+    set_error("bf_contour_rasters: null points");
+    return BF_ERR_INVALID;
+  }
+  if (!words) {  // layout only, on the host
+    for (uint64_t s = 0; s < n_seg; ++s)
+      if (seg_pt[s + 1] < seg_pt[s]) {
+        set_error("bf_contour_rasters: seg_pt must be non-decreasing");
+        return BF_ERR_INVALID;
+      }
+    std::vector<IsoDev> iso;
+    uint64_t total = 0;
+    if (!layout(xy, seg_pt, iso_seg, n_iso, cell_m, has_anchor, anchor_xy, dilation, rasters, iso,
+                &total)) {
+      set_error("bf_contour_rasters: a raster extends beyond 32-bit cell coordinates");
+      return BF_ERR_INVALID;
+    }
+    *n_words = total;
+    return BF_OK;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev || device >= 64) {
+    cudaGetLastError();
+    set_error("bf_contour_rasters: no such device");
+    return BF_ERR_INVALID;
+  }
+  // per-device workspace kept across calls: one stream, grow-only buffers
+  Workspace& ws = workspace(device);
+  std::lock_guard<std::mutex> lk(ws.mu);
+  if (!ws.st) BF_CUDA(cudaStreamCreateWithFlags(&ws.st, cudaStreamNonBlocking));
+  cudaStream_t st = ws.st;
+  double2* d_xy = nullptr;
+  uint64_t *d_seg = nullptr, *d_iseg = nullptr;
+  cudaError_t e = ws_get(ws, S_XY, n_pts * sizeof(double2), &d_xy);
+  if (e == cudaSuccess) e = ws_get(ws, S_SEG, (n_seg + 1) * 8, &d_seg);
+  if (e == cudaSuccess) e = ws_get(ws, S_ISEG, ((uint64_t)n_iso + 1) * 8, &d_iseg);
+  if (e == cudaSuccess && n_pts) e = cudaMemcpyAsync(d_xy, xy, n_pts * 16, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_seg, seg_pt, (n_seg + 1) * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_iseg, iso_seg, ((uint64_t)n_iso + 1) * 8, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_status(e, "bf_contour_rasters: upload");
+  return rasters_core(ws, st, d_xy, d_seg, d_iseg, n_seg, n_pts, n_iso, cell_m, has_anchor,
+                      anchor_xy, dilation, erosion, rasters, words, n_words);
 }
 
 void bf_contour_free(uint64_t* words) { std::free(words); }
@@ -559,7 +589,7 @@ void bf_contour_release(int device) {
     return;
   }
   if (ws.st) cudaStreamSynchronize(ws.st);
-  for (int i = 0; i < 16; ++i) {
+  for (int i = 0; i < N_SLOTS; ++i) {
     if (ws.buf[i]) cudaFree(ws.buf[i]);
     ws.buf[i] = nullptr;
     ws.cap[i] = 0;
@@ -847,12 +877,23 @@ void bf_contour_free_polygons(double* lonlat) { std::free(lonlat); }
 
 #include <chrono>
 
+// Device copy of a geometry (uploaded on first use on that device).
+struct GeoDev {
+  bool ready = false;
+  uint64_t* off = nullptr;
+  uint32_t* w = nullptr;
+  double2* xy = nullptr;
+  int2* e7 = nullptr;
+};
+
 struct bf_geometry {
   uint32_t n = 0;
   std::vector<uint64_t> off;   // polyline of rank r: points [off[r], off[r + 1])
   std::vector<int32_t> e7;     // (lat_e7, lon_e7) per point
   std::vector<double> xy;      // Web-Mercator (x, y) per point
   std::vector<uint32_t> w;     // traversal weight per rank
+  mutable std::mutex mu;
+  mutable GeoDev dev[64];
 };
 
 namespace {
@@ -862,6 +903,290 @@ void mercator_e7(int32_t lat_e7, int32_t lon_e7, double* x, double* y) {
   const double lat = (double)lat_e7 / 1e7, lon = (double)lon_e7 / 1e7;
   *x = lon * (PI_D / 180.0) * EARTH_R;
   *y = std::log(std::tan(lat * (PI_D / 180.0) / 2.0 + PI_D / 4.0)) * EARTH_R;
+}
+
+// ---- reachable road segments of a wave of isochrones, on the device ----
+//
+// build_isochrone_geometry_sparse (server/geometry.rs:281-418): every settled
+// rank whose road is stamped contributes its polyline whole, or, on the
+// frontier (distance + weight beyond the threshold), cut with the
+// reference's f32 arithmetic: frac = (T - d) / w, the first floor(frac * n)
+// + 1 points and an interpolated cut point. The anchor is the first vertex
+// of the first settled road (ranks ascending) of minimum distance.
+// Entry i of the wave is settled (rank, dist) pair i; lane l owns entries
+// [lane_off[l], lane_off[l + 1]). Counting, a one-block scan of the block
+// totals and an ordered write give each segment its offsets; the cut
+// points go to the host for projection (host libm, as the reference) and
+// come back by a scatter.
+struct WaveIn {
+  const uint32_t* ranks;
+  const uint32_t* dists;
+  const uint64_t* lane_off;
+  uint32_t kw;
+  const uint32_t* thr;  // per lane
+  const uint64_t* g_off;
+  const uint32_t* g_w;
+  const double2* g_xy;
+  const int2* g_e7;
+  uint32_t g_n;
+  uint64_t n;  // entries
+};
+
+struct Road {
+  uint64_t p0, take;
+  uint32_t rank, dist;
+  int32_t clat, clon;
+  uint32_t seg, cut;  // 0 or 1
+  bool anchor;        // a stamped road: an anchor candidate
+};
+
+constexpr uint32_t SEG_TPB = 256, SEG_ITEMS = 8, SEG_BLOCK = SEG_TPB * SEG_ITEMS;
+
+__device__ __forceinline__ uint32_t lane_at(const uint64_t* __restrict__ off, uint32_t kw,
+                                            uint64_t i) {
+  uint32_t lo = 0, hi = kw;  // off[lo] <= i < off[hi]
+  while (hi - lo > 1) {
+    const uint32_t m = (lo + hi) >> 1;
+    if (off[m] <= i)
+      lo = m;
+    else
+      hi = m;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ Road road_of(const WaveIn& a, uint64_t i, uint32_t l, uint32_t* err) {
+  Road R{};
+  const uint32_t r = a.ranks[i], d = a.dists[i], T = a.thr[l];
+  R.rank = r;
+  R.dist = d;
+  if (r >= a.g_n) {
+    atomicOr(err, 4u);
+    return R;
+  }
+  if (d > T) return R;
+  const uint32_t w = a.g_w[r];
+  if (w == 0 || w == 0xFFFFFFFFu) return R;
+  const uint64_t p0 = a.g_off[r], np = a.g_off[r + 1] - p0;
+  if (np == 0) return R;
+  R.anchor = true;
+  R.p0 = p0;
+  const uint32_t d_end = (d + w < d) ? 0xFFFFFFFFu : d + w;
+  uint64_t take = np;
+  if (d_end > T) {
+    const float frac = __fdiv_rn(__uint2float_rn(T - d), __uint2float_rn(w));
+    if (frac <= 0.0f) return R;
+    if (np > 1 && frac < 1.0f) {
+      const uint64_t nsg = np - 1;
+      const float sf = __fmul_rn(frac, __ull2float_rn(nsg));
+      const uint64_t si = min((uint64_t)floorf(sf), nsg - 1);
+      const float lf = __fsub_rn(sf, __ull2float_rn(si));
+      take = si + 1;
+      if (lf > 0.0f && si + 1 < np) {
+        const int2 pa = a.g_e7[p0 + si], pb = a.g_e7[p0 + si + 1];
+        R.clat = pa.x + __float2int_rz(__fmul_rn(__int2float_rn(pb.x - pa.x), lf));
+        R.clon = pa.y + __float2int_rz(__fmul_rn(__int2float_rn(pb.y - pa.y), lf));
+        R.cut = 1;
+      }
+    } else if (np == 1) {
+      take = 1;
+    }
+  }
+  R.take = take;
+  R.seg = 1;
+  return R;
+}
+
+// Per block of SEG_BLOCK entries: segment, point and cut totals; per lane:
+// segment counts and the anchor key (dist << 32 | rank), aggregated over a
+// warp whose entries share a lane.
+__global__ void __launch_bounds__(SEG_TPB)
+    k_seg_count(WaveIn a, unsigned long long* __restrict__ blk,
+                unsigned long long* __restrict__ lane_seg,
+                unsigned long long* __restrict__ lane_anchor, uint32_t* err) {
+  __shared__ unsigned long long red[3][SEG_TPB / 32];
+  const unsigned FULL = 0xFFFFFFFFu;
+  const uint64_t base = (uint64_t)blockIdx.x * SEG_BLOCK;
+  unsigned long long s = 0, p = 0, c = 0;
+  for (uint32_t j = 0; j < SEG_ITEMS; ++j) {
+    const uint64_t i = base + (uint64_t)j * SEG_TPB + threadIdx.x;
+    const bool in = i < a.n;
+    if (!__any_sync(FULL, in)) continue;
+    uint32_t l = 0;
+    Road R{};
+    if (in) {
+      l = lane_at(a.lane_off, a.kw, i);
+      R = road_of(a, i, l, err);
+    }
+    s += R.seg;
+    p += R.take + R.cut;
+    c += R.cut;
+    const unsigned long long key =
+        R.anchor ? (((unsigned long long)R.dist << 32) | R.rank) : ~0ull;
+    const uint32_t l0 = __shfl_sync(FULL, l, 0);  // thread 0 holds the warp's first entry
+    if (__all_sync(FULL, !in || l == l0)) {
+      const uint32_t cnt = __popc(__ballot_sync(FULL, R.seg != 0));
+      unsigned long long k = key;
+      for (int o = 16; o > 0; o >>= 1) k = min(k, __shfl_xor_sync(FULL, k, o));
+      if ((threadIdx.x & 31) == 0) {
+        if (cnt) atomicAdd(lane_seg + l0, (unsigned long long)cnt);
+        if (k != ~0ull) atomicMin(lane_anchor + l0, k);
+      }
+    } else if (in) {
+      if (R.seg) atomicAdd(lane_seg + l, 1ull);
+      if (key != ~0ull) atomicMin(lane_anchor + l, key);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(FULL, s, o);
+    p += __shfl_xor_sync(FULL, p, o);
+    c += __shfl_xor_sync(FULL, c, o);
+  }
+  const uint32_t warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][warp] = s;
+    red[1][warp] = p;
+    red[2][warp] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    unsigned long long t = 0;
+    for (uint32_t w = 0; w < SEG_TPB / 32; ++w) t += red[threadIdx.x][w];
+    blk[3 * (uint64_t)blockIdx.x + threadIdx.x] = t;
+  }
+}
+
+// Exclusive scan of the nb block totals (one block), the wave's totals last.
+__global__ void __launch_bounds__(1024)
+    k_seg_scan(uint64_t nb, const unsigned long long* __restrict__ blk,
+               unsigned long long* __restrict__ bscan, unsigned long long* __restrict__ tot) {
+  __shared__ unsigned long long sh[3][32];
+  const unsigned FULL = 0xFFFFFFFFu;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long carry[3] = {0, 0, 0};
+  for (uint64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+    const uint64_t b = b0 + threadIdx.x;
+    unsigned long long v[3], x[3];
+    for (int q = 0; q < 3; ++q) {
+      v[q] = b < nb ? blk[3 * b + q] : 0;
+      x[q] = v[q];
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long y = __shfl_up_sync(FULL, x[q], d);
+        if (lane >= d) x[q] += y;
+      }
+      if (lane == 31) sh[q][warp] = x[q];
+    }
+    __syncthreads();
+    if (warp == 0)
+      for (int q = 0; q < 3; ++q) {
+        unsigned long long t = lane < (blockDim.x >> 5) ? sh[q][lane] : 0;
+        for (int d = 1; d < 32; d <<= 1) {
+          const unsigned long long y = __shfl_up_sync(FULL, t, d);
+          if (lane >= d) t += y;
+        }
+        sh[q][lane] = t;
+      }
+    __syncthreads();
+    for (int q = 0; q < 3; ++q) {
+      if (b < nb) bscan[3 * b + q] = carry[q] + (warp ? sh[q][warp - 1] : 0) + x[q] - v[q];
+      carry[q] += sh[q][(blockDim.x >> 5) - 1];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) tot[threadIdx.x] = carry[threadIdx.x];
+}
+
+template <class T>
+__device__ __forceinline__ T block_excl_scan(T v, T* sh, T* total) {
+  const unsigned FULL = 0xFFFFFFFFu;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T x = v;
+  for (int d = 1; d < 32; d <<= 1) {
+    const T y = __shfl_up_sync(FULL, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  T pre = 0, t = 0;
+  for (uint32_t w = 0; w < SEG_TPB / 32; ++w) {
+    const T sv = sh[w];
+    if (w < warp) pre += sv;
+    t += sv;
+  }
+  __syncthreads();
+  *total = t;
+  return pre + x - v;
+}
+
+// Ordered write: segment s of the wave ends at seg_pt[s + 1]; its points
+// are gathered from the projected geometry, its cut point (if any) is
+// recorded as cut c at point cut_pos[c].
+__global__ void __launch_bounds__(SEG_TPB)
+    k_seg_write(WaveIn a, const unsigned long long* __restrict__ bscan,
+                uint64_t* __restrict__ seg_pt, double2* __restrict__ xy,
+                int2* __restrict__ cut_e7, uint64_t* __restrict__ cut_pos, uint32_t* err) {
+  __shared__ uint32_t sh32[SEG_TPB / 32];
+  __shared__ unsigned long long sh64[SEG_TPB / 32];
+  const uint64_t base = (uint64_t)blockIdx.x * SEG_BLOCK;
+  uint64_t s = bscan[3 * (uint64_t)blockIdx.x], p = bscan[3 * (uint64_t)blockIdx.x + 1],
+           c = bscan[3 * (uint64_t)blockIdx.x + 2];
+  for (uint32_t j = 0; j < SEG_ITEMS; ++j) {
+    const uint64_t i = base + (uint64_t)j * SEG_TPB + threadIdx.x;
+    Road R{};
+    if (i < a.n) R = road_of(a, i, lane_at(a.lane_off, a.kw, i), err);
+    uint32_t sc_tot;
+    unsigned long long p_tot;
+    const uint32_t sc = block_excl_scan<uint32_t>(R.seg | (R.cut << 16), sh32, &sc_tot);
+    const unsigned long long pe =
+        block_excl_scan<unsigned long long>(R.take + R.cut, sh64, &p_tot);
+    if (R.seg) {
+      const uint64_t ms = s + (sc & 0xFFFFu), mp = p + pe, mc = c + (sc >> 16);
+      for (uint64_t q = 0; q < R.take; ++q) xy[mp + q] = a.g_xy[R.p0 + q];
+      if (R.cut) {
+        cut_e7[mc] = make_int2(R.clat, R.clon);
+        cut_pos[mc] = mp + R.take;
+      }
+      seg_pt[ms + 1] = mp + R.take + R.cut;
+    }
+    s += sc_tot & 0xFFFFu;
+    c += sc_tot >> 16;
+    p += p_tot;
+  }
+}
+
+__global__ void k_cut_scatter(uint64_t n_cut, const uint64_t* __restrict__ pos,
+                              const double2* __restrict__ cxy, double2* __restrict__ xy) {
+  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < n_cut;
+       c += (uint64_t)gridDim.x * blockDim.x)
+    xy[pos[c]] = cxy[c];
+}
+
+// The geometry's device copy on `device` (uploaded on first use).
+bf_status geo_device(const bf_geometry* geo, int device, GeoDev** out) {
+  std::lock_guard<std::mutex> lk(geo->mu);
+  GeoDev& d = geo->dev[device];
+  if (!d.ready) {
+    const uint64_t np = geo->off[geo->n];
+    cudaError_t e = cudaMalloc(&d.off, ((uint64_t)geo->n + 1) * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&d.w, std::max<uint64_t>(geo->n, 1) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&d.xy, std::max<uint64_t>(np, 1) * 16);
+    if (e == cudaSuccess) e = cudaMalloc(&d.e7, std::max<uint64_t>(np, 1) * 8);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(d.off, geo->off.data(), ((uint64_t)geo->n + 1) * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && geo->n)
+      e = cudaMemcpy(d.w, geo->w.data(), (uint64_t)geo->n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && np) e = cudaMemcpy(d.xy, geo->xy.data(), np * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && np) e = cudaMemcpy(d.e7, geo->e7.data(), np * 8, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      for (void* q : {(void*)d.off, (void*)d.w, (void*)d.xy, (void*)d.e7})
+        if (q) cudaFree(q);
+      d = GeoDev{};
+      return cuda_status(e, "bf_isochrone_polygons: geometry upload");
+    }
+    d.ready = true;
+  }
+  *out = &d;
+  return BF_OK;
 }
 
 }  // namespace
@@ -946,7 +1271,20 @@ bf_status bf_geometry_create(uint32_t n_nodes, const uint64_t* poly_off, const i
   return BF_OK;
 }
 
-void bf_geometry_destroy(bf_geometry* geo) { delete geo; }
+void bf_geometry_destroy(bf_geometry* geo) {
+  if (!geo) return;
+  int cur = -1;
+  cudaGetDevice(&cur);
+  for (int dv = 0; dv < 64; ++dv) {
+    GeoDev& d = geo->dev[dv];
+    if (!d.ready) continue;
+    if (cudaSetDevice(dv) == cudaSuccess)
+      for (void* q : {(void*)d.off, (void*)d.w, (void*)d.xy, (void*)d.e7}) cudaFree(q);
+    cudaGetLastError();
+  }
+  if (cur >= 0) cudaSetDevice(cur);
+  delete geo;
+}
 
 bf_status bf_isochrone_polygons(bf_graph* g, const bf_geometry* geo, const uint32_t* origins,
                                 const uint32_t* thresholds, const uint32_t* tier_thresholds,
@@ -966,152 +1304,175 @@ bf_status bf_isochrone_polygons(bf_graph* g, const bf_geometry* geo, const uint3
     set_error("bf_isochrone_polygons: too many origins in one call");
     return BF_ERR_INVALID;
   }
+  if (gr->device < 0 || gr->device >= 64) {
+    set_error("bf_isochrone_polygons: device ordinal out of range");
+    return BF_ERR_INVALID;
+  }
   using clk = std::chrono::steady_clock;
   auto ms = [](clk::time_point a) {
     return std::chrono::duration<double, std::milli>(clk::now() - a).count();
   };
   double ph[4] = {0, 0, 0, 0};
-  auto t0 = clk::now();
-  // 1. settled sets of every origin
-  std::vector<uint64_t> soff(n + 1, 0);
-  uint32_t *sr = nullptr, *sd = nullptr;
-  bf_status rc = bf_isochrone_settled(g, origins, thresholds, n, soff.data(), &sr, &sd, nullptr);
-  if (rc) return rc;
-  ph[0] = ms(t0);
-  t0 = clk::now();
-  // 2. reachable segments (host threads): one walk per isochrone counts,
-  // a second writes the points straight into a page-locked buffer kept
-  // across calls (it is also the rasters' upload source)
+  auto mark = clk::now();
   std::vector<double> cell(n), simp(n);
   uint32_t dil = 0, ero = 0;
   for (uint64_t k = 0; k < n; ++k)
     bf_contour_config(mode, tier_thresholds ? tier_thresholds[k] : thresholds[k], &cell[k], &dil,
                       &ero, &simp[k]);
-  std::vector<uint64_t> nseg(n, 0), npts(n, 0);
-  std::vector<uint8_t> has(n, 0);
-  std::vector<double> anc(2 * n, 0.0);
-  // walk(k, f): f(p0, take, cut, clat, clon) for every stamped road of isochrone k
-  auto walk = [&](uint64_t k, auto&& f) {
-    const uint32_t T = thresholds[k];
-    uint32_t best = 0xFFFFFFFFu;
-    for (uint64_t i = soff[k]; i < soff[k + 1]; ++i) {
-      const uint32_t r = sr[i], d = sd[i];
-      if (d > T) continue;
-      const uint32_t w = geo->w[r];
-      if (w == 0 || w == 0xFFFFFFFFu) continue;
-      const uint64_t p0 = geo->off[r], np = geo->off[r + 1] - p0;
-      if (np == 0) continue;
-      if (d < best) {
-        best = d;
-        has[k] = 1;
-        anc[2 * k] = geo->xy[2 * p0];
-        anc[2 * k + 1] = geo->xy[2 * p0 + 1];
-      }
-      const uint32_t d_end = (d + w < d) ? 0xFFFFFFFFu : d + w;
-      uint64_t take = np;  // whole polyline
-      bool cut = false;
-      int32_t clat = 0, clon = 0;
-      if (d_end > T) {  // frontier road: the reference's f32 cut
-        const float frac = (float)(T - d) / (float)w;
-        if (frac <= 0.0f) continue;
-        if (np > 1 && frac < 1.0f) {
-          const uint64_t nsg = np - 1;
-          const float sf = frac * (float)nsg;
-          const uint64_t si = std::min<uint64_t>((uint64_t)std::floor(sf), nsg - 1);
-          const float lf = sf - (float)si;
-          take = si + 1;
-          if (lf > 0.0f && si + 1 < np) {
-            const int32_t* a = &geo->e7[2 * (p0 + si)];
-            const int32_t* b = a + 2;
-            clat = a[0] + (int32_t)((float)(b[0] - a[0]) * lf);
-            clon = a[1] + (int32_t)((float)(b[1] - a[1]) * lf);
-            cut = true;
-          }
-        } else if (np == 1) {
-          take = 1;
-        }
-      }
-      f(p0, take, cut, clat, clon);
-    }
+  // one ring per origin, gathered wave by wave
+  std::vector<uint64_t> r_len(n, 0), r_at(n, 0);
+  std::vector<double*> wave_ll;
+  auto free_waves = [&]() {
+    for (double* q : wave_ll) bf_contour_free_polygons(q);
   };
-  parallel_for(n, [&](uint64_t k) {
-    walk(k, [&](uint64_t, uint64_t take, bool cut, int32_t, int32_t) {
-      ++nseg[k];
-      npts[k] += take + (cut ? 1 : 0);
-    });
-  });
-  std::vector<uint64_t> iso_seg(n + 1, 0), pt_base(n + 1, 0);
-  for (uint64_t k = 0; k < n; ++k) {
-    iso_seg[k + 1] = iso_seg[k] + nseg[k];
-    pt_base[k + 1] = pt_base[k] + npts[k];
-  }
-  const uint64_t n_pts = pt_base[n];
-  static std::mutex stage_mu;  // the page-locked staging of this entry point
-  static double* stage_xy = nullptr;
-  static uint64_t stage_cap = 0;
-  static std::vector<uint64_t> seg_pt;
-  std::lock_guard<std::mutex> stage_lk(stage_mu);
-  if (stage_cap < n_pts) {
-    if (stage_xy) cudaFreeHost(stage_xy);
-    stage_xy = nullptr;
-    stage_cap = 0;
-    const uint64_t want = n_pts + n_pts / 4;
-    if (cudaHostAlloc((void**)&stage_xy, std::max<uint64_t>(want, 1) * 16, cudaHostAllocDefault) !=
-        cudaSuccess) {
-      cudaGetLastError();
-      bf_settled_free(sr);
-      bf_settled_free(sd);
-      set_error("bf_isochrone_polygons: page-locked staging allocation failed");
-      return BF_ERR_OOM;
+  std::lock_guard<std::mutex> glk(gr->mu);
+  if (cudaSetDevice(gr->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  GeoDev* gd = nullptr;
+  bf_status rc = geo_device(geo, gr->device, &gd);
+  if (rc) return rc;
+  Workspace& ws = workspace(gr->device);
+  std::lock_guard<std::mutex> wlk(ws.mu);
+  if (ws.st) BF_CUDA(cudaStreamSynchronize(ws.st));
+  SettledSink sink;
+  sink.on_wave = [&](const uint32_t* d_r, const uint32_t* d_d, const uint64_t* d_off,
+                     const std::vector<uint64_t>& off, const std::vector<uint32_t>& rows,
+                     cudaStream_t st) -> bf_status {
+    ph[0] += ms(mark);
+    auto t0 = clk::now();
+    const uint32_t kw = (uint32_t)rows.size();
+    const uint64_t E = off[kw];
+    const uint64_t nb = (E + SEG_BLOCK - 1) / SEG_BLOCK;
+    std::vector<uint32_t> thr_l(kw);
+    std::vector<double> cell_l(kw), simp_l(kw);
+    for (uint32_t l = 0; l < kw; ++l) {
+      thr_l[l] = thresholds[rows[l]];
+      cell_l[l] = cell[rows[l]];
+      simp_l[l] = simp[rows[l]];
     }
-    stage_cap = want;
+    uint32_t *d_thr = nullptr, *d_err = nullptr;
+    unsigned long long *d_blk = nullptr, *d_lane = nullptr;
+    cudaError_t e = ws_get(ws, S_THR, (uint64_t)kw * 4, &d_thr);
+    if (e == cudaSuccess) e = ws_get(ws, S_ERR, 4, &d_err);
+    if (e == cudaSuccess) e = ws_get(ws, S_BLK, std::max<uint64_t>(nb, 1) * 6 * 8, &d_blk);
+    if (e == cudaSuccess) e = ws_get(ws, S_LANE, (2ull * kw + 3) * 8, &d_lane);
+    if (e != cudaSuccess) return cuda_status(e, "bf_isochrone_polygons: device memory");
+    unsigned long long *lane_seg = d_lane, *lane_anchor = d_lane + kw, *tot = d_lane + 2 * kw;
+    const WaveIn a{d_r, d_d, d_off, kw, d_thr, gd->off, gd->w, gd->xy, gd->e7, geo->n, E};
+    BF_CUDA(cudaMemcpyAsync(d_thr, thr_l.data(), (uint64_t)kw * 4, cudaMemcpyHostToDevice, st));
+    BF_CUDA(cudaMemsetAsync(lane_seg, 0, (uint64_t)kw * 8, st));
+    BF_CUDA(cudaMemsetAsync(lane_anchor, 0xFF, (uint64_t)kw * 8, st));
+    BF_CUDA(cudaMemsetAsync(tot, 0, 24, st));
+    BF_CUDA(cudaMemsetAsync(d_err, 0, 4, st));
+    if (E) {
+      k_seg_count<<<(unsigned)nb, SEG_TPB, 0, st>>>(a, d_blk, lane_seg, lane_anchor, d_err);
+      k_seg_scan<<<1, 1024, 0, st>>>(nb, d_blk, d_blk + 3 * nb, tot);
+      BF_CUDA(cudaGetLastError());
+    }
+    std::vector<unsigned long long> lane(2ull * kw + 3);
+    uint32_t verr = 0;
+    BF_CUDA(cudaMemcpyAsync(lane.data(), d_lane, lane.size() * 8, cudaMemcpyDeviceToHost, st));
+    BF_CUDA(cudaMemcpyAsync(&verr, d_err, 4, cudaMemcpyDeviceToHost, st));
+    BF_CUDA(cudaStreamSynchronize(st));
+    if (verr) {
+      set_error("bf_isochrone_polygons: a settled rank lies outside the geometry");
+      return BF_ERR_DEVICE;
+    }
+    const uint64_t n_seg = lane[2 * kw], n_pts = lane[2 * kw + 1], n_cut = lane[2 * kw + 2];
+    std::vector<uint64_t> iso_seg(kw + 1, 0);
+    std::vector<uint8_t> has(kw, 0);
+    std::vector<double> anc(2ull * kw, 0.0);
+    for (uint32_t l = 0; l < kw; ++l) {
+      iso_seg[l + 1] = iso_seg[l] + lane[l];
+      const unsigned long long key = lane[kw + l];
+      if (key != ~0ull && lane[l]) {  // no segment: the reference returns no contour
+        const uint64_t p0 = geo->off[(uint32_t)key];
+        has[l] = 1;
+        anc[2 * l] = geo->xy[2 * p0];
+        anc[2 * l + 1] = geo->xy[2 * p0 + 1];
+      }
+    }
+    if (iso_seg[kw] != n_seg) {
+      set_error("bf_isochrone_polygons: segment counts disagree");
+      return BF_ERR_DEVICE;
+    }
+    double2 *d_xy = nullptr, *d_cxy = nullptr;
+    uint64_t *d_seg = nullptr, *d_iseg = nullptr, *d_cpos = nullptr;
+    int2* d_ce7 = nullptr;
+    e = ws_get(ws, S_XY, n_pts * 16, &d_xy);
+    if (e == cudaSuccess) e = ws_get(ws, S_SEG, (n_seg + 1) * 8, &d_seg);
+    if (e == cudaSuccess) e = ws_get(ws, S_ISEG, ((uint64_t)kw + 1) * 8, &d_iseg);
+    if (e == cudaSuccess) e = ws_get(ws, S_CUT, n_cut * 16, &d_cpos);
+    if (e == cudaSuccess) e = ws_get(ws, S_CUTXY, n_cut * 16, &d_cxy);
+    if (e != cudaSuccess) return cuda_status(e, "bf_isochrone_polygons: device memory");
+    d_ce7 = reinterpret_cast<int2*>(d_cpos + n_cut);
+    BF_CUDA(cudaMemsetAsync(d_seg, 0, 8, st));
+    BF_CUDA(cudaMemcpyAsync(d_iseg, iso_seg.data(), ((uint64_t)kw + 1) * 8, cudaMemcpyHostToDevice,
+                            st));
+    if (E) {
+      k_seg_write<<<(unsigned)nb, SEG_TPB, 0, st>>>(a, d_blk + 3 * nb, d_seg, d_xy, d_ce7, d_cpos,
+                                                    d_err);
+      BF_CUDA(cudaGetLastError());
+    }
+    if (n_cut) {
+      std::vector<int32_t> ce7(2 * n_cut);
+      std::vector<double> cxy(2 * n_cut);
+      BF_CUDA(cudaMemcpyAsync(ce7.data(), d_ce7, n_cut * 8, cudaMemcpyDeviceToHost, st));
+      BF_CUDA(cudaStreamSynchronize(st));
+      if ((rc = bf_mercator(n_cut, ce7.data(), cxy.data()))) return rc;
+      BF_CUDA(cudaMemcpyAsync(d_cxy, cxy.data(), n_cut * 16, cudaMemcpyHostToDevice, st));
+      k_cut_scatter<<<grid_of(n_cut), 256, 0, st>>>(n_cut, d_cpos, d_cxy, d_xy);
+      BF_CUDA(cudaGetLastError());
+    }
+    ph[1] += ms(t0);
+    t0 = clk::now();
+    std::vector<bf_raster> ras(std::max<uint32_t>(kw, 1));
+    uint64_t* words = nullptr;
+    uint64_t n_words = 0;
+    if ((rc = rasters_core(ws, st, d_xy, d_seg, d_iseg, n_seg, n_pts, kw, cell_l.data(), has.data(),
+                           anc.data(), dil, ero, ras.data(), &words, &n_words)))
+      return rc;
+    ph[2] += ms(t0);
+    t0 = clk::now();
+    std::vector<uint64_t> roff(kw + 1, 0);
+    double* ll = nullptr;
+    rc = bf_contour_polygons(ras.data(), words, kw, cell_l.data(), simp_l.data(), has.data(),
+                             anc.data(), roff.data(), &ll);
+    bf_contour_free(words);
+    if (rc) return rc;
+    wave_ll.push_back(ll);
+    for (uint32_t l = 0; l < kw; ++l) {
+      r_len[rows[l]] = roff[l + 1] - roff[l];
+      r_at[rows[l]] = (uint64_t)(wave_ll.size() - 1) << 40 | roff[l];  // (wave, point)
+    }
+    ph[3] += ms(t0);
+    mark = clk::now();
+    return BF_OK;
+  };
+  if ((rc = settled_waves(gr, origins, thresholds, n, sink, nullptr))) {
+    free_waves();
+    return rc;
   }
-  try {
-    seg_pt.resize(iso_seg[n] + 1);
-  } catch (const std::bad_alloc&) {
-    bf_settled_free(sr);
-    bf_settled_free(sd);
+  ph[0] += ms(mark);
+  auto t0 = clk::now();
+  ring_off[0] = 0;
+  for (uint64_t k = 0; k < n; ++k) ring_off[k + 1] = ring_off[k] + r_len[k];
+  double* out = (double*)std::malloc(std::max<uint64_t>(ring_off[n], 1) * 16);
+  if (!out) {
+    free_waves();
     set_error("out of host memory");
     return BF_ERR_OOM;
   }
-  seg_pt[0] = 0;
   parallel_for(n, [&](uint64_t k) {
-    uint64_t s = iso_seg[k], p = pt_base[k];
-    walk(k, [&](uint64_t p0, uint64_t take, bool cut, int32_t clat, int32_t clon) {
-      std::memcpy(stage_xy + 2 * p, geo->xy.data() + 2 * p0, take * 16);
-      p += take;
-      if (cut) {
-        mercator_e7(clat, clon, stage_xy + 2 * p, stage_xy + 2 * p + 1);
-        ++p;
-      }
-      seg_pt[++s] = p;
-    });
+    if (!r_len[k]) return;
+    const double* src = wave_ll[r_at[k] >> 40] + 2 * (r_at[k] & ((1ull << 40) - 1));
+    std::memcpy(out + 2 * ring_off[k], src, r_len[k] * 16);
   });
-  bf_settled_free(sr);
-  bf_settled_free(sd);
-  for (uint64_t k = 0; k < n; ++k)
-    if (!nseg[k]) has[k] = 0;  // no segment: the reference returns no contour
-  const double* xy = stage_xy;
-  ph[1] = ms(t0);
-  t0 = clk::now();
-  // 3. rasters (GPU)
-  std::vector<bf_raster> ras(std::max<uint64_t>(n, 1));
-  uint64_t* words = nullptr;
-  uint64_t n_words = 0;
-  if ((rc = bf_contour_rasters(xy, seg_pt.data(), iso_seg.data(), (uint32_t)n, cell.data(),
-                               has.data(), anc.data(), dil, ero, gr->device, ras.data(), &words,
-                               &n_words)))
-    return rc;
-  ph[2] = ms(t0);
-  t0 = clk::now();
-  // 4. polygons (host threads)
-  rc = bf_contour_polygons(ras.data(), words, (uint32_t)n, cell.data(), simp.data(), has.data(),
-                           anc.data(), ring_off, lonlat);
-  bf_contour_free(words);
-  ph[3] = ms(t0);
+  free_waves();
+  *lonlat = out;
+  ph[3] += ms(t0);
   if (phase_ms)
     for (int i = 0; i < 4; ++i) phase_ms[i] = ph[i];
-  return rc;
+  return BF_OK;
 }
 
 }  // extern "C"

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <functional>
 #include <mutex>
 #include <thread>
 #include <string>
@@ -331,12 +332,23 @@ bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, co
 // Settled (rank, distance) lists of bulk isochrones, filled wave by wave:
 // per origin of the call (its index in the call), ranks ascending.
 // Where the bulk settled sets land: the graph's page-locked staging buffer
-// (appended wave by wave) and each origin's place in it.
+// (appended wave by wave) and each origin's place in it, or, with `on_wave`,
+// a consumer of each wave's sets while they are on the device: ranks and
+// distances of lane l at [off[l], off[l + 1]) of d_ranks / d_dists (device
+// lane offsets in d_off), lane l being origin rows[l] of the call.
 struct SettledSink {
   uint64_t base = 0;                     // input index of the chunk's first origin
   uint64_t used = 0;                     // u32 entries of the staging buffer in use
   std::vector<uint64_t> r_at, d_at, cnt;  // per origin: ranks, distances, entries
+  std::function<bf_status(const uint32_t* d_ranks, const uint32_t* d_dists, const uint64_t* d_off,
+                          const std::vector<uint64_t>& off, const std::vector<uint32_t>& rows,
+                          cudaStream_t st)>
+      on_wave;
 };
+// The waves of bf_isochrone_settled for n origins (chunked by bitset memory)
+// into `sink`; the caller holds the graph's lock.
+bf_status settled_waves(Graph* g, const uint32_t* orig, const uint32_t* thr, uint64_t n,
+                        SettledSink& sink, bf_stats* st);
 bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint32_t* d_thr, uint64_t n,
                             uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,
                             bf_stats* stats, SettledSink* sink = nullptr);

@@ -393,6 +393,11 @@ bf_status emit_settled(const T* slab, uint32_t Kp, Graph* g, Sched& sc, const ui
   k_emit<T><<<eg, 256, 0, st>>>(slab, Kp, sc.d_cidx, g->n, bits, w32, d_lane_row, g->d_set_pre,
                                 g->d_set_off, total, g->d_set_out, g->d_set_out + total);
   BF_CUDA(cudaGetLastError());
+  if (sink->on_wave) {
+    std::vector<uint32_t> rows(kw);
+    for (uint32_t l = 0; l < kw; ++l) rows[l] = (uint32_t)(sink->base + h_lane_row[l]);
+    return sink->on_wave(g->d_set_out, g->d_set_out + total, g->d_set_off, off, rows, st);
+  }
   // the wave's ranks then distances, appended to the page-locked staging
   const uint64_t need = sink->used + 2 * total;
   if (need > g->set_stage_cap) {
