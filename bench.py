@@ -441,6 +441,9 @@ def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
     t0 = time.perf_counter()
     rings, ph = bfphast.isochrone_polygons(g, gm, origins, thr, tiers)
     sec = time.perf_counter() - t0
+    _, wst = g.isochrone_settled(origins, thr, stats=True)  # the settled-set wave's device split
+    wave = {k: round(wst[k], 2) for k in ("upward_ms", "downward_ms", "extract_ms", "total_ms")}
+    wave["launches"] = wst["kernel_launches"]
     c = orc.Cch.from_dict(cch)
     pick = [0, count // 2, count - 1][:count]
     exact, cpu_s = True, 0.0
@@ -457,6 +460,7 @@ def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
             "ms": round(sec * 1e3, 2),
             "phases_ms": {"settled_sets": round(ph[0], 2), "segments": round(ph[1], 2),
                           "rasters": round(ph[2], 2), "polygons": round(ph[3], 2)},
+            "settled_wave": wave,
             "mean_ring_vertices": round(float(np.mean([len(r) for r in rings])), 1),
             "geometry_create_ms": round(geo_ms, 1),
             "bit_exact_sample": {"isochrones": len(pick), "equal": exact},
