@@ -97,6 +97,8 @@ struct Sched {
   uint64_t n_items = 0;
   uint64_t n_edges = 0;
   std::vector<uint32_t> lvl_item;  // level -> first work item, n_levels + 1
+  uint32_t* d_lvl = nullptr;     // device copy of lvl_item
+  size_t cap_lvl = 0;
   uint32_t* d_cidx = nullptr;    // [n] rank -> compact row or NONE
   uint4* d_item = nullptr;       // {row, edge0, edge1, split flag}
   uint2* d_erec = nullptr;       // {source row, w}

@@ -333,6 +333,9 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   if ((s = ensure(&sc.d_trow, sc.cap_t, T, g))) return s;
   if ((s = ensure(&c.d_pairs, c.cap_pairs, pairs.size() * 2, g))) return s;
   if ((s = ensure(&sc.d_split, sc.cap_split, split_bits.size(), g))) return s;
+  if ((s = ensure(&sc.d_lvl, sc.cap_lvl, sc.lvl_item.size(), g))) return s;
+  BF_CUDA(cudaMemcpyAsync(sc.d_lvl, sc.lvl_item.data(), sc.lvl_item.size() * 4,
+                          cudaMemcpyHostToDevice, st));
   BF_CUDA(cudaMemcpyAsync(sc.d_split, split_bits.data(), split_bits.size() * 4,
                           cudaMemcpyHostToDevice, st));
   if (!sc.cidx_ready) {
@@ -607,7 +610,8 @@ uint64_t ctx_budget(Graph* g, Ctx& c) {
 }
 
 static void free_sched(Sched& sc) {
-  void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_elen, sc.d_trow, sc.d_split, sc.d_hub};
+  void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_elen, sc.d_trow, sc.d_split, sc.d_hub,
+               sc.d_lvl};
   for (void* q : p)
     if (q) cudaFree(q);
   if (sc.gexec) cudaGraphExecDestroy(sc.gexec);

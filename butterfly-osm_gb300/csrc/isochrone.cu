@@ -59,105 +59,180 @@ __device__ __forceinline__ void atomic_min_u16x2(uint32_t* p, uint32_t v, uint32
 // block does not own one item: the level's items [i0, i1) are dealt out
 // block-stride over a grid sized to the GPU, and a skipped item costs one
 // warp ballot instead of a block launch.
-__global__ void __launch_bounds__(128, 16)
+// One work item of the 16-bit gated sweep for this thread's 8 lanes: every
+// warp evaluates the item's in-edges 32 at a time (warp lane t holds edge
+// base + t, preloaded in r0 for the first 32) and a ballot gives the edges
+// whose source row is active (the same masks in every warp of the item).
+// With CG, rows and activity bits are read through L2: other warps of the
+// same launch may have written them. Every thread of the warp calls it.
+template <bool CG>
+__device__ __forceinline__ void gated16_item(const uint4 it, const uint2 r0,
+                                             const uint2* __restrict__ erec,
+                                             uint16_t* __restrict__ slab, uint32_t Kp,
+                                             uint32_t* __restrict__ active,
+                                             const uint32_t* __restrict__ thr, uint32_t lane,
+                                             bool live, uint32_t valid_lanes,
+                                             const uint32_t* __restrict__ seeded,
+                                             uint32_t* __restrict__ err) {
+  const unsigned FULL = 0xFFFFFFFFu;
+  const uint32_t t = threadIdx.x & 31;
+  uint4 acc = make_uint4(~0u, ~0u, ~0u, ~0u);
+  bool any = false;
+  for (uint32_t base = it.y; base < it.z; base += 32) {
+    const uint32_t e = base + t;
+    uint2 r = make_uint2(0, 0);
+    bool a = false;
+    if (e < it.z) {
+      r = base == it.y ? r0 : erec[e];
+      const uint32_t aw = CG ? __ldcg(active + (r.x >> 5)) : active[r.x >> 5];
+      a = (aw >> (r.x & 31)) & 1u;
+    }
+    uint32_t m = __ballot_sync(FULL, a);
+    any |= m != 0;
+    // gather the active sources four at a time (loads in flight together)
+    while (m) {
+      uint32_t j[4], k = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        j[q] = m ? (uint32_t)(__ffs(m) - 1) : 0u;
+        if (m) {
+          m &= m - 1;
+          ++k;
+        }
+      }
+      uint32_t src[4], w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        src[q] = __shfl_sync(FULL, r.x, j[q]);
+        w[q] = __shfl_sync(FULL, r.y, j[q]);
+      }
+      if (live) {
+        uint4 v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint4* row = reinterpret_cast<const uint4*>(slab + (size_t)src[q] * Kp + lane);
+          v[q] = q < (int)k ? (CG ? __ldcg(row) : *row) : make_uint4(~0u, ~0u, ~0u, ~0u);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint32_t w16 = min(w[q], 0xFFFFu), ww = w16 | (w16 << 16);
+          acc.x = __vminu2(acc.x, __vaddus2(v[q].x, ww));
+          acc.y = __vminu2(acc.y, __vaddus2(v[q].y, ww));
+          acc.z = __vminu2(acc.z, __vaddus2(v[q].z, ww));
+          acc.w = __vminu2(acc.w, __vaddus2(v[q].w, ww));
+        }
+      }
+    }
+  }
+  if (!any) return;  // uniform across the item's warps: the row keeps its seed or INF
+  // clamp each lane to its threshold
+  uint32_t* aw = &acc.x;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    uint32_t lo = aw[q] & 0xFFFFu, hi = aw[q] >> 16;
+    if (2 * q >= (int)valid_lanes || lo > thr[lane + 2 * q]) lo = 0xFFFFu;
+    if (2 * q + 1 >= (int)valid_lanes || hi > thr[lane + 2 * q + 1]) hi = 0xFFFFu;
+    aw[q] = lo | (hi << 16);
+  }
+  if (live) {
+    uint32_t* dst = reinterpret_cast<uint32_t*>(slab + (size_t)it.x * Kp + lane);
+    if (it.w) {
+      atomic_min_u16x2(dst + 0, acc.x, err);
+      atomic_min_u16x2(dst + 1, acc.y, err);
+      atomic_min_u16x2(dst + 2, acc.z, err);
+      atomic_min_u16x2(dst + 3, acc.w, err);
+    } else {
+      // without a full slab reset only seeded rows hold valid data here
+      const bool valid = (seeded[it.x >> 5] >> (it.x & 31)) & 1u;
+      const uint4* d4 = reinterpret_cast<const uint4*>(dst);
+      const uint4 c = valid ? (CG ? __ldcg(d4) : *d4) : make_uint4(~0u, ~0u, ~0u, ~0u);
+      uint4 v;
+      v.x = __vminu2(c.x, acc.x);
+      v.y = __vminu2(c.y, acc.y);
+      v.z = __vminu2(c.z, acc.z);
+      v.w = __vminu2(c.w, acc.w);
+      *reinterpret_cast<uint4*>(dst) = v;
+    }
+  }
+  const bool act = live && (acc.x & acc.y & acc.z & acc.w) != ~0u;
+  const unsigned am = __ballot_sync(FULL, act);
+  if (am && t == (unsigned)(__ffs(am) - 1)) atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
+}
+
+// IPB = 1: the block's warps share each item (lane slices of blockDim.x * 8
+// lanes per y-block); IPB > 1 (waves of at most 256 lanes): each of the
+// block's IPB warps takes its own item, so small waves keep as many items in
+// flight per SM as large ones.
+template <uint32_t IPB>
+__global__ void __launch_bounds__(128, IPB > 1 ? 12 : 16)
     k_sweep_gated16(const uint4* __restrict__ item, uint32_t i0, uint32_t i1,
                     const uint2* __restrict__ erec, uint16_t* __restrict__ slab, uint32_t Kp,
                     uint32_t* __restrict__ active, const uint32_t* __restrict__ thr, uint32_t kw,
                     const uint32_t* __restrict__ seeded, uint32_t* __restrict__ err) {
   asm volatile("griddepcontrol.launch_dependents;");
-  const unsigned FULL = 0xFFFFFFFFu;
   const uint32_t t = threadIdx.x & 31;
-  const uint32_t lane = (blockIdx.y * blockDim.x + threadIdx.x) * 8;
+  constexpr uint32_t ipb = IPB;
+  const uint32_t lane = ipb > 1 ? t * 8 : (blockIdx.y * blockDim.x + threadIdx.x) * 8;
   const uint32_t wbase = lane - 8 * t;
   if (wbase >= Kp) return;  // the whole warp is past the last lane
   const bool live = lane < Kp;
   // lanes of this thread inside the wave (the rest clamp to 0xFFFF)
   const uint32_t valid_lanes = live ? min(8u, kw > lane ? kw - lane : 0u) : 0u;
+  const uint32_t first = ipb > 1 ? blockIdx.x * ipb + (threadIdx.x >> 5) : blockIdx.x;
+  const uint32_t stride = gridDim.x * ipb;
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  for (uint32_t ii = i0 + blockIdx.x; ii < i1; ii += gridDim.x) {
+  for (uint32_t ii = i0 + first; ii < i1; ii += stride) {
     const uint4 it = item[ii];
-    // every warp evaluates the item's in-edges 32 at a time: warp lane t holds
-    // edge base + t, and a ballot gives the edges whose source row is active
-    // (the same masks in every warp)
-    uint4 acc = make_uint4(~0u, ~0u, ~0u, ~0u);
-    bool any = false;
-    for (uint32_t base = it.y; base < it.z; base += 32) {
-      const uint32_t e = base + t;
-      uint2 r = make_uint2(0, 0);
-      bool a = false;
-      if (e < it.z) {
-        r = erec[e];
-        a = (active[r.x >> 5] >> (r.x & 31)) & 1u;
+    const uint2 r0 = it.y + t < it.z ? erec[it.y + t] : make_uint2(0, 0);
+    gated16_item<false>(it, r0, erec, slab, Kp, active, thr, lane, live, valid_lanes, seeded, err);
+  }
+}
+
+// A run of consecutive small levels [l0, l1) of the 16-bit gated sweep in one
+// block of 1024 threads instead of a launch per level: wpi = ceil(Kp / 256)
+// warps share an item (a 256-lane slice each), the block takes 32 / wpi items
+// at a time, and __syncthreads separates the levels (the block's global
+// writes before it are visible to the block after it). Each warp loads its
+// first item record and edge records of the next level before the barrier:
+// they do not depend on the sweep's values. lvl: level -> first item.
+__global__ void __launch_bounds__(1024, 1)
+    k_sweep_run16(const uint4* __restrict__ item, const uint32_t* __restrict__ lvl, uint32_t l0,
+                  uint32_t l1, const uint2* __restrict__ erec, uint16_t* __restrict__ slab,
+                  uint32_t Kp, uint32_t* __restrict__ active, const uint32_t* __restrict__ thr,
+                  uint32_t kw, const uint32_t* __restrict__ seeded, uint32_t* __restrict__ err) {
+  asm volatile("griddepcontrol.launch_dependents;");
+  const uint32_t t = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t wpi = (Kp + 255) / 256;  // 1..32 (the host launches this for Kp <= 8192)
+  const uint32_t slots = 32 / wpi, slot = warp / wpi;
+  const uint32_t lane = (warp % wpi) * 256 + t * 8;
+  const bool warp_live = slot < slots && (warp % wpi) * 256 < Kp;
+  const bool live = warp_live && lane < Kp;
+  const uint32_t valid_lanes = live ? min(8u, kw > lane ? kw - lane : 0u) : 0u;
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  uint32_t i1 = lvl[l0 + 1], ii = lvl[l0] + slot;
+  uint4 it = make_uint4(0, 0, 0, 0);
+  uint2 r0 = make_uint2(0, 0);
+  if (warp_live && ii < i1) {
+    it = item[ii];
+    r0 = it.y + t < it.z ? erec[it.y + t] : make_uint2(0, 0);
+  }
+  for (uint32_t l = l0; l < l1; ++l) {
+    for (bool first = true; warp_live && ii < i1; ii += slots, first = false) {
+      if (!first) {
+        it = item[ii];
+        r0 = it.y + t < it.z ? erec[it.y + t] : make_uint2(0, 0);
       }
-      uint32_t m = __ballot_sync(FULL, a);
-      any |= m != 0;
-      // gather the active sources four at a time (loads in flight together)
-      while (m) {
-        uint32_t j[4], k = 0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          j[q] = m ? (uint32_t)(__ffs(m) - 1) : 0u;
-          if (m) {
-            m &= m - 1;
-            ++k;
-          }
-        }
-        uint32_t src[4], w[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          src[q] = __shfl_sync(FULL, r.x, j[q]);
-          w[q] = __shfl_sync(FULL, r.y, j[q]);
-        }
-        if (live) {
-          uint4 v[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-            v[q] = q < (int)k ? *reinterpret_cast<const uint4*>(slab + (size_t)src[q] * Kp + lane)
-                              : make_uint4(~0u, ~0u, ~0u, ~0u);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const uint32_t w16 = min(w[q], 0xFFFFu), ww = w16 | (w16 << 16);
-            acc.x = __vminu2(acc.x, __vaddus2(v[q].x, ww));
-            acc.y = __vminu2(acc.y, __vaddus2(v[q].y, ww));
-            acc.z = __vminu2(acc.z, __vaddus2(v[q].z, ww));
-            acc.w = __vminu2(acc.w, __vaddus2(v[q].w, ww));
-          }
-        }
-      }
+      gated16_item<true>(it, r0, erec, slab, Kp, active, thr, lane, live, valid_lanes, seeded, err);
     }
-    if (!any) continue;  // uniform across the block: the row keeps its seed or INF
-    // clamp each lane to its threshold
-    uint32_t* aw = &acc.x;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      uint32_t lo = aw[q] & 0xFFFFu, hi = aw[q] >> 16;
-      if (2 * q >= (int)valid_lanes || lo > thr[lane + 2 * q]) lo = 0xFFFFu;
-      if (2 * q + 1 >= (int)valid_lanes || hi > thr[lane + 2 * q + 1]) hi = 0xFFFFu;
-      aw[q] = lo | (hi << 16);
-    }
-    if (live) {
-      uint32_t* dst = reinterpret_cast<uint32_t*>(slab + (size_t)it.x * Kp + lane);
-      if (it.w) {
-        atomic_min_u16x2(dst + 0, acc.x, err);
-        atomic_min_u16x2(dst + 1, acc.y, err);
-        atomic_min_u16x2(dst + 2, acc.z, err);
-        atomic_min_u16x2(dst + 3, acc.w, err);
-      } else {
-        // without a full slab reset only seeded rows hold valid data here
-        const bool valid = (seeded[it.x >> 5] >> (it.x & 31)) & 1u;
-        const uint4 c =
-            valid ? *reinterpret_cast<const uint4*>(dst) : make_uint4(~0u, ~0u, ~0u, ~0u);
-        uint4 v;
-        v.x = __vminu2(c.x, acc.x);
-        v.y = __vminu2(c.y, acc.y);
-        v.z = __vminu2(c.z, acc.z);
-        v.w = __vminu2(c.w, acc.w);
-        *reinterpret_cast<uint4*>(dst) = v;
+    if (l + 1 < l1) {  // the next level's first item, before the barrier
+      i1 = lvl[l + 2];
+      ii = lvl[l + 1] + slot;
+      if (warp_live && ii < i1) {
+        it = item[ii];
+        r0 = it.y + t < it.z ? erec[it.y + t] : make_uint2(0, 0);
       }
     }
-    const bool act = live && (acc.x & acc.y & acc.z & acc.w) != ~0u;
-    const unsigned am = __ballot_sync(FULL, act);
-    if (am && t == (unsigned)(__ffs(am) - 1)) atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
+    __syncthreads();
   }
 }
 
@@ -520,11 +595,31 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
     if (stats) BF_CUDA(cudaEventRecord(c.ev[1], st));
     if (half) {
       const bool pdl = g->tune.pdl != 0;
+      // runs of consecutive levels of at most two rounds of one block's items
+      // go to k_sweep_run16 (one launch per run)
+      const uint32_t wpi = (Kp + 255) / 256;
+      const uint32_t small = wpi <= 32 ? 2 * (32 / wpi) : 0;
       for (uint32_t l = 0; l < g->n_levels; ++l) {
         const uint32_t i0 = sc.lvl_item[l], i1 = sc.lvl_item[l + 1];
         if (i1 == i0) continue;
-        const uint32_t blocks = std::min<uint32_t>(i1 - i0, GATED16_BLOCKS);
-        BF_CUDA(launch_level(k_sweep_gated16, dim3(blocks, lane_blocks), tpb, pdl, st,
+        if (i1 - i0 <= small) {
+          uint32_t l1 = l + 1;
+          while (l1 < g->n_levels && sc.lvl_item[l1 + 1] - sc.lvl_item[l1] <= small) ++l1;
+          if (l1 - l >= 2) {
+            BF_CUDA(launch_level(k_sweep_run16, dim3(1), 1024, pdl, st, (const uint4*)sc.d_item,
+                                 (const uint32_t*)sc.d_lvl, l, l1, (const uint2*)sc.d_erec,
+                                 slab16, Kp, d_active, (const uint32_t*)(p_thr + s0), (uint32_t)kw,
+                                 (const uint32_t*)d_seeded, g->d_err));
+            ++launches;
+            l = l1 - 1;
+            continue;
+          }
+        }
+        const bool own = Kp <= 256;  // four warps per block with their own items
+        const uint32_t blocks = own ? std::min<uint32_t>((i1 - i0 + 3) / 4, 152 * 12)
+                                    : std::min<uint32_t>(i1 - i0, GATED16_BLOCKS);
+        BF_CUDA(launch_level(own ? k_sweep_gated16<4> : k_sweep_gated16<1>,
+                             dim3(blocks, own ? 1 : lane_blocks), own ? 128 : tpb, pdl, st,
                              (const uint4*)sc.d_item, i0, i1, (const uint2*)sc.d_erec, slab16,
                              Kp, d_active, (const uint32_t*)(p_thr + s0), (uint32_t)kw,
                              (const uint32_t*)d_seeded, g->d_err));
