@@ -703,25 +703,38 @@ double seg_dist(PtD p, PtD s, PtD e) {
   return std::sqrt(pdx * pdx + pdy * pdy);
 }
 
+// Douglas-Peucker (sparse_contour.rs douglas_peucker) on indices: a range
+// [s, e] keeps its farthest interior point (the first of equal distances)
+// when that distance exceeds tol and splits there; the output is every
+// kept point in order, exactly the recursive form's result.
 std::vector<PtD> simplify(const std::vector<PtD>& pts, double tol) {
-  if (pts.size() <= 2) return pts;
-  double max_d = 0.0;
-  size_t max_i = 0;
-  for (size_t i = 1; i + 1 < pts.size(); ++i) {
-    const double d = seg_dist(pts[i], pts.front(), pts.back());
-    if (d > max_d) {
-      max_d = d;
-      max_i = i;
+  const size_t n = pts.size();
+  if (n <= 2) return pts;
+  std::vector<uint8_t> keep(n, 0);
+  keep[0] = keep[n - 1] = 1;
+  std::vector<std::pair<size_t, size_t>> todo{{0, n - 1}};
+  while (!todo.empty()) {
+    const auto [a, b] = todo.back();
+    todo.pop_back();
+    double max_d = 0.0;
+    size_t max_i = 0;
+    for (size_t i = a + 1; i < b; ++i) {
+      const double d = seg_dist(pts[i], pts[a], pts[b]);
+      if (d > max_d) {
+        max_d = d;
+        max_i = i;
+      }
+    }
+    if (max_d > tol) {
+      keep[max_i] = 1;
+      todo.emplace_back(max_i, b);
+      todo.emplace_back(a, max_i);
     }
   }
-  if (max_d > tol) {
-    std::vector<PtD> left = simplify(std::vector<PtD>(pts.begin(), pts.begin() + max_i + 1), tol);
-    std::vector<PtD> right = simplify(std::vector<PtD>(pts.begin() + max_i, pts.end()), tol);
-    left.pop_back();
-    left.insert(left.end(), right.begin(), right.end());
-    return left;
-  }
-  return {pts.front(), pts.back()};
+  std::vector<PtD> out;
+  for (size_t i = 0; i < n; ++i)
+    if (keep[i]) out.push_back(pts[i]);
+  return out;
 }
 
 // The outer ring of one closed raster, as (lon, lat).
@@ -774,7 +787,15 @@ std::vector<PtD> polygon_of(const bf_raster& R, const uint64_t* words, double ce
       }
     }
   if (n_tiles == 0) return {};
-  std::sort(starts.begin(), starts.end());
+  {  // (col, row) order: the scan gives rows ascending, so a stable counting sort by column
+    const uint64_t ncol = (uint64_t)R.width_words * 64;
+    std::vector<uint32_t> at(ncol + 1, 0);
+    for (const auto& st : starts) ++at[(uint64_t)(std::get<0>(st) - R.col0) + 1];
+    for (uint64_t c = 0; c < ncol; ++c) at[c + 1] += at[c];
+    std::vector<std::tuple<int32_t, int32_t, uint8_t>> by_col(starts.size());
+    for (const auto& st : starts) by_col[at[(uint64_t)(std::get<0>(st) - R.col0)]++] = st;
+    starts.swap(by_col);
+  }
   t.seen.assign(t.cols * R.height, 0);
   const uint64_t max_iter = n_tiles * 64 * 64 * 4;
   std::vector<std::vector<PtD>> rings;
