@@ -737,6 +737,33 @@ std::vector<PtD> simplify(const std::vector<PtD>& pts, double tol) {
   return out;
 }
 
+// Visited-edge arrays of the tracer, reused across isochrones and calls
+// (first-touch page faults of a fresh array cost as much as the trace).
+struct SeenPool {
+  std::mutex mu;
+  std::vector<std::vector<uint8_t>> free;
+};
+SeenPool& seen_pool() {
+  static SeenPool p;
+  return p;
+}
+struct SeenLease {
+  std::vector<uint8_t>& v;
+  explicit SeenLease(std::vector<uint8_t>& x) : v(x) {
+    SeenPool& p = seen_pool();
+    std::lock_guard<std::mutex> lk(p.mu);
+    if (!p.free.empty()) {
+      v.swap(p.free.back());
+      p.free.pop_back();
+    }
+  }
+  ~SeenLease() {
+    SeenPool& p = seen_pool();
+    std::lock_guard<std::mutex> lk(p.mu);
+    if (p.free.size() < 64) p.free.push_back(std::move(v));
+  }
+};
+
 // The outer ring of one closed raster, as (lon, lat).
 std::vector<PtD> polygon_of(const bf_raster& R, const uint64_t* words, double cell,
                             double simplify_m, const PtD* anchor_xy) {
@@ -796,7 +823,9 @@ std::vector<PtD> polygon_of(const bf_raster& R, const uint64_t* words, double ce
     for (const auto& st : starts) by_col[at[(uint64_t)(std::get<0>(st) - R.col0)]++] = st;
     starts.swap(by_col);
   }
-  t.seen.assign(t.cols * R.height, 0);
+  SeenLease lease(t.seen);
+  if (t.seen.size() < t.cols * R.height) t.seen.resize(t.cols * R.height);
+  std::memset(t.seen.data(), 0, t.cols * R.height);
   const uint64_t max_iter = n_tiles * 64 * 64 * 4;
   std::vector<std::vector<PtD>> rings;
   for (const auto& s : starts) {
