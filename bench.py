@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=100.0, help="arrivals per second")
     ap.add_argument("--isochrones", type=int, default=100000,
                     help="bulk isochrone origins (0 = skip)")
+    ap.add_argument("--no-tiles", action="store_true",
+                    help="skip the matrix tile emission leg")
     ap.add_argument("--no-customize", action="store_true",
                     help="skip the CCH customization leg")
     ap.add_argument("--contours", type=int, default=64,
@@ -288,6 +290,8 @@ def run_ours(args, rank, world, dist):
         res["contours"] = run_contours(g, cch, args.contours, args.cols)
     if not args.no_customize and rank == 0:
         res["customize"] = run_customize(cch, args.steps, args.warmup, not args.no_cpu)
+    if not args.no_tiles and rank == 0:
+        res["tiles"] = run_tiles(out_dev, args.steps, args.warmup, not args.no_cpu)
     return res, cch, src, tgt, out_dev
 
 
@@ -469,6 +473,111 @@ def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
                              "sample": "%d origins of the batch from the origin (bounded query "
                                        "and geometry), %.1f s" % (len(pick), cpu_s)},
             "data": "synthetic lattice coordinates, straight tail -> head road polylines"}
+
+
+def run_tiles(mat, steps, warmup, with_cpu, seed=13):
+    """Matrix tile emission (build_matrix_batch / build_matrix_tile_batch,
+    flight.rs:432-589) of the 10k x 10k matrix just computed: the four UInt32
+    RecordBatch columns. `dense`: every cell, no bound (20 algorithmic bytes
+    per cell: the duration read, four u32 written), through
+    bf_tile_emit_device on the device-resident matrix, CUDA events on the
+    launching stream; `sparse`: a seeded radius mask keeping 20 % of each
+    row's destinations and a 30-minute bound, sentinel cells dropped. `e2e`:
+    bf_tile_emit with page-locked host arrays (matrix in, columns out). The
+    CPU baseline is the oracle's single-threaded builder loop (the reference
+    builds a tile on one thread) on a row sample; a row sample of both forms
+    is compared column for column."""
+    import numpy as np
+    import torch
+    import bfphast
+    from oracle import oracle as orc
+    S, T = mat.shape
+    n = S * T
+    dev = torch.device("cuda:0")
+    d_m = torch.from_numpy(np.ascontiguousarray(mat).reshape(-1).view(np.int32)).to(dev)
+    d_s = torch.arange(S, dtype=torch.int32, device=dev)
+    d_t = torch.arange(T, dtype=torch.int32, device=dev)
+    cols = [torch.empty(n, dtype=torch.int32, device=dev) for _ in range(4)]
+    rng = np.random.default_rng(seed)
+    counts, flat = np.zeros(S, np.int64), []
+    for r0 in range(0, S, 1000):  # each destination kept with probability 0.2
+        rr, cc = np.nonzero(rng.random((min(1000, S - r0), T)) < 0.2)
+        counts[r0:r0 + 1000] = np.bincount(rr, minlength=min(1000, S - r0))
+        flat.append(cc.astype(np.uint32))
+    mask = np.concatenate(flat)
+    moff = np.zeros(S + 1, np.uint64)
+    moff[1:] = np.cumsum(counts)
+    n_mask = len(mask)
+    d_moff = torch.from_numpy(moff.view(np.int64)).to(dev)
+    d_mask = torch.from_numpy(mask.view(np.int32)).to(dev)
+    bound = 18000  # 30 minutes in the graph's deciseconds
+    stream = torch.cuda.current_stream()
+
+    def emit(sparse):
+        return bfphast.tile_emit_device(
+            d_m.data_ptr(), S, T, d_s.data_ptr(), d_t.data_ptr(), [c.data_ptr() for c in cols],
+            bound if sparse else bfphast.INF, d_moff.data_ptr() if sparse else None,
+            d_mask.data_ptr() if sparse else None, S if sparse else 0,
+            n_mask if sparse else 0, None, sparse, 0, stream.cuda_stream)
+
+    out = {}
+    for sparse in (False, True):
+        for _ in range(warmup):
+            rows = emit(sparse)
+        times = []
+        for _ in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            rows = emit(sparse)
+            b.record(stream)
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b))
+        ms = float(np.median(times))
+        got = [c[:min(rows, 200 * T)].cpu().numpy().view(np.uint32) for c in cols]
+        sample = 200
+        want = orc.tile_emit(mat[:sample], sample, T, np.arange(sample), np.arange(T),
+                             bound if sparse else orc.INF,
+                             (moff[:sample + 1], mask[:int(moff[sample])]) if sparse else None,
+                             None, sparse)
+        exact = all(np.array_equal(g[:len(w)], w) for g, w in zip(got, want))
+        alg = (4 * n + 16 * rows) + ((4 * n_mask) if sparse else 0)
+        out["sparse" if sparse else "dense"] = {
+            "rows": int(rows), "ms": round(ms, 3), "cells_per_s": round(n / ms * 1e3, 1),
+            "gpu_launches": 3 if sparse else 1,
+            "roofline": {"bound": "hbm", "achieved": round(alg / ms / 1e6, 1), "peak": 6775.9,
+                         "unit": "GB/s", "frac": round(alg / ms / 1e6 / 6775.9, 3),
+                         "algorithmic_bytes": int(alg), "peak_source": "measured"},
+            "bit_exact_sample": {"rows": sample, "equal": bool(exact)}}
+    # end to end: page-locked host matrix in, page-locked columns out
+    pin = lambda k: torch.empty(k, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    h_m = pin(n)
+    h_m[:] = mat.reshape(-1)
+    h_cols = [pin(n) for _ in range(4)]
+    sr, tr = np.arange(S, dtype=np.uint32), np.arange(T, dtype=np.uint32)
+    for sparse in (False, True):
+        kw = dict(threshold=bound if sparse else bfphast.INF,
+                  mask=(moff, mask) if sparse else None, sparse=sparse, out=h_cols)
+        bfphast.tile_emit(h_m, S, T, sr, tr, **kw)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            r = bfphast.tile_emit(h_m, S, T, sr, tr, **kw)
+        sec = (time.perf_counter() - t0) / steps
+        rows = len(r[0])
+        out["sparse" if sparse else "dense"]["e2e"] = {
+            "value": round(n / sec, 1), "unit": "cells/s", "ms": round(sec * 1e3, 2),
+            "h2d_bytes_per_step": int(4 * n + (8 * (S + 1) + 4 * n_mask if sparse else 0)),
+            "d2h_bytes_per_step": int(16 * rows)}
+    if with_cpu:
+        rows_cpu = 300
+        t0 = time.perf_counter()
+        orc.tile_emit(mat[:rows_cpu], rows_cpu, T, np.arange(rows_cpu), np.arange(T))
+        sec = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(rows_cpu * T / sec, 1), "unit": "cells/s",
+                               "cores": 1, "kind": "port",
+                               "sample": "%d rows x %d targets, dense, %.2f s" % (rows_cpu, T, sec)}
+    out["workload"] = "10k x 10k matrix of the country graph (device-resident), original indices = positions"
+    return out
 
 
 def run_customize(cch, steps, warmup, with_cpu):

@@ -143,6 +143,11 @@ class Raster(ctypes.Structure):
                 ("origin_y", ctypes.c_double)]
 
 
+class TileColumns(ctypes.Structure):
+    _fields_ = [("source_idx", ctypes.c_void_p), ("target_idx", ctypes.c_void_p),
+                ("duration_ms", ctypes.c_void_p), ("distance_m", ctypes.c_void_p)]
+
+
 # Every symbol include/bf_phast.h declares, with its ctypes signature.
 _SIGNATURES = {
     "bf_graph_create": (ctypes.c_int, [ctypes.POINTER(CchCsr), ctypes.POINTER(Config),
@@ -236,6 +241,18 @@ _SIGNATURES = {
                                              ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                              _u64p, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
                                              ctypes.c_void_p]),
+    "bf_tile_emit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                    ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                    ctypes.POINTER(TileColumns), _u64p]),
+    "bf_tile_emit_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                           ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32,
+                                           ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.POINTER(TileColumns), _u64p]),
+    "bf_tile_release": (None, [ctypes.c_int]),
     "bf_last_error": (ctypes.c_char_p, []),
 }
 
@@ -797,3 +814,53 @@ def isochrone_polygons(graph, geometry, origins, thresholds, tier_thresholds=Non
     finally:
         lib.bf_contour_free_polygons(out)
     return [flat[2 * int(off[k]):2 * int(off[k + 1])].reshape(-1, 2) for k in range(len(o))], ph
+
+
+def _mask_csr(mask):
+    if mask is None:
+        return None, None, 0
+    if isinstance(mask, tuple):
+        off, flat = np.ascontiguousarray(mask[0], np.uint64), np.ascontiguousarray(mask[1], np.uint32)
+    else:
+        off = np.zeros(len(mask) + 1, np.uint64)
+        off[1:] = np.cumsum([len(m) for m in mask]) if len(mask) else []
+        flat = np.asarray([v for m in mask for v in m], np.uint32)
+    return off, (flat if len(flat) else np.zeros(1, np.uint32)), len(off) - 1
+
+
+def tile_emit(matrix, n_src, n_dst, src_orig, dst_orig, threshold=INF, mask=None, lat=None,
+              sparse=False, device=0, out=None):
+    """bf_tile_emit on host arrays: (source_idx, target_idx, duration_ms,
+    distance_m) of a row-major n_src x n_dst block. `mask`: list (by original
+    source index) of sorted original destination indices, or (offsets, flat).
+    `out`: optional four u32 arrays of n_src * n_dst values to write into."""
+    lib = load()
+    m = np.ascontiguousarray(np.asarray(matrix).reshape(-1), np.uint32)
+    so, do = _u32(src_orig), _u32(dst_orig)
+    la = None if lat is None else np.ascontiguousarray(np.asarray(lat).reshape(-1), np.uint32)
+    moff, mflat, n_mask = _mask_csr(mask)
+    cap = max(1, n_src * n_dst)
+    cols = out if out is not None else [np.empty(cap, np.uint32) for _ in range(4)]
+    tc = TileColumns(*[c.ctypes.data for c in cols])
+    rows = ctypes.c_uint64(0)
+    _check(lib.bf_tile_emit(m.ctypes.data, None if la is None else la.ctypes.data, n_src, n_dst,
+                            so.ctypes.data, do.ctypes.data, threshold,
+                            None if moff is None else moff.ctypes.data,
+                            None if mflat is None else mflat.ctypes.data, n_mask, int(sparse),
+                            device, ctypes.byref(tc), ctypes.byref(rows)))
+    k = rows.value
+    return tuple(c[:k] for c in cols)
+
+
+def tile_emit_device(d_matrix, n_src, n_dst, d_src_orig, d_dst_orig, d_cols, threshold=INF,
+                     d_mask_off=None, d_mask=None, n_mask_src=0, n_mask=0, d_lat=None,
+                     sparse=False, device=0, stream=None):
+    """bf_tile_emit_device on device addresses (integers); d_cols: four device
+    addresses of n_src * n_dst u32 each. Returns the rows written."""
+    tc = TileColumns(*d_cols)
+    rows = ctypes.c_uint64(0)
+    _check(load().bf_tile_emit_device(d_matrix, d_lat, n_src, n_dst, d_src_orig, d_dst_orig,
+                                      threshold, d_mask_off, d_mask, n_mask_src, n_mask,
+                                      int(sparse), device, stream, ctypes.byref(tc),
+                                      ctypes.byref(rows)))
+    return rows.value

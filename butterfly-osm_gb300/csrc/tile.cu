@@ -1,0 +1,492 @@
+// Matrix tile emission on the device: the four UInt32 columns of a matrix
+// RecordBatch (source_idx, target_idx, duration_ms, distance_m) from a
+// row-major block of durations, as build_matrix_batch and
+// build_matrix_tile_batch build them on the host
+// (route/src/server/flight.rs:432-500, :509-589):
+//   * cells in row-major order; a cell is pruned when the source's sorted
+//     radius list (indexed by the source's original index) lacks the
+//     destination's original index (:452-456, :528-532);
+//   * a pruned cell reads u32::MAX, any other the matrix value, u32::MAX
+//     above the time bound (:459, :534-539);
+//   * sparse output drops cells whose duration is u32::MAX (:465, :542);
+//   * duration_ms = d.saturating_mul(1000); distance_m = the lat matrix's
+//     cell or u32::MAX; both u32::MAX on a sentinel cell (:470-483, :548-566).
+// The columns come out as plain u32 arrays: Arrow's layout of a UInt32 array
+// without nulls, so the caller wraps them without a copy.
+//
+// Dense: one thread per cell, or per four cells with 16-byte accesses when
+// rows are a multiple of four cells (2D grid: columns x rows), reads and the
+// four column writes coalesced. Sparse: an order-preserving compaction - per
+// block of 2048 cells a count, a one-block scan of the counts, then an
+// ordered write in which each 256-cell step is scanned within the block.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+
+using namespace bf;
+
+namespace {
+
+constexpr uint32_t MAXV = 0xFFFFFFFFu;
+constexpr uint32_t TPB = 256, ITEMS = 8, CELLS = TPB * ITEMS;
+constexpr uint32_t ERR_NO_LIST = 1u, ERR_BAD_LIST = 2u;
+
+struct TileIn {
+  const uint32_t* m;
+  const uint32_t* lat;  // may be null
+  uint32_t n_src, n_dst;
+  const uint32_t* src_orig;
+  const uint32_t* dst_orig;
+  uint32_t threshold;
+  const uint64_t* mask_off;  // null: no radius mask
+  const uint32_t* mask;
+  uint32_t n_mask_src;
+  uint64_t n_mask;
+  uint32_t sparse;
+};
+
+struct TileOut {
+  uint32_t *s, *t, *du, *di;
+};
+
+// (row, column) of a flat cell index; 32-bit division when the block allows.
+__device__ __forceinline__ void split(uint64_t i, uint32_t n_dst, bool narrow, uint32_t* si,
+                                      uint32_t* di) {
+  if (narrow) {
+    const uint32_t q = (uint32_t)i / n_dst;
+    *si = q;
+    *di = (uint32_t)i - q * n_dst;
+  } else {
+    *si = (uint32_t)(i / n_dst);
+    *di = (uint32_t)(i % n_dst);
+  }
+}
+
+// The cell's duration d (already loaded) after pruning and the time bound
+// (both give u32::MAX, so the bound is tested first and only cells within
+// it search the radius list); os, od: the original indices.
+__device__ __forceinline__ uint32_t decide(const TileIn& a, uint32_t d, uint32_t os, uint32_t od,
+                                           uint32_t* err) {
+  if (a.mask_off && os >= a.n_mask_src) {  // the reference indexes every row's list
+    atomicOr(err, ERR_NO_LIST);
+    return MAXV;
+  }
+  if (d > a.threshold) return MAXV;
+  if (a.mask_off) {
+    uint64_t lo = a.mask_off[os], hi = a.mask_off[os + 1];
+    if (hi < lo || hi > a.n_mask) {
+      atomicOr(err, ERR_BAD_LIST);
+      return MAXV;
+    }
+    bool found = false;
+    while (lo < hi) {  // binary_search on the sorted list
+      const uint64_t mid = lo + ((hi - lo) >> 1);
+      const uint32_t v = a.mask[mid];
+      if (v < od) {
+        lo = mid + 1;
+      } else if (v > od) {
+        hi = mid;
+      } else {
+        found = true;
+        break;
+      }
+    }
+    if (!found) return MAXV;
+  }
+  return d;
+}
+
+__device__ __forceinline__ uint32_t cell_value(const TileIn& a, uint32_t si, uint32_t di,
+                                               uint64_t cell, uint32_t* os, uint32_t* od,
+                                               uint32_t* err) {
+  *os = a.src_orig[si];
+  *od = a.dst_orig[di];
+  return decide(a, a.m[cell], *os, *od, err);
+}
+
+__device__ __forceinline__ void put(const TileIn& a, const TileOut& o, uint64_t k, uint64_t cell,
+                                    uint32_t os, uint32_t od, uint32_t d) {
+  o.s[k] = os;
+  o.t[k] = od;
+  if (d == MAXV) {
+    o.du[k] = MAXV;
+    o.di[k] = MAXV;
+  } else {
+    const uint64_t ms = (uint64_t)d * 1000u;
+    o.du[k] = ms > MAXV ? MAXV : (uint32_t)ms;
+    o.di[k] = a.lat ? a.lat[cell] : MAXV;
+  }
+}
+
+
+__global__ void __launch_bounds__(TPB) k_tile_dense(TileIn a, TileOut o, uint32_t* err) {
+  for (uint32_t si = blockIdx.y; si < a.n_src; si += gridDim.y)
+    for (uint32_t di = blockIdx.x * TPB + threadIdx.x; di < a.n_dst; di += gridDim.x * TPB) {
+      const uint64_t cell = (uint64_t)si * a.n_dst + di;
+      uint32_t os, od;
+      const uint32_t d = cell_value(a, si, di, cell, &os, &od, err);
+      put(a, o, cell, cell, os, od, d);
+    }
+}
+
+// Dense with four cells per thread (n_dst a multiple of 4, arrays 16-byte
+// aligned): one 16-byte load of durations (and lat) and one 16-byte store
+// per column.
+__global__ void __launch_bounds__(TPB) k_tile_dense4(TileIn a, TileOut o, uint32_t* err) {
+  const uint32_t q4 = a.n_dst >> 2;
+  for (uint32_t si = blockIdx.y; si < a.n_src; si += gridDim.y) {
+    const uint32_t os = a.src_orig[si];
+    const bool no_list = a.mask_off && os >= a.n_mask_src;
+    if (no_list && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_NO_LIST);
+    for (uint32_t q = blockIdx.x * TPB + threadIdx.x; q < q4; q += gridDim.x * TPB) {
+      const uint64_t cell = (uint64_t)si * a.n_dst + 4ull * q;
+      const uint4 m4 = *reinterpret_cast<const uint4*>(a.m + cell);
+      const uint4 l4 = a.lat ? *reinterpret_cast<const uint4*>(a.lat + cell)
+                             : make_uint4(MAXV, MAXV, MAXV, MAXV);
+      const uint4 od = *reinterpret_cast<const uint4*>(a.dst_orig + 4ull * q);
+      const uint32_t dv[4] = {m4.x, m4.y, m4.z, m4.w}, lv[4] = {l4.x, l4.y, l4.z, l4.w};
+      const uint32_t ov[4] = {od.x, od.y, od.z, od.w};
+      uint32_t du[4], di[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        uint32_t d = no_list || dv[k] > a.threshold ? MAXV : dv[k];
+        if (d != MAXV && a.mask_off) {
+          uint64_t lo = a.mask_off[os], hi = a.mask_off[os + 1];
+          if (hi < lo || hi > a.n_mask) {
+            atomicOr(err, ERR_BAD_LIST);
+            d = MAXV;
+          } else {
+            bool found = false;
+            while (lo < hi) {
+              const uint64_t mid = lo + ((hi - lo) >> 1);
+              const uint32_t v = a.mask[mid];
+              if (v < ov[k]) {
+                lo = mid + 1;
+              } else if (v > ov[k]) {
+                hi = mid;
+              } else {
+                found = true;
+                break;
+              }
+            }
+            if (!found) d = MAXV;
+          }
+        }
+        if (d == MAXV) {
+          du[k] = MAXV;
+          di[k] = MAXV;
+        } else {
+          const uint64_t ms = (uint64_t)d * 1000u;
+          du[k] = ms > MAXV ? MAXV : (uint32_t)ms;
+          di[k] = lv[k];
+        }
+      }
+      *reinterpret_cast<uint4*>(o.s + cell) = make_uint4(os, os, os, os);
+      *reinterpret_cast<uint4*>(o.t + cell) = od;
+      *reinterpret_cast<uint4*>(o.du + cell) = make_uint4(du[0], du[1], du[2], du[3]);
+      *reinterpret_cast<uint4*>(o.di + cell) = make_uint4(di[0], di[1], di[2], di[3]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TPB)
+    k_tile_count(TileIn a, uint64_t n, bool narrow, unsigned long long* __restrict__ cnt,
+                 uint32_t* err) {
+  __shared__ uint32_t red[TPB / 32];
+  const uint64_t base = (uint64_t)blockIdx.x * CELLS;
+  uint32_t c = 0;
+  for (uint32_t j = 0; j < ITEMS; ++j) {
+    const uint64_t i = base + (uint64_t)j * TPB + threadIdx.x;
+    if (i >= n) break;
+    uint32_t si, di, os, od;
+    split(i, a.n_dst, narrow, &si, &di);
+    c += cell_value(a, si, di, i, &os, &od, err) != MAXV;
+  }
+  for (int s = 16; s > 0; s >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (uint32_t w = 0; w < TPB / 32; ++w) t += red[w];
+    cnt[blockIdx.x] = t;
+  }
+}
+
+// Exclusive scan of nb block counts in one block; the total last.
+__global__ void __launch_bounds__(1024)
+    k_tile_scan(uint64_t nb, const unsigned long long* __restrict__ cnt,
+                unsigned long long* __restrict__ pre, unsigned long long* __restrict__ total) {
+  __shared__ unsigned long long sh[32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long carry = 0;
+  for (uint64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+    const uint64_t b = b0 + threadIdx.x;
+    const unsigned long long v = b < nb ? cnt[b] : 0;
+    unsigned long long x = v;
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned long long s = lane < (blockDim.x >> 5) ? sh[lane] : 0;
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, s, d);
+        if (lane >= d) s += y;
+      }
+      sh[lane] = s;
+    }
+    __syncthreads();
+    if (b < nb) pre[b] = carry + (warp ? sh[warp - 1] : 0) + x - v;
+    carry += sh[(blockDim.x >> 5) - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(TPB)
+    k_tile_write(TileIn a, TileOut o, uint64_t n, bool narrow,
+                 const unsigned long long* __restrict__ pre, uint32_t* err) {
+  __shared__ uint32_t sh[TPB / 32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t base = (uint64_t)blockIdx.x * CELLS;
+  uint64_t k0 = pre[blockIdx.x];
+  for (uint32_t j = 0; j < ITEMS; ++j) {
+    const uint64_t i = base + (uint64_t)j * TPB + threadIdx.x;
+    if (base + (uint64_t)j * TPB >= n) break;  // uniform across the block
+    uint32_t si = 0, di = 0, os = 0, od = 0, d = MAXV;
+    if (i < n) {
+      split(i, a.n_dst, narrow, &si, &di);
+      d = cell_value(a, si, di, i, &os, &od, err);
+    }
+    const uint32_t keep = i < n && d != MAXV;
+    const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
+    if (lane == 0) sh[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t before = 0, step = 0;
+    for (uint32_t w = 0; w < TPB / 32; ++w) {
+      if (w < warp) before += sh[w];
+      step += sh[w];
+    }
+    __syncthreads();
+    if (keep) put(a, o, k0 + before + __popc(bal & ((1u << lane) - 1u)), i, os, od, d);
+    k0 += step;
+  }
+}
+
+// Scratch of the device variant and the host variant's copies, per device.
+struct TileWs {
+  std::mutex mu;
+  cudaStream_t st = nullptr;
+  void* buf[12] = {};
+  size_t cap[12] = {};
+};
+TileWs& tile_ws(int device) {
+  static TileWs ws[64];
+  return ws[device];
+}
+
+template <class T>
+cudaError_t ws_get(TileWs& ws, int i, size_t bytes, T** p) {
+  bytes = std::max<size_t>(bytes, 16);
+  if (ws.cap[i] < bytes) {
+    if (ws.buf[i]) cudaFree(ws.buf[i]);
+    ws.buf[i] = nullptr;
+    ws.cap[i] = 0;
+    const cudaError_t e = cudaMalloc(&ws.buf[i], bytes);
+    if (e != cudaSuccess) return e;
+    ws.cap[i] = bytes;
+  }
+  *p = reinterpret_cast<T*>(ws.buf[i]);
+  return cudaSuccess;
+}
+
+bf_status check_args(uint32_t n_src, uint32_t n_dst, const void* m, const void* so,
+                     const void* dor, const bf_tile_columns* out, uint64_t* n_rows,
+                     const void* mask_off, const void* mask, uint64_t n_mask) {
+  if (!out || !n_rows || (n_src && n_dst && (!m || !so || !dor)) ||
+      (uint64_t)n_src * n_dst && (!out->source_idx || !out->target_idx || !out->duration_ms ||
+                                  !out->distance_m) ||
+      (mask_off && n_mask && !mask)) {
+    set_error("bf_tile_emit: null argument");
+    return BF_ERR_INVALID;
+  }
+  (void)mask_off;
+  return BF_OK;
+}
+
+// Emission from device inputs into device columns on `st`; *n_rows after a
+// synchronisation of the stream.
+bf_status emit_device(TileWs& ws, const TileIn& a, const TileOut& o, cudaStream_t st,
+                      uint64_t* n_rows) {
+  const uint64_t n = (uint64_t)a.n_src * a.n_dst;
+  uint32_t* d_err = nullptr;
+  BF_CUDA(ws_get(ws, 0, 4, &d_err));
+  BF_CUDA(cudaMemsetAsync(d_err, 0, 4, st));
+  uint64_t rows = 0;
+  if (n && !a.sparse) {
+    auto al = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
+    const bool v4 = a.n_dst % 4 == 0 && al(a.m) && (!a.lat || al(a.lat)) && al(a.dst_orig) &&
+                    al(o.s) && al(o.t) && al(o.du) && al(o.di);
+    const uint32_t per_row = v4 ? a.n_dst / 4 : a.n_dst;
+    const unsigned gx = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((per_row + TPB - 1) / TPB, 64));
+    const unsigned gy = (unsigned)std::min<uint64_t>(a.n_src, 65535);
+    if (v4)
+      k_tile_dense4<<<dim3(gx, gy), TPB, 0, st>>>(a, o, d_err);
+    else
+      k_tile_dense<<<dim3(gx, gy), TPB, 0, st>>>(a, o, d_err);
+    BF_CUDA(cudaGetLastError());
+    rows = n;
+  } else if (n) {
+    const uint64_t nb = (n + CELLS - 1) / CELLS;
+    if (nb > 0x7FFFFFFFull) {
+      set_error("bf_tile_emit: block too large");
+      return BF_ERR_INVALID;
+    }
+    unsigned long long* d_cnt = nullptr;
+    BF_CUDA(ws_get(ws, 1, (2 * nb + 1) * 8, &d_cnt));
+    const bool narrow = n <= 0xFFFFFFFFull;
+    k_tile_count<<<(unsigned)nb, TPB, 0, st>>>(a, n, narrow, d_cnt, d_err);
+    k_tile_scan<<<1, 1024, 0, st>>>(nb, d_cnt, d_cnt + nb, d_cnt + 2 * nb);
+    k_tile_write<<<(unsigned)nb, TPB, 0, st>>>(a, o, n, narrow, d_cnt + nb, d_err);
+    BF_CUDA(cudaGetLastError());
+    BF_CUDA(cudaMemcpyAsync(&rows, d_cnt + 2 * nb, 8, cudaMemcpyDeviceToHost, st));
+  }
+  uint32_t err = 0;
+  BF_CUDA(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, st));
+  BF_CUDA(cudaStreamSynchronize(st));
+  if (err & ERR_NO_LIST) {
+    set_error("bf_tile_emit: a source's original index has no radius list");
+    return BF_ERR_INVALID;
+  }
+  if (err & ERR_BAD_LIST) {
+    set_error("bf_tile_emit: radius list offsets are not non-decreasing within the lists");
+    return BF_ERR_INVALID;
+  }
+  *n_rows = rows;
+  return BF_OK;
+}
+
+bf_status set_device(int device) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev || device >= 64) {
+    cudaGetLastError();
+    set_error("bf_tile_emit: no such device");
+    return BF_ERR_INVALID;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  return BF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+bf_status bf_tile_emit_device(const uint32_t* d_matrix, const uint32_t* d_lat, uint32_t n_src,
+                              uint32_t n_dst, const uint32_t* d_src_orig,
+                              const uint32_t* d_dst_orig, uint32_t threshold,
+                              const uint64_t* d_mask_off, const uint32_t* d_mask,
+                              uint32_t n_mask_src, uint64_t n_mask, uint32_t sparse, int device,
+                              void* stream, const bf_tile_columns* d_out, uint64_t* n_rows) {
+  bf_status rc;
+  if ((rc = check_args(n_src, n_dst, d_matrix, d_src_orig, d_dst_orig, d_out, n_rows, d_mask_off,
+                       d_mask, n_mask)))
+    return rc;
+  if ((rc = set_device(device))) return rc;
+  TileWs& ws = tile_ws(device);
+  std::lock_guard<std::mutex> lk(ws.mu);
+  if (!ws.st) BF_CUDA(cudaStreamCreateWithFlags(&ws.st, cudaStreamNonBlocking));
+  cudaStream_t st = stream ? (cudaStream_t)stream : ws.st;
+  const TileIn a{d_matrix, d_lat, n_src, n_dst, d_src_orig, d_dst_orig, threshold,
+                 d_mask_off, d_mask, n_mask_src, n_mask, sparse};
+  const TileOut o{d_out->source_idx, d_out->target_idx, d_out->duration_ms, d_out->distance_m};
+  return emit_device(ws, a, o, st, n_rows);
+}
+
+bf_status bf_tile_emit(const uint32_t* matrix, const uint32_t* lat, uint32_t n_src,
+                       uint32_t n_dst, const uint32_t* src_orig, const uint32_t* dst_orig,
+                       uint32_t threshold, const uint64_t* mask_off, const uint32_t* mask,
+                       uint32_t n_mask_src, uint32_t sparse, int device,
+                       const bf_tile_columns* out, uint64_t* n_rows) {
+  const uint64_t n_mask = mask_off ? mask_off[n_mask_src] : 0;
+  bf_status rc;
+  if ((rc = check_args(n_src, n_dst, matrix, src_orig, dst_orig, out, n_rows, mask_off, mask,
+                       n_mask)))
+    return rc;
+  if (mask_off)
+    for (uint32_t s = 0; s < n_mask_src; ++s)
+      if (mask_off[s + 1] < mask_off[s]) {
+        set_error("bf_tile_emit: radius list offsets must be non-decreasing");
+        return BF_ERR_INVALID;
+      }
+  if ((rc = set_device(device))) return rc;
+  TileWs& ws = tile_ws(device);
+  std::lock_guard<std::mutex> lk(ws.mu);
+  if (!ws.st) BF_CUDA(cudaStreamCreateWithFlags(&ws.st, cudaStreamNonBlocking));
+  cudaStream_t st = ws.st;
+  const uint64_t n = (uint64_t)n_src * n_dst;
+  uint32_t *dm = nullptr, *dl = nullptr, *ds = nullptr, *dd = nullptr, *dmask = nullptr;
+  uint64_t* dmoff = nullptr;
+  uint32_t* dcol = nullptr;
+  cudaError_t e = ws_get(ws, 2, n * 4, &dm);
+  if (e == cudaSuccess && lat) e = ws_get(ws, 3, n * 4, &dl);
+  if (e == cudaSuccess) e = ws_get(ws, 4, (uint64_t)n_src * 4, &ds);
+  if (e == cudaSuccess) e = ws_get(ws, 5, (uint64_t)n_dst * 4, &dd);
+  if (e == cudaSuccess && mask_off) e = ws_get(ws, 6, ((uint64_t)n_mask_src + 1) * 8, &dmoff);
+  if (e == cudaSuccess && mask_off) e = ws_get(ws, 7, n_mask * 4, &dmask);
+  if (e == cudaSuccess) e = ws_get(ws, 8, n * 16, &dcol);
+  if (e != cudaSuccess) return cuda_status(e, "bf_tile_emit: device memory");
+  auto up = [&](void* d, const void* h, uint64_t bytes) {
+    if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st);
+  };
+  up(dm, matrix, n * 4);
+  if (lat) up(dl, lat, n * 4);
+  up(ds, src_orig, (uint64_t)n_src * 4);
+  up(dd, dst_orig, (uint64_t)n_dst * 4);
+  if (mask_off) {
+    up(dmoff, mask_off, ((uint64_t)n_mask_src + 1) * 8);
+    up(dmask, mask, n_mask * 4);
+  }
+  if (e != cudaSuccess) return cuda_status(e, "bf_tile_emit: upload");
+  const TileIn a{dm, lat ? dl : nullptr, n_src, n_dst, ds, dd, threshold,
+                 mask_off ? dmoff : nullptr, dmask, n_mask_src, n_mask, sparse};
+  const TileOut o{dcol, dcol + n, dcol + 2 * n, dcol + 3 * n};
+  uint64_t rows = 0;
+  if ((rc = emit_device(ws, a, o, st, &rows))) return rc;
+  uint32_t* dst_cols[4] = {out->source_idx, out->target_idx, out->duration_ms, out->distance_m};
+  for (int c = 0; c < 4 && rows; ++c)
+    BF_CUDA(cudaMemcpyAsync(dst_cols[c], dcol + (uint64_t)c * n, rows * 4, cudaMemcpyDeviceToHost,
+                            st));
+  BF_CUDA(cudaStreamSynchronize(st));
+  *n_rows = rows;
+  return BF_OK;
+}
+
+void bf_tile_release(int device) {
+  if (device < 0 || device >= 64) return;
+  TileWs& ws = tile_ws(device);
+  std::lock_guard<std::mutex> lk(ws.mu);
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  if (ws.st) cudaStreamSynchronize(ws.st);
+  for (int i = 0; i < 12; ++i) {
+    if (ws.buf[i]) cudaFree(ws.buf[i]);
+    ws.buf[i] = nullptr;
+    ws.cap[i] = 0;
+  }
+  if (ws.st) cudaStreamDestroy(ws.st);
+  ws.st = nullptr;
+}
+
+}  // extern "C"

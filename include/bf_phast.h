@@ -32,6 +32,7 @@
  *   bf_contour_rasters     generate_sparse_contour_anchored, steps 1-3  route/src/range/sparse_contour.rs:650
  *   bf_contour_polygons    generate_sparse_contour_anchored, steps 4-5  sparse_contour.rs:770
  *   bf_isochrone_polygons  build_isochrone_geometry for many origins  route/src/server/geometry.rs:239
+ *   bf_tile_emit[_device]  build_matrix_batch / build_matrix_tile_batch  route/src/server/flight.rs:432,509
  *
  * Conventions (as in the reference):
  *   - node ids are CCH ranks (rank-aligned CCH, node_id == rank);
@@ -580,6 +581,51 @@ bf_status bf_isochrone_polygons(bf_graph* g, const bf_geometry* geo, const uint3
                                 const uint32_t* thresholds, const uint32_t* tier_thresholds,
                                 uint64_t n, uint32_t mode, uint64_t* ring_off, double** lonlat,
                                 double* phase_ms);
+
+/* ---- matrix tile emission: the RecordBatch columns of a matrix block ----
+ *
+ * build_matrix_batch / build_matrix_tile_batch (route/src/server/flight.rs:
+ * 432-500, 509-589) on the GPU. The n_src x n_dst row-major durations
+ * `matrix` (and the optional length-along-time `lat`, same shape) become the
+ * columns source_idx, target_idx, duration_ms, distance_m in row-major cell
+ * order: source_idx / target_idx are the original indices src_orig[si] /
+ * dst_orig[di]; a cell is pruned (u32::MAX) when the radius mask is given
+ * (mask_off != NULL: source o's sorted list of original destination indices
+ * is mask[mask_off[o] .. mask_off[o + 1]), o < n_mask_src) and lacks the
+ * destination; a cell above `threshold` reads u32::MAX (0xFFFFFFFF = no
+ * bound, as build_matrix_batch); with `sparse` cells whose duration is
+ * u32::MAX are dropped; duration_ms = min(d * 1000, u32::MAX), distance_m =
+ * lat's cell or u32::MAX, both u32::MAX on a dropped-duration cell. Each
+ * column must hold n_src * n_dst values; *n_rows gets the rows written (0
+ * for an all-sentinel sparse block: the reference's None). The columns are
+ * Arrow UInt32 arrays without nulls, ready to wrap.
+ */
+typedef struct bf_tile_columns {
+  uint32_t* source_idx;
+  uint32_t* target_idx;
+  uint32_t* duration_ms;
+  uint32_t* distance_m;
+} bf_tile_columns;
+
+/* Host arrays in and out (page-locked host memory copies fastest). */
+bf_status bf_tile_emit(const uint32_t* matrix, const uint32_t* lat, uint32_t n_src,
+                       uint32_t n_dst, const uint32_t* src_orig, const uint32_t* dst_orig,
+                       uint32_t threshold, const uint64_t* mask_off, const uint32_t* mask,
+                       uint32_t n_mask_src, uint32_t sparse, int device,
+                       const bf_tile_columns* out, uint64_t* n_rows);
+
+/* Device arrays of `device` in and out (for example the output of
+ * bf_matrix_device), on `stream` (NULL: the library's own); n_mask is the
+ * length of d_mask. Returns after the work completed. */
+bf_status bf_tile_emit_device(const uint32_t* d_matrix, const uint32_t* d_lat, uint32_t n_src,
+                              uint32_t n_dst, const uint32_t* d_src_orig,
+                              const uint32_t* d_dst_orig, uint32_t threshold,
+                              const uint64_t* d_mask_off, const uint32_t* d_mask,
+                              uint32_t n_mask_src, uint64_t n_mask, uint32_t sparse, int device,
+                              void* stream, const bf_tile_columns* d_out, uint64_t* n_rows);
+
+/* Frees the tile emission's device buffers and stream on `device`. */
+void bf_tile_release(int device);
 
 const char* bf_last_error(void);
 

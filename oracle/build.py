@@ -1,6 +1,6 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles phast_oracle.cpp and contour_oracle.cpp into
+Compiles phast_oracle.cpp, contour_oracle.cpp and tile_oracle.cpp into
 oracle/_build/liboracle.so (no floating-point contraction, so every step
 rounds as written). Only tests/, __graft_entry__.smoke() and bench.py's
 CPU-baseline leg load it.
@@ -14,7 +14,7 @@ OUT = HERE / "_build"
 
 def build_oracle():
     OUT.mkdir(exist_ok=True)
-    srcs = [HERE / "phast_oracle.cpp", HERE / "contour_oracle.cpp"]
+    srcs = [HERE / "phast_oracle.cpp", HERE / "contour_oracle.cpp", HERE / "tile_oracle.cpp"]
     so = OUT / "liboracle.so"
     if not so.exists() or any(so.stat().st_mtime < s.stat().st_mtime for s in srcs):
         r = subprocess.run(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",

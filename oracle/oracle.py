@@ -69,6 +69,10 @@ def load():
         lib.orc_cch_relax_lex.restype = ctypes.c_uint32
         lib.orc_cch_bottom_up.argtypes = [ctypes.c_uint32] + [_V] * 12
         lib.orc_cch_bottom_up.restype = ctypes.c_uint32
+        lib.orc_tile_emit.argtypes = ([_V, _V, ctypes.c_uint32, ctypes.c_uint32, _V, _V,
+                                       ctypes.c_uint32, _V, _V, ctypes.c_uint32, ctypes.c_int]
+                                      + [_V] * 4)
+        lib.orc_tile_emit.restype = ctypes.c_uint64
         _lib = lib
     return _lib
 
@@ -470,3 +474,39 @@ def sparse_closed(segments, cell_m, dilation, erosion, anchor=None):
         if n <= cap:
             return cells[:2 * n].reshape(-1, 2), grid
         cap = int(n)
+
+
+def mask_csr(mask):
+    """A radius mask (list, indexed by original source, of sorted lists of
+    original destination indices) as (offsets u64, flat u32)."""
+    off = np.zeros(len(mask) + 1, np.uint64)
+    off[1:] = np.cumsum([len(m) for m in mask]) if len(mask) else []
+    flat = np.asarray([v for m in mask for v in m], np.uint32)
+    return off, flat
+
+
+def tile_emit(matrix, n_src, n_dst, src_orig, dst_orig, threshold=INF, mask=None, lat=None,
+              sparse=False):
+    """build_matrix_batch / build_matrix_tile_batch (flight.rs:432-589):
+    (source_idx, target_idx, duration_ms, distance_m) columns of a row-major
+    n_src x n_dst block. `mask` as in mask_csr (or an (offsets, flat) pair)."""
+    m = _a(np.asarray(matrix).reshape(-1), np.uint32)
+    so, do = _a(src_orig, np.uint32), _a(dst_orig, np.uint32)
+    la = None if lat is None else _a(np.asarray(lat).reshape(-1), np.uint32)
+    if mask is not None and not (isinstance(mask, tuple) and len(mask) == 2
+                                 and isinstance(mask[0], np.ndarray)):
+        mask = mask_csr(mask)
+    cap = max(1, n_src * n_dst)
+    cols = [np.empty(cap, np.uint32) for _ in range(4)]
+    moff, mflat = (None, None) if mask is None else (_a(mask[0], np.uint64),
+                                                     _a(mask[1], np.uint32))
+    n_mask = 0 if mask is None else len(moff) - 1
+    keep = np.zeros(1, np.uint32) if mflat is None or len(mflat) == 0 else mflat
+    k = load().orc_tile_emit(m.ctypes.data, None if la is None else la.ctypes.data, n_src, n_dst,
+                             so.ctypes.data, do.ctypes.data, threshold,
+                             None if moff is None else moff.ctypes.data,
+                             None if moff is None else keep.ctypes.data, n_mask, int(sparse),
+                             *[c.ctypes.data for c in cols])
+    if k == 0xFFFFFFFFFFFFFFFF:
+        raise IndexError("a source's original index has no radius list")
+    return tuple(c[:k].copy() for c in cols)

@@ -21,6 +21,10 @@ reference_kats.json
         through external middle 0 or 1 (lengths 13 and 105), the packed
         (weight, middle) order, and the three (time, length) lexicographic
         middle elections
+      * route/src/server/flight.rs:4976-5380  matrix RecordBatch emission
+        (matrix_sparse_tests): the small-path and tile fixtures, radius
+        masks, the time bound, sparse dropping, non-contiguous original
+        indices, all-sentinel blocks and the lat (distance) column
       * route/src/range/sparse_contour.rs:1187-1672  isochrone contour:
         cell-centre rings of a 3x3 block and an L-shape, anchored component
         selection, the largest component without an anchor, and the
@@ -108,7 +112,38 @@ def kats():
         "base": {"car": [30.0, 2, 2, 30.0], "bike": [40.0, 3, 3, 40.0], "foot": [25.0, 3, 3, 25.0],
                  "truck": [30.0, 2, 2, 30.0]},
     }
+    MAX = INF
+    tile_emit = {
+        "source": "route/src/server/flight.rs:4976-5380",
+        # small_fixture (:5002-5015): rows are (source, target, duration_ms[, distance_m])
+        "small": dict(m=[100, MAX, 300, MAX, 200, 250], src=[0, 1], dst=[0, 1, 2],
+                      mask=[[0, 2], [1]], lat=[1100, MAX, 3300, MAX, 2200, 2500],
+                      dense_rows=6, dense_sentinels=3,
+                      sparse=[[0, 0, 100000], [0, 2, 300000], [1, 1, 200000]],
+                      sparse_lat=[[0, 0, 1100], [0, 2, 3300], [1, 1, 2200]],
+                      no_mask_sparse_pairs=[[0, 0], [0, 2], [1, 1], [1, 2]]),
+        # small_no_sentinels_sparse_equals_dense (:5123-5133)
+        "all_reachable": dict(m=[10, 20, 30, 40, 50, 60], src=[0, 1], dst=[0, 1, 2], rows=6),
+        # small_original_indices_preserved (:5138-5150)
+        "noncontig": dict(m=[70, MAX, MAX, 90], src=[2, 5], dst=[1, 4],
+                          sparse=[[2, 1, 70000], [5, 4, 90000]]),
+        # tile_fixture (:5168-5180), threshold 500
+        "tile": dict(m=[50, MAX, 300, MAX, 120, 999], src=[0, 3], dst=[1, 2, 4],
+                     mask=[[1, 2, 4], [], [], [2, 4]], threshold=500, dense_rows=6,
+                     dense_sentinels=3,
+                     sparse=[[0, 1, 50000], [0, 4, 300000], [3, 2, 120000]],
+                     unbounded_pairs=[[0, 1], [0, 4], [3, 2], [3, 4]]),
+        # tile_radius_mask_prunes_reachable (:5240-5262)
+        "radius": dict(m=[40, 80], src=[0], dst=[1, 2], mask=[[2]], sparse=[[0, 2, 80000]]),
+        # tile_sparse_all_sentinels_is_none (:5264-5285)
+        "all_sentinel": dict(m=[MAX] * 4, src=[0, 1], dst=[0, 1]),
+        "pruned_empty": dict(m=[10, 20], src=[0], dst=[0, 1], mask=[[]]),
+        # tile_emits_lat_as_distance_when_present (:5340-5355)
+        "tile_lat": dict(m=[50, 100], lat=[700, 1400], src=[0], dst=[0, 1],
+                         rows=[[0, 50000, 700], [1, 100000, 1400]]),
+    }
     return {
+        "tile_emit": tile_emit,
         "sparse_contour": contour,
         "cch_customize": customize,
         "five_node": {
