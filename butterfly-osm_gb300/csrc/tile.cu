@@ -17,8 +17,8 @@
 // Dense: one thread per cell, or per four cells with 16-byte accesses when
 // rows are a multiple of four cells (2D grid: columns x rows), reads and the
 // four column writes coalesced. Sparse: an order-preserving compaction - per
-// block of 2048 cells a count, a one-block scan of the counts, then an
-// ordered write in which each 256-cell step is scanned within the block.
+// block of 2048 cells a count and the kept-cell ballots, a one-block scan of
+// the counts, then an ordered write of the kept cells only.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -69,6 +69,18 @@ __device__ __forceinline__ void split(uint64_t i, uint32_t n_dst, bool narrow, u
   }
 }
 
+// binary_search's answer (present or not) on a sorted list: halving steps on
+// 32-bit offsets, one comparison at the end.
+__device__ __forceinline__ bool in_list(const uint32_t* __restrict__ v, uint32_t len, uint32_t x) {
+  if (len == 0) return false;
+  while (len > 1) {
+    const uint32_t half = len >> 1;
+    if (v[half] <= x) v += half;
+    len -= half;
+  }
+  return *v == x;
+}
+
 // The cell's duration d (already loaded) after pruning and the time bound
 // (both give u32::MAX, so the bound is tested first and only cells within
 // it search the radius list); os, od: the original indices.
@@ -80,25 +92,12 @@ __device__ __forceinline__ uint32_t decide(const TileIn& a, uint32_t d, uint32_t
   }
   if (d > a.threshold) return MAXV;
   if (a.mask_off) {
-    uint64_t lo = a.mask_off[os], hi = a.mask_off[os + 1];
-    if (hi < lo || hi > a.n_mask) {
+    const uint64_t lo = a.mask_off[os], hi = a.mask_off[os + 1];
+    if (hi < lo || hi > a.n_mask || hi - lo > 0xFFFFFFFFull) {
       atomicOr(err, ERR_BAD_LIST);
       return MAXV;
     }
-    bool found = false;
-    while (lo < hi) {  // binary_search on the sorted list
-      const uint64_t mid = lo + ((hi - lo) >> 1);
-      const uint32_t v = a.mask[mid];
-      if (v < od) {
-        lo = mid + 1;
-      } else if (v > od) {
-        hi = mid;
-      } else {
-        found = true;
-        break;
-      }
-    }
-    if (!found) return MAXV;
+    if (!in_list(a.mask + lo, (uint32_t)(hi - lo), od)) return MAXV;
   }
   return d;
 }
@@ -157,28 +156,7 @@ __global__ void __launch_bounds__(TPB) k_tile_dense4(TileIn a, TileOut o, uint32
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         uint32_t d = no_list || dv[k] > a.threshold ? MAXV : dv[k];
-        if (d != MAXV && a.mask_off) {
-          uint64_t lo = a.mask_off[os], hi = a.mask_off[os + 1];
-          if (hi < lo || hi > a.n_mask) {
-            atomicOr(err, ERR_BAD_LIST);
-            d = MAXV;
-          } else {
-            bool found = false;
-            while (lo < hi) {
-              const uint64_t mid = lo + ((hi - lo) >> 1);
-              const uint32_t v = a.mask[mid];
-              if (v < ov[k]) {
-                lo = mid + 1;
-              } else if (v > ov[k]) {
-                hi = mid;
-              } else {
-                found = true;
-                break;
-              }
-            }
-            if (!found) d = MAXV;
-          }
-        }
+        if (d != MAXV && a.mask_off) d = decide(a, d, os, ov[k], err);
         if (d == MAXV) {
           du[k] = MAXV;
           di[k] = MAXV;
@@ -196,18 +174,42 @@ __global__ void __launch_bounds__(TPB) k_tile_dense4(TileIn a, TileOut o, uint32
   }
 }
 
+// Sparse pass 1: per block the kept cells, per (step, warp) the ballot of
+// kept cells (bit lane of word (cell / 32)); rows and columns advance by
+// TPB cells a step instead of a division per cell.
 __global__ void __launch_bounds__(TPB)
     k_tile_count(TileIn a, uint64_t n, bool narrow, unsigned long long* __restrict__ cnt,
-                 uint32_t* err) {
+                 uint32_t* __restrict__ keep_bits, uint32_t* err) {
   __shared__ uint32_t red[TPB / 32];
   const uint64_t base = (uint64_t)blockIdx.x * CELLS;
-  uint32_t c = 0;
+  uint32_t c = 0, si = 0, di = 0;
+  split(base + threadIdx.x, a.n_dst, narrow, &si, &di);
+  uint32_t dur[ITEMS];  // the block's durations, all loads in flight before any decision
+#pragma unroll
   for (uint32_t j = 0; j < ITEMS; ++j) {
     const uint64_t i = base + (uint64_t)j * TPB + threadIdx.x;
-    if (i >= n) break;
-    uint32_t si, di, os, od;
-    split(i, a.n_dst, narrow, &si, &di);
-    c += cell_value(a, si, di, i, &os, &od, err) != MAXV;
+    dur[j] = i < n ? a.m[i] : MAXV;
+  }
+#pragma unroll
+  for (uint32_t j = 0; j < ITEMS; ++j) {
+    const uint64_t i = base + (uint64_t)j * TPB + threadIdx.x;
+    if (base + (uint64_t)j * TPB >= n) break;  // uniform across the block
+    if (j) {
+      if (a.n_dst >= TPB) {
+        di += TPB;
+        if (di >= a.n_dst) {
+          di -= a.n_dst;
+          ++si;
+        }
+      } else {
+        split(i, a.n_dst, narrow, &si, &di);
+      }
+    }
+    bool keep = false;
+    if (i < n) keep = decide(a, dur[j], a.src_orig[si], a.dst_orig[di], err) != MAXV;
+    const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
+    if ((threadIdx.x & 31) == 0) keep_bits[(base + (uint64_t)j * TPB) / 32 + (threadIdx.x >> 5)] = bal;
+    c += keep;
   }
   for (int s = 16; s > 0; s >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, s);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
@@ -252,33 +254,36 @@ __global__ void __launch_bounds__(1024)
   if (threadIdx.x == 0) *total = carry;
 }
 
+// Sparse pass 2: the block's kept cells, in order, from pass 1's ballots:
+// a thread's output slot is the block's offset plus the kept cells of the
+// earlier words of the block and the lower lanes of its own word.
 __global__ void __launch_bounds__(TPB)
     k_tile_write(TileIn a, TileOut o, uint64_t n, bool narrow,
-                 const unsigned long long* __restrict__ pre, uint32_t* err) {
-  __shared__ uint32_t sh[TPB / 32];
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                 const unsigned long long* __restrict__ pre,
+                 const uint32_t* __restrict__ keep_bits, uint32_t* err) {
+  __shared__ uint32_t wpre[CELLS / 32 + 1];
+  const uint32_t lane = threadIdx.x & 31;
   const uint64_t base = (uint64_t)blockIdx.x * CELLS;
-  uint64_t k0 = pre[blockIdx.x];
-  for (uint32_t j = 0; j < ITEMS; ++j) {
-    const uint64_t i = base + (uint64_t)j * TPB + threadIdx.x;
-    if (base + (uint64_t)j * TPB >= n) break;  // uniform across the block
-    uint32_t si = 0, di = 0, os = 0, od = 0, d = MAXV;
-    if (i < n) {
-      split(i, a.n_dst, narrow, &si, &di);
-      d = cell_value(a, si, di, i, &os, &od, err);
+  const uint64_t w0 = base / 32, nw = (n + 31) / 32;
+  if (threadIdx.x == 0) {  // exclusive prefix of the block's 64 word counts
+    uint32_t acc = 0;
+    for (uint32_t w = 0; w < CELLS / 32; ++w) {
+      wpre[w] = acc;
+      acc += w0 + w < nw ? __popc(keep_bits[w0 + w]) : 0;
     }
-    const uint32_t keep = i < n && d != MAXV;
-    const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
-    if (lane == 0) sh[warp] = __popc(bal);
-    __syncthreads();
-    uint32_t before = 0, step = 0;
-    for (uint32_t w = 0; w < TPB / 32; ++w) {
-      if (w < warp) before += sh[w];
-      step += sh[w];
-    }
-    __syncthreads();
-    if (keep) put(a, o, k0 + before + __popc(bal & ((1u << lane) - 1u)), i, os, od, d);
-    k0 += step;
+    wpre[CELLS / 32] = acc;
+  }
+  __syncthreads();
+  const uint64_t k0 = pre[blockIdx.x];
+  for (uint32_t w = threadIdx.x >> 5; w < CELLS / 32; w += TPB / 32) {
+    if (w0 + w >= nw) break;
+    const uint32_t bits = keep_bits[w0 + w];
+    if (!((bits >> lane) & 1u)) continue;
+    const uint64_t i = (w0 + w) * 32 + lane;
+    uint32_t si, di, os, od;
+    split(i, a.n_dst, narrow, &si, &di);
+    const uint32_t d = cell_value(a, si, di, i, &os, &od, err);
+    put(a, o, k0 + wpre[w] + __popc(bits & ((1u << lane) - 1u)), i, os, od, d);
   }
 }
 
@@ -353,11 +358,13 @@ bf_status emit_device(TileWs& ws, const TileIn& a, const TileOut& o, cudaStream_
       return BF_ERR_INVALID;
     }
     unsigned long long* d_cnt = nullptr;
+    uint32_t* d_bits = nullptr;
     BF_CUDA(ws_get(ws, 1, (2 * nb + 1) * 8, &d_cnt));
+    BF_CUDA(ws_get(ws, 9, nb * (CELLS / 32) * 4, &d_bits));
     const bool narrow = n <= 0xFFFFFFFFull;
-    k_tile_count<<<(unsigned)nb, TPB, 0, st>>>(a, n, narrow, d_cnt, d_err);
+    k_tile_count<<<(unsigned)nb, TPB, 0, st>>>(a, n, narrow, d_cnt, d_bits, d_err);
     k_tile_scan<<<1, 1024, 0, st>>>(nb, d_cnt, d_cnt + nb, d_cnt + 2 * nb);
-    k_tile_write<<<(unsigned)nb, TPB, 0, st>>>(a, o, n, narrow, d_cnt + nb, d_err);
+    k_tile_write<<<(unsigned)nb, TPB, 0, st>>>(a, o, n, narrow, d_cnt + nb, d_bits, d_err);
     BF_CUDA(cudaGetLastError());
     BF_CUDA(cudaMemcpyAsync(&rows, d_cnt + 2 * nb, 8, cudaMemcpyDeviceToHost, st));
   }
