@@ -149,8 +149,12 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
         return BF_ERR_INVALID;
       }
   }
-  // finite UP / DOWN edges, validated
+  // finite UP / DOWN edges, validated; parallel UP edges (one target listed
+  // twice) become one record with the smallest (time, length), which is what
+  // relaxing each of them gives - and the upward kernel relies on one record
+  // per (source, target)
   std::vector<uint64_t> up_off(n + 1, 0), dn_cnt(n + 1, 0);
+  std::vector<uint32_t> last_src(n, NONE);
   for (uint32_t u = 0; u < n; ++u) {
     uint64_t c = 0;
     for (uint64_t k = uo[u]; k < uo[u + 1]; ++k) {
@@ -160,7 +164,10 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
                   " does not go to a higher rank");
         return BF_ERR_INVALID;
       }
-      if (csr->up_weights[k] != INF) ++c;
+      if (csr->up_weights[k] != INF && last_src[t] != u) {
+        last_src[t] = u;
+        ++c;
+      }
     }
     up_off[u + 1] = up_off[u] + c;
     for (uint64_t k = dno[u]; k < dno[u + 1]; ++k) {
@@ -236,19 +243,36 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
     run_end[r] = (parent[r] == r + 1) ? run_end[r + 1] : r;
   }
   g->max_depth = maxd;
-  // UP records
+  // UP records, one per (source, target)
   std::vector<uint2> up_rec(g->n_up);
   std::vector<uint32_t> up_l(two ? g->n_up : 0);
+  std::fill(last_src.begin(), last_src.end(), NONE);
+  std::vector<uint64_t> rec_at(n, 0);
   for (uint32_t u = 0; u < n; ++u) {
     uint64_t p = up_off[u];
     for (uint64_t k = uo[u]; k < uo[u + 1]; ++k) {
       uint32_t w = csr->up_weights[k];
       if (w == INF) continue;
       uint32_t v = csr->up_targets[k];
-      if (two) up_l[p] = up_len[k];
+      const uint32_t l = two ? up_len[k] : 0;
+      if (last_src[v] == u) {  // a parallel edge: keep the smaller (time, length)
+        const uint64_t q = rec_at[v];
+        if (w < up_rec[q].y || (two && w == up_rec[q].y && l < up_l[q])) {
+          up_rec[q].y = w;
+          if (two) up_l[q] = l;
+        }
+        continue;
+      }
+      last_src[v] = u;
+      rec_at[v] = p;
+      if (two) up_l[p] = l;
       up_rec[p++] = make_uint2(depth[u] - depth[v], w);
     }
   }
+  last_src.clear();
+  last_src.shrink_to_fit();
+  rec_at.clear();
+  rec_at.shrink_to_fit();
   // levels of the pull DAG
   std::vector<uint32_t> level(n, 0);
   uint32_t maxl = 0;

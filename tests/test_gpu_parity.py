@@ -195,3 +195,47 @@ def test_page_locked_output(built, grid100, mapped):
         m = g.matrix(gold["sources"], gold["targets"], out=out)
         assert m is out or np.shares_memory(m, out)
         assert np.array_equal(out, gold["matrix"])
+
+
+def _with_parallel_up_edges(d, seed):
+    """The CSR with a copy of every fifth finite UP edge listed again (weights
+    above, equal to and below the original), in shuffled order within each
+    source's list."""
+    rng = np.random.default_rng(seed)
+    n = d["n"]
+    off, tgt, w = d["up_off"], d["up_tgt"], d["up_w"]
+    new_off, new_t, new_w = [0], [], []
+    for u in range(n):
+        t = list(tgt[off[u]:off[u + 1]])
+        ww = list(w[off[u]:off[u + 1]])
+        for k in range(len(t)):
+            if ww[k] != INF and rng.random() < 0.2:
+                t.append(t[k])
+                ww.append(int(max(0, min(INF - 1, int(ww[k]) + int(rng.integers(-3, 4))))))
+        order = rng.permutation(len(t))
+        new_t += [t[i] for i in order]
+        new_w += [ww[i] for i in order]
+        new_off.append(len(new_t))
+    out = dict(d)
+    out["up_off"] = np.asarray(new_off, np.uint64)
+    out["up_tgt"] = np.asarray(new_t, np.uint32)
+    out["up_w"] = np.asarray(new_w, np.uint32)
+    return out
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+def test_parallel_up_edges(built, grid100, engine):
+    # a CSR that lists some UP edges twice: every relaxation takes the smaller
+    # weight, as the oracle relaxing each listed edge does
+    _, base = grid100
+    d = _with_parallel_up_edges(base, 11)
+    g = _graph(d)
+    _engine(g, engine)
+    c = orc.Cch(**{x: d[x] for x in ("n", "up_off", "up_tgt", "up_w", "down_off", "down_tgt",
+                                      "down_w")})
+    rng = np.random.default_rng(3)
+    src = rng.choice(d["n"], 40, replace=False)
+    tgt = rng.choice(d["n"], 300, replace=False)
+    want, _ = c.matrix(src, tgt)
+    assert np.array_equal(g.matrix(src, tgt), want)
+    assert g.info()["n_up"] == int((base["up_w"] != INF).sum())
