@@ -317,14 +317,13 @@ cudaError_t ws_get(TileWs& ws, int i, size_t bytes, T** p) {
 bf_status check_args(uint32_t n_src, uint32_t n_dst, const void* m, const void* so,
                      const void* dor, const bf_tile_columns* out, uint64_t* n_rows,
                      const void* mask_off, const void* mask, uint64_t n_mask) {
-  if (!out || !n_rows || (n_src && n_dst && (!m || !so || !dor)) ||
-      (uint64_t)n_src * n_dst && (!out->source_idx || !out->target_idx || !out->duration_ms ||
-                                  !out->distance_m) ||
+  const bool cells = (uint64_t)n_src * n_dst != 0;
+  if (!out || !n_rows || (cells && (!m || !so || !dor)) ||
+      (cells && (!out->source_idx || !out->target_idx || !out->duration_ms || !out->distance_m)) ||
       (mask_off && n_mask && !mask)) {
     set_error("bf_tile_emit: null argument");
     return BF_ERR_INVALID;
   }
-  (void)mask_off;
   return BF_OK;
 }
 
@@ -376,7 +375,7 @@ bf_status emit_device(TileWs& ws, const TileIn& a, const TileOut& o, cudaStream_
     return BF_ERR_INVALID;
   }
   if (err & ERR_BAD_LIST) {
-    set_error("bf_tile_emit: radius list offsets are not non-decreasing within the lists");
+    set_error("bf_tile_emit: a radius list's offsets decrease or run past the list array");
     return BF_ERR_INVALID;
   }
   *n_rows = rows;
