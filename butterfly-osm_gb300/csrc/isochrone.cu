@@ -188,6 +188,84 @@ __global__ void __launch_bounds__(128, IPB > 1 ? 12 : 16)
   }
 }
 
+// Waves of at most 64 lanes: G = Kp / 8 threads (8 lanes each) per item, so
+// a warp holds 32 / G items. Each thread walks its item's in-edges itself,
+// four at a time (edge records, activity words and rows of four edges in
+// flight together); the G threads of an item read the same edges and
+// activity bits, so they agree on whether any source is active. Items whose
+// edge counts differ simply leave the loop at different times.
+template <uint32_t G>
+__global__ void __launch_bounds__(128, 12)
+    k_sweep_group16(const uint4* __restrict__ item, uint32_t i0, uint32_t i1,
+                    const uint2* __restrict__ erec, uint16_t* __restrict__ slab, uint32_t Kp,
+                    uint32_t* __restrict__ active, const uint32_t* __restrict__ thr, uint32_t kw,
+                    const uint32_t* __restrict__ seeded, uint32_t* __restrict__ err) {
+  asm volatile("griddepcontrol.launch_dependents;");
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = (tid % G) * 8;
+  const bool live = lane < Kp;
+  const uint32_t valid_lanes = live ? min(8u, kw > lane ? kw - lane : 0u) : 0u;
+  const uint32_t groups = gridDim.x * (blockDim.x / G);
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  for (uint32_t ii = i0 + tid / G; ii < i1; ii += groups) {
+    const uint4 it = item[ii];
+    uint4 acc = make_uint4(~0u, ~0u, ~0u, ~0u);
+    bool any = false;
+    for (uint32_t e0 = it.y; e0 < it.z; e0 += 4) {
+      uint2 r[4];
+      uint32_t aw[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) r[q] = e0 + q < it.z ? erec[e0 + q] : make_uint2(0, 0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) aw[q] = e0 + q < it.z ? active[r[q].x >> 5] : 0u;
+      uint4 v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool a = (aw[q] >> (r[q].x & 31)) & 1u;
+        any |= a;
+        v[q] = a && live ? *reinterpret_cast<const uint4*>(slab + (size_t)r[q].x * Kp + lane)
+                         : make_uint4(~0u, ~0u, ~0u, ~0u);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t w16 = min(r[q].y, 0xFFFFu), ww = w16 | (w16 << 16);
+        acc.x = __vminu2(acc.x, __vaddus2(v[q].x, ww));
+        acc.y = __vminu2(acc.y, __vaddus2(v[q].y, ww));
+        acc.z = __vminu2(acc.z, __vaddus2(v[q].z, ww));
+        acc.w = __vminu2(acc.w, __vaddus2(v[q].w, ww));
+      }
+    }
+    if (!any) continue;  // the row keeps its seed or INF
+    uint32_t* a4 = &acc.x;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t lo = a4[q] & 0xFFFFu, hi = a4[q] >> 16;
+      if (2 * q >= (int)valid_lanes || lo > thr[lane + 2 * q]) lo = 0xFFFFu;
+      if (2 * q + 1 >= (int)valid_lanes || hi > thr[lane + 2 * q + 1]) hi = 0xFFFFu;
+      a4[q] = lo | (hi << 16);
+    }
+    if (!live) continue;
+    uint32_t* dst = reinterpret_cast<uint32_t*>(slab + (size_t)it.x * Kp + lane);
+    if (it.w) {
+      atomic_min_u16x2(dst + 0, acc.x, err);
+      atomic_min_u16x2(dst + 1, acc.y, err);
+      atomic_min_u16x2(dst + 2, acc.z, err);
+      atomic_min_u16x2(dst + 3, acc.w, err);
+    } else {
+      const bool valid = (seeded[it.x >> 5] >> (it.x & 31)) & 1u;
+      const uint4 c =
+          valid ? *reinterpret_cast<const uint4*>(dst) : make_uint4(~0u, ~0u, ~0u, ~0u);
+      uint4 nv;
+      nv.x = __vminu2(c.x, acc.x);
+      nv.y = __vminu2(c.y, acc.y);
+      nv.z = __vminu2(c.z, acc.z);
+      nv.w = __vminu2(c.w, acc.w);
+      *reinterpret_cast<uint4*>(dst) = nv;
+    }
+    if ((acc.x & acc.y & acc.z & acc.w) != ~0u) atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
+  }
+}
+
 // A run of consecutive small levels [l0, l1) of the 16-bit gated sweep in one
 // block of 1024 threads instead of a launch per level: wpi = ceil(Kp / 256)
 // warps share an item (a 256-lane slice each), the block takes 32 / wpi items
@@ -614,6 +692,20 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
             l = l1 - 1;
             continue;
           }
+        }
+        if (Kp <= 64) {  // thread groups of Kp / 8 threads per item
+          const uint32_t G = Kp <= 8 ? 1 : Kp <= 16 ? 2 : Kp <= 32 ? 4 : 8;
+          const uint32_t per_block = 128 / G;
+          const uint32_t blocks = std::min<uint32_t>((i1 - i0 + per_block - 1) / per_block,
+                                                     GATED16_BLOCKS);
+          auto kern = G == 1 ? k_sweep_group16<1> : G == 2 ? k_sweep_group16<2>
+                    : G == 4 ? k_sweep_group16<4> : k_sweep_group16<8>;
+          BF_CUDA(launch_level(kern, dim3(blocks), 128, pdl, st, (const uint4*)sc.d_item, i0, i1,
+                               (const uint2*)sc.d_erec, slab16, Kp, d_active,
+                               (const uint32_t*)(p_thr + s0), (uint32_t)kw,
+                               (const uint32_t*)d_seeded, g->d_err));
+          ++launches;
+          continue;
         }
         const bool own = Kp <= 256;  // four warps per block with their own items
         const uint32_t blocks = own ? std::min<uint32_t>((i1 - i0 + 3) / 4, 152 * 12)
