@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(128, IPB > 1 ? 12 : 16)
   }
 }
 
-// Waves of at most 64 lanes: G = Kp / 8 threads (8 lanes each) per item, so
+// Waves of at most 128 lanes: G = Kp / 8 threads (8 lanes each) per item, so
 // a warp holds 32 / G items. Each thread walks its item's in-edges itself,
 // four at a time (edge records, activity words and rows of four edges in
 // flight together); the G threads of an item read the same edges and
@@ -693,13 +693,14 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
             continue;
           }
         }
-        if (Kp <= 64) {  // thread groups of Kp / 8 threads per item
-          const uint32_t G = Kp <= 8 ? 1 : Kp <= 16 ? 2 : Kp <= 32 ? 4 : 8;
+        if (Kp <= 128) {  // thread groups of Kp / 8 threads per item
+          const uint32_t G = Kp <= 8 ? 1 : Kp <= 16 ? 2 : Kp <= 32 ? 4 : Kp <= 64 ? 8 : 16;
           const uint32_t per_block = 128 / G;
           const uint32_t blocks = std::min<uint32_t>((i1 - i0 + per_block - 1) / per_block,
                                                      GATED16_BLOCKS);
           auto kern = G == 1 ? k_sweep_group16<1> : G == 2 ? k_sweep_group16<2>
-                    : G == 4 ? k_sweep_group16<4> : k_sweep_group16<8>;
+                    : G == 4 ? k_sweep_group16<4> : G == 8 ? k_sweep_group16<8>
+                                                          : k_sweep_group16<16>;
           BF_CUDA(launch_level(kern, dim3(blocks), 128, pdl, st, (const uint4*)sc.d_item, i0, i1,
                                (const uint2*)sc.d_erec, slab16, Kp, d_active,
                                (const uint32_t*)(p_thr + s0), (uint32_t)kw,
