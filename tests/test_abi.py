@@ -143,3 +143,59 @@ def test_contour_and_customization_input_errors(built):
     t.down_targets = keep[3].ctypes.data_as(bfphast._u32p)
     h = ctypes.c_void_p()
     assert lib.bf_cch_create(ctypes.byref(t), 0, ctypes.byref(h)) == bfphast.BF_ERR_INVALID
+
+
+def test_tile_polygon_and_geometry_input_errors(built):
+    # null arguments and malformed offsets are BF_ERR_INVALID before any
+    # device is touched (tile emission, geometry, polygons, settled sets)
+    import ctypes
+    import numpy as np
+    import bfphast
+    lib = bfphast.load()
+    m = np.zeros(4, np.uint32)
+    ids = np.arange(2, dtype=np.uint32)
+    cols = [np.zeros(4, np.uint32) for _ in range(4)]
+    tc = bfphast.TileColumns(*[c.ctypes.data for c in cols])
+    rows = ctypes.c_uint64(0)
+    # no output struct / no row count / no matrix for a non-empty block
+    assert lib.bf_tile_emit(m.ctypes.data, None, 2, 2, ids.ctypes.data, ids.ctypes.data,
+                            bfphast.INF, None, None, 0, 0, 0, None,
+                            ctypes.byref(rows)) == bfphast.BF_ERR_INVALID
+    assert lib.bf_tile_emit(m.ctypes.data, None, 2, 2, ids.ctypes.data, ids.ctypes.data,
+                            bfphast.INF, None, None, 0, 0, 0, ctypes.byref(tc),
+                            None) == bfphast.BF_ERR_INVALID
+    assert lib.bf_tile_emit(None, None, 2, 2, ids.ctypes.data, ids.ctypes.data, bfphast.INF,
+                            None, None, 0, 0, 0, ctypes.byref(tc),
+                            ctypes.byref(rows)) == bfphast.BF_ERR_INVALID
+    # radius list offsets that decrease
+    moff = np.array([0, 2, 1], np.uint64)
+    mask = np.array([0, 1], np.uint32)
+    assert lib.bf_tile_emit(m.ctypes.data, None, 2, 2, ids.ctypes.data, ids.ctypes.data,
+                            bfphast.INF, moff.ctypes.data, mask.ctypes.data, 2, 1, 0,
+                            ctypes.byref(tc), ctypes.byref(rows)) == bfphast.BF_ERR_INVALID
+    assert b"radius list" in lib.bf_last_error()
+    # geometry: decreasing polyline offsets, null output
+    off = np.array([0, 2, 1], np.uint64)
+    e7 = np.zeros(4, np.int32)
+    w = np.ones(2, np.uint32)
+    h = ctypes.c_void_p()
+    assert lib.bf_geometry_create(2, off.ctypes.data_as(bfphast._u64p), e7.ctypes.data,
+                                  w.ctypes.data_as(bfphast._u32p),
+                                  ctypes.byref(h)) == bfphast.BF_ERR_INVALID
+    assert lib.bf_geometry_create(2, off.ctypes.data_as(bfphast._u64p), e7.ctypes.data,
+                                  w.ctypes.data_as(bfphast._u32p), None) == bfphast.BF_ERR_INVALID
+    # polygons and settled sets without a graph
+    ro = np.zeros(2, np.uint64)
+    out = ctypes.POINTER(ctypes.c_double)()
+    assert lib.bf_isochrone_polygons(None, None, ids.ctypes.data_as(bfphast._u32p),
+                                     ids.ctypes.data_as(bfphast._u32p), None, 1, 0,
+                                     ro.ctypes.data_as(bfphast._u64p), ctypes.byref(out),
+                                     None) == bfphast.BF_ERR_INVALID
+    r, d = ctypes.POINTER(ctypes.c_uint32)(), ctypes.POINTER(ctypes.c_uint32)()
+    assert lib.bf_isochrone_settled(None, ids.ctypes.data_as(bfphast._u32p),
+                                    ids.ctypes.data_as(bfphast._u32p), 1,
+                                    ro.ctypes.data_as(bfphast._u64p), ctypes.byref(r),
+                                    ctypes.byref(d), None) == bfphast.BF_ERR_INVALID
+    # the tier table and projection are host functions: checked against known values
+    c, dl, er, sm = bfphast.contour_config(bfphast.MODE_CAR, 1800)
+    assert (c, dl, er, sm) == (60.0, 2, 2, 60.0)
