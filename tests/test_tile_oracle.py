@@ -101,3 +101,42 @@ def test_saturation_and_missing_mask_row():
     assert du.tolist() == [4294967000, MAX, MAX]  # u32::saturating_mul(1000)
     with pytest.raises(IndexError):
         orc.tile_emit([1], 1, 1, [3], [0], mask=[[0]])
+
+
+def _numpy_emit(m, n_src, n_dst, src, dst, threshold, mask, lat, sparse):
+    """An independent vectorised statement of the same rules."""
+    m = np.asarray(m, np.uint64).reshape(n_src, n_dst)
+    src, dst = np.asarray(src, np.uint64), np.asarray(dst, np.uint64)
+    d = m.copy()
+    if mask is not None:
+        keep = np.array([[int(t) in set(mask[int(s)]) for t in dst] for s in src], bool).reshape(
+            n_src, n_dst)
+        d[~keep] = MAX
+    d[(d > threshold) & (d != MAX)] = MAX
+    s_col = np.repeat(src, n_dst).reshape(n_src, n_dst)
+    t_col = np.tile(dst, n_src).reshape(n_src, n_dst)
+    dur = np.where(d == MAX, MAX, np.minimum(d * 1000, MAX))
+    dist = np.full((n_src, n_dst), MAX, np.uint64)
+    if lat is not None:
+        dist = np.where(d == MAX, MAX, np.asarray(lat, np.uint64).reshape(n_src, n_dst))
+    sel = (d != MAX) if sparse else np.ones_like(d, bool)
+    return tuple(a[sel].astype(np.uint32) for a in (s_col, t_col, dur, dist))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_against_numpy_restatement(seed):
+    rng = np.random.default_rng(seed)
+    n_src, n_dst = int(rng.integers(0, 9)), int(rng.integers(0, 13))
+    m = rng.integers(0, 9_000_000, n_src * n_dst).astype(np.uint32)
+    m[rng.random(n_src * n_dst) < 0.25] = MAX
+    src = rng.choice(20, n_src, replace=False).astype(np.uint32)
+    dst = rng.choice(30, n_dst, replace=False).astype(np.uint32)
+    mask = [sorted(rng.choice(30, int(rng.integers(0, 30)), replace=False).tolist())
+            for _ in range(20)] if seed % 2 else None
+    lat = rng.integers(0, 1 << 32, n_src * n_dst, dtype=np.uint64).astype(np.uint32) \
+        if seed % 3 else None
+    for sparse in (False, True):
+        for thr in (MAX, 5_000_000):
+            got = orc.tile_emit(m, n_src, n_dst, src, dst, thr, mask, lat, sparse)
+            want = _numpy_emit(m, n_src, n_dst, src, dst, thr, mask, lat, sparse)
+            assert all(np.array_equal(a, b) for a, b in zip(got, want))
