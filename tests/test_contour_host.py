@@ -58,3 +58,44 @@ def test_projection_and_tiers_match_oracle(built):
     for mode, name in ((0, "car"), (1, "bike"), (2, "foot")):
         for t in (0, 300, 600, 601, 1800, 1801, 3600, 3601, 7200):
             assert bfphast.contour_config(mode, t) == orc.contour_config(name, t)
+
+
+def test_host_polygons_concurrent_calls(built):
+    # bf_contour_polygons from several host threads at once (the tracer's
+    # visited-edge arrays come from a shared pool): every call returns the
+    # single-threaded rings
+    import threading
+    import bfphast
+    rng = np.random.default_rng(21)
+    rasters, words, cells_m, simp_m = [], [], [], []
+    off = 0
+    for k in range(6):
+        segs, _ = contourgen.isochrone(rng, int(rng.integers(20, 200)), spread=0.01)
+        cell, dil, ero, simp = orc.contour_config("car", 600 + 600 * k)
+        cells, grid = orc.sparse_closed(segs, cell, dil, ero)
+        r, w = _raster(cells, grid, off)
+        off += len(w)
+        rasters.append(r)
+        words.append(w)
+        cells_m.append(cell)
+        simp_m.append(simp)
+    flat = np.concatenate(words)
+    want = bfphast.contour_polygons(rasters, flat, cells_m, simp_m)
+    got, errors = {}, []
+
+    def run(i):
+        try:
+            for _ in range(3):
+                got[i] = bfphast.contour_polygons(rasters[::-1], flat, cells_m[::-1], simp_m[::-1])
+        except Exception as e:  # pragma: no cover - reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(i,)) for i in range(6)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors
+    for rings in got.values():
+        for a, b in zip(rings, want[::-1]):
+            assert np.array_equal(a, b)
