@@ -35,7 +35,7 @@ _u64p = ctypes.POINTER(ctypes.c_uint64)
 
 
 class CchCsr(ctypes.Structure):
-    _fields_ = [("n_nodes", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+    _fields_ = [("n_nodes", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
                 ("up_offsets", _u64p), ("up_targets", _u32p), ("up_weights", _u32p),
                 ("down_offsets", _u64p), ("down_targets", _u32p), ("down_weights", _u32p)]
 

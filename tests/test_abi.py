@@ -199,3 +199,43 @@ def test_tile_polygon_and_geometry_input_errors(built):
     # the tier table and projection are host functions: checked against known values
     c, dl, er, sm = bfphast.contour_config(bfphast.MODE_CAR, 1800)
     assert (c, dl, er, sm) == (60.0, 2, 2, 60.0)
+
+
+def test_struct_layouts_match_header(built, tmp_path):
+    # every public struct of the header against its ctypes mirror: size and
+    # the offset of every field, from a C program compiled against the header
+    import ctypes
+    import shutil
+    import subprocess
+    import bfphast
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    pairs = {"bf_cch_csr": bfphast.CchCsr, "bf_config": bfphast.Config,
+             "bf_graph_info": bfphast.GraphInfo, "bf_stats": bfphast.Stats,
+             "bf_tune": bfphast.Tune, "bf_seed": bfphast.Seed, "bf_router": bfphast.Router,
+             "bf_server_cfg": bfphast.ServerCfg, "bf_request": bfphast.Request,
+             "bf_completion": bfphast.Completion, "bf_cch_topo": bfphast.CchTopo,
+             "bf_cch_stats": bfphast.CchStats, "bf_raster": bfphast.Raster,
+             "bf_tile_columns": bfphast.TileColumns}
+    if hasattr(bfphast, "Seed2"):
+        pairs["bf_seed2"] = bfphast.Seed2
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "bf_phast.h"',
+             'int main(void) {']
+    for c, py in pairs.items():
+        lines.append(f'  printf("{c} size %zu\\n", sizeof({c}));')
+        for name, _ in py._fields_:
+            lines.append(f'  printf("{c} {name} %zu\\n", offsetof({c}, {name}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    root = pathlib.Path(__file__).resolve().parents[1]
+    r = subprocess.run(["gcc", "-I", str(root / "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out.splitlines()}
+    for c, py in pairs.items():
+        assert got[(c, "size")] == ctypes.sizeof(py), c
+        for name, _ in py._fields_:
+            assert got[(c, name)] == getattr(py, name).offset, (c, name)
