@@ -92,7 +92,8 @@ constexpr uint32_t UPWARD_WARPS = 4;
 // A sweep schedule (target-restricted or full graph) with its cached CUDA graph.
 struct Sched {
   bool valid = false;
-  uint64_t key = 0;              // hash of the target positions
+  uint64_t key = 0;              // hash of the targets and split settings (a pre-check)
+  std::vector<uint32_t> tgt;     // the targets the schedule was built for (compared exactly)
   uint32_t n_r = 0;              // restricted nodes
   uint64_t n_items = 0;
   uint64_t n_edges = 0;
@@ -374,6 +375,9 @@ bf_status bounded_seeded_2ch(Graph* g, Ctx& c, const bf_seed2* seeds, uint32_t n
                              uint32_t* out_len, uint64_t cap, uint64_t* n_out);
 
 // noalloc.cu
+// Device address of the static scratch array on `device` (current), resolved
+// (and the array's module loaded) on the first call per device.
+bf_status na_scratch(int device, uint32_t** out);
 bf_status query_batch_noalloc(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,
                               uint32_t* d_out, cudaStream_t st);
 

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <queue>
 #include <thread>
@@ -31,7 +32,13 @@ namespace bf {
 namespace {
 
 
+// Hash of a target list: only a fast pre-check before the exact comparison
+// of the cached schedule's targets. Setting BF_TEST_SCHED_KEY_COLLIDE in the
+// environment makes every list hash alike (a test hook: schedules must then
+// still be told apart by the comparison).
 uint64_t hash_targets(const uint32_t* t, uint64_t T) {
+  static const bool collide = std::getenv("BF_TEST_SCHED_KEY_COLLIDE") != nullptr;
+  if (collide) return 0x5EEDull;
   uint64_t h = 1469598103934665603ull ^ T;
   for (uint64_t i = 0; i < T; ++i) {
     h ^= t[i];
@@ -118,7 +125,9 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   const uint64_t key = (all ? 0x9E3779B97F4A7C15ull : hash_targets(h_tgt, T)) ^
                        ((uint64_t)SPLIT << 56) ^ ((uint64_t)SMALL_SPLIT << 48) ^
                        ((uint64_t)SMALL_ROWS << 20);
-  if (sc.valid && sc.key == key && sc.T == T) {
+  // reuse only for the same split settings and exactly the same targets
+  if (sc.valid && sc.key == key && sc.T == T &&
+      (all || (sc.tgt.size() == T && (T == 0 || std::memcmp(sc.tgt.data(), h_tgt, T * 4) == 0)))) {
     ++sc.uses;
     return BF_OK;
   }
@@ -367,6 +376,10 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   sc.n_edges = n_e;
   sc.T = T;
   sc.key = key;
+  if (all)
+    sc.tgt.clear();
+  else
+    sc.tgt.assign(h_tgt, h_tgt + T);
   sc.valid = true;
   return BF_OK;
 }
