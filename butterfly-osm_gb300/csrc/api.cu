@@ -158,6 +158,13 @@ static bf_status graph_create(const bf_cch_csr* csr, const uint32_t* up_len,
   try {
     s = build_graph(csr, &c, g, up_len, down_len);
     if (s == BF_OK) s = batched_prepare(g, c.subtree_nodes);
+    if (s == BF_OK) {
+      // load the no-alloc entry point's module and static scratch now, while
+      // the caller still expects allocations (a failure here is reported by
+      // that entry point's own first call instead)
+      uint32_t* na = nullptr;
+      if (na_scratch(g->device, &na) != BF_OK) cudaGetLastError();
+    }
   } catch (const std::bad_alloc&) {
     set_error("out of host memory");
     s = BF_ERR_OOM;

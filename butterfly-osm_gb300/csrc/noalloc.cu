@@ -12,10 +12,14 @@
 // library holds that array until the process exits.
 //
 // Host code never uses the array's name as an address (on the host it is only
-// a stand-in symbol): the first call on each device, with that device
-// current, resolves the device address with cudaGetSymbolAddress and caches
-// it; later calls pass the cached pointer to the kernels. Make that first
-// call on a device before starting any stream capture.
+// a stand-in symbol): the device address is resolved with
+// cudaGetSymbolAddress, once per device with that device current, and cached;
+// calls pass the cached pointer to the kernels. CUDA loads this file's module
+// (and with it the array) lazily, at that first resolution, and the loading
+// itself allocates device memory. So bf_graph_create resolves it on the
+// graph's device, and a call with k = 0 does too (a warm-up): a caller that
+// reserves all remaining device memory for its own pool after creating the
+// graph, or that captures streams, has the array in place before either.
 //
 // All calls share the array and it keeps the last call's contents, so each
 // call re-initialises every scratch entry it reads. Calls whose kernels
@@ -40,6 +44,8 @@ static __device__ __align__(256) uint32_t g_noalloc_scratch[NA_WORDS];
 std::mutex na_mu;
 uint32_t* na_ptr[NA_MAX_DEVICES] = {};
 
+}  // namespace
+
 // Resolve the scratch array's device address on `device` (current).
 bf_status na_scratch(int device, uint32_t** out) {
   std::lock_guard<std::mutex> lk(na_mu);
@@ -56,6 +62,8 @@ bf_status na_scratch(int device, uint32_t** out) {
   *out = na_ptr[device];
   return BF_OK;
 }
+
+namespace {
 
 __global__ void k_na_fill(uint32_t* __restrict__ d, uint64_t m) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
@@ -170,10 +178,11 @@ bf_status query_batch_noalloc(Graph* g, const uint32_t* d_src, uint32_t k, uint3
               "scratch holds " + std::to_string((uint64_t)BF_NOALLOC_SCRATCH_BYTES) + " bytes");
     return BF_ERR_INVALID;
   }
-  if (k == 0) return BF_OK;
+  // resolved before the k == 0 return, so that an empty call is a warm-up
   uint32_t* scratch = nullptr;
   bf_status s;
   if ((s = na_scratch(g->device, &scratch))) return s;
+  if (k == 0) return BF_OK;
   const uint64_t m = (uint64_t)k * g->n;
   const unsigned fill_blocks = (unsigned)std::min<uint64_t>((m + 255) / 256, 152 * 32);
   k_na_fill<<<fill_blocks, 256, 0, st>>>(d_out, m);

@@ -216,11 +216,14 @@ bf_status bf_query_batch(bf_graph* g, const uint32_t* sources, uint32_t k, uint3
  * (the upward pass's ancestor paths, 8 * (max_depth + 1) bytes per source) is
  * a static device array of BF_NOALLOC_SCRATCH_BYTES that every GPU loading the
  * library holds until exit. Limits: k <= 32 and k * 8 * (max_depth + 1) <=
- * BF_NOALLOC_SCRATCH_BYTES, else BF_ERR_INVALID. The first call on a device
- * resolves the array's device address; make it before any stream capture.
- * All calls share the array: calls whose work overlaps on the GPU race and
- * must be serialised by the caller. stream is a cudaStream_t or NULL for the
- * graph's stream; the call returns after the work completed. */
+ * BF_NOALLOC_SCRATCH_BYTES, else BF_ERR_INVALID. CUDA loads the array (and
+ * the code that uses it) lazily; bf_graph_create loads it on the graph's
+ * device, and a call with k = 0 loads it and resolves its address without
+ * doing any work: make such a call before reserving the rest of the device
+ * memory for another allocator and before any stream capture. All calls
+ * share the array: calls whose work overlaps on the GPU race and must be
+ * serialised by the caller. stream is a cudaStream_t or NULL for the graph's
+ * stream; the call returns after the work completed. */
 bf_status bf_query_batch_noalloc(bf_graph* g, const uint32_t* d_sources, uint32_t k,
                                  uint32_t threshold, uint32_t* d_dist_out, void* stream);
 
