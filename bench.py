@@ -55,9 +55,14 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the library's default tunables (short profiling runs)")
-    ap.add_argument("--serve-s", type=float, default=15.0,
-                    help="seconds of Poisson arrivals for the serving run (0 = skip)")
-    ap.add_argument("--serve-rate", type=float, default=100.0, help="arrivals per second")
+    ap.add_argument("--serve-s", type=float, default=60.0,
+                    help="seconds of Poisson arrivals per serving rate (0 = skip)")
+    ap.add_argument("--serve-rates", default="50,100,250,500",
+                    help="arrival rates (requests per second), comma-separated")
+    ap.add_argument("--fresh-steps", type=int, default=10,
+                    help="timed steps with a new target set each (0 = skip)")
+    ap.add_argument("--plain-sources", type=int, default=1000,
+                    help="plain-engine matrix side (sources = targets, K = 32)")
     ap.add_argument("--isochrones", type=int, default=100000,
                     help="bulk isochrone origins (0 = skip)")
     ap.add_argument("--no-tiles", action="store_true",
@@ -247,16 +252,13 @@ def run_ours(args, rank, world, dist):
             "alg_bytes_per_sweep": alg_bytes, "sweep_ms": round(st["downward_ms"], 3),
             "swept_nodes": N, "swept_edges": M, "lanes": K}
 
-    # plain GPU sweep on a slice of the same workload (the >= 10x denominator)
-    g.set_engine(bfphast.ENGINE_PLAIN)
-    ps = 64
-    g.matrix(src[:32], tgt)
-    t0 = time.perf_counter()
-    pm = g.matrix(src[:ps], tgt)
-    plain_s = time.perf_counter() - t0
-    g.set_engine(bfphast.ENGINE_BATCHED)
-    plain_ok = bool(np.array_equal(pm, out_dev[:ps]))
-    plain_cps = ps * T / plain_s
+    # plain GPU sweep on its own workload (1000 x 1000, K = 32 batches): the
+    # >= 10x denominator, CUDA events on the launching stream
+    plain = run_plain(g, src, tgt, out_dev, args.plain_sources, stream)
+    fresh = None
+    if args.fresh_steps > 0:
+        fresh = run_fresh(g, cch, src, S, T, args.fresh_steps, max(3, args.warmup), stream,
+                          rank, dist)
 
     res = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_all, 3),
@@ -274,18 +276,23 @@ def run_ours(args, rank, world, dist):
                    "ms_per_step": round(e2e_s * 1e3, 3), "matches_device_run": e2e_ok},
            "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
            "roofline": roof,
-           "plain_gpu": {"value": round(plain_cps, 1), "unit": UNIT,
-                         "sample": "%d x %d rows, K=32 per launch sequence" % (ps, T),
-                         "bit_exact_vs_batched": plain_ok,
-                         "speedup_batched_over_plain": round(value / world / plain_cps, 2)},
+           "plain_gpu": dict(plain, speedup_batched_over_plain=round(
+               value / world / plain["value"], 2)),
            "phases_ms": {"upward": round(st["upward_ms"], 3),
                          "downward": round(st["downward_ms"], 3),
                          "extract": round(st["extract_ms"], 3)},
            "clocks": clk.summary()}
+    if fresh:
+        res["fresh_targets"] = fresh
     if args.isochrones > 0:
         res["isochrones"] = run_isochrones(g, cch, args.isochrones, seed=42 + rank)
     if args.serve_s > 0 and rank == 0:
-        res["serving"] = run_serving(g, cch["n"], args.serve_s, args.serve_rate)
+        rates = [float(x) for x in args.serve_rates.split(",") if x.strip()]
+        runs = [run_serving(g, cch["n"], args.serve_s, r) for r in rates]
+        res["serving"] = {"by_rate": runs,
+                          "mix": runs[0]["mix"] if runs else None,
+                          "workload": "Poisson arrivals for %.0f s at each rate on the "
+                                      "country graph" % args.serve_s}
     if args.contours > 0 and rank == 0:
         res["contours"] = run_contours(g, cch, args.contours, args.cols)
     if not args.no_customize and rank == 0:
@@ -293,6 +300,105 @@ def run_ours(args, rank, world, dist):
     if not args.no_tiles and rank == 0:
         res["tiles"] = run_tiles(out_dev, args.steps, args.warmup, not args.no_cpu)
     return res, cch, src, tgt, out_dev
+
+
+def run_plain(g, src, tgt, out_dev, side, stream):
+    """The plain engine (one K = 32 batch at a time) on a side x side matrix
+    of the same graph: CUDA events around one call after a warm-up call,
+    checked against the batched engine's cells."""
+    import numpy as np
+    import torch
+    import bfphast
+    side = min(side, len(src), len(tgt))
+    d_s = torch.from_numpy(src[:side].view(np.int32)).cuda()
+    d_t = torch.from_numpy(tgt[:side].view(np.int32)).cuda()
+    d_o = torch.empty(side * side, dtype=torch.int32, device="cuda")
+    g.set_engine(bfphast.ENGINE_PLAIN)
+    try:
+        g.matrix_device(d_s.data_ptr(), side, d_t.data_ptr(), side, d_o.data_ptr(),
+                        stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = g.matrix_device(d_s.data_ptr(), side, d_t.data_ptr(), side, d_o.data_ptr(),
+                             stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    finally:
+        g.set_engine(bfphast.ENGINE_BATCHED)
+    ms = e0.elapsed_time(e1)
+    got = d_o.view(side, side).cpu().numpy().view(np.uint32)
+    return {"value": round(side * side / ms * 1e3, 1), "unit": UNIT, "ms": round(ms, 3),
+            "workload": "%d x %d matrix, K = 32 lanes per batch, %d batches"
+                        % (side, side, (side + 31) // 32),
+            "gpu_launches": int(st["kernel_launches"]),
+            "bit_exact_vs_batched": bool(np.array_equal(got, out_dev[:side, :side]))}
+
+
+def run_fresh(g, cch, src, S, T, steps, warmup, stream, rank, dist):
+    """10k x 10k matrices with a NEW seeded target set every step (the
+    caller shape of a matrix server: each request brings its own targets), so
+    every step builds its target-restricted schedule: device-resident ids
+    (`value`) and through bf_matrix with page-locked host buffers (`e2e`).
+    The last step's matrix is checked on a row sample against the oracle."""
+    import numpy as np
+    import torch
+    import replicas
+    import workload
+    from oracle import oracle as orc
+    n = cch["n"]
+    sets = [workload.uniform_ids(n, T, 7001 + 97 * i + rank) for i in range(warmup + steps)]
+    d_sets = [torch.from_numpy(t.view(np.int32)).cuda() for t in sets]
+    d_src = torch.from_numpy(src.view(np.int32)).cuda()
+    d_out = torch.empty(S * T, dtype=torch.int32, device="cuda")
+
+    def step(i):
+        return g.matrix_device(d_src.data_ptr(), S, d_sets[i].data_ptr(), T, d_out.data_ptr(),
+                               stream=stream.cuda_stream)
+
+    for i in range(warmup):
+        step(i)
+    sync = (lambda: dist.barrier()) if dist else (lambda: None)
+    sync()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    e0.record(stream)
+    for i in range(warmup, warmup + steps):
+        stats.append(step(i))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = replicas.max_over_ranks(e0.elapsed_time(e1) / steps, dist, device="cuda")
+    last = d_out.view(S, T).cpu().numpy().view(np.uint32)
+    pick = np.linspace(0, S - 1, 16).astype(np.int64)
+    want, _ = orc.Cch.from_dict(cch).matrix(src[pick], sets[-1], threads=os.cpu_count() or 1)
+    exact = bool(np.array_equal(last[pick], want))
+    # end to end with page-locked host buffers, a new target set per step
+    pin = lambda a: torch.from_numpy(a.view(np.int32)).pin_memory().numpy().view(np.uint32)
+    h_src = pin(src)
+    h_sets = [pin(t) for t in sets]
+    h_out = torch.empty(S * T, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    h_out = h_out.reshape(S, T)
+    g.matrix(h_src, h_sets[0], out=h_out)
+    sync()
+    t0 = time.perf_counter()
+    for i in range(warmup, warmup + steps):
+        g.matrix(h_src, h_sets[i], out=h_out)
+    e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / steps, dist, device="cuda")
+    sched = [s_["schedule_ms"] for s_ in stats]
+    return {"value": round(replicas.whole_job_rate(S * T, 1, ms / 1e3), 1), "unit": UNIT,
+            "ms_per_step": round(ms, 3), "steps": steps,
+            "schedule_ms_mean": round(float(np.mean(sched)), 3),
+            "schedule_ms_max": round(float(np.max(sched)), 3),
+            "upward_ms": round(float(np.mean([s_["upward_ms"] for s_ in stats])), 3),
+            "downward_ms": round(float(np.mean([s_["downward_ms"] for s_ in stats])), 3),
+            "swept_nodes_mean": round(float(np.mean([s_["swept_nodes"] for s_ in stats])), 1),
+            "gpu_launches": int(sum(s_["kernel_launches"] for s_ in stats)),
+            "e2e": {"value": round(replicas.whole_job_rate(S * T, 1, e2e_s), 1), "unit": UNIT,
+                    "h2d_bytes_per_step": (S + T) * 4, "d2h_bytes_per_step": S * T * 4,
+                    "ms_per_step": round(e2e_s * 1e3, 3)},
+            "bit_exact_sample": {"rows": len(pick), "targets": T, "equal": exact},
+            "workload": "10k x 10k, a new seeded 10k-target set every step"}
 
 
 def run_serving(g, n, seconds, rate, seed=7):
@@ -316,17 +422,23 @@ def run_serving(g, n, seconds, rate, seed=7):
             specs.append(("i", int(rng.integers(0, n)), int(rng.integers(3000, 36001))))
     srv = bfphast.Server(g, hbm_budget=60 << 30, max_inflight=64)
     kinds, done = {}, {}
+    rejected = 0
     t0 = time.perf_counter()
     for i, (at, sp) in enumerate(zip(arrivals, specs)):
         wait = t0 + at - time.perf_counter()
         if wait > 0:
             time.sleep(wait)
-        if sp[0] == "m":
-            t, _ = srv.submit_matrix(sp[1], sp[2], tag=i)
-            kinds[t] = ("m", len(sp[1]) * len(sp[2]))
-        else:
-            t, _ = srv.submit_isochrone(sp[1], sp[2], tag=i)
-            kinds[t] = ("i", 0)
+        try:
+            if sp[0] == "m":
+                t, _ = srv.submit_matrix(sp[1], sp[2], tag=i)
+                kinds[t] = ("m", len(sp[1]) * len(sp[2]))
+            else:
+                t, _ = srv.submit_isochrone(sp[1], sp[2], tag=i)
+                kinds[t] = ("i", 0)
+        except bfphast.BfError as e:
+            if e.status != bfphast.BF_ERR_BUSY:
+                raise
+            rejected += 1
         for c in srv.poll(wait_ms=0):
             done[c["ticket"]] = c
     while len(done) < len(kinds) and time.perf_counter() - t0 < seconds + 120:
@@ -344,7 +456,9 @@ def run_serving(g, n, seconds, rate, seed=7):
             cells += cl
     alll = lat["m"] + lat["i"]
     pct = lambda v, q: round(float(np.percentile(v, q)), 2) if v else None
-    return {"requests": count, "completed_ok": ok, "seconds": seconds, "rate_req_s": rate,
+    return {"requests": count, "completed_ok": ok, "rejected_busy": rejected,
+            "failed": len(done) - ok, "unfinished": len(kinds) - len(done),
+            "seconds": seconds, "rate_req_s": rate, "elapsed_s": round(elapsed, 2),
             "p50_ms": pct(alll, 50), "p99_ms": pct(alll, 99),
             "matrix_p50_ms": pct(lat["m"], 50), "matrix_p99_ms": pct(lat["m"], 99),
             "isochrone_p50_ms": pct(lat["i"], 50), "isochrone_p99_ms": pct(lat["i"], 99),

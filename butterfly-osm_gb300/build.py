@@ -17,7 +17,7 @@ OBJ = PKG / "_build"
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_UNITS = ["graph", "engine_plain", "engine_batched", "isochrone", "seeded", "twochannel", "customize", "contour", "tile", "server", "noalloc", "api"]
+CU_UNITS = ["graph", "engine_plain", "engine_batched", "schedule", "isochrone", "seeded", "twochannel", "customize", "contour", "tile", "server", "noalloc", "api"]
 CU_HEADERS = ["engine.cuh"]
 
 

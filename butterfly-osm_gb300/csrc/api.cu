@@ -272,6 +272,7 @@ static bf_tune to_c(const Tune& t) {
   o.overlap_upward = t.overlap_up;
   o.mapped_output = t.mapped_out;
   o.hub_l2_mb = t.hub_mb;
+  o.device_schedule = t.dev_sched;
   return o;
 }
 
@@ -298,6 +299,7 @@ bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
   h->g.tune.overlap_up = t->overlap_upward ? 1 : 0;
   h->g.tune.mapped_out = t->mapped_output ? 1 : 0;
   h->g.tune.hub_mb = std::min<uint32_t>(t->hub_l2_mb, 1024);
+  h->g.tune.dev_sched = t->device_schedule ? 1 : 0;
   return BF_OK;
 }
 

@@ -131,7 +131,20 @@ struct Sched {
   uint32_t hub_rows = 0;         // rows set in d_hub
   std::vector<uint32_t> ranks;   // ranks whose d_cidx entry is set (reset on rebuild)
   bool cidx_ready = false;       // d_cidx holds NONE outside `ranks`
+  size_t cap_cidx = 0;
+  // built on the device (schedule.cu): d_cidx was rewritten whole, gather
+  // counts per row in d_uses feed the hub choice on the device
+  bool dev_built = false;
+  bool cidx_dirty = false;       // d_cidx entries outside `ranks` may be set
+  uint32_t peel_left = 0;        // frontier left when the peeling round limit ended (0 = exact)
+  uint32_t* d_uses = nullptr;    // [rows] gathers per row
+  size_t cap_uses = 0;
+  uint32_t* d_hub_h = nullptr;   // hub histogram (65536 bins) and threshold
+  size_t cap_hub_h = 0;
 };
+
+struct SchedScratch;  // device schedule builder scratch (schedule.cu)
+void free_sched_scratch(SchedScratch* s);
 
 // Execution context of the batched engine: schedules, the distance slab and
 // scratch of one in-flight computation. The C-ABI calls use the graph's
@@ -159,6 +172,7 @@ struct Ctx {
   size_t cap_one = 0;
   void* h_stage = nullptr;         // page-locked staging arena for schedule uploads
   size_t stage_bytes = 0;
+  SchedScratch* sd = nullptr;      // device schedule builder scratch
 };
 
 // Tunables of the batched sweep (chosen by bf_autotune).
@@ -175,6 +189,7 @@ struct Tune {
   uint32_t overlap_up = 1;   // upward pass on a side stream during the slab reset
   uint32_t hub_mb = 48;      // L2 megabytes the most-gathered rows may keep (0 = off)
   uint32_t mapped_out = 1;   // bf_matrix writes a page-locked output buffer directly
+  uint32_t dev_sched = 1;    // build target-restricted schedules on the device
 };
 
 struct Graph {
@@ -210,6 +225,8 @@ struct Graph {
   // device: level-ordered pull CSR (plain engine)
   uint64_t* d_in_off = nullptr;   // [n+1] by slab position
   uint2* d_in_rec = nullptr;      // {source slab position, w}
+  uint32_t* d_in_len = nullptr;   // length weight per d_in_rec entry (two-channel graphs)
+  uint32_t* d_lvl_start = nullptr;  // [n_levels + 1] level -> first slab position
   // device: plain engine work buffers
   uint32_t* d_dist = nullptr;     // [n][32]
   uint32_t* d_seed = nullptr;     // [n][32], all INF between calls
@@ -304,7 +321,12 @@ __global__ void k_extract(const uint32_t* __restrict__ slab, uint32_t slab_strid
 // engine_batched.cu
 bf_status batched_prepare(Graph* g, uint32_t split_edges);
 bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
-                         cudaStream_t st);
+                         cudaStream_t st, const uint32_t* d_tgt = nullptr);
+// schedule.cu: the target-restricted schedule of h_tgt (host) / d_tgt (the
+// same targets on the device, or null) built on the device
+bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt,
+                                const uint32_t* d_tgt, uint64_t T, uint64_t key, cudaStream_t st);
+bf_status hub_rows_device(Graph* g, Sched& sc, uint32_t H, cudaStream_t st);
 bf_status sweep_levels(Graph* g, Sched& sc, uint32_t* slab, uint32_t Kp, unsigned lane_blocks,
                        unsigned tpb, cudaStream_t st, uint64_t* launches,
                        const uint32_t* seeded);

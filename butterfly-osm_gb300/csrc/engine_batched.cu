@@ -118,7 +118,7 @@ __global__ void k_scatter_pairs(const uint2* __restrict__ pr, uint64_t m,
 // map is patched in place: entries of the previous schedule are reset to
 // NONE and the new ones set.
 bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uint64_t T, bool all,
-                         cudaStream_t st) {
+                         cudaStream_t st, const uint32_t* d_tgt) {
   const uint32_t SPLIT = std::max<uint32_t>(1, g->tune.split);
   const uint32_t SMALL_ROWS = g->tune.small_rows;
   const uint32_t SMALL_SPLIT = std::max<uint32_t>(1, std::min(SPLIT, g->tune.small_split));
@@ -140,6 +140,16 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   if (sc.one_exec) {
     cudaGraphExecDestroy(sc.one_exec);
     sc.one_exec = nullptr;
+  }
+  // restricted schedules are built on the device (schedule.cu) unless turned
+  // off; the totals it reads back carry edges in 32 bits
+  if (!all && T && g->tune.dev_sched && g->n_down < 0xFFFFFFFFull)
+    return build_schedule_device(g, c, sc, h_tgt, d_tgt, T, key, st);
+  sc.dev_built = false;
+  if (sc.cidx_dirty) {  // the device build wrote every rank: reset the map whole
+    sc.ranks.clear();
+    sc.cidx_ready = false;
+    sc.cidx_dirty = false;
   }
   const uint32_t n = g->n;
   if (c.rowmap.size() != n) c.rowmap.assign(n, NONE);
@@ -334,8 +344,7 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   }
   for (uint32_t p : R) c.rowmap[p] = NONE;
   bf_status s;
-  size_t cap_c = sc.d_cidx ? n : 0;
-  if ((s = ensure(&sc.d_cidx, cap_c, n, g))) return s;
+  if ((s = ensure(&sc.d_cidx, sc.cap_cidx, n, g))) return s;
   if ((s = ensure(&sc.d_item, sc.cap_items, n_i, g))) return s;
   if ((s = ensure(&sc.d_erec, sc.cap_edges, n_e, g))) return s;
   if (two && (s = ensure(&sc.d_elen, sc.cap_elen, n_e, g))) return s;
@@ -624,7 +633,7 @@ uint64_t ctx_budget(Graph* g, Ctx& c) {
 
 static void free_sched(Sched& sc) {
   void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_elen, sc.d_trow, sc.d_split, sc.d_hub,
-               sc.d_lvl};
+               sc.d_lvl, sc.d_uses, sc.d_hub_h};
   for (void* q : p)
     if (q) cudaFree(q);
   if (sc.gexec) cudaGraphExecDestroy(sc.gexec);
@@ -642,6 +651,7 @@ void free_ctx(Ctx& c) {
   if (c.d_cseed) cudaFree(c.d_cseed);
   if (c.d_one) cudaFree(c.d_one);
   if (c.h_stage) cudaFreeHost(c.h_stage);
+  free_sched_scratch(c.sd);
   for (auto& e : c.ev)
     if (e) cudaEventDestroy(e);
   if (c.fork) cudaEventDestroy(c.fork);
@@ -668,11 +678,15 @@ bf_status batched_prepare(Graph* g, uint32_t) {
 bf_status hub_rows(Graph* g, Sched& sc, uint64_t row_bytes, cudaStream_t st, const uint32_t** hub) {
   *hub = nullptr;
   uint32_t H = 0;
+  const uint64_t ranked = sc.dev_built ? std::min<uint32_t>(sc.n_r, 65536) : sc.hub_order.size();
   if (g->tune.hub_mb && row_bytes)
-    H = (uint32_t)std::min<uint64_t>(sc.hub_order.size(),
-                                     ((uint64_t)g->tune.hub_mb << 20) / row_bytes);
+    H = (uint32_t)std::min<uint64_t>(ranked, ((uint64_t)g->tune.hub_mb << 20) / row_bytes);
   if (!H) return BF_OK;
-  if (H != sc.hub_rows) {
+  if (H != sc.hub_rows && sc.dev_built) {
+    bf_status rc;
+    if ((rc = hub_rows_device(g, sc, H, st))) return rc;
+    sc.hub_rows = H;
+  } else if (H != sc.hub_rows) {
     std::vector<uint32_t> bits((std::max<uint32_t>(sc.n_r, 1) + 31) / 32, 0);
     for (uint32_t i = 0; i < H; ++i) bits[sc.hub_order[i] >> 5] |= 1u << (sc.hub_order[i] & 31);
     bf_status s;
@@ -865,7 +879,7 @@ bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, co
       return BF_ERR_INVALID;
     }
   const auto tb = std::chrono::steady_clock::now();
-  if ((s = build_schedule(g, c, c.sc, h_tgt.data(), T, false, st))) return s;
+  if ((s = build_schedule(g, c, c.sc, h_tgt.data(), T, false, st, d_tgt))) return s;
   if (stats)
     stats->schedule_ms +=
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();

@@ -337,6 +337,8 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
   if ((s = dev_upload(&g->d_rank_at, rank_at.data(), n, g))) return s;
   if ((s = dev_upload(&g->d_in_off, in_off.data(), n + 1, g))) return s;
   if ((s = dev_upload(&g->d_in_rec, in_rec.data(), in_rec.size(), g))) return s;
+  if (two && (s = dev_upload(&g->d_in_len, in_len.data(), in_len.size(), g))) return s;
+  if ((s = dev_upload(&g->d_lvl_start, g->lvl_start.data(), g->lvl_start.size(), g))) return s;
   uint32_t zero = 0;
   if ((s = dev_upload(&g->d_err, &zero, 1, g))) return s;
   g->rank_at = std::move(rank_at);
@@ -352,7 +354,8 @@ void free_graph(Graph* g) {
   if (!g) return;
   cudaSetDevice(g->device);
   void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec, g->d_up_len,
-                  g->d_pos_of,  g->d_rank_at, g->d_in_off, g->d_in_rec, g->d_dist,
+                  g->d_pos_of,  g->d_rank_at, g->d_in_off, g->d_in_rec, g->d_in_len,
+                  g->d_lvl_start, g->d_dist,
                   g->d_seed,    g->d_flag,    g->d_err,    g->d_io,
                   g->d_iso,     g->d_set_pre, g->d_set_out, g->d_set_off};
   for (void* p : ptrs)

@@ -186,6 +186,8 @@ typedef struct bf_tune {
                                   written by the extraction kernel directly     */
   uint32_t hub_l2_mb;          /* L2 megabytes kept for the most-gathered rows
                                   (evict-last cache hints; 0 = no hints)         */
+  uint32_t device_schedule;    /* 1: target-restricted schedules are built on
+                                  the device; 0: by host threads (same rows)    */
 } bf_tune;
 
 /* Time candidate tunables on a sample matrix (device buffers: d_sources,
