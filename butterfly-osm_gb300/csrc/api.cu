@@ -143,6 +143,7 @@ static bf_status graph_create(const bf_cch_csr* csr, const uint32_t* up_len,
   Graph* g = &h->g;
   g->device = c.device;
   g->l2_bytes = l2_bytes;
+  g->sm_count = (uint32_t)prop.multiProcessorCount;
   g->engine = c.engine == BF_ENGINE_AUTO ? BF_ENGINE_BATCHED : c.engine;
   g->k_lanes = c.k_lanes;
   if (cudaSetDevice(c.device) != cudaSuccess) {
@@ -273,6 +274,7 @@ static bf_tune to_c(const Tune& t) {
   o.mapped_output = t.mapped_out;
   o.hub_l2_mb = t.hub_mb;
   o.device_schedule = t.dev_sched;
+  o.persistent_sweep = t.persist;
   return o;
 }
 
@@ -300,6 +302,7 @@ bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
   h->g.tune.mapped_out = t->mapped_output ? 1 : 0;
   h->g.tune.hub_mb = std::min<uint32_t>(t->hub_l2_mb, 1024);
   h->g.tune.dev_sched = t->device_schedule ? 1 : 0;
+  h->g.tune.persist = t->persistent_sweep & 3u;
   return BF_OK;
 }
 

@@ -83,6 +83,57 @@ __device__ __forceinline__ bool is_hub(const uint32_t* hub, uint32_t r) {
   return hub && ((hub[r >> 5] >> (r & 31)) & 1u);
 }
 
+// ---- persistent level loops -------------------------------------------------
+// A persistent sweep is one cooperative launch whose blocks walk the levels
+// themselves, separated by a software grid barrier, instead of one launch per
+// level. Its level program lists segments: one level for the whole grid
+// (followed by a barrier), or a run of consecutive small levels that block 0
+// sweeps alone with __syncthreads between them (one barrier after the run).
+// A segment is {first level, last level + 1 | PROG_RUN}.
+constexpr uint32_t PROG_RUN = 0x80000000u;
+// Cycles a block waits at a grid barrier before it gives up (about 2 s).
+constexpr long long BARRIER_TIMEOUT_CYCLES = 4000000000ll;
+
+// Grid barrier number b of a cooperative launch: bar[0] counts arrivals
+// (monotonic over the launch, zeroed before it), bar[1] is set by a block
+// that gave up. Every wait is bounded: past `timeout` cycles the block sets
+// DEVERR_TIMEOUT and the abort flag, and all blocks leave (returns false).
+// The release/acquire pair orders each block's writes before the barrier
+// against every block's reads after it; callers read data other blocks wrote
+// through L2 (ld.cg), never through L1.
+__device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t b, long long timeout,
+                                             uint32_t* err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t target = (b + 1) * gridDim.x;
+    __threadfence();
+    atomicAdd(bar, 1u);
+    const long long t0 = clock64();
+    int ok = 1;
+    for (;;) {
+      uint32_t v, ab;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+      if (v >= target) break;
+      asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(ab) : "l"(bar + 1) : "memory");
+      if (ab) {
+        ok = 0;
+        break;
+      }
+      if (clock64() - t0 > timeout) {
+        atomicOr(err, DEVERR_TIMEOUT);
+        atomicExch(bar + 1, 1u);
+        ok = 0;
+        break;
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 // Lanes per batch of the plain engine (one warp lane per source).
 constexpr uint32_t PLAIN_K = 32;
 // Ancestor-path entries a warp keeps in shared memory during the upward pass.
@@ -173,6 +224,12 @@ struct Ctx {
   void* h_stage = nullptr;         // page-locked staging arena for schedule uploads
   size_t stage_bytes = 0;
   SchedScratch* sd = nullptr;      // device schedule builder scratch
+  // level program of the persistent isochrone sweep (full schedule)
+  std::vector<uint2> iso_prog;
+  uint2* d_iso_prog = nullptr;
+  size_t iso_prog_bytes = 0;
+  uint32_t iso_prog_slots = 0;
+  size_t iso_prog_levels = 0;
 };
 
 // Tunables of the batched sweep (chosen by bf_autotune).
@@ -190,6 +247,8 @@ struct Tune {
   uint32_t hub_mb = 48;      // L2 megabytes the most-gathered rows may keep (0 = off)
   uint32_t mapped_out = 1;   // bf_matrix writes a page-locked output buffer directly
   uint32_t dev_sched = 1;    // build target-restricted schedules on the device
+  uint32_t persist = 1;      // bit 0: the plain engine's sweep, bit 1: isochrone waves'
+                             // sweeps as one persistent launch instead of one per level
 };
 
 struct Graph {
@@ -203,6 +262,12 @@ struct Graph {
   std::atomic<uint64_t> device_bytes{0};
   uint64_t hbm_budget = 0;
   uint64_t l2_bytes = 0;          // L2 size of the device (cache-hint decisions)
+  uint32_t sm_count = 0;          // streaming multiprocessors (persistent grids)
+  uint32_t* d_bar = nullptr;      // grid-barrier words of persistent launches (2 per stream use)
+  std::vector<uint2> plain_prog;  // level program of the plain engine's persistent sweep
+  uint2* d_plain_prog = nullptr;
+  size_t plain_prog_bytes = 0;
+  size_t plain_prog_levels = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
   std::mutex mu;
@@ -255,6 +320,35 @@ struct Graph {
   uint64_t set_stage_cap = 0;      // u32 entries
 };
 
+// Level program of a persistent sweep over levels whose sizes are
+// first[l + 1] - first[l] (rows or work items): levels of at most `small`
+// units form runs for block 0 when two or more are consecutive.
+inline std::vector<uint2> level_program(const std::vector<uint32_t>& first, uint32_t n_levels,
+                                        uint32_t small) {
+  std::vector<uint2> prog;
+  for (uint32_t l = 0; l < n_levels; ++l) {
+    const uint32_t m = first[l + 1] - first[l];
+    if (!m) continue;
+    if (m <= small) {
+      uint32_t l1 = l + 1;
+      while (l1 < n_levels && first[l1 + 1] - first[l1] <= small) ++l1;
+      if (l1 - l >= 2) {
+        prog.push_back(make_uint2(l, l1 | PROG_RUN));
+        l = l1 - 1;
+        continue;
+      }
+    }
+    prog.push_back(make_uint2(l, l + 1));
+  }
+  return prog;
+}
+
+// Test hook of the persistent sweeps: with BF_TEST_WITHHOLD_ARRIVAL set in
+// the environment, a persistent sweep runs on two blocks, block 1 leaves
+// before its first grid-barrier arrival and the waits end after about a
+// millisecond, so the call must report BF_ERR_TIMEOUT.
+bool test_withhold_arrival();
+
 // f(i) for i in [0, n) on up to 64 host threads (dynamic assignment).
 template <class F>
 inline void parallel_for(uint64_t n, F&& f) {
@@ -287,6 +381,26 @@ inline cudaError_t launch_level(void (*kern)(P...), dim3 grid, unsigned tpb, boo
   cfg.numAttrs = pdl ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kern, args...);
 }
+
+// Cooperative launch of a persistent sweep kernel on `blocks` blocks.
+template <class... P, class... A>
+inline cudaError_t launch_persistent(void (*kern)(P...), unsigned blocks, unsigned tpb,
+                                     cudaStream_t s, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(tpb);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+// engine_plain.cu: co-resident blocks of a persistent kernel (at most cap,
+// two under the test hook) and the graph's grid-barrier words
+unsigned persistent_blocks(Graph* g, const void* kern, unsigned tpb, unsigned cap);
+bf_status ensure_barrier(Graph* g);
 
 // graph.cu
 bf_status build_graph(const bf_cch_csr* csr, const bf_config* cfg, Graph* g,

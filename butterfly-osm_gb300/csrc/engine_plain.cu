@@ -14,6 +14,7 @@
 //      matrix through a shared-memory transpose (batched_phast.rs:693-701).
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "engine.cuh"
 
@@ -207,6 +208,128 @@ __global__ void __launch_bounds__(256)
   dist[(size_t)p * PLAIN_K + lane] = best;
 }
 
+// The node step of the plain sweep for slab position p (a warp, lane =
+// source): the seed, then the min-plus pull over the DOWN in-edges. Rows of
+// earlier levels are read through L2 (other blocks of a persistent launch
+// wrote them).
+__device__ __forceinline__ void plain_node(uint32_t p, uint32_t lane,
+                                           const uint64_t* __restrict__ in_off,
+                                           const uint2* __restrict__ in_rec,
+                                           uint32_t* __restrict__ dist, uint32_t* __restrict__ seed,
+                                           uint32_t* __restrict__ flag, uint32_t threshold) {
+  uint32_t best = INF;
+  const uint32_t bit = 1u << (p & 31);
+  if (flag[p >> 5] & bit) {
+    best = seed[(size_t)p * PLAIN_K + lane];
+    seed[(size_t)p * PLAIN_K + lane] = INF;
+    __syncwarp();
+    if (lane == 0) atomicAnd(&flag[p >> 5], ~bit);
+  }
+  uint64_t e = in_off[p];
+  const uint64_t e1 = in_off[p + 1];
+  for (; e + 4 <= e1; e += 4) {
+    const uint2 r0 = in_rec[e], r1 = in_rec[e + 1], r2 = in_rec[e + 2], r3 = in_rec[e + 3];
+    const uint32_t a0 = __ldcg(&dist[(size_t)r0.x * PLAIN_K + lane]);
+    const uint32_t a1 = __ldcg(&dist[(size_t)r1.x * PLAIN_K + lane]);
+    const uint32_t a2 = __ldcg(&dist[(size_t)r2.x * PLAIN_K + lane]);
+    const uint32_t a3 = __ldcg(&dist[(size_t)r3.x * PLAIN_K + lane]);
+    best = min(best, min(min(sat_add(a0, r0.y), sat_add(a1, r1.y)),
+                         min(sat_add(a2, r2.y), sat_add(a3, r3.y))));
+  }
+  for (; e < e1; ++e) {
+    const uint2 r = in_rec[e];
+    best = min(best, sat_add(__ldcg(&dist[(size_t)r.x * PLAIN_K + lane]), r.y));
+  }
+  if (best > threshold) best = INF;
+  dist[(size_t)p * PLAIN_K + lane] = best;
+}
+
+// The whole plain sweep of one K = 32 batch in one cooperative launch over
+// the full-graph schedule (rows = slab positions; nodes of high in-degree are
+// split into work items of at most 16 in-edges, combined with atomicMin). A
+// warp owns an item, lane = source. Phase 0 sets the rows that are read
+// before they are fully written (no in-edges, or split) to their seed or INF;
+// then the blocks walk the level program (a level spread over every warp of
+// the grid, or a run of small levels swept by block 0 alone) with a grid
+// barrier between segments. Values above the threshold become INF in every
+// item (a split row's minimum is then still the clamped minimum). `withhold`
+// (a test hook, NONE otherwise) names a block that leaves before its first
+// barrier arrival.
+__global__ void __launch_bounds__(512)
+    k_plain_persist(const uint2* __restrict__ prog, uint32_t P, const uint32_t* __restrict__ lvl,
+                    const uint4* __restrict__ item, const uint2* __restrict__ erec,
+                    const uint32_t* __restrict__ reset_bits, uint32_t words,
+                    uint32_t* __restrict__ dist, uint32_t* __restrict__ seed,
+                    uint32_t* __restrict__ flag, uint32_t threshold, uint32_t* __restrict__ bar,
+                    long long timeout, uint32_t withhold, uint32_t* __restrict__ err) {
+  const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const uint32_t gw = blockIdx.x * wpb + wib, tw = gridDim.x * wpb;
+  for (uint32_t w = gw; w < words; w += tw) {
+    const uint32_t m = reset_bits[w];
+    if (!m) continue;
+    const uint32_t f = flag[w];
+    for (uint32_t mm = m; mm;) {
+      const uint32_t b = __ffs(mm) - 1;
+      mm &= mm - 1;
+      const size_t at = (size_t)(w * 32 + b) * PLAIN_K + lane;
+      uint32_t v = INF;
+      if ((f >> b) & 1u) {
+        v = seed[at];
+        seed[at] = INF;
+      }
+      dist[at] = v > threshold ? INF : v;
+    }
+    __syncwarp();
+    if (lane == 0 && (f & m)) atomicAnd(&flag[w], ~(f & m));
+  }
+  if (blockIdx.x == withhold) return;
+  if (!grid_barrier(bar, 0, timeout, err)) return;
+  for (uint32_t s = 0; s < P; ++s) {
+    const uint2 sg = prog[s];
+    const bool run = (sg.y & PROG_RUN) != 0;
+    const uint32_t l0 = sg.x, l1 = run ? (blockIdx.x == 0 ? sg.y & ~PROG_RUN : l0) : l0 + 1;
+    const uint32_t first = run ? wib : gw, stride = run ? wpb : tw;
+    for (uint32_t l = l0; l < l1; ++l) {
+      const uint32_t i1 = lvl[l + 1];
+      for (uint32_t ii = lvl[l] + first; ii < i1; ii += stride) {
+        const uint4 it = item[ii];
+        uint32_t acc = INF;
+        uint32_t e = it.y;
+        for (; e + 4 <= it.z; e += 4) {
+          const uint2 r0 = erec[e], r1 = erec[e + 1], r2 = erec[e + 2], r3 = erec[e + 3];
+          const uint32_t a0 = __ldcg(&dist[(size_t)r0.x * PLAIN_K + lane]);
+          const uint32_t a1 = __ldcg(&dist[(size_t)r1.x * PLAIN_K + lane]);
+          const uint32_t a2 = __ldcg(&dist[(size_t)r2.x * PLAIN_K + lane]);
+          const uint32_t a3 = __ldcg(&dist[(size_t)r3.x * PLAIN_K + lane]);
+          acc = min(acc, min(min(sat_add(a0, r0.y), sat_add(a1, r1.y)),
+                             min(sat_add(a2, r2.y), sat_add(a3, r3.y))));
+        }
+        for (; e < it.z; ++e) {
+          const uint2 r = erec[e];
+          acc = min(acc, sat_add(__ldcg(&dist[(size_t)r.x * PLAIN_K + lane]), r.y));
+        }
+        const size_t at = (size_t)it.x * PLAIN_K + lane;
+        if (it.w) {  // a slice of a split row, initialised in phase 0
+          if (acc <= threshold) atomicMin(&dist[at], acc);
+        } else {
+          const uint32_t bit = 1u << (it.x & 31);
+          uint32_t best = acc;
+          if (flag[it.x >> 5] & bit) {
+            best = min(best, seed[at]);
+            seed[at] = INF;
+            __syncwarp();
+            if (lane == 0) atomicAnd(&flag[it.x >> 5], ~bit);
+          }
+          dist[at] = best > threshold ? INF : best;
+        }
+      }
+      if (run) __syncthreads();
+    }
+    if (s + 1 == P) break;
+    if (!grid_barrier(bar, s + 1, timeout, err)) return;
+  }
+}
+
 // out[(row0 + l) * T + t] = slab[tpos[t]][l] for l < k; tiles of 32 targets.
 __global__ void __launch_bounds__(256)
     k_extract(const uint32_t* __restrict__ slab, uint32_t slab_stride,
@@ -255,12 +378,25 @@ bf_status check_device_error(Graph* g, cudaStream_t st) {
   if (h) {
     BF_CUDA(cudaMemsetAsync(g->d_err, 0, 4, st));
     BF_CUDA(cudaStreamSynchronize(st));
+    if (h & DEVERR_TIMEOUT) {
+      // a sweep that gave up may have left seeds in the plain engine's
+      // buffers, which must be all INF / clear between calls
+      if (g->d_seed) {
+        BF_CUDA(cudaMemsetAsync(g->d_seed, 0xFF, (size_t)g->n * PLAIN_K * 4, st));
+        BF_CUDA(cudaMemsetAsync(g->d_flag, 0, ((g->n + 31) / 32) * 4, st));
+        BF_CUDA(cudaStreamSynchronize(st));
+      }
+      set_error("a bounded device wait ran out (error bits 0x" + std::to_string(h) + ")");
+      return BF_ERR_TIMEOUT;
+    }
     set_error("device reported error bits 0x" + std::to_string(h) +
               " (invalid node id or CCH inconsistent with its elimination tree)");
     return BF_ERR_INVALID;
   }
   return BF_OK;
 }
+
+bool test_withhold_arrival() { return std::getenv("BF_TEST_WITHHOLD_ARRIVAL") != nullptr; }
 
 static bf_status plain_buffers(Graph* g) {
   if (g->d_dist) return BF_OK;
@@ -346,7 +482,64 @@ static bf_status plain_upward(Graph* g, const uint32_t* d_src, uint32_t k, uint3
   return launch_upward(g, d_src, k, threshold, g->d_pos_of, g->d_seed, PLAIN_K, g->d_flag, st);
 }
 
+// Blocks of a persistent launch: as many as are co-resident (the cooperative
+// launch guarantees they run together), at most `cap`; two under the test hook.
+unsigned persistent_blocks(Graph* g, const void* kern, unsigned tpb, unsigned cap) {
+  if (test_withhold_arrival()) return 2;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)tpb, 0) != cudaSuccess) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return std::max(1u, std::min(cap, (unsigned)std::max(per_sm, 1) * g->sm_count));
+}
+
+bf_status ensure_barrier(Graph* g) {
+  if (g->d_bar) return BF_OK;
+  BF_CUDA(cudaMalloc(&g->d_bar, 64));
+  g->device_bytes += 64;
+  return BF_OK;
+}
+
+static bf_status plain_sweep_persistent(Graph* g, uint32_t threshold, cudaStream_t st,
+                                        uint64_t* launches) {
+  constexpr unsigned TPB = 512;
+  bf_status s;
+  if ((s = ensure_barrier(g))) return s;
+  Ctx& c = g->ctx;
+  if ((s = build_schedule(g, c, c.full, nullptr, 0, true, st))) return s;
+  Sched& sc = c.full;
+  if (g->plain_prog.empty() || g->plain_prog_levels != sc.lvl_item.size()) {
+    // runs: levels of at most two rounds of one block's warps
+    g->plain_prog = level_program(sc.lvl_item, g->n_levels, 2 * (TPB / 32));
+    if (g->d_plain_prog) {
+      cudaFree(g->d_plain_prog);
+      g->device_bytes -= g->plain_prog_bytes;
+      g->d_plain_prog = nullptr;
+    }
+    g->plain_prog_bytes = std::max<size_t>(g->plain_prog.size(), 1) * sizeof(uint2);
+    BF_CUDA(cudaMalloc(&g->d_plain_prog, g->plain_prog_bytes));
+    g->device_bytes += g->plain_prog_bytes;
+    BF_CUDA(cudaMemcpyAsync(g->d_plain_prog, g->plain_prog.data(),
+                            g->plain_prog.size() * sizeof(uint2), cudaMemcpyHostToDevice, st));
+    g->plain_prog_levels = sc.lvl_item.size();
+  }
+  const bool hook = test_withhold_arrival();
+  const unsigned blocks = persistent_blocks(g, (const void*)k_plain_persist, TPB, 4 * g->sm_count);
+  BF_CUDA(cudaMemsetAsync(g->d_bar, 0, 8, st));
+  BF_CUDA(launch_persistent(k_plain_persist, blocks, TPB, st, (const uint2*)g->d_plain_prog,
+                            (uint32_t)g->plain_prog.size(), (const uint32_t*)sc.d_lvl,
+                            (const uint4*)sc.d_item, (const uint2*)sc.d_erec,
+                            (const uint32_t*)sc.d_split, (uint32_t)((g->n + 31) / 32), g->d_dist,
+                            g->d_seed, g->d_flag, threshold, g->d_bar,
+                            hook ? 2000000ll : BARRIER_TIMEOUT_CYCLES, hook ? 1u : NONE,
+                            g->d_err));
+  ++*launches;
+  return BF_OK;
+}
+
 static bf_status plain_sweep(Graph* g, uint32_t threshold, cudaStream_t st, uint64_t* launches) {
+  if (g->tune.persist & 1u) return plain_sweep_persistent(g, threshold, st, launches);
   for (uint32_t l = 0; l < g->n_levels; ++l) {
     uint32_t p0 = g->lvl_start[l], p1 = g->lvl_start[l + 1];
     if (p1 == p0) continue;

@@ -355,7 +355,7 @@ void free_graph(Graph* g) {
   cudaSetDevice(g->device);
   void* ptrs[] = {g->d_parent, g->d_run_end, g->d_depth, g->d_up_off, g->d_up_rec, g->d_up_len,
                   g->d_pos_of,  g->d_rank_at, g->d_in_off, g->d_in_rec, g->d_in_len,
-                  g->d_lvl_start, g->d_dist,
+                  g->d_lvl_start, g->d_bar, g->d_plain_prog, g->d_dist,
                   g->d_seed,    g->d_flag,    g->d_err,    g->d_io,
                   g->d_iso,     g->d_set_pre, g->d_set_out, g->d_set_off};
   for (void* p : ptrs)

@@ -188,6 +188,75 @@ __global__ void __launch_bounds__(128, IPB > 1 ? 12 : 16)
   }
 }
 
+// One work item for one thread of a group of Kp / 8 threads (8 lanes each):
+// the thread walks the item's in-edges four at a time (edge records,
+// activity words and rows of four edges in flight together). With CG, rows
+// and activity bits are read through L2 (other blocks may have written them).
+template <bool CG>
+__device__ __forceinline__ void group16_item(const uint4 it, const uint2* __restrict__ erec,
+                                             uint16_t* __restrict__ slab, uint32_t Kp,
+                                             uint32_t* __restrict__ active,
+                                             const uint32_t* __restrict__ thr, uint32_t lane,
+                                             bool live, uint32_t valid_lanes,
+                                             const uint32_t* __restrict__ seeded,
+                                             uint32_t* __restrict__ err) {
+  uint4 acc = make_uint4(~0u, ~0u, ~0u, ~0u);
+  bool any = false;
+  for (uint32_t e0 = it.y; e0 < it.z; e0 += 4) {
+    uint2 r[4];
+    uint32_t aw[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) r[q] = e0 + q < it.z ? erec[e0 + q] : make_uint2(0, 0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      aw[q] = e0 + q < it.z ? (CG ? __ldcg(active + (r[q].x >> 5)) : active[r[q].x >> 5]) : 0u;
+    uint4 v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const bool a = (aw[q] >> (r[q].x & 31)) & 1u;
+      any |= a;
+      const uint4* row = reinterpret_cast<const uint4*>(slab + (size_t)r[q].x * Kp + lane);
+      v[q] = a && live ? (CG ? __ldcg(row) : *row) : make_uint4(~0u, ~0u, ~0u, ~0u);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t w16 = min(r[q].y, 0xFFFFu), ww = w16 | (w16 << 16);
+      acc.x = __vminu2(acc.x, __vaddus2(v[q].x, ww));
+      acc.y = __vminu2(acc.y, __vaddus2(v[q].y, ww));
+      acc.z = __vminu2(acc.z, __vaddus2(v[q].z, ww));
+      acc.w = __vminu2(acc.w, __vaddus2(v[q].w, ww));
+    }
+  }
+  if (!any) return;  // the row keeps its seed or INF
+  uint32_t* a4 = &acc.x;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    uint32_t lo = a4[q] & 0xFFFFu, hi = a4[q] >> 16;
+    if (2 * q >= (int)valid_lanes || lo > thr[lane + 2 * q]) lo = 0xFFFFu;
+    if (2 * q + 1 >= (int)valid_lanes || hi > thr[lane + 2 * q + 1]) hi = 0xFFFFu;
+    a4[q] = lo | (hi << 16);
+  }
+  if (!live) return;
+  uint32_t* dst = reinterpret_cast<uint32_t*>(slab + (size_t)it.x * Kp + lane);
+  if (it.w) {
+    atomic_min_u16x2(dst + 0, acc.x, err);
+    atomic_min_u16x2(dst + 1, acc.y, err);
+    atomic_min_u16x2(dst + 2, acc.z, err);
+    atomic_min_u16x2(dst + 3, acc.w, err);
+  } else {
+    const bool valid = (seeded[it.x >> 5] >> (it.x & 31)) & 1u;
+    const uint4* d4 = reinterpret_cast<const uint4*>(dst);
+    const uint4 c = valid ? (CG ? __ldcg(d4) : *d4) : make_uint4(~0u, ~0u, ~0u, ~0u);
+    uint4 nv;
+    nv.x = __vminu2(c.x, acc.x);
+    nv.y = __vminu2(c.y, acc.y);
+    nv.z = __vminu2(c.z, acc.z);
+    nv.w = __vminu2(c.w, acc.w);
+    *reinterpret_cast<uint4*>(dst) = nv;
+  }
+  if ((acc.x & acc.y & acc.z & acc.w) != ~0u) atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
+}
+
 // Waves of at most 128 lanes: G = Kp / 8 threads (8 lanes each) per item, so
 // a warp holds 32 / G items. Each thread walks its item's in-edges itself,
 // four at a time (edge records, activity words and rows of four edges in
@@ -207,63 +276,9 @@ __global__ void __launch_bounds__(128, 12)
   const uint32_t valid_lanes = live ? min(8u, kw > lane ? kw - lane : 0u) : 0u;
   const uint32_t groups = gridDim.x * (blockDim.x / G);
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  for (uint32_t ii = i0 + tid / G; ii < i1; ii += groups) {
-    const uint4 it = item[ii];
-    uint4 acc = make_uint4(~0u, ~0u, ~0u, ~0u);
-    bool any = false;
-    for (uint32_t e0 = it.y; e0 < it.z; e0 += 4) {
-      uint2 r[4];
-      uint32_t aw[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) r[q] = e0 + q < it.z ? erec[e0 + q] : make_uint2(0, 0);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) aw[q] = e0 + q < it.z ? active[r[q].x >> 5] : 0u;
-      uint4 v[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const bool a = (aw[q] >> (r[q].x & 31)) & 1u;
-        any |= a;
-        v[q] = a && live ? *reinterpret_cast<const uint4*>(slab + (size_t)r[q].x * Kp + lane)
-                         : make_uint4(~0u, ~0u, ~0u, ~0u);
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const uint32_t w16 = min(r[q].y, 0xFFFFu), ww = w16 | (w16 << 16);
-        acc.x = __vminu2(acc.x, __vaddus2(v[q].x, ww));
-        acc.y = __vminu2(acc.y, __vaddus2(v[q].y, ww));
-        acc.z = __vminu2(acc.z, __vaddus2(v[q].z, ww));
-        acc.w = __vminu2(acc.w, __vaddus2(v[q].w, ww));
-      }
-    }
-    if (!any) continue;  // the row keeps its seed or INF
-    uint32_t* a4 = &acc.x;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      uint32_t lo = a4[q] & 0xFFFFu, hi = a4[q] >> 16;
-      if (2 * q >= (int)valid_lanes || lo > thr[lane + 2 * q]) lo = 0xFFFFu;
-      if (2 * q + 1 >= (int)valid_lanes || hi > thr[lane + 2 * q + 1]) hi = 0xFFFFu;
-      a4[q] = lo | (hi << 16);
-    }
-    if (!live) continue;
-    uint32_t* dst = reinterpret_cast<uint32_t*>(slab + (size_t)it.x * Kp + lane);
-    if (it.w) {
-      atomic_min_u16x2(dst + 0, acc.x, err);
-      atomic_min_u16x2(dst + 1, acc.y, err);
-      atomic_min_u16x2(dst + 2, acc.z, err);
-      atomic_min_u16x2(dst + 3, acc.w, err);
-    } else {
-      const bool valid = (seeded[it.x >> 5] >> (it.x & 31)) & 1u;
-      const uint4 c =
-          valid ? *reinterpret_cast<const uint4*>(dst) : make_uint4(~0u, ~0u, ~0u, ~0u);
-      uint4 nv;
-      nv.x = __vminu2(c.x, acc.x);
-      nv.y = __vminu2(c.y, acc.y);
-      nv.z = __vminu2(c.z, acc.z);
-      nv.w = __vminu2(c.w, acc.w);
-      *reinterpret_cast<uint4*>(dst) = nv;
-    }
-    if ((acc.x & acc.y & acc.z & acc.w) != ~0u) atomicOr(&active[it.x >> 5], 1u << (it.x & 31));
-  }
+  for (uint32_t ii = i0 + tid / G; ii < i1; ii += groups)
+    group16_item<false>(item[ii], erec, slab, Kp, active, thr, lane, live, valid_lanes, seeded,
+                        err);
 }
 
 // A run of consecutive small levels [l0, l1) of the 16-bit gated sweep in one
@@ -311,6 +326,96 @@ __global__ void __launch_bounds__(1024, 1)
       }
     }
     __syncthreads();
+  }
+}
+
+// A whole 16-bit gated wave sweep in one cooperative launch (waves of at most
+// 4096 lanes): the blocks walk the level program, a level's items spread
+// over the grid's item slots or a run of small levels swept by block 0
+// alone, with a grid barrier between segments. G > 0: groups of G = Kp / 8
+// threads per item (group16_item); G = 0: wpi = ceil(Kp / 256) warps per
+// item, a 256-lane slice each (gated16_item). `withhold` is the test hook of
+// the grid barrier (a block that leaves before its first arrival; NONE
+// otherwise). lvl: level -> first item.
+template <uint32_t G>
+__global__ void __launch_bounds__(512, 2)
+    k_iso_persist(const uint2* __restrict__ prog, uint32_t P, const uint32_t* __restrict__ lvl,
+                  const uint4* __restrict__ item, const uint2* __restrict__ erec,
+                  uint16_t* __restrict__ slab, uint32_t Kp, uint32_t* __restrict__ active,
+                  const uint32_t* __restrict__ thr, uint32_t kw,
+                  const uint32_t* __restrict__ seeded, uint32_t* __restrict__ bar,
+                  long long timeout, uint32_t withhold, uint32_t* __restrict__ err) {
+  const uint32_t t = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t lane, slot, slots;  // this thread's lanes, item slot in the block, slots per block
+  bool live, slot_live;
+  if (G) {
+    lane = (threadIdx.x % G) * 8;
+    slot = threadIdx.x / G;
+    slots = blockDim.x / G;
+    slot_live = true;
+  } else {
+    const uint32_t wpi = (Kp + 255) / 256;
+    lane = (warp % wpi) * 256 + t * 8;
+    slot = warp / wpi;
+    slots = (blockDim.x >> 5) / wpi;
+    slot_live = slot < slots && (warp % wpi) * 256 < Kp;
+  }
+  live = slot_live && lane < Kp;
+  const uint32_t valid_lanes = live ? min(8u, kw > lane ? kw - lane : 0u) : 0u;
+  // The first item of this slot in the next level is loaded before the
+  // barrier (or __syncthreads) that precedes that level: the schedule does
+  // not depend on the sweep's values, so only the activity and row loads
+  // remain after the wait.
+  uint32_t pre_ii = NONE;
+  uint4 pre_it = make_uint4(0, 0, 0, 0);
+  for (uint32_t s = 0; s < P; ++s) {
+    const uint2 sg = prog[s];
+    const bool run = (sg.y & PROG_RUN) != 0;
+    const uint32_t l0 = sg.x, l1 = run ? (blockIdx.x == 0 ? sg.y & ~PROG_RUN : l0) : l0 + 1;
+    // a run is swept by block 0 level by level; a grid segment by every block
+    const uint32_t first = run ? slot : blockIdx.x * slots + slot;
+    const uint32_t stride = run ? slots : gridDim.x * slots;
+    for (uint32_t l = l0; l < l1; ++l) {
+      const uint32_t i1 = lvl[l + 1];
+      if (slot_live)
+        for (uint32_t ii = lvl[l] + first; ii < i1; ii += stride) {
+          const uint4 it = ii == pre_ii ? pre_it : item[ii];
+          if (G) {
+            group16_item<true>(it, erec, slab, Kp, active, thr, lane, live, valid_lanes, seeded,
+                               err);
+          } else {
+            const uint2 r0 = it.y + t < it.z ? erec[it.y + t] : make_uint2(0, 0);
+            gated16_item<true>(it, r0, erec, slab, Kp, active, thr, lane, live, valid_lanes,
+                               seeded, err);
+          }
+        }
+      if (run) {
+        pre_ii = NONE;
+        if (slot_live && l + 1 < l1) {
+          const uint32_t nx = lvl[l + 1] + first;
+          if (nx < lvl[l + 2]) {
+            pre_ii = nx;
+            pre_it = item[nx];
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (s + 1 == P) break;
+    pre_ii = NONE;
+    {  // this slot's first item of the next segment
+      const uint2 nsg = prog[s + 1];
+      const bool nrun = (nsg.y & PROG_RUN) != 0;
+      if (slot_live && (!nrun || blockIdx.x == 0)) {
+        const uint32_t nx = lvl[nsg.x] + (nrun ? slot : blockIdx.x * slots + slot);
+        if (nx < lvl[nsg.x + 1]) {
+          pre_ii = nx;
+          pre_it = item[nx];
+        }
+      }
+    }
+    if (blockIdx.x == withhold) return;
+    if (!grid_barrier(bar, s, timeout, err)) return;
   }
 }
 
@@ -576,6 +681,51 @@ bf_status emit_settled(const T* slab, uint32_t Kp, Graph* g, Sched& sc, const ui
   return BF_OK;
 }
 
+constexpr unsigned ISO_PERSIST_TPB = 512;
+
+// One persistent launch of k_iso_persist for a wave of Kp <= 4096 lanes; the
+// level program (runs of levels with at most two rounds of block 0's item
+// slots) is cached per context and lane width.
+bf_status iso_sweep_persistent(Graph* g, Ctx& c, Sched& sc, uint16_t* slab16, uint32_t Kp,
+                               uint32_t* d_active, const uint32_t* d_thr, uint32_t kw,
+                               const uint32_t* d_seeded, cudaStream_t st) {
+  const uint32_t G = Kp <= 8 ? 1 : Kp <= 16 ? 2 : Kp <= 32 ? 4 : Kp <= 64 ? 8 : Kp <= 128 ? 16 : 0;
+  const uint32_t slots = G ? ISO_PERSIST_TPB / G : (ISO_PERSIST_TPB / 32) / ((Kp + 255) / 256);
+  bf_status s;
+  if ((s = ensure_barrier(g))) return s;
+  if (c.iso_prog_slots != slots || c.iso_prog_levels != sc.lvl_item.size()) {
+    c.iso_prog = level_program(sc.lvl_item, g->n_levels, 2 * slots);
+    const size_t bytes = std::max<size_t>(c.iso_prog.size(), 1) * sizeof(uint2);
+    if (bytes > c.iso_prog_bytes) {
+      if (c.d_iso_prog) {
+        cudaFree(c.d_iso_prog);
+        g->device_bytes -= c.iso_prog_bytes;
+      }
+      c.d_iso_prog = nullptr;
+      c.iso_prog_bytes = 0;
+      BF_CUDA(cudaMalloc(&c.d_iso_prog, bytes));
+      c.iso_prog_bytes = bytes;
+      g->device_bytes += bytes;
+    }
+    BF_CUDA(cudaMemcpyAsync(c.d_iso_prog, c.iso_prog.data(), c.iso_prog.size() * sizeof(uint2),
+                            cudaMemcpyHostToDevice, st));
+    c.iso_prog_slots = slots;
+    c.iso_prog_levels = sc.lvl_item.size();
+  }
+  auto kern = G == 1 ? k_iso_persist<1> : G == 2 ? k_iso_persist<2> : G == 4 ? k_iso_persist<4>
+            : G == 8 ? k_iso_persist<8> : G == 16 ? k_iso_persist<16> : k_iso_persist<0>;
+  const bool hook = test_withhold_arrival();
+  const unsigned blocks = persistent_blocks(g, (const void*)kern, ISO_PERSIST_TPB, 2 * g->sm_count);
+  uint32_t* bar = g->d_bar + 2;  // the plain engine's sweep uses words 0-1
+  BF_CUDA(cudaMemsetAsync(bar, 0, 8, st));
+  BF_CUDA(launch_persistent(kern, blocks, ISO_PERSIST_TPB, st, (const uint2*)c.d_iso_prog,
+                            (uint32_t)c.iso_prog.size(), (const uint32_t*)sc.d_lvl,
+                            (const uint4*)sc.d_item, (const uint2*)sc.d_erec, slab16, Kp, d_active,
+                            d_thr, kw, d_seeded, bar, hook ? 2000000ll : BARRIER_TIMEOUT_CYCLES,
+                            hook ? 1u : NONE, g->d_err));
+  return BF_OK;
+}
+
 }  // namespace
 
 // d_bits: n rows of ceil(n_nodes / 64) u64 words; d_counts: n u64.
@@ -671,7 +821,12 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
       return s;
     ++launches;
     if (stats) BF_CUDA(cudaEventRecord(c.ev[1], st));
-    if (half) {
+    if (half && (g->tune.persist & 2u) && Kp <= 4096) {
+      if ((s = iso_sweep_persistent(g, c, sc, slab16, Kp, d_active, p_thr + s0, (uint32_t)kw,
+                                    d_seeded, st)))
+        return s;
+      ++launches;
+    } else if (half) {
       const bool pdl = g->tune.pdl != 0;
       // runs of consecutive levels of at most two rounds of one block's items
       // go to k_sweep_run16 (one launch per run)

@@ -255,6 +255,9 @@ void worker(Server* sv, int si) {
     }
     bf_status rc = kind == BF_REQ_MATRIX ? run_matrix_batch(sv, sl, batch)
                                          : run_iso_batch(sv, sl, batch);
+    // a device-side error of the batch (a grid barrier that ran out, an
+    // inconsistent id) fails its requests
+    if (rc == BF_OK) rc = check_device_error(sv->g, sl.stream);
     if (rc != BF_OK && rc != BF_ERR_TIMEOUT) cudaStreamSynchronize(sl.stream);
     if (rc == BF_ERR_TIMEOUT) {
       // the jobs complete with TIMEOUT now; the slot is reused only after its

@@ -188,6 +188,12 @@ typedef struct bf_tune {
                                   (evict-last cache hints; 0 = no hints)         */
   uint32_t device_schedule;    /* 1: target-restricted schedules are built on
                                   the device; 0: by host threads (same rows)    */
+  uint32_t persistent_sweep;   /* bit 0 (default): the plain engine's sweep of a
+                                  K = 32 batch, bit 1: each 16-bit isochrone
+                                  wave's sweep, runs as one cooperative launch
+                                  walking all levels (grid barriers with a
+                                  deadline: BF_ERR_TIMEOUT if one runs out);
+                                  clear: one launch per level                    */
 } bf_tune;
 
 /* Time candidate tunables on a sample matrix (device buffers: d_sources,

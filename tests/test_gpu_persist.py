@@ -1,0 +1,88 @@
+"""Persistent sweeps (one cooperative launch walking every level, grid
+barriers between levels) against the per-level launches and the oracle
+(tolerance 0: u32 min-plus), and the grid barrier's deadline.
+
+The deadline is tested without faulting anything: the test hook
+BF_TEST_WITHHOLD_ARRIVAL makes the persistent sweep run on two blocks of
+which block 1 leaves before its first barrier arrival; block 0's wait runs
+out after about a millisecond, it sets the error flag and returns, and the
+call reports BF_ERR_TIMEOUT. The next call without the hook must be exact."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+INF = 0xFFFFFFFF
+
+
+@pytest.mark.parametrize("which", ["grid100", "country_small"])
+def test_plain_persistent_matches_levels(built, grid100, country_small, which):
+    import bfphast
+    _, cch = grid100 if which == "grid100" else country_small
+    n = cch["n"]
+    c = orc.Cch.from_dict(cch)
+    g = bfphast.Graph.from_cch(cch)
+    g.set_engine(bfphast.ENGINE_PLAIN)
+    rng = np.random.default_rng(4)
+    src = rng.choice(n, 70, replace=False).astype(np.uint32)  # three K = 32 batches
+    tgt = rng.choice(n, 500, replace=False).astype(np.uint32)
+    want, _ = c.matrix(src, tgt)
+    for persist in (1, 0):
+        g.set_tune(persistent_sweep=persist)
+        got, st = g.matrix(src, tgt, stats=True)
+        assert np.array_equal(got, want), persist
+        if persist:  # one sweep launch per batch (+ upward and extraction)
+            assert st["kernel_launches"] == 3 * 3 + 1  # + target positions
+        for thr in (0, 2000):
+            m = g.matrix(src, tgt, threshold=thr)
+            assert np.array_equal(m, np.where(want <= thr, want, INF)), (persist, thr)
+
+
+@pytest.mark.parametrize("lanes", [8, 64, 128, 256, 1024])
+def test_isochrone_persistent_matches_oracle(built, country_small, lanes):
+    import bfphast
+    import workload
+    _, cch = country_small
+    c = orc.Cch.from_dict(cch)
+    g = bfphast.Graph.from_cch(cch)
+    origins, thr = workload.isochrone_workload(cch["n"], min(lanes, 96) + 5, seed=lanes)
+    want_bits, want_counts = c.isochrone_bitsets(origins, thr)
+    for persist in (3, 1):  # bit 1: isochrone waves in one persistent launch
+        g.set_tune(isochrone_lanes=lanes if lanes >= 32 else 32, persistent_sweep=persist)
+        bits, counts = g.isochrone_bitsets(origins, thr)
+        assert np.array_equal(bits, want_bits), persist
+        assert np.array_equal(counts, want_counts), persist
+
+
+def test_barrier_deadline_reports_timeout(built, grid100):
+    import bfphast
+    _, cch = grid100
+    n = cch["n"]
+    c = orc.Cch.from_dict(cch)
+    g = bfphast.Graph.from_cch(cch)
+    src = np.array([3, 1000, 30000], dtype=np.uint32)
+    tgt = np.arange(0, n, 7, dtype=np.uint32)
+    # 200 origins in one 256-lane wave: item slots of one warp, so the
+    # grid100 levels above 32 items are grid segments with barriers
+    origins = np.arange(0, n, n // 200, dtype=np.uint32)[:200]
+    thr = np.full(200, 3000, dtype=np.uint32)
+    g.set_tune(isochrone_lanes=256, persistent_sweep=3)
+    g.set_engine(bfphast.ENGINE_PLAIN)
+    os.environ["BF_TEST_WITHHOLD_ARRIVAL"] = "1"
+    try:
+        with pytest.raises(bfphast.BfError) as e:
+            g.matrix(src, tgt)
+        assert e.value.status == bfphast.BF_ERR_TIMEOUT
+        with pytest.raises(bfphast.BfError) as e:
+            g.isochrone_bitsets(origins, thr)
+        assert e.value.status == bfphast.BF_ERR_TIMEOUT
+    finally:
+        del os.environ["BF_TEST_WITHHOLD_ARRIVAL"]
+    want, _ = c.matrix(src, tgt)
+    assert np.array_equal(g.matrix(src, tgt), want)
+    bits, _ = g.isochrone_bitsets(origins, thr)
+    wb, _ = c.isochrone_bitsets(origins, thr)
+    assert np.array_equal(bits, wb)
