@@ -102,6 +102,11 @@ class ClockSampler:
                  "--format=csv,noheader,nounits", "-lms", "200"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
+            # nvidia-smi's start-up holds driver locks that stall CUDA calls:
+            # let it deliver its first sample before the timed region opens
+            t0 = time.perf_counter()
+            while not self.rows and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.01)
         except OSError:
             self._proc = None
         return self
@@ -492,6 +497,7 @@ def run_isochrones(g, cch, count, seed=42):
     launches = 0
     counts = np.zeros(count, dtype=np.uint64)
     last = None
+    sweep_bytes, sweep_ms, waves, lanes = 0, 0.0, 0, 0
     e0.record(stream)
     for c0 in range(0, count, chunk):
         m = min(chunk, count - c0)
@@ -499,6 +505,10 @@ def run_isochrones(g, cch, count, seed=42):
                                         d_b.data_ptr(), d_c.data_ptr(),
                                         stream=stream.cuda_stream)
         launches += st["kernel_launches"]
+        sweep_bytes += st["sweep_bytes"]
+        sweep_ms += st["downward_ms"]
+        waves += st["waves"]
+        lanes = max(lanes, st["lanes"])
         counts[c0:c0 + m] = d_c[:m].cpu().numpy().view(np.uint64)
         last = (c0, m)
     e1.record(stream)
@@ -507,21 +517,52 @@ def run_isochrones(g, cch, count, seed=42):
     # bit-exact sample from the last chunk + CPU oracle rate on the host cores
     c = orc.Cch.from_dict(cch)
     c0, m = last
-    pick = np.linspace(c0, c0 + m - 1, 32).astype(np.int64)
+    pick = np.linspace(c0, c0 + m - 1, min(m, 1024)).astype(np.int64)
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     wb, wc = c.isochrone_bitsets(o[pick], t[pick], threads=threads)
     cpu_s = time.perf_counter() - t0
     got = d_b.view(chunk, w64)[torch.from_numpy(pick - c0)].cpu().numpy().view(np.uint64)
     exact = bool(np.array_equal(got, wb)) and bool(np.array_equal(counts[pick], wc))
+    peak, peak_kind = measured_peak()
+    achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9 if sweep_ms else 0.0
     return {"origins": count, "value": round(count / sec, 1), "unit": "isochrones/s",
             "seconds": round(sec, 3), "gpu_launches": int(launches),
             "mean_reachable_nodes": round(float(counts.mean()), 1),
             "thresholds_s": list(workload.ISO_THRESHOLDS_S),
+            "waves": int(waves), "lanes_per_wave": int(lanes),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                         "peak_kind": peak_kind, "kernel": "k_sweep_gated16 (all waves)",
+                         "alg_bytes": int(sweep_bytes), "sweep_ms": round(sweep_ms, 3),
+                         "bytes_rule": "per wave: 16 B per work item + 8 B per edge record "
+                                       "scanned, 2 B x lanes per active source row gathered "
+                                       "and per row written"},
+            "e2e": run_isochrones_e2e(g, o, t, w64, min(count, 2048)),
             "bit_exact_sample": {"origins": len(pick), "equal": exact},
             "cpu_baseline": {"value": round(len(pick) / cpu_s, 2), "unit": "isochrones/s",
                              "cores": threads, "kind": "port",
                              "sample": "%d origins of the last chunk, %.1f s" % (len(pick), cpu_s)}}
+
+
+def run_isochrones_e2e(g, o, t, w64, m):
+    """bf_isochrone_bitsets with page-locked host buffers on the first m
+    origins of the workload: origins and thresholds in, every bitset row
+    (ceil(n / 64) words per origin) and count out, inside the timed call."""
+    import numpy as np
+    import torch
+    pin = lambda k, dt: torch.empty(k, dtype=dt, pin_memory=True).numpy()
+    h_o, h_t = pin(m, torch.int32).view(np.uint32), pin(m, torch.int32).view(np.uint32)
+    h_o[:], h_t[:] = o[:m], t[:m]
+    bits = pin(m * w64, torch.int64).view(np.uint64).reshape(m, w64)
+    counts = pin(m, torch.int64).view(np.uint64)
+    g.isochrone_bitsets(h_o, h_t, out=(bits, counts))
+    t0 = time.perf_counter()
+    g.isochrone_bitsets(h_o, h_t, out=(bits, counts))
+    sec = time.perf_counter() - t0
+    return {"value": round(m / sec, 1), "unit": "isochrones/s", "origins": m,
+            "ms": round(sec * 1e3, 2), "h2d_bytes_per_step": 8 * m,
+            "d2h_bytes_per_step": 8 * m * (w64 + 1)}
 
 
 def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):

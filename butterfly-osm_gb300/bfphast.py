@@ -63,7 +63,8 @@ class Stats(ctypes.Structure):
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("swept_nodes", ctypes.c_uint64), ("swept_edges", ctypes.c_uint64),
                 ("lanes", ctypes.c_uint64), ("waves", ctypes.c_uint64),
-                ("schedule_ms", ctypes.c_double)]
+                ("schedule_ms", ctypes.c_double), ("sweep_bytes", ctypes.c_uint64),
+                ("active_rows", ctypes.c_uint64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -102,7 +103,7 @@ ROUTE_AUTO, ROUTE_BUCKET, ROUTE_PHAST = 0, 1, 2
 class ServerCfg(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
                 ("max_queue", ctypes.c_uint32), ("timeout_ms", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("slots", ctypes.c_uint32)]
 
 
 class Request(ctypes.Structure):
@@ -499,11 +500,17 @@ class Graph:
         out = [(ranks[off[i]:off[i + 1]], dists[off[i]:off[i + 1]]) for i in range(len(o))]
         return (out, st.as_dict()) if stats else out
 
-    def isochrone_bitsets(self, origins, thresholds, stats=False):
+    def isochrone_bitsets(self, origins, thresholds, stats=False, out=None):
+        """out: optional (bits, counts) arrays to fill (e.g. page-locked)."""
         o, t = _u32(origins), _u32(thresholds)
         words = (self.n + 63) // 64
-        bits = np.empty((len(o), words), dtype=np.uint64)
-        counts = np.empty(len(o), dtype=np.uint64)
+        if out is None:
+            bits = np.empty((len(o), words), dtype=np.uint64)
+            counts = np.empty(len(o), dtype=np.uint64)
+        else:
+            bits, counts = out
+            assert bits.shape == (len(o), words) and bits.dtype == np.uint64
+            assert counts.shape == (len(o),) and counts.dtype == np.uint64
         st = Stats()
         _check(load().bf_isochrone_bitsets(self._h, _ptr(o), _ptr(t), len(o), _ptr(bits, _u64p),
                                            _ptr(counts, _u64p), ctypes.byref(st)))
@@ -522,9 +529,9 @@ class Server:
     """Continuous-batching serving loop (bf_server_*). Output buffers of
     submitted requests are kept alive here until their completion is polled."""
 
-    def __init__(self, graph, hbm_budget=0, max_inflight=0, max_queue=0, timeout_ms=0):
+    def __init__(self, graph, hbm_budget=0, max_inflight=0, max_queue=0, timeout_ms=0, slots=0):
         self.graph = graph
-        cfg = ServerCfg(hbm_budget, max_inflight, max_queue, timeout_ms, 0)
+        cfg = ServerCfg(hbm_budget, max_inflight, max_queue, timeout_ms, slots)
         h = ctypes.c_void_p()
         _check(load().bf_server_create(graph.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h

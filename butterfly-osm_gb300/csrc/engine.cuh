@@ -230,6 +230,8 @@ struct Ctx {
   size_t iso_prog_bytes = 0;
   uint32_t iso_prog_slots = 0;
   size_t iso_prog_levels = 0;
+  uint64_t* d_count = nullptr;     // [2] algorithmic-byte and row counters of isochrone sweeps
+  Sched* shared_full = nullptr;    // a full-graph schedule owned elsewhere (serving slots)
 };
 
 // Tunables of the batched sweep (chosen by bf_autotune).

@@ -651,6 +651,7 @@ void free_ctx(Ctx& c) {
   if (c.d_cseed) cudaFree(c.d_cseed);
   if (c.d_one) cudaFree(c.d_one);
   if (c.d_iso_prog) cudaFree(c.d_iso_prog);
+  if (c.d_count) cudaFree(c.d_count);
   if (c.h_stage) cudaFreeHost(c.h_stage);
   free_sched_scratch(c.sd);
   for (auto& e : c.ev)

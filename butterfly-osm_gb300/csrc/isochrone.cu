@@ -180,10 +180,21 @@ __global__ void __launch_bounds__(128, IPB > 1 ? 12 : 16)
   const uint32_t valid_lanes = live ? min(8u, kw > lane ? kw - lane : 0u) : 0u;
   const uint32_t first = ipb > 1 ? blockIdx.x * ipb + (threadIdx.x >> 5) : blockIdx.x;
   const uint32_t stride = gridDim.x * ipb;
+  // the first item and its edge records do not depend on the previous
+  // level: load them while that level drains
+  uint4 it = make_uint4(0, 0, 0, 0);
+  uint2 r0 = make_uint2(0, 0);
+  uint32_t ii = i0 + first;
+  if (ii < i1) {
+    it = item[ii];
+    r0 = it.y + t < it.z ? erec[it.y + t] : make_uint2(0, 0);
+  }
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  for (uint32_t ii = i0 + first; ii < i1; ii += stride) {
-    const uint4 it = item[ii];
-    const uint2 r0 = it.y + t < it.z ? erec[it.y + t] : make_uint2(0, 0);
+  for (; ii < i1; ii += stride) {
+    if (ii != i0 + first) {
+      it = item[ii];
+      r0 = it.y + t < it.z ? erec[it.y + t] : make_uint2(0, 0);
+    }
     gated16_item<false>(it, r0, erec, slab, Kp, active, thr, lane, live, valid_lanes, seeded, err);
   }
 }
@@ -275,10 +286,18 @@ __global__ void __launch_bounds__(128, 12)
   const bool live = lane < Kp;
   const uint32_t valid_lanes = live ? min(8u, kw > lane ? kw - lane : 0u) : 0u;
   const uint32_t groups = gridDim.x * (blockDim.x / G);
+  // the first item record does not depend on the previous level: load it,
+  // and bring its edge records towards L2, while that level drains
+  const uint32_t f = i0 + tid / G;
+  uint4 it0 = make_uint4(0, 0, 0, 0);
+  if (f < i1) {
+    it0 = item[f];
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(erec + it0.y));
+  }
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  for (uint32_t ii = i0 + tid / G; ii < i1; ii += groups)
-    group16_item<false>(item[ii], erec, slab, Kp, active, thr, lane, live, valid_lanes, seeded,
-                        err);
+  for (uint32_t ii = f; ii < i1; ii += groups)
+    group16_item<false>(ii == f ? it0 : item[ii], erec, slab, Kp, active, thr, lane, live,
+                        valid_lanes, seeded, err);
 }
 
 // A run of consecutive small levels [l0, l1) of the 16-bit gated sweep in one
@@ -349,9 +368,10 @@ __global__ void __launch_bounds__(512, 2)
   uint32_t lane, slot, slots;  // this thread's lanes, item slot in the block, slots per block
   bool live, slot_live;
   if (G) {
-    lane = (threadIdx.x % G) * 8;
-    slot = threadIdx.x / G;
-    slots = blockDim.x / G;
+    constexpr uint32_t g1 = G ? G : 1;  // (G = 0 never takes this branch)
+    lane = (threadIdx.x % g1) * 8;
+    slot = threadIdx.x / g1;
+    slots = blockDim.x / g1;
     slot_live = true;
   } else {
     const uint32_t wpi = (Kp + 255) / 256;
@@ -681,6 +701,38 @@ bf_status emit_settled(const T* slab, uint32_t Kp, Graph* g, Sched& sc, const ui
   return BF_OK;
 }
 
+// Algorithmic bytes of one gated wave sweep, counted after it from its final
+// activity bitmap: an item is processed when one of its in-edge source rows
+// is active; it then gathers each active source row and writes its row
+// (row_bytes each). Block sums go to counts[0] (bytes) and counts[1] (rows).
+__global__ void __launch_bounds__(256)
+    k_iso_count(const uint4* __restrict__ item, uint64_t n_items, const uint2* __restrict__ erec,
+                const uint32_t* __restrict__ active, uint32_t row_bytes,
+                unsigned long long* __restrict__ counts) {
+  uint64_t bytes = 0, rows = 0;
+  for (uint64_t ii = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; ii < n_items;
+       ii += (uint64_t)gridDim.x * blockDim.x) {
+    const uint4 it = item[ii];
+    uint32_t a = 0;
+    for (uint32_t e = it.y; e < it.z; ++e) {
+      const uint32_t r = erec[e].x;
+      a += (active[r >> 5] >> (r & 31)) & 1u;
+    }
+    if (a) {
+      bytes += (uint64_t)(a + 1) * row_bytes;
+      ++rows;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    bytes += __shfl_down_sync(0xFFFFFFFFu, bytes, o);
+    rows += __shfl_down_sync(0xFFFFFFFFu, rows, o);
+  }
+  if ((threadIdx.x & 31) == 0 && bytes) {
+    atomicAdd(&counts[0], (unsigned long long)bytes);
+    atomicAdd(&counts[1], (unsigned long long)rows);
+  }
+}
+
 constexpr unsigned ISO_PERSIST_TPB = 512;
 
 // One persistent launch of k_iso_persist for a wave of Kp <= 4096 lanes; the
@@ -736,8 +788,8 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
                             uint64_t* d_bits, uint64_t* d_counts, cudaStream_t st,
                             bf_stats* stats, SettledSink* sink) {
   bf_status s;
-  if ((s = build_schedule(g, c, c.full, nullptr, 0, true, st))) return s;
-  Sched& sc = c.full;
+  if (!c.shared_full && (s = build_schedule(g, c, c.full, nullptr, 0, true, st))) return s;
+  Sched& sc = c.shared_full ? *c.shared_full : c.full;
   const uint64_t rows = g->n;
   const uint64_t w64 = (g->n + 63) / 64;
   const uint64_t aw = (rows + 31) / 32;  // active-bitmap words
@@ -807,6 +859,13 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
   uint16_t* slab16 = reinterpret_cast<uint16_t*>(c.d_slab);
   uint64_t launches = 0;
   float t_up = 0, t_dn = 0, t_ex = 0;
+  if (stats) {  // algorithmic-byte counters of the sweeps (k_iso_count)
+    if (!c.d_count) {
+      BF_CUDA(cudaMalloc(&c.d_count, 16));
+      g->device_bytes += 16;
+    }
+    BF_CUDA(cudaMemsetAsync(c.d_count, 0, 16, st));
+  }
   for (uint64_t s0 = 0; s0 < n; s0 += wave) {
     const uint64_t kw = std::min<uint64_t>(wave, n - s0);
     if (stats) BF_CUDA(cudaEventRecord(c.ev[0], st));
@@ -907,6 +966,11 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
     }
     if (stats) {
       BF_CUDA(cudaEventRecord(c.ev[3], st));
+      // outside the timed phases: count the wave's algorithmic sweep bytes
+      k_iso_count<<<(unsigned)std::min<uint64_t>((sc.n_items + 255) / 256, 152 * 8), 256, 0, st>>>(
+          (const uint4*)sc.d_item, sc.n_items, (const uint2*)sc.d_erec, d_active, Kp * lb,
+          reinterpret_cast<unsigned long long*>(c.d_count));
+      BF_CUDA(cudaGetLastError());
       BF_CUDA(cudaEventSynchronize(c.ev[3]));
       float ea, eb, ec;
       BF_CUDA(cudaEventElapsedTime(&ea, c.ev[0], c.ev[1]));
@@ -929,6 +993,12 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
     stats->swept_nodes = sc.n_r;
     stats->swept_edges = sc.n_edges;
     stats->lanes = Kp;
+    uint64_t cnt[2] = {0, 0};
+    BF_CUDA(cudaMemcpyAsync(cnt, c.d_count, 16, cudaMemcpyDeviceToHost, st));
+    BF_CUDA(cudaStreamSynchronize(st));
+    // + every wave scans the schedule: 16 B per item and 8 B per edge record
+    stats->sweep_bytes += cnt[0] + waves * (16 * sc.n_items + 8 * sc.n_edges);
+    stats->active_rows += cnt[1];
   }
   return BF_OK;
 }

@@ -4,12 +4,14 @@
 // run one engine call per request on a CPU pool (do_matrix with 1000-source
 // tiles, route/src/server/flight.rs:589,957-1110; isochrone_bulk_handler,
 // route/src/server/isochrone_handler.rs:1535-1750). Here requests are queued
-// and two worker slots, each with its own stream, distance slab and
-// schedule (a Ctx), form batches continuously: whenever a slot is free it
-// takes the waiting requests of one kind (in arrival order, up to the slot's
-// lane budget and max_inflight), so requests that arrive while the other slot
-// computes are admitted as soon as that slot frees, and the two slots' work
-// overlaps on the device.
+// and worker slots (four by default), each with its own stream, distance
+// slab and schedule (a Ctx), form batches continuously: whenever a slot is
+// free it takes the waiting requests of one kind (in arrival order, up to the
+// slot's lane cap and max_inflight, and while their device I/O fits the
+// budget and the device's free memory), so requests that arrive while other
+// slots compute are admitted as soon as a slot frees, and the slots' work
+// overlaps on the device: a sweep is a chain of ~1100 dependent levels, most
+// of them far too small to fill the GPU, so concurrent sweeps share it.
 //
 //   matrix batch     the sources of all admitted requests are the lanes of
 //                    one sweep restricted to the union of their targets; each
@@ -47,7 +49,13 @@ struct Job {
   std::vector<uint32_t> src, tgt;  // copies of the request's ids
   double submit_s = 0, admit_s = 0;
   bool cancelled = false;
+  uint64_t io_bytes = 0;           // device I/O of the request in a batch
 };
+
+constexpr int MAX_SLOTS = 8;
+// free device memory a batch leaves untouched (other users of the device,
+// schedule growth, the slab's own reallocation)
+constexpr uint64_t FREE_MARGIN = 1ull << 30;
 
 struct Slot {
   Ctx ctx;
@@ -55,6 +63,9 @@ struct Slot {
   cudaEvent_t done = nullptr;
   uint8_t* d_buf = nullptr;  // per-batch device I/O
   size_t buf_bytes = 0;
+  double batch_start_s = 0;  // host clock when the current batch began
+  void* h_stage = nullptr;   // page-locked staging of results bound for pageable buffers
+  size_t stage_bytes = 0;
   std::thread th;
 };
 
@@ -70,7 +81,12 @@ struct Server {
   std::vector<bf_completion> done;
   uint64_t next_ticket = 1;
   bool stop = false;
-  Slot slot[2];
+  int n_slots = 4;
+  Ctx shared;                   // holds the full-graph schedule every slot sweeps
+  uint64_t budget = 0;          // device bytes for request I/O and slabs
+  uint64_t io_budget = 0;       // the part of it request I/O may take
+  uint64_t admitted_io = 0;     // I/O bytes of the batches in flight
+  Slot slot[MAX_SLOTS];
 };
 
 namespace {
@@ -93,10 +109,11 @@ bf_status grow(Graph* g, Slot& sl, size_t need) {
   return BF_OK;
 }
 
-// Wait for the slot's stream with a deadline (no unbounded device wait).
+// Wait for the slot's stream with a deadline: the batch's device work may
+// take timeout_ms from the batch's start (no unbounded device wait).
 bf_status wait_slot(Slot& sl, uint32_t timeout_ms) {
   BF_CUDA(cudaEventRecord(sl.done, sl.stream));
-  const double deadline = wall_s() + timeout_ms * 1e-3;
+  const double deadline = sl.batch_start_s + timeout_ms * 1e-3;
   for (;;) {
     cudaError_t e = cudaEventQuery(sl.done);
     if (e == cudaSuccess) return BF_OK;
@@ -192,13 +209,44 @@ bf_status run_matrix_batch(Server* sv, Slot& sl, std::vector<Job*>& jobs) {
     }
     BF_CUDA(cudaGetLastError());
   }
+  // Results go straight into page-locked caller buffers; pageable ones are
+  // staged in the slot's page-locked buffer and copied on the host after the
+  // bounded wait (a copy into pageable memory would block this thread until
+  // the device finished, defeating the bound, and nothing may write a
+  // caller's buffer after its request completed with BF_ERR_TIMEOUT).
+  std::vector<std::pair<size_t, uint64_t>> staged;  // (job, offset in the staging buffer)
+  uint64_t stage_need = 0;
   for (size_t i = 0; i < jobs.size(); ++i) {
     const uint64_t cells = jobs[i]->src.size() * jobs[i]->tgt.size();
-    if (cells)
+    if (!cells) continue;
+    cudaPointerAttributes pa{};
+    const bool pinned = cudaPointerGetAttributes(&pa, jobs[i]->r.out) == cudaSuccess &&
+                        pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    if (pinned) {
       BF_CUDA(cudaMemcpyAsync(jobs[i]->r.out, d_out + o_off[i], cells * 4, cudaMemcpyDeviceToHost,
                               st));
+    } else {
+      staged.emplace_back(i, stage_need);
+      stage_need += cells * 4;
+    }
   }
-  return wait_slot(sl, sv->cfg.timeout_ms);
+  if (stage_need > sl.stage_bytes) {
+    if (sl.h_stage) cudaFreeHost(sl.h_stage);
+    sl.h_stage = nullptr;
+    sl.stage_bytes = 0;
+    BF_CUDA(cudaHostAlloc(&sl.h_stage, stage_need, cudaHostAllocDefault));
+    sl.stage_bytes = stage_need;
+  }
+  for (auto& [i, off] : staged)
+    BF_CUDA(cudaMemcpyAsync(static_cast<uint8_t*>(sl.h_stage) + off, d_out + o_off[i],
+                            jobs[i]->src.size() * jobs[i]->tgt.size() * 4, cudaMemcpyDeviceToHost,
+                            st));
+  if ((s = wait_slot(sl, sv->cfg.timeout_ms))) return s;
+  for (auto& [i, off] : staged)
+    std::memcpy(jobs[i]->r.out, static_cast<uint8_t*>(sl.h_stage) + off,
+                jobs[i]->src.size() * jobs[i]->tgt.size() * 4);
+  return BF_OK;
 }
 
 bf_status run_iso_batch(Server* sv, Slot& sl, std::vector<Job*>& jobs) {
@@ -224,19 +272,42 @@ bf_status run_iso_batch(Server* sv, Slot& sl, std::vector<Job*>& jobs) {
   return wait_slot(sl, sv->cfg.timeout_ms);
 }
 
+// Device bytes a slot's batch of these requests needs for its I/O buffers
+// (the d_buf layout of run_matrix_batch / run_iso_batch).
+uint64_t io_bytes_of(const Job* j, uint64_t n) {
+  if (j->r.kind == BF_REQ_ISOCHRONE) return 16 + 8 + ((n + 63) / 64) * 8;
+  return (j->src.size() + 2 * j->tgt.size() + j->src.size() * j->tgt.size()) * 4;
+}
+
 void worker(Server* sv, int si) {
   Slot& sl = sv->slot[si];
   cudaSetDevice(sv->g->device);
-  const uint64_t lane_cap[3] = {0, 16384, 4096};
+  // lanes per batch: a matrix batch sweeps the union of its requests'
+  // targets for all their sources, so its work grows with (sources) x (rows
+  // reaching the union); the cap keeps batching from outgrowing what it saves
+  // (one sweep's fixed cost of ~1100 dependent levels per batch)
+  const uint64_t lane_cap[3] = {0, 4096, 4096};
   for (;;) {
     std::vector<Job*> batch;
     uint32_t kind = 0;
+    uint64_t io = 0;
     {
       std::unique_lock<std::mutex> lk(sv->mu);
       sv->cv_work.wait(lk, [&] { return sv->stop || !sv->queue.empty(); });
       if (sv->stop) return;
       kind = sv->queue.front()->r.kind;
       uint64_t lanes = 0;
+      // admission: the batch's I/O must fit what the budget leaves beside the
+      // batches in flight and, with a margin, the device's free memory now
+      size_t fr = 0, tot = 0;
+      if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        fr = 0;
+      }
+      const uint64_t room_budget =
+          sv->io_budget > sv->admitted_io ? sv->io_budget - sv->admitted_io : 0;
+      const uint64_t room_free = fr > FREE_MARGIN ? fr - FREE_MARGIN : 0;
+      const uint64_t room = std::min(room_budget, room_free + sl.buf_bytes);
       const double now = wall_s();
       for (auto it = sv->queue.begin(); it != sv->queue.end() && batch.size() < sv->cfg.max_inflight;) {
         Job* j = *it;
@@ -246,13 +317,23 @@ void worker(Server* sv, int si) {
         }
         const uint64_t add = kind == BF_REQ_MATRIX ? j->src.size() : 1;
         if (!batch.empty() && lanes + add > lane_cap[kind]) break;
+        if (io + j->io_bytes > room) break;  // waits for memory (arrival order kept)
         batch.push_back(j);
         lanes += add;
+        io += j->io_bytes;
         it = sv->queue.erase(it);
         j->admit_s = now;
         sv->inflight[j->ticket] = j;
       }
+      if (batch.empty()) {
+        // nothing fits now: wait for a batch in flight to complete and free
+        // memory (or, if none is in flight, for the device's memory to free)
+        sv->cv_work.wait_for(lk, std::chrono::milliseconds(2));
+        continue;
+      }
+      sv->admitted_io += io;
     }
+    sl.batch_start_s = wall_s();
     bf_status rc = kind == BF_REQ_MATRIX ? run_matrix_batch(sv, sl, batch)
                                          : run_iso_batch(sv, sl, batch);
     // a device-side error of the batch (a grid barrier that ran out, an
@@ -260,13 +341,19 @@ void worker(Server* sv, int si) {
     if (rc == BF_OK) rc = check_device_error(sv->g, sl.stream);
     if (rc != BF_OK && rc != BF_ERR_TIMEOUT) cudaStreamSynchronize(sl.stream);
     if (rc == BF_ERR_TIMEOUT) {
-      // the jobs complete with TIMEOUT now; the slot is reused only after its
-      // stream drained (the kernels themselves always terminate)
-      for (Job* j : batch) complete(sv, j, rc);
+      // the jobs complete with TIMEOUT once the slot's stream has drained
+      // (the kernels always terminate): no copy may still be writing into a
+      // caller's buffer after its completion is reported
       cudaStreamSynchronize(sl.stream);
-      continue;
+      for (Job* j : batch) complete(sv, j, rc);
+    } else {
+      for (Job* j : batch) complete(sv, j, rc);
     }
-    for (Job* j : batch) complete(sv, j, rc);
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      sv->admitted_io -= io;
+    }
+    sv->cv_work.notify_all();  // memory freed: waiting slots may admit now
   }
 }
 
@@ -300,6 +387,7 @@ bf_status bf_server_create(bf_graph* gh, const bf_server_cfg* cfg, bf_server** o
   if (!sv->cfg.max_inflight) sv->cfg.max_inflight = 64;
   if (!sv->cfg.max_queue) sv->cfg.max_queue = 4096;
   if (!sv->cfg.timeout_ms) sv->cfg.timeout_ms = 10000;
+  sv->n_slots = sv->cfg.slots ? (int)std::min<uint32_t>(sv->cfg.slots, MAX_SLOTS) : 4;
   if (cudaSetDevice(g->device) != cudaSuccess) {
     delete h;
     return cuda_status(cudaGetLastError(), "cudaSetDevice");
@@ -310,28 +398,38 @@ bf_status bf_server_create(bf_graph* gh, const bf_server_cfg* cfg, bf_server** o
     cudaMemGetInfo(&fr, &tot);
     budget = (uint64_t)(fr * 0.8);
   }
-  for (Slot& sl : sv->slot) {
-    sl.ctx.budget = budget / 2;
+  // half of the budget for request I/O, half for the slots' distance slabs
+  sv->budget = budget;
+  sv->io_budget = budget / 2;
+  // the full-graph schedule that isochrone batches sweep is built here, once
+  // for all slots (it is read-only while sweeping), so no request waits for it
+  bf_status rc0 = init_ctx(sv->shared);
+  if (rc0 == BF_OK) {
+    try {
+      rc0 = build_schedule(g, sv->shared, sv->shared.full, nullptr, 0, true, g->stream);
+    } catch (const std::bad_alloc&) {
+      set_error("out of host memory");
+      rc0 = BF_ERR_OOM;
+    }
+  }
+  if (rc0 != BF_OK) {
+    bf_server_destroy(h);
+    return rc0;
+  }
+  for (int i = 0; i < sv->n_slots; ++i) {
+    Slot& sl = sv->slot[i];
+    sl.ctx.budget = budget / 2 / sv->n_slots;
+    sl.ctx.shared_full = &sv->shared.full;
     bf_status rc = init_ctx(sl.ctx);
     if (rc == BF_OK && (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
                         cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess))
       rc = cuda_status(cudaGetLastError(), "stream/event create");
-    // the full-graph schedule isochrone batches sweep is built here, once per
-    // slot, so that no request waits for it
-    if (rc == BF_OK) {
-      try {
-        rc = build_schedule(g, sl.ctx, sl.ctx.full, nullptr, 0, true, sl.stream);
-      } catch (const std::bad_alloc&) {
-        set_error("out of host memory");
-        rc = BF_ERR_OOM;
-      }
-    }
     if (rc != BF_OK) {
       bf_server_destroy(h);
       return rc;
     }
   }
-  for (int i = 0; i < 2; ++i) sv->slot[i].th = std::thread(worker, sv, i);
+  for (int i = 0; i < sv->n_slots; ++i) sv->slot[i].th = std::thread(worker, sv, i);
   *out = h;
   return BF_OK;
 }
@@ -374,6 +472,15 @@ bf_status bf_server_submit(bf_server* h, const bf_request* req, uint64_t* ticket
       set_error("bf_server_submit: target id out of range");
       return BF_ERR_INVALID;
     }
+  j->io_bytes = io_bytes_of(j, n);
+  if (j->io_bytes > sv->io_budget) {
+    const uint64_t need = j->io_bytes;
+    delete j;
+    set_error("bf_server_submit: the request's " + std::to_string(need) +
+              " bytes of device I/O exceed the server's budget for request I/O (" +
+              std::to_string(sv->io_budget) + " bytes)");
+    return BF_ERR_BUSY;
+  }
   j->submit_s = wall_s();
   {
     std::lock_guard<std::mutex> lk(sv->mu);
@@ -449,6 +556,7 @@ void bf_server_destroy(bf_server* h) {
     if (sl.th.joinable()) sl.th.join();
   cudaSetDevice(sv->g->device);
   for (Job* j : sv->queue) delete j;
+  free_ctx(sv->shared);
   for (Slot& sl : sv->slot) {
     free_ctx(sl.ctx);
     if (sl.d_buf) {
@@ -456,6 +564,7 @@ void bf_server_destroy(bf_server* h) {
       sv->g->device_bytes -= sl.buf_bytes;
     }
     if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.h_stage) cudaFreeHost(sl.h_stage);
     if (sl.stream) cudaStreamDestroy(sl.stream);
   }
   delete h;

@@ -151,6 +151,10 @@ typedef struct bf_stats {
   uint64_t lanes;             /* lanes (sources) per wave, padded to 4            */
   uint64_t waves;             /* sweeps run                                       */
   double schedule_ms;         /* host time building sweep schedules (0 on reuse)  */
+  uint64_t sweep_bytes;       /* isochrone calls: algorithmic bytes of the gated
+                                 sweeps (schedule records scanned, active source
+                                 rows gathered, rows written), summed over waves */
+  uint64_t active_rows;       /* isochrone calls: rows written by the sweeps      */
 } bf_stats;
 
 bf_status bf_graph_create(const bf_cch_csr* csr, const bf_config* cfg, bf_graph** out);
@@ -374,11 +378,17 @@ void bf_settled_free(uint32_t* p);
 typedef struct bf_server bf_server;
 
 typedef struct bf_server_cfg {
-  uint64_t hbm_budget_bytes;  /* device memory for in-flight request slabs        */
-  uint32_t max_inflight;      /* requests admitted at once (0 = 64)               */
+  uint64_t hbm_budget_bytes;  /* device memory for in-flight requests: their I/O
+                                 buffers and the slots' distance slabs (0 = 80%
+                                 of free memory at creation)                     */
+  uint32_t max_inflight;      /* requests admitted into one batch (0 = 64)        */
   uint32_t max_queue;         /* queued requests before BF_ERR_BUSY (0 = 4096)    */
-  uint32_t timeout_ms;        /* bound on every device wait (0 = 10000)           */
-  uint32_t reserved;
+  uint32_t timeout_ms;        /* bound on a matrix batch's device work from its
+                                 start; past it the batch's requests complete
+                                 with BF_ERR_TIMEOUT (outputs undefined) once its
+                                 stream drained (0 = 10000)                       */
+  uint32_t slots;             /* worker slots computing batches concurrently, each
+                                 with its own stream (0 = 4, at most 8)          */
 } bf_server_cfg;
 
 typedef enum bf_request_kind { BF_REQ_MATRIX = 1, BF_REQ_ISOCHRONE = 2 } bf_request_kind;
@@ -411,7 +421,11 @@ typedef struct bf_completion {
 
 bf_status bf_server_create(bf_graph* g, const bf_server_cfg* cfg, bf_server** out);
 /* Queue a request; *ticket identifies it. Returns BF_ERR_BUSY when the queue
- * is full or the request alone exceeds the HBM budget. */
+ * is full or the request's device I/O alone exceeds the HBM budget.
+ * Admission: a free slot forms a batch from the waiting requests of one kind
+ * while their device I/O fits both what the budget leaves beside the batches
+ * in flight and the device's free memory (cudaMemGetInfo, less a margin); a
+ * request that does not fit waits until a batch completes. */
 bf_status bf_server_submit(bf_server* s, const bf_request* req, uint64_t* ticket);
 /* Collect up to cap completions; waits up to wait_ms for the first one. */
 bf_status bf_server_poll(bf_server* s, bf_completion* out, uint32_t cap, uint32_t wait_ms,
