@@ -17,8 +17,8 @@ OBJ = PKG / "_build"
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_UNITS = ["graph", "engine_plain", "engine_batched", "schedule", "isochrone", "seeded", "twochannel", "customize", "contour", "tile", "server", "noalloc", "api"]
-CU_HEADERS = ["engine.cuh"]
+CU_UNITS = ["graph", "engine_plain", "engine_batched", "schedule", "isochrone", "seeded", "twochannel", "customize", "contour", "trace", "tile", "server", "noalloc", "api"]
+CU_HEADERS = ["engine.cuh", "scan.cuh"]
 
 
 def _stale(out, deps):

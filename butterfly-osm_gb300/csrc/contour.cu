@@ -402,7 +402,7 @@ bf_status rasters_core(Workspace& ws, cudaStream_t st, const double2* d_xy, cons
                        const uint64_t* d_iseg, uint64_t n_seg, uint64_t n_pts, uint32_t n_iso,
                        const double* cell_m, const uint8_t* has_anchor, const double* anchor_xy,
                        uint32_t dilation, uint32_t erosion, bf_raster* rasters, uint64_t** words,
-                       uint64_t* n_words) {
+                       uint64_t* n_words, const uint64_t** d_words_out = nullptr) {
   cudaError_t e = cudaSuccess;
   uint32_t *d_siso = nullptr, *d_err = nullptr;
   double* d_cell = nullptr;
@@ -462,8 +462,11 @@ bf_status rasters_core(Workspace& ws, cudaStream_t st, const double2* d_xy, cons
     return BF_ERR_INVALID;
   }
   *n_words = total;
-  uint64_t* h_words = (uint64_t*)std::malloc(std::max<uint64_t>(total, 1) * 8);
-  if (!h_words) {
+  // with d_words_out the closed rasters stay on the device (in the
+  // workspace, valid until its next use) and nothing is downloaded
+  uint64_t* h_words =
+      d_words_out ? nullptr : (uint64_t*)std::malloc(std::max<uint64_t>(total, 1) * 8);
+  if (!h_words && !d_words_out) {
     set_error("out of host memory");
     return BF_ERR_OOM;
   }
@@ -495,7 +498,11 @@ bf_status rasters_core(Workspace& ws, cudaStream_t st, const double2* d_xy, cons
       std::swap(cur, nxt);
     }
     if ((r = cudaGetLastError())) return r;
-    if (total && (r = cudaMemcpyAsync(h_words, cur, total * 8, cudaMemcpyDeviceToHost, st))) return r;
+    if (d_words_out) {
+      *d_words_out = reinterpret_cast<const uint64_t*>(cur);
+    } else if (total && (r = cudaMemcpyAsync(h_words, cur, total * 8, cudaMemcpyDeviceToHost, st))) {
+      return r;
+    }
     return cudaStreamSynchronize(st);
   };
   e = stage2();
@@ -507,7 +514,7 @@ bf_status rasters_core(Workspace& ws, cudaStream_t st, const double2* d_xy, cons
     set_error("bf_contour_rasters: a stamped cell fell outside its raster");
     return BF_ERR_DEVICE;
   }
-  *words = h_words;
+  if (words) *words = h_words;
   return BF_OK;
 }
 
@@ -601,276 +608,15 @@ void bf_contour_release(int device) {
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
-// Steps 4-5 on the host, per isochrone in parallel: Moore boundary tracing of
-// the closed raster with cell-centre vertices, the ring containing the anchor
-// (else the largest, the last of equal length), Web-Mercator back-projection
-// and Douglas-Peucker (sparse_contour.rs:770-1183). Sequential per ring.
-
-#include <atomic>
-#include <thread>
-#include <unordered_set>
+// Steps 4-5 (sparse_contour.rs:770-1183): boundary tracing with cell-centre
+// vertices, the ring containing the anchor (else the largest, the last of
+// equal length), back-projection and Douglas-Peucker, on the GPU
+// (csrc/trace.cu) for rasters the caller holds on the host.
 
 namespace {
 
 constexpr double EARTH_R = 6378137.0;
 constexpr double PI_D = 3.14159265358979323846264338;
-
-struct RasterView {
-  const bf_raster* r;
-  const uint64_t* w;
-  bool get(int32_t c, int32_t row) const {
-    const int64_t lc = (int64_t)c - r->col0, lr = (int64_t)row - r->row0;
-    if (lc < 0 || lr < 0 || lc >= (int64_t)r->width_words * 64 || lr >= (int64_t)r->height) return false;
-    return (w[r->word_offset + (uint64_t)lr * r->width_words + (uint64_t)(lc >> 6)] >> (lc & 63)) & 1;
-  }
-};
-
-using PtD = std::pair<double, double>;
-
-struct Tracer {
-  RasterView v;
-  std::vector<uint8_t> seen;  // 4 bits per cell: visited edges
-  uint64_t cols = 0;
-  bool visited(int32_t c, int32_t r, uint8_t e) const {
-    return (seen[(uint64_t)(r - v.r->row0) * cols + (uint64_t)(c - v.r->col0)] >> e) & 1;
-  }
-  void mark(int32_t c, int32_t r, uint8_t e) {
-    seen[(uint64_t)(r - v.r->row0) * cols + (uint64_t)(c - v.r->col0)] |= (uint8_t)(1u << e);
-  }
-  void next(int32_t c, int32_t r, uint8_t e, int32_t* nc, int32_t* nr, uint8_t* ne) const {
-    switch (e) {  // next_boundary_edge, sparse_contour.rs:1049-1130
-      case 0:
-        if (v.get(c + 1, r - 1)) { *nc = c + 1; *nr = r - 1; *ne = 3; }
-        else if (v.get(c + 1, r)) { *nc = c + 1; *nr = r; *ne = 0; }
-        else { *nc = c; *nr = r; *ne = 1; }
-        return;
-      case 1:
-        if (v.get(c + 1, r + 1)) { *nc = c + 1; *nr = r + 1; *ne = 0; }
-        else if (v.get(c, r + 1)) { *nc = c; *nr = r + 1; *ne = 1; }
-        else { *nc = c; *nr = r; *ne = 2; }
-        return;
-      case 2:
-        if (v.get(c - 1, r + 1)) { *nc = c - 1; *nr = r + 1; *ne = 1; }
-        else if (v.get(c - 1, r)) { *nc = c - 1; *nr = r; *ne = 2; }
-        else { *nc = c; *nr = r; *ne = 3; }
-        return;
-      default:
-        if (v.get(c - 1, r - 1)) { *nc = c - 1; *nr = r - 1; *ne = 2; }
-        else if (v.get(c, r - 1)) { *nc = c; *nr = r - 1; *ne = 3; }
-        else { *nc = c; *nr = r; *ne = 0; }
-    }
-  }
-};
-
-bool in_ring(PtD p, const std::vector<PtD>& ring) {
-  bool inside = false;
-  const size_t n = ring.size();
-  for (size_t i = 0; i < n; ++i) {
-    const PtD a = ring[i], b = ring[(i + 1) % n];
-    if ((a.second > p.second) != (b.second > p.second) &&
-        p.first < (b.first - a.first) * (p.second - a.second) / (b.second - a.second) + a.first)
-      inside = !inside;
-  }
-  return inside;
-}
-
-bool near_ring(PtD p, const std::vector<PtD>& ring, double tol) {
-  const size_t n = ring.size();
-  for (size_t i = 0; i < n; ++i) {
-    const PtD a = ring[i], b = ring[(i + 1) % n];
-    const double dx = b.first - a.first, dy = b.second - a.second;
-    const double len2 = dx * dx + dy * dy;
-    double t = 0.0;
-    if (len2 > 0.0)
-      t = std::min(std::max(((p.first - a.first) * dx + (p.second - a.second) * dy) / len2, 0.0), 1.0);
-    const double cx = a.first + t * dx, cy = a.second + t * dy;
-    if ((p.first - cx) * (p.first - cx) + (p.second - cy) * (p.second - cy) <= tol * tol) return true;
-  }
-  return false;
-}
-
-double seg_dist(PtD p, PtD s, PtD e) {
-  const double dx = e.first - s.first, dy = e.second - s.second;
-  const double len_sq = dx * dx + dy * dy;
-  if (len_sq < 1e-12) {
-    const double pdx = p.first - s.first, pdy = p.second - s.second;
-    return std::sqrt(pdx * pdx + pdy * pdy);
-  }
-  double t = ((p.first - s.first) * dx + (p.second - s.second) * dy) / len_sq;
-  t = std::min(std::max(t, 0.0), 1.0);
-  const double px = s.first + t * dx, py = s.second + t * dy;
-  const double pdx = p.first - px, pdy = p.second - py;
-  return std::sqrt(pdx * pdx + pdy * pdy);
-}
-
-// Douglas-Peucker (sparse_contour.rs douglas_peucker) on indices: a range
-// [s, e] keeps its farthest interior point (the first of equal distances)
-// when that distance exceeds tol and splits there; the output is every
-// kept point in order, exactly the recursive form's result.
-std::vector<PtD> simplify(const std::vector<PtD>& pts, double tol) {
-  const size_t n = pts.size();
-  if (n <= 2) return pts;
-  std::vector<uint8_t> keep(n, 0);
-  keep[0] = keep[n - 1] = 1;
-  std::vector<std::pair<size_t, size_t>> todo{{0, n - 1}};
-  while (!todo.empty()) {
-    const auto [a, b] = todo.back();
-    todo.pop_back();
-    double max_d = 0.0;
-    size_t max_i = 0;
-    for (size_t i = a + 1; i < b; ++i) {
-      const double d = seg_dist(pts[i], pts[a], pts[b]);
-      if (d > max_d) {
-        max_d = d;
-        max_i = i;
-      }
-    }
-    if (max_d > tol) {
-      keep[max_i] = 1;
-      todo.emplace_back(max_i, b);
-      todo.emplace_back(a, max_i);
-    }
-  }
-  std::vector<PtD> out;
-  for (size_t i = 0; i < n; ++i)
-    if (keep[i]) out.push_back(pts[i]);
-  return out;
-}
-
-// Visited-edge arrays of the tracer, reused across isochrones and calls
-// (first-touch page faults of a fresh array cost as much as the trace).
-struct SeenPool {
-  std::mutex mu;
-  std::vector<std::vector<uint8_t>> free;
-};
-SeenPool& seen_pool() {
-  static SeenPool p;
-  return p;
-}
-struct SeenLease {
-  std::vector<uint8_t>& v;
-  explicit SeenLease(std::vector<uint8_t>& x) : v(x) {
-    SeenPool& p = seen_pool();
-    std::lock_guard<std::mutex> lk(p.mu);
-    if (!p.free.empty()) {
-      v.swap(p.free.back());
-      p.free.pop_back();
-    }
-  }
-  ~SeenLease() {
-    SeenPool& p = seen_pool();
-    std::lock_guard<std::mutex> lk(p.mu);
-    if (p.free.size() < 64) p.free.push_back(std::move(v));
-  }
-};
-
-// The outer ring of one closed raster, as (lon, lat).
-std::vector<PtD> polygon_of(const bf_raster& R, const uint64_t* words, double cell,
-                            double simplify_m, const PtD* anchor_xy) {
-  if (R.height == 0) return {};
-  Tracer t{RasterView{&R, words}, {}, (uint64_t)R.width_words * 64};
-  // boundary starts in (col, row) order, one per boundary cell, found with
-  // word masks in the reference's edge priority (N, W, E, S); the iteration
-  // cap counts the reference's non-empty 64x64 tiles (aligned at multiples
-  // of 64 in grid cells), marked per word from its lowest and highest bits
-  std::vector<std::tuple<int32_t, int32_t, uint8_t>> starts;
-  const int32_t tx0 = R.col0 >> 6, ty0 = R.row0 >> 6;
-  const int32_t tx1 = (R.col0 + (int32_t)(R.width_words * 64) - 1) >> 6;
-  const int32_t ty1 = (R.row0 + (int32_t)R.height - 1) >> 6;
-  const uint64_t ntx = (uint64_t)(tx1 - tx0 + 1);
-  std::vector<uint8_t> tile_set(ntx * (uint64_t)(ty1 - ty0 + 1), 0);
-  auto W = [&](int64_t lr, int64_t j) -> uint64_t {
-    if (lr < 0 || lr >= (int64_t)R.height || j < 0 || j >= (int64_t)R.width_words) return 0;
-    return words[R.word_offset + (uint64_t)lr * R.width_words + (uint64_t)j];
-  };
-  uint64_t n_tiles = 0;
-  for (uint32_t lr = 0; lr < R.height; ++lr)
-    for (uint32_t j = 0; j < R.width_words; ++j) {
-      const uint64_t cur = W(lr, j);
-      if (!cur) continue;
-      const int32_t r = R.row0 + (int32_t)lr, cb = R.col0 + (int32_t)(j * 64);
-      for (int32_t c : {cb + __builtin_ctzll(cur), cb + 63 - __builtin_clzll(cur)}) {
-        uint8_t& t = tile_set[(uint64_t)((r >> 6) - ty0) * ntx + (uint64_t)((c >> 6) - tx0)];
-        if (!t) {
-          t = 1;
-          ++n_tiles;
-        }
-      }
-      const uint64_t north = W((int64_t)lr - 1, j), south = W((int64_t)lr + 1, j);
-      const uint64_t west = (cur << 1) | (W(lr, (int64_t)j - 1) >> 63);
-      const uint64_t east = (cur >> 1) | (W(lr, (int64_t)j + 1) << 63);
-      // edge 0 (N), then 3 (W), then 1 (E), then 2 (S)
-      const uint64_t mn = cur & ~north;
-      const uint64_t mw = cur & north & ~west;
-      const uint64_t me = cur & north & west & ~east;
-      const uint64_t ms = cur & north & west & east & ~south;
-      const uint64_t any = mn | mw | me | ms;
-      for (uint64_t b = any; b;) {
-        const int i = __builtin_ctzll(b);
-        b &= b - 1;
-        const uint64_t bit = 1ull << i;
-        const uint8_t e = (mn & bit) ? 0 : (mw & bit) ? 3 : (me & bit) ? 1 : 2;
-        starts.emplace_back(cb + i, r, e);
-      }
-    }
-  if (n_tiles == 0) return {};
-  {  // (col, row) order: the scan gives rows ascending, so a stable counting sort by column
-    const uint64_t ncol = (uint64_t)R.width_words * 64;
-    std::vector<uint32_t> at(ncol + 1, 0);
-    for (const auto& st : starts) ++at[(uint64_t)(std::get<0>(st) - R.col0) + 1];
-    for (uint64_t c = 0; c < ncol; ++c) at[c + 1] += at[c];
-    std::vector<std::tuple<int32_t, int32_t, uint8_t>> by_col(starts.size());
-    for (const auto& st : starts) by_col[at[(uint64_t)(std::get<0>(st) - R.col0)]++] = st;
-    starts.swap(by_col);
-  }
-  SeenLease lease(t.seen);
-  if (t.seen.size() < t.cols * R.height) t.seen.resize(t.cols * R.height);
-  std::memset(t.seen.data(), 0, t.cols * R.height);
-  const uint64_t max_iter = n_tiles * 64 * 64 * 4;
-  std::vector<std::vector<PtD>> rings;
-  for (const auto& s : starts) {
-    const int32_t sc = std::get<0>(s), sr = std::get<1>(s);
-    const uint8_t se = std::get<2>(s);
-    if (t.visited(sc, sr, se)) continue;
-    std::vector<PtD> ring;
-    int32_t c = sc, r = sr;
-    uint8_t e = se;
-    for (uint64_t it = 1;; ++it) {
-      if (it > max_iter) break;
-      t.mark(c, r, e);
-      const PtD v{(double)c + 0.5, (double)r + 0.5};
-      if (ring.empty() || ring.back() != v) ring.push_back(v);
-      int32_t nc, nr;
-      uint8_t ne;
-      t.next(c, r, e, &nc, &nr, &ne);
-      if (nc == sc && nr == sr && ne == se) break;
-      c = nc;
-      r = nr;
-      e = ne;
-    }
-    while (ring.size() > 1 && ring.back() == ring.front()) ring.pop_back();
-    if (ring.size() >= 3) rings.push_back(std::move(ring));
-  }
-  const std::vector<PtD>* best = nullptr;
-  if (anchor_xy) {
-    const PtD a{(anchor_xy->first - R.origin_x) / cell, (anchor_xy->second - R.origin_y) / cell};
-    for (const auto& rg : rings)
-      if ((in_ring(a, rg) || near_ring(a, rg, 1.0)) && (!best || rg.size() > best->size())) best = &rg;
-  }
-  if (!best)
-    for (const auto& rg : rings)
-      if (!best || rg.size() >= best->size()) best = &rg;
-  if (!best) return {};
-  std::vector<PtD> wgs;
-  wgs.reserve(best->size());
-  for (const PtD& p : *best) {
-    const double x = R.origin_x + p.first * cell, y = R.origin_y + p.second * cell;
-    const double lon = (x / EARTH_R) * (180.0 / PI_D);
-    const double lat = (2.0 * std::atan(std::exp(y / EARTH_R)) - PI_D / 2.0) * (180.0 / PI_D);
-    wgs.emplace_back(lon, lat);
-  }
-  return simplify(wgs, simplify_m / 111000.0);
-}
 
 }  // namespace
 
@@ -885,32 +631,38 @@ bf_status bf_contour_polygons(const bf_raster* rasters, const uint64_t* words, u
     set_error("bf_contour_polygons: null argument");
     return BF_ERR_INVALID;
   }
-  std::vector<std::vector<PtD>> rings(n_iso);
-  std::atomic<uint32_t> next{0};
-  auto work = [&]() {
-    for (uint32_t k; (k = next.fetch_add(1)) < n_iso;) {
-      const PtD a = has_anchor ? PtD{anchor_xy[2 * k], anchor_xy[2 * k + 1]} : PtD{0, 0};
-      rings[k] = polygon_of(rasters[k], words, cell_m[k], simplify_m[k],
-                            (has_anchor && has_anchor[k]) ? &a : nullptr);
-    }
-  };
-  const unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), n_iso));
-  std::vector<std::thread> pool;
-  for (unsigned i = 1; i < nt; ++i) pool.emplace_back(work);
-  work();
-  for (auto& th : pool) th.join();
-  ring_off[0] = 0;
-  for (uint32_t k = 0; k < n_iso; ++k) ring_off[k + 1] = ring_off[k] + rings[k].size();
-  double* out = (double*)std::malloc(std::max<uint64_t>(ring_off[n_iso], 1) * 16);
+  uint64_t total = 0;
+  for (uint32_t k = 0; k < n_iso; ++k)
+    total = std::max<uint64_t>(total, rasters[k].word_offset +
+                                          (uint64_t)rasters[k].width_words * rasters[k].height);
+  if (total && !words) {
+    set_error("bf_contour_polygons: null words");
+    return BF_ERR_INVALID;
+  }
+  int dev = 0;
+  BF_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("bf_contour_polygons: device ordinal out of range");
+    return BF_ERR_INVALID;
+  }
+  Workspace& ws = workspace(dev);
+  std::lock_guard<std::mutex> lk(ws.mu);
+  if (!ws.st) BF_CUDA(cudaStreamCreateWithFlags(&ws.st, cudaStreamNonBlocking));
+  uint64_t* d_words = nullptr;
+  BF_CUDA(ws_get(ws, S_A, std::max<uint64_t>(total, 1) * 8, &d_words));
+  if (total) BF_CUDA(cudaMemcpyAsync(d_words, words, total * 8, cudaMemcpyHostToDevice, ws.st));
+  std::vector<uint64_t> off;
+  std::vector<double> ll;
+  bf_status rc = trace_rings_device(d_words, rasters, n_iso, cell_m, simplify_m, has_anchor,
+                                    anchor_xy, ws.st, off, ll);
+  if (rc) return rc;
+  double* out = (double*)std::malloc(std::max<size_t>(ll.size(), 2) * 8);
   if (!out) {
     set_error("out of host memory");
     return BF_ERR_OOM;
   }
-  for (uint32_t k = 0; k < n_iso; ++k)
-    for (size_t i = 0; i < rings[k].size(); ++i) {
-      out[2 * (ring_off[k] + i)] = rings[k][i].first;
-      out[2 * (ring_off[k] + i) + 1] = rings[k][i].second;
-    }
+  if (!ll.empty()) std::memcpy(out, ll.data(), ll.size() * 8);
+  for (uint32_t k = 0; k <= n_iso; ++k) ring_off[k] = off[k];
   *lonlat = out;
   return BF_OK;
 }
@@ -1476,19 +1228,24 @@ bf_status bf_isochrone_polygons(bf_graph* g, const bf_geometry* geo, const uint3
     ph[1] += ms(t0);
     t0 = clk::now();
     std::vector<bf_raster> ras(std::max<uint32_t>(kw, 1));
-    uint64_t* words = nullptr;
+    const uint64_t* d_words = nullptr;
     uint64_t n_words = 0;
     if ((rc = rasters_core(ws, st, d_xy, d_seg, d_iseg, n_seg, n_pts, kw, cell_l.data(), has.data(),
-                           anc.data(), dil, ero, ras.data(), &words, &n_words)))
+                           anc.data(), dil, ero, ras.data(), nullptr, &n_words, &d_words)))
       return rc;
     ph[2] += ms(t0);
     t0 = clk::now();
-    std::vector<uint64_t> roff(kw + 1, 0);
-    double* ll = nullptr;
-    rc = bf_contour_polygons(ras.data(), words, kw, cell_l.data(), simp_l.data(), has.data(),
-                             anc.data(), roff.data(), &ll);
-    bf_contour_free(words);
-    if (rc) return rc;
+    std::vector<uint64_t> roff;
+    std::vector<double> ll_v;
+    if ((rc = trace_rings_device(d_words, ras.data(), kw, cell_l.data(), simp_l.data(), has.data(),
+                                 anc.data(), st, roff, ll_v)))
+      return rc;
+    double* ll = (double*)std::malloc(std::max<size_t>(ll_v.size(), 2) * 8);
+    if (!ll) {
+      set_error("out of host memory");
+      return BF_ERR_OOM;
+    }
+    if (!ll_v.empty()) std::memcpy(ll, ll_v.data(), ll_v.size() * 8);
     wave_ll.push_back(ll);
     for (uint32_t l = 0; l < kw; ++l) {
       r_len[rows[l]] = roff[l + 1] - roff[l];

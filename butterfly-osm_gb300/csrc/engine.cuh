@@ -519,6 +519,14 @@ bf_status na_scratch(int device, uint32_t** out);
 bf_status query_batch_noalloc(Graph* g, const uint32_t* d_src, uint32_t k, uint32_t threshold,
                               uint32_t* d_out, cudaStream_t st);
 
+// trace.cu: the chosen, back-projected and simplified ring of each of n_iso
+// closed rasters whose words are on the current device (d_words, laid out as
+// `ras`), as bf_contour_polygons returns them; runs on st.
+bf_status trace_rings_device(const uint64_t* d_words, const bf_raster* ras, uint32_t n_iso,
+                             const double* cell_m, const double* simplify_m,
+                             const uint8_t* has_anchor, const double* anchor_xy, cudaStream_t st,
+                             std::vector<uint64_t>& ring_off, std::vector<double>& lonlat);
+
 // k_extract_lanes (engine_batched.cu): out[s * T + t] = slab[trow[t]][s]
 void launch_extract_lanes(const uint32_t* slab, uint32_t Kp, const uint32_t* trow, uint64_t T,
                           uint32_t S, uint32_t threshold, uint32_t* out, cudaStream_t st);

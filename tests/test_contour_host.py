@@ -1,8 +1,10 @@
-"""bf_contour_polygons (host tracing, anchored ring, back-projection,
-Douglas-Peucker) on rasters built from the oracle's closed cells, against the
-oracle's whole contour pipeline (route/src/range/sparse_contour.rs:770-1183).
-CPU only."""
+"""bf_contour_polygons (boundary tracing, anchored ring, back-projection,
+Douglas-Peucker, on the GPU) on rasters built from the oracle's closed cells,
+against the oracle's whole contour pipeline
+(route/src/range/sparse_contour.rs:770-1183), vertex for vertex; the
+projection and tier helpers run on the host."""
 import numpy as np
+import pytest
 
 import contourgen
 from oracle import oracle as orc
@@ -21,6 +23,7 @@ def _raster(cells, grid, off):
     return r, words
 
 
+@pytest.mark.gpu
 def test_host_polygons_match_oracle(built):
     import bfphast
     rng = np.random.default_rng(9)
@@ -60,10 +63,11 @@ def test_projection_and_tiers_match_oracle(built):
             assert bfphast.contour_config(mode, t) == orc.contour_config(name, t)
 
 
+@pytest.mark.gpu
 def test_host_polygons_concurrent_calls(built):
     # bf_contour_polygons from several host threads at once (the tracer's
-    # visited-edge arrays come from a shared pool): every call returns the
-    # single-threaded rings
+    # device workspace is shared and its calls are serialised): every call
+    # returns the single-threaded rings
     import threading
     import bfphast
     rng = np.random.default_rng(21)
