@@ -558,13 +558,13 @@ void bf_contour_free(uint64_t* words);
 void bf_contour_release(int device);
 
 /* Steps 4-5 of generate_sparse_contour_anchored (sparse_contour.rs:770-830,
- * 831-1183) on the rasters of bf_contour_rasters, one host thread per
- * isochrone: Moore boundary tracing with cell-centre vertices, the ring
- * containing the anchor (Mercator x, y; else the ring with the most
- * vertices, the last of equal length), back-projection to (lon, lat) and
- * Douglas-Peucker with tolerance simplify_m[k] / 111000 degrees. Ring k is
- * points [ring_off[k], ring_off[k + 1]) of *lonlat (n_iso + 1 offsets), a
- * buffer released with bf_contour_free_polygons. */
+ * 831-1183) on the rasters of bf_contour_rasters (host arrays, in any order),
+ * on the current CUDA device: boundary tracing with cell-centre vertices,
+ * the ring containing the anchor (Mercator x, y; else the ring with the
+ * most vertices, the last of equal length), back-projection to (lon, lat)
+ * and Douglas-Peucker with tolerance simplify_m[k] / 111000 degrees. Ring k
+ * is points [ring_off[k], ring_off[k + 1]) of *lonlat (n_iso + 1 offsets),
+ * a buffer released with bf_contour_free_polygons. */
 bf_status bf_contour_polygons(const bf_raster* rasters, const uint64_t* words, uint32_t n_iso,
                               const double* cell_m, const double* simplify_m,
                               const uint8_t* has_anchor, const double* anchor_xy,
