@@ -78,7 +78,8 @@ class Tune(ctypes.Structure):
                 ("small_level_edges", ctypes.c_uint32), ("overlap_levels", ctypes.c_uint32),
                 ("isochrone_16bit", ctypes.c_uint32), ("overlap_upward", ctypes.c_uint32),
                 ("mapped_output", ctypes.c_uint32), ("hub_l2_mb", ctypes.c_uint32),
-                ("device_schedule", ctypes.c_uint32), ("persistent_sweep", ctypes.c_uint32)]
+                ("device_schedule", ctypes.c_uint32), ("persistent_sweep", ctypes.c_uint32),
+                ("staged_levels", ctypes.c_uint32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -362,11 +363,12 @@ class Graph:
     def set_tune(self, threads_per_block=128, edges_per_item=16, graph_capture=1,
                  lanes_per_wave=0, isochrone_lanes=1024, small_level_rows=64,
                  small_level_edges=8, overlap_levels=1, isochrone_16bit=1, overlap_upward=1,
-                 mapped_output=1, hub_l2_mb=48, device_schedule=1, persistent_sweep=1):
+                 mapped_output=1, hub_l2_mb=48, device_schedule=1, persistent_sweep=1,
+                 staged_levels=0):
         t = Tune(threads_per_block, edges_per_item, graph_capture, lanes_per_wave, 0.0, 0,
                  isochrone_lanes, small_level_rows, small_level_edges, overlap_levels,
                  isochrone_16bit, overlap_upward, mapped_output, hub_l2_mb, device_schedule,
-                 persistent_sweep)
+                 persistent_sweep, staged_levels)
         _check(load().bf_set_tune(self._h, ctypes.byref(t)))
 
     def get_tune(self):

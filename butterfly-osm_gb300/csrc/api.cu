@@ -275,6 +275,7 @@ static bf_tune to_c(const Tune& t) {
   o.hub_l2_mb = t.hub_mb;
   o.device_schedule = t.dev_sched;
   o.persistent_sweep = t.persist;
+  o.staged_levels = t.staged;
   return o;
 }
 
@@ -303,6 +304,7 @@ bf_status bf_set_tune(bf_graph* h, const bf_tune* t) {
   h->g.tune.hub_mb = std::min<uint32_t>(t->hub_l2_mb, 1024);
   h->g.tune.dev_sched = t->device_schedule ? 1 : 0;
   h->g.tune.persist = t->persistent_sweep & 3u;
+  h->g.tune.staged = t->staged_levels ? 1 : 0;
   return BF_OK;
 }
 

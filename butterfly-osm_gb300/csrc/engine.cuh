@@ -192,6 +192,9 @@ struct Sched {
   size_t cap_uses = 0;
   uint32_t* d_hub_h = nullptr;   // hub histogram (65536 bins) and threshold
   size_t cap_hub_h = 0;
+  uint32_t* d_lvl_erec = nullptr;  // [levels + 1] level -> first edge record (host builds)
+  size_t cap_lvl_erec = 0;
+  bool lvl_erec_ready = false;
 };
 
 struct SchedScratch;  // device schedule builder scratch (schedule.cu)
@@ -251,6 +254,8 @@ struct Tune {
   uint32_t dev_sched = 1;    // build target-restricted schedules on the device
   uint32_t persist = 1;      // bit 0: the plain engine's sweep, bit 1: isochrone waves'
                              // sweeps as one persistent launch instead of one per level
+  uint32_t staged = 0;       // runs of small isochrone levels stage each level's items and
+                             // edge records in shared memory by bulk copies
 };
 
 struct Graph {

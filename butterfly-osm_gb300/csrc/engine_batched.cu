@@ -299,6 +299,10 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   });
   sc.lvl_item.assign(g->n_levels + 1, 0);
   for (uint32_t l = 0; l <= g->n_levels; ++l) sc.lvl_item[l] = (uint32_t)ioff[row_lvl[l]];
+  // the edge records of a level's rows are contiguous: level -> first record
+  std::vector<uint32_t> lvl_erec(g->n_levels + 1);
+  for (uint32_t l = 0; l <= g->n_levels; ++l) lvl_erec[l] = (uint32_t)eoff[row_lvl[l]];
+  sc.lvl_erec_ready = true;
   // rows by gather count, most-used first (up to 65536 of them): the matrix
   // sweep keeps the head of this list in L2. A counting sort by count; the
   // full-graph schedule (isochrones, bounded queries) does not use it.
@@ -346,11 +350,16 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   bf_status s;
   if ((s = ensure(&sc.d_cidx, sc.cap_cidx, n, g))) return s;
   if ((s = ensure(&sc.d_item, sc.cap_items, n_i, g))) return s;
-  if ((s = ensure(&sc.d_erec, sc.cap_edges, n_e, g))) return s;
+  // two records of padding: a bulk copy of a level's records rounds its end
+  // up to 16 bytes
+  if ((s = ensure(&sc.d_erec, sc.cap_edges, n_e + 2, g))) return s;
   if (two && (s = ensure(&sc.d_elen, sc.cap_elen, n_e, g))) return s;
   if ((s = ensure(&sc.d_trow, sc.cap_t, T, g))) return s;
   if ((s = ensure(&c.d_pairs, c.cap_pairs, pairs.size() * 2, g))) return s;
   if ((s = ensure(&sc.d_split, sc.cap_split, split_bits.size(), g))) return s;
+  if ((s = ensure(&sc.d_lvl_erec, sc.cap_lvl_erec, lvl_erec.size(), g))) return s;
+  BF_CUDA(cudaMemcpyAsync(sc.d_lvl_erec, lvl_erec.data(), lvl_erec.size() * 4,
+                          cudaMemcpyHostToDevice, st));
   if ((s = ensure(&sc.d_lvl, sc.cap_lvl, sc.lvl_item.size(), g))) return s;
   BF_CUDA(cudaMemcpyAsync(sc.d_lvl, sc.lvl_item.data(), sc.lvl_item.size() * 4,
                           cudaMemcpyHostToDevice, st));
@@ -633,7 +642,7 @@ uint64_t ctx_budget(Graph* g, Ctx& c) {
 
 static void free_sched(Sched& sc) {
   void* p[] = {sc.d_cidx, sc.d_item, sc.d_erec, sc.d_elen, sc.d_trow, sc.d_split, sc.d_hub,
-               sc.d_lvl, sc.d_uses, sc.d_hub_h};
+               sc.d_lvl, sc.d_uses, sc.d_hub_h, sc.d_lvl_erec};
   for (void* q : p)
     if (q) cudaFree(q);
   if (sc.gexec) cudaGraphExecDestroy(sc.gexec);

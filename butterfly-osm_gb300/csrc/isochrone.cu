@@ -348,6 +348,151 @@ __global__ void __launch_bounds__(1024, 1)
   }
 }
 
+// ---- bulk-copy staging of a level's schedule -------------------------------
+// mbarrier and cp.async.bulk helpers (shared memory of this CTA).
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bytes (a multiple of 16) from 16-byte aligned global src to shared dst
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes,
+                                          uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+constexpr uint32_t STAGE_ITEMS = 128;   // items of a staged level at most
+constexpr uint32_t STAGE_EREC = 2048;   // edge records of a staged level at most
+constexpr uint32_t STAGE_POLLS = 1u << 22;  // bound on a wait for a staged level
+
+// The variant of k_sweep_run16 whose levels come through shared memory:
+// thread 0 bulk-copies the next level's work items and the edge records of
+// its rows (one contiguous range, start rounded down and end up to 16
+// bytes) into the other of two buffers while the block sweeps the current
+// level from its buffer, each buffer completing on its own mbarrier. A
+// level too large for a buffer, or a wait that gives up after STAGE_POLLS
+// polls (the thread then sets DEVERR_TIMEOUT), reads the same records from
+// global memory: the result does not depend on the staging.
+__global__ void __launch_bounds__(1024, 1)
+    k_sweep_run16_staged(const uint4* __restrict__ item, const uint32_t* __restrict__ lvl,
+                         const uint32_t* __restrict__ lvl_erec, uint32_t l0, uint32_t l1,
+                         const uint2* __restrict__ erec, uint16_t* __restrict__ slab, uint32_t Kp,
+                         uint32_t* __restrict__ active, const uint32_t* __restrict__ thr,
+                         uint32_t kw, const uint32_t* __restrict__ seeded,
+                         uint32_t* __restrict__ err) {
+  __shared__ __align__(16) uint4 s_item[2][STAGE_ITEMS];
+  __shared__ __align__(16) uint2 s_erec[2][STAGE_EREC];
+  __shared__ __align__(8) uint64_t s_bar[2];
+  asm volatile("griddepcontrol.launch_dependents;");
+  const uint32_t t = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t wpi = (Kp + 255) / 256;  // 1..32 (launched for Kp <= 8192)
+  const uint32_t slots = 32 / wpi, slot = warp / wpi;
+  const uint32_t lane = (warp % wpi) * 256 + t * 8;
+  const bool warp_live = slot < slots && (warp % wpi) * 256 < Kp;
+  const bool live = warp_live && lane < Kp;
+  const uint32_t valid_lanes = live ? min(8u, kw > lane ? kw - lane : 0u) : 0u;
+  if (threadIdx.x == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // whether level l fits a buffer (every thread computes the same answer)
+  auto fits = [&](uint32_t l, uint32_t* e0, uint32_t* eb) {
+    const uint32_t n_it = lvl[l + 1] - lvl[l];
+    const uint32_t a = lvl_erec[l] & ~1u, b = (lvl_erec[l + 1] + 1) & ~1u;
+    *e0 = a;
+    *eb = b - a;
+    return n_it <= STAGE_ITEMS && b - a <= STAGE_EREC;
+  };
+  auto issue = [&](uint32_t l, uint32_t buf) {  // thread 0 only
+    uint32_t e0, ne;
+    if (!fits(l, &e0, &ne)) return;
+    const uint32_t n_it = lvl[l + 1] - lvl[l];
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&s_bar[buf], n_it * 16 + ne * 8);
+    if (n_it) bulk_copy(s_item[buf], item + lvl[l], n_it * 16, &s_bar[buf]);
+    if (ne) bulk_copy(s_erec[buf], erec + e0, ne * 8, &s_bar[buf]);
+  };
+  __shared__ int s_giveup;
+  if (threadIdx.x == 0) s_giveup = 0;
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  __syncthreads();
+  // per buffer: the phase to wait for and whether a copy into it is pending
+  // (the same in every thread: fits() and the give-up flag are uniform)
+  uint32_t phase[2] = {0, 0};
+  bool pending[2] = {false, false};
+  bool giveup = false;
+  uint32_t e0, ne;
+  if (fits(l0, &e0, &ne)) {
+    if (threadIdx.x == 0) issue(l0, 0);
+    pending[0] = true;
+  }
+  for (uint32_t l = l0; l < l1; ++l) {
+    const uint32_t buf = (l - l0) & 1u;
+    if (!giveup && l + 1 < l1 && fits(l + 1, &e0, &ne)) {
+      if (threadIdx.x == 0) issue(l + 1, buf ^ 1u);
+      pending[buf ^ 1u] = true;
+    }
+    const bool staged = fits(l, &e0, &ne) && pending[buf] && !giveup;
+    bool ready = false;
+    if (staged) {
+      ready = true;
+      for (uint32_t polls = 0; !mbar_try_wait(&s_bar[buf], phase[buf]);)
+        if (++polls >= STAGE_POLLS) {  // give up staging: global records from here on
+          atomicOr(err, DEVERR_TIMEOUT);
+          s_giveup = 1;
+          ready = false;
+          break;
+        }
+      if (ready) {
+        phase[buf] ^= 1u;
+        pending[buf] = false;
+      }
+    }
+    // records through shared memory when staged, else from global memory;
+    // erec indices stay global: the staged copy starts at record e0
+    const uint4* it_src = ready ? s_item[buf] - lvl[l] : item;
+    const uint2* er_src = ready ? s_erec[buf] - e0 : erec;
+    const uint32_t i1 = lvl[l + 1];
+    if (warp_live)
+      for (uint32_t ii = lvl[l] + slot; ii < i1; ii += slots) {
+        const uint4 it = it_src[ii];
+        const uint2 r0 = it.y + t < it.z ? er_src[it.y + t] : make_uint2(0, 0);
+        gated16_item<true>(it, r0, er_src, slab, Kp, active, thr, lane, live, valid_lanes,
+                           seeded, err);
+      }
+    __syncthreads();
+    giveup = s_giveup != 0;
+  }
+  // no copy may still be writing this block's shared memory when it exits:
+  // wait (bounded) for any copy issued but not consumed
+  for (uint32_t b = 0; b < 2; ++b)
+    if (pending[b])
+      for (uint32_t polls = 0; !mbar_try_wait(&s_bar[b], phase[b]) && polls < STAGE_POLLS;)
+        ++polls;
+}
+
 // A whole 16-bit gated wave sweep in one cooperative launch (waves of at most
 // 4096 lanes): the blocks walk the level program, a level's items spread
 // over the grid's item slots or a run of small levels swept by block 0
@@ -898,10 +1043,17 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
           uint32_t l1 = l + 1;
           while (l1 < g->n_levels && sc.lvl_item[l1 + 1] - sc.lvl_item[l1] <= small) ++l1;
           if (l1 - l >= 2) {
-            BF_CUDA(launch_level(k_sweep_run16, dim3(1), 1024, pdl, st, (const uint4*)sc.d_item,
-                                 (const uint32_t*)sc.d_lvl, l, l1, (const uint2*)sc.d_erec,
-                                 slab16, Kp, d_active, (const uint32_t*)(p_thr + s0), (uint32_t)kw,
-                                 (const uint32_t*)d_seeded, g->d_err));
+            if (g->tune.staged && sc.lvl_erec_ready)
+              BF_CUDA(launch_level(k_sweep_run16_staged, dim3(1), 1024, pdl, st,
+                                   (const uint4*)sc.d_item, (const uint32_t*)sc.d_lvl,
+                                   (const uint32_t*)sc.d_lvl_erec, l, l1, (const uint2*)sc.d_erec,
+                                   slab16, Kp, d_active, (const uint32_t*)(p_thr + s0),
+                                   (uint32_t)kw, (const uint32_t*)d_seeded, g->d_err));
+            else
+              BF_CUDA(launch_level(k_sweep_run16, dim3(1), 1024, pdl, st, (const uint4*)sc.d_item,
+                                   (const uint32_t*)sc.d_lvl, l, l1, (const uint2*)sc.d_erec,
+                                   slab16, Kp, d_active, (const uint32_t*)(p_thr + s0),
+                                   (uint32_t)kw, (const uint32_t*)d_seeded, g->d_err));
             ++launches;
             l = l1 - 1;
             continue;

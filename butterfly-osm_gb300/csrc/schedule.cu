@@ -538,7 +538,7 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
   sc.valid = false;
   const bool two = g->has_len;
   if ((rc = ensure_dev(&sc.d_item, sc.cap_items, n_i, g)) ||
-      (rc = ensure_dev(&sc.d_erec, sc.cap_edges, n_e, g)) ||
+      (rc = ensure_dev(&sc.d_erec, sc.cap_edges, n_e + 2, g)) ||
       (two && (rc = ensure_dev(&sc.d_elen, sc.cap_elen, n_e, g))) ||
       (rc = ensure_dev(&sc.d_trow, sc.cap_t, T, g)) ||
       (rc = ensure_dev(&sc.d_lvl, sc.cap_lvl, (size_t)L + 1, g)) ||
@@ -566,6 +566,7 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
   sc.tgt.assign(h_tgt, h_tgt + T);
   sc.uses = 0;
   sc.dev_built = true;
+  sc.lvl_erec_ready = false;
   sc.peel_left = s.h_back[3];
   sc.ranks.clear();
   sc.cidx_ready = true;

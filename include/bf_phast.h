@@ -198,6 +198,12 @@ typedef struct bf_tune {
                                   walking all levels (grid barriers with a
                                   deadline: BF_ERR_TIMEOUT if one runs out);
                                   clear: one launch per level                    */
+  uint32_t staged_levels;      /* 1: runs of small levels of 16-bit isochrone
+                                  waves bulk-copy each level's work items and
+                                  edge records into shared memory (cp.async.bulk
+                                  with an mbarrier) while the previous level is
+                                  swept; 0: the records are read from global
+                                  memory (same results)                          */
 } bf_tune;
 
 /* Time candidate tunables on a sample matrix (device buffers: d_sources,

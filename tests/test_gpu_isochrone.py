@@ -115,3 +115,20 @@ def test_16bit_boundary_thresholds(built, grid100):
         bits, counts = g.isochrone_bitsets(origins, thr)
         want_bits, want_counts = c.isochrone_bitsets(origins, thr)
         assert np.array_equal(bits, want_bits) and np.array_equal(counts, want_counts)
+
+
+@pytest.mark.parametrize("lanes", [64, 256, 1024])
+def test_staged_levels_match_oracle(built, country_small, lanes):
+    """Runs of small levels whose items and edge records are bulk-copied into
+    shared memory give the oracle's bitsets, like the global-memory form."""
+    import workload
+    _, cch = country_small
+    c = orc.Cch.from_dict(cch)
+    g = _graph(cch)
+    origins, thr = workload.isochrone_workload(cch["n"], min(lanes, 96) + 3, seed=lanes + 1)
+    want_bits, want_counts = c.isochrone_bitsets(origins, thr)
+    for staged in (1, 0):
+        g.set_tune(isochrone_lanes=lanes, staged_levels=staged)
+        bits, counts = g.isochrone_bitsets(origins, thr)
+        assert np.array_equal(bits, want_bits), staged
+        assert np.array_equal(counts, want_counts), staged
