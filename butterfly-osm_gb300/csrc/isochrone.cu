@@ -650,73 +650,74 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// 16-bit form of k_bits: lane tiles of 64, a thread loads two lanes, so a
-// warp reads one 128-byte line per slab row. Lanes hold 0xFFFF beyond their
+// 16-bit form of k_bits, written for the output's layout: a block owns
+// 2048 ranks x 64 lanes, so every lane's 64 words (256 bytes) of output are
+// written as one contiguous run (each origin's bitset row is 1.5 MB long on
+// the country graph; 32-byte pieces scattered over a wave's rows cost more
+// than the rest of the wave). A warp takes 32 ranks at a time: each thread
+// loads its rank's row of 64 lanes (128 bytes, active rows only), and 64
+// ballots turn the 32 x 64 lane values into one word per lane, staged in
+// shared memory and written lane by lane. Lanes hold 0xFFFF beyond their
 // threshold (the sweep and the upward pass clamp), so a bit is just
 // "not 0xFFFF" on an active row.
-constexpr uint32_t TILE_L16 = 64;
+constexpr uint32_t BT_RANKS = 2048;  // ranks per block: 64 words per lane
+constexpr uint32_t BT_LANES = 64;    // lanes per block
 
 __global__ void __launch_bounds__(256)
     k_bits16(const uint16_t* __restrict__ slab, uint32_t Kp, const uint32_t* __restrict__ cidx,
              uint32_t n, uint32_t kw, uint32_t* __restrict__ bits, uint64_t w32,
              unsigned long long* __restrict__ counts, const uint32_t* __restrict__ active,
              const uint32_t* __restrict__ out_row) {
-  __shared__ uint32_t tile[TILE_R][TILE_L16 / 2 + 1];  // two lanes per word
-  __shared__ uint32_t srow[TILE_R];
-  __shared__ int any_active;
-  const uint32_t r0 = blockIdx.x * TILE_R;
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) any_active = 0;
-  __syncthreads();
-  {
-    const uint32_t rank = r0 + threadIdx.x;
+  __shared__ uint32_t sw[BT_LANES][BT_RANKS / 32 + 1];
+  const uint32_t r0 = blockIdx.x * BT_RANKS, l0 = blockIdx.y * BT_LANES;
+  const uint32_t warp = threadIdx.x >> 5, t = threadIdx.x & 31;
+  const unsigned FULL = 0xFFFFFFFFu;
+  for (uint32_t gi = warp; gi < BT_RANKS / 32; gi += 8) {
+    const uint32_t rank = r0 + gi * 32 + t;
     uint32_t row = NONE;
     if (rank < n) {
       const uint32_t c = cidx[rank];
       if ((active[c >> 5] >> (c & 31)) & 1u) row = c;
     }
-    srow[threadIdx.x] = row;
-    if (__any_sync(0xFFFFFFFFu, row != NONE) && lane == 0) any_active = 1;
+    if (!__any_sync(FULL, row != NONE)) {  // no active rank here: zero words
+      sw[t][gi] = 0;
+      sw[t + 32][gi] = 0;
+      continue;
+    }
+    uint4 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      v[q] = (row != NONE && l0 + 8 * q < Kp)
+                 ? *reinterpret_cast<const uint4*>(slab + (size_t)row * Kp + l0 + 8 * q)
+                 : make_uint4(~0u, ~0u, ~0u, ~0u);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint32_t w4[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
+#pragma unroll
+      for (int h = 0; h < 8; ++h) {
+        const uint32_t d = (w4[h >> 1] >> ((h & 1) * 16)) & 0xFFFFu;
+        const uint32_t word = __ballot_sync(FULL, d != 0xFFFFu);
+        const uint32_t j = 8 * q + h;  // lane within the block
+        if (t == (j & 31)) sw[j][gi] = word;
+      }
+    }
   }
   __syncthreads();
-  const bool live = any_active != 0;
-  const uint64_t wbase = r0 / 32;
-  const uint32_t lend = min(kw, (blockIdx.y + 1) * TILE_L16 * LANE_TILES_PER_BLOCK);
-  for (uint32_t l0 = blockIdx.y * TILE_L16 * LANE_TILES_PER_BLOCK; l0 < lend; l0 += TILE_L16) {
-    if (live) {
-      for (uint32_t r = warp; r < TILE_R; r += 8) {
-        const uint32_t row = srow[r], l = l0 + 2 * lane;  // even: 4-byte aligned
-        tile[r][lane] = (row != NONE && l < lend)
-                            ? *reinterpret_cast<const uint32_t*>(slab + (size_t)row * Kp + l)
-                            : 0xFFFFFFFFu;
-      }
-      __syncthreads();
-    }
-    for (uint32_t q = 0; q < 8; ++q) {
-      const uint32_t li = warp * 8 + q, l = l0 + li;
-      if (l >= lend) continue;  // warp-uniform
-      const uint64_t orow = out_row[l];
-      uint32_t mine = 0;
-      if (live) {
-        for (uint32_t c = 0; c < TILE_R / 32; ++c) {
-          const uint32_t wd = tile[c * 32 + lane][li >> 1];
-          const uint32_t d = (li & 1) ? (wd >> 16) : (wd & 0xFFFFu);
-          const uint32_t word = __ballot_sync(0xFFFFFFFFu, d != 0xFFFFu);
-          if (lane == c) mine = word;
-        }
-      }
-      const uint64_t wi = wbase + lane;
-      uint32_t pc = 0;
-      if (lane < TILE_R / 32 && wi < w32) {
-        bits[orow * w32 + wi] = mine;
-        pc = __popc(mine);
-      }
-      if (live) {
-        for (int o = 16; o > 0; o >>= 1) pc += __shfl_down_sync(0xFFFFFFFFu, pc, o);
-        if (lane == 0 && pc) atomicAdd(&counts[orow], (unsigned long long)pc);
+  const uint32_t nl = kw > l0 ? min(BT_LANES, kw - l0) : 0u;
+  const uint64_t wbase = r0 >> 5;
+  for (uint32_t j = warp; j < nl; j += 8) {
+    const uint64_t orow = out_row[l0 + j];
+    uint32_t pc = 0;
+    for (uint32_t k = t; k < BT_RANKS / 32; k += 32) {
+      const uint64_t wi = wbase + k;
+      if (wi < w32) {
+        const uint32_t word = sw[j][k];
+        bits[orow * w32 + wi] = word;
+        pc += __popc(word);
       }
     }
-    if (live) __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) pc += __shfl_down_sync(FULL, pc, o);
+    if (t == 0 && pc) atomicAdd(&counts[orow], (unsigned long long)pc);
   }
 }
 
@@ -1092,8 +1093,8 @@ bf_status isochrone_bitsets(Graph* g, Ctx& c, const uint32_t* d_orig, const uint
     dim3 bgrid((unsigned)((g->n + TILE_R - 1) / TILE_R),
                (unsigned)((kw + TILE_L * LANE_TILES_PER_BLOCK - 1) / (TILE_L * LANE_TILES_PER_BLOCK)));
     if (half) {
-      dim3 bg16(bgrid.x, (unsigned)((kw + TILE_L16 * LANE_TILES_PER_BLOCK - 1) /
-                                    (TILE_L16 * LANE_TILES_PER_BLOCK)));
+      dim3 bg16((unsigned)((g->n + BT_RANKS - 1) / BT_RANKS),
+                (unsigned)((kw + BT_LANES - 1) / BT_LANES));
       k_bits16<<<bg16, 256, 0, st>>>(slab16, Kp, sc.d_cidx, g->n, (uint32_t)kw,
                                      reinterpret_cast<uint32_t*>(d_bits), 2 * w64,
                                      reinterpret_cast<unsigned long long*>(d_counts), d_active,
