@@ -490,6 +490,12 @@ def run_isochrones(g, cch, count, seed=42):
     d_o = torch.from_numpy(o.view(np.int32)).cuda()
     d_t = torch.from_numpy(t.view(np.int32)).cuda()
     stream = torch.cuda.current_stream()
+    # wave width and form tuned on another sample of the same shape
+    to, tt = workload.isochrone_workload(n, min(count, 4096), seed=seed + 1000)
+    d_to = torch.from_numpy(to.view(np.int32)).cuda()
+    d_tt = torch.from_numpy(tt.view(np.int32)).cuda()
+    tune = g.autotune_isochrones(d_to.data_ptr(), d_tt.data_ptr(), len(to), reps=1)
+    del d_to, d_tt
     g.isochrone_bitsets_device(d_o.data_ptr(), d_t.data_ptr(), min(count, 1024),
                                d_b.data_ptr(), d_c.data_ptr())  # warm-up
     torch.cuda.synchronize()
@@ -531,6 +537,9 @@ def run_isochrones(g, cch, count, seed=42):
             "mean_reachable_nodes": round(float(counts.mean()), 1),
             "thresholds_s": list(workload.ISO_THRESHOLDS_S),
             "waves": int(waves), "lanes_per_wave": int(lanes),
+            "tune": {"isochrone_lanes": tune["isochrone_lanes"],
+                     "persistent_waves": bool(tune["persistent_sweep"] & 2),
+                     "candidates": tune["tried"], "sample_ms": round(tune["step_ms"], 2)},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
                          "peak_kind": peak_kind, "kernel": "k_sweep_gated16 (all waves)",

@@ -166,6 +166,11 @@ _SIGNATURES = {
                                    ctypes.POINTER(Tune)]),
     "bf_set_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tune)]),
     "bf_get_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tune)]),
+    "bf_autotune_isochrones": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_uint64, ctypes.c_uint32,
+                                              ctypes.POINTER(Tune)]),
+    "bf_tune_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "bf_tune_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "bf_query_batch": (ctypes.c_int, [ctypes.c_void_p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
                                       _u32p]),
     "bf_phast_query": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _u32p]),
@@ -375,6 +380,19 @@ class Graph:
         t = Tune()
         _check(load().bf_get_tune(self._h, ctypes.byref(t)))
         return t.as_dict()
+
+    def autotune_isochrones(self, d_orig, d_thr, n, reps=2):
+        """Time bulk-isochrone candidates on a device-resident sample; keeps the best."""
+        t = Tune()
+        _check(load().bf_autotune_isochrones(self._h, ctypes.c_void_p(d_orig),
+                                             ctypes.c_void_p(d_thr), n, reps, ctypes.byref(t)))
+        return t.as_dict()
+
+    def tune_save(self, path):
+        _check(load().bf_tune_save(self._h, str(path).encode()))
+
+    def tune_load(self, path):
+        _check(load().bf_tune_load(self._h, str(path).encode()))
 
     def query_batch(self, sources, threshold=INF):
         s = _u32(sources)

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cstring>
 #include <new>
 
@@ -396,6 +397,181 @@ bf_status bf_autotune(bf_graph* h, const uint32_t* d_src, uint64_t S, const uint
   best->step_ms = best_ms;
   best->tried = tried;
   return BF_OK;
+}
+
+bf_status bf_autotune_isochrones(bf_graph* h, const uint32_t* d_orig, const uint32_t* d_thr,
+                                 uint64_t n, uint32_t reps, bf_tune* best) {
+  if (!h || !d_orig || !d_thr || !n || !best) {
+    set_error("bf_autotune_isochrones: null argument or empty sample");
+    return BF_ERR_INVALID;
+  }
+  Graph* g = &h->g;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (cudaSetDevice(g->device) != cudaSuccess) return cuda_status(cudaGetLastError(), "cudaSetDevice");
+  if (reps == 0) reps = 2;
+  cudaStream_t s = g->stream;
+  const uint64_t w64 = (g->n + 63) / 64;
+  DevBuf bits, counts;
+  bf_status rc;
+  if ((rc = bits.alloc(n * w64 * 8)) || (rc = counts.alloc(n * 8))) return rc;
+  const Tune saved = g->tune;
+  // wave widths (origins per wave) and the persistent form of the waves
+  std::vector<Tune> cands;
+  for (uint32_t lanes : {256u, 512u, 1024u, 2048u})
+    for (uint32_t pers : {0u, 2u}) {
+      if (lanes > ((n + 31) & ~31ull) && lanes != 256u) continue;  // wider than the sample
+      Tune t = saved;
+      t.iso_lanes = lanes;
+      t.persist = (saved.persist & 1u) | pers;
+      cands.push_back(t);
+    }
+  double best_ms = 1e300;
+  Tune best_t = saved;
+  for (const Tune& t : cands) {
+    g->tune = t;
+    double sum = 0;
+    for (uint32_t r = 0; r <= reps; ++r) {
+      bf_stats st{};
+      BF_CUDA(cudaEventRecord(g->ev[4], s));
+      rc = isochrone_bitsets(g, g->ctx, d_orig, d_thr, n, bits.as<uint64_t>(),
+                             counts.as<uint64_t>(), s, nullptr);
+      if (rc == BF_OK) rc = check_device_error(g, s);
+      if (rc != BF_OK) {
+        g->tune = saved;
+        return rc;
+      }
+      BF_CUDA(cudaEventRecord(g->ev[5], s));
+      BF_CUDA(cudaEventSynchronize(g->ev[5]));
+      float ms = 0;
+      BF_CUDA(cudaEventElapsedTime(&ms, g->ev[4], g->ev[5]));
+      if (r) sum += ms;
+    }
+    if (sum / reps < best_ms) {
+      best_ms = sum / reps;
+      best_t = t;
+    }
+  }
+  g->tune = best_t;
+  *best = to_c(best_t);
+  best->step_ms = best_ms;
+  best->tried = (uint32_t)cands.size();
+  return BF_OK;
+}
+
+// A tune cache file: one JSON object with the graph's fingerprint and the
+// tunables. The fingerprint is the graph's counts and an FNV-1a hash of its
+// level sizes, so a cache is applied only to the graph it was measured on.
+namespace {
+
+uint64_t graph_fingerprint(const Graph* g) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&h](uint64_t v) {
+    for (int i = 0; i < 8; ++i) {
+      h ^= (v >> (8 * i)) & 0xFF;
+      h *= 1099511628211ull;
+    }
+  };
+  mix(g->n);
+  mix(g->n_up);
+  mix(g->n_down);
+  mix(g->n_levels);
+  mix(g->max_depth);
+  for (uint32_t v : g->lvl_start) mix(v);
+  return h;
+}
+
+const char* const TUNE_KEYS[] = {"threads_per_block", "edges_per_item", "graph_capture",
+                                 "lanes_per_wave",    "isochrone_lanes", "small_level_rows",
+                                 "small_level_edges", "overlap_levels",  "isochrone_16bit",
+                                 "overlap_upward",    "mapped_output",   "hub_l2_mb",
+                                 "device_schedule",   "persistent_sweep", "staged_levels"};
+
+void tune_fields(bf_tune& t, uint32_t* f[15]) {
+  uint32_t* p[15] = {&t.threads_per_block, &t.edges_per_item, &t.graph_capture,
+                     &t.lanes_per_wave,    &t.isochrone_lanes, &t.small_level_rows,
+                     &t.small_level_edges, &t.overlap_levels,  &t.isochrone_16bit,
+                     &t.overlap_upward,    &t.mapped_output,   &t.hub_l2_mb,
+                     &t.device_schedule,   &t.persistent_sweep, &t.staged_levels};
+  for (int i = 0; i < 15; ++i) f[i] = p[i];
+}
+
+}  // namespace
+
+bf_status bf_tune_save(const bf_graph* h, const char* path) {
+  if (!h || !path) {
+    set_error("bf_tune_save: null argument");
+    return BF_ERR_INVALID;
+  }
+  bf_tune t = to_c(h->g.tune);
+  uint32_t* f[15];
+  tune_fields(t, f);
+  std::string js = "{\"graph\": \"" + std::to_string(graph_fingerprint(&h->g)) + "\"";
+  for (int i = 0; i < 15; ++i) js += ", \"" + std::string(TUNE_KEYS[i]) + "\": " + std::to_string(*f[i]);
+  js += "}\n";
+  FILE* fp = std::fopen(path, "w");
+  if (!fp) {
+    set_error(std::string("bf_tune_save: cannot write ") + path);
+    return BF_ERR_INVALID;
+  }
+  const bool ok = std::fwrite(js.data(), 1, js.size(), fp) == js.size();
+  if (std::fclose(fp) != 0 || !ok) {
+    set_error(std::string("bf_tune_save: write to ") + path + " failed");
+    return BF_ERR_INVALID;
+  }
+  return BF_OK;
+}
+
+bf_status bf_tune_load(bf_graph* h, const char* path) {
+  if (!h || !path) {
+    set_error("bf_tune_load: null argument");
+    return BF_ERR_INVALID;
+  }
+  FILE* fp = std::fopen(path, "r");
+  if (!fp) {
+    set_error(std::string("bf_tune_load: cannot read ") + path);
+    return BF_ERR_INVALID;
+  }
+  std::string js;
+  char buf[512];
+  for (size_t k; (k = std::fread(buf, 1, sizeof(buf), fp)) > 0;) js.append(buf, k);
+  std::fclose(fp);
+  auto value_of = [&js](const std::string& key, std::string* out) {
+    const std::string pat = "\"" + key + "\":";
+    const size_t at = js.find(pat);
+    if (at == std::string::npos) return false;
+    size_t i = at + pat.size();
+    while (i < js.size() && (js[i] == ' ' || js[i] == '"')) ++i;
+    size_t j = i;
+    while (j < js.size() && js[j] >= '0' && js[j] <= '9') ++j;
+    if (j == i) return false;
+    *out = js.substr(i, j - i);
+    return true;
+  };
+  std::string v;
+  if (!value_of("graph", &v) || v != std::to_string(graph_fingerprint(&h->g))) {
+    set_error(std::string("bf_tune_load: ") + path + " holds no tunables for this graph");
+    return BF_ERR_INVALID;
+  }
+  bf_tune t{};
+  {
+    std::lock_guard<std::mutex> lk(h->g.mu);
+    t = to_c(h->g.tune);
+  }
+  uint32_t* f[15];
+  tune_fields(t, f);
+  for (int i = 0; i < 15; ++i) {
+    if (!value_of(TUNE_KEYS[i], &v) || v.size() > 10) {
+      set_error(std::string("bf_tune_load: ") + path + " lacks " + TUNE_KEYS[i]);
+      return BF_ERR_INVALID;
+    }
+    const unsigned long long x = std::stoull(v);
+    if (x > 0xFFFFFFFFull) {
+      set_error(std::string("bf_tune_load: ") + TUNE_KEYS[i] + " out of range");
+      return BF_ERR_INVALID;
+    }
+    *f[i] = (uint32_t)x;
+  }
+  return bf_set_tune(h, &t);
 }
 
 bf_status bf_matrix(bf_graph* h, const uint32_t* src, uint64_t S, const uint32_t* tgt, uint64_t T,

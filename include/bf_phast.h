@@ -216,6 +216,24 @@ bf_status bf_autotune(bf_graph* g, const uint32_t* d_sources, uint64_t n_sources
 bf_status bf_set_tune(bf_graph* g, const bf_tune* t);
 bf_status bf_get_tune(const bf_graph* g, bf_tune* t);
 
+/* Time bulk-isochrone candidates on a device-resident sample of n origins
+ * and thresholds (isochrone_lanes in {256, 512, 1024, 2048} up to the sample
+ * size, with and without persistent waves, bit 1 of persistent_sweep) and
+ * keep the fastest for this graph; the other tunables are left as they are.
+ * No reference counterpart: the reference's isochrone batch width is the
+ * fixed K_LANES (route/src/range/batched_isochrone.rs). */
+bf_status bf_autotune_isochrones(bf_graph* g, const uint32_t* d_origins,
+                                 const uint32_t* d_thresholds, uint64_t n, uint32_t reps,
+                                 bf_tune* best);
+
+/* Tune cache: write the graph's current tunables to a JSON file keyed by a
+ * fingerprint of the graph (node and edge counts, levels, depth and the
+ * level sizes), and apply such a file to a graph; a file written for
+ * another graph, or incomplete, is refused with BF_ERR_INVALID. No
+ * reference counterpart. */
+bf_status bf_tune_save(const bf_graph* g, const char* path);
+bf_status bf_tune_load(bf_graph* g, const char* path);
+
 /* Distances from k sources to every node: dist_out[lane * n_nodes + node]
  * (the AoS Vec<Vec<u32>> of query_batch). threshold == BF_INF is unbounded;
  * otherwise entries above the threshold are BF_INF. k is at most 128. */

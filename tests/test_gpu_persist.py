@@ -86,3 +86,44 @@ def test_barrier_deadline_reports_timeout(built, grid100):
     bits, _ = g.isochrone_bitsets(origins, thr)
     wb, _ = c.isochrone_bitsets(origins, thr)
     assert np.array_equal(bits, wb)
+
+
+def test_isochrone_autotune_and_tune_cache(built, country_small, tmp_path):
+    """bf_autotune_isochrones keeps the fastest wave form; the tune cache
+    restores it on the same graph and refuses another graph's."""
+    import torch
+
+    import bfphast
+    import workload
+    _, cch = country_small
+    c = orc.Cch.from_dict(cch)
+    g = bfphast.Graph.from_cch(cch)
+    origins, thr = workload.isochrone_workload(cch["n"], 600, seed=17)
+    d_o = torch.from_numpy(origins.view(np.int32)).cuda()
+    d_t = torch.from_numpy(thr.view(np.int32)).cuda()
+    best = g.autotune_isochrones(d_o.data_ptr(), d_t.data_ptr(), len(origins), reps=1)
+    assert best["tried"] >= 2 and best["isochrone_lanes"] in (256, 512, 1024, 2048)
+    bits, counts = g.isochrone_bitsets(origins[:50], thr[:50])
+    wb, wc = c.isochrone_bitsets(origins[:50], thr[:50])
+    assert np.array_equal(bits, wb) and np.array_equal(counts, wc)
+    path = tmp_path / "tune.json"
+    g.tune_save(path)
+    h = bfphast.Graph.from_cch(cch)
+    h.tune_load(path)
+    got = h.get_tune()
+    for k in ("isochrone_lanes", "persistent_sweep", "threads_per_block", "edges_per_item"):
+        assert got[k] == best[k], k
+    _, other = (None, _chain_like())
+    o = bfphast.Graph.from_cch(other)
+    with pytest.raises(bfphast.BfError) as e:
+        o.tune_load(path)
+    assert e.value.status == bfphast.BF_ERR_INVALID
+
+
+def _chain_like():
+    n = 64
+    up_off = np.minimum(np.arange(n + 1), n - 1).astype(np.uint64)
+    down_off = np.concatenate([[0], np.arange(n)]).astype(np.uint64)
+    return dict(n=n, up_off=up_off, up_tgt=np.arange(1, n, dtype=np.uint32),
+                up_w=np.ones(n - 1, np.uint32), down_off=down_off,
+                down_tgt=np.arange(0, n - 1, dtype=np.uint32), down_w=np.ones(n - 1, np.uint32))
