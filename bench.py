@@ -63,6 +63,9 @@ def parse():
                     help="timed steps with a new target set each (0 = skip)")
     ap.add_argument("--plain-sources", type=int, default=1000,
                     help="plain-engine matrix side (sources = targets, K = 32)")
+    ap.add_argument("--level-table", default="",
+                    help="write the matrix schedule's per-level items / edges / rows (JSON) "
+                         "to this path, to attribute profiled sweep launches to levels")
     ap.add_argument("--isochrones", type=int, default=100000,
                     help="bulk isochrone origins (0 = skip)")
     ap.add_argument("--no-tiles", action="store_true",
@@ -257,6 +260,12 @@ def run_ours(args, rank, world, dist):
             "alg_bytes_per_sweep": alg_bytes, "sweep_ms": round(st["downward_ms"], 3),
             "swept_nodes": N, "swept_edges": M, "lanes": K}
 
+    if args.level_table:
+        items, edges, rows = g.schedule_levels()
+        keep = items > 0  # launches go to levels with work items, in order
+        pathlib.Path(args.level_table).write_text(json.dumps({
+            "lanes": int(st["lanes"]), "items": items[keep].tolist(),
+            "edges": edges[keep].tolist(), "rows": rows[keep].tolist()}))
     # plain GPU sweep on its own workload (1000 x 1000, K = 32 batches): the
     # >= 10x denominator, CUDA events on the launching stream
     plain = run_plain(g, src, tgt, out_dev, args.plain_sources, stream)

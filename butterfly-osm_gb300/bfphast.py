@@ -169,6 +169,8 @@ _SIGNATURES = {
     "bf_autotune_isochrones": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_uint64, ctypes.c_uint32,
                                               ctypes.POINTER(Tune)]),
+    "bf_schedule_levels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _u64p, _u64p, _u64p,
+                                          ctypes.POINTER(ctypes.c_uint32)]),
     "bf_tune_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "bf_tune_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "bf_query_batch": (ctypes.c_int, [ctypes.c_void_p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
@@ -387,6 +389,15 @@ class Graph:
         _check(load().bf_autotune_isochrones(self._h, ctypes.c_void_p(d_orig),
                                              ctypes.c_void_p(d_thr), n, reps, ctypes.byref(t)))
         return t.as_dict()
+
+    def schedule_levels(self):
+        """(items, edges, rows) per level of the last restricted matrix schedule."""
+        cap = self.info()["n_levels"]
+        a = [np.zeros(cap, np.uint64) for _ in range(3)]
+        L = ctypes.c_uint32()
+        _check(load().bf_schedule_levels(self._h, cap, _ptr(a[0], _u64p), _ptr(a[1], _u64p),
+                                         _ptr(a[2], _u64p), ctypes.byref(L)))
+        return [x[:L.value] for x in a]
 
     def tune_save(self, path):
         _check(load().bf_tune_save(self._h, str(path).encode()))

@@ -399,6 +399,28 @@ bf_status bf_autotune(bf_graph* h, const uint32_t* d_src, uint64_t S, const uint
   return BF_OK;
 }
 
+bf_status bf_schedule_levels(const bf_graph* h, uint32_t cap, uint64_t* items, uint64_t* edges,
+                             uint64_t* rows, uint32_t* n_levels) {
+  if (!h || !n_levels || (cap && (!items || !edges || !rows))) {
+    set_error("bf_schedule_levels: null argument");
+    return BF_ERR_INVALID;
+  }
+  const Sched& sc = h->g.ctx.sc;
+  if (!sc.valid || sc.lvl_item.size() < 2 || sc.lvl_row.size() != sc.lvl_item.size() ||
+      sc.lvl_edge.size() != sc.lvl_item.size()) {
+    set_error("bf_schedule_levels: no target-restricted schedule built yet");
+    return BF_ERR_INVALID;
+  }
+  const uint32_t L = (uint32_t)sc.lvl_item.size() - 1;
+  *n_levels = L;
+  for (uint32_t l = 0; l < std::min(cap, L); ++l) {
+    items[l] = sc.lvl_item[l + 1] - sc.lvl_item[l];
+    edges[l] = sc.lvl_edge[l + 1] - sc.lvl_edge[l];
+    rows[l] = sc.lvl_row[l + 1] - sc.lvl_row[l];
+  }
+  return BF_OK;
+}
+
 bf_status bf_autotune_isochrones(bf_graph* h, const uint32_t* d_orig, const uint32_t* d_thr,
                                  uint64_t n, uint32_t reps, bf_tune* best) {
   if (!h || !d_orig || !d_thr || !n || !best) {

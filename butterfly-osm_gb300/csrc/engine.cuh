@@ -192,6 +192,8 @@ struct Sched {
   size_t cap_uses = 0;
   uint32_t* d_hub_h = nullptr;   // hub histogram (65536 bins) and threshold
   size_t cap_hub_h = 0;
+  std::vector<uint32_t> lvl_row;   // level -> first row, n_levels + 1
+  std::vector<uint32_t> lvl_edge;  // level -> first edge record, n_levels + 1
   uint32_t* d_lvl_erec = nullptr;  // [levels + 1] level -> first edge record (host builds)
   size_t cap_lvl_erec = 0;
   bool lvl_erec_ready = false;

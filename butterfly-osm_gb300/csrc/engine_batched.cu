@@ -303,6 +303,8 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   std::vector<uint32_t> lvl_erec(g->n_levels + 1);
   for (uint32_t l = 0; l <= g->n_levels; ++l) lvl_erec[l] = (uint32_t)eoff[row_lvl[l]];
   sc.lvl_erec_ready = true;
+  sc.lvl_row = row_lvl;
+  sc.lvl_edge = lvl_erec;
   // rows by gather count, most-used first (up to 65536 of them): the matrix
   // sweep keeps the head of this list in L2. A counting sort by count; the
   // full-graph schedule (isochrones, bounded queries) does not use it.

@@ -277,6 +277,13 @@ __global__ void __launch_bounds__(SCAN_TPB)
   if (threadIdx.x == 0) lvl_item[L] = carry;
 }
 
+// Per level: first row and first edge record (for the per-level table).
+__global__ void k_sd_lvledge(const uint32_t* __restrict__ lvlrow, const uint64_t* __restrict__ rpre,
+                             uint32_t L, uint32_t* __restrict__ lvl_edge) {
+  const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l <= L) lvl_edge[l] = (uint32_t)rpre[lvlrow[l]];
+}
+
 // 4a. Edge records, work items and gather counts, one thread per row.
 __global__ void __launch_bounds__(256)
     k_sd_fill(const uint32_t* __restrict__ rowpos, const uint32_t* __restrict__ n_r_p,
@@ -466,7 +473,7 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
     set_error("device schedule: level table missing");
     return BF_ERR_DEVICE;
   }
-  const size_t back = 4 + (size_t)L + 1;
+  const size_t back = 4 + 3 * ((size_t)L + 1);
   if (back > s.back_words) {
     if (s.h_back) cudaFreeHost(s.h_back);
     s.h_back = nullptr;
@@ -519,11 +526,17 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
   k_scan_top<uint64_t><<<1, SCAN_TPB, 0, st>>>(s.bsum64, nbr);
   k_scan_out<uint64_t><<<nbr, SCAN_TPB, 0, st>>>(uv, 0, d_nr, s.bsum64, nbr, s.rpre);
   k_sd_cursor<<<1, SCAN_TPB, 0, st>>>(s.hist, L, cfg.s1, s.lvl_item);
+  // level -> first edge record, into the peeling frontier (free by now)
+  k_sd_lvledge<<<(L + 1 + 255) / 256, 256, 0, st>>>(s.lvlrow, s.rpre, L, s.front);
   BF_CUDA(cudaGetLastError());
   // read back: n_r, total (edges | items << 32), peel rounds used, level items
   BF_CUDA(cudaMemcpyAsync(s.h_back, d_nr, 4, cudaMemcpyDeviceToHost, st));
   BF_CUDA(cudaMemcpyAsync(s.h_back + 1, s.bsum64 + nbr, 8, cudaMemcpyDeviceToHost, st));
   BF_CUDA(cudaMemcpyAsync(s.h_back + 3, s.meta + PEEL_ROUNDS, 4, cudaMemcpyDeviceToHost, st));
+  BF_CUDA(cudaMemcpyAsync(s.h_back + 4 + (L + 1), s.lvlrow, ((size_t)L + 1) * 4,
+                          cudaMemcpyDeviceToHost, st));
+  BF_CUDA(cudaMemcpyAsync(s.h_back + 4 + 2 * (L + 1), s.front, ((size_t)L + 1) * 4,
+                          cudaMemcpyDeviceToHost, st));
   BF_CUDA(cudaMemcpyAsync(s.h_back + 4, s.lvl_item, ((size_t)L + 1) * 4, cudaMemcpyDeviceToHost,
                           st));
   BF_CUDA(cudaStreamSynchronize(st));
@@ -558,6 +571,8 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
                           st));
   BF_CUDA(cudaGetLastError());
   sc.lvl_item.assign(s.h_back + 4, s.h_back + 4 + L + 1);
+  sc.lvl_row.assign(s.h_back + 4 + (L + 1), s.h_back + 4 + 2 * (L + 1));
+  sc.lvl_edge.assign(s.h_back + 4 + 2 * (L + 1), s.h_back + 4 + 3 * (L + 1));
   sc.n_r = n_r;
   sc.n_items = n_i;
   sc.n_edges = n_e;

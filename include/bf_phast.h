@@ -226,6 +226,13 @@ bf_status bf_autotune_isochrones(bf_graph* g, const uint32_t* d_origins,
                                  const uint32_t* d_thresholds, uint64_t n, uint32_t reps,
                                  bf_tune* best);
 
+/* Per level of the last target-restricted schedule of the graph's C-ABI
+ * matrix calls: work items, edge records and rows (first min(cap, levels)
+ * entries; *n_levels = levels). For profiling: the k-th launch of a sweep
+ * processes the k-th level with items. No reference counterpart. */
+bf_status bf_schedule_levels(const bf_graph* g, uint32_t cap, uint64_t* items, uint64_t* edges,
+                             uint64_t* rows, uint32_t* n_levels);
+
 /* Tune cache: write the graph's current tunables to a JSON file keyed by a
  * fingerprint of the graph (node and edge counts, levels, depth and the
  * level sizes), and apply such a file to a graph; a file written for

@@ -78,3 +78,24 @@ def test_device_then_host_schedule_on_one_graph(built, country_small):
         g.set_tune(device_schedule=k % 2)
         tgt = rng.choice(n, 200, replace=False).astype(np.uint32)
         assert np.array_equal(g.matrix(src, tgt), full[:, tgt]), k
+
+
+def test_schedule_levels_table(built, country_small):
+    """bf_schedule_levels reports the last restricted schedule per level: its
+    totals are the swept rows and edges, alike for both builders."""
+    import bfphast
+    _, cch = country_small
+    n = cch["n"]
+    rng = np.random.default_rng(5)
+    src = rng.choice(n, 8, replace=False).astype(np.uint32)
+    tgt = rng.choice(n, 400, replace=False).astype(np.uint32)
+    tables = []
+    for dev in (1, 0):
+        g = bfphast.Graph.from_cch(cch)
+        g.set_tune(device_schedule=dev)
+        _, st = g.matrix(src, tgt, stats=True)
+        items, edges, rows = g.schedule_levels()
+        assert int(rows.sum()) == st["swept_nodes"] and int(edges.sum()) == st["swept_edges"]
+        tables.append((items, edges, rows))
+    for a, b in zip(tables[0], tables[1]):
+        assert np.array_equal(a, b)
