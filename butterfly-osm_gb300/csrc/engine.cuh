@@ -266,6 +266,7 @@ struct Graph {
   uint32_t n = 0;
   uint64_t n_up = 0, n_down = 0;
   uint32_t n_levels = 0, max_depth = 0;
+  uint32_t max_runs = 0;  // most runs of consecutive ranks on one root path
   uint32_t engine = BF_ENGINE_BATCHED;
   uint32_t k_lanes = 0;
   std::atomic<uint64_t> device_bytes{0};

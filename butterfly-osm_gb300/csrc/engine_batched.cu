@@ -47,8 +47,10 @@ uint64_t hash_targets(const uint32_t* t, uint64_t T) {
   return h;
 }
 
+// Grow a device array to `need` elements (1/8 more with `slack`, for arrays
+// sized by a schedule's rows, items or edges, which vary between targets).
 template <class T>
-bf_status ensure(T** p, size_t& cap, size_t need, Graph* g) {
+bf_status ensure(T** p, size_t& cap, size_t need, Graph* g, bool slack = false) {
   if (need <= cap && *p) return BF_OK;
   if (*p) {
     cudaFree(*p);
@@ -56,7 +58,7 @@ bf_status ensure(T** p, size_t& cap, size_t need, Graph* g) {
   }
   *p = nullptr;
   cap = 0;
-  size_t n = std::max<size_t>(need, 1);
+  size_t n = std::max<size_t>(slack ? need + need / 8 : need, 1);
   if (cudaMalloc((void**)p, n * sizeof(T)) != cudaSuccess) {
     cudaGetLastError();
     *p = nullptr;
@@ -351,15 +353,15 @@ bf_status build_schedule(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_tgt, uin
   for (uint32_t p : R) c.rowmap[p] = NONE;
   bf_status s;
   if ((s = ensure(&sc.d_cidx, sc.cap_cidx, n, g))) return s;
-  if ((s = ensure(&sc.d_item, sc.cap_items, n_i, g))) return s;
+  if ((s = ensure(&sc.d_item, sc.cap_items, n_i, g, true))) return s;
   // two records of padding: a bulk copy of a level's records rounds its end
   // up to 16 bytes
-  if ((s = ensure(&sc.d_erec, sc.cap_edges, n_e + 2, g))) return s;
-  if (two && (s = ensure(&sc.d_elen, sc.cap_elen, n_e, g))) return s;
-  if ((s = ensure(&sc.d_trow, sc.cap_t, T, g))) return s;
-  if ((s = ensure(&c.d_pairs, c.cap_pairs, pairs.size() * 2, g))) return s;
+  if ((s = ensure(&sc.d_erec, sc.cap_edges, n_e + 2, g, true))) return s;
+  if (two && (s = ensure(&sc.d_elen, sc.cap_elen, n_e, g, true))) return s;
+  if ((s = ensure(&sc.d_trow, sc.cap_t, T, g, true))) return s;
+  if ((s = ensure(&c.d_pairs, c.cap_pairs, pairs.size() * 2, g, true))) return s;
   if ((s = ensure(&sc.d_split, sc.cap_split, split_bits.size(), g))) return s;
-  if ((s = ensure(&sc.d_lvl_erec, sc.cap_lvl_erec, lvl_erec.size(), g))) return s;
+  if ((s = ensure(&sc.d_lvl_erec, sc.cap_lvl_erec, lvl_erec.size(), g, true))) return s;
   BF_CUDA(cudaMemcpyAsync(sc.d_lvl_erec, lvl_erec.data(), lvl_erec.size() * 4,
                           cudaMemcpyHostToDevice, st));
   if ((s = ensure(&sc.d_lvl, sc.cap_lvl, sc.lvl_item.size(), g))) return s;
@@ -616,14 +618,26 @@ __global__ void __launch_bounds__(256)
 namespace bf {
 
 // Grow the context's distance slab to at least `need` bytes.
+// A slab that grows takes 1/16 more than asked when the budget allows:
+// restricted row counts vary by a few percent between target sets, and each
+// regrowth (cudaFree + cudaMalloc of gigabytes) stalls the stream.
 bf_status ensure_slab(Graph* g, Ctx& c, size_t need) {
   if (need <= c.slab_bytes) return BF_OK;
+  const size_t roomy = need + need / 16;
+  const size_t alloc = roomy <= ctx_budget(g, c) ? roomy : need;
   if (c.d_slab) {
     cudaFree(c.d_slab);
     g->device_bytes -= c.slab_bytes;
     c.d_slab = nullptr;
     c.slab_bytes = 0;
   }
+  if (alloc > need && cudaMalloc(&c.d_slab, alloc) == cudaSuccess) {
+    c.slab_bytes = alloc;
+    g->device_bytes += alloc;
+    return BF_OK;
+  }
+  cudaGetLastError();
+  c.d_slab = nullptr;
   if (cudaMalloc(&c.d_slab, need) != cudaSuccess) {
     cudaGetLastError();
     set_error("cannot allocate the batched distance slab (" + std::to_string(need) + " bytes)");

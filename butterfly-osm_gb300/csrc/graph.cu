@@ -243,6 +243,19 @@ static bf_status build_graph_impl(const bf_cch_csr* csr, const bf_config* cfg, G
     run_end[r] = (parent[r] == r + 1) ? run_end[r + 1] : r;
   }
   g->max_depth = maxd;
+  // runs of consecutive ranks on the longest (in runs) root path: r's path
+  // continues r + 1's run, or starts a run below its parent's path
+  {
+    std::vector<uint32_t> runs(n, 0);
+    uint32_t maxr = 0;
+    for (uint32_t r = n; r-- > 0;) {
+      if (parent[r] == NONE) runs[r] = 1;
+      else if (parent[r] == r + 1) runs[r] = runs[r + 1];
+      else runs[r] = runs[parent[r]] + 1;
+      maxr = std::max(maxr, runs[r]);
+    }
+    g->max_runs = maxr;
+  }
   // UP records, one per (source, target)
   std::vector<uint2> up_rec(g->n_up);
   std::vector<uint32_t> up_l(two ? g->n_up : 0);

@@ -15,9 +15,13 @@
 //                  row counts its out-edges into C (one atomic per in-edge of
 //                  a C row); rows with count 0 start a frontier, and every
 //                  dead row decrements its in-edge sources, which die at 0.
-//                  Rounds run until the frontier is empty (38 rounds for
+//                  All rounds run in one cooperative launch, separated by a
+//                  grid barrier, until the frontier is empty (38 rounds for
 //                  10 000 targets on the country graph); a row still alive
 //                  when the round limit ends it would only be swept in vain.
+//                  A row's in-edges are spread over a warp's lanes, 32 edges
+//                  a step (counting, peeling and the fill alike), so rows
+//                  with thousands of in-edges do not hold one thread.
 //   3. compaction  rows are the live positions in slab-position order, so
 //                  they come grouped by level; row(p) = popcount prefix of
 //                  the live bitmap. A scan gives each row its edge and work-
@@ -41,11 +45,19 @@ namespace bf {
 
 namespace {
 
-constexpr uint32_t PEEL_ROUNDS = 96;
+// Peeling rounds at most (10 000 targets on the country graph take 38).
+constexpr uint32_t PEEL_ROUNDS = 4096;
+// meta words: three rotating frontier sizes, the row count, the candidate
+// count, peeling rounds run and frontier left, the grid-barrier words
+constexpr uint32_t META_NR = 3, META_NC = 4, META_ROUNDS = 5, META_LEFT = 6, META_BAR = 8,
+                   META_WORDS = 16;
 constexpr uint32_t HUB_BINS = 65536;
 
+// Grow a device array to `need` elements (1/8 more with `slack`: arrays
+// sized by a schedule's rows, items or edges, which vary a little between
+// target sets, so most new sets reuse them instead of reallocating).
 template <class T>
-bf_status ensure_dev(T** p, size_t& cap, size_t need, Graph* g) {
+bf_status ensure_dev(T** p, size_t& cap, size_t need, Graph* g, bool slack = false) {
   if (need <= cap && *p) return BF_OK;
   if (*p) {
     cudaFree(*p);
@@ -53,7 +65,7 @@ bf_status ensure_dev(T** p, size_t& cap, size_t need, Graph* g) {
   }
   *p = nullptr;
   cap = 0;
-  const size_t m = std::max<size_t>(need, 1);
+  const size_t m = std::max<size_t>(slack ? need + need / 8 : need, 1);
   if (cudaMalloc((void**)p, m * sizeof(T)) != cudaSuccess) {
     cudaGetLastError();
     *p = nullptr;
@@ -76,10 +88,13 @@ __device__ __forceinline__ uint32_t row_of(const uint32_t* __restrict__ alive,
 }
 
 // 1. Mark the ancestor paths of the targets (positions) and the targets.
+// Every newly marked position is appended to the candidate list `clist`
+// (count in *nc), which the counting and the first frontier walk.
 __global__ void __launch_bounds__(128)
     k_sd_mark(const uint32_t* __restrict__ tgt, uint32_t T, const uint32_t* __restrict__ parent,
               const uint32_t* __restrict__ run_end, const uint32_t* __restrict__ pos_of, uint32_t n,
               uint32_t* __restrict__ alive, uint32_t* __restrict__ ist, uint32_t* __restrict__ cnt,
+              uint32_t* __restrict__ clist, uint32_t* __restrict__ nc,
               uint32_t* __restrict__ err) {
   const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (w >= T) return;
@@ -102,73 +117,180 @@ __global__ void __launch_bounds__(128)
       if (lane == 0) atomicOr(err, DEVERR_PATH);
       return;
     }
-    for (uint32_t r = x + lane; r <= e; r += 32) {
-      const uint32_t p = pos_of[r], b = 1u << (p & 31);
-      if (!(atomicOr(&alive[p >> 5], b) & b)) cnt[p] = 0;
+    for (uint32_t r0 = x; r0 <= e; r0 += 32) {
+      const uint32_t r = r0 + lane;
+      uint32_t p = 0;
+      bool fresh = false;
+      if (r <= e) {
+        p = pos_of[r];
+        const uint32_t b = 1u << (p & 31);
+        fresh = !(atomicOr(&alive[p >> 5], b) & b);
+        if (fresh) cnt[p] = 0;
+      }
+      const uint32_t f = __ballot_sync(0xFFFFFFFFu, fresh);
+      uint32_t base = 0;
+      if (lane == 0 && f) base = atomicAdd(nc, (uint32_t)__popc(f));
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (fresh) clist[base + __popc(f & ((1u << lane) - 1u))] = p;
     }
     __syncwarp();
     x = parent[e];
   }
 }
 
-// 2a. cnt[u] = DOWN out-edges of u into C (every in-edge source of a C row is
-// an ancestor of it, hence in C).
-__global__ void __launch_bounds__(256)
-    k_sd_count(const uint32_t* __restrict__ alive, uint32_t W, const uint64_t* __restrict__ in_off,
-               const uint2* __restrict__ in_rec, uint32_t* __restrict__ cnt) {
-  for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < W; w += gridDim.x * blockDim.x) {
-    uint32_t m = alive[w];
-    while (m) {
-      const uint32_t p = w * 32 + (__ffs(m) - 1);
-      m &= m - 1;
-      const uint64_t k1 = in_off[p + 1];
-      for (uint64_t k = in_off[p]; k < k1; ++k) atomicAdd(&cnt[in_rec[k].x], 1u);
+// Edges of 32 rows, one row per lane (k0: first in-edge, deg: in-degree, 0
+// for no row), spread over the warp's lanes, 32 edges per step whatever the
+// degrees, so a row with thousands of in-edges does not hold one thread for
+// thousands of steps. Every lane calls f(on, k, owner lane) once per step
+// (f may use warp collectives); `on` is false past the last edge.
+template <class F>
+__device__ __forceinline__ void warp_edges(uint64_t k0, uint32_t deg, uint32_t lane, F& f) {
+  constexpr unsigned FULL = 0xFFFFFFFFu;
+  uint32_t inc = deg;
+#pragma unroll
+  for (uint32_t o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(FULL, inc, o);
+    if (lane >= o) inc += t;
+  }
+  const uint32_t total = __shfl_sync(FULL, inc, 31), exc = inc - deg;
+  for (uint32_t e0 = 0; e0 < total; e0 += 32) {
+    const uint32_t e = e0 + lane;
+    // owner: the last lane whose first edge is at or below e
+    uint32_t lo = 0;
+#pragma unroll
+    for (uint32_t b = 16; b; b >>= 1) {
+      const uint32_t ex = __shfl_sync(FULL, exc, lo + b);
+      if (ex <= e) lo += b;
     }
+    const uint64_t kb = __shfl_sync(FULL, k0, lo);
+    const uint32_t xo = __shfl_sync(FULL, exc, lo);
+    f(e < total, kb + (e - xo), lo);
   }
 }
 
-// 2b. First frontier: rows of C that are no target and have no out-edge into C.
+// 2a. cnt[u] = DOWN out-edges of u into C (every in-edge source of a C row is
+// an ancestor of it, hence in C): one atomic per in-edge of a candidate.
+struct CountEdge {
+  const uint2* in_rec;
+  uint32_t* cnt;
+  __device__ __forceinline__ void operator()(bool on, uint64_t k, uint32_t) {
+    if (on) atomicAdd(&cnt[in_rec[k].x], 1u);
+  }
+};
+
 __global__ void __launch_bounds__(256)
-    k_sd_front0(uint32_t* __restrict__ alive, const uint32_t* __restrict__ ist, uint32_t W,
+    k_sd_count(const uint32_t* __restrict__ clist, const uint32_t* __restrict__ nc_p,
+               const uint64_t* __restrict__ in_off, const uint2* __restrict__ in_rec,
+               uint32_t* __restrict__ cnt) {
+  const uint32_t nc = *nc_p, lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * blockDim.x / 32;
+  CountEdge f{in_rec, cnt};
+  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < nc;
+       base += warps * 32) {
+    uint64_t k0 = 0;
+    uint32_t deg = 0;
+    if (base + lane < nc) {
+      const uint32_t p = clist[base + lane];
+      k0 = in_off[p];
+      deg = (uint32_t)(in_off[p + 1] - k0);
+    }
+    warp_edges(k0, deg, lane, f);
+  }
+}
+
+// 2b. First frontier: candidates that are no target and have no out-edge
+// into C.
+__global__ void __launch_bounds__(256)
+    k_sd_front0(const uint32_t* __restrict__ clist, const uint32_t* __restrict__ nc_p,
+                uint32_t* __restrict__ alive, const uint32_t* __restrict__ ist,
                 const uint32_t* __restrict__ cnt, uint32_t* __restrict__ front,
                 uint32_t* __restrict__ fcount) {
-  for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < W; w += gridDim.x * blockDim.x) {
-    uint32_t m = alive[w] & ~ist[w], dead = 0;
-    while (m) {
-      const uint32_t b = __ffs(m) - 1;
-      m &= m - 1;
-      if (cnt[w * 32 + b] == 0) dead |= 1u << b;
+  const uint32_t nc = *nc_p, lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * blockDim.x / 32;
+  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < nc;
+       base += warps * 32) {
+    uint32_t p = 0;
+    bool dead = false;
+    if (base + lane < nc) {
+      p = clist[base + lane];
+      dead = !bit_of(ist, p) && cnt[p] == 0;
+      if (dead) atomicAnd(&alive[p >> 5], ~(1u << (p & 31)));
     }
-    if (!dead) continue;
-    alive[w] &= ~dead;  // this thread alone owns word w here
-    uint32_t slot = atomicAdd(fcount, (uint32_t)__popc(dead));
-    while (dead) {
-      const uint32_t b = __ffs(dead) - 1;
-      dead &= dead - 1;
-      front[slot++] = w * 32 + b;
-    }
+    const uint32_t d = __ballot_sync(0xFFFFFFFFu, dead);
+    uint32_t slot = 0;
+    if (lane == 0 && d) slot = atomicAdd(fcount, (uint32_t)__popc(d));
+    slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+    if (dead) front[slot + __popc(d & ((1u << lane) - 1u))] = p;
   }
 }
 
-// 2c. One peeling round: every dead row of the frontier releases its in-edge
-// sources; a source whose count reaches 0 (and is no target) dies.
-__global__ void __launch_bounds__(256)
-    k_sd_peel(const uint32_t* __restrict__ fin, const uint32_t* __restrict__ nin,
-              uint32_t* __restrict__ fout, uint32_t* __restrict__ nout,
-              const uint64_t* __restrict__ in_off, const uint2* __restrict__ in_rec,
-              uint32_t* __restrict__ cnt, uint32_t* __restrict__ alive,
-              const uint32_t* __restrict__ ist) {
-  const uint32_t m = *nin;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-    const uint32_t v = fin[i];
-    const uint64_t k1 = in_off[v + 1];
-    for (uint64_t k = in_off[v]; k < k1; ++k) {
-      const uint32_t u = in_rec[k].x;
-      if (atomicSub(&cnt[u], 1u) == 1u && !bit_of(ist, u)) {
-        atomicAnd(&alive[u >> 5], ~(1u << (u & 31)));
-        fout[atomicAdd(nout, 1u)] = u;
-      }
+// 2c. Peeling rounds, one cooperative launch: in round r every dead row of
+// frontier r releases its in-edge sources; a source whose count reaches 0
+// (and is no target) dies and joins frontier r + 1. Frontiers alternate
+// between the two halves of `front`; their sizes rotate through meta[0..2]
+// (round r reads meta[r % 3], counts into meta[(r + 1) % 3], and block 0
+// clears meta[(r + 2) % 3], which no block touches in round r). Rounds are
+// separated by the bounded grid barrier; all blocks leave together once a
+// frontier is empty or after `rounds` rounds (meta[META_LEFT] then holds
+// the frontier left, whose rows stay live: a superset is still closed under
+// in-edge sources, so it is swept correctly, only in vain).
+struct PeelEdge {
+  const uint2* in_rec;
+  uint32_t* cnt;
+  uint32_t* alive;
+  const uint32_t* ist;
+  uint32_t* fout;
+  uint32_t* nout;
+  uint32_t lane;
+  __device__ __forceinline__ void operator()(bool on, uint64_t k, uint32_t) {
+    uint32_t u = 0;
+    bool dead = false;
+    if (on) {
+      u = in_rec[k].x;
+      dead = atomicSub(&cnt[u], 1u) == 1u && !bit_of(ist, u);
+      if (dead) atomicAnd(&alive[u >> 5], ~(1u << (u & 31)));
     }
+    const uint32_t d = __ballot_sync(0xFFFFFFFFu, dead);
+    uint32_t slot = 0;
+    if (lane == 0 && d) slot = atomicAdd(nout, (uint32_t)__popc(d));
+    slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+    if (dead) fout[slot + __popc(d & ((1u << lane) - 1u))] = u;
+  }
+};
+
+__global__ void __launch_bounds__(256)
+    k_sd_peel(uint32_t* __restrict__ front, uint32_t n, uint32_t* __restrict__ meta,
+              uint32_t rounds, const uint64_t* __restrict__ in_off,
+              const uint2* __restrict__ in_rec, uint32_t* __restrict__ cnt,
+              uint32_t* __restrict__ alive, const uint32_t* __restrict__ ist,
+              long long timeout, uint32_t* __restrict__ err) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * blockDim.x / 32;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  uint32_t r = 0, m = 0;
+  for (; r < rounds; ++r) {
+    // frontier r was completed before the barrier: read it through L2
+    m = __ldcg(&meta[r % 3]);
+    if (m == 0) break;
+    const uint32_t* fin = front + (size_t)(r & 1) * n;
+    PeelEdge f{in_rec, cnt, alive, ist, front + (size_t)((r + 1) & 1) * n,
+               meta + (r + 1) % 3, lane};
+    if (blockIdx.x == 0 && threadIdx.x == 0) meta[(r + 2) % 3] = 0;
+    for (uint32_t base = wid * 32; base < m; base += warps * 32) {
+      uint64_t k0 = 0;
+      uint32_t deg = 0;
+      if (base + lane < m) {
+        const uint32_t v = __ldcg(&fin[base + lane]);
+        k0 = in_off[v];
+        deg = (uint32_t)(in_off[v + 1] - k0);
+      }
+      warp_edges(k0, deg, lane, f);
+    }
+    if (!grid_barrier(meta + META_BAR, r, timeout, err)) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    meta[META_ROUNDS] = r;
+    meta[META_LEFT] = r < rounds ? 0u : __ldcg(&meta[r % 3]);
   }
 }
 
@@ -284,7 +406,32 @@ __global__ void k_sd_lvledge(const uint32_t* __restrict__ lvlrow, const uint64_t
   if (l <= L) lvl_edge[l] = (uint32_t)rpre[lvlrow[l]];
 }
 
-// 4a. Edge records, work items and gather counts, one thread per row.
+// 4a. Edge records, work items and gather counts: 32 rows per warp step,
+// their edges spread over the lanes; each lane then cuts its own row into
+// work items (one cursor atomic for all full-size items of the row).
+struct FillEdge {
+  const uint2* in_rec;
+  const uint32_t* in_len;
+  const uint32_t* alive;
+  const uint32_t* wpre;
+  uint2* erec;
+  uint32_t* elen;
+  uint32_t* uses;
+  uint64_t kbase;  // this lane's row: first in-edge and first edge record
+  uint32_t ebase;
+  __device__ __forceinline__ void operator()(bool on, uint64_t k, uint32_t owner) {
+    const uint64_t kb = __shfl_sync(0xFFFFFFFFu, kbase, owner);
+    const uint32_t eb = __shfl_sync(0xFFFFFFFFu, ebase, owner);
+    if (!on) return;
+    const uint2 r = in_rec[k];
+    const uint32_t src = row_of(alive, wpre, r.x);
+    const uint32_t e = eb + (uint32_t)(k - kb);
+    erec[e] = make_uint2(src, r.y);
+    if (elen) elen[e] = in_len[k];
+    atomicAdd(&uses[src], 1u);
+  }
+};
+
 __global__ void __launch_bounds__(256)
     k_sd_fill(const uint32_t* __restrict__ rowpos, const uint32_t* __restrict__ n_r_p,
               const uint64_t* __restrict__ rpre, const uint64_t* __restrict__ in_off,
@@ -293,27 +440,36 @@ __global__ void __launch_bounds__(256)
               const uint32_t* __restrict__ lvlrow, uint32_t L, SplitCfg c,
               uint32_t* __restrict__ cursor, uint4* __restrict__ item, uint2* __restrict__ erec,
               uint32_t* __restrict__ elen, uint32_t* __restrict__ uses) {
-  const uint32_t n_r = *n_r_p;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_r; i += gridDim.x * blockDim.x) {
-    const uint32_t p = rowpos[i];
-    const uint32_t e0 = (uint32_t)rpre[i];  // edges never reach 2^32 (checked by the host)
-    const uint64_t k0 = in_off[p];
-    const uint32_t deg = (uint32_t)(in_off[p + 1] - k0);
-    for (uint32_t j = 0; j < deg; ++j) {
-      const uint2 r = in_rec[k0 + j];
-      const uint32_t src = row_of(alive, wpre, r.x);
-      erec[e0 + j] = make_uint2(src, r.y);
-      if (elen) elen[e0 + j] = in_len[k0 + j];
-      atomicAdd(&uses[src], 1u);
+  const uint32_t n_r = *n_r_p, lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * blockDim.x / 32;
+  FillEdge f{in_rec, in_len, alive, wpre, erec, elen, uses, 0, 0};
+  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < n_r;
+       base += warps * 32) {
+    const uint32_t i = base + lane;
+    uint64_t k0 = 0;
+    uint32_t deg = 0, e0 = 0;
+    if (i < n_r) {
+      const uint32_t p = rowpos[i];
+      e0 = (uint32_t)rpre[i];  // edges never reach 2^32 (checked by the host)
+      k0 = in_off[p];
+      deg = (uint32_t)(in_off[p + 1] - k0);
     }
+    f.kbase = k0;
+    f.ebase = e0;
+    warp_edges(k0, deg, lane, f);
     if (!deg) continue;
     const uint32_t l = level_of_row(lvlrow, L, i);
     const uint32_t sp = split_of_level(lvlrow, l, c);
     const uint32_t split = deg > sp ? 1u : 0u;
-    for (uint32_t a = 0; a < deg; a += sp) {
-      const uint32_t sz = min(sp, deg - a);
-      const uint32_t slot = atomicAdd(&cursor[(size_t)l * c.s1 + sz], 1u);
-      item[slot] = make_uint4(i, e0 + a, e0 + a + sz, split);
+    const uint32_t full = deg / sp, rest = deg % sp;
+    if (full) {
+      const uint32_t slot = atomicAdd(&cursor[(size_t)l * c.s1 + sp], full);
+      for (uint32_t q = 0; q < full; ++q)
+        item[slot + q] = make_uint4(i, e0 + q * sp, e0 + (q + 1) * sp, split);
+    }
+    if (rest) {
+      const uint32_t slot = atomicAdd(&cursor[(size_t)l * c.s1 + rest], 1u);
+      item[slot] = make_uint4(i, e0 + full * sp, e0 + deg, split);
     }
   }
 }
@@ -414,19 +570,21 @@ struct SchedScratch {
   uint32_t* lvlrow = nullptr;  // [L + 1]
   uint32_t* lvl_item = nullptr;  // [L + 1]
   uint32_t* hist = nullptr;   // [L * s1]
-  uint32_t* meta = nullptr;   // [PEEL_ROUNDS + 8]: frontier sizes, n_r, hub threshold
+  uint32_t* clist = nullptr;  // [n] candidate positions (ancestors of the targets)
+  uint32_t* meta = nullptr;   // [META_WORDS]: frontier sizes, n_r, candidates, barrier
   uint32_t* tgt = nullptr;    // uploaded targets
   uint32_t* h_back = nullptr;  // page-locked read-back: meta words, totals, lvl_item
   size_t cap_alive = 0, cap_ist = 0, cap_cnt = 0, cap_front = 0, cap_wpre = 0, cap_rowpos = 0,
          cap_rdeg = 0, cap_rpre = 0, cap_b64 = 0, cap_b32 = 0, cap_lvlrow = 0, cap_lvli = 0,
-         cap_hist = 0, cap_meta = 0, cap_tgt = 0;
+         cap_hist = 0, cap_meta = 0, cap_tgt = 0, cap_clist = 0;
+  unsigned peel_blocks = 0;  // co-resident blocks of the peeling launch
   size_t back_words = 0;
 };
 
 void free_sched_scratch(SchedScratch* s) {
   if (!s) return;
   void* p[] = {s->alive, s->ist, s->cnt, s->front, s->wpre, s->rowpos, s->rdeg, s->rpre,
-               s->bsum64, s->bsum32, s->lvlrow, s->lvl_item, s->hist, s->meta, s->tgt};
+               s->bsum64, s->bsum32, s->lvlrow, s->lvl_item, s->hist, s->meta, s->tgt, s->clist};
   for (void* q : p)
     if (q) cudaFree(q);
   if (s->h_back) cudaFreeHost(s->h_back);
@@ -453,6 +611,7 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
   const uint64_t nb_words = (W + 1 + SCAN_BLOCK - 1) / SCAN_BLOCK + 1;
   bf_status rc;
   if ((rc = ensure_dev(&s.alive, s.cap_alive, W + 1, g)) ||
+      (rc = ensure_dev(&s.clist, s.cap_clist, n, g)) ||
       (rc = ensure_dev(&s.ist, s.cap_ist, W + 1, g)) ||
       (rc = ensure_dev(&s.cnt, s.cap_cnt, n, g)) ||
       (rc = ensure_dev(&s.front, s.cap_front, 2 * (size_t)n, g)) ||
@@ -465,7 +624,7 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
       (rc = ensure_dev(&s.lvlrow, s.cap_lvlrow, (size_t)L + 1, g)) ||
       (rc = ensure_dev(&s.lvl_item, s.cap_lvli, (size_t)L + 1, g)) ||
       (rc = ensure_dev(&s.hist, s.cap_hist, (size_t)L * cfg.s1, g)) ||
-      (rc = ensure_dev(&s.meta, s.cap_meta, PEEL_ROUNDS + 8, g)) ||
+      (rc = ensure_dev(&s.meta, s.cap_meta, META_WORDS, g)) ||
       (rc = ensure_dev(&sc.d_split, sc.cap_split, (size_t)W + 1, g)) ||
       (rc = ensure_dev(&sc.d_cidx, sc.cap_cidx, n, g)))
     return rc;
@@ -492,29 +651,36 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
   }
   BF_CUDA(cudaMemsetAsync(s.alive, 0, (size_t)(W + 1) * 4, st));
   BF_CUDA(cudaMemsetAsync(s.ist, 0, (size_t)(W + 1) * 4, st));
-  BF_CUDA(cudaMemsetAsync(s.meta, 0, (PEEL_ROUNDS + 8) * 4, st));
+  BF_CUDA(cudaMemsetAsync(s.meta, 0, META_WORDS * 4, st));
   BF_CUDA(cudaMemsetAsync(s.hist, 0, (size_t)L * cfg.s1 * 4, st));
   // 1. ancestors of the targets
+  uint32_t* d_nc = s.meta + META_NC;
   if (T)
     k_sd_mark<<<(unsigned)((T + 3) / 4), 128, 0, st>>>(d_tgt, (uint32_t)T, g->d_parent,
                                                         g->d_run_end, g->d_pos_of, n, s.alive,
-                                                        s.ist, s.cnt, g->d_err);
+                                                        s.ist, s.cnt, s.clist, d_nc, g->d_err);
   // 2. peeling
-  k_sd_count<<<grid_for(W, 256), 256, 0, st>>>(s.alive, W, g->d_in_off, g->d_in_rec, s.cnt);
-  k_sd_front0<<<grid_for(W, 256), 256, 0, st>>>(s.alive, s.ist, W, s.cnt, s.front, s.meta);
-  for (uint32_t r = 0; r < PEEL_ROUNDS; ++r) {
-    uint32_t* fin = s.front + (size_t)(r & 1) * n;
-    uint32_t* fout = s.front + (size_t)((r + 1) & 1) * n;
-    k_sd_peel<<<152 * 4, 256, 0, st>>>(fin, s.meta + r, fout, s.meta + r + 1, g->d_in_off,
-                                        g->d_in_rec, s.cnt, s.alive, s.ist);
+  k_sd_count<<<152 * 8, 256, 0, st>>>(s.clist, d_nc, g->d_in_off, g->d_in_rec, s.cnt);
+  k_sd_front0<<<152 * 8, 256, 0, st>>>(s.clist, d_nc, s.alive, s.ist, s.cnt, s.front, s.meta);
+  if (!s.peel_blocks) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sd_peel, 256, 0) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    s.peel_blocks = std::max(1u, std::min(4u, (unsigned)std::max(per_sm, 1)) * g->sm_count);
   }
+  BF_CUDA(launch_persistent(k_sd_peel, s.peel_blocks, 256, st, s.front, n, s.meta, PEEL_ROUNDS,
+                            (const uint64_t*)g->d_in_off, (const uint2*)g->d_in_rec, s.cnt,
+                            s.alive, (const uint32_t*)s.ist, BARRIER_TIMEOUT_CYCLES, g->d_err));
   // 3. compaction
   const unsigned nbw = (unsigned)((W + 1 + SCAN_BLOCK - 1) / SCAN_BLOCK);
   PopVal pv{s.alive};
   k_scan_sums<uint32_t><<<nbw, SCAN_TPB, 0, st>>>(pv, W, nullptr, s.bsum32);
   k_scan_top<uint32_t><<<1, SCAN_TPB, 0, st>>>(s.bsum32, nbw);
   k_scan_out<uint32_t><<<nbw, SCAN_TPB, 0, st>>>(pv, W, nullptr, s.bsum32, nbw, s.wpre);
-  uint32_t* d_nr = s.meta + PEEL_ROUNDS + 2;
+  uint32_t* d_nr = s.meta + META_NR;
   k_sd_rows<<<grid_for(W, 256), 256, 0, st>>>(s.alive, s.wpre, W, s.rowpos);
   k_sd_lvlrow<<<(L + 1 + 255) / 256, 256, 0, st>>>(g->d_lvl_start, L, s.alive, s.wpre, s.lvlrow,
                                                     d_nr, W);
@@ -532,7 +698,7 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
   // read back: n_r, total (edges | items << 32), peel rounds used, level items
   BF_CUDA(cudaMemcpyAsync(s.h_back, d_nr, 4, cudaMemcpyDeviceToHost, st));
   BF_CUDA(cudaMemcpyAsync(s.h_back + 1, s.bsum64 + nbr, 8, cudaMemcpyDeviceToHost, st));
-  BF_CUDA(cudaMemcpyAsync(s.h_back + 3, s.meta + PEEL_ROUNDS, 4, cudaMemcpyDeviceToHost, st));
+  BF_CUDA(cudaMemcpyAsync(s.h_back + 3, s.meta + META_LEFT, 4, cudaMemcpyDeviceToHost, st));
   BF_CUDA(cudaMemcpyAsync(s.h_back + 4 + (L + 1), s.lvlrow, ((size_t)L + 1) * 4,
                           cudaMemcpyDeviceToHost, st));
   BF_CUDA(cudaMemcpyAsync(s.h_back + 4 + 2 * (L + 1), s.front, ((size_t)L + 1) * 4,
@@ -550,12 +716,12 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
   }
   sc.valid = false;
   const bool two = g->has_len;
-  if ((rc = ensure_dev(&sc.d_item, sc.cap_items, n_i, g)) ||
-      (rc = ensure_dev(&sc.d_erec, sc.cap_edges, n_e + 2, g)) ||
-      (two && (rc = ensure_dev(&sc.d_elen, sc.cap_elen, n_e, g))) ||
-      (rc = ensure_dev(&sc.d_trow, sc.cap_t, T, g)) ||
+  if ((rc = ensure_dev(&sc.d_item, sc.cap_items, n_i, g, true)) ||
+      (rc = ensure_dev(&sc.d_erec, sc.cap_edges, n_e + 2, g, true)) ||
+      (two && (rc = ensure_dev(&sc.d_elen, sc.cap_elen, n_e, g, true))) ||
+      (rc = ensure_dev(&sc.d_trow, sc.cap_t, T, g, true)) ||
       (rc = ensure_dev(&sc.d_lvl, sc.cap_lvl, (size_t)L + 1, g)) ||
-      (rc = ensure_dev(&sc.d_uses, sc.cap_uses, (size_t)n_r + 1, g)))
+      (rc = ensure_dev(&sc.d_uses, sc.cap_uses, (size_t)n_r + 1, g, true)))
     return rc;
   BF_CUDA(cudaMemsetAsync(sc.d_uses, 0, (size_t)std::max<uint32_t>(n_r, 1) * 4, st));
   // 4. fill

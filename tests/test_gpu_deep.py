@@ -75,3 +75,57 @@ def test_deep_chain_threshold_calls(built):
     src = [[(0, 0)], [(100, 3), (200, 1)]]
     tgt = [[(N - 1, 0)], [(50, 2)], [(3000, 0), (3001, 4)]]
     assert np.array_equal(g.matrix_seeded(src, tgt), orc.table_phast_lopsided(c, src, tgt, INF)[0])
+
+
+def _zigzag(n):
+    """Two chains of ranks of one parity (0, 2, 4, ... and 1, 3, 5, ...) that
+    meet at the top (n - 2 -> n - 1, n even): every rank's parent is two
+    ranks up, so an ancestor path is a run of single ranks, about n / 2 runs."""
+    up = {u: [] for u in range(n)}
+    for u in range(n - 2):
+        up[u].append(u + 2)
+    up[n - 2].append(n - 1)
+    up_off = np.zeros(n + 1, np.uint64)
+    up_off[1:] = np.cumsum([len(up[u]) for u in range(n)])
+    up_tgt = np.array([v for u in range(n) for v in up[u]], np.uint32)
+    up_w = (3 + np.arange(len(up_tgt)) % 11).astype(np.uint32)
+    down = {v: [] for v in range(n)}
+    for u in range(n):
+        for v in up[u]:
+            down[v].append(u)
+    down_off = np.zeros(n + 1, np.uint64)
+    down_off[1:] = np.cumsum([len(down[v]) for v in range(n)])
+    down_tgt = np.array([u for v in range(n) for u in down[v]], np.uint32)
+    down_w = (1 + np.arange(len(down_tgt)) % 5).astype(np.uint32)
+    return dict(n=n, up_off=up_off, up_tgt=up_tgt, up_w=up_w, down_off=down_off,
+                down_tgt=down_tgt, down_w=down_w)
+
+
+@pytest.mark.parametrize("n", [60, 400])
+def test_path_runs_both_upward_forms(built, n):
+    """Ancestor paths of at most 32 runs take the run-indexed upward kernel,
+    longer ones the path-array kernel: n = 60 gives paths of ~30 runs, n = 400
+    of ~200. Both against the oracle, for the matrix engines, per-lane
+    thresholds and seeded units."""
+    import bfphast
+    cch = _zigzag(n)
+    c = orc.Cch.from_dict(cch)
+    g = bfphast.Graph.from_cch(cch)
+    rng = np.random.default_rng(n)
+    src = rng.choice(n, 20, replace=False).astype(np.uint32)
+    tgt = rng.choice(n, 25, replace=False).astype(np.uint32)
+    want, _ = c.matrix(src, tgt)
+    for eng in (bfphast.ENGINE_BATCHED, bfphast.ENGINE_PLAIN):
+        g.set_engine(eng)
+        assert np.array_equal(g.matrix(src, tgt), want), eng
+        assert np.array_equal(g.matrix(src, tgt, threshold=150),
+                              np.where(want <= 150, want, INF)), eng
+    origins = src[:6]
+    thr = np.array([10, 40, 90, 200, 500, 3000], dtype=np.uint32)
+    bits, counts = g.isochrone_bitsets(origins, thr)
+    want_bits, want_counts = c.isochrone_bitsets(origins, thr)
+    assert np.array_equal(bits, want_bits) and np.array_equal(counts, want_counts)
+    seeds = [(int(src[0]), 3), (int(src[1]), 0)]
+    rk, ds = g.phast_bounded_seeded(seeds, 300)
+    wr, wd = c.bounded_seeded(seeds, 300)
+    assert np.array_equal(rk, wr) and np.array_equal(ds, wd)
