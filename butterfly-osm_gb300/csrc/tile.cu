@@ -17,8 +17,9 @@
 // Dense: one thread per cell, or per four cells with 16-byte accesses when
 // rows are a multiple of four cells (2D grid: columns x rows), reads and the
 // four column writes coalesced. Sparse: an order-preserving compaction - per
-// block of 2048 cells a count and the kept-cell ballots, a one-block scan of
-// the counts, then an ordered write of the kept cells only.
+// block of 2048 cells a count and the kept-cell ballots (radius lists of the
+// block's rows searched in shared memory), a device-wide scan of the counts,
+// then an ordered write of the kept cells only.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -29,6 +30,7 @@
 #include <vector>
 
 #include "engine.cuh"
+#include "scan.cuh"
 
 using namespace bf;
 
@@ -174,13 +176,59 @@ __global__ void __launch_bounds__(TPB) k_tile_dense4(TileIn a, TileOut o, uint32
   }
 }
 
+// Radius lists of the (at most two) rows a count block spans, staged in
+// shared memory when each holds at most LIST_STAGE entries: the in-bound
+// cells then search them there instead of through a chain of global loads.
+constexpr uint32_t LIST_STAGE = 4096;
+struct ListStage {
+  uint32_t v[2][LIST_STAGE];
+  uint32_t len[2];
+  uint32_t row0;
+  int ok;
+};
+
+// Stages the lists of rows [si0, si1] (si1 - si0 <= 1) when both are valid
+// and short enough; a row with a bad or missing list is left to decide()
+// (which reports it). Returns true when the block searches shared memory.
+__device__ __forceinline__ bool stage_lists(const TileIn& a, uint32_t si0, uint32_t si1,
+                                            ListStage& ls) {
+  if (threadIdx.x == 0) {
+    int ok = si1 - si0 <= 1;
+    for (uint32_t r = 0; ok && r <= si1 - si0; ++r) {
+      const uint32_t os = a.src_orig[si0 + r];
+      if (os >= a.n_mask_src) {
+        ok = 0;
+        break;
+      }
+      const uint64_t lo = a.mask_off[os], hi = a.mask_off[os + 1];
+      if (hi < lo || hi > a.n_mask || hi - lo > LIST_STAGE) {
+        ok = 0;
+        break;
+      }
+      ls.len[r] = (uint32_t)(hi - lo);
+    }
+    ls.row0 = si0;
+    ls.ok = ok;
+  }
+  __syncthreads();
+  if (!ls.ok) return false;
+  for (uint32_t r = 0; r <= si1 - si0; ++r) {
+    const uint32_t* src = a.mask + a.mask_off[a.src_orig[si0 + r]];
+    for (uint32_t k = threadIdx.x; k < ls.len[r]; k += blockDim.x) ls.v[r][k] = src[k];
+  }
+  __syncthreads();
+  return true;
+}
+
 // Sparse pass 1: per block the kept cells, per (step, warp) the ballot of
 // kept cells (bit lane of word (cell / 32)); rows and columns advance by
-// TPB cells a step instead of a division per cell.
+// TPB cells a step instead of a division per cell. With a radius mask, the
+// lists of the block's rows are searched in shared memory when they fit.
 __global__ void __launch_bounds__(TPB)
     k_tile_count(TileIn a, uint64_t n, bool narrow, unsigned long long* __restrict__ cnt,
                  uint32_t* __restrict__ keep_bits, uint32_t* err) {
   __shared__ uint32_t red[TPB / 32];
+  __shared__ ListStage ls;
   const uint64_t base = (uint64_t)blockIdx.x * CELLS;
   uint32_t c = 0, si = 0, di = 0;
   split(base + threadIdx.x, a.n_dst, narrow, &si, &di);
@@ -189,6 +237,13 @@ __global__ void __launch_bounds__(TPB)
   for (uint32_t j = 0; j < ITEMS; ++j) {
     const uint64_t i = base + (uint64_t)j * TPB + threadIdx.x;
     dur[j] = i < n ? a.m[i] : MAXV;
+  }
+  bool staged = false;
+  if (a.mask_off && a.n_dst >= TPB) {
+    uint32_t s0, s1, d0, d1;
+    split(base, a.n_dst, narrow, &s0, &d0);
+    split(min(base + CELLS, n) - 1, a.n_dst, narrow, &s1, &d1);
+    staged = stage_lists(a, s0, s1, ls);
   }
 #pragma unroll
   for (uint32_t j = 0; j < ITEMS; ++j) {
@@ -206,7 +261,18 @@ __global__ void __launch_bounds__(TPB)
       }
     }
     bool keep = false;
-    if (i < n) keep = decide(a, dur[j], a.src_orig[si], a.dst_orig[di], err) != MAXV;
+    if (i < n) {
+      if (staged) {
+        // decide() with the row's list read from shared memory
+        const uint32_t d = dur[j];
+        if (d <= a.threshold && d != MAXV) {
+          const uint32_t r = si - ls.row0;
+          keep = in_list(ls.v[r], ls.len[r], a.dst_orig[di]);
+        }
+      } else {
+        keep = decide(a, dur[j], a.src_orig[si], a.dst_orig[di], err) != MAXV;
+      }
+    }
     const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
     if ((threadIdx.x & 31) == 0) keep_bits[(base + (uint64_t)j * TPB) / 32 + (threadIdx.x >> 5)] = bal;
     c += keep;
@@ -221,69 +287,46 @@ __global__ void __launch_bounds__(TPB)
   }
 }
 
-// Exclusive scan of nb block counts in one block; the total last.
-__global__ void __launch_bounds__(1024)
-    k_tile_scan(uint64_t nb, const unsigned long long* __restrict__ cnt,
-                unsigned long long* __restrict__ pre, unsigned long long* __restrict__ total) {
-  __shared__ unsigned long long sh[32];
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned long long carry = 0;
-  for (uint64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
-    const uint64_t b = b0 + threadIdx.x;
-    const unsigned long long v = b < nb ? cnt[b] : 0;
-    unsigned long long x = v;
-    for (int d = 1; d < 32; d <<= 1) {
-      const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, d);
-      if (lane >= d) x += y;
-    }
-    if (lane == 31) sh[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      unsigned long long s = lane < (blockDim.x >> 5) ? sh[lane] : 0;
-      for (int d = 1; d < 32; d <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, s, d);
-        if (lane >= d) s += y;
-      }
-      sh[lane] = s;
-    }
-    __syncthreads();
-    if (b < nb) pre[b] = carry + (warp ? sh[warp - 1] : 0) + x - v;
-    carry += sh[(blockDim.x >> 5) - 1];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *total = carry;
-}
-
 // Sparse pass 2: the block's kept cells, in order, from pass 1's ballots:
 // a thread's output slot is the block's offset plus the kept cells of the
-// earlier words of the block and the lower lanes of its own word.
+// earlier words of the block (a two-warp shuffle scan of the word counts)
+// and the lower lanes of its own word. A kept cell passed the bound and its
+// radius list in pass 1, so its duration is written as read.
 __global__ void __launch_bounds__(TPB)
     k_tile_write(TileIn a, TileOut o, uint64_t n, bool narrow,
                  const unsigned long long* __restrict__ pre,
-                 const uint32_t* __restrict__ keep_bits, uint32_t* err) {
-  __shared__ uint32_t wpre[CELLS / 32 + 1];
-  const uint32_t lane = threadIdx.x & 31;
+                 const uint32_t* __restrict__ keep_bits) {
+  constexpr uint32_t WORDS = CELLS / 32;
+  static_assert(WORDS == 64 && TPB >= 64, "two warps scan the block's 64 ballot words");
+  __shared__ uint32_t wpre[WORDS];
+  __shared__ uint32_t half;
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned long long k0 = pre[blockIdx.x];
+  if (pre[blockIdx.x + 1] == k0) return;  // nothing kept in this block (uniform)
   const uint64_t base = (uint64_t)blockIdx.x * CELLS;
   const uint64_t w0 = base / 32, nw = (n + 31) / 32;
-  if (threadIdx.x == 0) {  // exclusive prefix of the block's 64 word counts
-    uint32_t acc = 0;
-    for (uint32_t w = 0; w < CELLS / 32; ++w) {
-      wpre[w] = acc;
-      acc += w0 + w < nw ? __popc(keep_bits[w0 + w]) : 0;
+  if (wid < 2) {
+    const uint32_t w = wid * 32 + lane;
+    const uint32_t c = w0 + w < nw ? __popc(keep_bits[w0 + w]) : 0;
+    uint32_t inc = c;
+#pragma unroll
+    for (uint32_t d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, d);
+      if (lane >= d) inc += y;
     }
-    wpre[CELLS / 32] = acc;
+    wpre[w] = inc - c;
+    if (wid == 0 && lane == 31) half = inc;
   }
   __syncthreads();
-  const uint64_t k0 = pre[blockIdx.x];
-  for (uint32_t w = threadIdx.x >> 5; w < CELLS / 32; w += TPB / 32) {
+  for (uint32_t w = wid; w < WORDS; w += TPB / 32) {
     if (w0 + w >= nw) break;
     const uint32_t bits = keep_bits[w0 + w];
     if (!((bits >> lane) & 1u)) continue;
     const uint64_t i = (w0 + w) * 32 + lane;
-    uint32_t si, di, os, od;
+    uint32_t si, di;
     split(i, a.n_dst, narrow, &si, &di);
-    const uint32_t d = cell_value(a, si, di, i, &os, &od, err);
-    put(a, o, k0 + wpre[w] + __popc(bits & ((1u << lane) - 1u)), i, os, od, d);
+    const uint32_t slot = wpre[w] + (w >= 32 ? half : 0u) + __popc(bits & ((1u << lane) - 1u));
+    put(a, o, k0 + slot, i, a.src_orig[si], a.dst_orig[di], a.m[i]);
   }
 }
 
@@ -358,12 +401,22 @@ bf_status emit_device(TileWs& ws, const TileIn& a, const TileOut& o, cudaStream_
     }
     unsigned long long* d_cnt = nullptr;
     uint32_t* d_bits = nullptr;
+    uint64_t* d_bsum = nullptr;
+    const uint64_t nsb = (nb + SCAN_BLOCK - 1) / SCAN_BLOCK;
     BF_CUDA(ws_get(ws, 1, (2 * nb + 1) * 8, &d_cnt));
     BF_CUDA(ws_get(ws, 9, nb * (CELLS / 32) * 4, &d_bits));
+    BF_CUDA(ws_get(ws, 10, (nsb + 2) * 8, &d_bsum));
     const bool narrow = n <= 0xFFFFFFFFull;
     k_tile_count<<<(unsigned)nb, TPB, 0, st>>>(a, n, narrow, d_cnt, d_bits, d_err);
-    k_tile_scan<<<1, 1024, 0, st>>>(nb, d_cnt, d_cnt + nb, d_cnt + 2 * nb);
-    k_tile_write<<<(unsigned)nb, TPB, 0, st>>>(a, o, n, narrow, d_cnt + nb, d_bits, d_err);
+    // exclusive scan of the block counts (total at [2 nb])
+    uint64_t* pre = reinterpret_cast<uint64_t*>(d_cnt + nb);
+    k_scan_sums<uint64_t><<<(unsigned)nsb, SCAN_TPB, 0, st>>>(
+        U64Val{reinterpret_cast<const uint64_t*>(d_cnt)}, nb, nullptr, d_bsum);
+    k_scan_top<uint64_t><<<1, SCAN_TPB, 0, st>>>(d_bsum, (uint32_t)nsb);
+    k_scan_out<uint64_t><<<(unsigned)nsb, SCAN_TPB, 0, st>>>(
+        U64Val{reinterpret_cast<const uint64_t*>(d_cnt)}, nb, nullptr, d_bsum, (uint32_t)nsb,
+        pre);
+    k_tile_write<<<(unsigned)nb, TPB, 0, st>>>(a, o, n, narrow, d_cnt + nb, d_bits);
     BF_CUDA(cudaGetLastError());
     BF_CUDA(cudaMemcpyAsync(&rows, d_cnt + 2 * nb, 8, cudaMemcpyDeviceToHost, st));
   }

@@ -106,3 +106,24 @@ def test_missing_radius_list_is_an_error(bf):
     # the library stays usable afterwards
     assert same(bf.tile_emit([1, 2], 1, 2, [0], [0, 1], mask=[[1]], sparse=True),
                 orc.tile_emit([1, 2], 1, 2, [0], [0, 1], mask=[[1]], sparse=True))
+
+
+@pytest.mark.parametrize("n_dst,list_max", [(2048, 600), (5000, 4096), (3000, 5000)])
+def test_sparse_radius_lists_staged(bf, n_dst, list_max):
+    """Sparse emission with radius lists short enough (at most 4096 entries)
+    to be searched in shared memory by every count block (rows of 2048 or
+    more cells: a block spans at most two rows), including lists of exactly
+    the staging limit and, for list_max 5000, rows whose list is too long,
+    whose blocks search global memory."""
+    rng = np.random.default_rng(n_dst + list_max)
+    n_src = 37
+    m, src, dst, _, lat = random_case(rng, n_src, n_dst, False, True)
+    span = 3 * n_dst + 5
+    mask = []
+    for r in range(3 * n_src + 5):
+        k = list_max if r % 3 == 0 else int(rng.integers(0, list_max + 1))
+        mask.append(np.sort(rng.choice(span, min(k, span), replace=False)).astype(np.uint32)
+                    .tolist())
+    for thr in (MAX, 100_000):
+        args = (m, n_src, n_dst, src, dst, thr, mask, lat, True)
+        assert same(bf.tile_emit(*args), orc.tile_emit(*args)), thr
