@@ -16,10 +16,11 @@
 //
 // Dense: one thread per cell, or per four cells with 16-byte accesses when
 // rows are a multiple of four cells (2D grid: columns x rows), reads and the
-// four column writes coalesced. Sparse: an order-preserving compaction - per
-// block of 2048 cells a count and the kept-cell ballots (radius lists of the
-// block's rows searched in shared memory), a device-wide scan of the counts,
-// then an ordered write of the kept cells only.
+// four column writes coalesced. Sparse: an order-preserving compaction - a
+// count and the kept-cell ballots per block (a row segment of up to 16384
+// cells for rows of 2048 cells or more, its radius list read once and
+// searched in shared memory when it fits; else 2048 consecutive cells), a
+// device-wide scan of the counts, then an ordered write of the kept cells.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -176,59 +177,13 @@ __global__ void __launch_bounds__(TPB) k_tile_dense4(TileIn a, TileOut o, uint32
   }
 }
 
-// Radius lists of the (at most two) rows a count block spans, staged in
-// shared memory when each holds at most LIST_STAGE entries: the in-bound
-// cells then search them there instead of through a chain of global loads.
-constexpr uint32_t LIST_STAGE = 4096;
-struct ListStage {
-  uint32_t v[2][LIST_STAGE];
-  uint32_t len[2];
-  uint32_t row0;
-  int ok;
-};
-
-// Stages the lists of rows [si0, si1] (si1 - si0 <= 1) when both are valid
-// and short enough; a row with a bad or missing list is left to decide()
-// (which reports it). Returns true when the block searches shared memory.
-__device__ __forceinline__ bool stage_lists(const TileIn& a, uint32_t si0, uint32_t si1,
-                                            ListStage& ls) {
-  if (threadIdx.x == 0) {
-    int ok = si1 - si0 <= 1;
-    for (uint32_t r = 0; ok && r <= si1 - si0; ++r) {
-      const uint32_t os = a.src_orig[si0 + r];
-      if (os >= a.n_mask_src) {
-        ok = 0;
-        break;
-      }
-      const uint64_t lo = a.mask_off[os], hi = a.mask_off[os + 1];
-      if (hi < lo || hi > a.n_mask || hi - lo > LIST_STAGE) {
-        ok = 0;
-        break;
-      }
-      ls.len[r] = (uint32_t)(hi - lo);
-    }
-    ls.row0 = si0;
-    ls.ok = ok;
-  }
-  __syncthreads();
-  if (!ls.ok) return false;
-  for (uint32_t r = 0; r <= si1 - si0; ++r) {
-    const uint32_t* src = a.mask + a.mask_off[a.src_orig[si0 + r]];
-    for (uint32_t k = threadIdx.x; k < ls.len[r]; k += blockDim.x) ls.v[r][k] = src[k];
-  }
-  __syncthreads();
-  return true;
-}
-
 // Sparse pass 1: per block the kept cells, per (step, warp) the ballot of
 // kept cells (bit lane of word (cell / 32)); rows and columns advance by
-// TPB cells a step instead of a division per cell. With a radius mask, the
-// lists of the block's rows are searched in shared memory when they fit.
+// TPB cells a step instead of a division per cell.
 __global__ void __launch_bounds__(TPB)
     k_tile_count(TileIn a, uint64_t n, bool narrow, unsigned long long* __restrict__ cnt,
                  uint32_t* __restrict__ keep_bits, uint32_t* err) {
   __shared__ uint32_t red[TPB / 32];
-  __shared__ ListStage ls;
   const uint64_t base = (uint64_t)blockIdx.x * CELLS;
   uint32_t c = 0, si = 0, di = 0;
   split(base + threadIdx.x, a.n_dst, narrow, &si, &di);
@@ -237,13 +192,6 @@ __global__ void __launch_bounds__(TPB)
   for (uint32_t j = 0; j < ITEMS; ++j) {
     const uint64_t i = base + (uint64_t)j * TPB + threadIdx.x;
     dur[j] = i < n ? a.m[i] : MAXV;
-  }
-  bool staged = false;
-  if (a.mask_off && a.n_dst >= TPB) {
-    uint32_t s0, s1, d0, d1;
-    split(base, a.n_dst, narrow, &s0, &d0);
-    split(min(base + CELLS, n) - 1, a.n_dst, narrow, &s1, &d1);
-    staged = stage_lists(a, s0, s1, ls);
   }
 #pragma unroll
   for (uint32_t j = 0; j < ITEMS; ++j) {
@@ -261,18 +209,7 @@ __global__ void __launch_bounds__(TPB)
       }
     }
     bool keep = false;
-    if (i < n) {
-      if (staged) {
-        // decide() with the row's list read from shared memory
-        const uint32_t d = dur[j];
-        if (d <= a.threshold && d != MAXV) {
-          const uint32_t r = si - ls.row0;
-          keep = in_list(ls.v[r], ls.len[r], a.dst_orig[di]);
-        }
-      } else {
-        keep = decide(a, dur[j], a.src_orig[si], a.dst_orig[di], err) != MAXV;
-      }
-    }
+    if (i < n) keep = decide(a, dur[j], a.src_orig[si], a.dst_orig[di], err) != MAXV;
     const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
     if ((threadIdx.x & 31) == 0) keep_bits[(base + (uint64_t)j * TPB) / 32 + (threadIdx.x >> 5)] = bal;
     c += keep;
@@ -284,6 +221,304 @@ __global__ void __launch_bounds__(TPB)
     uint32_t t = 0;
     for (uint32_t w = 0; w < TPB / 32; ++w) t += red[w];
     cnt[blockIdx.x] = t;
+  }
+}
+
+// Wide rows (n_dst >= ROW_MIN): a block per row segment of up to SEG cells,
+// so a row's radius list is read once per segment: staged in shared memory
+// when it holds at most LIST_STAGE entries, else searched in place. Ballot
+// words are per row (wpr = ceil(n_dst / 32) words each), counts per
+// segment, in cell order.
+constexpr uint32_t ROW_MIN = 2048, SEG = 16384, SEG_WORDS = SEG / 32, LIST_STAGE = 4096;
+enum : uint32_t { RL_NONE = 0, RL_SMEM = 1, RL_GLOBAL = 2, RL_BAD = 3, RL_MISSING = 4 };
+// A staged list is also set into a bitmap of original indices below
+// BITMAP_BITS, so a destination id below it is one shared-memory word test
+// (ids at or above it are searched in the staged list).
+constexpr uint32_t BITMAP_BITS = 1u << 17, BITMAP_WORDS = BITMAP_BITS / 32;
+
+struct RowList {
+  uint32_t v[LIST_STAGE];
+  uint32_t bmp[BITMAP_WORDS];
+};
+
+// Stages len list entries (block-uniform call) and sets the bitmap's first
+// nbw words (ids below 32 nbw: the destination ids' range, capped).
+__device__ __forceinline__ void stage_row_list(RowList& rl, const uint32_t* __restrict__ src,
+                                               uint32_t len, uint32_t nbw) {
+  for (uint32_t k = threadIdx.x; k < nbw; k += TPB) rl.bmp[k] = 0;
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < len; k += TPB) {
+    const uint32_t x = src[k];
+    rl.v[k] = x;
+    if (x < nbw * 32) atomicOr(&rl.bmp[x >> 5], 1u << (x & 31));
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool in_row_list(const RowList& rl, uint32_t len, uint32_t nbw,
+                                            uint32_t x) {
+  if (x < nbw * 32) return (rl.bmp[x >> 5] >> (x & 31)) & 1u;
+  return in_list(rl.v, len, x);
+}
+
+// Per wide row, once per call: how its radius list is read ({mode, len, list
+// offset low and high words}, decide()'s rules), and into bound[0] the
+// largest destination id (the bitmap's range).
+__global__ void __launch_bounds__(TPB) k_tile_rowinfo(TileIn a, uint4* __restrict__ info,
+                                                      uint32_t* __restrict__ bound) {
+  const uint32_t stride = gridDim.x * TPB;
+  for (uint32_t si = blockIdx.x * TPB + threadIdx.x; si < a.n_src; si += stride) {
+    uint32_t mode = RL_NONE, len = 0;
+    uint64_t lo = 0;
+    if (a.mask_off) {
+      const uint32_t os = a.src_orig[si];
+      if (os >= a.n_mask_src) {
+        mode = RL_MISSING;
+      } else {
+        lo = a.mask_off[os];
+        const uint64_t hi = a.mask_off[os + 1];
+        if (hi < lo || hi > a.n_mask || hi - lo > 0xFFFFFFFFull) {
+          mode = RL_BAD;
+          lo = 0;
+        } else {
+          len = (uint32_t)(hi - lo);
+          mode = len <= LIST_STAGE ? RL_SMEM : RL_GLOBAL;
+        }
+      }
+    }
+    info[si] = make_uint4(mode, len, (uint32_t)lo, (uint32_t)(lo >> 32));
+  }
+  uint32_t mx = 0;
+  for (uint32_t c = blockIdx.x * TPB + threadIdx.x; c < a.n_dst; c += stride)
+    mx = max(mx, a.dst_orig[c]);
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(bound, mx);
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red) {
+  for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  uint32_t t = 0;
+  for (uint32_t w = 0; w < TPB / 32; ++w) t += red[w];
+  return t;
+}
+
+// Sparse pass 1 for wide rows: the segment's kept cells and ballots, with
+// decide()'s rules: a row without a list keeps nothing (ERR_NO_LIST), a bad
+// list keeps nothing and is an error once a cell is within the bound.
+__global__ void __launch_bounds__(TPB)
+    k_tile_count_rows(TileIn a, uint32_t segs, uint32_t wpr, const uint4* __restrict__ info,
+                      const uint32_t* __restrict__ bound, unsigned long long* __restrict__ cnt,
+                      uint32_t* __restrict__ keep_bits, uint32_t* err) {
+  __shared__ RowList rl;
+  __shared__ uint32_t red[TPB / 32];
+  const uint32_t si = blockIdx.x / segs, sg = blockIdx.x % segs;
+  const uint32_t c_begin = sg * SEG, c_end = min(c_begin + SEG, a.n_dst);
+  const uint32_t lane = threadIdx.x & 31;
+  // the first step's durations load while the row's list is looked up
+  const uint32_t* row = a.m + (uint64_t)si * a.n_dst;
+  uint32_t dur[ITEMS];
+#pragma unroll
+  for (uint32_t j = 0; j < ITEMS; ++j) {
+    const uint32_t col = c_begin + j * TPB + threadIdx.x;
+    dur[j] = col < c_end ? row[col] : MAXV;
+  }
+  const uint4 ri = info[si];  // {mode, len, list offset (lo, hi words)}
+  const uint32_t nbw = min(BITMAP_WORDS, (*bound >> 5) + 1);
+  const uint32_t mode = ri.x, len = ri.y;
+  const uint64_t lo = ri.z | ((uint64_t)ri.w << 32);
+  if (mode == RL_MISSING && threadIdx.x == 0) atomicOr(err, ERR_NO_LIST);
+  // uniform: every thread read the same row record
+  if (mode == RL_SMEM) stage_row_list(rl, a.mask + lo, len, nbw);
+  const uint32_t* lg = a.mask + lo;
+  uint32_t* bits = keep_bits + (uint64_t)si * wpr;
+  const bool listed = mode == RL_SMEM || mode == RL_GLOBAL;
+  uint32_t c = 0;
+  bool bad_hit = false;
+  for (uint32_t b0 = c_begin; b0 < c_end; b0 += CELLS) {
+    // the next step's durations are in flight while this step decides
+    uint32_t nxt[ITEMS];
+#pragma unroll
+    for (uint32_t j = 0; j < ITEMS; ++j) {
+      const uint32_t col = b0 + CELLS + j * TPB + threadIdx.x;
+      nxt[j] = col < c_end ? row[col] : MAXV;
+    }
+    // in-bound cells' destination ids, all loads issued before any search
+    bool inb[ITEMS];
+    uint32_t od[ITEMS];
+#pragma unroll
+    for (uint32_t j = 0; j < ITEMS; ++j) {
+      const uint32_t col = b0 + j * TPB + threadIdx.x;
+      inb[j] = col < c_end && dur[j] <= a.threshold && dur[j] != MAXV;
+      od[j] = inb[j] && listed ? a.dst_orig[col] : 0u;
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < ITEMS; ++j) {
+      bool keep = false;
+      if (inb[j]) {
+        if (mode == RL_NONE) keep = true;
+        else if (mode == RL_SMEM) keep = in_row_list(rl, len, nbw, od[j]);
+        else if (mode == RL_GLOBAL) keep = in_list(lg, len, od[j]);
+        else if (mode == RL_BAD) bad_hit = true;
+      }
+      const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
+      const uint32_t wcell = b0 + j * TPB + (threadIdx.x & ~31u);
+      if (lane == 0 && wcell < c_end) bits[wcell / 32] = bal;
+      c += keep;
+      dur[j] = nxt[j];
+    }
+  }
+  if (bad_hit) atomicOr(err, ERR_BAD_LIST);
+  const uint32_t t = block_sum(c, red);
+  if (threadIdx.x == 0) cnt[blockIdx.x] = t;
+}
+
+// k_tile_count_rows with 16-byte accesses (rows a multiple of 4 cells, the
+// matrix and the destination ids 16-byte aligned): a thread takes 4
+// consecutive cells per load and VEC loads per step, so each SM keeps twice
+// the bytes in flight; the 4-cell keep bits of 8 lanes are OR-combined by
+// shuffles into one ballot word.
+constexpr uint32_t VEC = 4, CELLS4 = TPB * 4 * VEC;
+
+__global__ void __launch_bounds__(TPB)
+    k_tile_count_rows4(TileIn a, uint32_t segs, uint32_t wpr, const uint4* __restrict__ info,
+                       const uint32_t* __restrict__ bound, unsigned long long* __restrict__ cnt,
+                       uint32_t* __restrict__ keep_bits, uint32_t* err) {
+  __shared__ RowList rl;
+  __shared__ uint32_t red[TPB / 32];
+  const uint32_t si = blockIdx.x / segs, sg = blockIdx.x % segs;
+  const uint32_t c_begin = sg * SEG, c_end = min(c_begin + SEG, a.n_dst);
+  const uint32_t lane = threadIdx.x & 31;
+  const uint4* row4 = reinterpret_cast<const uint4*>(a.m + (uint64_t)si * a.n_dst);
+  const uint4* od4 = reinterpret_cast<const uint4*>(a.dst_orig);
+  // the first step's durations load while the row's list is looked up
+  uint4 dur[VEC];
+#pragma unroll
+  for (uint32_t u = 0; u < VEC; ++u) {
+    const uint32_t col = c_begin + (u * TPB + threadIdx.x) * 4;
+    dur[u] = col < c_end ? row4[col / 4] : make_uint4(MAXV, MAXV, MAXV, MAXV);
+  }
+  const uint4 ri = info[si];  // {mode, len, list offset (lo, hi words)}
+  const uint32_t nbw = min(BITMAP_WORDS, (*bound >> 5) + 1);
+  const uint32_t mode = ri.x, len = ri.y;
+  const uint64_t lo = ri.z | ((uint64_t)ri.w << 32);
+  if (mode == RL_MISSING && threadIdx.x == 0) atomicOr(err, ERR_NO_LIST);
+  // uniform: every thread read the same row record
+  if (mode == RL_SMEM) stage_row_list(rl, a.mask + lo, len, nbw);
+  const uint32_t* lg = a.mask + lo;
+  uint32_t* bits = keep_bits + (uint64_t)si * wpr;
+  // a cell is within the bound iff d <= thr1 (the u32::MAX sentinel never
+  // is); cells past the segment read as the sentinel, so no column test
+  const uint32_t thr1 = min(a.threshold, MAXV - 1);
+  const bool listed = mode == RL_SMEM || mode == RL_GLOBAL;
+  // staged lists whose ids all fall in the bitmap are tested branch-free
+  const bool bitmap_only = mode == RL_SMEM && (*bound >> 5) < BITMAP_WORDS;
+  const uint32_t lim = nbw * 32;
+  uint32_t c = 0;
+  bool bad_hit = false;
+  for (uint32_t b0 = c_begin; b0 < c_end; b0 += CELLS4) {
+    uint4 nxt[VEC];
+#pragma unroll
+    for (uint32_t u = 0; u < VEC; ++u) {
+      const uint32_t col = b0 + CELLS4 + (u * TPB + threadIdx.x) * 4;
+      nxt[u] = col < c_end ? row4[col / 4] : make_uint4(MAXV, MAXV, MAXV, MAXV);
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < VEC; ++u) {
+      const uint32_t col = b0 + (u * TPB + threadIdx.x) * 4;  // < c_end or all four out
+      const uint4 d = dur[u];
+      const uint32_t inb = (uint32_t)(d.x <= thr1) | ((uint32_t)(d.y <= thr1) << 1) |
+                           ((uint32_t)(d.z <= thr1) << 2) | ((uint32_t)(d.w <= thr1) << 3);
+      uint32_t k4 = 0;
+      if (mode == RL_NONE) {
+        k4 = inb;
+      } else if (bitmap_only) {
+        // every destination id is below lim: one shared word per cell
+        const uint4 o = col < c_end ? od4[col / 4] : make_uint4(0, 0, 0, 0);
+        const uint32_t m4 = ((rl.bmp[o.x >> 5] >> (o.x & 31)) & 1u) |
+                            (((rl.bmp[o.y >> 5] >> (o.y & 31)) & 1u) << 1) |
+                            (((rl.bmp[o.z >> 5] >> (o.z & 31)) & 1u) << 2) |
+                            (((rl.bmp[o.w >> 5] >> (o.w & 31)) & 1u) << 3);
+        k4 = inb & m4;
+      } else if (inb) {
+        if (listed) {
+          const uint4 o = od4[col / 4];
+          const uint32_t ov[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+          for (uint32_t k = 0; k < 4; ++k)
+            if (((inb >> k) & 1u) &&
+                (mode == RL_SMEM ? (ov[k] < lim ? ((rl.bmp[ov[k] >> 5] >> (ov[k] & 31)) & 1u) != 0
+                                                : in_list(rl.v, len, ov[k]))
+                                 : in_list(lg, len, ov[k])))
+              k4 |= 1u << k;
+        } else if (mode == RL_BAD) {
+          bad_hit = true;
+        }
+      }
+      // lanes 8q .. 8q + 7 hold the 32 cells of ballot word q of this warp's 128
+      uint32_t word = k4 << ((lane & 7) * 4);
+      word |= __shfl_xor_sync(0xFFFFFFFFu, word, 1);
+      word |= __shfl_xor_sync(0xFFFFFFFFu, word, 2);
+      word |= __shfl_xor_sync(0xFFFFFFFFu, word, 4);
+      const uint32_t wcell = b0 + (u * TPB + (threadIdx.x & ~31u)) * 4 + (lane >> 3) * 32;
+      if ((lane & 7) == 0 && wcell < c_end) bits[wcell / 32] = word;
+      c += __popc(k4);
+      dur[u] = nxt[u];
+    }
+  }
+  if (bad_hit) atomicOr(err, ERR_BAD_LIST);
+  const uint32_t t = block_sum(c, red);
+  if (threadIdx.x == 0) cnt[blockIdx.x] = t;
+}
+
+// Sparse pass 2 for wide rows: the segment's kept cells in order, a warp
+// per row segment (no block barrier): 32 ballot words at a time (the next
+// 32 loading meanwhile), a shuffle scan of their popcounts for each word's
+// offset, then the kept cells word by word with a lane per cell (words
+// without kept cells are skipped by ballot).
+__global__ void __launch_bounds__(TPB)
+    k_tile_write_rows(TileIn a, TileOut o, uint64_t nseg, uint32_t segs, uint32_t wpr,
+                      const unsigned long long* __restrict__ pre,
+                      const uint32_t* __restrict__ keep_bits) {
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint64_t seg = (uint64_t)blockIdx.x * (TPB / 32) + wid;
+  if (seg >= nseg) return;
+  const unsigned long long k0 = pre[seg];
+  if (pre[seg + 1] == k0) return;  // nothing kept in this segment (uniform per warp)
+  const uint32_t si = (uint32_t)(seg / segs), sg = (uint32_t)(seg % segs);
+  const uint32_t w_begin = sg * SEG_WORDS, w_end = min(w_begin + SEG_WORDS, wpr);
+  const uint32_t* bits_row = keep_bits + (uint64_t)si * wpr;
+  const uint32_t os = a.src_orig[si];
+  const uint64_t row0 = (uint64_t)si * a.n_dst;
+  uint32_t carry = 0;
+  uint32_t bits = w_begin + lane < w_end ? bits_row[w_begin + lane] : 0u;
+  for (uint32_t w0 = w_begin; w0 < w_end; w0 += 32) {
+    const uint32_t wn = w0 + 32 + lane;
+    const uint32_t nbits = wn < w_end ? bits_row[wn] : 0u;
+    const uint32_t cn = __popc(bits);
+    uint32_t inc = cn;
+#pragma unroll
+    for (uint32_t d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, d);
+      if (lane >= d) inc += y;
+    }
+    const uint32_t ex = carry + inc - cn;
+    carry += __shfl_sync(0xFFFFFFFFu, inc, 31);
+    uint32_t nz = __ballot_sync(0xFFFFFFFFu, bits != 0u);
+    while (nz) {
+      const uint32_t q = __ffs(nz) - 1;
+      nz &= nz - 1;
+      const uint32_t b = __shfl_sync(0xFFFFFFFFu, bits, q);
+      const uint32_t off = __shfl_sync(0xFFFFFFFFu, ex, q);
+      if ((b >> lane) & 1u) {
+        const uint32_t col = (w0 + q) * 32 + lane;
+        const uint64_t cell = row0 + col;
+        put(a, o, k0 + off + __popc(b & ((1u << lane) - 1u)), cell, os, a.dst_orig[col],
+            a.m[cell]);
+      }
+    }
+    bits = nbits;
   }
 }
 
@@ -393,6 +628,44 @@ bf_status emit_device(TileWs& ws, const TileIn& a, const TileOut& o, cudaStream_
       k_tile_dense<<<dim3(gx, gy), TPB, 0, st>>>(a, o, d_err);
     BF_CUDA(cudaGetLastError());
     rows = n;
+  } else if (n && a.n_dst >= ROW_MIN &&
+             (uint64_t)a.n_src * ((a.n_dst + SEG - 1) / SEG) <= 0x7FFFFFFFull) {
+    const uint32_t segs = (a.n_dst + SEG - 1) / SEG, wpr = (a.n_dst + 31) / 32;
+    const uint64_t nb = (uint64_t)a.n_src * segs;
+    unsigned long long* d_cnt = nullptr;
+    uint32_t* d_bits = nullptr;
+    uint64_t* d_bsum = nullptr;
+    const uint64_t nsb = (nb + SCAN_BLOCK - 1) / SCAN_BLOCK;
+    BF_CUDA(ws_get(ws, 1, (2 * nb + 1) * 8, &d_cnt));
+    BF_CUDA(ws_get(ws, 9, (uint64_t)a.n_src * wpr * 4, &d_bits));
+    BF_CUDA(ws_get(ws, 10, (nsb + 2) * 8, &d_bsum));
+    // per-row list records and the destination ids' range (bound[0], from
+    // which the count blocks size their bitmaps)
+    uint4* d_info = nullptr;
+    BF_CUDA(ws_get(ws, 11, (uint64_t)a.n_src * 16 + 16, &d_info));
+    uint32_t* d_bound = reinterpret_cast<uint32_t*>(d_info + a.n_src);
+    BF_CUDA(cudaMemsetAsync(d_bound, 0, 4, st));
+    const unsigned gi = (unsigned)std::min<uint64_t>(
+        (std::max(a.n_src, a.n_dst) + TPB - 1) / TPB, 152 * 8);
+    k_tile_rowinfo<<<gi, TPB, 0, st>>>(a, d_info, d_bound);
+    auto al = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
+    if (a.n_dst % 4 == 0 && al(a.m) && al(a.dst_orig))
+      k_tile_count_rows4<<<(unsigned)nb, TPB, 0, st>>>(a, segs, wpr, d_info, d_bound, d_cnt, d_bits,
+                                                       d_err);
+    else
+      k_tile_count_rows<<<(unsigned)nb, TPB, 0, st>>>(a, segs, wpr, d_info, d_bound, d_cnt, d_bits,
+                                                      d_err);
+    uint64_t* pre = reinterpret_cast<uint64_t*>(d_cnt + nb);
+    k_scan_sums<uint64_t><<<(unsigned)nsb, SCAN_TPB, 0, st>>>(
+        U64Val{reinterpret_cast<const uint64_t*>(d_cnt)}, nb, nullptr, d_bsum);
+    k_scan_top<uint64_t><<<1, SCAN_TPB, 0, st>>>(d_bsum, (uint32_t)nsb);
+    k_scan_out<uint64_t><<<(unsigned)nsb, SCAN_TPB, 0, st>>>(
+        U64Val{reinterpret_cast<const uint64_t*>(d_cnt)}, nb, nullptr, d_bsum, (uint32_t)nsb,
+        pre);
+    k_tile_write_rows<<<(unsigned)((nb + TPB / 32 - 1) / (TPB / 32)), TPB, 0, st>>>(
+        a, o, nb, segs, wpr, d_cnt + nb, d_bits);
+    BF_CUDA(cudaGetLastError());
+    BF_CUDA(cudaMemcpyAsync(&rows, d_cnt + 2 * nb, 8, cudaMemcpyDeviceToHost, st));
   } else if (n) {
     const uint64_t nb = (n + CELLS - 1) / CELLS;
     if (nb > 0x7FFFFFFFull) {

@@ -108,17 +108,22 @@ def test_missing_radius_list_is_an_error(bf):
                 orc.tile_emit([1, 2], 1, 2, [0], [0, 1], mask=[[1]], sparse=True))
 
 
-@pytest.mark.parametrize("n_dst,list_max", [(2048, 600), (5000, 4096), (3000, 5000)])
-def test_sparse_radius_lists_staged(bf, n_dst, list_max):
-    """Sparse emission with radius lists short enough (at most 4096 entries)
-    to be searched in shared memory by every count block (rows of 2048 or
-    more cells: a block spans at most two rows), including lists of exactly
-    the staging limit and, for list_max 5000, rows whose list is too long,
-    whose blocks search global memory."""
+@pytest.mark.parametrize("n_dst,list_max,span", [(2048, 600, 0), (5000, 4096, 0),
+                                                  (3000, 5000, 0), (3000, 2000, 400_000)])
+def test_sparse_radius_lists_staged(bf, n_dst, list_max, span):
+    """Sparse emission of wide rows (2048 cells or more: a block per row
+    segment) with radius lists short enough (at most 4096 entries) to be
+    searched in shared memory, including lists of exactly the staging limit
+    and, for list_max 5000, rows whose list is too long, whose blocks search
+    global memory; with span 400 000, destination ids beyond the shared
+    bitmap's 2^17 ids, which are searched in the staged list."""
     rng = np.random.default_rng(n_dst + list_max)
     n_src = 37
     m, src, dst, _, lat = random_case(rng, n_src, n_dst, False, True)
-    span = 3 * n_dst + 5
+    if span:
+        dst = rng.choice(span, n_dst, replace=False).astype(np.uint32)
+    else:
+        span = 3 * n_dst + 5
     mask = []
     for r in range(3 * n_src + 5):
         k = list_max if r % 3 == 0 else int(rng.integers(0, list_max + 1))
@@ -127,3 +132,19 @@ def test_sparse_radius_lists_staged(bf, n_dst, list_max):
     for thr in (MAX, 100_000):
         args = (m, n_src, n_dst, src, dst, thr, mask, lat, True)
         assert same(bf.tile_emit(*args), orc.tile_emit(*args)), thr
+
+
+def test_wide_rows_missing_radius_list_is_an_error(bf):
+    """A wide row (a block per row segment) whose source has no radius list
+    is an error whether or not the sparse form runs; the next call works."""
+    rng = np.random.default_rng(21)
+    n_src, n_dst = 3, 20000  # two segments per row
+    m, src, dst, _, _ = random_case(rng, n_src, n_dst, False, False)
+    src = np.array([0, 1, 5], dtype=np.uint32)  # original index 5 has no list
+    mask = [[1, 2, 3], list(range(0, 60000, 7)), [4]]
+    for sparse in (False, True):
+        with pytest.raises(bf.BfError, match="radius list"):
+            bf.tile_emit(m, n_src, n_dst, src, dst, MAX, mask, None, sparse)
+    src = np.array([0, 1, 2], dtype=np.uint32)
+    args = (m, n_src, n_dst, src, dst, 150_000, mask, None, True)
+    assert same(bf.tile_emit(*args), orc.tile_emit(*args))
