@@ -434,10 +434,14 @@ bf_status launch_upward(Graph* g, const uint32_t* d_src, uint64_t k, uint32_t th
 // Output of the upward pass: the u32 slab, a 16-bit slab (isochrone lanes), or
 // a compact per-source buffer of k x (max_depth + 1) {row, dist} entries that
 // launch_scatter_seeds writes into the slab later (so the pass can overlap
-// the slab reset).
+// the slab reset, or run before the restricted schedule exists: with a null
+// pos_map the entries hold ranks, which the scatter maps through `cidx`).
 enum : uint32_t { UPWARD_OUT_SLAB32 = 0, UPWARD_OUT_SLAB16 = 1, UPWARD_OUT_COMPACT = 2 };
+// Entries of sources [0, k) read at columns col0 .. col0 + k - 1 of rows
+// `stride` entries wide (stride 0: k).
 bf_status launch_scatter_seeds(Graph* g, const void* cseed, uint64_t k, const uint32_t* d_src,
-                               uint32_t* slab, uint32_t Kp, cudaStream_t st);
+                               uint32_t* slab, uint32_t Kp, cudaStream_t st, uint64_t stride = 0,
+                               uint64_t col0 = 0, const uint32_t* cidx = nullptr);
 __global__ void k_extract(const uint32_t* __restrict__ slab, uint32_t slab_stride,
                           const uint32_t* __restrict__ tpos, uint64_t T, uint32_t k,
                           uint32_t* __restrict__ out);
@@ -471,8 +475,12 @@ bf_status hub_rows(Graph* g, Sched& sc, uint64_t row_bytes, cudaStream_t st, con
 uint64_t ctx_budget(Graph* g, Ctx& c);
 void free_ctx(Ctx& c);
 bf_status init_ctx(Ctx& c);
+// pre_stride != 0: the wave's upward pass already ran (compact entries at
+// columns pre_col .. pre_col + kw - 1 of rows pre_stride wide, c.join marks
+// its end on the side stream).
 bf_status batched_wave(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t kw, uint32_t Kp,
-                       cudaStream_t st, uint64_t* launches, bool timed);
+                       cudaStream_t st, uint64_t* launches, bool timed, uint64_t pre_stride = 0,
+                       uint64_t pre_col = 0);
 bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, const uint32_t* d_tgt,
                          uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                          bf_stats* stats);

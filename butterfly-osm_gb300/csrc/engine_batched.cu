@@ -854,7 +854,8 @@ bf_status prepare_rows(Graph* g, Ctx& c, Sched& sc, const uint32_t* d_src, uint6
 // slab, upward pass for kw sources, restricted sweep. Records c.ev[0..2]
 // around the phases when `timed`.
 bf_status batched_wave(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t kw, uint32_t Kp,
-                       cudaStream_t st, uint64_t* launches, bool timed) {
+                       cudaStream_t st, uint64_t* launches, bool timed, uint64_t pre_stride,
+                       uint64_t pre_col) {
   bf_status s;
   Sched& sc = c.sc;
   const uint64_t rows = std::max<uint32_t>(sc.n_r, 1);
@@ -864,26 +865,33 @@ bf_status batched_wave(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t kw, uin
   if (timed) BF_CUDA(cudaEventRecord(c.ev[0], st));
   // the upward pass is latency-bound and the slab reset bandwidth-bound: with
   // a shallow enough tree the pass runs on the side stream into a compact
-  // buffer while the reset runs here, and a scatter joins them
+  // buffer of ranks while the reset runs here, and a scatter maps them to
+  // rows (the pass may also have run before the schedule was built)
   const uint32_t dcap = ((g->max_depth + 1) + 31) & ~31u;
-  const bool overlap = g->tune.overlap_up && c.aux && (size_t)UPWARD_WARPS * 2 * dcap * 4 <= 200 * 1024;
+  const bool overlap =
+      pre_stride || (g->tune.overlap_up && c.aux && (size_t)UPWARD_WARPS * 2 * dcap * 4 <= 200 * 1024);
   if (overlap) {
     const uint32_t words = (std::max<uint32_t>(sc.n_r, 1) + 31) / 32;
     if ((s = ensure(&c.d_seeded, c.cap_seeded, words, g))) return s;
-    if ((s = ensure(&c.d_cseed, c.cap_cseed, kw * (g->max_depth + 1), g))) return s;
+    if (!pre_stride && (s = ensure(&c.d_cseed, c.cap_cseed, kw * (g->max_depth + 1), g))) return s;
     BF_CUDA(cudaMemsetAsync(c.d_seeded, 0, (size_t)words * 4, st));
     launch_mark_paths(g, d_src, kw, sc.d_cidx, c.d_seeded, st);
-    BF_CUDA(cudaEventRecord(c.fork, st));
-    BF_CUDA(cudaStreamWaitEvent(c.aux, c.fork, 0));
-    if ((s = launch_upward(g, d_src, kw, INF, sc.d_cidx, reinterpret_cast<uint32_t*>(c.d_cseed),
-                           (uint32_t)kw, nullptr, c.aux, nullptr, nullptr, nullptr,
-                           UPWARD_OUT_COMPACT)))
-      return s;
-    BF_CUDA(cudaEventRecord(c.join, c.aux));
+    if (!pre_stride) {
+      BF_CUDA(cudaEventRecord(c.fork, st));
+      BF_CUDA(cudaStreamWaitEvent(c.aux, c.fork, 0));
+      if ((s = launch_upward(g, d_src, kw, INF, nullptr, reinterpret_cast<uint32_t*>(c.d_cseed),
+                             (uint32_t)kw, nullptr, c.aux, nullptr, nullptr, nullptr,
+                             UPWARD_OUT_COMPACT)))
+        return s;
+      BF_CUDA(cudaEventRecord(c.join, c.aux));
+      ++*launches;
+    }
     BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)std::max<uint32_t>(sc.n_r, 1) * Kp * 4, st));
     BF_CUDA(cudaStreamWaitEvent(st, c.join, 0));
-    if ((s = launch_scatter_seeds(g, c.d_cseed, kw, d_src, c.d_slab, Kp, st))) return s;
-    *launches += 3;
+    if ((s = launch_scatter_seeds(g, c.d_cseed, kw, d_src, c.d_slab, Kp, st,
+                                  pre_stride ? pre_stride : kw, pre_col, sc.d_cidx)))
+      return s;
+    *launches += 2;
   } else {
     if ((s = prepare_rows(g, c, sc, d_src, kw, Kp, st, launches))) return s;
     if ((s = launch_upward(g, d_src, kw, INF, sc.d_cidx, c.d_slab, Kp, nullptr, st))) return s;
@@ -897,6 +905,26 @@ bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, co
                          uint64_t T, uint32_t threshold, uint32_t* d_out, cudaStream_t st,
                          bf_stats* stats) {
   bf_status s;
+  // the upward pass needs only the sources: with a shallow tree it runs on
+  // the side stream from here, beside the target check and the restricted
+  // schedule's build, into a compact buffer of ranks for all S sources
+  const uint32_t dcap = ((g->max_depth + 1) + 31) & ~31u;
+  const uint64_t pre_entries = S * (uint64_t)(g->max_depth + 1);
+  const bool pre = S && g->tune.overlap_up && c.aux &&
+                   (size_t)UPWARD_WARPS * 2 * dcap * 4 <= 200 * 1024 &&
+                   pre_entries * sizeof(uint2) <= (1ull << 30);
+  uint64_t pre_launches = 0;
+  if (pre) {
+    if ((s = ensure(&c.d_cseed, c.cap_cseed, pre_entries, g))) return s;
+    BF_CUDA(cudaEventRecord(c.fork, st));
+    BF_CUDA(cudaStreamWaitEvent(c.aux, c.fork, 0));
+    if ((s = launch_upward(g, d_src, S, INF, nullptr, reinterpret_cast<uint32_t*>(c.d_cseed),
+                           (uint32_t)S, nullptr, c.aux, nullptr, nullptr, nullptr,
+                           UPWARD_OUT_COMPACT)))
+      return s;
+    BF_CUDA(cudaEventRecord(c.join, c.aux));
+    pre_launches = 1;
+  }
   std::vector<uint32_t> h_tgt(T);
   BF_CUDA(cudaMemcpyAsync(h_tgt.data(), d_tgt, T * 4, cudaMemcpyDeviceToHost, st));
   BF_CUDA(cudaStreamSynchronize(st));
@@ -923,11 +951,13 @@ bf_status batched_matrix(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t S, co
   const uint64_t wave = std::min<uint64_t>(max_lanes, (S + 3) & ~3ull);
   const uint32_t Kp = (uint32_t)((wave + 3) & ~3ull);
   if ((s = ensure_slab(g, c, (size_t)rows * Kp * 4))) return s;
-  uint64_t launches = 0;
+  uint64_t launches = pre_launches;
   float t_up = 0, t_dn = 0, t_ex = 0;
   for (uint64_t s0 = 0; s0 < S; s0 += wave) {
     const uint64_t kw = std::min<uint64_t>(wave, S - s0);
-    if ((s = batched_wave(g, c, d_src + s0, kw, Kp, st, &launches, stats != nullptr))) return s;
+    if ((s = batched_wave(g, c, d_src + s0, kw, Kp, st, &launches, stats != nullptr,
+                          pre ? S : 0, s0)))
+      return s;
     if (stats) BF_CUDA(cudaEventRecord(c.ev[2], st));
     dim3 eg((unsigned)((T + 31) / 32), (unsigned)((kw + 31) / 32)), eb(32, 8);
     k_extract_lanes<<<eg, eb, 0, st>>>(c.d_slab, Kp, sc.d_trow, T, (uint32_t)kw, threshold,

@@ -141,7 +141,8 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 4)
     uint2* out = reinterpret_cast<uint2*>(seed);
     for (uint32_t l = lane; l < D; l += 32) {
       const uint32_t d = pd_load<GLOBAL>(&pd[l]);
-      const uint32_t p = (d == INF || d > threshold) ? NONE : pos_of[PN(l)];
+      const uint32_t x = PN(l);
+      const uint32_t p = (d == INF || d > threshold) ? NONE : (pos_of ? pos_of[x] : x);
       out[(size_t)(D - 1 - l) * seed_stride + w] = make_uint2(p, d);
     }
     return;
@@ -298,7 +299,7 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 10)
       const uint32_t x = path_node(min(l, D - 1), r_node, r_idx);
       if (l >= D) continue;
       const uint32_t d = pd[l];
-      const uint32_t p = (d == INF || d > threshold) ? NONE : pos_of[x];
+      const uint32_t p = (d == INF || d > threshold) ? NONE : (pos_of ? pos_of[x] : x);
       out[(size_t)(D - 1 - l) * seed_stride + w] = make_uint2(p, d);
     }
     return;
@@ -322,14 +323,19 @@ __global__ void __launch_bounds__(UPWARD_WARPS * 32, 10)
 // Compact upward output -> slab: thread (w, i) writes entry i (counted from
 // the root) of source w's ancestor path into lane w of its row. Consecutive
 // threads are consecutive lanes, and near the root their rows coincide, so
-// those writes are whole lines.
+// those writes are whole lines. Entries are read at column col0 + w of rows
+// `stride` wide; with `cidx` they name ranks, mapped to rows here (NONE: a
+// rank outside the restricted schedule).
 __global__ void __launch_bounds__(256)
     k_scatter_seeds(const uint2* __restrict__ cseed, uint32_t k, const uint32_t* __restrict__ src,
-                    const uint32_t* __restrict__ depth, uint32_t* __restrict__ slab, uint32_t Kp) {
+                    const uint32_t* __restrict__ depth, uint32_t* __restrict__ slab, uint32_t Kp,
+                    uint32_t stride, uint32_t col0, const uint32_t* __restrict__ cidx) {
   const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
   if (w >= k || i > depth[src[w]]) return;
-  const uint2 e = cseed[(size_t)i * k + w];
-  if (e.x != NONE) slab[(size_t)e.x * Kp + w] = e.y;
+  const uint2 e = cseed[(size_t)i * stride + col0 + w];
+  if (e.x == NONE) return;
+  const uint32_t row = cidx ? cidx[e.x] : e.x;
+  if (row != NONE) slab[(size_t)row * Kp + w] = e.y;
 }
 
 // One level of the pull sweep: positions [p0, p1), a warp per node.
@@ -573,11 +579,13 @@ static bf_status plain_buffers(Graph* g) {
 }
 
 bf_status launch_scatter_seeds(Graph* g, const void* cseed, uint64_t k, const uint32_t* d_src,
-                               uint32_t* slab, uint32_t Kp, cudaStream_t st) {
+                               uint32_t* slab, uint32_t Kp, cudaStream_t st, uint64_t stride,
+                               uint64_t col0, const uint32_t* cidx) {
   if (!k) return BF_OK;
   dim3 grid((unsigned)((k + 255) / 256), g->max_depth + 1);
   k_scatter_seeds<<<grid, 256, 0, st>>>(reinterpret_cast<const uint2*>(cseed), (uint32_t)k, d_src,
-                                       g->d_depth, slab, Kp);
+                                       g->d_depth, slab, Kp, (uint32_t)(stride ? stride : k),
+                                       (uint32_t)col0, cidx);
   BF_CUDA(cudaGetLastError());
   return BF_OK;
 }
