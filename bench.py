@@ -549,6 +549,19 @@ def run_isochrones(g, cch, count, seed=42):
     cpu_s = time.perf_counter() - t0
     got = d_b.view(chunk, w64)[torch.from_numpy(pick - c0)].cpu().numpy().view(np.uint64)
     exact = bool(np.array_equal(got, wb)) and bool(np.array_equal(counts[pick], wc))
+    del wb
+    # the CPU rate on about 10 s of work: further 1024-origin pieces of the
+    # chunk (other origins than the checked ones), results dropped
+    cpu_n = len(pick)
+    rest = np.setdiff1d(np.arange(c0, c0 + m), pick)
+    for k0 in range(0, len(rest), 1024):
+        if cpu_s >= 10.0:
+            break
+        part = rest[k0:k0 + 1024]
+        t0 = time.perf_counter()
+        c.isochrone_bitsets(o[part], t[part], threads=threads)
+        cpu_s += time.perf_counter() - t0
+        cpu_n += len(part)
     peak, peak_kind = measured_peak()
     achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9 if sweep_ms else 0.0
     return {"origins": count, "value": round(count / sec, 1), "unit": "isochrones/s",
@@ -568,9 +581,9 @@ def run_isochrones(g, cch, count, seed=42):
                                        "and per row written"},
             "e2e": run_isochrones_e2e(g, o, t, w64, min(count, 2048)),
             "bit_exact_sample": {"origins": len(pick), "equal": exact},
-            "cpu_baseline": {"value": round(len(pick) / cpu_s, 2), "unit": "isochrones/s",
+            "cpu_baseline": {"value": round(cpu_n / cpu_s, 2), "unit": "isochrones/s",
                              "cores": threads, "kind": "port",
-                             "sample": "%d origins of the last chunk, %.1f s" % (len(pick), cpu_s)}}
+                             "sample": "%d origins of the last chunk, %.1f s" % (cpu_n, cpu_s)}}
 
 
 def run_isochrones_e2e(g, o, t, w64, m):
