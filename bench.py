@@ -645,15 +645,22 @@ def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
     wave = {k: round(wst[k], 2) for k in ("upward_ms", "downward_ms", "extract_ms", "total_ms")}
     wave["launches"] = wst["kernel_launches"]
     c = orc.Cch.from_dict(cch)
+    # three origins checked ring for ring; the CPU rate over about 5 s of the
+    # batch's origins (one host thread, as the reference builds one request)
     pick = [0, count // 2, count - 1][:count]
-    exact, cpu_s = True, 0.0
-    for k in pick:
+    order = pick + [k for k in range(count) if k not in pick]
+    exact, cpu_s, cpu_n = True, 0.0, 0
+    for k in order:
+        if k not in pick and cpu_s >= 5.0:
+            break
         t0 = time.perf_counter()
         rk, ds = c.bounded_seeded([(int(origins[k]), 0)], int(thr[k]))
         want, _, _ = orc.isochrone_geometry(rk, ds, int(thr[k]), w, off, poly,
                                             "car", tier=threshold_s)
         cpu_s += time.perf_counter() - t0
-        exact = exact and bool(np.array_equal(rings[k], want))
+        cpu_n += 1
+        if k in pick:
+            exact = exact and bool(np.array_equal(rings[k], want))
     cell, dil, ero, simp = bfphast.contour_config(bfphast.MODE_CAR, threshold_s)
     return {"isochrones": count, "threshold_s": threshold_s, "cell_m": cell,
             "morphology": [dil, ero], "value": round(count / sec, 1), "unit": "polygons/s",
@@ -664,10 +671,10 @@ def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
             "mean_ring_vertices": round(float(np.mean([len(r) for r in rings])), 1),
             "geometry_create_ms": round(geo_ms, 1),
             "bit_exact_sample": {"isochrones": len(pick), "equal": exact},
-            "cpu_baseline": {"value": round(len(pick) / cpu_s, 3), "unit": "polygons/s",
+            "cpu_baseline": {"value": round(cpu_n / cpu_s, 3), "unit": "polygons/s",
                              "cores": 1, "kind": "port",
                              "sample": "%d origins of the batch from the origin (bounded query "
-                                       "and geometry), %.1f s" % (len(pick), cpu_s)},
+                                       "and geometry), %.1f s" % (cpu_n, cpu_s)},
             "data": "synthetic lattice coordinates, straight tail -> head road polylines"}
 
 
