@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(256)
               uint32_t rounds, const uint64_t* __restrict__ in_off,
               const uint2* __restrict__ in_rec, uint32_t* __restrict__ cnt,
               uint32_t* __restrict__ alive, const uint32_t* __restrict__ ist,
-              long long timeout, uint32_t* __restrict__ err) {
+              long long timeout, uint32_t withhold, uint32_t* __restrict__ err) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * blockDim.x / 32;
   const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -286,7 +286,8 @@ __global__ void __launch_bounds__(256)
       }
       warp_edges(k0, deg, lane, f);
     }
-    if (!grid_barrier(meta + META_BAR, r, timeout, err)) return;
+    // (test hook: block `withhold` leaves before its first arrival)
+    if (blockIdx.x == withhold || !grid_barrier(meta + META_BAR, r, timeout, err)) return;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     meta[META_ROUNDS] = r;
@@ -671,9 +672,12 @@ bf_status build_schedule_device(Graph* g, Ctx& c, Sched& sc, const uint32_t* h_t
     }
     s.peel_blocks = std::max(1u, std::min(4u, (unsigned)std::max(per_sm, 1)) * g->sm_count);
   }
-  BF_CUDA(launch_persistent(k_sd_peel, s.peel_blocks, 256, st, s.front, n, s.meta, PEEL_ROUNDS,
-                            (const uint64_t*)g->d_in_off, (const uint2*)g->d_in_rec, s.cnt,
-                            s.alive, (const uint32_t*)s.ist, BARRIER_TIMEOUT_CYCLES, g->d_err));
+  const bool hook = test_withhold_arrival();
+  BF_CUDA(launch_persistent(k_sd_peel, hook ? 2u : s.peel_blocks, 256, st, s.front, n, s.meta,
+                            PEEL_ROUNDS, (const uint64_t*)g->d_in_off,
+                            (const uint2*)g->d_in_rec, s.cnt, s.alive, (const uint32_t*)s.ist,
+                            hook ? 2000000ll : BARRIER_TIMEOUT_CYCLES, hook ? 1u : NONE,
+                            g->d_err));
   // 3. compaction
   const unsigned nbw = (unsigned)((W + 1 + SCAN_BLOCK - 1) / SCAN_BLOCK);
   PopVal pv{s.alive};

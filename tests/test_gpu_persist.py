@@ -127,3 +127,32 @@ def _chain_like():
     return dict(n=n, up_off=up_off, up_tgt=np.arange(1, n, dtype=np.uint32),
                 up_w=np.ones(n - 1, np.uint32), down_off=down_off,
                 down_tgt=np.arange(0, n - 1, dtype=np.uint32), down_w=np.ones(n - 1, np.uint32))
+
+
+def test_schedule_peeling_deadline_reports_timeout(built, grid100):
+    """The device schedule builder's peeling rounds run in one cooperative
+    launch; with the hook, block 1 leaves before its first barrier arrival,
+    block 0's wait runs out, and the matrix call reports BF_ERR_TIMEOUT. Rows
+    are only ever removed when nothing reads them, so the schedule left is a
+    correct superset: the next calls, with and without the hook's targets,
+    are exact."""
+    import bfphast
+    _, cch = grid100
+    n = cch["n"]
+    c = orc.Cch.from_dict(cch)
+    g = bfphast.Graph.from_cch(cch)
+    g.set_tune(device_schedule=1)
+    src = np.array([3, 1000, 30000, 17], dtype=np.uint32)
+    tgt = np.arange(5, n, 97, dtype=np.uint32)
+    os.environ["BF_TEST_WITHHOLD_ARRIVAL"] = "1"
+    try:
+        with pytest.raises(bfphast.BfError) as e:
+            g.matrix(src, tgt)
+        assert e.value.status == bfphast.BF_ERR_TIMEOUT
+    finally:
+        del os.environ["BF_TEST_WITHHOLD_ARRIVAL"]
+    want, _ = c.matrix(src, tgt)
+    assert np.array_equal(g.matrix(src, tgt), want)
+    tgt2 = np.arange(11, n, 89, dtype=np.uint32)
+    want2, _ = c.matrix(src, tgt2)
+    assert np.array_equal(g.matrix(src, tgt2), want2)
