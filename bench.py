@@ -609,15 +609,16 @@ def run_isochrones_e2e(g, o, t, w64, m):
 def run_contours(g, cch, count, cols, threshold_s=1800, seed=11):
     """Isochrone polygons for `count` origins through bf_isochrone_polygons:
     settled sets in bulk, each reachable road whole or cut at the threshold
-    (the reference's f32 cut), contour rasters on the GPU, tracing and
-    simplification on host threads. Road geometry: synthetic lattice
+    (the reference's f32 cut), contour rasters, ring tracing and
+    simplification on the GPU. Road geometry: synthetic lattice
     coordinates (about 100 m spacing), each road a straight tail -> head
     polyline, the fixture's node weights. Distances are deciseconds (the
     graph's unit); the contour tier comes from the threshold in seconds. The
     whole call runs once as warm-up, then is timed. A sample of origins is
     checked ring for ring against the oracle's pipeline from the origin
     (bounded query, then build_isochrone_geometry_sparse), which is timed on
-    one host thread as the CPU baseline."""
+    one host thread over about 5 s of the batch's origins as the CPU
+    baseline."""
     import numpy as np
     import bfphast
     from oracle import oracle as orc
