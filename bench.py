@@ -539,6 +539,9 @@ def run_isochrones(g, cch, count, seed=42):
     e1.record(stream)
     torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) / 1e3
+    # end to end through the host-buffer call, before the CPU sample's host
+    # allocations
+    e2e = run_isochrones_e2e(g, o, t, w64, min(count, 2048))
     # bit-exact sample from the last chunk + CPU oracle rate on the host cores
     c = orc.Cch.from_dict(cch)
     c0, m = last
@@ -579,7 +582,7 @@ def run_isochrones(g, cch, count, seed=42):
                          "bytes_rule": "per wave: 16 B per work item + 8 B per edge record "
                                        "scanned, 2 B x lanes per active source row gathered "
                                        "and per row written"},
-            "e2e": run_isochrones_e2e(g, o, t, w64, min(count, 2048)),
+            "e2e": e2e,
             "bit_exact_sample": {"origins": len(pick), "equal": exact},
             "cpu_baseline": {"value": round(cpu_n / cpu_s, 2), "unit": "isochrones/s",
                              "cores": threads, "kind": "port",
