@@ -840,13 +840,13 @@ bf_status prepare_rows(Graph* g, Ctx& c, Sched& sc, const uint32_t* d_src, uint6
   bf_status s;
   if ((s = ensure(&c.d_seeded, c.cap_seeded, words, g))) return s;
   BF_CUDA(cudaMemsetAsync(c.d_seeded, 0, (size_t)words * 4, st));
-  // the restricted rows are mostly on some source's ancestor path, so one
-  // streaming reset of the slab beats resetting the marked rows one by one;
-  // the seeded bits still let the sweep skip reading unseeded rows
-  BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)std::max<uint32_t>(sc.n_r, 1) * Kp * 4, st));
   launch_mark_paths(g, d_src, kw, sc.d_cidx, c.d_seeded, st);
+  // only rows the sweep does not overwrite whole need INF first (seeded,
+  // split and in-edge-free rows; 10k x 10k: 2.8 against 3.5 ms for a reset
+  // of the whole slab beside the upward pass)
+  launch_init_rows(c.d_seeded, sc.d_split, words, c.d_slab, Kp, st);
   BF_CUDA(cudaGetLastError());
-  *launches += 1;
+  *launches += 2;
   return BF_OK;
 }
 
@@ -863,7 +863,7 @@ bf_status batched_wave(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t kw, uin
   const unsigned lane_blocks = (Kp / 4 + tpb - 1) / tpb;
   (void)rows;
   if (timed) BF_CUDA(cudaEventRecord(c.ev[0], st));
-  // the upward pass is latency-bound and the slab reset bandwidth-bound: with
+  // the upward pass is latency-bound and the row reset bandwidth-bound: with
   // a shallow enough tree the pass runs on the side stream into a compact
   // buffer of ranks while the reset runs here, and a scatter maps them to
   // rows (the pass may also have run before the schedule was built)
@@ -886,12 +886,15 @@ bf_status batched_wave(Graph* g, Ctx& c, const uint32_t* d_src, uint64_t kw, uin
       BF_CUDA(cudaEventRecord(c.join, c.aux));
       ++*launches;
     }
-    BF_CUDA(cudaMemsetAsync(c.d_slab, 0xFF, (size_t)std::max<uint32_t>(sc.n_r, 1) * Kp * 4, st));
+    // only rows the sweep does not overwrite whole need INF first: seeded
+    // rows (read back by their item), split rows (atomicMin targets) and rows
+    // without in-edges (read, never written) - sc.d_split marks the last two
+    launch_init_rows(c.d_seeded, sc.d_split, words, c.d_slab, Kp, st);
     BF_CUDA(cudaStreamWaitEvent(st, c.join, 0));
     if ((s = launch_scatter_seeds(g, c.d_cseed, kw, d_src, c.d_slab, Kp, st,
                                   pre_stride ? pre_stride : kw, pre_col, sc.d_cidx)))
       return s;
-    *launches += 2;
+    *launches += 3;
   } else {
     if ((s = prepare_rows(g, c, sc, d_src, kw, Kp, st, launches))) return s;
     if ((s = launch_upward(g, d_src, kw, INF, sc.d_cidx, c.d_slab, Kp, nullptr, st))) return s;
