@@ -90,9 +90,10 @@ def test_broom_closed_form_and_bounds(built, kats, n_leaf):
                     assert t not in got
 
 
-def test_batched_equals_single(built, grid100):
+@pytest.mark.parametrize("graph", ["grid100", "country_small"])
+def test_batched_equals_single(built, request, graph):
     # bench/main.rs:1393-1414: every batched cell equals the single-source query
-    _, cch = grid100
+    _, cch = request.getfixturevalue(graph)
     c = orc.Cch.from_dict(cch)
     rng = np.random.default_rng(1)
     src = rng.integers(0, c.n, 8)
@@ -101,6 +102,11 @@ def test_batched_equals_single(built, grid100):
         assert np.array_equal(batch[lane], c.phast_query(s))
     m, _ = c.matrix(src, np.arange(c.n))
     assert np.array_equal(m, batch)
+    # the threaded matrix over more sources than one K-lane batch
+    src2 = rng.integers(0, c.n, 21)
+    tgt = rng.integers(0, c.n, 40)
+    m2, _ = c.matrix(src2, tgt, threads=4)
+    assert np.array_equal(m2, np.stack([c.phast_query(s)[tgt] for s in src2]))
 
 
 def test_bounded_agrees_with_unbounded(built, grid100):
